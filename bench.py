@@ -1,0 +1,535 @@
+#!/usr/bin/env python
+"""Benchmark of the lens image-simulation path on GB300.
+
+Workload (one "step"): a batch of 1024 EPL+SHEAR lens systems, 180x180 pixels at
+0.04"/pix, supersampling 3 (540x540 rays per system), SERSIC_ELLIPSE source and
+lens light, one 31x31 Moffat PSF per system -- simulated in ONE batched launch
+sequence of the FP32-split kernels, inputs resident in HBM.
+
+Reported beside it: the plain FP64 kernel at one request per launch, single-
+request latency, FP32-vs-FP64 and FP64-vs-oracle errors, the end-to-end rate
+through the public API with host buffers, the roofline of the dominant kernel,
+and the CPU baseline (the FP64 oracle on the host cores).
+
+``--impl reference`` times the reference's CPU path instead: the reference
+itself (JAXtronomy on JAX) cannot be installed here, so this arm times the FP64
+NumPy restatement of it (``oracle/``) on all host cores.
+"""
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "images/s + p50/p99 latency, batched FP32-split vs plain FP64, rel err<=1e-5"
+WORKLOAD = "batch_epl_180x180_s3_psf31"
+N_PIX, DPIX, SS, KSIZE = 180, 0.04, 3, 31
+
+# Algorithmic work per supersampled ray and per output pixel ("flop" = add, mul
+# or compare with FMA = 2; "T" = one transcendental call), counted from the
+# reference formulas: EPL 60 + 8 nmax flop / 7 T, SHEAR 8, SIE 20 / 5 T,
+# SERSIC_ELLIPSE 15 / 4 T, s x s re-binning 1; direct convolution 2 K^2 per pixel.
+FLOP_EPL_BASE, FLOP_EPL_PER_TERM, T_EPL = 60, 8, 7
+FLOP_SHEAR = 8
+FLOP_SERSIC, T_SERSIC = 15, 4
+FLOP_REDUCE = 1
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle port), run in spawn-started worker processes
+# ---------------------------------------------------------------------------
+
+_JOB_CACHE = {}
+
+
+def _oracle_inputs(seed):
+    if seed not in _JOB_CACHE:
+        from jaxtronomy_gb300 import workloads as W
+        model, lens, src, ll, kern = W.batch_epl(seed=seed, batch=8)
+        g = W.grid_kwargs(N_PIX, DPIX)
+        jobs = []
+        for i in range(8):
+            scene = dict(nx=N_PIX, ny=N_PIX, supersampling_factor=SS, psf_type="PIXEL",
+                         kernel=kern[i], lens_model_list=model["lens_model_list"],
+                         source_light_model_list=model["source_light_model_list"],
+                         lens_light_model_list=model["lens_light_model_list"], **g)
+            jobs.append((scene, W.instance(lens, i), W.instance(src, i), W.instance(ll, i)))
+        _JOB_CACHE[seed] = jobs
+    return _JOB_CACHE[seed]
+
+
+def _oracle_job(args):
+    seed, i = args
+    import warnings
+    warnings.simplefilter("ignore")
+    from oracle import image as oimage
+    scene, kl, ks, kll = _oracle_inputs(seed)[i % 8]
+    t = time.perf_counter()
+    oimage.image(scene, kl, ks, kll)
+    return time.perf_counter() - t
+
+
+def _spawn_pool(cores):
+    for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[v] = "1"
+    pool = mp.get_context("spawn").Pool(cores)
+    pool.map(_oracle_job, [(2001, 0)] * cores, chunksize=1)  # imports + input cache
+    return pool
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_cpu_sample(pool, cores, n_images, seed=2001):
+    jobs = [(seed, i % 8) for i in range(n_images)]
+    t0 = time.perf_counter()
+    pool.map(_oracle_job, jobs, chunksize=1)
+    return time.perf_counter() - t0
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def reference_arm(args):
+    """CPU reference path: the FP64 oracle over all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = cpu_cores()
+    per_step = 2 * cores
+    pool = _spawn_pool(cores)
+    try:
+        for _ in range(args.warmup):
+            run_cpu_sample(pool, cores, per_step)
+        times = [run_cpu_sample(pool, cores, per_step) for _ in range(args.steps)]
+    finally:
+        pool.close()
+    sec = statistics.mean(times)
+    value = per_step / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "images/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "batch_per_step": per_step, "grid": N_PIX,
+                   "supersampling": SS, "psf": KSIZE},
+        "cpu_baseline": {"value": value, "unit": "images/s", "cores": cores, "kind": "port",
+                         "sample": "%d systems of the workload per step, one per worker "
+                                   "process (spawn pool of %d), FP64 NumPy oracle; JAXtronomy "
+                                   "itself needs jax, which is not installable offline"
+                                   % (per_step, cores),
+                         "cpu": cpu_model()},
+        "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        outdir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else tempfile.gettempdir()
+        self.path = os.path.join(outdir, "clocks_rank%d.csv" % gpu_index)
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names[1:], p[5:9]):
+                if v.lower() in ("active", "0x1") or v == "Active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def ray_work(lens, n_inst, nmax_list):
+    rays = (N_PIX * SS) ** 2
+    flop = 0
+    tcount = 0
+    for nm in nmax_list:
+        flop += rays * (FLOP_EPL_BASE + FLOP_EPL_PER_TERM * nm + FLOP_SHEAR + 2 * FLOP_SERSIC
+                        + FLOP_REDUCE)
+        tcount += rays * (T_EPL + 2 * T_SERSIC)
+    return flop, tcount
+
+
+def epl_nmax(e1, e2):
+    import numpy as np
+    c = np.minimum(np.hypot(e1, e2), 0.9999)
+    q = (1 - c) / (1 + c)
+    f = (1 - q) / (1 + q)
+    out = []
+    for v in f:
+        if v == 0:
+            out.append(0)
+        elif v < 0.12:
+            out.append(10)
+        elif v < 0.4:
+            out.append(20)
+        elif v < 0.6:
+            out.append(35)
+        elif v < 0.73:
+            out.append(50)
+        elif v < 0.86:
+            out.append(100)
+        elif v < 0.92:
+            out.append(200)
+        else:
+            out.append(500)
+    return out
+
+
+def percentile(v, q):
+    v = sorted(v)
+    k = (len(v) - 1) * q
+    lo, hi = int(k), min(int(k) + 1, len(v) - 1)
+    return v[lo] + (v[hi] - v[lo]) * (k - lo)
+
+
+def gpu_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    cores = cpu_cores()
+    pool = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # spawn the oracle pool before the first CUDA call
+        pool = _spawn_pool(cores)
+
+    import numpy as np
+    import torch
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import _lib, workloads as W
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    B = args.batch
+    model, lens, src, ll, kern = W.batch_epl(seed=1001 + rank, batch=B, num_pix=N_PIX,
+                                             delta_pix=DPIX, supersampling=SS, kernel_size=KSIZE)
+    g = W.grid_kwargs(N_PIX, DPIX)
+
+    def make(precision):
+        data = J.ImageData(np.zeros((N_PIX, N_PIX)), exposure_time=1000.0, background_rms=0.01,
+                           **g)
+        return J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                            J.LensModel(model["lens_model_list"]),
+                            J.LightModel(model["source_light_model_list"]),
+                            J.LightModel(model["lens_light_model_list"]),
+                            kwargs_numerics={"supersampling_factor": SS, "precision": precision})
+
+    im32 = make("fp32")
+    im64 = make("fp64")
+    rows_host = im32.pack_params(lens, src, ll)
+    rows_dev = torch.as_tensor(rows_host).cuda()
+    psf32 = torch.as_tensor(kern, dtype=torch.float32).cuda().contiguous()
+    psf64 = torch.as_tensor(kern, dtype=torch.float64).cuda().contiguous()
+    out32 = torch.empty((B, N_PIX, N_PIX), dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        im32.image_batch(rows=rows_dev, psf_kernels=psf32, out=out32)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()  # evict L2 between timed steps (outside the step events)
+        starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = statistics.mean(step_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = B * world / (ms / 1e3)
+
+    extra = {}
+    if rank == 0:
+        # --- FP32 vs FP64 over the whole batch (FP64 batched, outside timing)
+        out64 = im64.image_batch(rows=rows_dev, psf_kernels=psf64)
+        a = out32.double()
+        b = out64
+        scale = b.abs().amax(dim=(1, 2), keepdim=True)
+        sig = b.abs() >= 1e-3 * scale
+        rel = ((a - b).abs() / b.abs().clamp_min(1e-300))[sig]
+        extra["fp32_vs_fp64_rel_err_max"] = float(rel.max())
+        extra["fp32_vs_fp64_rel_err_median"] = float(rel.median())
+        extra["fp32_vs_fp64_maxnorm_err_max"] = float(((a - b).abs() / scale).amax())
+        # --- FP64 kernel against the oracle on two systems
+        import warnings
+        warnings.simplefilter("ignore")
+        from oracle import image as oimage
+        errs = []
+        for i in range(2):
+            scene = dict(nx=N_PIX, ny=N_PIX, supersampling_factor=SS, psf_type="PIXEL",
+                         kernel=kern[i], lens_model_list=model["lens_model_list"],
+                         source_light_model_list=model["source_light_model_list"],
+                         lens_light_model_list=model["lens_light_model_list"], **g)
+            ref = oimage.image(scene, W.instance(lens, i), W.instance(src, i), W.instance(ll, i))
+            got = out64[i].cpu().numpy()
+            errs.append(float(np.max(np.abs(got - ref) / np.abs(ref))))
+            ref32 = out32[i].double().cpu().numpy()
+            errs.append(None)
+            extra.setdefault("fp32_vs_oracle_rel_err_max", 0.0)
+            extra["fp32_vs_oracle_rel_err_max"] = max(extra["fp32_vs_oracle_rel_err_max"],
+                                                      float(np.max(np.abs(ref32 - ref) / np.abs(ref))))
+        extra["fp64_vs_oracle_rel_err_max"] = max(e for e in errs if e is not None)
+
+        # --- plain FP64, one request per launch
+        n_plain = args.plain_sample
+        e0 = [torch.cuda.Event(enable_timing=True) for _ in range(n_plain)]
+        e1 = [torch.cuda.Event(enable_timing=True) for _ in range(n_plain)]
+        one64 = torch.empty((1, N_PIX, N_PIX), dtype=torch.float64, device="cuda")
+        im64.image_batch(rows=rows_dev[:1], psf_kernels=psf64[0], out=one64)
+        torch.cuda.synchronize()
+        for i in range(n_plain):
+            e0[i].record(stream)
+            im64.image_batch(rows=rows_dev[i:i + 1], psf_kernels=psf64[i], out=one64)
+            e1[i].record(stream)
+        torch.cuda.synchronize()
+        plain_ms = [a.elapsed_time(b) for a, b in zip(e0, e1)]
+        plain_ips = 1e3 / statistics.mean(plain_ms)
+        extra["fp64_plain_images_per_s"] = plain_ips
+        extra["fp64_plain_latency_ms_p50"] = percentile(plain_ms, 0.5)
+        extra["speedup_vs_fp64_plain"] = value / world / plain_ips
+
+        # --- FP32 single-request latency (one system per launch)
+        n1 = args.plain_sample * 2
+        one32 = torch.empty((1, N_PIX, N_PIX), dtype=torch.float32, device="cuda")
+        lat = []
+        for i in range(n1):
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            im32.image_batch(rows=rows_dev[i:i + 1], psf_kernels=psf32[i], out=one32)
+            s1.record(stream)
+            s1.synchronize()
+            lat.append(s0.elapsed_time(s1))
+        extra["fp32_single_request_latency_ms_p50"] = percentile(lat, 0.5)
+        extra["fp32_single_request_latency_ms_p99"] = percentile(lat, 0.99)
+
+        # --- stage timing for the roofline (L2 flushed before each rep)
+        low = torch.empty_like(out32)
+        lib = _lib.load()
+        from jaxtronomy_gb300 import _device
+        m32 = im32._model(range(2), range(1), range(1))
+        reps = 5
+        rt_ms, cv_ms = [], []
+        for _ in range(reps):
+            flush.zero_()
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            im32.image_batch(rows=rows_dev, psf_kernels=psf32, out=low, unconvolved=True)
+            a1.record(stream)
+            flush.zero_()
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record(stream)
+            _lib.check(lib.lensgb_convolve(m32.handle, _device.ptr(low), B, _device.ptr(psf32),
+                                           KSIZE * KSIZE, _device.ptr(out32),
+                                           _device.stream_handle()))
+            c1.record(stream)
+            torch.cuda.synchronize()
+            rt_ms.append(a0.elapsed_time(a1))
+            cv_ms.append(c0.elapsed_time(c1))
+        nm = epl_nmax(lens[0]["e1"], lens[0]["e2"])
+        flop_ray, t_ray = ray_work(lens, B, nm)
+        flop_conv = 2 * KSIZE * KSIZE * N_PIX * N_PIX * B
+        rt = statistics.mean(rt_ms) / 1e3
+        cv = statistics.mean(cv_ms) / 1e3
+        sm_mhz = clk.get("sm_mhz") or 2070.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
+        extra["roofline"] = {
+            "kernel": "raytrace_kernel<float>", "bound": "fp32", "unit": "TFLOP/s",
+            "achieved": flop_ray / rt / 1e12, "peak": fp32_peak,
+            "frac": flop_ray / rt / 1e12 / fp32_peak,
+            "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2) at the sampled "
+                           "median SM clock; MEASURED_PEAKS.json has no FP32 figure",
+            "algorithmic_gflop_per_launch": flop_ray / 1e9,
+            "transcendentals_per_s": t_ray / rt, "launch_ms": rt * 1e3, "traffic": None,
+        }
+        hbm_peak = 6784.5
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                hbm_peak = float(json.load(f)["hbm_gbs"])
+        except Exception:
+            pass
+        conv_bytes = B * N_PIX * N_PIX * 4 * 2 + B * KSIZE * KSIZE * 4
+        extra["roofline_conv"] = {
+            "kernel": "conv_kernel<float>", "bound": "fp32", "unit": "TFLOP/s",
+            "achieved": flop_conv / cv / 1e12, "peak": fp32_peak,
+            "frac": flop_conv / cv / 1e12 / fp32_peak, "launch_ms": cv * 1e3,
+            "hbm_gbs": conv_bytes / cv / 1e9, "hbm_frac_of_measured": conv_bytes / cv / 1e9 / hbm_peak,
+        }
+
+        # --- end to end through the public API with host buffers
+        rows_pin = torch.as_tensor(rows_host).pin_memory()
+        psf_pin = torch.as_tensor(kern, dtype=torch.float32).pin_memory()
+        out_pin = torch.empty((B, N_PIX, N_PIX), dtype=torch.float32).pin_memory()
+        rows_e = torch.empty_like(rows_dev)
+        psf_e = torch.empty_like(psf32)
+
+        def e2e_step():
+            rows_e.copy_(rows_pin, non_blocking=True)
+            psf_e.copy_(psf_pin, non_blocking=True)
+            im32.image_batch(rows=rows_e, psf_kernels=psf_e, out=out32)
+            out_pin.copy_(out32, non_blocking=True)
+
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = f0.elapsed_time(f1) / args.steps
+        h2d = rows_pin.numel() * 8 + psf_pin.numel() * 4
+        d2h = out_pin.numel() * 4
+        extra["e2e"] = {"value": B / (e2e_ms / 1e3), "unit": "images/s",
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": e2e_ms,
+                        "path": "ImageModel.image_batch -> lensgb_image, pinned host rows/PSFs "
+                                "in, images out, one stream"}
+
+        # --- CPU baseline (oracle port, bounded sample)
+        if pool is not None:
+            n_img = 4 * cores
+            sec = run_cpu_sample(pool, cores, n_img)
+            extra["cpu_baseline"] = {
+                "value": n_img / sec, "unit": "images/s", "cores": cores, "kind": "port",
+                "sample": "%d systems of the workload, FP64 NumPy oracle, spawn pool of %d "
+                          "workers" % (n_img, cores), "cpu": cpu_model()}
+            pool.close()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "batch_per_gpu": B, "grid": N_PIX,
+                       "delta_pix": DPIX, "supersampling": SS, "psf": KSIZE,
+                       "lens": "EPL+SHEAR", "light": "SERSIC_ELLIPSE source + lens light",
+                       "precision": "FP32 bulk, FP64 set-up / offsets / reductions",
+                       "l2": "flushed between timed steps by a 512 MiB memset outside the "
+                             "per-step CUDA events",
+                       "timing": "per-step CUDA events on the launch stream, mean over steps, "
+                                 "max over ranks"},
+            "latency_ms_p50": percentile(step_ms, 0.5), "latency_ms_p99": percentile(step_ms, 0.99),
+            "wall_s_timed_region": t_wall,
+            "gpu_launches": 3 * args.steps,
+            "clocks": clk,
+        }
+        line.update(extra)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--plain-sample", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

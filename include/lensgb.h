@@ -1,0 +1,180 @@
+/*
+ * lensgb.h -- C ABI of the GB300 lens image-simulation library (liblensgb.so).
+ *
+ * The library replaces the XLA program that JAXtronomy builds for
+ * ImageModel.image and the functions it calls:
+ *   ImageModel.image                  jaxtronomy/ImSim/image_model.py:432-492
+ *   ImageModel.likelihood_data_given_model  image_model.py:163-221
+ *   LensModel.ray_shooting / alpha    jaxtronomy/LensModel/lens_model.py:237-252,353-381
+ *                                     -> SinglePlane.ray_shooting/alpha single_plane.py:39-56,113-139
+ *   LightModel.surface_brightness     jaxtronomy/LightModel/light_model_base.py:230-252
+ *   Numerics.re_size_convolve         jaxtronomy/ImSim/Numerics/numerics.py:158-177
+ *
+ * Conventions
+ *  - Every pointer named *_dev is a device pointer; the caller owns all
+ *    buffers.  Arrays are dense, row-major and contiguous.
+ *  - Every entry point is asynchronous on the given CUDA stream (a
+ *    cudaStream_t passed as void*; NULL is the legacy default stream).
+ *  - Every entry point returns a status code (LENSGB_OK == 0) and never aborts.
+ *    lensgb_last_error() returns a thread-local description of the last
+ *    failure on the calling thread.
+ *  - A model handle owns device scratch and is used by one stream at a time.
+ *
+ * Per-system parameters are one row of doubles: the lens profiles' kwargs,
+ * then the source profiles', then the lens-light profiles', each profile in
+ * the order of its reference param_names (missing optional centres must be
+ * filled with their default 0):
+ *   SIE            theta_E e1 e2 center_x center_y                 (sie.py:40)
+ *   NIE            theta_E e1 e2 s_scale center_x center_y         (nie.py:19)
+ *   EPL            theta_E gamma e1 e2 center_x center_y           (epl.py:50)
+ *   SHEAR          gamma1 gamma2 ra_0 dec_0                        (shear.py:16)
+ *   NFW            Rs alpha_Rs center_x center_y                   (nfw.py:49)
+ *   TNFW           Rs alpha_Rs r_trunc center_x center_y           (tnfw.py:27)
+ *   SERSIC         amp R_sersic n_sersic center_x center_y         (sersic.py:27)
+ *   SERSIC_ELLIPSE amp R_sersic n_sersic e1 e2 center_x center_y   (sersic_ellipse.py:25)
+ */
+#ifndef LENSGB_H
+#define LENSGB_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LENSGB_OK 0
+#define LENSGB_ERR_INVALID 1     /* bad argument, shape or size            */
+#define LENSGB_ERR_UNSUPPORTED 2 /* unknown profile code or option         */
+#define LENSGB_ERR_OOM 3         /* device allocation failed               */
+#define LENSGB_ERR_CUDA 4        /* kernel launch / runtime failure        */
+
+/* ---- profile codes ------------------------------------------------------- */
+#define LENSGB_LENS_SIE 1
+#define LENSGB_LENS_NIE 2
+#define LENSGB_LENS_EPL 3
+#define LENSGB_LENS_SHEAR 4
+#define LENSGB_LENS_NFW 5
+#define LENSGB_LENS_TNFW 6
+
+#define LENSGB_LIGHT_SERSIC 1
+#define LENSGB_LIGHT_SERSIC_ELLIPSE 2
+
+/* ---- numerics ------------------------------------------------------------ */
+#define LENSGB_PSF_NONE 0
+#define LENSGB_PSF_PIXEL 1    /* zero-padded "same" convolution            */
+#define LENSGB_PSF_GAUSSIAN 2 /* edge-padded "same" convolution            */
+
+#define LENSGB_FP64 0       /* plain FP64 arithmetic throughout             */
+#define LENSGB_FP32_SPLIT 1 /* FP32 bulk; FP64 set-up and FP64-accurate offsets */
+
+#define LENSGB_MAX_PROFILES 8
+
+/* flags of lensgb_image */
+#define LENSGB_UNCONVOLVED 1   /* image(..., unconvolved=True)     */
+#define LENSGB_NO_SOURCE 2     /* image(..., source_add=False)     */
+#define LENSGB_NO_LENS_LIGHT 4 /* image(..., lens_light_add=False) */
+
+typedef struct lensgb_model lensgb_model;
+
+typedef struct {
+    int n_lens;
+    int lens_codes[LENSGB_MAX_PROFILES];
+    int n_source;
+    int source_codes[LENSGB_MAX_PROFILES];
+    double deflection_scaling[LENSGB_MAX_PROFILES]; /* per source, 1 = none */
+    int n_lens_light;
+    int lens_light_codes[LENSGB_MAX_PROFILES];
+    int nx, ny;            /* image columns, rows                               */
+    int supersampling;     /* supersampling_factor (>= 1)                       */
+    double transform_pix2angle[4]; /* row-major 2x2                             */
+    double ra_at_xy_0, dec_at_xy_0;
+    double flux_scaling;   /* ImageData.flux_scaling                             */
+    double alpha_scaling;  /* SinglePlane alpha_scaling                          */
+    int psf_type;          /* LENSGB_PSF_*                                       */
+    int kernel_size;       /* odd side of the PSF kernel (0 for NONE)            */
+    int precision;         /* LENSGB_FP64 or LENSGB_FP32_SPLIT                   */
+} lensgb_model_desc;
+
+/* Build a model (the "compile" step of ImageModel.__init__,
+ * image_model.py:27-150).  Validates codes and sizes; allocates nothing on the
+ * device until the first call that needs it. */
+int lensgb_model_create(const lensgb_model_desc* desc, lensgb_model** out);
+int lensgb_model_destroy(lensgb_model* model);
+
+/* Number of doubles per system row for this model. */
+int lensgb_model_param_count(const lensgb_model* model);
+
+/* ImageModel.image for n_inst systems (image_model.py:432-492).
+ *  params_dev : n_inst x param_count doubles
+ *  psf_dev    : PSF kernels, kernel_size^2 values each, FP64 for LENSGB_FP64
+ *               and FP32 for LENSGB_FP32_SPLIT, normalised by the caller;
+ *               psf_stride = elements between consecutive systems' kernels
+ *               (0 = one kernel shared by all systems).  Ignored for
+ *               LENSGB_PSF_NONE.
+ *  out_dev    : n_inst x ny x nx images, FP64 (LENSGB_FP64) or FP32.
+ *  flags      : LENSGB_UNCONVOLVED | LENSGB_NO_SOURCE | LENSGB_NO_LENS_LIGHT */
+int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
+                 const void* psf_dev, long long psf_stride, void* out_dev, int flags,
+                 void* stream);
+
+/* PixelKernelConvolution.convolution2d / GaussianConvolution.convolution2d
+ * (jaxtronomy/ImSim/Numerics/convolution.py:74-86,215-235) on n_inst images of
+ * the model's grid: "same"-mode convolution with the model's PSF type (PIXEL:
+ * zero padding, GAUSSIAN: edge padding).  in_dev / out_dev: n_inst x ny x nx in
+ * the model precision; psf_dev / psf_stride as for lensgb_image. */
+int lensgb_convolve(const lensgb_model* model, const void* in_dev, int n_inst,
+                    const void* psf_dev, long long psf_stride, void* out_dev, void* stream);
+
+/* Noise model of the likelihood (ImageData / ImageNoise,
+ * jaxtronomy/Data/imaging_data.py:159-182, image_noise.py:16-137).  Strides are
+ * elements between consecutive systems; 0 shares one array across systems. */
+typedef struct {
+    const double* data_dev;       /* ny x nx data per system                      */
+    long long data_stride;
+    const double* mask_dev;       /* ny x nx likelihood mask (0/1), NULL = all 1   */
+    const double* noise_map_dev;  /* ny x nx 1-sigma noise map, NULL = use below   */
+    long long noise_stride;
+    const double* exposure_map_dev; /* ny x nx exposure map (floored at 1e-10), NULL = scalar */
+    long long exposure_stride;
+    double exposure_time;         /* scalar exposure (floored at 1e-10)            */
+    double background_rms;
+    const double* error_map_dev;  /* additional variance map, NULL = none          */
+} lensgb_noise_desc;
+
+/* ImageModel.likelihood_data_given_model for n_inst systems
+ * (image_model.py:163-221): simulates the images into image_out_dev (caller
+ * buffer, same layout as lensgb_image's output) and writes one FP64
+ * log-likelihood per system to logl_dev. */
+int lensgb_loglike(lensgb_model* model, const double* params_dev, int n_inst,
+                   const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
+                   void* image_out_dev, double* logl_dev, void* stream);
+
+/* SinglePlane.ray_shooting for one parameter set over n arbitrary points
+ * (single_plane.py:39-56), FP64.  params_dev holds the lens profiles' kwargs
+ * only (the lens part of a system row). */
+int lensgb_ray_shooting(const lensgb_model* model, const double* params_dev,
+                        const double* x_dev, const double* y_dev, double* beta_x_dev,
+                        double* beta_y_dev, long long n, void* stream);
+
+/* SinglePlane.alpha (single_plane.py:113-139): deflection angles, same
+ * arguments as lensgb_ray_shooting. */
+int lensgb_alpha(const lensgb_model* model, const double* params_dev, const double* x_dev,
+                 const double* y_dev, double* alpha_x_dev, double* alpha_y_dev, long long n,
+                 void* stream);
+
+/* LightModel.surface_brightness of the model's source (which = 0) or lens
+ * light (which = 1) profiles over n arbitrary points (light_model_base.py:230-252),
+ * FP64.  params_dev holds that light model's kwargs only. */
+int lensgb_surface_brightness(const lensgb_model* model, int which, const double* params_dev,
+                              const double* x_dev, const double* y_dev, double* out_dev,
+                              long long n, void* stream);
+
+/* Description of the last error on the calling thread ("" if none). */
+const char* lensgb_last_error(void);
+
+/* ABI version of this header (major * 100 + minor). */
+int lensgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LENSGB_H */

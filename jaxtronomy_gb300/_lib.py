@@ -1,0 +1,155 @@
+"""ctypes binding of liblensgb.so (the C ABI declared in include/lensgb.h).
+
+The library is the only compute path: if it is missing this module raises,
+and there is no CPU fallback.
+"""
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblensgb.so")
+
+MAX_PROFILES = 8
+
+# status codes
+OK = 0
+ERR_INVALID = 1
+ERR_UNSUPPORTED = 2
+ERR_OOM = 3
+ERR_CUDA = 4
+
+# profile codes
+LENS_CODES = {"SIE": 1, "NIE": 2, "EPL": 3, "SHEAR": 4, "NFW": 5, "TNFW": 6}
+LIGHT_CODES = {"SERSIC": 1, "SERSIC_ELLIPSE": 2}
+
+PSF_NONE, PSF_PIXEL, PSF_GAUSSIAN = 0, 1, 2
+FP64, FP32_SPLIT = 0, 1
+
+UNCONVOLVED = 1
+NO_SOURCE = 2
+NO_LENS_LIGHT = 4
+
+# exported symbols (must match include/lensgb.h)
+SYMBOLS = [
+    "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
+    "lensgb_image", "lensgb_convolve", "lensgb_loglike", "lensgb_ray_shooting", "lensgb_alpha",
+    "lensgb_surface_brightness",
+    "lensgb_last_error", "lensgb_version",
+]
+
+
+class ModelDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_lens", ctypes.c_int),
+        ("lens_codes", ctypes.c_int * MAX_PROFILES),
+        ("n_source", ctypes.c_int),
+        ("source_codes", ctypes.c_int * MAX_PROFILES),
+        ("deflection_scaling", ctypes.c_double * MAX_PROFILES),
+        ("n_lens_light", ctypes.c_int),
+        ("lens_light_codes", ctypes.c_int * MAX_PROFILES),
+        ("nx", ctypes.c_int),
+        ("ny", ctypes.c_int),
+        ("supersampling", ctypes.c_int),
+        ("transform_pix2angle", ctypes.c_double * 4),
+        ("ra_at_xy_0", ctypes.c_double),
+        ("dec_at_xy_0", ctypes.c_double),
+        ("flux_scaling", ctypes.c_double),
+        ("alpha_scaling", ctypes.c_double),
+        ("psf_type", ctypes.c_int),
+        ("kernel_size", ctypes.c_int),
+        ("precision", ctypes.c_int),
+    ]
+
+
+class NoiseDesc(ctypes.Structure):
+    _fields_ = [
+        ("data_dev", ctypes.c_void_p),
+        ("data_stride", ctypes.c_longlong),
+        ("mask_dev", ctypes.c_void_p),
+        ("noise_map_dev", ctypes.c_void_p),
+        ("noise_stride", ctypes.c_longlong),
+        ("exposure_map_dev", ctypes.c_void_p),
+        ("exposure_stride", ctypes.c_longlong),
+        ("exposure_time", ctypes.c_double),
+        ("background_rms", ctypes.c_double),
+        ("error_map_dev", ctypes.c_void_p),
+    ]
+
+
+class LensgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("liblensgb error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load liblensgb.so once; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            "liblensgb.so is not built (%s); run `python -m jaxtronomy_gb300.build`" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, dp, i, ll = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+    lib.lensgb_model_create.argtypes = [ctypes.POINTER(ModelDesc), ctypes.POINTER(vp)]
+    lib.lensgb_model_create.restype = i
+    lib.lensgb_model_destroy.argtypes = [vp]
+    lib.lensgb_model_destroy.restype = i
+    lib.lensgb_model_param_count.argtypes = [vp]
+    lib.lensgb_model_param_count.restype = i
+    lib.lensgb_image.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
+    lib.lensgb_image.restype = i
+    lib.lensgb_convolve.argtypes = [vp, vp, i, vp, ll, vp, vp]
+    lib.lensgb_convolve.restype = i
+    lib.lensgb_loglike.argtypes = [vp, dp, i, vp, ll, ctypes.POINTER(NoiseDesc), vp, dp, vp]
+    lib.lensgb_loglike.restype = i
+    lib.lensgb_ray_shooting.argtypes = [vp, dp, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_ray_shooting.restype = i
+    lib.lensgb_alpha.argtypes = [vp, dp, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_alpha.restype = i
+    lib.lensgb_surface_brightness.argtypes = [vp, i, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_surface_brightness.restype = i
+    lib.lensgb_last_error.argtypes = []
+    lib.lensgb_last_error.restype = ctypes.c_char_p
+    lib.lensgb_version.argtypes = []
+    lib.lensgb_version.restype = i
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != OK:
+        msg = load().lensgb_last_error().decode("utf-8", "replace")
+        raise LensgbError(rc, msg)
+
+
+class Model:
+    """Owner of one lensgb_model handle."""
+
+    def __init__(self, desc):
+        lib = load()
+        h = ctypes.c_void_p()
+        check(lib.lensgb_model_create(ctypes.byref(desc), ctypes.byref(h)))
+        self._h = h
+        self.desc = desc
+        self.param_count = lib.lensgb_model_param_count(h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            load().lensgb_model_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

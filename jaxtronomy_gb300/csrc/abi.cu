@@ -1,0 +1,363 @@
+// C ABI of liblensgb.so (declared in include/lensgb.h).
+//
+// A model handle is the compiled form of one ImageModel
+// (JAXtronomy ImSim/image_model.py:27-150): the profile stack, the pixel grid
+// and numerics options, plus grow-only device scratch for the per-profile
+// records, the EPL coefficient tables and the un-convolved image.
+#include <math.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "launch.h"
+
+using namespace lensgb;
+
+struct lensgb_model {
+    lensgb_model_desc desc;
+    GridDesc grid;
+    StackDesc st;
+    double pixel_width;
+    int cap_inst = 0;
+    double* rec_d = nullptr;
+    float* rec_f = nullptr;
+    double* coef_d = nullptr;
+    float* coef_f = nullptr;
+    void* lowres = nullptr;
+};
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+static int lens_param_count(int code) {
+    switch (code) {
+        case LENSGB_LENS_SIE: return 5;
+        case LENSGB_LENS_NIE: return 6;
+        case LENSGB_LENS_EPL: return 6;
+        case LENSGB_LENS_SHEAR: return 4;
+        case LENSGB_LENS_NFW: return 4;
+        case LENSGB_LENS_TNFW: return 5;
+        default: return -1;
+    }
+}
+
+static int light_param_count(int code) {
+    switch (code) {
+        case LENSGB_LIGHT_SERSIC: return 5;
+        case LENSGB_LIGHT_SERSIC_ELLIPSE: return 7;
+        default: return -1;
+    }
+}
+
+static int check_cuda(const char* where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return fail(LENSGB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    return LENSGB_OK;
+}
+
+static void free_scratch(lensgb_model* m) {
+    cudaFree(m->rec_d);
+    cudaFree(m->rec_f);
+    cudaFree(m->coef_d);
+    cudaFree(m->coef_f);
+    cudaFree(m->lowres);
+    m->rec_d = nullptr;
+    m->rec_f = nullptr;
+    m->coef_d = nullptr;
+    m->coef_f = nullptr;
+    m->lowres = nullptr;
+    m->cap_inst = 0;
+}
+
+static int ensure_scratch(lensgb_model* m, int n_inst) {
+    if (n_inst <= m->cap_inst) return LENSGB_OK;
+    int cap = m->cap_inst > 0 ? m->cap_inst : 1;
+    while (cap < n_inst) cap *= 2;
+    free_scratch(m);
+    const int n_prof = m->st.n_lens + m->st.n_src + m->st.n_ll;
+    const size_t nrec = (size_t)cap * (n_prof > 0 ? n_prof : 1);
+    const size_t ncoef = (size_t)cap * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
+    const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
+    const size_t nimg = (size_t)cap * m->grid.nx * m->grid.ny;
+    if (cudaMalloc(&m->rec_d, nrec * REC_D * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->rec_f, nrec * REC_F * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->coef_d, ncoef * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->coef_f, ncoef * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&m->lowres, nimg * esz) != cudaSuccess) {
+        cudaGetLastError();
+        free_scratch(m);
+        return fail(LENSGB_ERR_OOM, "device allocation of model scratch failed");
+    }
+    m->cap_inst = cap;
+    return LENSGB_OK;
+}
+
+// Number of significant bits of the FP32 "exact" step so that index * step
+// stays exact for every supersampled index of the grid.
+static int exact_bits(int n) {
+    int b = 0;
+    while ((1 << b) < n) ++b;
+    int bits = 24 - b;
+    return bits < 1 ? 1 : bits;
+}
+
+extern "C" {
+
+int lensgb_version(void) { return 100; }
+
+const char* lensgb_last_error(void) { return g_last_error.c_str(); }
+
+int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
+    if (!d || !out) return fail(LENSGB_ERR_INVALID, "null descriptor or output pointer");
+    *out = nullptr;
+    if (d->n_lens < 0 || d->n_lens > LENSGB_MAX_PROFILES || d->n_source < 0 ||
+        d->n_source > LENSGB_MAX_PROFILES || d->n_lens_light < 0 ||
+        d->n_lens_light > LENSGB_MAX_PROFILES)
+        return fail(LENSGB_ERR_INVALID, "profile count out of range (0..8 per list)");
+    if (d->nx <= 0 || d->ny <= 0 || d->supersampling < 1)
+        return fail(LENSGB_ERR_INVALID, "grid size and supersampling must be positive");
+    if (d->supersampling > 32)
+        return fail(LENSGB_ERR_INVALID, "supersampling factor above 32 is not supported");
+    if ((long long)d->nx * d->supersampling > (1 << 22) ||
+        (long long)d->ny * d->supersampling > (1 << 22))
+        return fail(LENSGB_ERR_INVALID, "supersampled grid side exceeds 2^22");
+    if (d->precision != LENSGB_FP64 && d->precision != LENSGB_FP32_SPLIT)
+        return fail(LENSGB_ERR_UNSUPPORTED, "unknown precision mode");
+    if (d->psf_type != LENSGB_PSF_NONE && d->psf_type != LENSGB_PSF_PIXEL &&
+        d->psf_type != LENSGB_PSF_GAUSSIAN)
+        return fail(LENSGB_ERR_UNSUPPORTED, "psf_type must be NONE, PIXEL or GAUSSIAN");
+    if (d->psf_type != LENSGB_PSF_NONE && (d->kernel_size < 1 || d->kernel_size % 2 == 0 ||
+                                           d->kernel_size > 255))
+        return fail(LENSGB_ERR_INVALID, "kernel_size must be odd and in 1..255");
+    lensgb_model* m = new lensgb_model();
+    m->desc = *d;
+    StackDesc& st = m->st;
+    st.n_lens = d->n_lens;
+    st.n_src = d->n_source;
+    st.n_ll = d->n_lens_light;
+    int off = 0;
+    st.n_epl = 0;
+    for (int i = 0; i < MAX_PROF; ++i) {
+        st.lens[i] = st.src[i] = st.ll[i] = 0;
+        st.lens_off[i] = st.src_off[i] = st.ll_off[i] = 0;
+        st.epl_slot[i] = -1;
+        st.src_scale[i] = 1.0;
+    }
+    for (int i = 0; i < d->n_lens; ++i) {
+        int c = lens_param_count(d->lens_codes[i]);
+        if (c < 0) {
+            delete m;
+            return fail(LENSGB_ERR_UNSUPPORTED, "unsupported lens profile code");
+        }
+        st.lens[i] = d->lens_codes[i];
+        st.lens_off[i] = off;
+        off += c;
+        if (d->lens_codes[i] == LENSGB_LENS_EPL) st.epl_slot[i] = st.n_epl++;
+    }
+    for (int i = 0; i < d->n_source; ++i) {
+        int c = light_param_count(d->source_codes[i]);
+        if (c < 0) {
+            delete m;
+            return fail(LENSGB_ERR_UNSUPPORTED, "unsupported source light profile code");
+        }
+        st.src[i] = d->source_codes[i];
+        st.src_off[i] = off;
+        st.src_scale[i] = d->deflection_scaling[i];
+        off += c;
+    }
+    for (int i = 0; i < d->n_lens_light; ++i) {
+        int c = light_param_count(d->lens_light_codes[i]);
+        if (c < 0) {
+            delete m;
+            return fail(LENSGB_ERR_UNSUPPORTED, "unsupported lens light profile code");
+        }
+        st.ll[i] = d->lens_light_codes[i];
+        st.ll_off[i] = off;
+        off += c;
+    }
+    st.n_params = off;
+    st.alpha_scaling = d->alpha_scaling;
+    st.flux_scaling = d->flux_scaling;
+
+    GridDesc& g = m->grid;
+    const double* M = d->transform_pix2angle;
+    const int s = d->supersampling;
+    g.nx = d->nx;
+    g.ny = d->ny;
+    g.s = s;
+    const double f0 = 0.5 / s - 0.5;
+    g.ra00 = d->ra_at_xy_0 + M[0] * f0 + M[1] * f0;
+    g.dec00 = d->dec_at_xy_0 + M[2] * f0 + M[3] * f0;
+    g.ax = M[0] / s;
+    g.bx = M[1] / s;
+    g.ay = M[2] / s;
+    g.by = M[3] / s;
+    const int bits = exact_bits((d->nx > d->ny ? d->nx : d->ny) * s);
+    split_bits(g.ax, bits, g.ax_hi, g.ax_lo);
+    split_bits(g.bx, bits, g.bx_hi, g.bx_lo);
+    split_bits(g.ay, bits, g.ay_hi, g.ay_lo);
+    split_bits(g.by, bits, g.by_hi, g.by_lo);
+    m->pixel_width = sqrt(fabs(M[0] * M[3] - M[1] * M[2]));
+    *out = m;
+    return LENSGB_OK;
+}
+
+int lensgb_model_destroy(lensgb_model* m) {
+    if (!m) return LENSGB_OK;
+    free_scratch(m);
+    delete m;
+    return LENSGB_OK;
+}
+
+int lensgb_model_param_count(const lensgb_model* m) { return m ? m->st.n_params : -1; }
+
+int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                 long long psf_stride, void* out, int flags, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!out || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    int rc = ensure_scratch(m, n_inst);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_prepare(m->grid, m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    const double scale = m->pixel_width * m->pixel_width;
+    void* target = conv ? m->lowres : out;
+    launch_raytrace(m->grid, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
+                    flags, scale, m->desc.precision, s);
+    if ((rc = check_cuda("raytrace launch"))) return rc;
+    if (conv) {
+        if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                        m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
+                        m->desc.precision, s))
+            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = check_cuda("convolution launch"))) return rc;
+    }
+    return LENSGB_OK;
+}
+
+int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const void* psf,
+                    long long psf_stride, void* out, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (m->desc.psf_type == LENSGB_PSF_NONE)
+        return fail(LENSGB_ERR_INVALID, "model has psf_type NONE");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!in || !out || !psf) return fail(LENSGB_ERR_INVALID, "null image or PSF pointer");
+    if (in == out) return fail(LENSGB_ERR_INVALID, "in-place convolution is not supported");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    if (launch_conv(in, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                    m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
+                    m->desc.precision, (cudaStream_t)stream))
+        return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+    return check_cuda("convolution launch");
+}
+
+int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                   long long psf_stride, const lensgb_noise_desc* nd, void* image_out,
+                   double* logl, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
+    if (!image_out || !logl) return fail(LENSGB_ERR_INVALID, "null image or logL output");
+    if (!nd->noise_map_dev && !nd->exposure_map_dev && !(nd->exposure_time > 0))
+        return fail(LENSGB_ERR_INVALID, "exposure time must be positive without a noise map");
+    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0)
+        return fail(LENSGB_ERR_INVALID, "negative stride");
+    int rc = lensgb_image(m, params, n_inst, psf, psf_stride, image_out, 0, stream);
+    if (rc) return rc;
+    if (n_inst == 0) return LENSGB_OK;
+    LoglikeArgs a;
+    a.data = nd->data_dev;
+    a.data_stride = nd->data_stride;
+    a.mask = nd->mask_dev;
+    a.noise_map = nd->noise_map_dev;
+    a.noise_stride = nd->noise_stride;
+    a.exposure = nd->exposure_map_dev;
+    a.exposure_stride = nd->exposure_stride;
+    a.exposure_time = nd->exposure_time;
+    a.background_rms = nd->background_rms;
+    a.error_map = nd->error_map_dev;
+    launch_loglike(image_out, n_inst, (long long)m->grid.nx * m->grid.ny, a, logl,
+                   m->desc.precision, (cudaStream_t)stream);
+    return check_cuda("likelihood launch");
+}
+
+static int ray_points(const lensgb_model* mc, const double* params, const double* x,
+                      const double* y, double* bx, double* by, long long n, int want_alpha,
+                      void* stream) {
+    lensgb_model* m = const_cast<lensgb_model*>(mc);
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n < 0) return fail(LENSGB_ERR_INVALID, "negative point count");
+    if (n == 0) return LENSGB_OK;
+    if (!x || !y || !bx || !by) return fail(LENSGB_ERR_INVALID, "null coordinate pointer");
+    if (!params && m->st.n_lens > 0) return fail(LENSGB_ERR_INVALID, "null params pointer");
+    int rc = ensure_scratch(m, 1);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    // only the lens part of the row is meaningful; light records are unused
+    StackDesc st = m->st;
+    st.n_src = 0;
+    st.n_ll = 0;
+    launch_prepare(m->grid, st, params, 1, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    launch_ray_shoot_points(st, m->rec_d, m->coef_d, x, y, bx, by, n, want_alpha, s);
+    return check_cuda("ray shooting launch");
+}
+
+int lensgb_ray_shooting(const lensgb_model* m, const double* params, const double* x,
+                        const double* y, double* bx, double* by, long long n, void* stream) {
+    return ray_points(m, params, x, y, bx, by, n, 0, stream);
+}
+
+int lensgb_alpha(const lensgb_model* m, const double* params, const double* x, const double* y,
+                 double* ax, double* ay, long long n, void* stream) {
+    return ray_points(m, params, x, y, ax, ay, n, 1, stream);
+}
+
+int lensgb_surface_brightness(const lensgb_model* mc, int which, const double* params,
+                              const double* x, const double* y, double* out, long long n,
+                              void* stream) {
+    lensgb_model* m = const_cast<lensgb_model*>(mc);
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (which != 0 && which != 1) return fail(LENSGB_ERR_INVALID, "which must be 0 or 1");
+    if (n < 0) return fail(LENSGB_ERR_INVALID, "negative point count");
+    if (n == 0) return LENSGB_OK;
+    if (!x || !y || !out) return fail(LENSGB_ERR_INVALID, "null coordinate pointer");
+    int rc = ensure_scratch(m, 1);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    // records for a row holding only this light model: offsets start at 0
+    StackDesc st = m->st;
+    st.n_lens = 0;
+    const int base = which == 0 ? m->st.src_off[0] : m->st.ll_off[0];
+    if (which == 0) {
+        st.n_ll = 0;
+        for (int k = 0; k < st.n_src; ++k) st.src_off[k] -= base;
+    } else {
+        st.n_src = 0;
+        for (int k = 0; k < m->st.n_ll; ++k) {
+            st.src[k] = m->st.ll[k];
+            st.src_off[k] = m->st.ll_off[k] - base;
+        }
+        st.n_src = m->st.n_ll;
+        st.n_ll = 0;
+    }
+    launch_prepare(m->grid, st, params, 1, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    launch_light_points(st, 0, m->rec_d, x, y, out, n, s);
+    return check_cuda("surface brightness launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// Shared definitions of the lens image kernels: per-profile parameter
+// records, error-free FP32 transforms and small math helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lensgb.h"
+
+namespace lensgb {
+
+// Derived per-(system, profile) record written by the prepare kernel.  Doubles
+// serve the FP64 kernels and FP64 set-up; floats serve the FP32 kernels.
+constexpr int REC_D = 24;
+constexpr int REC_F = 24;
+// EPL series coefficient table length (largest reference nmax, epl.py:311-319)
+constexpr int EPL_NMAX = 500;
+constexpr int MAX_PROF = LENSGB_MAX_PROFILES;
+
+// Common record slots
+//   d[0], d[1]           profile centre (center_x, center_y) or (ra_0, dec_0)
+//   f[0..3]              FP32 split of the centre offset of the supersampled
+//                        ray (0, 0):  X0 = ra(0,0) - cx = f0 + f1,
+//                        Y0 = dec(0,0) - cy = f2 + f3
+constexpr int RD_CX = 0, RD_CY = 1;
+constexpr int RF_X0H = 0, RF_X0L = 1, RF_Y0H = 2, RF_Y0L = 3;
+
+// Grid description shared by all kernels of one model.
+struct GridDesc {
+    int nx, ny, s;            // columns, rows, supersampling
+    double ra00, dec00;       // coordinate of supersampled ray (0, 0)
+    double ax, bx, ay, by;    // coordinate steps per supersampled column / row
+    float ax_hi, ax_lo, bx_hi, bx_lo, ay_hi, ay_lo, by_hi, by_lo;
+};
+
+// Static description of the profile stack of a model.
+struct StackDesc {
+    int n_lens, n_src, n_ll;
+    int lens[MAX_PROF];
+    int src[MAX_PROF];
+    int ll[MAX_PROF];
+    int lens_off[MAX_PROF];   // column of each profile in a system row
+    int src_off[MAX_PROF];
+    int ll_off[MAX_PROF];
+    int epl_slot[MAX_PROF];   // EPL coefficient slot of each lens profile (-1: none)
+    int n_epl;
+    int n_params;
+    double src_scale[MAX_PROF];  // deflection_scaling per source
+    double alpha_scaling;
+    double flux_scaling;
+};
+
+// ---------------------------------------------------------------------------
+// FP32 error-free transforms (Knuth TwoSum, Dekker split)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+    float s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// x - centre for the supersampled ray (I, J), as a float carrying the
+// accuracy of an FP64 subtraction: the centre offset X0 is an FP64 value split
+// into (hi, lo) floats, and J*a_hi is exact because a_hi has at most 12
+// significant bits.
+__device__ __forceinline__ float split_offset(float x0h, float x0l, float p_exact, float p_small) {
+    float e;
+    float s = two_sum(x0h, p_exact, e);
+    return __fadd_rn(s, __fadd_rn(e, __fadd_rn(x0l, p_small)));
+}
+
+// Host/device: split an FP64 value into a float with at most `bits`
+// significant bits and the float remainder.
+__host__ __device__ inline void split_bits(double v, int bits, float& hi, float& lo) {
+    if (v == 0.0) { hi = 0.f; lo = 0.f; return; }
+    int e;
+    double m = frexp(v, &e);                 // v = m * 2^e, 0.5 <= |m| < 1
+    double scale = ldexp(1.0, bits);
+    double mh = trunc(m * scale) / scale;    // keep `bits` bits
+    double h = ldexp(mh, e);
+    hi = (float)h;
+    lo = (float)(v - h);
+}
+
+__host__ __device__ inline void split_double(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+// nan_to_num(posinf=1e10, neginf=-1e10), as used at epl.py:391-392
+template <typename R>
+__device__ __forceinline__ R nan_to_num_1e10(R v) {
+    if (isnan(v)) return R(0);
+    if (isinf(v)) return v > 0 ? R(1e10) : R(-1e10);
+    return v;
+}
+
+// nan_to_num() with NumPy defaults, as used at sersic_utils.py:267
+template <typename R>
+__device__ __forceinline__ R nan_to_num_max(R v) {
+    if (isnan(v)) return R(0);
+    if (isinf(v)) return v > 0 ? (sizeof(R) == 8 ? R(1.7976931348623157e308) : R(3.4028234663852886e38))
+                               : (sizeof(R) == 8 ? R(-1.7976931348623157e308) : R(-3.4028234663852886e38));
+    return v;
+}
+
+}  // namespace lensgb

@@ -1,0 +1,125 @@
+// Direct "same"-mode 2-D PSF convolution with a shared-memory halo tile.
+//
+// Replaces PixelKernelConvolution.convolution2d (fftconvolve / convolve2d,
+// "same" mode, zero boundary; JAXtronomy ImSim/Numerics/convolution.py:74-86)
+// and the edge-padded GaussianConvolution.convolution2d (convolution.py:215-235).
+// For odd K with h = K/2:
+//   out[y][x] = sum_{u,v} ker[K-1-u][K-1-v] * in[y+u-h][x+v-h]
+// with in[] = 0 outside the image (zero padding) or clamped to the nearest edge
+// pixel (edge padding).
+//
+// Each CTA computes a TILE_H x TILE_W output tile of one system; the flipped
+// kernel and the (TILE_H+K-1) x (TILE_W+KP-1) input halo tile sit in shared
+// memory.  Each thread accumulates an RY x CX register block, streaming one
+// input row segment at a time through registers and reusing it for every
+// output row of its block that the row touches.
+#include "launch.h"
+
+namespace lensgb {
+
+constexpr int CONV_TX = 8, CONV_TY = 16;
+
+template <typename R, int CX, int RY, int VC>
+__global__ void __launch_bounds__(CONV_TX* CONV_TY)
+conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__ ker,
+            long long kstride, int ny, int nx, int K, int edge) {
+    constexpr int W = CONV_TX * CX, H = CONV_TY * RY;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R* sk = (R*)smem_raw;
+    const int KP = ((K + VC - 1) / VC) * VC;
+    const int SW = W + KP - 1 + 1;  // +1 keeps row starts off the same bank
+    const int SH = H + K - 1;
+    R* si = sk + K * KP;
+    const int inst = blockIdx.z;
+    const int ox0 = blockIdx.x * W, oy0 = blockIdx.y * H;
+    const int h = K / 2;
+    const int tid = threadIdx.y * CONV_TX + threadIdx.x;
+    const int nthr = CONV_TX * CONV_TY;
+    const R* kk = ker + (long long)inst * kstride;
+    for (int e = tid; e < K * KP; e += nthr) {
+        int u = e / KP, v = e - u * KP;
+        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : R(0);
+    }
+    const R* img = in + (long long)inst * ny * nx;
+    for (int e = tid; e < SH * SW; e += nthr) {
+        int r = e / SW, c = e - r * SW;
+        int gy = oy0 - h + r, gx = ox0 - h + c;
+        R v;
+        if (edge) {
+            gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+            gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+            v = img[(long long)gy * nx + gx];
+        } else {
+            v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : R(0);
+        }
+        si[e] = v;
+    }
+    __syncthreads();
+
+    R acc[RY][CX];
+#pragma unroll
+    for (int i = 0; i < RY; ++i)
+#pragma unroll
+        for (int c = 0; c < CX; ++c) acc[i][c] = 0;
+    const int c0 = threadIdx.x * CX, r0 = threadIdx.y * RY;
+    for (int ir = 0; ir < RY + K - 1; ++ir) {
+        const R* row = si + (r0 + ir) * SW + c0;
+        for (int v0 = 0; v0 < KP; v0 += VC) {
+            R seg[CX + VC - 1];
+#pragma unroll
+            for (int j = 0; j < CX + VC - 1; ++j) seg[j] = row[v0 + j];
+#pragma unroll
+            for (int i = 0; i < RY; ++i) {
+                const int u = ir - i;
+                if (u < 0 || u >= K) continue;
+                const R* kr = sk + u * KP + v0;
+#pragma unroll
+                for (int vv = 0; vv < VC; ++vv) {
+                    const R w = kr[vv];
+#pragma unroll
+                    for (int c = 0; c < CX; ++c) acc[i][c] = fma(w, seg[c + vv], acc[i][c]);
+                }
+            }
+        }
+    }
+    R* o = out + (long long)inst * ny * nx;
+#pragma unroll
+    for (int i = 0; i < RY; ++i) {
+        const int y = oy0 + r0 + i;
+        if (y >= ny) continue;
+#pragma unroll
+        for (int c = 0; c < CX; ++c) {
+            const int x = ox0 + c0 + c;
+            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+        }
+    }
+}
+
+template <typename R, int CX, int RY, int VC>
+static int run_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
+                    int ny, int nx, int K, int edge, cudaStream_t stream) {
+    constexpr int W = CONV_TX * CX, H = CONV_TY * RY;
+    const int KP = ((K + VC - 1) / VC) * VC;
+    const int SW = W + KP - 1 + 1;
+    const int SH = H + K - 1;
+    size_t smem = (size_t)(K * KP + SH * SW) * sizeof(R);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(conv_kernel<R, CX, RY, VC>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return -1;
+    }
+    dim3 grid((unsigned)((nx + W - 1) / W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
+    dim3 block(CONV_TX, CONV_TY);
+    conv_kernel<R, CX, RY, VC><<<grid, block, smem, stream>>>(
+        (const R*)in, (R*)out, (const R*)kernel, kstride, ny, nx, K, edge);
+    return 0;
+}
+
+int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
+                int ny, int nx, int K, int edge, int precision, cudaStream_t stream) {
+    if (precision == LENSGB_FP64)
+        return run_conv<double, 4, 4, 4>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
+    return run_conv<float, 8, 4, 8>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
+}
+
+}  // namespace lensgb

@@ -1,0 +1,51 @@
+// Host-side launchers shared between the kernel translation units and the
+// C ABI (abi.cu).  Internal to liblensgb.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace lensgb {
+
+int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
+                   double* rec_d, float* rec_f, double* coef_d, float* coef_f,
+                   cudaStream_t stream);
+
+// Supersampled ray tracing + light + s x s re-binning into a (ny, nx) image per
+// system, scaled by out_scale (pixel_width^2).  `precision` selects FP64 or FP32.
+int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
+                    const float* rec_f, const double* coef_d, const float* coef_f, void* out,
+                    int flags, double out_scale, int precision, cudaStream_t stream);
+
+// "same"-mode 2-D convolution of n_inst (ny, nx) images with K x K kernels
+// (kernel stride 0 = shared).  edge = 0: zero padding; 1: edge padding.
+int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
+                int ny, int nx, int K, int edge, int precision, cudaStream_t stream);
+
+// Noise description of the likelihood reduction (device pointers; strides in
+// elements between systems, 0 = shared by all systems).
+struct LoglikeArgs {
+    const double* data;
+    long long data_stride;
+    const double* mask;       // ny*nx or null (all pixels)
+    const double* noise_map;  // or null
+    long long noise_stride;
+    const double* exposure;   // exposure map (already floored) or null
+    long long exposure_stride;
+    double exposure_time;     // used when exposure is null
+    double background_rms;
+    const double* error_map;  // additional variance map or null
+};
+
+int launch_loglike(const void* model, int n_inst, long long npix, const LoglikeArgs& a,
+                   double* out, int precision, cudaStream_t stream);
+
+// Point-wise single-parameter-set evaluation (FP64).
+int launch_ray_shoot_points(const StackDesc& st, const double* rec_d, const double* coef_d,
+                            const double* x, const double* y, double* bx, double* by,
+                            long long n, int want_alpha, cudaStream_t stream);
+int launch_light_points(const StackDesc& st, int which, const double* rec_d, const double* x,
+                        const double* y, double* out, long long n, cudaStream_t stream);
+
+}  // namespace lensgb

@@ -1,0 +1,165 @@
+// Prepare kernel: converts each system's raw kwargs row into per-profile
+// records (FP64 and FP32 copies) and the EPL series coefficient tables.
+// One thread per (system, profile).  All arithmetic here is FP64.
+//
+// Parameter conversions follow (JAXtronomy source tree):
+//   ellipticity2phi_q   Util/param_util.py:88-99
+//   NIE._param_conv     LensModel/Profiles/nie.py:182-200, :255-272
+//   EPL._param_conv     LensModel/Profiles/epl.py:111-124; nmax choice :311-319
+//   F_n recurrence      Util/hyp2f1_util.py:156-166
+//   NFW.alpha2rho0      LensModel/Profiles/nfw.py:386-395 (Rs floor :100)
+//   SersicUtil.b_n      LensModel/Profiles/sersic_utils.py:69-80, floors :239-258
+//   product average     Util/param_util.py:103-123
+#include <math.h>
+
+#include "launch.h"
+#include "profiles.cuh"
+
+namespace lensgb {
+
+__device__ static void ellip_phi_q(double e1, double e2, double& phi, double& q) {
+    phi = atan2(e2, e1) / 2;
+    double c = sqrt(e1 * e1 + e2 * e2);
+    c = c < 0.9999 ? c : 0.9999;
+    q = (1 - c) / (1 + c);
+}
+
+__device__ static int epl_nmax_of(double f) {
+    if (f == 0) return 0;
+    if (f < 0.12) return 10;
+    if (f < 0.4) return 20;
+    if (f < 0.6) return 35;
+    if (f < 0.73) return 50;
+    if (f < 0.86) return 100;
+    if (f < 0.92) return 200;
+    return 500;
+}
+
+// FP32 split of the offset between the supersampled ray (0,0) and a centre.
+__device__ static void write_offsets(const GridDesc& g, double cx, double cy, float* f) {
+    split_double(g.ra00 - cx, f[RF_X0H], f[RF_X0L]);
+    split_double(g.dec00 - cy, f[RF_Y0H], f[RF_Y0L]);
+}
+
+__global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
+                               int n_inst, double* __restrict__ rec_d, float* __restrict__ rec_f,
+                               double* __restrict__ coef_d, float* __restrict__ coef_f) {
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)n_inst * n_prof) return;
+    const int inst = (int)(gid / n_prof);
+    const int p = (int)(gid % n_prof);
+    const double* P = params + (long long)inst * st.n_params;
+    double* d = rec_d + ((long long)inst * n_prof + p) * REC_D;
+    float* f = rec_f + ((long long)inst * n_prof + p) * REC_F;
+    for (int k = 0; k < REC_D; ++k) d[k] = 0.0;
+
+    int kind, code, off;
+    if (p < st.n_lens) {
+        kind = 0; code = st.lens[p]; off = st.lens_off[p];
+    } else if (p < st.n_lens + st.n_src) {
+        kind = 1; code = st.src[p - st.n_lens]; off = st.src_off[p - st.n_lens];
+    } else {
+        kind = 2; code = st.ll[p - st.n_lens - st.n_src]; off = st.ll_off[p - st.n_lens - st.n_src];
+    }
+    const double* a = P + off;
+
+    if (kind == 0) {
+        if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
+            double theta_E = a[0], e1 = a[1], e2 = a[2];
+            double s_scale = code == LENSGB_LENS_SIE ? 0.0000000001 : a[3];
+            int co = code == LENSGB_LENS_SIE ? 3 : 4;
+            double phi, q;
+            ellip_phi_q(e1, e2, phi, q);
+            double theta_E_conv = theta_E / sqrt((1.0 + q * q) / (2.0 * q));
+            double b = theta_E_conv * sqrt((1 + q * q) / 2);
+            double s = s_scale / sqrt(q);
+            double qc = q >= 1 ? 0.99999999 : q;   // NIEMajorAxis.derivatives clamp
+            double sq = sqrt(1.0 - qc * qc);
+            d[RD_CX] = a[co];
+            d[RD_CY] = a[co + 1];
+            d[2] = b; d[3] = s; d[4] = qc; d[5] = cos(phi); d[6] = sin(phi);
+            d[7] = sq; d[8] = b / sq; d[9] = qc * qc; d[10] = qc * qc * s; d[11] = qc * qc * s * s;
+        } else if (code == LENSGB_LENS_EPL) {
+            double theta_E = a[0], gamma = a[1], e1 = a[2], e2 = a[3];
+            double phi, q;
+            ellip_phi_q(e1, e2, phi, q);
+            double t = gamma - 1;
+            double b = theta_E * sqrt(q);
+            double fq = (1.0 - q) / (1.0 + q);
+            int nmax = epl_nmax_of(fq);
+            d[RD_CX] = a[4];
+            d[RD_CY] = a[5];
+            d[2] = b; d[3] = t; d[4] = q; d[5] = cos(phi); d[6] = sin(phi); d[7] = fq;
+            d[8] = (double)nmax; d[9] = 2.0 / (1.0 + q) * pow(b, t);
+            int slot_e = st.epl_slot[p];
+            double* Fd = coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
+            float* Ff = coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
+            // F_0 = 1, F_1 = 1 - 2B/C, F_n = ((n-1) F_{n-2} - (2B-C) F_{n-1}) / (C+n-1)
+            double B = t / 2.0, C = 2.0 - B;
+            double fpp = 1.0, fp = 1.0 - 2.0 * B / C;
+            if (nmax > 0) { Fd[0] = fpp; Ff[0] = (float)fpp; }
+            if (nmax > 1) { Fd[1] = fp; Ff[1] = (float)fp; }
+            for (int n = 2; n < nmax; ++n) {
+                double fn = ((n - 1.0) * fpp - (2.0 * B - C) * fp) / (C + n - 1.0);
+                Fd[n] = fn;
+                Ff[n] = (float)fn;
+                fpp = fp;
+                fp = fn;
+            }
+        } else if (code == LENSGB_LENS_SHEAR) {
+            d[RD_CX] = a[2];
+            d[RD_CY] = a[3];
+            d[2] = a[0]; d[3] = a[1];
+        } else if (code == LENSGB_LENS_NFW) {
+            double Rs = a[0], alpha_Rs = a[1];
+            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+            double Rsf = Rs < 0.0000001 ? 0.0000001 : Rs;
+            d[RD_CX] = a[2];
+            d[RD_CY] = a[3];
+            d[2] = Rsf; d[3] = rho0; d[4] = 4 * rho0 * Rsf; d[5] = 1.0 / Rsf;
+        } else if (code == LENSGB_LENS_TNFW) {
+            double Rs = a[0], alpha_Rs = a[1], r_trunc = a[2];
+            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+            d[RD_CX] = a[3];
+            d[RD_CY] = a[4];
+            d[2] = Rs; d[3] = rho0; d[4] = r_trunc / Rs; d[5] = 4 * rho0 * Rs; d[6] = 1.0 / Rs;
+        }
+    } else {
+        // SERSIC / SERSIC_ELLIPSE
+        double amp = a[0], R_sersic = a[1], n = a[2];
+        double e1 = 0, e2 = 0, cx, cy;
+        if (code == LENSGB_LIGHT_SERSIC_ELLIPSE) {
+            e1 = a[3]; e2 = a[4]; cx = a[5]; cy = a[6];
+        } else {
+            cx = a[3]; cy = a[4];
+        }
+        R_sersic = R_sersic > 0 ? R_sersic : 0;          // sersic_ellipse.py:88
+        double Rs_ = R_sersic > 0.0001 ? R_sersic : 0.0001;  // _R_stable
+        double bn = 1.9992 * n - 0.3271;
+        bn = bn > 0.00001 ? bn : 0.00001;
+        double norm = sqrt(fabs(1 - e1 * e1 - e2 * e2));
+        norm = norm > 0.000001 ? norm : 0.000001;
+        d[RD_CX] = cx;
+        d[RD_CY] = cy;
+        d[2] = amp; d[3] = Rs_; d[4] = 1.0 / Rs_; d[5] = 1.0 / n; d[6] = bn;
+        d[7] = (1 - e1) / norm; d[8] = -e2 / norm; d[9] = -e2 / norm; d[10] = (1 + e1) / norm;
+    }
+    for (int k = 2; k + F_OFF < REC_F && k < REC_D; ++k) f[k + F_OFF] = (float)d[k];
+    write_offsets(g, d[RD_CX], d[RD_CY], f);
+}
+
+int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
+                   double* rec_d, float* rec_f, double* coef_d, float* coef_f,
+                   cudaStream_t stream) {
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    long long n = (long long)n_inst * n_prof;
+    if (n == 0) return 0;
+    int threads = 128;
+    int blocks = (int)((n + threads - 1) / threads);
+    prepare_kernel<<<blocks, threads, 0, stream>>>(g, st, params, n_inst, rec_d, rec_f, coef_d,
+                                                   coef_f);
+    return 0;
+}
+
+}  // namespace lensgb

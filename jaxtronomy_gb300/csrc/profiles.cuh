@@ -1,0 +1,315 @@
+// Per-ray lens deflections and light profiles, templated on the arithmetic
+// type.  The FP64 instantiation follows the reference formulas operation for
+// operation; the FP32 instantiation uses constants precomputed in FP64 by the
+// prepare kernel and forms that stay accurate in single precision.
+//
+// Reference formulas (JAXtronomy source tree):
+//   SIE/NIE   LensModel/Profiles/nie.py:86-107,182-200,280-294 (sie.py:105-124)
+//   EPL       LensModel/Profiles/epl.py:111-124,179-200,300-319,366-394,
+//             Util/hyp2f1_util.py:135-176
+//   SHEAR     LensModel/Profiles/shear.py:39-53
+//   NFW       LensModel/Profiles/nfw.py:88-105,259-279,347-365,386-395
+//   TNFW      LensModel/Profiles/tnfw.py:69-87,228-349
+//   SERSIC    LensModel/Profiles/sersic_utils.py:69-110,239-267,
+//             LightModel/Profiles/sersic_ellipse.py:62-93, sersic.py:54-73,
+//             Util/param_util.py:103-123
+#pragma once
+
+#include "common.cuh"
+
+namespace lensgb {
+
+// ---- record layouts (d[k] double, f[k+2] float for k >= 2) -----------------
+// SIE/NIE : d2 b, d3 s, d4 q (clamped < 1), d5 cos phi, d6 sin phi,
+//           d7 sqrt(1-q^2), d8 b/sqrt(1-q^2), d9 q^2, d10 q^2 s, d11 q^2 s^2
+// EPL     : d2 b, d3 t, d4 q, d5 cos phi, d6 sin phi, d7 f, d8 nmax,
+//           d9 2/(1+q) b^t
+// SHEAR   : d2 gamma1, d3 gamma2
+// NFW     : d2 Rs (floored), d3 rho0, d4 4 rho0 Rs, d5 1/Rs
+// TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs
+// SERSIC* : d2 amp, d3 R_sersic (floored), d4 1/R_sersic, d5 1/n, d6 b_n,
+//           d7..d10 product-average transform (m00 m01 m10 m11)
+constexpr int F_OFF = 2;  // float slot = double slot + F_OFF
+
+template <typename R>
+struct Rec {
+    const R* v;  // points at slot 0 of the record in the working precision
+    __device__ __forceinline__ R operator[](int k) const { return v[k]; }
+};
+
+// Slot of a type-specific value in the record of precision R.
+template <typename R>
+__device__ __forceinline__ int slot(int k) {
+    return sizeof(R) == 8 ? k : k + F_OFF;
+}
+
+// ---------------------------------------------------------------------------
+// NIE / SIE
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void nie_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    const R b = rec[slot<R>(2)], s = rec[slot<R>(3)], q = rec[slot<R>(4)];
+    const R c = rec[slot<R>(5)], sn = rec[slot<R>(6)];
+    const R sq = rec[slot<R>(7)], b_sq = rec[slot<R>(8)];
+    const R q2s = rec[slot<R>(10)];
+    (void)q;
+    R x = dx * c + dy * sn;
+    R y = -dx * sn + dy * c;
+    R fx, fy;
+    if (sizeof(R) == 8) {
+        // psi = sqrt(q^2 (s^2 + x^2) + y^2), nie.py:339-345
+        R psi = sqrt(q * q * (s * s + x * x) + y * y);
+        fx = b_sq * atan(sq * x / (psi + s));
+        fy = b_sq * atanh(sq * y / (psi + q2s));
+    } else {
+        const R q2 = rec[slot<R>(9)], q2s2 = rec[slot<R>(11)];
+        R psi = sqrtf(fmaf(q2, x * x, fmaf(y, y, q2s2)));
+        fx = b_sq * atanf(sq * x / (psi + s));
+        fy = b_sq * atanhf(sq * y / (psi + q2s));
+    }
+    ax = fx * c - fy * sn;
+    ay = fx * sn + fy * c;
+}
+
+// ---------------------------------------------------------------------------
+// EPL (Tessore & Metcalf 2015 with the Lopez-Temme series of 2F1)
+// ---------------------------------------------------------------------------
+// F holds the nmax coefficients F_n of the series
+//   2F1(1, t/2; 2 - t/2; z) = (1 - z/2)^-1 sum_n F_n w^n,  w = z / (z - 2)
+// (hyp2f1_util.py:135-176 with a = 1, where the Pochhammer prefactor is 1).
+template <typename R>
+__device__ __forceinline__ void epl_deflect(const R* rec, const R* F, R dx, R dy, R& ax, R& ay) {
+    const R t = rec[slot<R>(3)], q = rec[slot<R>(4)];
+    const R c = rec[slot<R>(5)], sn = rec[slot<R>(6)], f = rec[slot<R>(7)];
+    const int nmax = (int)rec[slot<R>(8)];
+    const R pref = rec[slot<R>(9)];
+    R x = dx * c + dy * sn;
+    R y = -dx * sn + dy * c;
+    R za = q * x, zb = y;               // Z = q x + i y
+    R r2 = za * za + zb * zb;
+    R Ra = (sizeof(R) == 8) ? hypot(za, zb) : sqrtf(r2);
+    R Rm = Ra > R(1e-9) ? Ra : R(1e-9);  // R = max(|Z|, 1e-9)
+    R hr = 1, hi = 0;                     // 2F1 value
+    bool nan_case = false;
+    if (nmax > 0) {
+        if (r2 == R(0)) {
+            nan_case = true;  // -f Z / conj(Z) is 0/0 at the centre -> NaN -> 0
+        } else {
+            // z = -f Z / conj(Z) = -f Z^2 / |Z|^2
+            R inv = R(1) / r2;
+            R zr = -f * (za * za - zb * zb) * inv;
+            R zi = -f * (R(2) * za * zb) * inv;
+            // w = z / (z - 2)
+            R dr = zr - R(2), di = zi;
+            R dd = R(1) / (dr * dr + di * di);
+            R wr = (zr * dr + zi * di) * dd;
+            R wi = (zi * dr - zr * di) * dd;
+            // Horner over the coefficient table
+            R sr = F[nmax - 1], si = 0;
+            for (int n = nmax - 2; n >= 0; --n) {
+                R nr = sr * wr - si * wi + F[n];
+                R ni = sr * wi + si * wr;
+                sr = nr;
+                si = ni;
+            }
+            // divide by (1 - z/2)
+            R er = R(1) - R(0.5) * zr, ei = -R(0.5) * zi;
+            R ee = R(1) / (er * er + ei * ei);
+            hr = (sr * er + si * ei) * ee;
+            hi = (si * er - sr * ei) * ee;
+        }
+    }
+    R fx, fy;
+    if (nan_case) {
+        fx = 0;
+        fy = 0;
+    } else {
+        // alpha = 2/(1+q) (b/R)^t Z 2F1
+        R amp;
+        if (sizeof(R) == 8)
+            amp = pref * pow(Rm, -t);
+        else
+            amp = pref * exp2f(-t * log2f(Rm));
+        R omr = za * hr - zb * hi;
+        R omi = za * hi + zb * hr;
+        fx = nan_to_num_1e10(amp * omr);
+        fy = nan_to_num_1e10(amp * omi);
+    }
+    ax = fx * c - fy * sn;
+    ay = fx * sn + fy * c;
+}
+
+// ---------------------------------------------------------------------------
+// SHEAR
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void shear_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    const R g1 = rec[slot<R>(2)], g2 = rec[slot<R>(3)];
+    ax = g1 * dx + g2 * dy;
+    ay = g2 * dx - g1 * dy;
+}
+
+// ---------------------------------------------------------------------------
+// NFW
+// ---------------------------------------------------------------------------
+// G(X) = arccosh(1/X)/sqrt(1-X^2) (X<1), arccos(1/X)/sqrt(X^2-1) (X>1), 1 (X=1)
+// is NFW's G and TNFW's F (tnfw.py:290-304).  FP32 evaluation:
+//  * |1-X^2| < 0.12: the series sum_k w^k/(2k+1) with w = 1-X^2 (the quotient
+//    of two vanishing numbers would lose all precision);
+//  * X < 1: ln((1+u)/X)/u with u = sqrt(1-X^2) (= atanh(u)/u without the
+//    1-u cancellation of atanh near 1);
+//  * X > 1: atan(v)/v with v = sqrt(X^2-1).
+__device__ __forceinline__ float nfw_G_f(float X) {
+    float w = (1.f - X) * (1.f + X);
+    if (fabsf(w) < 0.12f) {
+        float s = 1.f / 23.f;
+        s = fmaf(s, w, 1.f / 21.f);
+        s = fmaf(s, w, 1.f / 19.f);
+        s = fmaf(s, w, 1.f / 17.f);
+        s = fmaf(s, w, 1.f / 15.f);
+        s = fmaf(s, w, 1.f / 13.f);
+        s = fmaf(s, w, 1.f / 11.f);
+        s = fmaf(s, w, 1.f / 9.f);
+        s = fmaf(s, w, 1.f / 7.f);
+        s = fmaf(s, w, 1.f / 5.f);
+        s = fmaf(s, w, 1.f / 3.f);
+        return fmaf(s, w, 1.f);
+    }
+    if (w > 0.f) {
+        float u = sqrtf(w);
+        return logf((1.f + u) / X) / u;
+    }
+    float v = sqrtf(-w);
+    return atanf(v) / v;
+}
+
+// g(X) = ln(X/2) + G(X) (nfw.py:347-365).  For X < 1 the two terms cancel to
+// O(X^2 ln X); FP32 uses the equivalent cancellation-free form
+//   g = [M X^2/(1+u) + log1p(-X^2/(2(1+u)))] / u,  M = ln(2/X), u = sqrt(1-X^2).
+__device__ __forceinline__ float nfw_g_f(float X) {
+    X = X < 0.000001f ? 0.000001f : X;
+    float x2 = X * X;
+    float w = (1.f - X) * (1.f + X);
+    if (fabsf(w) < 0.12f) return logf(0.5f * X) + nfw_G_f(X);
+    if (X < 1.f) {
+        float u = sqrtf(w);
+        float opu = 1.f + u;
+        float M = logf(2.f / X);
+        return (M * x2 / opu + log1pf(-x2 / (2.f * opu))) / u;
+    }
+    float v = sqrtf(-w);
+    return logf(0.5f * X) + atanf(v) / v;
+}
+
+template <typename R>
+__device__ __forceinline__ R nfw_g(R X) {
+    if (sizeof(R) == 8) {
+        X = X < R(0.000001) ? R(0.000001) : X;
+        if (X < 1) return log(X / R(2)) + R(1) / sqrt(R(1) - X * X) * acosh(R(1) / X);
+        if (X == 1) return R(1) + log(R(1) / R(2));
+        return log(X / R(2)) + R(1) / sqrt(X * X - R(1)) * acos(R(1) / X);
+    } else {
+        return nfw_g_f(X);
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void nfw_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    const R inv_rs = rec[slot<R>(5)], a4 = rec[slot<R>(4)];
+    R Rr = sqrt(dx * dx + dy * dy);
+    Rr = Rr > R(0.00000001) ? Rr : R(0.00000001);
+    R X;
+    if (sizeof(R) == 8)
+        X = Rr / rec[slot<R>(2)];
+    else
+        X = Rr * inv_rs;
+    R a = a4 * nfw_g<R>(X) / (X * X);
+    ax = a * dx;
+    ay = a * dy;
+}
+
+// ---------------------------------------------------------------------------
+// TNFW
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double tnfw_F_d(double x) {
+    x = x > 0.001 ? x : 0.001;
+    if (x < 1) return pow(1 - x * x, -0.5) * atanh(pow(1 - x * x, 0.5));
+    if (x > 1) return pow(x * x - 1, -0.5) * atan(pow(x * x - 1, 0.5));
+    return x;
+}
+
+__device__ __forceinline__ double tnfw_g_d(double x, double tau) {
+    x = x > 0.001 ? x : 0.001;
+    double t2 = tau * tau;
+    double L = log(x * pow(tau + sqrt(t2 + x * x), -1.0));
+    return t2 / ((t2 + 1) * (t2 + 1)) *
+           ((t2 + 1 + 2 * (x * x - 1)) * tnfw_F_d(x) + tau * M_PI + (t2 - 1) * log(tau) +
+            sqrt(t2 + x * x) * (-M_PI + L * (t2 - 1) / tau));
+}
+
+// FP32 TNFW g.  The reference bracket (tnfw.py:339-348) cancels to O(x^2 ln x)
+// for small x; regrouped exactly as
+//   (t2-1) [x^2 L/(tau (tau+r)) - log1p(x^2/(2 tau (tau+r))) + g_NFW(x)]
+//   + 2 x^2 F(x) - pi x^2/(tau+r),   r = sqrt(t2+x^2), L = ln(x/(tau+r)),
+// every term of which is O(x^2 ln x) itself.
+__device__ __forceinline__ float tnfw_g_f(float x, float tau) {
+    x = x > 0.001f ? x : 0.001f;
+    float t2 = tau * tau;
+    float x2 = x * x;
+    float r = sqrtf(t2 + x2);
+    float tr = tau + r;
+    float L = logf(x / tr);
+    float B = x2 / (tau * tr) * L - log1pf(x2 / (2.f * tau * tr)) + nfw_g_f(x);
+    float br = (t2 - 1.f) * B + 2.f * x2 * nfw_G_f(x) - 3.14159265358979f * x2 / tr;
+    return t2 / ((t2 + 1.f) * (t2 + 1.f)) * br;
+}
+
+template <typename R>
+__device__ __forceinline__ void tnfw_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    const R Rs = rec[slot<R>(2)], tau = rec[slot<R>(4)], a4 = rec[slot<R>(5)];
+    R Rr = sqrt(dx * dx + dy * dy);
+    Rr = Rr > R(0.001) * Rs ? Rr : R(0.001) * Rs;
+    R X;
+    R g;
+    if (sizeof(R) == 8) {
+        X = Rr / Rs;
+        X = X > R(0.001) ? X : R(0.001);
+        g = tnfw_g_d(X, tau);
+    } else {
+        X = Rr * rec[slot<R>(6)];
+        X = X > R(0.001) ? X : R(0.001);
+        g = tnfw_g_f(X, tau);
+    }
+    R a = a4 * g / (X * X);
+    ax = a * dx;
+    ay = a * dy;
+}
+
+// ---------------------------------------------------------------------------
+// Sersic surface brightness (SERSIC and SERSIC_ELLIPSE share the record)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R sersic_flux(const R* rec, R dx, R dy) {
+    const R amp = rec[slot<R>(2)], inv_rs = rec[slot<R>(4)];
+    const R inv_n = rec[slot<R>(5)], bn = rec[slot<R>(6)];
+    const R m00 = rec[slot<R>(7)], m01 = rec[slot<R>(8)], m10 = rec[slot<R>(9)],
+            m11 = rec[slot<R>(10)];
+    R x = m00 * dx + m01 * dy;
+    R y = m10 * dx + m11 * dy;
+    R Rr = sqrt(x * x + y * y);
+    R Rst = Rr > R(0.0001) ? Rr : R(0.0001);
+    R frac;
+    R res;
+    if (sizeof(R) == 8) {
+        frac = Rst / rec[3];
+        R ex = -bn * (pow(frac, inv_n) - R(1));
+        res = frac <= R(1000) ? exp(ex) : R(0);
+    } else {
+        frac = Rst * inv_rs;
+        R ex = -bn * (exp2f(inv_n * log2f(frac)) - R(1));
+        res = frac <= R(1000) ? expf(ex) : R(0);
+    }
+    return amp * nan_to_num_max(res);
+}
+
+}  // namespace lensgb

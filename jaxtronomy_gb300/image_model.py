@@ -1,0 +1,419 @@
+"""``ImageModel``: lensed-source + lens-light image simulation on the GPU.
+
+Drop-in for ``jaxtronomy.ImSim.image_model.ImageModel`` (``image_model.py:27-492``)
+for the analytic-profile path without point sources, with the numerics of
+``Numerics`` / ``NumericsSubFrame`` (``ImSim/Numerics/numerics.py:24-177``,
+``numerics_subframe.py:20-100``) in regular compute mode.
+
+Besides the reference's one-system calls (``image``, ``source_surface_brightness``,
+``lens_surface_brightness``, ``likelihood_data_given_model``) it offers batched
+calls (``image_batch``, ``likelihood_batch``) that take kwargs whose values are
+arrays of length B -- the layout ``jax.vmap`` gives the reference -- and run
+the whole batch in one launch sequence.
+
+``kwargs_numerics`` accepts the reference keys plus ``precision``:
+``"fp64"`` (default; plain FP64 throughout) or ``"fp32"`` (FP32 bulk arithmetic
+with FP64 set-up, FP64-accurate coordinate offsets and an FP64 likelihood
+reduction).
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device, _lib, profiles
+from .data import PSF
+from .lens_model import LensModel
+from .light_model import LightModel
+
+_NUMERICS_KEYS = {
+    "supersampling_factor", "compute_mode", "supersampling_convolution",
+    "supersampling_kernel_size", "flux_evaluate_indexes", "supersampled_indexes",
+    "compute_indexes", "point_source_supersampling_factor", "convolution_kernel_size",
+    "convolution_type", "truncation_conv", "precision",
+}
+
+
+def fwhm2sigma(fwhm):
+    """``jaxtronomy/Util/util.py:56-63``."""
+    return fwhm / (2 * np.sqrt(2 * np.log(2)))
+
+
+def gaussian_kernel(sigma_pix, truncation):
+    """Kernel of ``GaussianConvolution`` (``convolution.py:199-206,254-273``):
+    side 2r+1 with r = max(round(sigma*truncation), 1), normalised to unit sum."""
+    radius = max(round(sigma_pix * truncation), 1)
+    n = 2 * radius + 1
+    c = np.arange(n) - (n - 1) / 2.0
+    xx, yy = np.meshgrid(c, c)
+    k = np.exp(-(xx ** 2 + yy ** 2) / (2 * sigma_pix ** 2)) / (2 * np.pi * sigma_pix ** 2)
+    return k / np.sum(k)
+
+
+def cut_psf(kernel, size):
+    """Centred odd-size cut of a kernel without renormalisation (lenstronomy
+    ``kernel_util.cut_psf(..., normalisation=False)``, used at numerics.py:196-213)."""
+    n = kernel.shape[0]
+    if size >= n:
+        return kernel
+    c = n // 2
+    h = size // 2
+    return kernel[c - h:c + h + 1, c - h:c + h + 1]
+
+
+class ImageModel:
+    """Lens image simulation (``image_model.py:27-150``)."""
+
+    def __init__(self, data_class, psf_class, lens_model_class=None, source_model_class=None,
+                 lens_light_model_class=None, point_source_class=None, extinction_class=None,
+                 kwargs_numerics=None, likelihood_mask=None, psf_error_map_bool_list=None,
+                 kwargs_pixelbased=None):
+        self.type = "single-band"
+        self.num_bands = 1
+        self.PSF = psf_class
+        self.Data = data_class
+        self._flux_scaling = getattr(data_class, "flux_scaling", 1)
+        self.PSF.set_pixel_size(self.Data.pixel_width)
+        kn = dict(kwargs_numerics or {})
+        unknown = set(kn) - _NUMERICS_KEYS
+        if unknown:
+            raise TypeError("unexpected kwargs_numerics keys %s" % sorted(unknown))
+        precision = kn.pop("precision", "fp64")
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self._precision = _lib.FP64 if precision == "fp64" else _lib.FP32_SPLIT
+        self._dtype = torch.float64 if precision == "fp64" else torch.float32
+        # Numerics.__init__ checks (numerics.py:68-146)
+        compute_mode = kn.get("compute_mode", "regular")
+        if compute_mode != "regular":
+            raise ValueError("compute_mode %s not supported; only 'regular'" % compute_mode)
+        s = kn.get("supersampling_factor", 1)
+        if not isinstance(s, (int, np.integer)) or isinstance(s, bool):
+            raise TypeError("supersampling_factor needs to be an integer! Current type is %s"
+                            % type(s))
+        s = int(s)
+        if s < 1:
+            raise ValueError("supersampling_factor must be >= 1")
+        ssc = kn.get("supersampling_convolution", False)
+        if s == 1:
+            ssc = False
+        if ssc:
+            raise ValueError("supersampling_convolution=True is not supported by this build")
+        if kn.get("flux_evaluate_indexes") is not None:
+            raise ValueError("flux_evaluate_indexes is not supported by this build")
+        conv_type = kn.get("convolution_type", "fft")
+        if conv_type not in ("fft", "grid", "fft_static"):
+            raise ValueError("convolution_type %s not supported!" % conv_type)
+        self._s = s
+        self._kwargs_numerics = dict(kwargs_numerics or {})
+        if kwargs_pixelbased is not None:
+            raise ValueError("pixelbased solver not supported")
+        if extinction_class is not None and getattr(extinction_class, "_profile_type_list", []):
+            raise ValueError("extinction is not supported")
+        if point_source_class is not None and len(getattr(point_source_class,
+                                                          "point_source_type_list", [])) > 0:
+            raise ValueError("point sources are not supported by this build")
+        if data_class.primary_beam is not None:
+            raise ValueError("primary beam not supported")
+        self.LensModel = lens_model_class if lens_model_class is not None else LensModel([])
+        self.SourceModel = source_model_class if source_model_class is not None else LightModel([])
+        self.LensLightModel = (lens_light_model_class if lens_light_model_class is not None
+                               else LightModel([]))
+        nx, ny = data_class.num_pixel_axes
+        if nx != ny:
+            raise ValueError("ImageModel needs a square pixel grid (got %d x %d)" % (nx, ny))
+        self._nx, self._ny = int(nx), int(ny)
+        if likelihood_mask is None:
+            likelihood_mask = np.ones((self._nx, self._ny))
+        self.likelihood_mask = np.array(likelihood_mask, dtype=bool)
+        self.num_data_evaluate = int(np.sum(self.likelihood_mask))
+        self._psf_error_map = self.PSF.psf_variance_map_bool
+
+        # PSF kernel for the convolution step (numerics.py:102-139)
+        pt = psf_class.psf_type
+        if pt == "PIXEL":
+            kernel = np.asarray(psf_class.kernel_point_source, dtype=float)
+            cks = kn.get("convolution_kernel_size")
+            if cks is not None:
+                size = cks if cks % 2 == 1 else cks + 1
+                kernel = cut_psf(kernel, size)
+            self._psf_type = _lib.PSF_PIXEL
+        elif pt == "GAUSSIAN":
+            trunc = kn.get("truncation_conv")
+            if trunc is None:
+                trunc = psf_class.truncation
+            sigma = fwhm2sigma(psf_class.fwhm) / data_class.pixel_width
+            kernel = gaussian_kernel(sigma, trunc)
+            self._psf_type = _lib.PSF_GAUSSIAN
+        elif pt == "NONE":
+            kernel = None
+            self._psf_type = _lib.PSF_NONE
+        else:
+            raise ValueError("psf_type %s not valid! Chose either NONE, GAUSSIAN or PIXEL." % pt)
+        self._kernel = kernel
+        self._kernel_size = 0 if kernel is None else int(kernel.shape[0])
+        self._kernel_dev = None
+        self._models = {}
+
+    # ------------------------------------------------------------------ models
+    def _desc(self, lens_idx, src_idx, ll_idx, lensed=True):
+        d = _lib.ModelDesc()
+        lm = self.LensModel.lens_model_list
+        d.n_lens = len(lens_idx) if lensed else 0
+        for j, i in enumerate(lens_idx if lensed else []):
+            d.lens_codes[j] = _lib.LENS_CODES[lm[i]]
+        sm = self.SourceModel.profile_type_list
+        dsl = self.SourceModel.deflection_scaling_list
+        d.n_source = len(src_idx)
+        for j, i in enumerate(src_idx):
+            d.source_codes[j] = _lib.LIGHT_CODES[sm[i]]
+            d.deflection_scaling[j] = 1.0 if dsl is None else float(dsl[i])
+        llm = self.LensLightModel.profile_type_list
+        d.n_lens_light = len(ll_idx)
+        for j, i in enumerate(ll_idx):
+            d.lens_light_codes[j] = _lib.LIGHT_CODES[llm[i]]
+        d.nx, d.ny = self._ny, self._nx  # columns, rows of an (nx, ny)-shaped array
+        d.supersampling = self._s
+        d.transform_pix2angle[:] = list(np.asarray(self.Data.transform_pix2angle, float).ravel())
+        ra0, dec0 = self.Data.radec_at_xy_0
+        d.ra_at_xy_0, d.dec_at_xy_0 = float(ra0), float(dec0)
+        d.flux_scaling = float(self._flux_scaling)
+        d.alpha_scaling = float(getattr(self.LensModel, "alpha_scaling", 1.0))
+        d.psf_type = self._psf_type
+        d.kernel_size = self._kernel_size
+        d.precision = self._precision
+        return d
+
+    def _model(self, lens_idx, src_idx, ll_idx, lensed=True):
+        key = (tuple(lens_idx), tuple(src_idx), tuple(ll_idx), lensed)
+        if key not in self._models:
+            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed))
+        return self._models[key]
+
+    def _kernel_tensor(self):
+        if self._kernel_dev is None and self._kernel is not None:
+            self._kernel_dev = torch.as_tensor(self._kernel, dtype=self._dtype).cuda().contiguous()
+        return self._kernel_dev
+
+    # ------------------------------------------------------------------ packing
+    def pack_params(self, kwargs_lens, kwargs_source, kwargs_lens_light, lens_idx=None,
+                    src_idx=None, ll_idx=None, lensed=True):
+        """(B, param_count) float64 rows for the given (possibly batched) kwargs."""
+        lm = self.LensModel.lens_model_list
+        sm = self.SourceModel.profile_type_list
+        llm = self.LensLightModel.profile_type_list
+        lens_idx = list(range(len(lm))) if lens_idx is None else lens_idx
+        src_idx = list(range(len(sm))) if src_idx is None else src_idx
+        ll_idx = list(range(len(llm))) if ll_idx is None else ll_idx
+        kl = [kwargs_lens[i] for i in lens_idx] if (lensed and lens_idx) else []
+        ks = [kwargs_source[i] for i in src_idx] if src_idx else []
+        kll = [kwargs_lens_light[i] for i in ll_idx] if ll_idx else []
+        B = profiles.batch_size(kl, ks, kll)
+        names_l = [lm[i] for i in lens_idx] if lensed else []
+        names_s = [sm[i] for i in src_idx]
+        names_ll = [llm[i] for i in ll_idx]
+        P = (profiles.n_params(names_l, profiles.LENS_PARAMS)
+             + profiles.n_params(names_s, profiles.LIGHT_PARAMS)
+             + profiles.n_params(names_ll, profiles.LIGHT_PARAMS))
+        rows = np.zeros((B, P), dtype=np.float64)
+        c = profiles.pack(names_l, profiles.LENS_PARAMS, kl, rows, 0, "Lens")
+        c = profiles.pack(names_s, profiles.LIGHT_PARAMS, ks, rows, c, "Source")
+        profiles.pack(names_ll, profiles.LIGHT_PARAMS, kll, rows, c, "Lens light")
+        return rows
+
+    def _psf_arg(self, psf_kernels, B):
+        if self._psf_type == _lib.PSF_NONE:
+            return None, 0, None
+        if psf_kernels is None:
+            k = self._kernel_tensor()
+            return k, 0, k
+        k = psf_kernels
+        if not isinstance(k, torch.Tensor):
+            k = torch.as_tensor(np.ascontiguousarray(k))
+        k = k.to(device="cuda", dtype=self._dtype).contiguous()
+        K = self._kernel_size
+        if k.dim() == 2:
+            if tuple(k.shape) != (K, K):
+                raise ValueError("psf kernel must be %dx%d" % (K, K))
+            return k, 0, k
+        if tuple(k.shape) != (B, K, K):
+            raise ValueError("per-system psf kernels must have shape (%d, %d, %d)" % (B, K, K))
+        return k, K * K, k
+
+    # ------------------------------------------------------------------ launches
+    def _launch(self, model, rows_dev, B, flags, psf_kernels=None, out=None, stream=None):
+        _device.require_cuda()
+        if out is None:
+            out = torch.empty((B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        elif out.dtype != self._dtype or not out.is_contiguous() or out.numel() < B * self._nx * self._ny:
+            raise ValueError("out must be a contiguous %s tensor of shape (B, %d, %d)"
+                             % (self._dtype, self._nx, self._ny))
+        kt, kstride, keep = self._psf_arg(psf_kernels, B)
+        kptr = ctypes.c_void_p(0) if kt is None else _device.ptr(kt)
+        _lib.check(_lib.load().lensgb_image(
+            model.handle, _device.ptr(rows_dev), B, kptr, kstride, _device.ptr(out), flags,
+            _device.stream_handle(stream)))
+        del keep
+        return out
+
+    def image_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                    unconvolved=False, source_add=True, lens_light_add=True, psf_kernels=None,
+                    out=None, stream=None, rows=None):
+        """Batched ``image``: kwargs values are arrays of length B (or scalars).
+        Returns a (B, ny, nx) CUDA tensor in the model precision.  ``psf_kernels``
+        may give one (K, K) kernel or one per system (B, K, K) in place of the
+        model PSF (normalised by the caller).  ``rows`` may pass pre-packed
+        parameter rows (host array or CUDA tensor, see :meth:`pack_params`)."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        if rows is None:
+            rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
+        rows_dev = _device.to_device_f64(rows)
+        B = rows_dev.shape[0]
+        flags = ((_lib.UNCONVOLVED if unconvolved else 0)
+                 | (0 if source_add else _lib.NO_SOURCE)
+                 | (0 if lens_light_add else _lib.NO_LENS_LIGHT))
+        return self._launch(model, rows_dev, B, flags, psf_kernels, out, stream)
+
+    # ------------------------------------------------------------------ reference API
+    def image(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None, kwargs_ps=None,
+              kwargs_extinction=None, kwargs_special=None, unconvolved=False, source_add=True,
+              lens_light_add=True, point_source_add=True):
+        """``image_model.py:432-492``: 2d array of the simulated image."""
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        im = self.image_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                              unconvolved=unconvolved, source_add=source_add,
+                              lens_light_add=lens_light_add)
+        return im[0].to(torch.float64).cpu().numpy()
+
+    def source_surface_brightness(self, kwargs_source, kwargs_lens=None, kwargs_extinction=None,
+                                  kwargs_special=None, unconvolved=False, de_lensed=False, k=None,
+                                  update_pixelbased_mapping=True):
+        """``image_model.py:224-266``."""
+        sm = self.SourceModel.profile_type_list
+        if len(sm) == 0:
+            return np.zeros((self._nx, self._ny))
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        src_idx = self.SourceModel._select(k)
+        lens_idx = list(range(len(self.LensModel.lens_model_list)))
+        lensed = not de_lensed
+        model = self._model(lens_idx, src_idx, [], lensed)
+        rows = self.pack_params(kwargs_lens, kwargs_source, None, lens_idx=lens_idx,
+                                src_idx=src_idx, ll_idx=[], lensed=lensed)
+        flags = (_lib.UNCONVOLVED if unconvolved else 0) | _lib.NO_LENS_LIGHT
+        im = self._launch(model, _device.to_device_f64(rows), rows.shape[0], flags)
+        return im[0].to(torch.float64).cpu().numpy()
+
+    def lens_surface_brightness(self, kwargs_lens_light, unconvolved=False, k=None):
+        """``image_model.py:371-393``."""
+        llm = self.LensLightModel.profile_type_list
+        if len(llm) == 0:
+            return np.zeros((self._nx, self._ny))
+        ll_idx = self.LensLightModel._select(k)
+        model = self._model([], [], ll_idx)
+        rows = self.pack_params(None, None, kwargs_lens_light, lens_idx=[], src_idx=[],
+                                ll_idx=ll_idx)
+        flags = (_lib.UNCONVOLVED if unconvolved else 0) | _lib.NO_SOURCE
+        im = self._launch(model, _device.to_device_f64(rows), rows.shape[0], flags)
+        return im[0].to(torch.float64).cpu().numpy()
+
+    def _noise_tensors(self, data=None):
+        """Device copies of data, mask and noise model (cached for the model's own
+        data; ``data`` may pass a (B, ny, nx) batch instead)."""
+        if data is None:
+            if getattr(self, "_noise_cache", None) is None:
+                self._noise_cache = self._make_noise(self.Data.data)
+            return self._noise_cache
+        return self._make_noise(data)
+
+    def _make_noise(self, data):
+        D = self.Data
+        t = {}
+        dt = data if isinstance(data, torch.Tensor) else torch.as_tensor(np.asarray(data, float))
+        dt = dt.to(device="cuda", dtype=torch.float64).contiguous()
+        t["data"] = dt
+        t["data_stride"] = self._nx * self._ny if dt.dim() == 3 else 0
+        t["mask"] = torch.as_tensor(self.likelihood_mask.astype(np.float64)).cuda()
+        nm = D.noise_map
+        t["noise"] = None if nm is None else torch.as_tensor(np.asarray(nm, float)).cuda()
+        em = D.exposure_map
+        if nm is None and em is not None and np.ndim(em) > 0:
+            t["expo"] = torch.as_tensor(np.broadcast_to(np.asarray(em, float),
+                                                        (self._nx, self._ny)).copy()).cuda()
+            t["expo_t"] = 1.0
+        else:
+            t["expo"] = None
+            t["expo_t"] = float(em) if em is not None else 1.0
+        return t
+
+    def likelihood_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                         data=None, psf_kernels=None, rows=None, image_out=None, stream=None):
+        """Batched ``likelihood_data_given_model``: (B,) FP64 CUDA tensor of
+        log-likelihoods; ``data`` optionally gives one (ny, nx) image per system."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        if rows is None:
+            rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
+        rows_dev = _device.to_device_f64(rows)
+        B = rows_dev.shape[0]
+        nt = self._noise_tensors(data)
+        nd = _lib.NoiseDesc()
+        nd.data_dev = nt["data"].data_ptr()
+        nd.data_stride = nt["data_stride"]
+        nd.mask_dev = nt["mask"].data_ptr()
+        nd.noise_map_dev = 0 if nt["noise"] is None else nt["noise"].data_ptr()
+        nd.noise_stride = 0
+        nd.exposure_map_dev = 0 if nt["expo"] is None else nt["expo"].data_ptr()
+        nd.exposure_stride = 0
+        nd.exposure_time = nt["expo_t"]
+        nd.background_rms = float(self.Data.background_rms)
+        nd.error_map_dev = 0
+        if image_out is None:
+            image_out = torch.empty((B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        logl = torch.empty((B,), dtype=torch.float64, device="cuda")
+        kt, kstride, keep = self._psf_arg(psf_kernels, B)
+        kptr = ctypes.c_void_p(0) if kt is None else _device.ptr(kt)
+        _lib.check(_lib.load().lensgb_loglike(
+            model.handle, _device.ptr(rows_dev), B, kptr, kstride, ctypes.byref(nd),
+            _device.ptr(image_out), _device.ptr(logl), _device.stream_handle(stream)))
+        del keep
+        return logl
+
+    def likelihood_data_given_model(self, kwargs_lens=None, kwargs_source=None,
+                                    kwargs_lens_light=None, kwargs_ps=None,
+                                    kwargs_extinction=None, kwargs_special=None,
+                                    source_marg=False, linear_prior=None,
+                                    check_positive_flux=False):
+        """``image_model.py:163-221``: log-likelihood of the data given the model."""
+        if check_positive_flux:
+            raise ValueError("check positive flux is not supported")
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        return float(self.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light)[0].cpu())
+
+    def point_source(self, kwargs_ps, kwargs_lens=None, kwargs_special=None, unconvolved=False,
+                     k=None):
+        """Point sources are not part of this build: always an empty image."""
+        return np.zeros((self._nx, self._ny))
+
+    def reduced_residuals(self, model, error_map=0):
+        """(data - model) / sqrt(C_D_model + |error_map|) on the host."""
+        model = np.asarray(model)
+        c_d = self.Data.C_D_model(model)
+        return (model - self.Data.data) / np.sqrt(c_d + np.abs(error_map)) * self.likelihood_mask
+
+    def update_psf(self, psf_class):
+        raise ValueError("Updating psf class not supported. Create a new instance of ImageModel "
+                         "instead.")
+
+    def update_data(self, data_class):
+        raise ValueError("Updating data class not supported. Create a new instance of ImageModel "
+                         "instead.")
+
+
+__all__ = ["ImageModel", "PSF"]

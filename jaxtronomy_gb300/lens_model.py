@@ -1,0 +1,122 @@
+"""``LensModel``: single-plane ray shooting through a list of lens profiles.
+
+Drop-in for ``jaxtronomy.LensModel.lens_model.LensModel``
+(``lens_model.py:25-252,353-381``) restricted to the single-plane path
+(``SinglePlane``, ``single_plane.py:39-139``).  All evaluation runs in
+liblensgb.so on the GPU in FP64.
+"""
+
+import numpy as np
+import torch
+
+from . import _device, _lib, profiles
+
+
+def _as_out(t, like):
+    return t if isinstance(like, torch.Tensor) else t.cpu().numpy()
+
+
+class LensModel:
+    """Class to handle an arbitrary list of single-plane lens models."""
+
+    def __init__(self, lens_model_list, z_lens=None, z_source=None, lens_redshift_list=None,
+                 cosmo=None, multi_plane=False, observed_convention_index=None,
+                 z_source_convention=None, cosmo_interp=False, z_interp_stop=None,
+                 num_z_interp=100, profile_kwargs_list=None, decouple_multi_plane=False,
+                 kwargs_multiplane_model=None, distance_ratio_sampling=False,
+                 cosmology_sampling=False, cosmology_model="FlatLambdaCDM"):
+        if cosmology_sampling:
+            raise ValueError("Cosmology sampling not supported")
+        if distance_ratio_sampling:
+            raise ValueError("Distance ratio sampling not supported")
+        if multi_plane or decouple_multi_plane:
+            raise ValueError("multi-plane lensing is not supported by this build")
+        if observed_convention_index is not None:
+            raise ValueError("observed_convention_index is not supported")
+        if len(lens_model_list) > _lib.MAX_PROFILES:
+            raise ValueError("at most %d lens profiles per model; use LensModelBulk for "
+                             "many deflectors" % _lib.MAX_PROFILES)
+        if z_source is not None and z_source_convention is not None and z_source != z_source_convention:
+            raise ValueError("z_source != z_source_convention needs a cosmology and is not "
+                             "supported by this build")
+        for kw in profile_kwargs_list or []:
+            if kw:
+                raise ValueError("non-default profile_kwargs are not supported")
+        profiles.check_names(lens_model_list, profiles.LENS_PARAMS, "Lens")
+        self.lens_model_list = list(lens_model_list)
+        self.z_lens = z_lens
+        self.z_source = z_source
+        self.redshift_list = lens_redshift_list
+        self.multi_plane = False
+        self.type = "SinglePlane"
+        self.alpha_scaling = 1.0
+        self.param_name_list = [profiles.LENS_PARAMS[n] for n in self.lens_model_list]
+        self._models = {}
+
+    def check_parameters(self, kwargs_list):
+        profiles.check_parameters(self.lens_model_list, profiles.LENS_PARAMS, kwargs_list, "Lens")
+
+    def _select(self, k):
+        if k is None:
+            return list(range(len(self.lens_model_list)))
+        if isinstance(k, (int, np.integer)):
+            return [int(k)]
+        k = list(k)
+        if len(k) and isinstance(k[0], (bool, np.bool_)):
+            return [i for i, b in enumerate(k) if b]
+        return [int(i) for i in k]
+
+    def _model(self, idx):
+        key = tuple(idx)
+        if key not in self._models:
+            d = _lib.ModelDesc()
+            d.n_lens = len(idx)
+            for j, i in enumerate(idx):
+                d.lens_codes[j] = _lib.LENS_CODES[self.lens_model_list[i]]
+            d.nx = d.ny = 1
+            d.supersampling = 1
+            d.transform_pix2angle[:] = [1.0, 0.0, 0.0, 1.0]
+            d.flux_scaling = 1.0
+            d.alpha_scaling = self.alpha_scaling
+            d.psf_type = _lib.PSF_NONE
+            d.precision = _lib.FP64
+            self._models[key] = _lib.Model(d)
+        return self._models[key]
+
+    def _row(self, idx, kwargs):
+        names = [self.lens_model_list[i] for i in idx]
+        kws = [kwargs[i] for i in idx]
+        row = np.zeros((1, profiles.n_params(names, profiles.LENS_PARAMS)))
+        profiles.pack(names, profiles.LENS_PARAMS, kws, row, 0, "Lens")
+        return row
+
+    def _points(self, fn, x, y, kwargs, k):
+        _device.require_cuda()
+        idx = self._select(k)
+        xt = _device.to_device_f64(x).reshape(-1)
+        yt = _device.to_device_f64(y).reshape(-1)
+        shape = np.shape(x) if not isinstance(x, torch.Tensor) else tuple(x.shape)
+        ox = torch.empty_like(xt)
+        oy = torch.empty_like(yt)
+        if len(idx) == 0:
+            if fn == "alpha":
+                ox.zero_()
+                oy.zero_()
+            else:
+                ox.copy_(xt)
+                oy.copy_(yt)
+        else:
+            m = self._model(idx)
+            p = _device.to_device_f64(self._row(idx, kwargs))
+            f = getattr(_lib.load(), "lensgb_" + fn)
+            _lib.check(f(m.handle, _device.ptr(p), _device.ptr(xt), _device.ptr(yt),
+                         _device.ptr(ox), _device.ptr(oy), xt.numel(), _device.stream_handle()))
+        return _as_out(ox.reshape(shape), x), _as_out(oy.reshape(shape), x)
+
+    def ray_shooting(self, x, y, kwargs, k=None):
+        """Maps image to source position, ``lens_model.py:237-252``."""
+        return self._points("ray_shooting", x, y, kwargs, k)
+
+    def alpha(self, x, y, kwargs, k=None):
+        """Deflection angles, ``lens_model.py:353-381``."""
+        return self._points("alpha", x, y, kwargs, k)

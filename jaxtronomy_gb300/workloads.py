@@ -1,0 +1,130 @@
+"""Seeded synthetic lens systems with the shapes of the benchmark workloads.
+
+No public dataset is involved: every system is drawn from
+``numpy.random.default_rng(seed)`` with the parameter distributions listed in
+each function's docstring.  Batched kwargs use the "vmap" layout accepted by
+:meth:`jaxtronomy_gb300.ImageModel.image_batch`: a list of dicts (one per
+profile) whose values are float64 arrays of length B.  ``instance(kw, i)``
+extracts the scalar kwargs of system ``i``.
+"""
+
+import numpy as np
+
+
+def grid_kwargs(num_pix, delta_pix):
+    """Pixel grid centred at 0 with a diagonal pix->angle transform (RA increasing
+    with column index), the layout of lenstronomy's
+    ``data_configure_simple(..., inverse=False)``."""
+    c = (num_pix - 1) / 2.0
+    return {
+        "transform_pix2angle": np.array([[delta_pix, 0.0], [0.0, delta_pix]]),
+        "ra_at_xy_0": -c * delta_pix,
+        "dec_at_xy_0": -c * delta_pix,
+    }
+
+
+def gaussian_pixel_kernel(fwhm, delta_pix, size):
+    """Circular Gaussian of the given FWHM sampled at pixel centres of a
+    size x size stamp, normalised to unit sum."""
+    sigma = fwhm / (2 * np.sqrt(2 * np.log(2))) / delta_pix
+    c = np.arange(size) - (size - 1) / 2.0
+    xx, yy = np.meshgrid(c, c)
+    k = np.exp(-(xx ** 2 + yy ** 2) / (2 * sigma ** 2))
+    return k / k.sum()
+
+
+def moffat_pixel_kernel(fwhm, beta, delta_pix, size):
+    """Moffat I ~ [1 + (r/alpha)^2]^-beta with alpha = FWHM / (2 sqrt(2^(1/beta)-1)),
+    sampled at pixel centres of a size x size stamp, normalised to unit sum."""
+    alpha = fwhm / (2 * np.sqrt(2 ** (1.0 / beta) - 1)) / delta_pix
+    c = np.arange(size) - (size - 1) / 2.0
+    xx, yy = np.meshgrid(c, c)
+    k = (1 + (xx ** 2 + yy ** 2) / alpha ** 2) ** (-beta)
+    return k / k.sum()
+
+
+def _ellip(rng, sigma, n, clip=None):
+    e1 = rng.normal(0, sigma, n)
+    e2 = rng.normal(0, sigma, n)
+    if clip is not None:
+        e = np.hypot(e1, e2)
+        scale = np.where(e >= clip, 0.999 * clip / np.maximum(e, 1e-300), 1.0)
+        e1, e2 = e1 * scale, e2 * scale
+    return e1, e2
+
+
+def _sersic_source(rng, n):
+    e1, e2 = _ellip(rng, 0.1, n)
+    return {
+        "amp": rng.uniform(10, 100, n), "R_sersic": rng.uniform(0.1, 0.5, n),
+        "n_sersic": rng.uniform(1, 4, n), "e1": e1, "e2": e2,
+        "center_x": rng.normal(0, 0.1, n), "center_y": rng.normal(0, 0.1, n),
+    }
+
+
+def _sersic_lens_light(rng, n, cx, cy):
+    e1, e2 = _ellip(rng, 0.1, n)
+    return {
+        "amp": rng.uniform(10, 100, n), "R_sersic": rng.uniform(0.5, 1.5, n),
+        "n_sersic": rng.uniform(2, 5, n), "e1": e1, "e2": e2,
+        "center_x": cx.copy(), "center_y": cy.copy(),
+    }
+
+
+def _shear(rng, n):
+    return {"gamma1": rng.normal(0, 0.05, n), "gamma2": rng.normal(0, 0.05, n)}
+
+
+def single_sie(seed=1000, batch=1):
+    """Single image: 60x60 at 0.05"/pix; SIE (theta_E~U(0.8,1.5), e1,e2~N(0,0.1)
+    clipped to |e|<0.4, centre~N(0,0.05)) + SHEAR (gamma~N(0,0.05)); source
+    SERSIC_ELLIPSE (amp~U(10,100), R~U(0.1,0.5), n~U(1,4), e~N(0,0.1),
+    centre~N(0,0.1)); lens light SERSIC_ELLIPSE (R~U(0.5,1.5), n~U(2,5), at the
+    lens centre); supersampling 1; 11x11 PIXEL kernel of a FWHM 0.1" Gaussian."""
+    rng = np.random.default_rng(seed)
+    n = batch
+    e1, e2 = _ellip(rng, 0.1, n, clip=0.4)
+    cx, cy = rng.normal(0, 0.05, n), rng.normal(0, 0.05, n)
+    lens = [{"theta_E": rng.uniform(0.8, 1.5, n), "e1": e1, "e2": e2,
+             "center_x": cx, "center_y": cy}, _shear(rng, n)]
+    src = [_sersic_source(rng, n)]
+    ll = [_sersic_lens_light(rng, n, cx, cy)]
+    model = dict(num_pix=60, delta_pix=0.05, supersampling_factor=1,
+                 lens_model_list=["SIE", "SHEAR"], source_light_model_list=["SERSIC_ELLIPSE"],
+                 lens_light_model_list=["SERSIC_ELLIPSE"])
+    kernels = np.stack([gaussian_pixel_kernel(0.1, 0.05, 11)] * n)
+    return model, lens, src, ll, kernels
+
+
+def batch_epl(seed=1001, batch=1024, num_pix=180, delta_pix=0.04, supersampling=3,
+              kernel_size=31):
+    """Batch of EPL+SHEAR systems: 180x180 at 0.04"/pix, supersampling 3; EPL
+    (theta_E~U(0.8,1.5), gamma~U(1.8,2.2), e1,e2~N(0,0.1)); light as
+    :func:`single_sie`; one 31x31 Moffat kernel per system (beta~U(2.5,4.5),
+    FWHM~U(0.08,0.15)")."""
+    rng = np.random.default_rng(seed)
+    n = batch
+    e1, e2 = _ellip(rng, 0.1, n)
+    cx, cy = rng.normal(0, 0.05, n), rng.normal(0, 0.05, n)
+    lens = [{"theta_E": rng.uniform(0.8, 1.5, n), "gamma": rng.uniform(1.8, 2.2, n),
+             "e1": e1, "e2": e2, "center_x": cx, "center_y": cy}, _shear(rng, n)]
+    src = [_sersic_source(rng, n)]
+    ll = [_sersic_lens_light(rng, n, cx, cy)]
+    betas = rng.uniform(2.5, 4.5, n)
+    fwhms = rng.uniform(0.08, 0.15, n)
+    kernels = np.stack([moffat_pixel_kernel(f, b, delta_pix, kernel_size)
+                        for f, b in zip(fwhms, betas)])
+    model = dict(num_pix=num_pix, delta_pix=delta_pix, supersampling_factor=supersampling,
+                 lens_model_list=["EPL", "SHEAR"], source_light_model_list=["SERSIC_ELLIPSE"],
+                 lens_light_model_list=["SERSIC_ELLIPSE"])
+    return model, lens, src, ll, kernels
+
+
+def instance(kwargs_list, i):
+    """Scalar kwargs of system ``i`` from a batched (vmap-layout) kwargs list."""
+    return [{k: float(np.asarray(v).reshape(-1)[i]) for k, v in kw.items()} for kw in kwargs_list]
+
+
+def subset(kwargs_list, idx):
+    """Batched kwargs restricted to the systems ``idx``."""
+    return [{k: np.asarray(v)[idx] for k, v in kw.items()} for kw in kwargs_list]

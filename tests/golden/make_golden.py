@@ -1,0 +1,241 @@
+"""Generate the golden vectors in this folder by running the reference itself.
+
+The reference (JAXtronomy) is pure Python on top of ``jax`` and ``lenstronomy``,
+neither of which is installed where this script runs.  ``refshim`` supplies a
+NumPy-backed ``jax`` and restates the handful of lenstronomy names on the image
+path, so that the reference's own source (``jaxtronomy/...``) computes every
+value stored here, in FP64.
+
+Usage (needs the reference source tree; the output files are committed):
+
+    python tests/golden/make_golden.py /path/to/jaxtronomy-source
+
+Outputs (all .npz, metadata as a JSON string under key ``meta``):
+  profiles.npz  per-profile deflections / surface brightness at seeded points
+  hyp2f1.npz    hyp2f1_lopez_temme_8 at the reference's own test points
+  images.npz    ImageModel.image and likelihood_data_given_model on small scenes
+"""
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import refshim  # noqa: E402
+
+
+def _points(rng, n, lo=-2.5, hi=2.5):
+    x = rng.uniform(lo, hi, n)
+    y = rng.uniform(lo, hi, n)
+    # include exact-centre and near-centre rays, which exercise the floors
+    x[:4] = [0.0, 1e-7, -3e-4, 0.02]
+    y[:4] = [0.0, 0.0, 2e-4, -0.01]
+    return x, y
+
+
+def gen_profiles(rng):
+    from jaxtronomy.LensModel.lens_model import LensModel
+    from jaxtronomy.LightModel.light_model import LightModel
+
+    cases = []
+    lens_cases = [
+        ("SIE", {"theta_E": 1.1, "e1": 0.12, "e2": -0.07, "center_x": 0.03, "center_y": -0.02}),
+        ("SIE", {"theta_E": 0.9, "e1": 0.0, "e2": 0.0, "center_x": 0.0, "center_y": 0.0}),
+        ("NIE", {"theta_E": 1.3, "e1": -0.2, "e2": 0.1, "s_scale": 0.05,
+                 "center_x": -0.1, "center_y": 0.05}),
+        ("SHEAR", {"gamma1": 0.03, "gamma2": -0.04, "ra_0": 0.1, "dec_0": -0.2}),
+        ("SHEAR", {"gamma1": -0.05, "gamma2": 0.02}),
+        ("NFW", {"Rs": 0.8, "alpha_Rs": 0.6, "center_x": 0.1, "center_y": -0.1}),
+        ("TNFW", {"Rs": 0.05, "alpha_Rs": 0.004, "r_trunc": 0.5, "center_x": 0.2,
+                  "center_y": 0.3}),
+        ("TNFW", {"Rs": 0.9, "alpha_Rs": 0.7, "r_trunc": 3.0, "center_x": 0.0,
+                  "center_y": 0.0}),
+    ]
+    # EPL across every series-length branch (f = |e|): 0, <0.12, <0.4, <0.6,
+    # <0.73, <0.86, <0.92, >=0.92
+    for e in [0.0, 0.05, 0.25, 0.5, 0.65, 0.8, 0.9, 0.95]:
+        lens_cases.append(("EPL", {"theta_E": 1.2, "gamma": 2.13, "e1": e * np.cos(0.7),
+                                   "e2": e * np.sin(0.7), "center_x": 0.04,
+                                   "center_y": -0.03}))
+    lens_cases.append(("EPL", {"theta_E": 0.85, "gamma": 1.82, "e1": -0.08, "e2": 0.03,
+                               "center_x": 0.0, "center_y": 0.0}))
+    for name, kw in lens_cases:
+        x, y = _points(rng, 64)
+        lm = LensModel([name])
+        ax, ay = lm.alpha(x, y, [kw])
+        cases.append({"kind": "lens", "name": name, "kwargs": kw, "x": x, "y": y,
+                      "out": np.stack([np.asarray(ax), np.asarray(ay)])})
+    light_cases = [
+        ("SERSIC", {"amp": 31.0, "R_sersic": 0.1, "n_sersic": 2.0, "center_x": 0.0,
+                    "center_y": 0.0}),
+        ("SERSIC_ELLIPSE", {"amp": 23.0, "R_sersic": 0.6, "n_sersic": 7.0, "e1": 0.05,
+                            "e2": 0.03, "center_x": 0.0, "center_y": 0.0}),
+        ("SERSIC_ELLIPSE", {"amp": 55.0, "R_sersic": 0.25, "n_sersic": 1.3, "e1": -0.12,
+                            "e2": 0.08, "center_x": 0.07, "center_y": -0.04}),
+        ("SERSIC_ELLIPSE", {"amp": 12.0, "R_sersic": 0.00005, "n_sersic": 4.0, "e1": 0.0,
+                            "e2": 0.0, "center_x": 0.0, "center_y": 0.0}),
+    ]
+    for name, kw in light_cases:
+        x, y = _points(rng, 64, -3.0, 3.0)
+        lm = LightModel([name])
+        out = lm.surface_brightness(x, y, [kw])
+        cases.append({"kind": "light", "name": name, "kwargs": kw, "x": x, "y": y,
+                      "out": np.asarray(out)[None, :]})
+    return cases
+
+
+def gen_hyp2f1():
+    from jaxtronomy.Util.hyp2f1_util import hyp2f1_lopez_temme_8
+    # the reference's own test points, test/test_Util/test_hyp2f1_util.py:87-112
+    a, b, c = 0.3, 0.7, 2.2
+    pts = [(complex(0.3, 0.5), 75), (complex(0.5, 2.1), 75), (complex(-0.6, 0.1), 75),
+           (complex(0.2, -1.6), 75), (complex(-3.2, 1.1), 75), (complex(0.99, 0.001), 200),
+           (complex(-10.99, 0.001), 75)]
+    z = np.array([p[0] for p in pts])
+    nmax = np.array([p[1] for p in pts])
+    out = np.array([complex(np.asarray(hyp2f1_lopez_temme_8(a, b, c, zz, nmax=int(n))))
+                    for zz, n in zip(z, nmax)])
+    return {"a": a, "b": b, "c": c, "z": z, "nmax": nmax, "out": out}
+
+
+def _image_model(num_pix, delta_pix, s, psf_kwargs, lens_list, src_list, ll_list,
+                 data=None, bkg=0.01, exp_time=1000.0, flux_scaling=1, deflection_scaling=None,
+                 convolution_type="fft"):
+    from jaxtronomy.Data.imaging_data import ImageData
+    from jaxtronomy.ImSim.image_model import ImageModel
+    from jaxtronomy.LensModel.lens_model import LensModel
+    from jaxtronomy.LightModel.light_model import LightModel
+    from jaxtronomy_gb300.workloads import grid_kwargs
+
+    g = grid_kwargs(num_pix, delta_pix)
+    if data is None:
+        data = np.zeros((num_pix, num_pix))
+    data_class = ImageData(image_data=data, exposure_time=exp_time, background_rms=bkg,
+                           ra_at_xy_0=g["ra_at_xy_0"], dec_at_xy_0=g["dec_at_xy_0"],
+                           transform_pix2angle=g["transform_pix2angle"],
+                           flux_scaling=flux_scaling)
+    psf = refshim.PSF(**psf_kwargs)
+    return ImageModel(data_class, psf, LensModel(lens_list),
+                      LightModel(src_list, deflection_scaling_list=deflection_scaling),
+                      LightModel(ll_list),
+                      kwargs_numerics={"supersampling_factor": s,
+                                       "convolution_type": convolution_type})
+
+
+def gen_images():
+    from jaxtronomy_gb300 import workloads as W
+
+    scenes = []
+    # 1) the single-image workload, 60x60, s=1, 11x11 Gaussian PIXEL kernel
+    model, lens, src, ll, kern = W.single_sie(seed=1000, batch=2)
+    for i in range(2):
+        kl, ks, kll = W.instance(lens, i), W.instance(src, i), W.instance(ll, i)
+        im = _image_model(60, 0.05, 1, {"psf_type": "PIXEL", "kernel_point_source": kern[i]},
+                          model["lens_model_list"], model["source_light_model_list"],
+                          model["lens_light_model_list"])
+        scenes.append({"tag": "single_sie_%d" % i, "num_pix": 60, "delta_pix": 0.05, "s": 1,
+                       "psf_type": "PIXEL", "kernel": kern[i], "lens": model["lens_model_list"],
+                       "src": model["source_light_model_list"],
+                       "ll": model["lens_light_model_list"], "kwargs_lens": kl,
+                       "kwargs_source": ks, "kwargs_lens_light": kll,
+                       "image": np.asarray(im.image(kl, ks, kll))})
+    # 2) EPL+SHEAR batch workload at a reduced grid (40x40, s=3, 11x11 Moffat)
+    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=3, num_pix=40, kernel_size=11)
+    for i in range(3):
+        kl, ks, kll = W.instance(lens, i), W.instance(src, i), W.instance(ll, i)
+        im = _image_model(40, 0.04, 3, {"psf_type": "PIXEL", "kernel_point_source": kern[i]},
+                          model["lens_model_list"], model["source_light_model_list"],
+                          model["lens_light_model_list"])
+        scenes.append({"tag": "batch_epl_%d" % i, "num_pix": 40, "delta_pix": 0.04, "s": 3,
+                       "psf_type": "PIXEL", "kernel": kern[i], "lens": model["lens_model_list"],
+                       "src": model["source_light_model_list"],
+                       "ll": model["lens_light_model_list"], "kwargs_lens": kl,
+                       "kwargs_source": ks, "kwargs_lens_light": kll,
+                       "image": np.asarray(im.image(kl, ks, kll))})
+    # 3) GAUSSIAN psf type (edge-padded Gaussian convolution), s=2, NFW+SHEAR lens,
+    #    two sources with deflection scaling, flux scaling 1.7
+    kl = [{"Rs": 1.2, "alpha_Rs": 0.9, "center_x": 0.05, "center_y": -0.02},
+          {"gamma1": 0.02, "gamma2": -0.03}]
+    ks = [{"amp": 40.0, "R_sersic": 0.2, "n_sersic": 1.5, "e1": 0.1, "e2": -0.05,
+           "center_x": 0.1, "center_y": 0.05},
+          {"amp": 15.0, "R_sersic": 0.3, "n_sersic": 2.5, "center_x": -0.2, "center_y": 0.1}]
+    kll = [{"amp": 30.0, "R_sersic": 0.8, "n_sersic": 3.0, "e1": 0.05, "e2": 0.02,
+            "center_x": 0.05, "center_y": -0.02}]
+    im = _image_model(32, 0.08, 2, {"psf_type": "GAUSSIAN", "fwhm": 0.2, "truncation": 4},
+                      ["NFW", "SHEAR"], ["SERSIC_ELLIPSE", "SERSIC"], ["SERSIC_ELLIPSE"],
+                      flux_scaling=1.7, deflection_scaling=[1.0, 0.6])
+    scenes.append({"tag": "gaussian_psf", "num_pix": 32, "delta_pix": 0.08, "s": 2,
+                   "psf_type": "GAUSSIAN", "fwhm": 0.2, "truncation": 4.0,
+                   "lens": ["NFW", "SHEAR"], "src": ["SERSIC_ELLIPSE", "SERSIC"],
+                   "ll": ["SERSIC_ELLIPSE"], "flux_scaling": 1.7,
+                   "deflection_scaling": [1.0, 0.6], "kwargs_lens": kl, "kwargs_source": ks,
+                   "kwargs_lens_light": kll, "image": np.asarray(im.image(kl, ks, kll))})
+    # 4) no PSF, TNFW+EPL+SHEAR, s=4, plus unconvolved / partial-component calls
+    kl = [{"theta_E": 1.0, "gamma": 1.95, "e1": 0.15, "e2": -0.1, "center_x": 0.0,
+           "center_y": 0.0},
+          {"Rs": 0.1, "alpha_Rs": 0.01, "r_trunc": 1.0, "center_x": 0.6, "center_y": 0.5},
+          {"gamma1": 0.01, "gamma2": 0.04}]
+    ks = [{"amp": 70.0, "R_sersic": 0.15, "n_sersic": 3.5, "e1": -0.1, "e2": 0.2,
+           "center_x": 0.02, "center_y": 0.03}]
+    kll = []
+    im = _image_model(24, 0.1, 4, {"psf_type": "NONE"}, ["EPL", "TNFW", "SHEAR"],
+                      ["SERSIC_ELLIPSE"], [])
+    scenes.append({"tag": "no_psf", "num_pix": 24, "delta_pix": 0.1, "s": 4,
+                   "psf_type": "NONE", "lens": ["EPL", "TNFW", "SHEAR"],
+                   "src": ["SERSIC_ELLIPSE"], "ll": [], "kwargs_lens": kl,
+                   "kwargs_source": ks, "kwargs_lens_light": kll,
+                   "image": np.asarray(im.image(kl, ks, kll))})
+    # 5) likelihood on the first single-image scene with noisy data
+    rng = np.random.default_rng(77)
+    base = scenes[0]
+    clean = base["image"]
+    data = clean + rng.normal(0, 0.01, clean.shape) \
+        + rng.poisson(np.clip(clean, 0, None) * 1000) / 1000 - np.clip(clean, 0, None)
+    im = _image_model(60, 0.05, 1, {"psf_type": "PIXEL", "kernel_point_source": base["kernel"]},
+                      base["lens"], base["src"], base["ll"], data=data, bkg=0.01,
+                      exp_time=1000.0)
+    logl = float(np.asarray(im.likelihood_data_given_model(
+        base["kwargs_lens"], base["kwargs_source"], base["kwargs_lens_light"])))
+    return scenes, {"data": data, "logL": logl, "bkg": 0.01, "exp_time": 1000.0,
+                    "scene": base["tag"]}
+
+
+def _save(path, arrays, meta):
+    np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
+
+
+def main(reference_root):
+    refshim.install(reference_root)
+    rng = np.random.default_rng(20240601)
+    cases = gen_profiles(rng)
+    arrays, meta = {}, []
+    for i, c in enumerate(cases):
+        arrays["x_%d" % i] = c["x"]
+        arrays["y_%d" % i] = c["y"]
+        arrays["out_%d" % i] = c["out"]
+        meta.append({"kind": c["kind"], "name": c["name"], "kwargs": c["kwargs"]})
+    _save(os.path.join(HERE, "profiles.npz"), arrays, meta)
+
+    h = gen_hyp2f1()
+    _save(os.path.join(HERE, "hyp2f1.npz"), {"z": h["z"], "nmax": h["nmax"], "out": h["out"]},
+          {"a": h["a"], "b": h["b"], "c": h["c"]})
+
+    scenes, like = gen_images()
+    arrays, meta = {}, []
+    for i, sc in enumerate(scenes):
+        arrays["image_%d" % i] = sc.pop("image")
+        if "kernel" in sc:
+            arrays["kernel_%d" % i] = sc.pop("kernel")
+        meta.append(sc)
+    arrays["like_data"] = like.pop("data")
+    _save(os.path.join(HERE, "images.npz"), arrays, {"scenes": meta, "likelihood": like})
+    print("wrote", len(cases), "profile cases,", len(scenes), "image scenes")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,481 @@
+"""Stand-ins that let the JAXtronomy reference source run under plain NumPy.
+
+Used only by ``make_golden.py`` in a container that holds the reference source
+tree but neither ``jax`` nor ``lenstronomy``.  Nothing here is imported by the
+library, the tests or the benchmark.
+
+* ``jax`` is replaced by a NumPy-backed module: ``jit`` / ``custom_jvp`` become
+  pass-throughs, ``lax`` control flow becomes Python loops, ``jax.numpy`` is
+  NumPy with arrays that support the ``.at[...].set/get`` update syntax, and
+  ``jax.scipy`` maps onto SciPy.  Running in FP64 mirrors the reference's
+  ``JAX_ENABLE_X64=True`` test configuration.
+* The few ``lenstronomy`` / ``astropy`` names the reference imports on the
+  image path are restated from lenstronomy's documented behaviour (pixel-grid
+  construction, supersampled sub-grid, single-plane source mapping, PSF
+  normalisation).  These are the *unpinned* conventions: the same restatement
+  appears in the oracle, so the golden vectors pin only the JAXtronomy-owned
+  arithmetic.
+"""
+
+import sys
+import types
+
+import numpy as np
+import scipy.ndimage
+import scipy.signal
+import scipy.special
+
+
+# ---------------------------------------------------------------------------
+# jax.numpy with .at[] support
+# ---------------------------------------------------------------------------
+
+
+class AtArray(np.ndarray):
+    @property
+    def at(self):
+        return _At(self)
+
+
+class _At:
+    def __init__(self, arr):
+        self.arr = arr
+
+    def __getitem__(self, idx):
+        return _AtIdx(self.arr, idx)
+
+
+class _AtIdx:
+    def __init__(self, arr, idx):
+        self.arr = arr
+        self.idx = idx
+
+    def set(self, v):
+        out = np.array(self.arr).view(AtArray)
+        out[self.idx] = v
+        return out
+
+    def add(self, v):
+        out = np.array(self.arr).view(AtArray)
+        out[self.idx] += v
+        return out
+
+    def get(self):
+        return self.arr[self.idx]
+
+
+def _wrap(fn):
+    def inner(*a, **k):
+        r = fn(*a, **k)
+        if isinstance(r, np.ndarray):
+            return r.view(AtArray)
+        return r
+    return inner
+
+
+def _make_jnp():
+    jnp = types.ModuleType("jax.numpy")
+    for name in dir(np):
+        if not name.startswith("__"):
+            setattr(jnp, name, getattr(np, name))
+    for name in ("array", "asarray", "zeros", "zeros_like", "ones", "ones_like", "full",
+                 "full_like", "where", "arange", "reshape", "concatenate", "stack",
+                 "atleast_1d", "pad", "empty", "meshgrid"):
+        fn = getattr(np, name)
+        if name == "meshgrid":
+            setattr(jnp, name, lambda *a, **k: [x.view(AtArray) for x in np.meshgrid(*a, **k)])
+        else:
+            setattr(jnp, name, _wrap(fn))
+    jnp.ndarray = np.ndarray
+    return jnp
+
+
+# ---------------------------------------------------------------------------
+# jax, jax.lax, jax.scipy, jax.tree_util
+# ---------------------------------------------------------------------------
+
+
+def jit(fun=None, static_argnums=None, static_argnames=None, **kwargs):
+    if fun is None:
+        return lambda f: f
+    return fun
+
+
+class custom_jvp:
+    def __init__(self, fun, nondiff_argnums=()):
+        if isinstance(fun, staticmethod):
+            fun = fun.__func__
+        self.fun = fun
+
+    def __call__(self, *args, **kwargs):
+        return self.fun(*args, **kwargs)
+
+    def defjvp(self, jvp_fn):
+        return jvp_fn
+
+
+def _tree_map(f, tree):
+    if isinstance(tree, dict):
+        return {k: _tree_map(f, v) for k, v in tree.items()}
+    if isinstance(tree, (list, tuple)):
+        return type(tree)(_tree_map(f, v) for v in tree)
+    return f(tree)
+
+
+def _make_lax():
+    lax = types.ModuleType("jax.lax")
+
+    def fori_loop(lower, upper, body, init):
+        val = init
+        for i in range(int(lower), int(upper)):
+            val = body(i, val)
+        return val
+
+    def switch(index, branches, *operands):
+        return branches[int(np.asarray(index))](*operands)
+
+    def cond(pred, true_fun, false_fun, *operands):
+        return true_fun(*operands) if bool(np.asarray(pred)) else false_fun(*operands)
+
+    def lax_map(f, xs):
+        leaves = []
+        _tree_map(lambda a: leaves.append(np.asarray(a)), xs)
+        n = leaves[0].shape[0]
+        outs = [f(_tree_map(lambda a, i=i: np.asarray(a)[i], xs)) for i in range(n)]
+        if isinstance(outs[0], (tuple, list)):
+            return tuple(np.stack([o[j] for o in outs]) for j in range(len(outs[0])))
+        return np.stack(outs)
+
+    def scan(f, init, xs):
+        carry = init
+        ys = []
+        leaves = []
+        _tree_map(lambda a: leaves.append(np.asarray(a)), xs)
+        n = leaves[0].shape[0]
+        for i in range(n):
+            carry, y = f(carry, _tree_map(lambda a, i=i: np.asarray(a)[i], xs))
+            ys.append(y)
+        return carry, ys
+
+    def dynamic_slice(operand, start_indices, slice_sizes):
+        sl = tuple(slice(int(s), int(s) + int(n)) for s, n in zip(start_indices, slice_sizes))
+        return np.asarray(operand)[sl]
+
+    lax.fori_loop = fori_loop
+    lax.switch = switch
+    lax.cond = cond
+    lax.map = lax_map
+    lax.scan = scan
+    lax.dynamic_slice = dynamic_slice
+    return lax
+
+
+def install_jax():
+    jax = types.ModuleType("jax")
+    jnp = _make_jnp()
+    lax = _make_lax()
+    tree_util = types.ModuleType("jax.tree_util")
+    tree_util.register_pytree_node = lambda *a, **k: None
+    tree_util.tree_map = _tree_map
+    jscipy = types.ModuleType("jax.scipy")
+    special = types.ModuleType("jax.scipy.special")
+    special.gamma = scipy.special.gamma
+    special.gammainc = scipy.special.gammainc
+    special.gammaln = scipy.special.gammaln
+    special.factorial = scipy.special.factorial
+    signal = types.ModuleType("jax.scipy.signal")
+    signal.fftconvolve = lambda in1, in2, mode="full": np.asarray(
+        scipy.signal.fftconvolve(in1, in2, mode=mode)).view(AtArray)
+    signal.convolve2d = lambda in1, in2, mode="full": np.asarray(
+        scipy.signal.convolve2d(in1, in2, mode=mode)).view(AtArray)
+    ndimage = types.ModuleType("jax.scipy.ndimage")
+    ndimage.map_coordinates = scipy.ndimage.map_coordinates
+    jscipy.special = special
+    jscipy.signal = signal
+    jscipy.ndimage = ndimage
+    config = types.SimpleNamespace(update=lambda *a, **k: None)
+    experimental = types.ModuleType("jax.experimental")
+    jax.numpy = jnp
+    jax.lax = lax
+    jax.tree_util = tree_util
+    jax.scipy = jscipy
+    jax.config = config
+    jax.experimental = experimental
+    jax.jit = jit
+    jax.custom_jvp = custom_jvp
+    jax.jvp = lambda *a, **k: (_ for _ in ()).throw(NotImplementedError("jvp"))
+    jax.grad = lambda *a, **k: (_ for _ in ()).throw(NotImplementedError("grad"))
+    jax.vmap = lambda f, *a, **k: f
+    jax.Array = np.ndarray
+    jax.devices = lambda *a, **k: ["cpu"]
+    jax.debug = types.SimpleNamespace(print=lambda *a, **k: None)
+    mods = {
+        "jax": jax, "jax.numpy": jnp, "jax.lax": lax, "jax.tree_util": tree_util,
+        "jax.scipy": jscipy, "jax.scipy.special": special, "jax.scipy.signal": signal,
+        "jax.scipy.ndimage": ndimage, "jax.experimental": experimental,
+    }
+    sys.modules.update(mods)
+
+
+# ---------------------------------------------------------------------------
+# lenstronomy / astropy names on the image path
+# ---------------------------------------------------------------------------
+
+
+def _make_grid(numPix, deltapix, subgrid_res=1, left_lower=False):
+    n = np.array([numPix, numPix], dtype=int) if np.isscalar(numPix) else np.asarray(numPix, int)
+    n_eff = (n * subgrid_res).astype(int)
+    d_eff = deltapix / float(subgrid_res)
+    xg = np.tile(np.arange(n_eff[0]), n_eff[1]) * d_eff
+    yg = np.repeat(np.arange(n_eff[1]), n_eff[0]) * d_eff
+    if left_lower:
+        shift = -1.0 / 2 + 1.0 / (2 * subgrid_res) * np.array([1, 1])
+    else:
+        shift = d_eff * (n_eff - 1) / 2
+    return xg - shift[0], yg - shift[1]
+
+
+def _array2image(array, nx=0, ny=0):
+    array = np.asarray(array)
+    if nx == 0 or ny == 0:
+        n = int(np.sqrt(len(array)))
+        nx = ny = n
+    return array.reshape(ny, nx)
+
+
+def _image2array(image):
+    return np.asarray(image).reshape(-1)
+
+
+def _make_subgrid(ra_coord, dec_coord, subgrid_res=2):
+    ra = _array2image(ra_coord)
+    dec = _array2image(dec_coord)
+    n = len(ra)
+    d_ra_x = ra[0][1] - ra[0][0]
+    d_ra_y = ra[1][0] - ra[0][0]
+    d_dec_x = dec[0][1] - dec[0][0]
+    d_dec_y = dec[1][0] - dec[0][0]
+    ra_new = np.zeros((n * subgrid_res, n * subgrid_res))
+    dec_new = np.zeros((n * subgrid_res, n * subgrid_res))
+    for i in range(subgrid_res):
+        fy = -0.5 + 1.0 / (2.0 * subgrid_res) + i / float(subgrid_res)
+        for j in range(subgrid_res):
+            fx = -0.5 + 1.0 / (2.0 * subgrid_res) + j / float(subgrid_res)
+            ra_new[i::subgrid_res, j::subgrid_res] = ra + d_ra_x * fx + d_ra_y * fy
+            dec_new[i::subgrid_res, j::subgrid_res] = dec + d_dec_x * fx + d_dec_y * fy
+    return _image2array(ra_new), _image2array(dec_new)
+
+
+def _convert_bool_list(n, k=None):
+    if k is None:
+        return [True] * n
+    if isinstance(k, (int, np.integer)):
+        out = [False] * n
+        out[k] = True
+        return out
+    k = list(k)
+    if len(k) and isinstance(k[0], (bool, np.bool_)):
+        return [bool(v) for v in k]
+    out = [False] * n
+    for i in k:
+        out[i] = True
+    return out
+
+
+def _grid_from_transform(nx, ny, M, ra0, dec0):
+    a = np.arange(nx)
+    b = np.arange(ny)
+    mat = np.dstack(np.meshgrid(a, b)).reshape(-1, 2)
+    x, y = mat[:, 0], mat[:, 1]
+    ra = x * M[0, 0] + y * M[0, 1] + ra0
+    dec = x * M[1, 0] + y * M[1, 1] + dec0
+    return ra, dec
+
+
+class Coordinates1D:
+    def __init__(self, transform_pix2angle, ra_at_xy_0, dec_at_xy_0):
+        self._Mpix2a = np.asarray(transform_pix2angle, float)
+        self._Ma2pix = np.linalg.inv(self._Mpix2a)
+        self._ra_at_xy_0 = ra_at_xy_0
+        self._dec_at_xy_0 = dec_at_xy_0
+        self._x_at_radec_0, self._y_at_radec_0 = self._Ma2pix.dot(
+            np.array([-ra_at_xy_0, -dec_at_xy_0]))
+
+    @property
+    def transform_pix2angle(self):
+        return self._Mpix2a
+
+    @property
+    def radec_at_xy_0(self):
+        return self._ra_at_xy_0, self._dec_at_xy_0
+
+    @property
+    def pixel_width(self):
+        return float(np.sqrt(abs(np.linalg.det(self._Mpix2a))))
+
+    def map_pix2coord(self, x, y):
+        ra = x * self._Mpix2a[0, 0] + y * self._Mpix2a[0, 1] + self._ra_at_xy_0
+        dec = x * self._Mpix2a[1, 0] + y * self._Mpix2a[1, 1] + self._dec_at_xy_0
+        return ra, dec
+
+    def coordinate_grid(self, nx, ny):
+        return _grid_from_transform(nx, ny, self._Mpix2a, self._ra_at_xy_0, self._dec_at_xy_0)
+
+
+class PixelGrid(Coordinates1D):
+    def __init__(self, nx, ny, transform_pix2angle, ra_at_xy_0, dec_at_xy_0,
+                 antenna_primary_beam=None):
+        super().__init__(transform_pix2angle, ra_at_xy_0, dec_at_xy_0)
+        self._nx = nx
+        self._ny = ny
+        self._pb = antenna_primary_beam
+
+    @property
+    def num_pixel_axes(self):
+        return self._nx, self._ny
+
+    @property
+    def num_pixel(self):
+        return self._nx * self._ny
+
+    @property
+    def width(self):
+        return self.pixel_width * np.array([self._nx, self._ny])
+
+    @property
+    def center(self):
+        return self.map_pix2coord((self._nx - 1) / 2.0, (self._ny - 1) / 2.0)
+
+    @property
+    def primary_beam(self):
+        return self._pb
+
+
+class PSF:
+    def __init__(self, psf_type="NONE", fwhm=None, truncation=5, kernel_point_source=None,
+                 psf_variance_map=None, point_source_supersampling_factor=1, **kw):
+        self.psf_type = psf_type
+        self._fwhm = fwhm
+        self._truncation = truncation
+        self._kernel = None
+        if psf_type == "PIXEL":
+            k = np.asarray(kernel_point_source, float)
+            self._kernel = k / np.sum(k)
+        self.psf_variance_map_bool = psf_variance_map is not None
+        self._pixel_size = None
+
+    @property
+    def kernel_point_source(self):
+        return self._kernel
+
+    @property
+    def fwhm(self):
+        return self._fwhm
+
+    @property
+    def truncation(self):
+        return self._truncation
+
+    def set_pixel_size(self, deltaPix):
+        self._pixel_size = deltaPix
+
+    point_source_supersampling_factor = 1
+
+    def kernel_point_source_supersampled(self, supersampling_factor, updata_cache=False):
+        if supersampling_factor != 1:
+            raise NotImplementedError("supersampled PSF kernels are not restated")
+        return self._kernel
+
+
+class Image2SourceMapping:
+    """Single lens plane: source i is evaluated at theta - scale_i * alpha(theta)."""
+
+    def __init__(self, lens_model, source_model):
+        self._lens = lens_model
+        self._source = source_model
+
+    def image_flux_joint(self, x, y, kwargs_lens, kwargs_source, kwargs_special=None, k=None):
+        scal = getattr(self._source, "deflection_scaling_list", None)
+        if scal is None:
+            bx, by = self._lens.ray_shooting(x, y, kwargs_lens)
+            return self._source.surface_brightness(bx, by, kwargs_source, k=k)
+        ax, ay = self._lens.alpha(x, y, kwargs_lens)
+        flux = np.zeros_like(np.asarray(x, float))
+        for i, func in enumerate(self._source.func_list):
+            if k is None or k == i:
+                flux = flux + func.function(x - scal[i] * ax, y - scal[i] * ay, **kwargs_source[i])
+        return flux
+
+
+def _exporter():
+    names = []
+
+    def export(obj):
+        names.append(obj.__name__)
+        return obj
+
+    return export, names
+
+
+class _Dummy:
+    def __init__(self, *a, **k):
+        pass
+
+    def __getattr__(self, name):
+        return _Dummy()
+
+    def __call__(self, *a, **k):
+        return _Dummy()
+
+
+def install_lenstronomy():
+    def mod(name, **attrs):
+        m = types.ModuleType(name)
+        for k, v in attrs.items():
+            setattr(m, k, v)
+        sys.modules[name] = m
+        return m
+
+    util = mod("lenstronomy.Util.util", make_grid=_make_grid, make_subgrid=_make_subgrid,
+               array2image=_array2image, image2array=_image2array,
+               convert_bool_list=_convert_bool_list, local_minima_2d=_Dummy(),
+               selectBest=_Dummy(), fwhm2sigma=lambda f: f / (2 * np.sqrt(2 * np.log(2))),
+               grid_from_coordinate_transform=_grid_from_transform)
+    package_util = mod("lenstronomy.Util.package_util", exporter=_exporter)
+    kernel_util = mod("lenstronomy.Util.kernel_util", cut_psf=_Dummy(), split_kernel=_Dummy())
+    constants = mod("lenstronomy.Util.constants")
+    cosmo_util = mod("lenstronomy.Util.cosmo_util", get_astropy_cosmology=_Dummy())
+    mod("lenstronomy.Util", util=util, package_util=package_util, kernel_util=kernel_util,
+        constants=constants, cosmo_util=cosmo_util)
+    base_profile = mod("lenstronomy.LensModel.Profiles.base_profile",
+                       LensProfileBase=type("LensProfileBase", (object,), {
+                           "__init__": lambda self, *a, **k: None,
+                           "set_static": lambda self, **k: None,
+                           "set_dynamic": lambda self: None}))
+    mod("lenstronomy.LensModel.Profiles", base_profile=base_profile)
+    mp = mod("lenstronomy.LensModel.MultiPlane.multi_plane", MultiPlane=_Dummy)
+    mod("lenstronomy.LensModel.MultiPlane", multi_plane=mp)
+    mod("lenstronomy.LensModel")
+    pg = mod("lenstronomy.Data.pixel_grid", PixelGrid=PixelGrid)
+    ct = mod("lenstronomy.Data.coord_transforms", Coordinates1D=Coordinates1D)
+    psf = mod("lenstronomy.Data.psf", PSF=PSF)
+    mod("lenstronomy.Data", pixel_grid=pg, coord_transforms=ct, psf=psf)
+    i2s = mod("lenstronomy.ImSim.image2source_mapping", Image2SourceMapping=Image2SourceMapping)
+    de = mod("lenstronomy.ImSim.differential_extinction", DifferentialExtinction=_Dummy)
+    mod("lenstronomy.ImSim", image2source_mapping=i2s, differential_extinction=de)
+    cl = mod("lenstronomy.Conf.config_loader", conventions_conf=lambda: {})
+    mod("lenstronomy.Conf", config_loader=cl)
+    lc = mod("lenstronomy.Cosmo.lens_cosmo", LensCosmo=_Dummy)
+    bg = mod("lenstronomy.Cosmo.background", Background=_Dummy)
+    mod("lenstronomy.Cosmo", lens_cosmo=lc, background=bg)
+    mod("lenstronomy")
+    cosmo = mod("astropy.cosmology", default_cosmology=_Dummy())
+    cosmo.__all__ = ["default_cosmology"]
+    mod("astropy", cosmology=cosmo)
+
+
+def install(reference_root):
+    install_jax()
+    install_lenstronomy()
+    if reference_root not in sys.path:
+        sys.path.insert(0, reference_root)

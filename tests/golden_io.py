@@ -1,0 +1,51 @@
+"""Readers for the committed golden fixtures (tests/golden/*.npz) and the
+scene dicts the oracle consumes."""
+
+import json
+import os
+
+import numpy as np
+
+from jaxtronomy_gb300.workloads import grid_kwargs
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    d = np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+    return d, json.loads(str(d["meta"]))
+
+
+def profile_cases():
+    d, meta = load("profiles.npz")
+    out = []
+    for i, m in enumerate(meta):
+        out.append(dict(m, x=d["x_%d" % i], y=d["y_%d" % i], out=d["out_%d" % i]))
+    return out
+
+
+def image_scenes():
+    d, meta = load("images.npz")
+    scenes = []
+    for i, sc in enumerate(meta["scenes"]):
+        sc = dict(sc)
+        sc["image"] = d["image_%d" % i]
+        sc["kernel"] = d["kernel_%d" % i] if ("kernel_%d" % i) in d.files else None
+        scenes.append(sc)
+    like = dict(meta["likelihood"])
+    like["data"] = d["like_data"]
+    return scenes, like
+
+
+def oracle_scene(sc):
+    """Scene dict of the oracle (oracle.image) for a golden image scene."""
+    g = grid_kwargs(sc["num_pix"], sc["delta_pix"])
+    kernel = sc.get("kernel")
+    if kernel is not None:
+        kernel = kernel / kernel.sum()
+    return dict(nx=sc["num_pix"], ny=sc["num_pix"], supersampling_factor=sc["s"],
+                psf_type=sc["psf_type"], kernel=kernel, fwhm=sc.get("fwhm"),
+                truncation=sc.get("truncation", 5.0), lens_model_list=sc["lens"],
+                source_light_model_list=sc["src"], lens_light_model_list=sc["ll"],
+                flux_scaling=sc.get("flux_scaling", 1.0),
+                deflection_scaling_list=sc.get("deflection_scaling"), **g)

@@ -116,6 +116,30 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
                  const void* psf_dev, long long psf_stride, void* out_dev, int flags,
                  void* stream);
 
+/* lensgb_image without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory on the
+ * call path -- e.g. a handler invoked from inside an XLA/JAX program (the way a
+ * JAX user of the reference would bind this library through jax.ffi), where
+ * XLA has already reserved most of the GPU's memory for its own pool, so a
+ * cudaMalloc can fail, and cudaFree would synchronize the device under XLA.
+ *
+ * Same arguments and results as lensgb_image.  The device scratch (profile
+ * records, EPL tables, un-convolved images) comes from a fixed array of
+ * LENSGB_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads
+ * the library holds until exit.  A call whose scratch would exceed it returns
+ * LENSGB_ERR_INVALID with the needed size (FP32, 180x180 pixels, EPL+SHEAR and
+ * two Sersic profiles: about 137 KB per system, so up to ~490 systems).
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU race, so issue them on one stream or serialise them.
+ * Each call writes every scratch element before reading it, so no state
+ * carries over between calls. */
+#define LENSGB_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int lensgb_image_noalloc(lensgb_model* model, const double* params_dev, int n_inst,
+                         const void* psf_dev, long long psf_stride, void* out_dev, int flags,
+                         void* stream);
+
 /* PixelKernelConvolution.convolution2d / GaussianConvolution.convolution2d
  * (jaxtronomy/ImSim/Numerics/convolution.py:74-86,215-235) on n_inst images of
  * the model's grid: "same"-mode convolution with the model's PSF type (PIXEL:

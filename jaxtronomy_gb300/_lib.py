@@ -33,7 +33,8 @@ NO_LENS_LIGHT = 4
 # exported symbols (must match include/lensgb.h)
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
-    "lensgb_image", "lensgb_convolve", "lensgb_loglike", "lensgb_ray_shooting", "lensgb_alpha",
+    "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
+    "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
     "lensgb_last_error", "lensgb_version",
 ]
@@ -104,6 +105,8 @@ def load():
     lib.lensgb_model_param_count.restype = i
     lib.lensgb_image.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
     lib.lensgb_image.restype = i
+    lib.lensgb_image_noalloc.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
+    lib.lensgb_image_noalloc.restype = i
     lib.lensgb_convolve.argtypes = [vp, vp, i, vp, ll, vp, vp]
     lib.lensgb_convolve.restype = i
     lib.lensgb_loglike.argtypes = [vp, dp, i, vp, ll, ctypes.POINTER(NoiseDesc), vp, dp, vp]

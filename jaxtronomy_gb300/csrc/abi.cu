@@ -361,3 +361,103 @@ int lensgb_surface_brightness(const lensgb_model* mc, int which, const double* p
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// lensgb_image_noalloc: lensgb_image without any device allocation.
+//
+// Its scratch (per-profile records, EPL coefficient tables and the
+// un-convolved image) lives in one fixed, file-scope device array of
+// LENSGB_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds
+// until the process exits.  In host code `g_noalloc_scratch` names only a
+// host-side stand-in, so its device address is looked up once per device with
+// cudaGetSymbolAddress (on the first call made with that device current) and
+// cached.  Every call overwrites each scratch element it later reads, so
+// nothing has to be cleared between calls; calls that overlap on the GPU share
+// the array and race.
+// ---------------------------------------------------------------------------
+
+#include <mutex>
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[LENSGB_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {nullptr};
+static std::mutex g_noalloc_mutex;
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static int noalloc_scratch_ptr(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return fail(LENSGB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return fail(LENSGB_ERR_INVALID, "device ordinal out of range for the no-alloc scratch");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(LENSGB_ERR_CUDA, std::string("cudaGetSymbolAddress(no-alloc scratch): ") +
+                                             cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return LENSGB_OK;
+}
+
+extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n_inst,
+                                    const void* psf, long long psf_stride, void* out, int flags,
+                                    void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!out || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    const int n_prof = m->st.n_lens + m->st.n_src + m->st.n_ll;
+    const size_t nrec = (size_t)n_inst * (n_prof > 0 ? n_prof : 1);
+    const size_t ncoef = (size_t)n_inst * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
+    const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
+    const size_t b_rec_d = align256(nrec * REC_D * sizeof(double));
+    const size_t b_rec_f = align256(nrec * REC_F * sizeof(float));
+    const size_t b_coef_d = align256(ncoef * sizeof(double));
+    const size_t b_coef_f = align256(ncoef * sizeof(float));
+    const size_t b_low = conv ? align256((size_t)n_inst * m->grid.nx * m->grid.ny * esz) : 0;
+    const size_t need = b_rec_d + b_rec_f + b_coef_d + b_coef_f + b_low;
+    if (need > (size_t)LENSGB_NOALLOC_SCRATCH_BYTES) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "this call needs %zu bytes of scratch; lensgb_image_noalloc holds at most %zu "
+                 "bytes (use fewer systems per call, or lensgb_image)",
+                 need, (size_t)LENSGB_NOALLOC_SCRATCH_BYTES);
+        return fail(LENSGB_ERR_INVALID, msg);
+    }
+    void* base = nullptr;
+    int rc = noalloc_scratch_ptr(&base);
+    if (rc) return rc;
+    unsigned char* p = (unsigned char*)base;
+    double* rec_d = (double*)p;
+    float* rec_f = (float*)(p + b_rec_d);
+    double* coef_d = (double*)(p + b_rec_d + b_rec_f);
+    float* coef_f = (float*)(p + b_rec_d + b_rec_f + b_coef_d);
+    void* low = p + b_rec_d + b_rec_f + b_coef_d + b_coef_f;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_prepare(m->grid, m->st, params, n_inst, rec_d, rec_f, coef_d, coef_f, s);
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    const double scale = m->pixel_width * m->pixel_width;
+    launch_raytrace(m->grid, m->st, n_inst, rec_d, rec_f, coef_d, coef_f, conv ? low : out, flags,
+                    scale, m->desc.precision, s);
+    if ((rc = check_cuda("raytrace launch"))) return rc;
+    if (conv) {
+        if (launch_conv(low, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                        m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
+                        m->desc.precision, s))
+            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = check_cuda("convolution launch"))) return rc;
+    }
+    return LENSGB_OK;
+}

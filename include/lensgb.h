@@ -103,6 +103,18 @@ int lensgb_model_destroy(lensgb_model* model);
 /* Number of doubles per system row for this model. */
 int lensgb_model_param_count(const lensgb_model* model);
 
+/* FP32-split models only: pixels whose predicted FP32 error exceeds `tau`
+ * (relative, per supersampled ray) are recomputed in FP64.  The prediction is
+ * (sum_k I_k |d ln I_k / d beta|) * kappa * (|alpha_x| + |alpha_y|) / I_ray, with
+ * kappa the FP32 relative error bound of the deflection.  Defaults: tau = 2e-5,
+ * kappa = 3e-7; tau <= 0 disables the FP64 pass.  No counterpart in the
+ * reference (which computes everything in FP64). */
+int lensgb_model_set_refine(lensgb_model* model, double tau, double kappa);
+
+/* Number of pixels the last image call of this model recomputed in FP64
+ * (synchronizes `stream`). */
+int lensgb_model_refined_pixels(const lensgb_model* model, void* stream, long long* n);
+
 /* ImageModel.image for n_inst systems (image_model.py:432-492).
  *  params_dev : n_inst x param_count doubles
  *  psf_dev    : PSF kernels, kernel_size^2 values each, FP64 for LENSGB_FP64
@@ -128,7 +140,7 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
  * LENSGB_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads
  * the library holds until exit.  A call whose scratch would exceed it returns
  * LENSGB_ERR_INVALID with the needed size (FP32, 180x180 pixels, EPL+SHEAR and
- * two Sersic profiles: about 137 KB per system, so up to ~490 systems).
+ * two Sersic profiles: about 267 KB per system, so up to ~250 systems).
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call
  * before any stream capture.  All calls share the one array: calls that

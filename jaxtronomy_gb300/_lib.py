@@ -33,6 +33,7 @@ NO_LENS_LIGHT = 4
 # exported symbols (must match include/lensgb.h)
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
+    "lensgb_model_set_refine", "lensgb_model_refined_pixels",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
@@ -103,6 +104,10 @@ def load():
     lib.lensgb_model_destroy.restype = i
     lib.lensgb_model_param_count.argtypes = [vp]
     lib.lensgb_model_param_count.restype = i
+    lib.lensgb_model_set_refine.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    lib.lensgb_model_set_refine.restype = i
+    lib.lensgb_model_refined_pixels.argtypes = [vp, vp, ctypes.POINTER(ll)]
+    lib.lensgb_model_refined_pixels.restype = i
     lib.lensgb_image.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
     lib.lensgb_image.restype = i
     lib.lensgb_image_noalloc.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
@@ -134,13 +139,20 @@ def check(rc):
 class Model:
     """Owner of one lensgb_model handle."""
 
-    def __init__(self, desc):
+    def __init__(self, desc, refine=None):
         lib = load()
         h = ctypes.c_void_p()
         check(lib.lensgb_model_create(ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
         self.desc = desc
         self.param_count = lib.lensgb_model_param_count(h)
+        if refine is not None:
+            check(lib.lensgb_model_set_refine(h, float(refine[0]), float(refine[1])))
+
+    def refined_pixels(self, stream):
+        n = ctypes.c_longlong(0)
+        check(load().lensgb_model_refined_pixels(self._h, stream, ctypes.byref(n)))
+        return int(n.value)
 
     @property
     def handle(self):

@@ -24,6 +24,10 @@ struct lensgb_model {
     double* coef_d = nullptr;
     float* coef_f = nullptr;
     void* lowres = nullptr;
+    unsigned int* refine_list = nullptr;  // FP32 models: one entry per pixel
+    unsigned int* refine_count = nullptr;
+    float refine_tau = 2e-5f;             // see lensgb_model_set_refine
+    float refine_kappa = 3e-7f;
 };
 
 static thread_local std::string g_last_error;
@@ -66,6 +70,10 @@ static void free_scratch(lensgb_model* m) {
     cudaFree(m->coef_d);
     cudaFree(m->coef_f);
     cudaFree(m->lowres);
+    cudaFree(m->refine_list);
+    cudaFree(m->refine_count);
+    m->refine_list = nullptr;
+    m->refine_count = nullptr;
     m->rec_d = nullptr;
     m->rec_f = nullptr;
     m->coef_d = nullptr;
@@ -88,7 +96,10 @@ static int ensure_scratch(lensgb_model* m, int n_inst) {
         cudaMalloc(&m->rec_f, nrec * REC_F * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&m->coef_d, ncoef * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&m->coef_f, ncoef * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&m->lowres, nimg * esz) != cudaSuccess) {
+        cudaMalloc(&m->lowres, nimg * esz) != cudaSuccess ||
+        (m->desc.precision == LENSGB_FP32_SPLIT &&
+         (cudaMalloc(&m->refine_list, nimg * sizeof(unsigned int)) != cudaSuccess ||
+          cudaMalloc(&m->refine_count, sizeof(unsigned int)) != cudaSuccess))) {
         cudaGetLastError();
         free_scratch(m);
         return fail(LENSGB_ERR_OOM, "device allocation of model scratch failed");
@@ -106,9 +117,55 @@ static int exact_bits(int n) {
     return bits < 1 ? 1 : bits;
 }
 
+// Refinement of the FP32 path: active for FP32 models with tau > 0, when the
+// global pixel index of the batch fits the 32-bit list entries.
+static RefineArgs refine_args(const lensgb_model* m, int n_inst, unsigned int* list,
+                              unsigned int* count) {
+    RefineArgs rf;
+    rf.list = list;
+    rf.count = count;
+    rf.kappa = m->refine_kappa;
+    rf.tau = 0.f;
+    if (m->desc.precision == LENSGB_FP32_SPLIT && m->refine_tau > 0.f && list && count)
+        rf.tau = m->refine_tau;
+    return rf;
+}
+
+// The refine list stores 32-bit batch-global pixel indices.
+static int check_refine_size(const lensgb_model* m, int n_inst) {
+    if (m->desc.precision == LENSGB_FP32_SPLIT && m->refine_tau > 0.f &&
+        (long long)n_inst * m->grid.nx * m->grid.ny >= (1LL << 32))
+        return fail(LENSGB_ERR_INVALID,
+                    "n_inst * nx * ny must stay below 2^32 for FP32 models; split the batch");
+    return LENSGB_OK;
+}
+
 extern "C" {
 
-int lensgb_version(void) { return 100; }
+int lensgb_version(void) { return 101; }
+
+int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (!(kappa > 0) || !(tau == tau)) return fail(LENSGB_ERR_INVALID, "kappa must be positive");
+    m->refine_tau = (float)tau;
+    m->refine_kappa = (float)kappa;
+    return LENSGB_OK;
+}
+
+int lensgb_model_refined_pixels(const lensgb_model* m, void* stream, long long* n) {
+    if (!m || !n) return fail(LENSGB_ERR_INVALID, "null model or output");
+    *n = 0;
+    if (!m->refine_count) return LENSGB_OK;
+    unsigned int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, m->refine_count, sizeof v, cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return fail(LENSGB_ERR_CUDA, std::string("reading the refine count: ") +
+                                         cudaGetErrorString(e));
+    *n = v;
+    return LENSGB_OK;
+}
 
 const char* lensgb_last_error(void) { return g_last_error.c_str(); }
 
@@ -183,6 +240,9 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     st.n_params = off;
     st.alpha_scaling = d->alpha_scaling;
     st.flux_scaling = d->flux_scaling;
+    st.alpha_scaling_f = (float)d->alpha_scaling;
+    st.flux_scaling_f = (float)d->flux_scaling;
+    for (int i = 0; i < MAX_PROF; ++i) st.src_scale_f[i] = (float)st.src_scale[i];
 
     GridDesc& g = m->grid;
     const double* M = d->transform_pix2angle;
@@ -227,15 +287,20 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
     if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
-    int rc = ensure_scratch(m, n_inst);
+    int rc = check_refine_size(m, n_inst);
+    if (rc) return rc;
+    rc = ensure_scratch(m, n_inst);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     launch_prepare(m->grid, m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
     if ((rc = check_cuda("prepare launch"))) return rc;
     const double scale = m->pixel_width * m->pixel_width;
     void* target = conv ? m->lowres : out;
+    RefineArgs rf = refine_args(m, n_inst, m->refine_list, m->refine_count);
+    if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), s) != cudaSuccess)
+        return check_cuda("refine counter reset");
     launch_raytrace(m->grid, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
-                    flags, scale, m->desc.precision, s);
+                    flags, scale, m->desc.precision, rf, s);
     if ((rc = check_cuda("raytrace launch"))) return rc;
     if (conv) {
         if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
@@ -427,7 +492,10 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
     const size_t b_coef_d = align256(ncoef * sizeof(double));
     const size_t b_coef_f = align256(ncoef * sizeof(float));
     const size_t b_low = conv ? align256((size_t)n_inst * m->grid.nx * m->grid.ny * esz) : 0;
-    const size_t need = b_rec_d + b_rec_f + b_coef_d + b_coef_f + b_low;
+    const bool fp32 = m->desc.precision == LENSGB_FP32_SPLIT;
+    const size_t b_list = fp32 ? align256((size_t)n_inst * m->grid.nx * m->grid.ny * 4) : 0;
+    const size_t b_cnt = fp32 ? 256 : 0;
+    const size_t need = b_rec_d + b_rec_f + b_coef_d + b_coef_f + b_low + b_list + b_cnt;
     if (need > (size_t)LENSGB_NOALLOC_SCRATCH_BYTES) {
         char msg[256];
         snprintf(msg, sizeof msg,
@@ -436,8 +504,10 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
                  need, (size_t)LENSGB_NOALLOC_SCRATCH_BYTES);
         return fail(LENSGB_ERR_INVALID, msg);
     }
+    int rc = check_refine_size(m, n_inst);
+    if (rc) return rc;
     void* base = nullptr;
-    int rc = noalloc_scratch_ptr(&base);
+    rc = noalloc_scratch_ptr(&base);
     if (rc) return rc;
     unsigned char* p = (unsigned char*)base;
     double* rec_d = (double*)p;
@@ -445,12 +515,17 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
     double* coef_d = (double*)(p + b_rec_d + b_rec_f);
     float* coef_f = (float*)(p + b_rec_d + b_rec_f + b_coef_d);
     void* low = p + b_rec_d + b_rec_f + b_coef_d + b_coef_f;
+    unsigned int* list = fp32 ? (unsigned int*)((unsigned char*)low + b_low) : nullptr;
+    unsigned int* cnt = fp32 ? (unsigned int*)((unsigned char*)low + b_low + b_list) : nullptr;
     cudaStream_t s = (cudaStream_t)stream;
     launch_prepare(m->grid, m->st, params, n_inst, rec_d, rec_f, coef_d, coef_f, s);
     if ((rc = check_cuda("prepare launch"))) return rc;
     const double scale = m->pixel_width * m->pixel_width;
+    RefineArgs rf = refine_args(m, n_inst, list, cnt);
+    if (rf.tau > 0.f && cudaMemsetAsync(cnt, 0, sizeof(unsigned int), s) != cudaSuccess)
+        return check_cuda("refine counter reset");
     launch_raytrace(m->grid, m->st, n_inst, rec_d, rec_f, coef_d, coef_f, conv ? low : out, flags,
-                    scale, m->desc.precision, s);
+                    scale, m->desc.precision, rf, s);
     if ((rc = check_cuda("raytrace launch"))) return rc;
     if (conv) {
         if (launch_conv(low, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,

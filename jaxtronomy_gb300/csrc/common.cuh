@@ -48,6 +48,19 @@ struct StackDesc {
     double src_scale[MAX_PROF];  // deflection_scaling per source
     double alpha_scaling;
     double flux_scaling;
+    // FP32 copies, so FP32 kernels never convert per ray
+    float src_scale_f[MAX_PROF];
+    float alpha_scaling_f;
+    float flux_scaling_f;
+};
+
+// Pixels of the FP32 pass whose predicted error exceeds `tau` are appended to
+// `list` (as system * nx * ny + pixel) and recomputed in FP64 by the refine pass.
+struct RefineArgs {
+    unsigned int* list;         // capacity: n_inst * nx * ny entries
+    unsigned int* count;        // zeroed on the stream before the FP32 pass
+    float tau;                  // tolerated predicted relative error per ray (<= 0: no refine)
+    float kappa;                // FP32 relative error bound of |alpha| (units of 1)
 };
 
 // ---------------------------------------------------------------------------

@@ -13,10 +13,13 @@ int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params,
                    cudaStream_t stream);
 
 // Supersampled ray tracing + light + s x s re-binning into a (ny, nx) image per
-// system, scaled by out_scale (pixel_width^2).  `precision` selects FP64 or FP32.
+// system, scaled by out_scale (pixel_width^2).  `precision` selects FP64 or FP32;
+// the FP32 path refines flagged pixels in FP64 as described by `rf`
+// (rf.count must be zero on the stream when the launch starts).
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,
-                    int flags, double out_scale, int precision, cudaStream_t stream);
+                    int flags, double out_scale, int precision, const RefineArgs& rf,
+                    cudaStream_t stream);
 
 // "same"-mode 2-D convolution of n_inst (ny, nx) images with K x K kernels
 // (kernel stride 0 = shared).  edge = 0: zero padding; 1: edge padding.

@@ -312,4 +312,25 @@ __device__ __forceinline__ R sersic_flux(const R* rec, R dx, R dy) {
     return amp * nan_to_num_max(res);
 }
 
+// FP32 Sersic flux plus g = |d ln I / dR| = b_n (R/R_s)^(1/n) / (n R), the
+// log-gradient that turns an absolute position error into a relative flux
+// error (0 inside the 1e-4 smoothing floor, where the profile is flat).
+__device__ __forceinline__ float sersic_flux_grad(const float* rec, float dx, float dy, float& g) {
+    const float amp = rec[slot<float>(2)], inv_rs = rec[slot<float>(4)];
+    const float inv_n = rec[slot<float>(5)], bn = rec[slot<float>(6)];
+    const float m00 = rec[slot<float>(7)], m01 = rec[slot<float>(8)], m10 = rec[slot<float>(9)],
+                m11 = rec[slot<float>(10)];
+    const float x = m00 * dx + m01 * dy;
+    const float y = m10 * dx + m11 * dy;
+    const float Rr = sqrtf(x * x + y * y);
+    const bool floored = !(Rr > 0.0001f);
+    const float Rst = floored ? 0.0001f : Rr;
+    const float frac = Rst * inv_rs;
+    const float v = exp2f(inv_n * log2f(frac));
+    const float ex = -bn * (v - 1.f);
+    const float res = frac <= 1000.f ? expf(ex) : 0.f;
+    g = floored ? 0.f : bn * inv_n * v / Rst;
+    return amp * nan_to_num_max(res);
+}
+
 }  // namespace lensgb

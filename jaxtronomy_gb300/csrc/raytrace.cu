@@ -1,13 +1,22 @@
-// Fused ray-tracing kernel: for every supersampled ray of every system,
+// Fused ray-tracing kernels: for every supersampled ray of every system,
 // deflection sum -> lensed source light -> lens light, then the s x s block
-// mean into the (ny, nx) pixel image.  The ray grid exists only in registers
-// and one shared-memory staging buffer; the image leaves the kernel already
-// multiplied by pixel_width^2 and flux_scaling.
+// mean into the (ny, nx) pixel image.  The ray grid exists only in registers;
+// the image leaves the kernel already multiplied by pixel_width^2 and
+// flux_scaling.
 //
-// Mapping: blockIdx.y = system; blockIdx.x = a run of P consecutive pixels
-// (row-major).  Each thread owns one supersampled ray per pass over the
-// CTA's P*s^2 rays; consecutive threads own neighbouring sub-rays, so warps
-// stay spatially coherent.
+// Mapping: blockIdx.y = system; each thread owns the s^2 supersampled rays of
+// one pixel at a time (pixels of a CTA are consecutive in row-major order, so
+// a warp covers 32 neighbouring pixels of a row and stays spatially coherent).
+// Profile records of the CTA's system sit in shared memory.
+//
+// FP32 path ("FP32 split"): the bulk arithmetic is FP32.  Coordinate offsets
+// from every profile centre are formed with FP64 accuracy (split_offset), and
+// each sub-ray predicts the relative error its FP32 deflection causes in the
+// source light (Sersic log-gradient x the FP32 error bound of beta = theta -
+// alpha, weighted by the source's share of the ray's flux).  Pixels where the
+// prediction exceeds `tau` -- rays landing close to a steep source centre,
+// where the lens equation cancels theta against alpha -- are appended to a
+// list that refine_kernel recomputes in FP64 with the code of the FP64 path.
 //
 // Reference path (JAXtronomy source tree):
 //   ray grid          ImSim/Numerics/grid.py:48-72 (lenstronomy make_subgrid)
@@ -21,25 +30,9 @@
 
 namespace lensgb {
 
-template <typename R>
-struct RayCtx {
-    // FP64: absolute ray coordinate; FP32: exact/small parts of the offset
-    // from supersampled ray (0,0)
-    double X, Y;
-    float px, lx, py, ly;
-};
-
-template <typename R>
-__device__ __forceinline__ void ray_offset(const RayCtx<R>& c, const R* rec, R& dx, R& dy) {
-    if (sizeof(R) == 8) {
-        dx = (R)(c.X - (double)rec[RD_CX]);
-        dy = (R)(c.Y - (double)rec[RD_CY]);
-    } else {
-        const float* fr = (const float*)rec;
-        dx = (R)split_offset(fr[RF_X0H], fr[RF_X0L], c.px, c.lx);
-        dy = (R)split_offset(fr[RF_Y0H], fr[RF_Y0L], c.py, c.ly);
-    }
-}
+// Lens-stack selector: C0/C1 are compile-time lens codes (0 = absent); C0 = -1
+// selects the generic kernel that walks the runtime stack.
+constexpr int GENERIC = -1;
 
 template <typename R>
 __device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F, R dx, R dy, R& ax,
@@ -55,82 +48,107 @@ __device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F,
     }
 }
 
-template <typename R>
-__device__ __forceinline__ R ray_flux(const GridDesc& g, const StackDesc& st, const R* srec,
-                                      const R* scoef, int recw, int I, int J, int flags) {
-    RayCtx<R> c;
-    if (sizeof(R) == 8) {
-        c.X = g.ra00 + (double)J * g.ax + (double)I * g.bx;
-        c.Y = g.dec00 + (double)J * g.ay + (double)I * g.by;
-    } else {
-        float fJ = (float)J, fI = (float)I;
-        c.px = fJ * g.ax_hi + fI * g.bx_hi;
-        c.lx = fJ * g.ax_lo + fI * g.bx_lo;
-        c.py = fJ * g.ay_hi + fI * g.by_hi;
-        c.ly = fJ * g.ay_lo + fI * g.by_lo;
-    }
-    R flux = 0;
-    const bool do_src = !(flags & LENSGB_NO_SOURCE) && st.n_src > 0;
-    if (do_src) {
-        R axs = 0, ays = 0;
-        for (int p = 0; p < st.n_lens; ++p) {
-            const R* rec = srec + p * recw;
-            R dx, dy, ax, ay;
-            ray_offset<R>(c, rec, dx, dy);
+// Offsets of the pixel's base ray (sub-ray 0, 0) from one profile centre.
+struct PixOff {
+    float bx, by;  // FP32 path: FP64-accurate offset of the base ray, rounded once
+};
+
+// FP32 base-ray offset of pixel (row, col) from the centre of record rec.
+__device__ __forceinline__ PixOff pix_offset_f(const GridDesc& g, const float* rec, float Jb,
+                                               float Ib) {
+    PixOff o;
+    o.bx = split_offset(rec[RF_X0H], rec[RF_X0L], Jb * g.ax_hi + Ib * g.bx_hi,
+                        Jb * g.ax_lo + Ib * g.bx_lo);
+    o.by = split_offset(rec[RF_Y0H], rec[RF_Y0L], Jb * g.ay_hi + Ib * g.by_hi,
+                        Jb * g.ay_lo + Ib * g.by_lo);
+    return o;
+}
+
+// Compile-time profile count helpers
+template <int C0, int C1>
+struct LensStackT {
+    static constexpr bool generic = (C0 == GENERIC);
+    static constexpr int n = generic ? 0 : ((C0 > 0) + (C1 > 0));
+    __host__ __device__ static constexpr int code(int i) { return i == 0 ? C0 : C1; }
+};
+
+// FP64 flux of one supersampled ray (I, J): the FP64 path and the refine pass.
+template <int C0, int C1, int NS, int NLL>
+__device__ __forceinline__ double ray_flux_d(const GridDesc& g, const StackDesc& st,
+                                             const double* srec, const double* scoef, int I,
+                                             int J, int flags) {
+    using LS = LensStackT<C0, C1>;
+    const double X = g.ra00 + (double)J * g.ax + (double)I * g.bx;
+    const double Y = g.dec00 + (double)J * g.ay + (double)I * g.by;
+    const int n_lens = LS::generic ? st.n_lens : LS::n;
+    const int n_src = NS >= 0 ? NS : st.n_src;
+    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
+    double flux = 0;
+    if (!(flags & LENSGB_NO_SOURCE) && n_src > 0) {
+        double axs = 0, ays = 0;
+#pragma unroll
+        for (int p = 0; p < (LS::generic ? MAX_PROF : LS::n); ++p) {
+            if (p >= n_lens) break;
+            const double* rec = srec + p * REC_D;
+            const int code = LS::generic ? st.lens[p] : LS::code(p);
             const int es = st.epl_slot[p];
-            lens_deflect<R>(st.lens[p], rec, es >= 0 ? scoef + es * EPL_NMAX : nullptr, dx, dy, ax,
-                            ay);
+            double ax, ay;
+            lens_deflect<double>(code, rec, es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                                 X - rec[RD_CX], Y - rec[RD_CY], ax, ay);
             axs += ax;
             ays += ay;
         }
-        axs *= (R)st.alpha_scaling;
-        ays *= (R)st.alpha_scaling;
-        R fs = 0;
-        for (int k = 0; k < st.n_src; ++k) {
-            const R* rec = srec + (st.n_lens + k) * recw;
-            const R sc = (R)st.src_scale[k];
-            R dx, dy;
-            if (sizeof(R) == 8) {
-                // beta = theta - scale * alpha, then the profile shift
-                double bxv = c.X - (double)(sc * axs);
-                double byv = c.Y - (double)(sc * ays);
-                dx = (R)(bxv - (double)rec[RD_CX]);
-                dy = (R)(byv - (double)rec[RD_CY]);
-            } else {
-                ray_offset<R>(c, rec, dx, dy);
-                dx -= sc * axs;
-                dy -= sc * ays;
-            }
-            fs += sersic_flux<R>(rec, dx, dy);
+        axs *= st.alpha_scaling;
+        ays *= st.alpha_scaling;
+        double fs = 0;
+#pragma unroll
+        for (int k = 0; k < (NS >= 0 ? NS : MAX_PROF); ++k) {
+            if (k >= n_src) break;
+            const double* rec = srec + (n_lens + k) * REC_D;
+            const double sc = st.src_scale[k];
+            // beta = theta - scale * alpha, then the profile shift
+            const double bxv = X - sc * axs, byv = Y - sc * ays;
+            fs += sersic_flux<double>(rec, bxv - rec[RD_CX], byv - rec[RD_CY]);
         }
         flux += fs;
     }
     if (!(flags & LENSGB_NO_LENS_LIGHT)) {
-        R fl = 0;
-        for (int k = 0; k < st.n_ll; ++k) {
-            const R* rec = srec + (st.n_lens + st.n_src + k) * recw;
-            R dx, dy;
-            ray_offset<R>(c, rec, dx, dy);
-            fl += sersic_flux<R>(rec, dx, dy);
+        double fl = 0;
+#pragma unroll
+        for (int k = 0; k < (NLL >= 0 ? NLL : MAX_PROF); ++k) {
+            if (k >= n_ll) break;
+            const double* rec = srec + (n_lens + n_src + k) * REC_D;
+            fl += sersic_flux<double>(rec, X - rec[RD_CX], Y - rec[RD_CY]);
         }
         flux += fl;
     }
-    return flux * (R)st.flux_scaling;
+    return flux * st.flux_scaling;
 }
 
+// FP64 value of pixel (row, col): mean over sub-columns then sub-rows
+// (image_util.py:93), times out_scale.
+template <int C0, int C1, int NS, int NLL>
+__device__ __forceinline__ double pixel_value_d(const GridDesc& g, const StackDesc& st,
+                                                const double* srec, const double* scoef, int row,
+                                                int col, int flags, double out_scale) {
+    const int s = g.s;
+    double acc = 0;
+    for (int si = 0; si < s; ++si) {
+        double rs = 0;
+        for (int sj = 0; sj < s; ++sj)
+            rs += ray_flux_d<C0, C1, NS, NLL>(g, st, srec, scoef, row * s + si, col * s + sj, flags);
+        acc += s == 1 ? rs : rs / (double)s;
+    }
+    if (s > 1) acc = acc / (double)s;
+    return acc * out_scale;
+}
+
+// Load the CTA's system records (and EPL tables) into shared memory.
 template <typename R>
-__global__ void __launch_bounds__(256)
-raytrace_kernel(GridDesc g, StackDesc st, int P, const R* __restrict__ rec, const R* __restrict__ coef,
-                R* __restrict__ out, int flags, double out_scale) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void load_records(const StackDesc& st, const R* rec, const R* coef,
+                                             int inst, R* srec, R* scoef) {
     const int recw = sizeof(R) == 8 ? REC_D : REC_F;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const int inst = blockIdx.y;
-    const int s = g.s, s2 = s * s;
-    R* srec = (R*)smem_raw;
-    R* scoef = srec + n_prof * recw;
-    R* sbuf = scoef + st.n_epl * EPL_NMAX;
-
     const R* grec = rec + (long long)inst * n_prof * recw;
     for (int k = threadIdx.x; k < n_prof * recw; k += blockDim.x) srec[k] = grec[k];
     __syncthreads();
@@ -142,82 +160,257 @@ raytrace_kernel(GridDesc g, StackDesc st, int P, const R* __restrict__ rec, cons
         for (int k = threadIdx.x; k < nmax; k += blockDim.x) scoef[es * EPL_NMAX + k] = gc[k];
     }
     __syncthreads();
+}
 
+// ---------------------------------------------------------------------------
+// FP64 kernel
+// ---------------------------------------------------------------------------
+template <int C0, int C1, int NS, int NLL>
+__global__ void __launch_bounds__(256)
+raytrace_fp64_kernel(GridDesc g, StackDesc st, int ppt, const double* __restrict__ rec,
+                     const double* __restrict__ coef, double* __restrict__ out, int flags,
+                     double out_scale) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    double* srec = (double*)smem_raw;
+    double* scoef = srec + n_prof * REC_D;
+    const int inst = blockIdx.y;
+    load_records<double>(st, rec, coef, inst, srec, scoef);
     const long long npix = (long long)g.nx * g.ny;
-    const long long pix0 = (long long)blockIdx.x * P;
-    const int nray = P * s2;
-    for (int r = threadIdx.x; r < nray; r += blockDim.x) {
-        const int p = r / s2, sub = r - p * s2;
-        const long long pix = pix0 + p;
-        R v = 0;
-        if (pix < npix) {
-            const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
-            const int si = sub / s, sj = sub - si * s;
-            v = ray_flux<R>(g, st, srec, scoef, recw, row * s + si, col * s + sj, flags);
-        }
-        sbuf[r] = v;
-    }
-    __syncthreads();
-    R* o = out + (long long)inst * npix;
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        const long long pix = pix0 + p;
+    double* o = out + (long long)inst * npix;
+    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
+    for (int k = 0; k < ppt; ++k) {
+        const long long pix = base + (long long)k * blockDim.x + threadIdx.x;
         if (pix >= npix) break;
-        const R* b = sbuf + p * s2;
-        R acc = 0;
-        if (s == 1) {
-            acc = b[0];
-        } else {
-            // mean over sub-columns, then over sub-rows (image_util.py:93)
-            for (int si = 0; si < s; ++si) {
-                R rs = 0;
-                for (int sj = 0; sj < s; ++sj) rs += b[si * s + sj];
-                acc += rs / (R)s;
-            }
-            acc = acc / (R)s;
-        }
-        o[pix] = acc * (R)out_scale;
+        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        o[pix] = pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, out_scale);
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 kernel (pass 1)
+// ---------------------------------------------------------------------------
+template <int C0, int C1, int NS, int NLL>
+__global__ void __launch_bounds__(256)
+raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict__ rec,
+                     const float* __restrict__ coef, float* __restrict__ out, int flags,
+                     float out_scale, RefineArgs rf) {
+    using LS = LensStackT<C0, C1>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    float* srec = (float*)smem_raw;
+    float* scoef = srec + n_prof * REC_F;
+    const int inst = blockIdx.y;
+    load_records<float>(st, rec, coef, inst, srec, scoef);
+
+    const int n_lens = LS::generic ? st.n_lens : LS::n;
+    const int n_src = NS >= 0 ? NS : st.n_src;
+    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
+    constexpr int ML = LS::generic ? MAX_PROF : (LS::n > 0 ? LS::n : 1);
+    constexpr int MS = NS >= 0 ? (NS > 0 ? NS : 1) : MAX_PROF;
+    constexpr int MLL = NLL >= 0 ? (NLL > 0 ? NLL : 1) : MAX_PROF;
+    const bool do_src = !(flags & LENSGB_NO_SOURCE) && n_src > 0;
+    const bool do_ll = !(flags & LENSGB_NO_LENS_LIGHT) && n_ll > 0;
+    const bool refine = rf.tau > 0.f && do_src;
+    const int s = g.s;
+    const float inv_s = 1.f / (float)s;
+    const long long npix = (long long)g.nx * g.ny;
+    float* o = out + (long long)inst * npix;
+    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
+
+    for (int kk = 0; kk < ppt; ++kk) {
+        const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
+        if (pix >= npix) break;
+        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        const float Jb = (float)(col * s), Ib = (float)(row * s);
+        // base-ray offsets from every profile centre, FP64-accurate
+        PixOff ol[ML], os[MS], oll[MLL];
+#pragma unroll
+        for (int p = 0; p < ML; ++p)
+            if (p < n_lens && do_src) ol[p] = pix_offset_f(g, srec + p * REC_F, Jb, Ib);
+#pragma unroll
+        for (int k = 0; k < MS; ++k)
+            if (k < n_src && do_src) os[k] = pix_offset_f(g, srec + (n_lens + k) * REC_F, Jb, Ib);
+#pragma unroll
+        for (int k = 0; k < MLL; ++k)
+            if (k < n_ll && do_ll)
+                oll[k] = pix_offset_f(g, srec + (n_lens + n_src + k) * REC_F, Jb, Ib);
+
+        float acc = 0.f;
+        bool flag = false;
+        for (int si = 0; si < s; ++si) {
+            float rs = 0.f;
+            for (int sj = 0; sj < s; ++sj) {
+                // sub-ray displacement from the base ray (small: rounding once keeps
+                // FP64-level absolute accuracy)
+                const float fj = (float)sj, fi = (float)si;
+                const float ddx = fj * g.ax_hi + fi * g.bx_hi + (fj * g.ax_lo + fi * g.bx_lo);
+                const float ddy = fj * g.ay_hi + fi * g.by_hi + (fj * g.ay_lo + fi * g.by_lo);
+                float flux = 0.f;
+                if (do_src) {
+                    float axs = 0.f, ays = 0.f;
+#pragma unroll
+                    for (int p = 0; p < ML; ++p) {
+                        if (p >= n_lens) break;
+                        const float* r = srec + p * REC_F;
+                        const int code = LS::generic ? st.lens[p] : LS::code(p);
+                        const int es = st.epl_slot[p];
+                        float ax, ay;
+                        lens_deflect<float>(code, r, es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                                            ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
+                        axs += ax;
+                        ays += ay;
+                    }
+                    axs *= st.alpha_scaling_f;
+                    ays *= st.alpha_scaling_f;
+                    float fsrc = 0.f, gsum = 0.f;
+#pragma unroll
+                    for (int k = 0; k < MS; ++k) {
+                        if (k >= n_src) break;
+                        const float* r = srec + (n_lens + k) * REC_F;
+                        const float sc = st.src_scale_f[k];
+                        float gk;
+                        const float fk = sersic_flux_grad(r, os[k].bx + ddx - sc * axs,
+                                                          os[k].by + ddy - sc * ays, gk);
+                        fsrc += fk;
+                        gsum += fk * gk * sc;
+                    }
+                    flux = fsrc;
+                    if (do_ll) {
+#pragma unroll
+                        for (int k = 0; k < MLL; ++k) {
+                            if (k >= n_ll) break;
+                            const float* r = srec + (n_lens + n_src + k) * REC_F;
+                            flux += sersic_flux<float>(r, oll[k].bx + ddx, oll[k].by + ddy);
+                        }
+                    }
+                    if (refine) {
+                        // predicted relative error of this ray's flux from the FP32
+                        // error of beta (kappa * |alpha|) through the source gradients
+                        const float dbeta = rf.kappa * (fabsf(axs) + fabsf(ays));
+                        flag |= gsum * dbeta > rf.tau * flux;
+                    }
+                } else if (do_ll) {
+#pragma unroll
+                    for (int k = 0; k < MLL; ++k) {
+                        if (k >= n_ll) break;
+                        const float* r = srec + (n_lens + n_src + k) * REC_F;
+                        flux += sersic_flux<float>(r, oll[k].bx + ddx, oll[k].by + ddy);
+                    }
+                }
+                rs += flux;
+            }
+            acc += s == 1 ? rs : rs * inv_s;
+        }
+        if (s > 1) acc *= inv_s;
+        o[pix] = acc * st.flux_scaling_f * out_scale;
+        if (flag) {
+            const unsigned int slot_i = atomicAdd(rf.count, 1u);
+            rf.list[slot_i] = (unsigned int)((long long)inst * npix + pix);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Refine pass: recompute the listed pixels in FP64 (records read from global
+// memory, one thread per listed pixel).
+// ---------------------------------------------------------------------------
+template <int C0, int C1, int NS, int NLL>
+__global__ void __launch_bounds__(128)
+refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
+              const double* __restrict__ coef, float* __restrict__ out, int flags,
+              double out_scale, RefineArgs rf) {
+    const unsigned int n = *rf.count;
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    const long long npix = (long long)g.nx * g.ny;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const long long e = (long long)rf.list[i];
+        const int inst = (int)(e / npix);
+        const long long pix = e - (long long)inst * npix;
+        const double* srec = rec + (long long)inst * n_prof * REC_D;
+        const double* scoef = coef + (long long)inst * st.n_epl * EPL_NMAX;
+        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        const double v =
+            pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, out_scale);
+        out[(long long)inst * npix + pix] = (float)v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
 static int g_num_sms = 0;
 
-int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
-                    const float* rec_f, const double* coef_d, const float* coef_f, void* out,
-                    int flags, double out_scale, int precision, cudaStream_t stream) {
+static int num_sms() {
     if (g_num_sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_num_sms <= 0) g_num_sms = 152;
     }
+    return g_num_sms;
+}
+
+template <int C0, int C1, int NS, int NLL>
+static void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
+                           const float* rec_f, const double* coef_d, const float* coef_f,
+                           void* out, int flags, double out_scale, int precision,
+                           const RefineArgs& rf, cudaStream_t stream) {
     const int threads = 256;
-    const int s2 = g.s * g.s;
     const long long npix = (long long)g.nx * g.ny;
-    // rays per thread: enough CTAs to fill the GPU several times, at most 9
-    long long rays = npix * s2 * (long long)n_inst;
-    long long target = (long long)g_num_sms * 8 * threads;
-    int rpt = (int)((rays + target - 1) / target);
-    rpt = rpt < 1 ? 1 : (rpt > 9 ? 9 : rpt);
-    int P = (rpt * threads) / s2;
-    if (P < 1) P = 1;
+    // pixels per thread: enough CTAs to fill the GPU several times over
+    long long target = (long long)num_sms() * 8 * threads;
+    long long total = npix * (long long)n_inst;
+    int ppt = (int)((total + target - 1) / target);
+    ppt = ppt < 1 ? 1 : (ppt > 8 ? 8 : ppt);
+    const long long per_cta = (long long)threads * ppt;
+    dim3 grid((unsigned)((npix + per_cta - 1) / per_cta), (unsigned)n_inst);
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const int esz = precision == LENSGB_FP64 ? 8 : 4;
-    const int recw = precision == LENSGB_FP64 ? REC_D : REC_F;
-    size_t smem = (size_t)(n_prof * recw + st.n_epl * EPL_NMAX + P * s2) * esz;
-    dim3 grid((unsigned)((npix + P - 1) / P), (unsigned)n_inst);
     if (precision == LENSGB_FP64) {
+        size_t smem = (size_t)(n_prof * REC_D + st.n_epl * EPL_NMAX) * sizeof(double);
         if (smem > 48 * 1024)
-            cudaFuncSetAttribute(raytrace_kernel<double>,
+            cudaFuncSetAttribute(raytrace_fp64_kernel<C0, C1, NS, NLL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        raytrace_kernel<double><<<grid, threads, smem, stream>>>(g, st, P, rec_d, coef_d,
-                                                                 (double*)out, flags, out_scale);
+        raytrace_fp64_kernel<C0, C1, NS, NLL><<<grid, threads, smem, stream>>>(
+            g, st, ppt, rec_d, coef_d, (double*)out, flags, out_scale);
     } else {
+        size_t smem = (size_t)(n_prof * REC_F + st.n_epl * EPL_NMAX) * sizeof(float);
         if (smem > 48 * 1024)
-            cudaFuncSetAttribute(raytrace_kernel<float>,
+            cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        raytrace_kernel<float><<<grid, threads, smem, stream>>>(g, st, P, rec_f, coef_f,
-                                                                (float*)out, flags, out_scale);
+        raytrace_fp32_kernel<C0, C1, NS, NLL><<<grid, threads, smem, stream>>>(
+            g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf);
+        if (rf.tau > 0.f && !(flags & LENSGB_NO_SOURCE) && st.n_src > 0) {
+            const int rblocks = num_sms() * 4;
+            refine_kernel<C0, C1, NS, NLL><<<rblocks, 128, 0, stream>>>(
+                g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf);
+        }
     }
+}
+
+int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
+                    const float* rec_f, const double* coef_d, const float* coef_f, void* out,
+                    int flags, double out_scale, int precision, const RefineArgs& rf,
+                    cudaStream_t stream) {
+    const bool one_light = st.n_ll <= 1;
+    const int a = st.n_lens == 2 ? st.lens[0] : 0, b = st.n_lens == 2 ? st.lens[1] : 0;
+#define LENSGB_VARIANT(C0, C1, NS, NLL)                                                        \
+    launch_variant<C0, C1, NS, NLL>(g, st, n_inst, rec_d, rec_f, coef_d, coef_f, out, flags, \
+                                    out_scale, precision, rf, stream)
+    if (one_light && st.n_src >= 1 && st.n_src <= 2 && b == LENSGB_LENS_SHEAR) {
+        if (a == LENSGB_LENS_EPL) {
+            if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 1); return 0; }
+            if (st.n_src == 2 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 2, 1); return 0; }
+            if (st.n_src == 1 && st.n_ll == 0) { LENSGB_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 0); return 0; }
+        }
+        if (a == LENSGB_LENS_SIE) {
+            if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 1, 1); return 0; }
+            if (st.n_src == 2 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 2, 1); return 0; }
+        }
+    }
+    LENSGB_VARIANT(GENERIC, 0, -1, -1);
+#undef LENSGB_VARIANT
     return 0;
 }
 

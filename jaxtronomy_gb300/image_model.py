@@ -31,7 +31,7 @@ _NUMERICS_KEYS = {
     "supersampling_factor", "compute_mode", "supersampling_convolution",
     "supersampling_kernel_size", "flux_evaluate_indexes", "supersampled_indexes",
     "compute_indexes", "point_source_supersampling_factor", "convolution_kernel_size",
-    "convolution_type", "truncation_conv", "precision",
+    "convolution_type", "truncation_conv", "precision", "fp32_refine_tol", "fp32_refine_kappa",
 }
 
 
@@ -84,6 +84,10 @@ class ImageModel:
             raise ValueError("precision must be 'fp64' or 'fp32'")
         self._precision = _lib.FP64 if precision == "fp64" else _lib.FP32_SPLIT
         self._dtype = torch.float64 if precision == "fp64" else torch.float32
+        # FP32 path: per-ray predicted relative error above which a pixel is
+        # recomputed in FP64 (<= 0 disables), and the FP32 deflection error bound
+        self._refine = (float(kn.pop("fp32_refine_tol", 2e-5)),
+                        float(kn.pop("fp32_refine_kappa", 3e-7)))
         # Numerics.__init__ checks (numerics.py:68-146)
         compute_mode = kn.get("compute_mode", "regular")
         if compute_mode != "regular":
@@ -188,8 +192,16 @@ class ImageModel:
     def _model(self, lens_idx, src_idx, ll_idx, lensed=True):
         key = (tuple(lens_idx), tuple(src_idx), tuple(ll_idx), lensed)
         if key not in self._models:
-            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed))
+            refine = self._refine if self._precision == _lib.FP32_SPLIT else None
+            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed), refine)
         return self._models[key]
+
+    def refined_pixels(self, stream=None):
+        """Pixels the last batched FP32 image call recomputed in FP64 (synchronizes)."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        return model.refined_pixels(_device.stream_handle(stream))
 
     def _kernel_tensor(self):
         if self._kernel_dev is None and self._kernel is not None:

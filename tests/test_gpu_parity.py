@@ -172,6 +172,34 @@ def test_flags_and_components(cuda, precision):
     np.testing.assert_allclose(src + ll, full, rtol=1e-4 if precision == "fp32" else 1e-12)
 
 
+def test_fp32_refinement_fixes_steep_source_cusp(cuda):
+    # system 207 of the 1024-system workload: an n=3.85, R_sersic=0.10" source whose
+    # centre images near the Einstein ring, where beta = theta - alpha cancels and
+    # the FP32 deflection error is amplified; the FP64 refine pass must bring the
+    # image within 1e-5 of FP64
+    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=208)
+    one = [W.subset(k, [207]) for k in (lens, src, ll)]
+    psf = kern[207]
+    g = W.grid_kwargs(180, 0.04)
+
+    def make(**kn):
+        data = J.ImageData(np.zeros((180, 180)), exposure_time=1000.0, background_rms=0.01, **g)
+        return J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=psf),
+                            J.LensModel(model["lens_model_list"]),
+                            J.LightModel(model["source_light_model_list"]),
+                            J.LightModel(model["lens_light_model_list"]),
+                            kwargs_numerics=dict(supersampling_factor=3, **kn))
+
+    ref = make(precision="fp64").image_batch(*one, psf_kernels=psf)[0].cpu().numpy()
+    off = make(precision="fp32", fp32_refine_tol=0.0)
+    on = make(precision="fp32")
+    e_off = rel_err(off.image_batch(*one, psf_kernels=psf)[0].double().cpu().numpy(), ref)[0]
+    e_on = rel_err(on.image_batch(*one, psf_kernels=psf)[0].double().cpu().numpy(), ref)[0]
+    assert on.refined_pixels() > 0
+    assert e_off > FP32_RTOL  # the case really is ill-conditioned in plain FP32
+    assert e_on < FP32_RTOL, (e_off, e_on)
+
+
 def test_batch_equals_single_bitwise_and_deterministic(cuda):
     model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=5, num_pix=40, kernel_size=11)
     for precision in ("fp64", "fp32"):

@@ -102,6 +102,21 @@ __host__ __device__ inline void split_double(double v, float& hi, float& lo) {
     lo = (float)(v - (double)hi);
 }
 
+// Hardware approximations (PTX lg2.approx / ex2.approx, flush-to-zero).  Used
+// only where their error (about 2^-22) is not amplified: the log2 of a radius
+// and the final exponential of a Sersic profile.
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // nan_to_num(posinf=1e10, neginf=-1e10), as used at epl.py:391-392
 template <typename R>
 __device__ __forceinline__ R nan_to_num_1e10(R v) {

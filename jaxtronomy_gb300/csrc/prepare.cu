@@ -92,6 +92,8 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
             d[RD_CY] = a[5];
             d[2] = b; d[3] = t; d[4] = q; d[5] = cos(phi); d[6] = sin(phi); d[7] = fq;
             d[8] = (double)nmax; d[9] = 2.0 / (1.0 + q) * pow(b, t);
+            // FP32-path constants: f^2/4, f/2, -t/2
+            d[12] = 0.25 * fq * fq; d[13] = 0.5 * fq; d[14] = -0.5 * t;
             int slot_e = st.epl_slot[p];
             double* Fd = coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
             float* Ff = coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
@@ -144,6 +146,8 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
         d[RD_CY] = cy;
         d[2] = amp; d[3] = Rs_; d[4] = 1.0 / Rs_; d[5] = 1.0 / n; d[6] = bn;
         d[7] = (1 - e1) / norm; d[8] = -e2 / norm; d[9] = -e2 / norm; d[10] = (1 + e1) / norm;
+        // FP32-path constants: log2(1/R_s), b_n log2(e), b_n / n
+        d[11] = log2(1.0 / Rs_); d[12] = bn * 1.4426950408889634; d[13] = bn / n;
     }
     for (int k = 2; k + F_OFF < REC_F && k < REC_D; ++k) f[k + F_OFF] = (float)d[k];
     write_offsets(g, d[RD_CX], d[RD_CY], f);

@@ -77,8 +77,70 @@ __device__ __forceinline__ void nie_deflect(const R* rec, R dx, R dy, R& ax, R& 
 // F holds the nmax coefficients F_n of the series
 //   2F1(1, t/2; 2 - t/2; z) = (1 - z/2)^-1 sum_n F_n w^n,  w = z / (z - 2)
 // (hyp2f1_util.py:135-176 with a = 1, where the Pochhammer prefactor is 1).
+// FP32 EPL.  With u = Z^2/|Z|^2 (|u| = 1) and z = -f u:
+//   |z - 2|^2 = 4 |1 - z/2|^2 = 4 (1 + f u_r + f^2/4),
+//   w = z/(z-2) = (f^2/4 + (f/2) u) / |1 - z/2|^2,
+//   2F1 = S(w) (1 + (f/2) conj(u)) / |1 - z/2|^2,
+// so one reciprocal serves both divisions, and (b/R)^t = b^t 2^(-t/2 log2 R^2)
+// needs no square root.  Record: f4 b, f5 t, f6 q, f7 cos, f8 sin, f9 f,
+// f10 nmax, f11 2/(1+q) b^t, f14 f^2/4, f15 f/2, f16 -t/2.
+__device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, float dx, float dy,
+                                              float& ax, float& ay) {
+    const float q = rec[6], c = rec[7], sn = rec[8];
+    const int nmax = (int)rec[10];
+    const float pref = rec[11], f2q = rec[14], fh = rec[15], mth = rec[16];
+    const float x = dx * c + dy * sn;
+    const float y = -dx * sn + dy * c;
+    const float za = q * x, zb = y;
+    const float r2 = za * za + zb * zb;
+    float hr = 1.f, hi = 0.f;
+    if (nmax > 0) {
+        if (r2 == 0.f) {  // reference: 0/0 at the centre -> NaN -> nan_to_num -> 0
+            ax = 0.f;
+            ay = 0.f;
+            return;
+        }
+        // u only sets the phase of z (|u| = 1): a 2-ulp reciprocal suffices
+        const float inv = __fdividef(1.f, r2);
+        const float ur = (za * za - zb * zb) * inv, ui = 2.f * za * zb * inv;
+        const float ee = 1.f / fmaf(2.f * fh, ur, 1.f + f2q);  // 1/|1 - z/2|^2
+        const float wr = fmaf(fh, ur, f2q) * ee, wi = fh * ui * ee;
+        float sr = F[nmax - 1], si = 0.f;
+        int n = nmax - 2;
+        if ((nmax & 1) == 0) {  // odd number of remaining terms: one step first
+            const float nr = fmaf(sr, wr, F[n]) - si * wi;
+            si = fmaf(sr, wi, si * wr);
+            sr = nr;
+            --n;
+        }
+        for (; n >= 1; n -= 2) {
+            // n is odd here, so (F[n-1], F[n]) is an aligned pair
+            const float2 fp = *reinterpret_cast<const float2*>(F + n - 1);
+            float nr = fmaf(sr, wr, fp.y) - si * wi;
+            float ni = fmaf(sr, wi, si * wr);
+            sr = fmaf(nr, wr, fp.x) - ni * wi;
+            si = fmaf(nr, wi, ni * wr);
+        }
+        // times (1 + (f/2) conj(u)) / |1 - z/2|^2
+        const float gr = fmaf(fh, ur, 1.f), gi = -fh * ui;
+        hr = (sr * gr - si * gi) * ee;
+        hi = (sr * gi + si * gr) * ee;
+    }
+    const float r2m = r2 > 1e-18f ? r2 : 1e-18f;  // R = max(|Z|, 1e-9)
+    const float amp = pref * exp2f(mth * log2f(r2m));
+    const float fx = amp * (za * hr - zb * hi);
+    const float fy = amp * (za * hi + zb * hr);
+    ax = fx * c - fy * sn;
+    ay = fx * sn + fy * c;
+}
+
 template <typename R>
 __device__ __forceinline__ void epl_deflect(const R* rec, const R* F, R dx, R dy, R& ax, R& ay) {
+    if (sizeof(R) == 4) {
+        epl_deflect_f((const float*)rec, (const float*)F, (float)dx, (float)dy, (float&)ax,
+                      (float&)ay);
+        return;
+    }
     const R t = rec[slot<R>(3)], q = rec[slot<R>(4)];
     const R c = rec[slot<R>(5)], sn = rec[slot<R>(6)], f = rec[slot<R>(7)];
     const int nmax = (int)rec[slot<R>(8)];
@@ -288,8 +350,15 @@ __device__ __forceinline__ void tnfw_deflect(const R* rec, R dx, R dy, R& ax, R&
 // ---------------------------------------------------------------------------
 // Sersic surface brightness (SERSIC and SERSIC_ELLIPSE share the record)
 // ---------------------------------------------------------------------------
+template <bool GRAD>
+__device__ __forceinline__ float sersic_f(const float* rec, float dx, float dy, float& g);
+
 template <typename R>
 __device__ __forceinline__ R sersic_flux(const R* rec, R dx, R dy) {
+    if (sizeof(R) == 4) {
+        float g;
+        return (R)sersic_f<false>((const float*)rec, (float)dx, (float)dy, g);
+    }
     const R amp = rec[slot<R>(2)], inv_rs = rec[slot<R>(4)];
     const R inv_n = rec[slot<R>(5)], bn = rec[slot<R>(6)];
     const R m00 = rec[slot<R>(7)], m01 = rec[slot<R>(8)], m10 = rec[slot<R>(9)],
@@ -312,25 +381,34 @@ __device__ __forceinline__ R sersic_flux(const R* rec, R dx, R dy) {
     return amp * nan_to_num_max(res);
 }
 
-// FP32 Sersic flux plus g = |d ln I / dR| = b_n (R/R_s)^(1/n) / (n R), the
-// log-gradient that turns an absolute position error into a relative flux
-// error (0 inside the 1e-4 smoothing floor, where the profile is flat).
-__device__ __forceinline__ float sersic_flux_grad(const float* rec, float dx, float dy, float& g) {
-    const float amp = rec[slot<float>(2)], inv_rs = rec[slot<float>(4)];
-    const float inv_n = rec[slot<float>(5)], bn = rec[slot<float>(6)];
-    const float m00 = rec[slot<float>(7)], m01 = rec[slot<float>(8)], m10 = rec[slot<float>(9)],
-                m11 = rec[slot<float>(10)];
+// FP32 Sersic without a square root: with r2 = R^2 floored at 1e-8 (R floored
+// at 1e-4),  log2(R/R_s) = log2(r2)/2 + log2(1/R_s),  v = (R/R_s)^(1/n),
+// I = amp 2^(b_n log2(e) (1 - v)), zero beyond R/R_s = 1000.  With `grad`, also
+// g = |d ln I / dR| = (b_n/n) v / R, the log-gradient that turns an absolute
+// position error into a relative flux error (0 inside the smoothing floor).
+// Record: f4 amp, f9..f12 transform, f13 log2(1/R_s), f14 b_n log2(e), f15 b_n/n.
+template <bool GRAD>
+__device__ __forceinline__ float sersic_f(const float* rec, float dx, float dy, float& g) {
+    const float amp = rec[4], inv_n = rec[7];
+    const float m00 = rec[9], m01 = rec[10], m10 = rec[11], m11 = rec[12];
+    const float l2irs = rec[13], bnl = rec[14];
     const float x = m00 * dx + m01 * dy;
     const float y = m10 * dx + m11 * dy;
-    const float Rr = sqrtf(x * x + y * y);
-    const bool floored = !(Rr > 0.0001f);
-    const float Rst = floored ? 0.0001f : Rr;
-    const float frac = Rst * inv_rs;
-    const float v = exp2f(inv_n * log2f(frac));
-    const float ex = -bn * (v - 1.f);
-    const float res = frac <= 1000.f ? expf(ex) : 0.f;
-    g = floored ? 0.f : bn * inv_n * v / Rst;
-    return amp * nan_to_num_max(res);
+    const float r2 = x * x + y * y;
+    const bool floored = !(r2 > 1e-8f);
+    const float r2m = floored ? 1e-8f : r2;
+    // log2(R/R_s): an absolute error of ~2^-22.6 here moves v by only ~4e-8/n
+    const float l2f = fmaf(0.5f, lg2_approx(r2m), l2irs);
+    // v is multiplied by b_n log2(e) (up to ~40) below, so it keeps the accurate exp2f
+    const float v = exp2f(inv_n * l2f);
+    // the argument's own FP32 rounding dominates this exponential's error
+    const float res = l2f <= 9.965784284662087f ? ex2_approx(bnl * (1.f - v)) : 0.f;
+    if (GRAD) g = floored ? 0.f : rec[15] * v * rsqrtf(r2m);
+    return amp * res;
+}
+
+__device__ __forceinline__ float sersic_flux_grad(const float* rec, float dx, float dy, float& g) {
+    return sersic_f<true>(rec, dx, dy, g);
 }
 
 }  // namespace lensgb

@@ -209,11 +209,24 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
     constexpr int ML = LS::generic ? MAX_PROF : (LS::n > 0 ? LS::n : 1);
     constexpr int MS = NS >= 0 ? (NS > 0 ? NS : 1) : MAX_PROF;
     constexpr int MLL = NLL >= 0 ? (NLL > 0 ? NLL : 1) : MAX_PROF;
+    // compile-time stacks keep every record in registers for the whole CTA
+    constexpr int NPC = LS::generic ? 1 : LS::n + MS + MLL;
+    float lr[NPC][REC_F];
+    if (!LS::generic) {
+#pragma unroll
+        for (int i = 0; i < NPC; ++i)
+#pragma unroll
+            for (int k = 0; k < REC_F; ++k)
+                lr[i][k] = i < n_prof ? srec[i * REC_F + k] : 0.f;
+    }
+#define REC(i) (LS::generic ? srec + (i) * REC_F : lr[(i)])
     const bool do_src = !(flags & LENSGB_NO_SOURCE) && n_src > 0;
     const bool do_ll = !(flags & LENSGB_NO_LENS_LIGHT) && n_ll > 0;
     const bool refine = rf.tau > 0.f && do_src;
     const int s = g.s;
     const float inv_s = 1.f / (float)s;
+    const float axf = g.ax_hi + g.ax_lo, bxf = g.bx_hi + g.bx_lo;
+    const float ayf = g.ay_hi + g.ay_lo, byf = g.by_hi + g.by_lo;
     const long long npix = (long long)g.nx * g.ny;
     float* o = out + (long long)inst * npix;
     const long long base = (long long)blockIdx.x * blockDim.x * ppt;
@@ -227,36 +240,35 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
         PixOff ol[ML], os[MS], oll[MLL];
 #pragma unroll
         for (int p = 0; p < ML; ++p)
-            if (p < n_lens && do_src) ol[p] = pix_offset_f(g, srec + p * REC_F, Jb, Ib);
+            if (p < n_lens && do_src) ol[p] = pix_offset_f(g, REC(p), Jb, Ib);
 #pragma unroll
         for (int k = 0; k < MS; ++k)
-            if (k < n_src && do_src) os[k] = pix_offset_f(g, srec + (n_lens + k) * REC_F, Jb, Ib);
+            if (k < n_src && do_src) os[k] = pix_offset_f(g, REC(n_lens + k), Jb, Ib);
 #pragma unroll
         for (int k = 0; k < MLL; ++k)
-            if (k < n_ll && do_ll)
-                oll[k] = pix_offset_f(g, srec + (n_lens + n_src + k) * REC_F, Jb, Ib);
+            if (k < n_ll && do_ll) oll[k] = pix_offset_f(g, REC(n_lens + n_src + k), Jb, Ib);
 
         float acc = 0.f;
         bool flag = false;
         for (int si = 0; si < s; ++si) {
             float rs = 0.f;
+            const float fi = (float)si;
             for (int sj = 0; sj < s; ++sj) {
-                // sub-ray displacement from the base ray (small: rounding once keeps
-                // FP64-level absolute accuracy)
-                const float fj = (float)sj, fi = (float)si;
-                const float ddx = fj * g.ax_hi + fi * g.bx_hi + (fj * g.ax_lo + fi * g.bx_lo);
-                const float ddy = fj * g.ay_hi + fi * g.by_hi + (fj * g.ay_lo + fi * g.by_lo);
+                // sub-ray displacement from the base ray: below one pixel, so a
+                // plain FP32 product keeps an absolute error of ~1e-9 pixel
+                const float fj = (float)sj;
+                const float ddx = fmaf(fi, bxf, fj * axf);
+                const float ddy = fmaf(fi, byf, fj * ayf);
                 float flux = 0.f;
                 if (do_src) {
                     float axs = 0.f, ays = 0.f;
 #pragma unroll
                     for (int p = 0; p < ML; ++p) {
                         if (p >= n_lens) break;
-                        const float* r = srec + p * REC_F;
                         const int code = LS::generic ? st.lens[p] : LS::code(p);
                         const int es = st.epl_slot[p];
                         float ax, ay;
-                        lens_deflect<float>(code, r, es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                        lens_deflect<float>(code, REC(p), es >= 0 ? scoef + es * EPL_NMAX : nullptr,
                                             ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
                         axs += ax;
                         ays += ay;
@@ -267,10 +279,9 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
 #pragma unroll
                     for (int k = 0; k < MS; ++k) {
                         if (k >= n_src) break;
-                        const float* r = srec + (n_lens + k) * REC_F;
                         const float sc = st.src_scale_f[k];
                         float gk;
-                        const float fk = sersic_flux_grad(r, os[k].bx + ddx - sc * axs,
+                        const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sc * axs,
                                                           os[k].by + ddy - sc * ays, gk);
                         fsrc += fk;
                         gsum += fk * gk * sc;
@@ -280,8 +291,8 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
 #pragma unroll
                         for (int k = 0; k < MLL; ++k) {
                             if (k >= n_ll) break;
-                            const float* r = srec + (n_lens + n_src + k) * REC_F;
-                            flux += sersic_flux<float>(r, oll[k].bx + ddx, oll[k].by + ddy);
+                            flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
+                                                       oll[k].by + ddy);
                         }
                     }
                     if (refine) {
@@ -294,8 +305,8 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
 #pragma unroll
                     for (int k = 0; k < MLL; ++k) {
                         if (k >= n_ll) break;
-                        const float* r = srec + (n_lens + n_src + k) * REC_F;
-                        flux += sersic_flux<float>(r, oll[k].bx + ddx, oll[k].by + ddy);
+                        flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
+                                                   oll[k].by + ddy);
                     }
                 }
                 rs += flux;
@@ -309,6 +320,7 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
             rf.list[slot_i] = (unsigned int)((long long)inst * npix + pix);
         }
     }
+#undef REC
 }
 
 // ---------------------------------------------------------------------------

@@ -177,7 +177,9 @@ def test_fp32_refinement_fixes_steep_source_cusp(cuda):
     # centre images near the Einstein ring, where beta = theta - alpha cancels and
     # the FP32 deflection error is amplified; the FP64 refine pass must bring the
     # image within 1e-5 of FP64
-    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=208)
+    # (the generator draws each parameter for the whole batch, so the batch size
+    # must be the workload's 1024 for system 207 to be the same system)
+    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=1024)
     one = [W.subset(k, [207]) for k in (lens, src, ll)]
     psf = kern[207]
     g = W.grid_kwargs(180, 0.04)

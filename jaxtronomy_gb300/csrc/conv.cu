@@ -95,6 +95,124 @@ conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__
     }
 }
 
+// FP32 variant: each thread owns 4 rows x 8 columns; input segments and kernel
+// rows come from shared memory as float4 (kernel rows zero-padded to KP, a
+// multiple of 8).  blockDim = (8, TY) with TY chosen per image height so that
+// the 4*TY-row tiles waste as few rows as possible.
+constexpr int C32_CX = 8, C32_RY = 4, C32_TX = 8, C32_W = C32_TX * C32_CX;
+
+__global__ void __launch_bounds__(C32_TX * 16)
+conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
+                const float* __restrict__ ker, long long kstride, int ny, int nx, int K, int edge) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int TY = blockDim.y;
+    const int H = TY * C32_RY;
+    const int KP = ((K + 7) / 8) * 8;
+    const int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
+    const int SH = H + K - 1;
+    float* sk = (float*)smem_raw;
+    float* si = sk + K * KP;
+    const int inst = blockIdx.z;
+    const int ox0 = blockIdx.x * C32_W, oy0 = blockIdx.y * H;
+    const int h = K / 2;
+    const int tid = threadIdx.y * C32_TX + threadIdx.x;
+    const int nthr = C32_TX * TY;
+    const float* kk = ker + (long long)inst * kstride;
+    for (int e = tid; e < K * KP; e += nthr) {
+        const int u = e / KP, v = e - u * KP;
+        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
+    }
+    const float* img = in + (long long)inst * ny * nx;
+    for (int e = tid; e < SH * SW; e += nthr) {
+        const int r = e / SW, c = e - r * SW;
+        int gy = oy0 - h + r, gx = ox0 - h + c;
+        float v;
+        if (edge) {
+            gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+            gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+            v = img[(long long)gy * nx + gx];
+        } else {
+            v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : 0.f;
+        }
+        si[e] = v;
+    }
+    __syncthreads();
+
+    float acc[C32_RY][C32_CX];
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i)
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
+    const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
+    for (int ir = 0; ir < C32_RY + K - 1; ++ir) {
+        const float4* row = reinterpret_cast<const float4*>(si + (r0 + ir) * SW + c0);
+        for (int v0 = 0; v0 < KP; v0 += 8) {
+            float seg[16];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 q = row[v0 / 4 + j];
+                seg[4 * j] = q.x;
+                seg[4 * j + 1] = q.y;
+                seg[4 * j + 2] = q.z;
+                seg[4 * j + 3] = q.w;
+            }
+#pragma unroll
+            for (int i = 0; i < C32_RY; ++i) {
+                const int u = ir - i;
+                if (u < 0 || u >= K) continue;
+                const float4* kr = reinterpret_cast<const float4*>(sk + u * KP + v0);
+                const float4 k0 = kr[0], k1 = kr[1];
+                const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+#pragma unroll
+                for (int vv = 0; vv < 8; ++vv)
+#pragma unroll
+                    for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+            }
+        }
+    }
+    float* o = out + (long long)inst * ny * nx;
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i) {
+        const int y = oy0 + r0 + i;
+        if (y >= ny) continue;
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) {
+            const int x = ox0 + c0 + c;
+            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+        }
+    }
+}
+
+static int run_conv_f32(const void* in, void* out, const void* kernel, long long kstride,
+                        int n_inst, int ny, int nx, int K, int edge, cudaStream_t stream) {
+    // tile height 4*TY with TY in 8..16: fewest padded rows, then the tallest tile
+    int best_ty = 16;
+    long long best_waste = -1;
+    for (int ty = 16; ty >= 8; --ty) {
+        const int H = 4 * ty;
+        const long long waste = (long long)((ny + H - 1) / H) * H - ny;
+        if (best_waste < 0 || waste < best_waste) {
+            best_waste = waste;
+            best_ty = ty;
+        }
+    }
+    const int H = 4 * best_ty;
+    const int KP = ((K + 7) / 8) * 8;
+    const int SW = C32_W + KP + 4;
+    const int SH = H + K - 1;
+    const size_t smem = (size_t)(K * KP + SH * SW) * sizeof(float);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(conv_f32_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return -1;
+    }
+    dim3 grid((unsigned)((nx + C32_W - 1) / C32_W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
+    dim3 block(C32_TX, best_ty);
+    conv_f32_kernel<<<grid, block, smem, stream>>>((const float*)in, (float*)out,
+                                                   (const float*)kernel, kstride, ny, nx, K, edge);
+    return 0;
+}
+
 template <typename R, int CX, int RY, int VC>
 static int run_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
                     int ny, int nx, int K, int edge, cudaStream_t stream) {
@@ -119,7 +237,7 @@ int launch_conv(const void* in, void* out, const void* kernel, long long kstride
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream) {
     if (precision == LENSGB_FP64)
         return run_conv<double, 4, 4, 4>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
-    return run_conv<float, 8, 4, 8>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
+    return run_conv_f32(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
 }
 
 }  // namespace lensgb

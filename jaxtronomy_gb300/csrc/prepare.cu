@@ -109,6 +109,21 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
                 fpp = fp;
                 fp = fn;
             }
+            // FP32 series length: since |w| <= f/(2-f), the terms n >= k change the
+            // sum by at most sum_{m>=k} |F_m| (f/(2-f))^m; stop once that bound is
+            // below 2^-27 (under FP32 resolution), never beyond the reference's nmax.
+            int n32 = nmax;
+            if (nmax > 1) {
+                const double wmax = fq / (2.0 - fq);
+                double tail = 0.0, wp = pow(wmax, (double)(nmax - 1));
+                for (int m = nmax - 1; m >= 1; --m) {
+                    tail += fabs(Fd[m]) * wp;
+                    if (tail > 7.450580596923828e-09) break;
+                    n32 = m;
+                    wp /= wmax;
+                }
+            }
+            d[15] = (double)n32;
         } else if (code == LENSGB_LENS_SHEAR) {
             d[RD_CX] = a[2];
             d[RD_CY] = a[3];

@@ -87,7 +87,9 @@ __device__ __forceinline__ void nie_deflect(const R* rec, R dx, R dy, R& ax, R& 
 __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, float dx, float dy,
                                               float& ax, float& ay) {
     const float q = rec[6], c = rec[7], sn = rec[8];
-    const int nmax = (int)rec[10];
+    // FP32 series length (f17): the reference's nmax shortened to where the
+    // remaining terms fall below FP32 resolution (set by the prepare kernel)
+    const int nmax = (int)rec[17];
     const float pref = rec[11], f2q = rec[14], fh = rec[15], mth = rec[16];
     const float x = dx * c + dy * sn;
     const float y = -dx * sn + dy * c;

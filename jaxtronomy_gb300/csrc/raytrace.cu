@@ -1,405 +1,11 @@
-// Fused ray-tracing kernels: for every supersampled ray of every system,
-// deflection sum -> lensed source light -> lens light, then the s x s block
-// mean into the (ny, nx) pixel image.  The ray grid exists only in registers;
-// the image leaves the kernel already multiplied by pixel_width^2 and
-// flux_scaling.
-//
-// Mapping: blockIdx.y = system; each thread owns the s^2 supersampled rays of
-// one pixel at a time (pixels of a CTA are consecutive in row-major order, so
-// a warp covers 32 neighbouring pixels of a row and stays spatially coherent).
-// Profile records of the CTA's system sit in shared memory.
-//
-// FP32 path ("FP32 split"): the bulk arithmetic is FP32.  Coordinate offsets
-// from every profile centre are formed with FP64 accuracy (split_offset), and
-// each sub-ray predicts the relative error its FP32 deflection causes in the
-// source light (Sersic log-gradient x the FP32 error bound of beta = theta -
-// alpha, weighted by the source's share of the ray's flux).  Pixels where the
-// prediction exceeds `tau` -- rays landing close to a steep source centre,
-// where the lens equation cancels theta against alpha -- are appended to a
-// list that refine_kernel recomputes in FP64 with the code of the FP64 path.
-//
-// Reference path (JAXtronomy source tree):
-//   ray grid          ImSim/Numerics/grid.py:48-72 (lenstronomy make_subgrid)
-//   deflection sum    LensModel/single_plane.py:39-56,113-139
-//   source mapping    ImSim/image_model.py:347-354 (lenstronomy Image2SourceMapping)
-//   light sum         LightModel/light_model_base.py:230-252
-//   re-binning        ImSim/Numerics/grid.py:102-117, Util/image_util.py:79-98
-//   pixel area        ImSim/Numerics/numerics.py:177
-#include "launch.h"
-#include "profiles.cuh"
+// Dispatch of the ray-tracing kernels (raytrace_kernels.cuh) to the profile
+// stack of a model.  Common stacks run compile-time specialisations (their
+// instantiations live in raytrace_epl.cu and raytrace_sie.cu so the build
+// compiles them in parallel); every other stack runs the generic kernel
+// (raytrace_generic.cu).
+#include "raytrace_variants.h"
 
 namespace lensgb {
-
-// Lens-stack selector: C0/C1 are compile-time lens codes (0 = absent); C0 = -1
-// selects the generic kernel that walks the runtime stack.
-constexpr int GENERIC = -1;
-
-template <typename R>
-__device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F, R dx, R dy, R& ax,
-                                             R& ay) {
-    switch (code) {
-        case LENSGB_LENS_SIE:
-        case LENSGB_LENS_NIE: nie_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_EPL: epl_deflect<R>(rec, F, dx, dy, ax, ay); break;
-        case LENSGB_LENS_SHEAR: shear_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_NFW: nfw_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_TNFW: tnfw_deflect<R>(rec, dx, dy, ax, ay); break;
-        default: ax = 0; ay = 0; break;
-    }
-}
-
-// Offsets of the pixel's base ray (sub-ray 0, 0) from one profile centre.
-struct PixOff {
-    float bx, by;  // FP32 path: FP64-accurate offset of the base ray, rounded once
-};
-
-// FP32 base-ray offset of pixel (row, col) from the centre of record rec.
-__device__ __forceinline__ PixOff pix_offset_f(const GridDesc& g, const float* rec, float Jb,
-                                               float Ib) {
-    PixOff o;
-    o.bx = split_offset(rec[RF_X0H], rec[RF_X0L], Jb * g.ax_hi + Ib * g.bx_hi,
-                        Jb * g.ax_lo + Ib * g.bx_lo);
-    o.by = split_offset(rec[RF_Y0H], rec[RF_Y0L], Jb * g.ay_hi + Ib * g.by_hi,
-                        Jb * g.ay_lo + Ib * g.by_lo);
-    return o;
-}
-
-// Compile-time profile count helpers
-template <int C0, int C1>
-struct LensStackT {
-    static constexpr bool generic = (C0 == GENERIC);
-    static constexpr int n = generic ? 0 : ((C0 > 0) + (C1 > 0));
-    __host__ __device__ static constexpr int code(int i) { return i == 0 ? C0 : C1; }
-};
-
-// FP64 flux of one supersampled ray (I, J): the FP64 path and the refine pass.
-template <int C0, int C1, int NS, int NLL>
-__device__ __forceinline__ double ray_flux_d(const GridDesc& g, const StackDesc& st,
-                                             const double* srec, const double* scoef, int I,
-                                             int J, int flags) {
-    using LS = LensStackT<C0, C1>;
-    const double X = g.ra00 + (double)J * g.ax + (double)I * g.bx;
-    const double Y = g.dec00 + (double)J * g.ay + (double)I * g.by;
-    const int n_lens = LS::generic ? st.n_lens : LS::n;
-    const int n_src = NS >= 0 ? NS : st.n_src;
-    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
-    double flux = 0;
-    if (!(flags & LENSGB_NO_SOURCE) && n_src > 0) {
-        double axs = 0, ays = 0;
-#pragma unroll
-        for (int p = 0; p < (LS::generic ? MAX_PROF : LS::n); ++p) {
-            if (p >= n_lens) break;
-            const double* rec = srec + p * REC_D;
-            const int code = LS::generic ? st.lens[p] : LS::code(p);
-            const int es = st.epl_slot[p];
-            double ax, ay;
-            lens_deflect<double>(code, rec, es >= 0 ? scoef + es * EPL_NMAX : nullptr,
-                                 X - rec[RD_CX], Y - rec[RD_CY], ax, ay);
-            axs += ax;
-            ays += ay;
-        }
-        axs *= st.alpha_scaling;
-        ays *= st.alpha_scaling;
-        double fs = 0;
-#pragma unroll
-        for (int k = 0; k < (NS >= 0 ? NS : MAX_PROF); ++k) {
-            if (k >= n_src) break;
-            const double* rec = srec + (n_lens + k) * REC_D;
-            const double sc = st.src_scale[k];
-            // beta = theta - scale * alpha, then the profile shift
-            const double bxv = X - sc * axs, byv = Y - sc * ays;
-            fs += sersic_flux<double>(rec, bxv - rec[RD_CX], byv - rec[RD_CY]);
-        }
-        flux += fs;
-    }
-    if (!(flags & LENSGB_NO_LENS_LIGHT)) {
-        double fl = 0;
-#pragma unroll
-        for (int k = 0; k < (NLL >= 0 ? NLL : MAX_PROF); ++k) {
-            if (k >= n_ll) break;
-            const double* rec = srec + (n_lens + n_src + k) * REC_D;
-            fl += sersic_flux<double>(rec, X - rec[RD_CX], Y - rec[RD_CY]);
-        }
-        flux += fl;
-    }
-    return flux * st.flux_scaling;
-}
-
-// FP64 value of pixel (row, col): mean over sub-columns then sub-rows
-// (image_util.py:93), times out_scale.
-template <int C0, int C1, int NS, int NLL>
-__device__ __forceinline__ double pixel_value_d(const GridDesc& g, const StackDesc& st,
-                                                const double* srec, const double* scoef, int row,
-                                                int col, int flags, double out_scale) {
-    const int s = g.s;
-    double acc = 0;
-    for (int si = 0; si < s; ++si) {
-        double rs = 0;
-        for (int sj = 0; sj < s; ++sj)
-            rs += ray_flux_d<C0, C1, NS, NLL>(g, st, srec, scoef, row * s + si, col * s + sj, flags);
-        acc += s == 1 ? rs : rs / (double)s;
-    }
-    if (s > 1) acc = acc / (double)s;
-    return acc * out_scale;
-}
-
-// Load the CTA's system records (and EPL tables) into shared memory.
-template <typename R>
-__device__ __forceinline__ void load_records(const StackDesc& st, const R* rec, const R* coef,
-                                             int inst, R* srec, R* scoef) {
-    const int recw = sizeof(R) == 8 ? REC_D : REC_F;
-    const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const R* grec = rec + (long long)inst * n_prof * recw;
-    for (int k = threadIdx.x; k < n_prof * recw; k += blockDim.x) srec[k] = grec[k];
-    __syncthreads();
-    for (int p = 0; p < st.n_lens; ++p) {
-        const int es = st.epl_slot[p];
-        if (es < 0) continue;
-        const int nmax = (int)srec[p * recw + slot<R>(8)];
-        const R* gc = coef + ((long long)inst * st.n_epl + es) * EPL_NMAX;
-        for (int k = threadIdx.x; k < nmax; k += blockDim.x) scoef[es * EPL_NMAX + k] = gc[k];
-    }
-    __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// FP64 kernel
-// ---------------------------------------------------------------------------
-template <int C0, int C1, int NS, int NLL>
-__global__ void __launch_bounds__(256)
-raytrace_fp64_kernel(GridDesc g, StackDesc st, int ppt, const double* __restrict__ rec,
-                     const double* __restrict__ coef, double* __restrict__ out, int flags,
-                     double out_scale) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    double* srec = (double*)smem_raw;
-    double* scoef = srec + n_prof * REC_D;
-    const int inst = blockIdx.y;
-    load_records<double>(st, rec, coef, inst, srec, scoef);
-    const long long npix = (long long)g.nx * g.ny;
-    double* o = out + (long long)inst * npix;
-    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
-    for (int k = 0; k < ppt; ++k) {
-        const long long pix = base + (long long)k * blockDim.x + threadIdx.x;
-        if (pix >= npix) break;
-        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
-        o[pix] = pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, out_scale);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// FP32 kernel (pass 1)
-// ---------------------------------------------------------------------------
-template <int C0, int C1, int NS, int NLL>
-__global__ void __launch_bounds__(256)
-raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict__ rec,
-                     const float* __restrict__ coef, float* __restrict__ out, int flags,
-                     float out_scale, RefineArgs rf) {
-    using LS = LensStackT<C0, C1>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    float* srec = (float*)smem_raw;
-    float* scoef = srec + n_prof * REC_F;
-    const int inst = blockIdx.y;
-    load_records<float>(st, rec, coef, inst, srec, scoef);
-
-    const int n_lens = LS::generic ? st.n_lens : LS::n;
-    const int n_src = NS >= 0 ? NS : st.n_src;
-    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
-    constexpr int ML = LS::generic ? MAX_PROF : (LS::n > 0 ? LS::n : 1);
-    constexpr int MS = NS >= 0 ? (NS > 0 ? NS : 1) : MAX_PROF;
-    constexpr int MLL = NLL >= 0 ? (NLL > 0 ? NLL : 1) : MAX_PROF;
-    // compile-time stacks keep every record in registers for the whole CTA
-    constexpr int NPC = LS::generic ? 1 : LS::n + MS + MLL;
-    float lr[NPC][REC_F];
-    if (!LS::generic) {
-#pragma unroll
-        for (int i = 0; i < NPC; ++i)
-#pragma unroll
-            for (int k = 0; k < REC_F; ++k)
-                lr[i][k] = i < n_prof ? srec[i * REC_F + k] : 0.f;
-    }
-#define REC(i) (LS::generic ? srec + (i) * REC_F : lr[(i)])
-    const bool do_src = !(flags & LENSGB_NO_SOURCE) && n_src > 0;
-    const bool do_ll = !(flags & LENSGB_NO_LENS_LIGHT) && n_ll > 0;
-    const bool refine = rf.tau > 0.f && do_src;
-    const int s = g.s;
-    const float inv_s = 1.f / (float)s;
-    const float axf = g.ax_hi + g.ax_lo, bxf = g.bx_hi + g.bx_lo;
-    const float ayf = g.ay_hi + g.ay_lo, byf = g.by_hi + g.by_lo;
-    const long long npix = (long long)g.nx * g.ny;
-    float* o = out + (long long)inst * npix;
-    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
-
-    for (int kk = 0; kk < ppt; ++kk) {
-        const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
-        if (pix >= npix) break;
-        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
-        const float Jb = (float)(col * s), Ib = (float)(row * s);
-        // base-ray offsets from every profile centre, FP64-accurate
-        PixOff ol[ML], os[MS], oll[MLL];
-#pragma unroll
-        for (int p = 0; p < ML; ++p)
-            if (p < n_lens && do_src) ol[p] = pix_offset_f(g, REC(p), Jb, Ib);
-#pragma unroll
-        for (int k = 0; k < MS; ++k)
-            if (k < n_src && do_src) os[k] = pix_offset_f(g, REC(n_lens + k), Jb, Ib);
-#pragma unroll
-        for (int k = 0; k < MLL; ++k)
-            if (k < n_ll && do_ll) oll[k] = pix_offset_f(g, REC(n_lens + n_src + k), Jb, Ib);
-
-        float acc = 0.f;
-        bool flag = false;
-        for (int si = 0; si < s; ++si) {
-            float rs = 0.f;
-            const float fi = (float)si;
-            for (int sj = 0; sj < s; ++sj) {
-                // sub-ray displacement from the base ray: below one pixel, so a
-                // plain FP32 product keeps an absolute error of ~1e-9 pixel
-                const float fj = (float)sj;
-                const float ddx = fmaf(fi, bxf, fj * axf);
-                const float ddy = fmaf(fi, byf, fj * ayf);
-                float flux = 0.f;
-                if (do_src) {
-                    float axs = 0.f, ays = 0.f;
-#pragma unroll
-                    for (int p = 0; p < ML; ++p) {
-                        if (p >= n_lens) break;
-                        const int code = LS::generic ? st.lens[p] : LS::code(p);
-                        const int es = st.epl_slot[p];
-                        float ax, ay;
-                        lens_deflect<float>(code, REC(p), es >= 0 ? scoef + es * EPL_NMAX : nullptr,
-                                            ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
-                        axs += ax;
-                        ays += ay;
-                    }
-                    axs *= st.alpha_scaling_f;
-                    ays *= st.alpha_scaling_f;
-                    float fsrc = 0.f, gsum = 0.f;
-#pragma unroll
-                    for (int k = 0; k < MS; ++k) {
-                        if (k >= n_src) break;
-                        const float sc = st.src_scale_f[k];
-                        float gk;
-                        const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sc * axs,
-                                                          os[k].by + ddy - sc * ays, gk);
-                        fsrc += fk;
-                        gsum += fk * gk * sc;
-                    }
-                    flux = fsrc;
-                    if (do_ll) {
-#pragma unroll
-                        for (int k = 0; k < MLL; ++k) {
-                            if (k >= n_ll) break;
-                            flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
-                                                       oll[k].by + ddy);
-                        }
-                    }
-                    if (refine) {
-                        // predicted relative error of this ray's flux from the FP32
-                        // error of beta (kappa * |alpha|) through the source gradients
-                        const float dbeta = rf.kappa * (fabsf(axs) + fabsf(ays));
-                        flag |= gsum * dbeta > rf.tau * flux;
-                    }
-                } else if (do_ll) {
-#pragma unroll
-                    for (int k = 0; k < MLL; ++k) {
-                        if (k >= n_ll) break;
-                        flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
-                                                   oll[k].by + ddy);
-                    }
-                }
-                rs += flux;
-            }
-            acc += s == 1 ? rs : rs * inv_s;
-        }
-        if (s > 1) acc *= inv_s;
-        o[pix] = acc * st.flux_scaling_f * out_scale;
-        if (flag) {
-            const unsigned int slot_i = atomicAdd(rf.count, 1u);
-            rf.list[slot_i] = (unsigned int)((long long)inst * npix + pix);
-        }
-    }
-#undef REC
-}
-
-// ---------------------------------------------------------------------------
-// Refine pass: recompute the listed pixels in FP64 (records read from global
-// memory, one thread per listed pixel).
-// ---------------------------------------------------------------------------
-template <int C0, int C1, int NS, int NLL>
-__global__ void __launch_bounds__(128)
-refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
-              const double* __restrict__ coef, float* __restrict__ out, int flags,
-              double out_scale, RefineArgs rf) {
-    const unsigned int n = *rf.count;
-    const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const long long npix = (long long)g.nx * g.ny;
-    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x) {
-        const long long e = (long long)rf.list[i];
-        const int inst = (int)(e / npix);
-        const long long pix = e - (long long)inst * npix;
-        const double* srec = rec + (long long)inst * n_prof * REC_D;
-        const double* scoef = coef + (long long)inst * st.n_epl * EPL_NMAX;
-        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
-        const double v =
-            pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, out_scale);
-        out[(long long)inst * npix + pix] = (float)v;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// host launchers
-// ---------------------------------------------------------------------------
-static int g_num_sms = 0;
-
-static int num_sms() {
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 152;
-    }
-    return g_num_sms;
-}
-
-template <int C0, int C1, int NS, int NLL>
-static void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
-                           const float* rec_f, const double* coef_d, const float* coef_f,
-                           void* out, int flags, double out_scale, int precision,
-                           const RefineArgs& rf, cudaStream_t stream) {
-    const int threads = 256;
-    const long long npix = (long long)g.nx * g.ny;
-    // pixels per thread: enough CTAs to fill the GPU several times over
-    long long target = (long long)num_sms() * 8 * threads;
-    long long total = npix * (long long)n_inst;
-    int ppt = (int)((total + target - 1) / target);
-    ppt = ppt < 1 ? 1 : (ppt > 8 ? 8 : ppt);
-    const long long per_cta = (long long)threads * ppt;
-    dim3 grid((unsigned)((npix + per_cta - 1) / per_cta), (unsigned)n_inst);
-    const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    if (precision == LENSGB_FP64) {
-        size_t smem = (size_t)(n_prof * REC_D + st.n_epl * EPL_NMAX) * sizeof(double);
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(raytrace_fp64_kernel<C0, C1, NS, NLL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        raytrace_fp64_kernel<C0, C1, NS, NLL><<<grid, threads, smem, stream>>>(
-            g, st, ppt, rec_d, coef_d, (double*)out, flags, out_scale);
-    } else {
-        size_t smem = (size_t)(n_prof * REC_F + st.n_epl * EPL_NMAX) * sizeof(float);
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        raytrace_fp32_kernel<C0, C1, NS, NLL><<<grid, threads, smem, stream>>>(
-            g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf);
-        if (rf.tau > 0.f && !(flags & LENSGB_NO_SOURCE) && st.n_src > 0) {
-            const int rblocks = num_sms() * 4;
-            refine_kernel<C0, C1, NS, NLL><<<rblocks, 128, 0, stream>>>(
-                g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf);
-        }
-    }
-}
 
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,

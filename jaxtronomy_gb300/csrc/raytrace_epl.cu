@@ -1,0 +1,8 @@
+// Ray-tracing kernels specialised for EPL + SHEAR lens stacks.
+#include "raytrace_kernels.cuh"
+
+namespace lensgb {
+LENSGB_DEFINE_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 1)
+LENSGB_DEFINE_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 2, 1)
+LENSGB_DEFINE_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 0)
+}  // namespace lensgb

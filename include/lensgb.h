@@ -30,6 +30,9 @@
  *   SHEAR          gamma1 gamma2 ra_0 dec_0                        (shear.py:16)
  *   NFW            Rs alpha_Rs center_x center_y                   (nfw.py:49)
  *   TNFW           Rs alpha_Rs r_trunc center_x center_y           (tnfw.py:27)
+ *   NFW_ELLIPSE_CSE Rs alpha_Rs e1 e2 center_x center_y            (nfw_ellipse_cse.py:172)
+ *   EPL_MULTIPOLE_M1M3M4 theta_E gamma e1 e2 center_x center_y a1_a delta_phi_m1
+ *                  a3_a delta_phi_m3 a4_a delta_phi_m4            (epl_multipole_m1m3m4.py:415-428)
  *   SERSIC         amp R_sersic n_sersic center_x center_y         (sersic.py:27)
  *   SERSIC_ELLIPSE amp R_sersic n_sersic e1 e2 center_x center_y   (sersic_ellipse.py:25)
  */
@@ -54,6 +57,8 @@ extern "C" {
 #define LENSGB_LENS_SHEAR 4
 #define LENSGB_LENS_NFW 5
 #define LENSGB_LENS_TNFW 6
+#define LENSGB_LENS_NFW_ELLIPSE_CSE 7
+#define LENSGB_LENS_EPL_MULTIPOLE_M1M3M4 8
 
 #define LENSGB_LIGHT_SERSIC 1
 #define LENSGB_LIGHT_SERSIC_ELLIPSE 2

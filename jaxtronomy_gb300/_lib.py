@@ -20,7 +20,8 @@ ERR_OOM = 3
 ERR_CUDA = 4
 
 # profile codes
-LENS_CODES = {"SIE": 1, "NIE": 2, "EPL": 3, "SHEAR": 4, "NFW": 5, "TNFW": 6}
+LENS_CODES = {"SIE": 1, "NIE": 2, "EPL": 3, "SHEAR": 4, "NFW": 5, "TNFW": 6,
+              "NFW_ELLIPSE_CSE": 7, "EPL_MULTIPOLE_M1M3M4": 8}
 LIGHT_CODES = {"SERSIC": 1, "SERSIC_ELLIPSE": 2}
 
 PSF_NONE, PSF_PIXEL, PSF_GAUSSIAN = 0, 1, 2

@@ -45,6 +45,8 @@ static int lens_param_count(int code) {
         case LENSGB_LENS_SHEAR: return 4;
         case LENSGB_LENS_NFW: return 4;
         case LENSGB_LENS_TNFW: return 5;
+        case LENSGB_LENS_NFW_ELLIPSE_CSE: return 6;
+        case LENSGB_LENS_EPL_MULTIPOLE_M1M3M4: return 12;
         default: return -1;
     }
 }
@@ -214,7 +216,10 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
         st.lens[i] = d->lens_codes[i];
         st.lens_off[i] = off;
         off += c;
-        if (d->lens_codes[i] == LENSGB_LENS_EPL) st.epl_slot[i] = st.n_epl++;
+        if (d->lens_codes[i] == LENSGB_LENS_EPL ||
+            d->lens_codes[i] == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4 ||
+            d->lens_codes[i] == LENSGB_LENS_NFW_ELLIPSE_CSE)
+            st.epl_slot[i] = st.n_epl++;
     }
     for (int i = 0; i < d->n_source; ++i) {
         int c = light_param_count(d->source_codes[i]);

@@ -11,8 +11,8 @@ namespace lensgb {
 
 // Derived per-(system, profile) record written by the prepare kernel.  Doubles
 // serve the FP64 kernels and FP64 set-up; floats serve the FP32 kernels.
-constexpr int REC_D = 24;
-constexpr int REC_F = 24;
+constexpr int REC_D = 32;
+constexpr int REC_F = 36;  // float slot k + 2 mirrors double slot k >= 2
 // EPL series coefficient table length (largest reference nmax, epl.py:311-319)
 constexpr int EPL_NMAX = 500;
 constexpr int MAX_PROF = LENSGB_MAX_PROFILES;
@@ -42,8 +42,9 @@ struct StackDesc {
     int lens_off[MAX_PROF];   // column of each profile in a system row
     int src_off[MAX_PROF];
     int ll_off[MAX_PROF];
-    int epl_slot[MAX_PROF];   // EPL coefficient slot of each lens profile (-1: none)
-    int n_epl;
+    int epl_slot[MAX_PROF];   // coefficient-table slot of each lens profile (-1: none):
+                              // EPL series F_n, or the CSE term constants
+    int n_epl;                // number of coefficient-table slots per system
     int n_params;
     double src_scale[MAX_PROF];  // deflection_scaling per source
     double alpha_scaling;
@@ -102,9 +103,10 @@ __host__ __device__ inline void split_double(double v, float& hi, float& lo) {
     lo = (float)(v - (double)hi);
 }
 
-// Hardware approximations (PTX lg2.approx / ex2.approx, flush-to-zero).  Used
-// only where their error (about 2^-22) is not amplified: the log2 of a radius
-// and the final exponential of a Sersic profile.
+// Hardware approximations (PTX lg2.approx / ex2.approx, flush-to-zero, relative
+// error about 2^-22).  The FP32 path uses them for the EPL power law and the
+// Sersic profile; the resulting image error is measured against FP64 and the
+// ill-conditioned rays are recomputed in FP64 anyway.
 __device__ __forceinline__ float lg2_approx(float x) {
     float r;
     asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));

@@ -7,19 +7,6 @@
 
 namespace lensgb {
 
-__device__ __forceinline__ void lens_deflect_d(int code, const double* rec, const double* F,
-                                               double dx, double dy, double& ax, double& ay) {
-    switch (code) {
-        case LENSGB_LENS_SIE:
-        case LENSGB_LENS_NIE: nie_deflect<double>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_EPL: epl_deflect<double>(rec, F, dx, dy, ax, ay); break;
-        case LENSGB_LENS_SHEAR: shear_deflect<double>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_NFW: nfw_deflect<double>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_TNFW: tnfw_deflect<double>(rec, dx, dy, ax, ay); break;
-        default: ax = 0; ay = 0; break;
-    }
-}
-
 __global__ void ray_shoot_points_kernel(StackDesc st, const double* __restrict__ rec,
                                         const double* __restrict__ coef,
                                         const double* __restrict__ x, const double* __restrict__ y,
@@ -33,7 +20,7 @@ __global__ void ray_shoot_points_kernel(StackDesc st, const double* __restrict__
         const double* r = rec + p * REC_D;
         const int es = st.epl_slot[p];
         double ax, ay;
-        lens_deflect_d(st.lens[p], r, es >= 0 ? coef + es * EPL_NMAX : nullptr, X - r[RD_CX],
+        lens_deflect<double>(st.lens[p], r, es >= 0 ? coef + es * EPL_NMAX : nullptr, X - r[RD_CX],
                        Y - r[RD_CY], ax, ay);
         axs += ax;
         ays += ay;

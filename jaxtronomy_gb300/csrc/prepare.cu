@@ -12,6 +12,7 @@
 //   product average     Util/param_util.py:103-123
 #include <math.h>
 
+#include "cse_table.h"
 #include "launch.h"
 #include "profiles.cuh"
 
@@ -80,7 +81,7 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
             d[RD_CY] = a[co + 1];
             d[2] = b; d[3] = s; d[4] = qc; d[5] = cos(phi); d[6] = sin(phi);
             d[7] = sq; d[8] = b / sq; d[9] = qc * qc; d[10] = qc * qc * s; d[11] = qc * qc * s * s;
-        } else if (code == LENSGB_LENS_EPL) {
+        } else if (code == LENSGB_LENS_EPL || code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
             double theta_E = a[0], gamma = a[1], e1 = a[2], e2 = a[3];
             double phi, q;
             ellip_phi_q(e1, e2, phi, q);
@@ -124,6 +125,42 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
                 }
             }
             d[15] = (double)n32;
+            if (code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
+                // multipoles m = 1, 3, 4 about the EPL centre, strengths a_m =
+                // a{m}_a theta_E / sqrt(q), angles phi_m = phi + delta_phi_m
+                // (epl_multipole_m1m3m4.py:495-535); m = 1 uses r_E = theta_E
+                const double rescale = theta_E / sqrt(q);
+                const double a1 = a[6] * rescale, p1 = phi + a[7];
+                const double a3 = a[8] * rescale, p3 = phi + a[9];
+                const double a4 = a[10] * rescale, p4 = phi + a[11];
+                d[16] = a1 / 2; d[17] = cos(p1); d[18] = sin(p1); d[19] = log(theta_E);
+                d[20] = a3 / (1.0 - 9.0); d[21] = cos(3 * p3); d[22] = sin(3 * p3);
+                d[23] = a4 / (1.0 - 16.0); d[24] = cos(4 * p4); d[25] = sin(4 * p4);
+                d[26] = p1; d[27] = a3; d[28] = p3; d[29] = a4; d[30] = p4; d[31] = theta_E;
+            }
+        } else if (code == LENSGB_LENS_NFW_ELLIPSE_CSE) {
+            double Rs = a[0], alpha_Rs = a[1], e1 = a[2], e2 = a[3];
+            double phi, q;
+            ellip_phi_q(e1, e2, phi, q);
+            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+            d[RD_CX] = a[4];
+            d[RD_CY] = a[5];
+            d[2] = Rs; d[3] = 1.0 / Rs; d[4] = q; d[5] = cos(phi); d[6] = sin(phi);
+            d[7] = sqrt(q); d[8] = 4.0 * CSE_NFW_TERMS; d[9] = 4 * rho0 * Rs * Rs * Rs / Rs;
+            d[10] = q * q; d[11] = 1.0 - q * q;
+            // per-term constants of the FP32 path, one float4 per term:
+            // (q^2 s^2, s, q^2 s, a/s)
+            int slot_e = st.epl_slot[p];
+            double* Cd = coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
+            float* Cf = coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
+            for (int k = 0; k < CSE_NFW_TERMS; ++k) {
+                const double s = kCseNfwS[k], ak = kCseNfwA[k];
+                const double v[4] = {q * q * s * s, s, q * q * s, ak / s};
+                for (int j = 0; j < 4; ++j) {
+                    Cd[4 * k + j] = v[j];
+                    Cf[4 * k + j] = (float)v[j];
+                }
+            }
         } else if (code == LENSGB_LENS_SHEAR) {
             d[RD_CX] = a[2];
             d[RD_CY] = a[3];

@@ -16,6 +16,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "cse_table.h"
 
 namespace lensgb {
 
@@ -129,7 +130,10 @@ __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, 
         hi = (sr * gi + si * gr) * ee;
     }
     const float r2m = r2 > 1e-18f ? r2 : 1e-18f;  // R = max(|Z|, 1e-9)
-    const float amp = pref * exp2f(mth * log2f(r2m));
+    // hardware lg2/ex2: on the 1024-system EPL workload this moved the maximum
+    // FP32 image error from 5.58e-6 to 5.69e-6 (rays it disturbs most are the
+    // ones the FP64 refine pass recomputes)
+    const float amp = pref * ex2_approx(mth * lg2_approx(r2m));
     const float fx = amp * (za * hr - zb * hi);
     const float fy = amp * (za * hi + zb * hr);
     ax = fx * c - fy * sn;
@@ -199,6 +203,145 @@ __device__ __forceinline__ void epl_deflect(const R* rec, const R* F, R dx, R dy
         fx = nan_to_num_1e10(amp * omr);
         fy = nan_to_num_1e10(amp * omi);
     }
+    ax = fx * c - fy * sn;
+    ay = fx * sn + fy * c;
+}
+
+// ---------------------------------------------------------------------------
+// Circular multipoles m = 1, 3, 4 of EPL_MULTIPOLE_M1M3M4 (Xu et al. 2013, B12;
+// multipole.py:72-119).  Record slots (double): d16 a1/2, d17 cos phi1,
+// d18 sin phi1, d19 ln r_E, d20 a3/(1-9), d21 cos 3phi3, d22 sin 3phi3,
+// d23 a4/(1-16), d24 cos 4phi4, d25 sin 4phi4, d26 phi1, d27 a3, d28 phi3,
+// d29 a4, d30 phi4, d31 r_E = theta_E.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void multipole134_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    if (sizeof(R) == 8) {
+        // reference form: polar angle via atan2 (atan2(0, 0) = 0 at the centre)
+        const double r0 = sqrt((double)dx * dx + (double)dy * dy);
+        const double phi = atan2((double)dy, (double)dx);
+        const double cph = cos(phi), sph = sin(phi);
+        const double a1 = 2 * (double)rec[16], p1 = rec[26], rE = rec[31];
+        const double r1 = r0 > 0.000001 ? r0 : 0.000001;
+        const double lr = log(r1 / rE);
+        double fx = a1 / 2 * (cos(p1) * lr + cos(phi - p1) * cph);
+        double fy = a1 / 2 * (sin(p1) * lr + cos(phi - p1) * sph);
+        const double am[2] = {rec[27], rec[29]}, pm[2] = {rec[28], rec[30]};
+        const double mm[2] = {3.0, 4.0};
+        for (int j = 0; j < 2; ++j) {
+            const double m = mm[j], a = am[j], pj = pm[j];
+            fx += cph * a / (1 - m * m) * cos(m * (phi - pj)) +
+                  sph * m * a / (1 - m * m) * sin(m * (phi - pj));
+            fy += sph * a / (1 - m * m) * cos(m * (phi - pj)) -
+                  cph * m * a / (1 - m * m) * sin(m * (phi - pj));
+        }
+        ax = (R)fx;
+        ay = (R)fy;
+    } else {
+        // FP32: cos/sin of the polar angle from the offsets, e^{i m phi} by powers
+        const float* f = (const float*)rec;
+        const float r2 = (float)dx * (float)dx + (float)dy * (float)dy;
+        float c = 1.f, s = 0.f;
+        if (r2 > 0.f) {
+            const float ri = rsqrtf(r2);
+            c = (float)dx * ri;
+            s = (float)dy * ri;
+        }
+        const float r2m = r2 > 1e-12f ? r2 : 1e-12f;  // r floored at 1e-6
+        const float lr = 0.5f * __logf(r2m) - f[21];
+        const float cd1 = c * f[19] + s * f[20];      // cos(phi - phi1)
+        float fx = f[18] * (f[19] * lr + cd1 * c);
+        float fy = f[18] * (f[20] * lr + cd1 * s);
+        const float C2 = c * c - s * s, S2 = 2.f * c * s;
+        // m = 3
+        const float C3 = C2 * c - S2 * s, S3 = S2 * c + C2 * s;
+        const float cm3 = C3 * f[23] + S3 * f[24], sm3 = S3 * f[23] - C3 * f[24];
+        fx += f[22] * (c * cm3 + 3.f * s * sm3);
+        fy += f[22] * (s * cm3 - 3.f * c * sm3);
+        // m = 4
+        const float C4 = C2 * C2 - S2 * S2, S4 = 2.f * C2 * S2;
+        const float cm4 = C4 * f[26] + S4 * f[27], sm4 = S4 * f[26] - C4 * f[27];
+        fx += f[25] * (c * cm4 + 4.f * s * sm4);
+        fy += f[25] * (s * cm4 - 4.f * c * sm4);
+        ax = (R)fx;
+        ay = (R)fy;
+    }
+}
+
+// EPL_MULTIPOLE_M1M3M4 = EPL + the three multipoles about the same centre
+// (epl_multipole_m1m3m4.py:608-678); the EPL part shares the EPL record layout.
+template <typename R>
+__device__ __forceinline__ void epl_multipole_deflect(const R* rec, const R* F, R dx, R dy, R& ax,
+                                                      R& ay) {
+    R ex, ey, mx, my;
+    epl_deflect<R>(rec, F, dx, dy, ex, ey);
+    multipole134_deflect<R>(rec, dx, dy, mx, my);
+    ax = ex + mx;
+    ay = ey + my;
+}
+
+// ---------------------------------------------------------------------------
+// NFW_ELLIPSE_CSE: 44 cored steep ellipsoids (Oguri 2021), product-average
+// coordinates (cored_steep_ellipsoid.py:227-245,434-477,536-564,
+// nfw_ellipse_cse.py:250-280).  Record (double): d2 Rs, d3 1/Rs, d4 q, d5 cos,
+// d6 sin, d7 sqrt(q), d9 4 rho0 Rs^2, d10 q^2, d11 1-q^2.  FP32 term table C:
+// one float4 (q^2 s^2, s, q^2 s, a/s) per term.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void nfw_cse_deflect(const R* rec, const R* C, R dx, R dy, R& ax,
+                                                R& ay);
+
+template <>
+__device__ __forceinline__ void nfw_cse_deflect<double>(const double* rec, const double* C,
+                                                        double dx, double dy, double& ax,
+                                                        double& ay) {
+    const double Rs = rec[2], q = rec[4], c = rec[5], sn = rec[6];
+    (void)C;
+    double x = dx * c + dy * sn;
+    double y = -dx * sn + dy * c;
+    x = x / Rs;
+    y = y / Rs;
+    const double sq = sqrt(q);
+    double fx = 0, fy = 0;
+    for (int k = 0; k < CSE_NFW_TERMS; ++k) {
+        const double a = kCseNfwA[k] / q, s = kCseNfwS[k];
+        const double xa = x * sq, ya = y * sq;
+        const double psi = sqrt(q * q * (s * s + xa * xa) + ya * ya);
+        const double Phi = (psi + s) * (psi + s) + (1 - q * q) * xa * xa;
+        const double gx = q * xa * (psi + q * q * s) / (s * psi * Phi);
+        const double gy = q * ya * (psi + s) / (s * psi * Phi);
+        fx += sq * (a * gx);
+        fy += sq * (a * gy);
+    }
+    const double cst = rec[9];
+    ax = cst * (fx * c - fy * sn);
+    ay = cst * (fx * sn + fy * c);
+}
+
+template <>
+__device__ __forceinline__ void nfw_cse_deflect<float>(const float* rec, const float* C, float dx,
+                                                       float dy, float& ax, float& ay) {
+    const float inv_rs = rec[5], c = rec[7], sn = rec[8], sq = rec[9];
+    const float q2 = rec[12], omq2 = rec[13];
+    const float x = (dx * c + dy * sn) * inv_rs * sq;  // product-average frame
+    const float y = (-dx * sn + dy * c) * inv_rs * sq;
+    const float B = q2 * x * x + y * y, D = omq2 * x * x;
+    float sx = 0.f, sy = 0.f;
+    const float4* T = reinterpret_cast<const float4*>(C);
+#pragma unroll 4
+    for (int k = 0; k < 44; ++k) {
+        const float4 t = T[k];                    // (q^2 s^2, s, q^2 s, a/s)
+        const float u = B + t.x;                  // psi^2 = q^2 (s^2 + x^2) + y^2
+        const float psi = u * rsqrtf(u);
+        const float ps = psi + t.y;
+        const float Phi = fmaf(ps, ps, D);
+        const float inv = __fdividef(t.w, psi * Phi);  // (a/s) / (psi Phi)
+        sx = fmaf(psi + t.z, inv, sx);
+        sy = fmaf(ps, inv, sy);
+    }
+    // sum_k a_k X (psi + q^2 s_k)/(s_k psi Phi), times sqrt(q) and the normalisation
+    const float cst = rec[11] * sq;
+    const float fx = cst * x * sx, fy = cst * y * sy;
     ax = fx * c - fy * sn;
     ay = fx * sn + fy * c;
 }
@@ -401,8 +544,9 @@ __device__ __forceinline__ float sersic_f(const float* rec, float dx, float dy, 
     const float r2m = floored ? 1e-8f : r2;
     // log2(R/R_s): an absolute error of ~2^-22.6 here moves v by only ~4e-8/n
     const float l2f = fmaf(0.5f, lg2_approx(r2m), l2irs);
-    // v is multiplied by b_n log2(e) (up to ~40) below, so it keeps the accurate exp2f
-    const float v = exp2f(inv_n * l2f);
+    // v is multiplied by b_n log2(e) (up to ~40) below; the hardware ex2 left the
+    // maximum image error of the 1024-system EPL workload unchanged (5.58e-6)
+    const float v = ex2_approx(inv_n * l2f);
     // the argument's own FP32 rounding dominates this exponential's error
     const float res = l2f <= 9.965784284662087f ? ex2_approx(bnl * (1.f - v)) : 0.f;
     if (GRAD) g = floored ? 0.f : rec[15] * v * rsqrtf(r2m);
@@ -411,6 +555,29 @@ __device__ __forceinline__ float sersic_f(const float* rec, float dx, float dy, 
 
 __device__ __forceinline__ float sersic_flux_grad(const float* rec, float dx, float dy, float& g) {
     return sersic_f<true>(rec, dx, dy, g);
+}
+
+// ---------------------------------------------------------------------------
+// Dispatch on the lens profile code (the name -> class table of
+// LensModel/profile_list_base.py:309-765 for the profiles of this library).
+// F is the profile's coefficient table (EPL series or CSE terms), if any.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F, R dx, R dy, R& ax,
+                                             R& ay) {
+    switch (code) {
+        case LENSGB_LENS_SIE:
+        case LENSGB_LENS_NIE: nie_deflect<R>(rec, dx, dy, ax, ay); break;
+        case LENSGB_LENS_EPL: epl_deflect<R>(rec, F, dx, dy, ax, ay); break;
+        case LENSGB_LENS_SHEAR: shear_deflect<R>(rec, dx, dy, ax, ay); break;
+        case LENSGB_LENS_NFW: nfw_deflect<R>(rec, dx, dy, ax, ay); break;
+        case LENSGB_LENS_TNFW: tnfw_deflect<R>(rec, dx, dy, ax, ay); break;
+        case LENSGB_LENS_NFW_ELLIPSE_CSE: nfw_cse_deflect<R>(rec, F, dx, dy, ax, ay); break;
+        case LENSGB_LENS_EPL_MULTIPOLE_M1M3M4:
+            epl_multipole_deflect<R>(rec, F, dx, dy, ax, ay);
+            break;
+        default: ax = 0; ay = 0; break;
+    }
 }
 
 }  // namespace lensgb

@@ -26,6 +26,14 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
             if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 1, 1); return 0; }
             if (st.n_src == 2 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 2, 1); return 0; }
         }
+        if (a == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
+            if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_EPL_MULTIPOLE_M1M3M4, LENSGB_LENS_SHEAR, 1, 1); return 0; }
+            if (st.n_src == 2 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_EPL_MULTIPOLE_M1M3M4, LENSGB_LENS_SHEAR, 2, 1); return 0; }
+        }
+        if (a == LENSGB_LENS_NFW_ELLIPSE_CSE) {
+            if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_NFW_ELLIPSE_CSE, LENSGB_LENS_SHEAR, 1, 1); return 0; }
+            if (st.n_src == 2 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_NFW_ELLIPSE_CSE, LENSGB_LENS_SHEAR, 2, 1); return 0; }
+        }
     }
     LENSGB_VARIANT(GENERIC, 0, -1, -1);
 #undef LENSGB_VARIANT

@@ -38,20 +38,6 @@ namespace lensgb {
 // Lens-stack selector: C0/C1 are compile-time lens codes (0 = absent); C0 =
 // GENERIC (-1, raytrace_variants.h) selects the kernel that walks the runtime stack.
 
-template <typename R>
-__device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F, R dx, R dy, R& ax,
-                                             R& ay) {
-    switch (code) {
-        case LENSGB_LENS_SIE:
-        case LENSGB_LENS_NIE: nie_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_EPL: epl_deflect<R>(rec, F, dx, dy, ax, ay); break;
-        case LENSGB_LENS_SHEAR: shear_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_NFW: nfw_deflect<R>(rec, dx, dy, ax, ay); break;
-        case LENSGB_LENS_TNFW: tnfw_deflect<R>(rec, dx, dy, ax, ay); break;
-        default: ax = 0; ay = 0; break;
-    }
-}
-
 // Offsets of the pixel's base ray (sub-ray 0, 0) from one profile centre.
 struct PixOff {
     float bx, by;  // FP32 path: FP64-accurate offset of the base ray, rounded once

@@ -28,6 +28,10 @@ LENSGB_DECLARE_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 2, 1)
 LENSGB_DECLARE_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 0)
 LENSGB_DECLARE_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 1, 1)
 LENSGB_DECLARE_VARIANT(LENSGB_LENS_SIE, LENSGB_LENS_SHEAR, 2, 1)
+LENSGB_DECLARE_VARIANT(LENSGB_LENS_EPL_MULTIPOLE_M1M3M4, LENSGB_LENS_SHEAR, 1, 1)
+LENSGB_DECLARE_VARIANT(LENSGB_LENS_EPL_MULTIPOLE_M1M3M4, LENSGB_LENS_SHEAR, 2, 1)
+LENSGB_DECLARE_VARIANT(LENSGB_LENS_NFW_ELLIPSE_CSE, LENSGB_LENS_SHEAR, 1, 1)
+LENSGB_DECLARE_VARIANT(LENSGB_LENS_NFW_ELLIPSE_CSE, LENSGB_LENS_SHEAR, 2, 1)
 LENSGB_DECLARE_VARIANT(GENERIC, 0, -1, -1)
 
 }  // namespace lensgb

@@ -2,7 +2,8 @@
 
 Parameter names and their order are the reference profiles' ``param_names``
 (JAXtronomy: ``LensModel/Profiles/sie.py:40``, ``nie.py:19``, ``epl.py:50``,
-``shear.py:16``, ``nfw.py:49``, ``tnfw.py:27``,
+``shear.py:16``, ``nfw.py:49``, ``tnfw.py:27``, ``nfw_ellipse_cse.py:172``,
+``epl_multipole_m1m3m4.py:415-428``,
 ``LightModel/Profiles/sersic.py:27``, ``sersic_ellipse.py:25``).  The packed
 row layout is the one documented in ``include/lensgb.h``.
 """
@@ -18,6 +19,9 @@ LENS_PARAMS = {
     "SHEAR": ["gamma1", "gamma2", "ra_0", "dec_0"],
     "NFW": ["Rs", "alpha_Rs", "center_x", "center_y"],
     "TNFW": ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"],
+    "NFW_ELLIPSE_CSE": ["Rs", "alpha_Rs", "e1", "e2", "center_x", "center_y"],
+    "EPL_MULTIPOLE_M1M3M4": ["theta_E", "gamma", "e1", "e2", "center_x", "center_y", "a1_a",
+                             "delta_phi_m1", "a3_a", "delta_phi_m3", "a4_a", "delta_phi_m4"],
 }
 
 LIGHT_PARAMS = {

@@ -242,6 +242,105 @@ def tnfw(x, y, Rs, alpha_Rs, r_trunc, center_x=0.0, center_y=0.0):
 
 
 # ---------------------------------------------------------------------------
+# NFW_ELLIPSE_CSE  (jaxtronomy/LensModel/Profiles/nfw_ellipse_cse.py,
+#                   cored_steep_ellipsoid.py)
+# ---------------------------------------------------------------------------
+
+# Oguri (2021, arXiv:2106.11464) Table 1: the 44-term cored-steep-ellipsoid
+# decomposition of the NFW profile, (a_k, s_k) in units of the scale radius,
+# as used by the reference's high_accuracy=True default (nfw_ellipse_cse.py:15-156).
+CSE_NFW_A = np.array([
+    1.648988e-18, 6.274458e-16, 3.646620e-17, 3.459206e-15, 2.457389e-14, 1.059319e-13,
+    4.211597e-13, 1.142832e-12, 4.391215e-12, 1.556500e-11, 6.951271e-11, 3.147466e-10,
+    1.379109e-09, 3.829778e-09, 1.384858e-08, 5.370951e-08, 1.804384e-07, 5.788608e-07,
+    3.205256e-06, 1.102422e-05, 4.093971e-05, 1.282206e-04, 4.575541e-04, 7.995270e-04,
+    5.013701e-03, 1.403508e-02, 5.230727e-02, 1.898907e-01, 3.643448e-01, 7.203734e-01,
+    1.717667e+00, 2.217566e+00, 3.187447e+00, 8.194898e+00, 1.765210e+01, 1.974319e+01,
+    2.783688e+01, 4.482311e+01, 5.598897e+01, 1.426485e+02, 2.279833e+02, 5.401335e+02,
+    9.743682e+02, 1.775124e+03])
+CSE_NFW_S = np.array([
+    1.082411e-06, 8.786566e-06, 3.292868e-06, 1.860019e-05, 3.274231e-05, 6.232485e-05,
+    9.256333e-05, 1.546762e-04, 2.097321e-04, 3.391140e-04, 5.178790e-04, 8.636736e-04,
+    1.405152e-03, 2.193855e-03, 3.179572e-03, 4.970987e-03, 7.631970e-03, 1.119413e-02,
+    1.827267e-02, 2.945251e-02, 4.562723e-02, 6.782509e-02, 1.596987e-01, 1.127751e-01,
+    2.169469e-01, 3.423835e-01, 5.194527e-01, 8.623185e-01, 1.382737e+00, 2.034929e+00,
+    3.402979e+00, 5.594276e+00, 8.052345e+00, 1.349045e+01, 2.603825e+01, 4.736823e+01,
+    6.559320e+01, 1.087932e+02, 1.477673e+02, 2.495341e+02, 4.305999e+02, 7.760206e+02,
+    2.143057e+03, 1.935749e+03])
+
+
+def cse_major_axis(x, y, a, s, q):
+    """``CSEMajorAxis.derivatives`` ``cored_steep_ellipsoid.py:227-245``."""
+    psi = np.sqrt(q ** 2 * (s ** 2 + x ** 2) + y ** 2)
+    Phi = (psi + s) ** 2 + (1 - q ** 2) * x ** 2
+    f_x = q * x * (psi + q ** 2 * s) / (s * psi * Phi)
+    f_y = q * y * (psi + s) / (s * psi * Phi)
+    return a * f_x, a * f_y
+
+
+def cse_product_avg_set(x, y, a_list, s_list, q):
+    """``CSEProductAvgSet.derivatives`` :536-564 over ``CSEProductAvg.derivatives``
+    :463-477 (product-average conversion :434-443)."""
+    fx = np.zeros_like(x)
+    fy = np.zeros_like(y)
+    for a, s in zip(a_list, s_list):
+        xa, ya = x * np.sqrt(q), y * np.sqrt(q)
+        ax, ay = cse_major_axis(xa, ya, a / q, s, q)
+        fx = fx + np.sqrt(q) * ax
+        fy = fy + np.sqrt(q) * ay
+    return fx, fy
+
+
+def nfw_ellipse_cse(x, y, Rs, alpha_Rs, e1, e2, center_x=0.0, center_y=0.0):
+    """``NFW_ELLIPSE_CSE.derivatives`` ``nfw_ellipse_cse.py:250-280`` with
+    ``_normalization`` :338-349."""
+    phi_q, q = ellipticity2phi_q(e1, e2)
+    x_, y_ = rotate(_f(x) - center_x, _f(y) - center_y, phi_q)
+    fx, fy = cse_product_avg_set(x_ / Rs, y_ / Rs, CSE_NFW_A, CSE_NFW_S, q)
+    fx, fy = rotate(fx, fy, -phi_q)
+    const = 4 * nfw_alpha2rho0(alpha_Rs, Rs) * Rs ** 3 / Rs
+    return const * fx, const * fy
+
+
+# ---------------------------------------------------------------------------
+# circular multipoles and EPL_MULTIPOLE_M1M3M4
+# (jaxtronomy/LensModel/Profiles/multipole.py, epl_multipole_m1m3m4.py)
+# ---------------------------------------------------------------------------
+
+
+def multipole(x, y, m, a_m, phi_m, center_x=0.0, center_y=0.0, r_E=1.0):
+    """``Multipole.derivatives`` ``multipole.py:72-119`` (Xu et al. 2013, B12)."""
+    dx = _f(x) - center_x
+    dy = _f(y) - center_y
+    r = np.sqrt(dx ** 2 + dy ** 2)
+    phi = np.arctan2(dy, dx)
+    if m == 1:
+        r = np.maximum(r, 0.000001)
+        f_x = a_m / 2 * (np.cos(phi_m) * np.log(r / r_E) + np.cos(phi - phi_m) * np.cos(phi))
+        f_y = a_m / 2 * (np.sin(phi_m) * np.log(r / r_E) + np.cos(phi - phi_m) * np.sin(phi))
+        return f_x, f_y
+    f_x = np.cos(phi) * a_m / (1 - m ** 2) * np.cos(m * (phi - phi_m)) \
+        + np.sin(phi) * m * a_m / (1 - m ** 2) * np.sin(m * (phi - phi_m))
+    f_y = np.sin(phi) * a_m / (1 - m ** 2) * np.cos(m * (phi - phi_m)) \
+        - np.cos(phi) * m * a_m / (1 - m ** 2) * np.sin(m * (phi - phi_m))
+    return f_x, f_y
+
+
+def epl_multipole_m1m3m4(x, y, theta_E, gamma, e1, e2, a1_a, delta_phi_m1, a3_a, delta_phi_m3,
+                         a4_a, delta_phi_m4, center_x=0.0, center_y=0.0):
+    """``EPL_MULTIPOLE_M1M3M4.derivatives`` ``epl_multipole_m1m3m4.py:608-678``
+    with ``_param_split`` :463-535."""
+    phi, q = ellipticity2phi_q(e1, e2)
+    rescale_am = theta_E / np.sqrt(q)
+    fx, fy = epl(x, y, theta_E, gamma, e1, e2, center_x, center_y)
+    f3 = multipole(x, y, 3, a3_a * rescale_am, phi + delta_phi_m3, center_x, center_y)
+    f4 = multipole(x, y, 4, a4_a * rescale_am, phi + delta_phi_m4, center_x, center_y)
+    f1 = multipole(x, y, 1, a1_a * rescale_am, phi + delta_phi_m1, center_x, center_y,
+                   r_E=theta_E)
+    return fx + f3[0] + f4[0] + f1[0], fy + f3[1] + f4[1] + f1[1]
+
+
+# ---------------------------------------------------------------------------
 # registry and single-plane ray shooting
 # ---------------------------------------------------------------------------
 
@@ -252,6 +351,10 @@ PROFILES = {
     "SHEAR": (shear, ["gamma1", "gamma2", "ra_0", "dec_0"]),
     "NFW": (nfw, ["Rs", "alpha_Rs", "center_x", "center_y"]),
     "TNFW": (tnfw, ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"]),
+    "NFW_ELLIPSE_CSE": (nfw_ellipse_cse, ["Rs", "alpha_Rs", "e1", "e2", "center_x", "center_y"]),
+    "EPL_MULTIPOLE_M1M3M4": (epl_multipole_m1m3m4,
+                             ["theta_E", "gamma", "e1", "e2", "center_x", "center_y", "a1_a",
+                              "delta_phi_m1", "a3_a", "delta_phi_m3", "a4_a", "delta_phi_m4"]),
 }
 
 # defaults of optional keyword arguments in the profile signatures

@@ -64,6 +64,20 @@ def gen_profiles(rng):
                                    "center_y": -0.03}))
     lens_cases.append(("EPL", {"theta_E": 0.85, "gamma": 1.82, "e1": -0.08, "e2": 0.03,
                                "center_x": 0.0, "center_y": 0.0}))
+    lens_cases += [
+        ("NFW_ELLIPSE_CSE", {"Rs": 8.0, "alpha_Rs": 1.3, "e1": 0.1, "e2": -0.2, "center_x": 0.1,
+                             "center_y": 0.0}),
+        ("NFW_ELLIPSE_CSE", {"Rs": 0.5, "alpha_Rs": 0.2, "e1": -0.05, "e2": 0.02,
+                             "center_x": -0.3, "center_y": 0.4}),
+        ("EPL_MULTIPOLE_M1M3M4", {"theta_E": 1.2, "gamma": 2.05, "e1": 0.1, "e2": 0.05,
+                                  "center_x": 0.02, "center_y": -0.01, "a1_a": 0.01,
+                                  "delta_phi_m1": 0.3, "a3_a": -0.012, "delta_phi_m3": 1.1,
+                                  "a4_a": 0.008, "delta_phi_m4": 2.0}),
+        ("EPL_MULTIPOLE_M1M3M4", {"theta_E": 0.9, "gamma": 1.9, "e1": -0.3, "e2": 0.25,
+                                  "center_x": 0.0, "center_y": 0.0, "a1_a": -0.02,
+                                  "delta_phi_m1": 2.9, "a3_a": 0.005, "delta_phi_m3": 0.2,
+                                  "a4_a": -0.015, "delta_phi_m4": 0.7}),
+    ]
     for name, kw in lens_cases:
         x, y = _points(rng, 64)
         lm = LensModel([name])
@@ -190,7 +204,33 @@ def gen_images():
                    "src": ["SERSIC_ELLIPSE"], "ll": [], "kwargs_lens": kl,
                    "kwargs_source": ks, "kwargs_lens_light": kll,
                    "image": np.asarray(im.image(kl, ks, kll))})
-    # 5) likelihood on the first single-image scene with noisy data
+    # 5) serving-stream lens stacks: EPL_MULTIPOLE_M1M3M4 + SHEAR with two sources,
+    #    NFW_ELLIPSE_CSE + SHEAR, both 36x36 at 0.08"/pix, s=2, 11x11 Gaussian kernel
+    kern_g = W.gaussian_pixel_kernel(0.2, 0.08, 11)
+    ks2 = [{"amp": 60.0, "R_sersic": 0.25, "n_sersic": 2.5, "e1": 0.05, "e2": 0.1,
+            "center_x": 0.05, "center_y": -0.05},
+           {"amp": 20.0, "R_sersic": 0.4, "n_sersic": 1.2, "e1": -0.1, "e2": 0.0,
+            "center_x": -0.15, "center_y": 0.1}]
+    kll2 = [{"amp": 35.0, "R_sersic": 1.0, "n_sersic": 3.5, "e1": 0.08, "e2": -0.04,
+             "center_x": 0.0, "center_y": 0.0}]
+    for tag, lens_list, kl in [
+        ("multipole", ["EPL_MULTIPOLE_M1M3M4", "SHEAR"],
+         [{"theta_E": 1.1, "gamma": 2.1, "e1": 0.12, "e2": -0.06, "center_x": 0.0,
+           "center_y": 0.0, "a1_a": 0.008, "delta_phi_m1": 0.4, "a3_a": -0.01,
+           "delta_phi_m3": 2.2, "a4_a": 0.012, "delta_phi_m4": 1.3},
+          {"gamma1": 0.03, "gamma2": 0.01}]),
+        ("nfw_cse", ["NFW_ELLIPSE_CSE", "SHEAR"],
+         [{"Rs": 12.0, "alpha_Rs": 1.6, "e1": 0.1, "e2": 0.05, "center_x": 0.0,
+           "center_y": 0.0}, {"gamma1": -0.02, "gamma2": 0.04}]),
+    ]:
+        im = _image_model(36, 0.08, 2, {"psf_type": "PIXEL", "kernel_point_source": kern_g},
+                          lens_list, ["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], ["SERSIC_ELLIPSE"])
+        scenes.append({"tag": tag, "num_pix": 36, "delta_pix": 0.08, "s": 2,
+                       "psf_type": "PIXEL", "kernel": kern_g, "lens": lens_list,
+                       "src": ["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], "ll": ["SERSIC_ELLIPSE"],
+                       "kwargs_lens": kl, "kwargs_source": ks2, "kwargs_lens_light": kll2,
+                       "image": np.asarray(im.image(kl, ks2, kll2))})
+    # 6) likelihood on the first single-image scene with noisy data
     rng = np.random.default_rng(77)
     base = scenes[0]
     clean = base["image"]

@@ -42,6 +42,150 @@ __device__ static void write_offsets(const GridDesc& g, double cx, double cy, fl
     split_double(g.dec00 - cy, f[RF_Y0H], f[RF_Y0L]);
 }
 
+// Record of lens profile `code` from its kwargs a[] (param_names order).  Fd/Ff
+// receive the profile's coefficient table (EPL series F_n, CSE term constants)
+// when it has one (else they may be null).  d[] must be zeroed by the caller.
+__device__ void prepare_lens_record(int code, const double* a, double* d, double* Fd, float* Ff) {
+    if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
+        double theta_E = a[0], e1 = a[1], e2 = a[2];
+        double s_scale = code == LENSGB_LENS_SIE ? 0.0000000001 : a[3];
+        int co = code == LENSGB_LENS_SIE ? 3 : 4;
+        double phi, q;
+        ellip_phi_q(e1, e2, phi, q);
+        double theta_E_conv = theta_E / sqrt((1.0 + q * q) / (2.0 * q));
+        double b = theta_E_conv * sqrt((1 + q * q) / 2);
+        double s = s_scale / sqrt(q);
+        double qc = q >= 1 ? 0.99999999 : q;   // NIEMajorAxis.derivatives clamp
+        double sq = sqrt(1.0 - qc * qc);
+        d[RD_CX] = a[co];
+        d[RD_CY] = a[co + 1];
+        d[2] = b; d[3] = s; d[4] = qc; d[5] = cos(phi); d[6] = sin(phi);
+        d[7] = sq; d[8] = b / sq; d[9] = qc * qc; d[10] = qc * qc * s; d[11] = qc * qc * s * s;
+    } else if (code == LENSGB_LENS_EPL || code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
+        double theta_E = a[0], gamma = a[1], e1 = a[2], e2 = a[3];
+        double phi, q;
+        ellip_phi_q(e1, e2, phi, q);
+        double t = gamma - 1;
+        double b = theta_E * sqrt(q);
+        double fq = (1.0 - q) / (1.0 + q);
+        int nmax = epl_nmax_of(fq);
+        d[RD_CX] = a[4];
+        d[RD_CY] = a[5];
+        d[2] = b; d[3] = t; d[4] = q; d[5] = cos(phi); d[6] = sin(phi); d[7] = fq;
+        d[8] = (double)nmax; d[9] = 2.0 / (1.0 + q) * pow(b, t);
+        // FP32-path constants: f^2/4, f/2, -t/2
+        d[12] = 0.25 * fq * fq; d[13] = 0.5 * fq; d[14] = -0.5 * t;
+        // F_0 = 1, F_1 = 1 - 2B/C, F_n = ((n-1) F_{n-2} - (2B-C) F_{n-1}) / (C+n-1)
+        double B = t / 2.0, C = 2.0 - B;
+        double fpp = 1.0, fp = 1.0 - 2.0 * B / C;
+        if (nmax > 0) { Fd[0] = fpp; Ff[0] = (float)fpp; }
+        if (nmax > 1) { Fd[1] = fp; Ff[1] = (float)fp; }
+        for (int n = 2; n < nmax; ++n) {
+            double fn = ((n - 1.0) * fpp - (2.0 * B - C) * fp) / (C + n - 1.0);
+            Fd[n] = fn;
+            Ff[n] = (float)fn;
+            fpp = fp;
+            fp = fn;
+        }
+        // FP32 series length: since |w| <= f/(2-f), the terms n >= k change the
+        // sum by at most sum_{m>=k} |F_m| (f/(2-f))^m; stop once that bound is
+        // below 2^-27 (under FP32 resolution), never beyond the reference's nmax.
+        int n32 = nmax;
+        if (nmax > 1) {
+            const double wmax = fq / (2.0 - fq);
+            double tail = 0.0, wp = pow(wmax, (double)(nmax - 1));
+            for (int m = nmax - 1; m >= 1; --m) {
+                tail += fabs(Fd[m]) * wp;
+                if (tail > 7.450580596923828e-09) break;
+                n32 = m;
+                wp /= wmax;
+            }
+        }
+        d[15] = (double)n32;
+        if (code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
+            // multipoles m = 1, 3, 4 about the EPL centre, strengths a_m =
+            // a{m}_a theta_E / sqrt(q), angles phi_m = phi + delta_phi_m
+            // (epl_multipole_m1m3m4.py:495-535); m = 1 uses r_E = theta_E
+            const double rescale = theta_E / sqrt(q);
+            const double a1 = a[6] * rescale, p1 = phi + a[7];
+            const double a3 = a[8] * rescale, p3 = phi + a[9];
+            const double a4 = a[10] * rescale, p4 = phi + a[11];
+            d[16] = a1 / 2; d[17] = cos(p1); d[18] = sin(p1); d[19] = log(theta_E);
+            d[20] = a3 / (1.0 - 9.0); d[21] = cos(3 * p3); d[22] = sin(3 * p3);
+            d[23] = a4 / (1.0 - 16.0); d[24] = cos(4 * p4); d[25] = sin(4 * p4);
+            d[26] = p1; d[27] = a3; d[28] = p3; d[29] = a4; d[30] = p4; d[31] = theta_E;
+        }
+    } else if (code == LENSGB_LENS_NFW_ELLIPSE_CSE) {
+        double Rs = a[0], alpha_Rs = a[1], e1 = a[2], e2 = a[3];
+        double phi, q;
+        ellip_phi_q(e1, e2, phi, q);
+        double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+        d[RD_CX] = a[4];
+        d[RD_CY] = a[5];
+        d[2] = Rs; d[3] = 1.0 / Rs; d[4] = q; d[5] = cos(phi); d[6] = sin(phi);
+        d[7] = sqrt(q); d[8] = 4.0 * CSE_NFW_TERMS; d[9] = 4 * rho0 * Rs * Rs * Rs / Rs;
+        d[10] = q * q; d[11] = 1.0 - q * q;
+        // per-term constants of the FP32 path, one float4 per term:
+        // (q^2 s^2, s, q^2 s, a/s)
+        double* Cd = Fd;
+        float* Cf = Ff;
+        for (int k = 0; k < CSE_NFW_TERMS; ++k) {
+            const double s = kCseNfwS[k], ak = kCseNfwA[k];
+            const double v[4] = {q * q * s * s, s, q * q * s, ak / s};
+            for (int j = 0; j < 4; ++j) {
+                Cd[4 * k + j] = v[j];
+                Cf[4 * k + j] = (float)v[j];
+            }
+        }
+    } else if (code == LENSGB_LENS_SHEAR) {
+        d[RD_CX] = a[2];
+        d[RD_CY] = a[3];
+        d[2] = a[0]; d[3] = a[1];
+    } else if (code == LENSGB_LENS_NFW) {
+        double Rs = a[0], alpha_Rs = a[1];
+        double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+        double Rsf = Rs < 0.0000001 ? 0.0000001 : Rs;
+        d[RD_CX] = a[2];
+        d[RD_CY] = a[3];
+        d[2] = Rsf; d[3] = rho0; d[4] = 4 * rho0 * Rsf; d[5] = 1.0 / Rsf;
+    } else if (code == LENSGB_LENS_TNFW) {
+        double Rs = a[0], alpha_Rs = a[1], r_trunc = a[2];
+        double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
+        d[RD_CX] = a[3];
+        d[RD_CY] = a[4];
+        d[2] = Rs; d[3] = rho0; d[4] = r_trunc / Rs; d[5] = 4 * rho0 * Rs; d[6] = 1.0 / Rs;
+    }
+}
+
+// Record of light profile `code` (SERSIC / SERSIC_ELLIPSE) from its kwargs a[].
+__device__ void prepare_light_record(int code, const double* a, double* d) {
+    // SERSIC / SERSIC_ELLIPSE
+    double amp = a[0], R_sersic = a[1], n = a[2];
+    double e1 = 0, e2 = 0, cx, cy;
+    if (code == LENSGB_LIGHT_SERSIC_ELLIPSE) {
+        e1 = a[3]; e2 = a[4]; cx = a[5]; cy = a[6];
+    } else {
+        cx = a[3]; cy = a[4];
+    }
+    R_sersic = R_sersic > 0 ? R_sersic : 0;          // sersic_ellipse.py:88
+    double Rs_ = R_sersic > 0.0001 ? R_sersic : 0.0001;  // _R_stable
+    double bn = 1.9992 * n - 0.3271;
+    bn = bn > 0.00001 ? bn : 0.00001;
+    double norm = sqrt(fabs(1 - e1 * e1 - e2 * e2));
+    norm = norm > 0.000001 ? norm : 0.000001;
+    d[RD_CX] = cx;
+    d[RD_CY] = cy;
+    d[2] = amp; d[3] = Rs_; d[4] = 1.0 / Rs_; d[5] = 1.0 / n; d[6] = bn;
+    d[7] = (1 - e1) / norm; d[8] = -e2 / norm; d[9] = -e2 / norm; d[10] = (1 + e1) / norm;
+    // FP32-path constants: log2(1/R_s), b_n log2(e), b_n / n
+    d[11] = log2(1.0 / Rs_); d[12] = bn * 1.4426950408889634; d[13] = bn / n;
+}
+
+// FP32 copy of a record (float slot k + 2 mirrors double slot k >= 2).
+__device__ void finish_record_f(const double* d, float* f) {
+    for (int k = 2; k + F_OFF < REC_F && k < REC_D; ++k) f[k + F_OFF] = (float)d[k];
+}
+
 __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                                int n_inst, double* __restrict__ rec_d, float* __restrict__ rec_f,
                                double* __restrict__ coef_d, float* __restrict__ coef_f) {
@@ -66,142 +210,14 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
     const double* a = P + off;
 
     if (kind == 0) {
-        if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
-            double theta_E = a[0], e1 = a[1], e2 = a[2];
-            double s_scale = code == LENSGB_LENS_SIE ? 0.0000000001 : a[3];
-            int co = code == LENSGB_LENS_SIE ? 3 : 4;
-            double phi, q;
-            ellip_phi_q(e1, e2, phi, q);
-            double theta_E_conv = theta_E / sqrt((1.0 + q * q) / (2.0 * q));
-            double b = theta_E_conv * sqrt((1 + q * q) / 2);
-            double s = s_scale / sqrt(q);
-            double qc = q >= 1 ? 0.99999999 : q;   // NIEMajorAxis.derivatives clamp
-            double sq = sqrt(1.0 - qc * qc);
-            d[RD_CX] = a[co];
-            d[RD_CY] = a[co + 1];
-            d[2] = b; d[3] = s; d[4] = qc; d[5] = cos(phi); d[6] = sin(phi);
-            d[7] = sq; d[8] = b / sq; d[9] = qc * qc; d[10] = qc * qc * s; d[11] = qc * qc * s * s;
-        } else if (code == LENSGB_LENS_EPL || code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
-            double theta_E = a[0], gamma = a[1], e1 = a[2], e2 = a[3];
-            double phi, q;
-            ellip_phi_q(e1, e2, phi, q);
-            double t = gamma - 1;
-            double b = theta_E * sqrt(q);
-            double fq = (1.0 - q) / (1.0 + q);
-            int nmax = epl_nmax_of(fq);
-            d[RD_CX] = a[4];
-            d[RD_CY] = a[5];
-            d[2] = b; d[3] = t; d[4] = q; d[5] = cos(phi); d[6] = sin(phi); d[7] = fq;
-            d[8] = (double)nmax; d[9] = 2.0 / (1.0 + q) * pow(b, t);
-            // FP32-path constants: f^2/4, f/2, -t/2
-            d[12] = 0.25 * fq * fq; d[13] = 0.5 * fq; d[14] = -0.5 * t;
-            int slot_e = st.epl_slot[p];
-            double* Fd = coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
-            float* Ff = coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
-            // F_0 = 1, F_1 = 1 - 2B/C, F_n = ((n-1) F_{n-2} - (2B-C) F_{n-1}) / (C+n-1)
-            double B = t / 2.0, C = 2.0 - B;
-            double fpp = 1.0, fp = 1.0 - 2.0 * B / C;
-            if (nmax > 0) { Fd[0] = fpp; Ff[0] = (float)fpp; }
-            if (nmax > 1) { Fd[1] = fp; Ff[1] = (float)fp; }
-            for (int n = 2; n < nmax; ++n) {
-                double fn = ((n - 1.0) * fpp - (2.0 * B - C) * fp) / (C + n - 1.0);
-                Fd[n] = fn;
-                Ff[n] = (float)fn;
-                fpp = fp;
-                fp = fn;
-            }
-            // FP32 series length: since |w| <= f/(2-f), the terms n >= k change the
-            // sum by at most sum_{m>=k} |F_m| (f/(2-f))^m; stop once that bound is
-            // below 2^-27 (under FP32 resolution), never beyond the reference's nmax.
-            int n32 = nmax;
-            if (nmax > 1) {
-                const double wmax = fq / (2.0 - fq);
-                double tail = 0.0, wp = pow(wmax, (double)(nmax - 1));
-                for (int m = nmax - 1; m >= 1; --m) {
-                    tail += fabs(Fd[m]) * wp;
-                    if (tail > 7.450580596923828e-09) break;
-                    n32 = m;
-                    wp /= wmax;
-                }
-            }
-            d[15] = (double)n32;
-            if (code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
-                // multipoles m = 1, 3, 4 about the EPL centre, strengths a_m =
-                // a{m}_a theta_E / sqrt(q), angles phi_m = phi + delta_phi_m
-                // (epl_multipole_m1m3m4.py:495-535); m = 1 uses r_E = theta_E
-                const double rescale = theta_E / sqrt(q);
-                const double a1 = a[6] * rescale, p1 = phi + a[7];
-                const double a3 = a[8] * rescale, p3 = phi + a[9];
-                const double a4 = a[10] * rescale, p4 = phi + a[11];
-                d[16] = a1 / 2; d[17] = cos(p1); d[18] = sin(p1); d[19] = log(theta_E);
-                d[20] = a3 / (1.0 - 9.0); d[21] = cos(3 * p3); d[22] = sin(3 * p3);
-                d[23] = a4 / (1.0 - 16.0); d[24] = cos(4 * p4); d[25] = sin(4 * p4);
-                d[26] = p1; d[27] = a3; d[28] = p3; d[29] = a4; d[30] = p4; d[31] = theta_E;
-            }
-        } else if (code == LENSGB_LENS_NFW_ELLIPSE_CSE) {
-            double Rs = a[0], alpha_Rs = a[1], e1 = a[2], e2 = a[3];
-            double phi, q;
-            ellip_phi_q(e1, e2, phi, q);
-            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
-            d[RD_CX] = a[4];
-            d[RD_CY] = a[5];
-            d[2] = Rs; d[3] = 1.0 / Rs; d[4] = q; d[5] = cos(phi); d[6] = sin(phi);
-            d[7] = sqrt(q); d[8] = 4.0 * CSE_NFW_TERMS; d[9] = 4 * rho0 * Rs * Rs * Rs / Rs;
-            d[10] = q * q; d[11] = 1.0 - q * q;
-            // per-term constants of the FP32 path, one float4 per term:
-            // (q^2 s^2, s, q^2 s, a/s)
-            int slot_e = st.epl_slot[p];
-            double* Cd = coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
-            float* Cf = coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX;
-            for (int k = 0; k < CSE_NFW_TERMS; ++k) {
-                const double s = kCseNfwS[k], ak = kCseNfwA[k];
-                const double v[4] = {q * q * s * s, s, q * q * s, ak / s};
-                for (int j = 0; j < 4; ++j) {
-                    Cd[4 * k + j] = v[j];
-                    Cf[4 * k + j] = (float)v[j];
-                }
-            }
-        } else if (code == LENSGB_LENS_SHEAR) {
-            d[RD_CX] = a[2];
-            d[RD_CY] = a[3];
-            d[2] = a[0]; d[3] = a[1];
-        } else if (code == LENSGB_LENS_NFW) {
-            double Rs = a[0], alpha_Rs = a[1];
-            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
-            double Rsf = Rs < 0.0000001 ? 0.0000001 : Rs;
-            d[RD_CX] = a[2];
-            d[RD_CY] = a[3];
-            d[2] = Rsf; d[3] = rho0; d[4] = 4 * rho0 * Rsf; d[5] = 1.0 / Rsf;
-        } else if (code == LENSGB_LENS_TNFW) {
-            double Rs = a[0], alpha_Rs = a[1], r_trunc = a[2];
-            double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
-            d[RD_CX] = a[3];
-            d[RD_CY] = a[4];
-            d[2] = Rs; d[3] = rho0; d[4] = r_trunc / Rs; d[5] = 4 * rho0 * Rs; d[6] = 1.0 / Rs;
-        }
+        const int slot_e = st.epl_slot[p];
+        double* Fd = slot_e >= 0 ? coef_d + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX : nullptr;
+        float* Ff = slot_e >= 0 ? coef_f + ((long long)inst * st.n_epl + slot_e) * EPL_NMAX : nullptr;
+        prepare_lens_record(code, a, d, Fd, Ff);
     } else {
-        // SERSIC / SERSIC_ELLIPSE
-        double amp = a[0], R_sersic = a[1], n = a[2];
-        double e1 = 0, e2 = 0, cx, cy;
-        if (code == LENSGB_LIGHT_SERSIC_ELLIPSE) {
-            e1 = a[3]; e2 = a[4]; cx = a[5]; cy = a[6];
-        } else {
-            cx = a[3]; cy = a[4];
-        }
-        R_sersic = R_sersic > 0 ? R_sersic : 0;          // sersic_ellipse.py:88
-        double Rs_ = R_sersic > 0.0001 ? R_sersic : 0.0001;  // _R_stable
-        double bn = 1.9992 * n - 0.3271;
-        bn = bn > 0.00001 ? bn : 0.00001;
-        double norm = sqrt(fabs(1 - e1 * e1 - e2 * e2));
-        norm = norm > 0.000001 ? norm : 0.000001;
-        d[RD_CX] = cx;
-        d[RD_CY] = cy;
-        d[2] = amp; d[3] = Rs_; d[4] = 1.0 / Rs_; d[5] = 1.0 / n; d[6] = bn;
-        d[7] = (1 - e1) / norm; d[8] = -e2 / norm; d[9] = -e2 / norm; d[10] = (1 + e1) / norm;
-        // FP32-path constants: log2(1/R_s), b_n log2(e), b_n / n
-        d[11] = log2(1.0 / Rs_); d[12] = bn * 1.4426950408889634; d[13] = bn / n;
+        prepare_light_record(code, a, d);
     }
-    for (int k = 2; k + F_OFF < REC_F && k < REC_D; ++k) f[k + F_OFF] = (float)d[k];
+    finish_record_f(d, f);
     write_offsets(g, d[RD_CX], d[RD_CY], f);
 }
 

@@ -241,6 +241,98 @@ def epl_nmax(e1, e2):
     return out
 
 
+# Substructure ray shooting (LensModelBulk): 1000^2 rays at 0.01"/pix through
+# EPL + SHEAR + 2000 TNFW subhalos.  Per (ray, TNFW) pair 35 flop and 8 T,
+# counted from the reference formulas (tnfw.py:69-87,228-349).
+FLOP_TNFW, T_TNFW = 35, 8
+SUB_PIX, SUB_DPIX, SUB_N = 1000, 0.01, 2000
+
+
+def substructure_section(steps, warmup, fp32_peak, flush):
+    """FP32 bulk ray shooting rate, FP32-vs-FP64 deflection and image error,
+    FP64-vs-oracle on a ray sample, and the oracle's CPU rate on a sample."""
+    import numpy as np
+    import torch
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import workloads as W
+    from oracle import lens as olens
+
+    x, y, ll, kw, src = W.substructure(num_pix=SUB_PIX, delta_pix=SUB_DPIX, n_sub=SUB_N)
+    unique = ["EPL", "SHEAR", "TNFW"]
+    b32 = J.LensModelBulk(unique, precision="fp32")
+    b64 = J.LensModelBulk(unique, precision="fp64")
+    rk = b32.prepare_ray_shooting_kwargs(ll, kw)
+    rk_dev = {"all_kwargs": {k: torch.as_tensor(v).cuda() for k, v in rk["all_kwargs"].items()},
+              "index_list": torch.as_tensor(rk["index_list"]).cuda()}
+    xt = torch.as_tensor(x).cuda()
+    yt = torch.as_tensor(y).cuda()
+    stream = torch.cuda.current_stream()
+    for _ in range(max(warmup, 3)):
+        b32.ray_shooting(xt, yt, rk_dev)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(steps, 3)):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bx32, by32 = b32.ray_shooting(xt, yt, rk_dev)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    bx64, by64 = b64.ray_shooting(xt, yt, rk_dev)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1)
+    d = torch.maximum((bx32 - bx64).abs(), (by32 - by64).abs())
+    lm = J.LightModel(["SERSIC_ELLIPSE"])
+    s32 = lm.surface_brightness(bx32, by32, src)
+    s64 = lm.surface_brightness(bx64, by64, src)
+    sig = s64.abs() >= 1e-3 * s64.abs().max()
+    rel = ((s32 - s64).abs()[sig] / s64.abs()[sig])
+    # FP64 vs the oracle on a ray sample
+    sample = np.arange(0, x.size, x.size // 256)[:256]
+    ox, oy = olens.bulk_ray_shooting(unique, x[sample], y[sample], rk["all_kwargs"],
+                                     rk["index_list"])
+    g64x = bx64.cpu().numpy()[sample]
+    g64y = by64.cpu().numpy()[sample]
+    orc = max(np.max(np.abs(g64x - ox) / np.maximum(np.abs(ox), 1e-300)),
+              np.max(np.abs(g64y - oy) / np.maximum(np.abs(oy), 1e-300)))
+    # oracle CPU rate on a ray sample (1 core, vectorised over rays)
+    cs = np.arange(0, x.size, x.size // 2000)[:2000]
+    t0 = time.perf_counter()
+    olens.bulk_ray_shooting(unique, x[cs], y[cs], rk["all_kwargs"], rk["index_list"])
+    cpu_s = time.perf_counter() - t0
+    n_pairs = x.size * len(ll)
+    flop = x.size * SUB_N * FLOP_TNFW
+    return {
+        "workload": "substructure_1000x1000_epl_shear_2000tnfw",
+        "rays": int(x.size), "deflectors": len(ll),
+        "ms_per_call": ms, "rays_per_s": x.size / (ms / 1e3),
+        "pairs_per_s": n_pairs / (ms / 1e3),
+        "fp64_ms_per_call": ms64, "speedup_vs_fp64": ms64 / ms,
+        "beta_err_fp32_vs_fp64_arcsec_max": d.max().item(),
+        "beta_err_fp32_vs_fp64_arcsec_median": d.median().item(),
+        "image_rel_err_fp32_vs_fp64_max": rel.max().item(),
+        "image_rel_err_fp32_vs_fp64_median": rel.median().item(),
+        "fp64_vs_oracle_rel_err_max": float(orc),
+        "roofline": {"kernel": "bulk_ray_kernel<FP32>", "bound": "fp32", "unit": "TFLOP/s",
+                     "achieved": flop / (ms / 1e3) / 1e12, "peak": fp32_peak,
+                     "frac": flop / (ms / 1e3) / 1e12 / fp32_peak,
+                     "algorithmic_gflop_per_launch": flop / 1e9,
+                     "transcendentals_per_s": x.size * SUB_N * T_TNFW / (ms / 1e3)},
+        "cpu_baseline": {"value": cs.size / cpu_s, "unit": "rays/s", "cores": 1, "kind": "port",
+                         "sample": "%d rays x %d deflectors, FP64 NumPy oracle "
+                                   "(SinglePlaneBulk restatement), vectorised over rays"
+                                   % (cs.size, len(ll))},
+        "timing": "CUDA events per call after %d warm-ups, L2 flushed before each" % max(warmup, 3),
+    }
+
+
 def percentile(v, q):
     v = sorted(v)
     k = (len(v) - 1) * q
@@ -426,7 +518,8 @@ def gpu_arm(args):
         sm_mhz = clk.get("sm_mhz") or 2070.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s at the sampled clock
         extra["roofline"] = {
-            "kernel": "raytrace_kernel<float>", "bound": "fp32", "unit": "TFLOP/s",
+            "kernel": "raytrace_fp32_kernel (with prepare_kernel and refine_kernel)",
+            "bound": "fp32", "unit": "TFLOP/s",
             "achieved": flop_ray / rt / 1e12, "peak": fp32_peak,
             "frac": flop_ray / rt / 1e12 / fp32_peak,
             "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2) at the sampled "
@@ -442,7 +535,7 @@ def gpu_arm(args):
             pass
         conv_bytes = B * N_PIX * N_PIX * 4 * 2 + B * KSIZE * KSIZE * 4
         extra["roofline_conv"] = {
-            "kernel": "conv_kernel<float>", "bound": "fp32", "unit": "TFLOP/s",
+            "kernel": "conv_f32_kernel", "bound": "fp32", "unit": "TFLOP/s",
             "achieved": flop_conv / cv / 1e12, "peak": fp32_peak,
             "frac": flop_conv / cv / 1e12 / fp32_peak, "launch_ms": cv * 1e3,
             "hbm_gbs": conv_bytes / cv / 1e9, "hbm_frac_of_measured": conv_bytes / cv / 1e9 / hbm_peak,
@@ -480,6 +573,11 @@ def gpu_arm(args):
                         "path": "ImageModel.image_batch -> lensgb_image, pinned host rows/PSFs "
                                 "in, images out, one stream"}
 
+        # --- substructure ray shooting (LensModelBulk, FP32 subhalo terms)
+        if not args.no_sub:
+            extra["substructure"] = substructure_section(args.steps, args.warmup, fp32_peak,
+                                                         flush)
+
         # --- CPU baseline (oracle port, bounded sample)
         if pool is not None:
             n_img = 4 * cores
@@ -506,7 +604,7 @@ def gpu_arm(args):
                                  "max over ranks"},
             "latency_ms_p50": percentile(step_ms, 0.5), "latency_ms_p99": percentile(step_ms, 0.99),
             "wall_s_timed_region": t_wall,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }
         line.update(extra)
@@ -525,6 +623,7 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sub", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -209,6 +209,44 @@ int lensgb_surface_brightness(const lensgb_model* model, int which, const double
                               const double* x_dev, const double* y_dev, double* out_dev,
                               long long n, void* stream);
 
+/* ---- many-deflector ray shooting --------------------------------------- */
+/* LensModelBulk(unique_lens_model_list, multi_plane=False)
+ * (jaxtronomy/LensModel/lens_model_bulk.py:18-128) -> SinglePlaneBulk
+ * (single_plane_bulk.py:20-131).  A bulk handle holds the unique profile
+ * codes; each call ray-shoots n points through n_deflectors deflectors:
+ *   index_dev   int32[n_deflectors]: position of each deflector's profile in
+ *               the unique list; n_unique (or larger) is the NULL profile and
+ *               negative values select entry 0, as lax.switch clamps
+ *               (the reference's index_list, single_plane_bulk.py:93-95)
+ *   params_dev  double[n_deflectors][LENSGB_BULK_PARAM_STRIDE]: each
+ *               deflector's kwargs in its profile's param_names order (the
+ *               table at the top), unused columns ignored (the reference's
+ *               all_kwargs dict of arrays, single_plane_bulk.py:97-106)
+ *   beta = x - sum_i alpha_i(x)               (single_plane_bulk.py:128-131)
+ * Precision LENSGB_FP64 evaluates every term in FP64.  LENSGB_FP32_SPLIT
+ * evaluates a deflector's terms in FP32 when its deflection is bounded by
+ * fp32_alpha_max (|alpha| <= theta_E for SIE/NIE/EPL/EPL_MULTIPOLE_M1M3M4,
+ * <= 2 alpha_Rs for NFW/TNFW/NFW_ELLIPSE_CSE; SHEAR never), sums those terms
+ * in FP32 over chunks of 64 deflectors and accumulates the chunk sums, and
+ * every FP64 term, in FP64.  The handle owns grow-only device scratch
+ * (about 300 B per deflector, plus 6 KB per deflector when an EPL-type or
+ * NFW_ELLIPSE_CSE profile is in the unique list) and serves one stream at a
+ * time. */
+#define LENSGB_LENS_NULL 0 /* the reference's "NULL" profile: no deflection */
+#define LENSGB_BULK_MAX_UNIQUE 16
+#define LENSGB_BULK_PARAM_STRIDE 12
+
+typedef struct lensgb_bulk lensgb_bulk;
+
+int lensgb_bulk_create(const int* unique_codes, int n_unique, int precision,
+                       lensgb_bulk** out);
+int lensgb_bulk_destroy(lensgb_bulk* bulk);
+/* Largest deflection bound (arcsec) evaluated in FP32 (default 0.05). */
+int lensgb_bulk_set_fp32_alpha_max(lensgb_bulk* bulk, double alpha_max);
+int lensgb_bulk_ray_shooting(lensgb_bulk* bulk, const int* index_dev, const double* params_dev,
+                             int n_deflectors, const double* x_dev, const double* y_dev,
+                             double* beta_x_dev, double* beta_y_dev, long long n, void* stream);
+
 /* Description of the last error on the calling thread ("" if none). */
 const char* lensgb_last_error(void);
 

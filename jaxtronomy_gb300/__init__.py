@@ -8,8 +8,9 @@ C ABI, ``include/lensgb.h``); build it with ``python -m jaxtronomy_gb300.build``
 from .data import ImageData, PSF, PixelGrid  # noqa: F401
 from .image_model import ImageModel  # noqa: F401
 from .lens_model import LensModel  # noqa: F401
+from .lens_model_bulk import LensModelBulk  # noqa: F401
 from .light_model import LightModel  # noqa: F401
 
 __version__ = "0.1.0"
 
-__all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LightModel"]
+__all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LensModelBulk", "LightModel"]

@@ -20,6 +20,9 @@ ERR_OOM = 3
 ERR_CUDA = 4
 
 # profile codes
+LENS_NULL = 0
+BULK_MAX_UNIQUE = 16
+BULK_PARAM_STRIDE = 12
 LENS_CODES = {"SIE": 1, "NIE": 2, "EPL": 3, "SHEAR": 4, "NFW": 5, "TNFW": 6,
               "NFW_ELLIPSE_CSE": 7, "EPL_MULTIPOLE_M1M3M4": 8}
 LIGHT_CODES = {"SERSIC": 1, "SERSIC_ELLIPSE": 2}
@@ -38,6 +41,8 @@ SYMBOLS = [
     "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
+    "lensgb_bulk_create", "lensgb_bulk_destroy", "lensgb_bulk_set_fp32_alpha_max",
+    "lensgb_bulk_ray_shooting",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -123,6 +128,14 @@ def load():
     lib.lensgb_alpha.restype = i
     lib.lensgb_surface_brightness.argtypes = [vp, i, dp, dp, dp, dp, ll, vp]
     lib.lensgb_surface_brightness.restype = i
+    lib.lensgb_bulk_create.argtypes = [ctypes.POINTER(ctypes.c_int), i, i, ctypes.POINTER(vp)]
+    lib.lensgb_bulk_create.restype = i
+    lib.lensgb_bulk_destroy.argtypes = [vp]
+    lib.lensgb_bulk_destroy.restype = i
+    lib.lensgb_bulk_set_fp32_alpha_max.argtypes = [vp, ctypes.c_double]
+    lib.lensgb_bulk_set_fp32_alpha_max.restype = i
+    lib.lensgb_bulk_ray_shooting.argtypes = [vp, vp, dp, i, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_bulk_ray_shooting.restype = i
     lib.lensgb_last_error.argtypes = []
     lib.lensgb_last_error.restype = ctypes.c_char_p
     lib.lensgb_version.argtypes = []
@@ -162,6 +175,34 @@ class Model:
     def close(self):
         if self._h:
             load().lensgb_model_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Bulk:
+    """Owner of one lensgb_bulk handle (unique profile codes + scratch)."""
+
+    def __init__(self, codes, precision, fp32_alpha_max=None):
+        lib = load()
+        arr = (ctypes.c_int * max(1, len(codes)))(*codes)
+        h = ctypes.c_void_p()
+        check(lib.lensgb_bulk_create(arr, len(codes), int(precision), ctypes.byref(h)))
+        self._h = h
+        if fp32_alpha_max is not None:
+            check(lib.lensgb_bulk_set_fp32_alpha_max(h, float(fp32_alpha_max)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            load().lensgb_bulk_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

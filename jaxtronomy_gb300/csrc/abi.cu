@@ -144,7 +144,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 101; }
+int lensgb_version(void) { return 102; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -428,6 +428,124 @@ int lensgb_surface_brightness(const lensgb_model* mc, int which, const double* p
     if ((rc = check_cuda("prepare launch"))) return rc;
     launch_light_points(st, 0, m->rec_d, x, y, out, n, s);
     return check_cuda("surface brightness launch");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Bulk handle: LensModelBulk / SinglePlaneBulk (lens_model_bulk.py:18-128,
+// single_plane_bulk.py:20-131) with grow-only per-deflector scratch.
+// ---------------------------------------------------------------------------
+struct lensgb_bulk {
+    BulkUnique u;
+    int precision;
+    double fp32_alpha_max = 0.05;
+    bool need_coef = false;  // an EPL-type or NFW_ELLIPSE_CSE profile is in the list
+    int cap = 0;
+    int* tag = nullptr;
+    double* rec_d = nullptr;
+    float* rec_f = nullptr;
+    double* coef_d = nullptr;
+    float* coef_f = nullptr;
+};
+
+static void bulk_free(lensgb_bulk* b) {
+    cudaFree(b->tag);
+    cudaFree(b->rec_d);
+    cudaFree(b->rec_f);
+    cudaFree(b->coef_d);
+    cudaFree(b->coef_f);
+    b->tag = nullptr;
+    b->rec_d = nullptr;
+    b->rec_f = nullptr;
+    b->coef_d = nullptr;
+    b->coef_f = nullptr;
+    b->cap = 0;
+}
+
+static int bulk_ensure(lensgb_bulk* b, int n_defl) {
+    if (n_defl <= b->cap) return LENSGB_OK;
+    bulk_free(b);
+    const size_t n = (size_t)n_defl;
+    bool ok = cudaMalloc(&b->tag, n * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&b->rec_d, n * REC_D * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&b->rec_f, n * REC_F * sizeof(float)) == cudaSuccess;
+    if (ok && b->need_coef)
+        ok = cudaMalloc(&b->coef_d, n * EPL_NMAX * sizeof(double)) == cudaSuccess &&
+             cudaMalloc(&b->coef_f, n * EPL_NMAX * sizeof(float)) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        bulk_free(b);
+        return fail(LENSGB_ERR_OOM, "bulk scratch allocation failed for " +
+                                        std::to_string(n_defl) + " deflectors");
+    }
+    b->cap = n_defl;
+    return LENSGB_OK;
+}
+
+extern "C" {
+
+int lensgb_bulk_create(const int* codes, int n_unique, int precision, lensgb_bulk** out) {
+    if (!out) return fail(LENSGB_ERR_INVALID, "null output handle pointer");
+    *out = nullptr;
+    if (n_unique < 0 || n_unique > LENSGB_BULK_MAX_UNIQUE)
+        return fail(LENSGB_ERR_INVALID, "n_unique must be in [0, " +
+                                            std::to_string(LENSGB_BULK_MAX_UNIQUE) + "]");
+    if (n_unique > 0 && !codes) return fail(LENSGB_ERR_INVALID, "null unique code list");
+    if (precision != LENSGB_FP64 && precision != LENSGB_FP32_SPLIT)
+        return fail(LENSGB_ERR_UNSUPPORTED, "unknown precision " + std::to_string(precision));
+    lensgb_bulk* b = new lensgb_bulk();
+    b->u.n = n_unique;
+    b->precision = precision;
+    for (int k = 0; k < LENSGB_BULK_MAX_UNIQUE; ++k) b->u.code[k] = LENSGB_LENS_NULL;
+    for (int k = 0; k < n_unique; ++k) {
+        const int c = codes[k];
+        if (c != LENSGB_LENS_NULL && lens_param_count(c) < 0) {
+            delete b;
+            return fail(LENSGB_ERR_UNSUPPORTED, "unknown lens profile code " + std::to_string(c));
+        }
+        b->u.code[k] = c;
+        if (c == LENSGB_LENS_EPL || c == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4 ||
+            c == LENSGB_LENS_NFW_ELLIPSE_CSE)
+            b->need_coef = true;
+    }
+    *out = b;
+    return LENSGB_OK;
+}
+
+int lensgb_bulk_destroy(lensgb_bulk* b) {
+    if (!b) return LENSGB_OK;
+    bulk_free(b);
+    delete b;
+    return LENSGB_OK;
+}
+
+int lensgb_bulk_set_fp32_alpha_max(lensgb_bulk* b, double alpha_max) {
+    if (!b) return fail(LENSGB_ERR_INVALID, "null bulk handle");
+    if (!(alpha_max >= 0.0)) return fail(LENSGB_ERR_INVALID, "alpha_max must be >= 0");
+    b->fp32_alpha_max = alpha_max;
+    return LENSGB_OK;
+}
+
+int lensgb_bulk_ray_shooting(lensgb_bulk* b, const int* index, const double* params, int n_defl,
+                             const double* x, const double* y, double* bx, double* by,
+                             long long n, void* stream) {
+    if (!b) return fail(LENSGB_ERR_INVALID, "null bulk handle");
+    if (n_defl < 0) return fail(LENSGB_ERR_INVALID, "negative deflector count");
+    if (n < 0) return fail(LENSGB_ERR_INVALID, "negative point count");
+    if (n == 0) return LENSGB_OK;
+    if (!x || !y || !bx || !by) return fail(LENSGB_ERR_INVALID, "null coordinate pointer");
+    if (n_defl > 0 && (!index || !params))
+        return fail(LENSGB_ERR_INVALID, "null index or params pointer");
+    int rc = bulk_ensure(b, n_defl);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_bulk_prepare(b->u, index, params, n_defl, b->fp32_alpha_max, b->tag, b->rec_d,
+                        b->rec_f, b->coef_d, b->coef_f, s);
+    if ((rc = check_cuda("bulk prepare launch"))) return rc;
+    launch_bulk_ray_shooting(b->tag, b->rec_d, b->rec_f, b->coef_d, b->coef_f, n_defl, x, y, bx,
+                             by, n, b->precision, s);
+    return check_cuda("bulk ray shooting launch");
 }
 
 }  // extern "C"

@@ -64,6 +64,18 @@ struct RefineArgs {
     float kappa;                // FP32 relative error bound of |alpha| (units of 1)
 };
 
+// Unique profile codes of a bulk handle (LensModelBulk's unique_lens_model_list);
+// index u.n stands for the NULL profile.
+struct BulkUnique {
+    int n;
+    int code[LENSGB_BULK_MAX_UNIQUE];
+};
+
+// Per-deflector tag of a bulk call: profile code in the low byte, plus this
+// flag when the deflector's terms run in FP64.
+constexpr int BULK_TAG_FP64 = 0x100;
+constexpr int BULK_CODE_MASK = 0xff;
+
 // ---------------------------------------------------------------------------
 // FP32 error-free transforms (Knuth TwoSum, Dekker split)
 // ---------------------------------------------------------------------------

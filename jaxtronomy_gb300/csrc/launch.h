@@ -51,4 +51,19 @@ int launch_ray_shoot_points(const StackDesc& st, const double* rec_d, const doub
 int launch_light_points(const StackDesc& st, int which, const double* rec_d, const double* x,
                         const double* y, double* out, long long n, cudaStream_t stream);
 
+// Many-deflector ray shooting (LensModelBulk).  The prepare step turns
+// n_defl kwargs rows (LENSGB_BULK_PARAM_STRIDE doubles each) into records and
+// tags; coef_d/coef_f hold EPL_NMAX entries per deflector (or are null when
+// no unique profile needs a coefficient table).
+int launch_bulk_prepare(const BulkUnique& u, const int* index, const double* params, int n_defl,
+                        double fp32_alpha_max, int* tag, double* rec_d, float* rec_f,
+                        double* coef_d, float* coef_f, cudaStream_t stream);
+// beta = x - sum_i alpha_i(x) over n rays.  precision FP64: every term in
+// FP64; FP32_SPLIT: deflectors without BULK_TAG_FP64 run in FP32, summed in
+// FP32 per chunk of deflectors and accumulated in FP64.
+int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* rec_f,
+                             const double* coef_d, const float* coef_f, int n_defl,
+                             const double* x, const double* y, double* bx, double* by,
+                             long long n, int precision, cudaStream_t stream);
+
 }  // namespace lensgb

@@ -235,3 +235,66 @@ int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params,
 }
 
 }  // namespace lensgb
+
+namespace lensgb {
+
+// Bound on |alpha| of one deflector, the quantity that decides whether its
+// terms may run in FP32 (deflection scale theta_E of the power laws; NFW-type
+// deflections peak near 1.01 alpha_Rs, doubled for ellipticity).  SHEAR grows
+// without bound away from its origin and always runs in FP64.
+__device__ static double bulk_alpha_bound(int code, const double* a) {
+    switch (code) {
+        case LENSGB_LENS_SIE:
+        case LENSGB_LENS_NIE:
+        case LENSGB_LENS_EPL:
+        case LENSGB_LENS_EPL_MULTIPOLE_M1M3M4: return fabs(a[0]);
+        case LENSGB_LENS_NFW:
+        case LENSGB_LENS_TNFW:
+        case LENSGB_LENS_NFW_ELLIPSE_CSE: return 2.0 * fabs(a[1]);
+        default: return INFINITY;
+    }
+}
+
+// One thread per deflector of a bulk call (SinglePlaneBulk.ray_shooting,
+// single_plane_bulk.py:109-131): index -> profile code with lax.switch's
+// clamping of out-of-range indices, record, coefficient table, and the
+// deflector's tag (code | precision flag) for the ray kernel.
+__global__ void bulk_prepare_kernel(BulkUnique u, const int* __restrict__ index,
+                                    const double* __restrict__ params, int n_defl,
+                                    double fp32_alpha_max, int* __restrict__ tag,
+                                    double* __restrict__ rec_d, float* __restrict__ rec_f,
+                                    double* __restrict__ coef_d, float* __restrict__ coef_f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_defl) return;
+    int k = index[i];
+    k = k < 0 ? 0 : (k > u.n ? u.n : k);  // slot u.n is the NULL profile
+    const int code = k < u.n ? u.code[k] : LENSGB_LENS_NULL;
+    const double* a = params + (long long)i * LENSGB_BULK_PARAM_STRIDE;
+    double* d = rec_d + (long long)i * REC_D;
+    float* f = rec_f + (long long)i * REC_F;
+    for (int j = 0; j < REC_D; ++j) d[j] = 0.0;
+    double* Fd = coef_d ? coef_d + (long long)i * EPL_NMAX : nullptr;
+    float* Ff = coef_f ? coef_f + (long long)i * EPL_NMAX : nullptr;
+    if (code != LENSGB_LENS_NULL) prepare_lens_record(code, a, d, Fd, Ff);
+    finish_record_f(d, f);
+    // FP32 split of the centre: x - c = (x_hi - c_hi) + (x_lo - c_lo) is then
+    // accurate to FP32 precision relative to the offset itself
+    split_double(d[RD_CX], f[RF_X0H], f[RF_X0L]);
+    split_double(d[RD_CY], f[RF_Y0H], f[RF_Y0L]);
+    int t = code;
+    if (code != LENSGB_LENS_NULL && !(bulk_alpha_bound(code, a) <= fp32_alpha_max))
+        t |= BULK_TAG_FP64;
+    tag[i] = t;
+}
+
+int launch_bulk_prepare(const BulkUnique& u, const int* index, const double* params, int n_defl,
+                        double fp32_alpha_max, int* tag, double* rec_d, float* rec_f,
+                        double* coef_d, float* coef_f, cudaStream_t stream) {
+    if (n_defl <= 0) return 0;
+    const int threads = 128;
+    bulk_prepare_kernel<<<(n_defl + threads - 1) / threads, threads, 0, stream>>>(
+        u, index, params, n_defl, fp32_alpha_max, tag, rec_d, rec_f, coef_d, coef_f);
+    return 0;
+}
+
+}  // namespace lensgb

@@ -24,6 +24,16 @@ LENS_PARAMS = {
                              "delta_phi_m1", "a3_a", "delta_phi_m3", "a4_a", "delta_phi_m4"],
 }
 
+# Positional order of each lens profile's ``derivatives`` signature where it
+# differs from ``param_names`` (epl_multipole_m1m3m4.py:608-622 vs :415-428).
+# The reference's bulk path binds parameter arrays positionally in param_names
+# order (profile_list_base.py:768-778), so for these profiles the bulk
+# evaluation sees the values shifted into the signature's slots.
+DERIVATIVES_SIGNATURE = {
+    "EPL_MULTIPOLE_M1M3M4": ["theta_E", "gamma", "e1", "e2", "a1_a", "delta_phi_m1", "a3_a",
+                             "delta_phi_m3", "a4_a", "delta_phi_m4", "center_x", "center_y"],
+}
+
 LIGHT_PARAMS = {
     "SERSIC": ["amp", "R_sersic", "n_sersic", "center_x", "center_y"],
     "SERSIC_ELLIPSE": ["amp", "R_sersic", "n_sersic", "e1", "e2", "center_x", "center_y"],

@@ -128,3 +128,32 @@ def instance(kwargs_list, i):
 def subset(kwargs_list, idx):
     """Batched kwargs restricted to the systems ``idx``."""
     return [{k: np.asarray(v)[idx] for k, v in kw.items()} for kw in kwargs_list]
+
+
+def substructure(seed=1004, num_pix=1000, delta_pix=0.01, n_sub=2000):
+    """Substructure ray shooting: a num_pix^2 grid of rays at delta_pix"/pix
+    (1000^2 = 1M rays at 0.01") through EPL + SHEAR (as :func:`batch_epl`) plus
+    n_sub TNFW subhalos (centres U(-2.5, 2.5)^2, Rs~U(0.01, 0.1), alpha_Rs
+    log-uniform in [1e-4, 1e-2], r_trunc = 10 Rs), then a SERSIC_ELLIPSE source
+    as in :func:`single_sie`.  Returns (x, y, lens_model_list, kwargs_lens,
+    kwargs_source) with x, y the flattened ray grid."""
+    rng = np.random.default_rng(seed)
+    e1, e2 = _ellip(rng, 0.1, 1)
+    cx, cy = rng.normal(0, 0.05, 1), rng.normal(0, 0.05, 1)
+    lens = [{"theta_E": float(rng.uniform(0.8, 1.5)), "gamma": float(rng.uniform(1.8, 2.2)),
+             "e1": float(e1[0]), "e2": float(e2[0]), "center_x": float(cx[0]),
+             "center_y": float(cy[0])},
+            {k: float(v[0]) for k, v in _shear(rng, 1).items()}]
+    sx = rng.uniform(-2.5, 2.5, n_sub)
+    sy = rng.uniform(-2.5, 2.5, n_sub)
+    rs = rng.uniform(0.01, 0.1, n_sub)
+    ars = 10.0 ** rng.uniform(-4, -2, n_sub)
+    for i in range(n_sub):
+        lens.append({"Rs": float(rs[i]), "alpha_Rs": float(ars[i]), "r_trunc": float(10 * rs[i]),
+                     "center_x": float(sx[i]), "center_y": float(sy[i])})
+    src = [{k: float(v[0]) for k, v in _sersic_source(rng, 1).items()}]
+    g = grid_kwargs(num_pix, delta_pix)
+    c = np.arange(num_pix) * delta_pix
+    xx, yy = np.meshgrid(g["ra_at_xy_0"] + c, g["dec_at_xy_0"] + c)
+    lens_list = ["EPL", "SHEAR"] + ["TNFW"] * n_sub
+    return xx.reshape(-1), yy.reshape(-1), lens_list, lens, src

@@ -384,3 +384,55 @@ def ray_shooting(lens_model_list, x, y, kwargs_list, alpha_scaling=1.0):
     """``SinglePlane.ray_shooting`` ``single_plane.py:39-56``."""
     ax, ay = alpha(lens_model_list, x, y, kwargs_list, alpha_scaling)
     return _f(x) - ax, _f(y) - ay
+
+
+# ---------------------------------------------------------------------------
+# many-deflector single-plane ray shooting
+# ---------------------------------------------------------------------------
+
+def bulk_prepare(unique_lens_model_list, lens_model_list, kwargs_lens, num_deflectors=None):
+    """``SinglePlaneBulk.prepare_ray_shooting_kwargs`` ``single_plane_bulk.py:47-106``."""
+    if len(lens_model_list) != len(kwargs_lens):
+        raise ValueError("length of lens model list and kwargs_lens do not match")
+    if num_deflectors is None:
+        num_deflectors = len(lens_model_list)
+    elif num_deflectors < len(lens_model_list):
+        raise ValueError("num_deflectors is smaller than the length of lens_model_list")
+    num_filler = num_deflectors - len(kwargs_lens)
+    index_list = [unique_lens_model_list.index(m) for m in lens_model_list]
+    index_list += [len(unique_lens_model_list)] * num_filler
+    names = set(p for m in unique_lens_model_list if m != "NULL" for p in PROFILES[m][1])
+    all_kwargs = {}
+    for k in names:
+        all_kwargs[k] = np.array([kw.get(k, 0) for kw in kwargs_lens] + [0] * num_filler,
+                                 dtype=float)
+    return {"all_kwargs": all_kwargs, "index_list": np.array(index_list)}
+
+
+def bulk_ray_shooting(unique_lens_model_list, x, y, all_kwargs, index_list):
+    """``SinglePlaneBulk.ray_shooting`` ``single_plane_bulk.py:109-131``: one
+    deflection per index (``lax.switch`` clamps the index into the unique list
+    plus the trailing NULL profile), summed over deflectors.
+
+    The reference binds each profile's arrays POSITIONALLY in ``param_names``
+    order (``_select_kwargs``, ``profile_list_base.py:768-778``).  For
+    EPL_MULTIPOLE_M1M3M4 that order (centre before the multipoles,
+    ``epl_multipole_m1m3m4.py:415-428``) differs from the ``derivatives``
+    signature (multipoles before the centre, :608-622), so in the bulk path its
+    centre values land in a1_a / delta_phi_m1 and so on; the positional call
+    below reproduces that."""
+    x = _f(x)
+    y = _f(y)
+    n_u = len(unique_lens_model_list)
+    fx = np.zeros_like(x)
+    fy = np.zeros_like(y)
+    for i, k in enumerate(np.asarray(index_list)):
+        k = min(max(int(k), 0), n_u)
+        name = unique_lens_model_list[k] if k < n_u else "NULL"
+        if name == "NULL":
+            continue
+        func, names = PROFILES[name]
+        ax, ay = func(x, y, *[float(all_kwargs[p][i]) for p in names])
+        fx = fx + ax
+        fy = fy + ay
+    return x - fx, y - fy

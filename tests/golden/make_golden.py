@@ -14,6 +14,7 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
   profiles.npz  per-profile deflections / surface brightness at seeded points
   hyp2f1.npz    hyp2f1_lopez_temme_8 at the reference's own test points
   images.npz    ImageModel.image and likelihood_data_given_model on small scenes
+  bulk.npz      LensModelBulk.ray_shooting through many deflectors
 """
 
 import json
@@ -245,6 +246,63 @@ def gen_images():
                     "scene": base["tag"]}
 
 
+def gen_bulk(rng):
+    """LensModelBulk (single plane) on a substructure scene and a mixed list."""
+    from jaxtronomy.LensModel.lens_model_bulk import LensModelBulk
+
+    cases = []
+    # main EPL + SHEAR plus TNFW subhalos drawn like the 1000^2-ray workload,
+    # padded with NULL deflectors through num_deflectors
+    n_sub = 60
+    lens_list = ["EPL", "SHEAR"] + ["TNFW"] * n_sub
+    kw = [{"theta_E": 1.2, "gamma": 2.05, "e1": 0.08, "e2": -0.05, "center_x": 0.01,
+           "center_y": -0.02},
+          {"gamma1": 0.03, "gamma2": -0.02}]
+    cx = rng.uniform(-2.5, 2.5, n_sub)
+    cy = rng.uniform(-2.5, 2.5, n_sub)
+    rs = rng.uniform(0.01, 0.1, n_sub)
+    ars = 10 ** rng.uniform(-4, -2, n_sub)
+    for i in range(n_sub):
+        kw.append({"Rs": float(rs[i]), "alpha_Rs": float(ars[i]), "r_trunc": float(10 * rs[i]),
+                   "center_x": float(cx[i]), "center_y": float(cy[i])})
+    x, y = _points(rng, 500)
+    # rays on and next to subhalo centres (the R floors)
+    x[4:10] = cx[:6] + np.array([0.0, 1e-6, 0.0, 3e-3, -0.02, 0.05])
+    y[4:10] = cy[:6] + np.array([0.0, 0.0, -2e-5, 0.0, 0.01, -0.03])
+    unique = ["EPL", "SHEAR", "TNFW"]
+    bulk = LensModelBulk(unique, multi_plane=False)
+    rk = bulk.prepare_ray_shooting_kwargs(lens_list, kw, num_deflectors=len(lens_list) + 5)
+    bx, by = bulk.ray_shooting(x, y, rk)
+    cases.append({"unique": unique, "lens_list": lens_list, "kwargs": kw,
+                  "num_deflectors": len(lens_list) + 5, "x": x, "y": y,
+                  "bx": np.asarray(bx), "by": np.asarray(by)})
+    # every profile type through the bulk switch, in mixed order
+    unique = ["TNFW", "NFW", "SIE", "EPL_MULTIPOLE_M1M3M4", "NFW_ELLIPSE_CSE", "SHEAR", "NIE"]
+    lens_list = ["SIE", "TNFW", "NFW", "TNFW", "EPL_MULTIPOLE_M1M3M4", "NFW_ELLIPSE_CSE",
+                 "SHEAR", "NIE", "NFW"]
+    kw = [{"theta_E": 0.9, "e1": 0.1, "e2": 0.05, "center_x": 0.1, "center_y": 0.0},
+          {"Rs": 0.05, "alpha_Rs": 0.003, "r_trunc": 0.4, "center_x": -0.5, "center_y": 0.7},
+          {"Rs": 0.3, "alpha_Rs": 0.05, "center_x": 1.1, "center_y": -0.4},
+          {"Rs": 0.02, "alpha_Rs": 0.0008, "r_trunc": 0.2, "center_x": 0.9, "center_y": 0.9},
+          {"theta_E": 0.4, "gamma": 1.9, "e1": -0.1, "e2": 0.12, "center_x": -1.0,
+           "center_y": -1.0, "a1_a": 0.01, "delta_phi_m1": 0.3, "a3_a": -0.005,
+           "delta_phi_m3": 1.1, "a4_a": 0.008, "delta_phi_m4": 2.4},
+          {"Rs": 6.0, "alpha_Rs": 0.7, "e1": 0.05, "e2": -0.08, "center_x": 0.0,
+           "center_y": 0.2},
+          {"gamma1": -0.02, "gamma2": 0.04, "ra_0": 0.1, "dec_0": 0.2},
+          {"theta_E": 0.2, "e1": 0.0, "e2": 0.1, "s_scale": 0.01, "center_x": 1.5,
+           "center_y": 1.5},
+          {"Rs": 0.1, "alpha_Rs": 0.01}]
+    x, y = _points(rng, 300)
+    bulk = LensModelBulk(unique, multi_plane=False)
+    rk = bulk.prepare_ray_shooting_kwargs(lens_list, kw)
+    bx, by = bulk.ray_shooting(x, y, rk)
+    cases.append({"unique": unique, "lens_list": lens_list, "kwargs": kw,
+                  "num_deflectors": None, "x": x, "y": y,
+                  "bx": np.asarray(bx), "by": np.asarray(by)})
+    return cases
+
+
 def _save(path, arrays, meta):
     np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
 
@@ -274,7 +332,16 @@ def main(reference_root):
         meta.append(sc)
     arrays["like_data"] = like.pop("data")
     _save(os.path.join(HERE, "images.npz"), arrays, {"scenes": meta, "likelihood": like})
-    print("wrote", len(cases), "profile cases,", len(scenes), "image scenes")
+
+    bulk = gen_bulk(np.random.default_rng(20240602))
+    arrays, meta = {}, []
+    for i, c in enumerate(bulk):
+        for k in ("x", "y", "bx", "by"):
+            arrays["%s_%d" % (k, i)] = c.pop(k)
+        meta.append(c)
+    _save(os.path.join(HERE, "bulk.npz"), arrays, meta)
+    print("wrote", len(cases), "profile cases,", len(scenes), "image scenes,", len(bulk),
+          "bulk cases")
 
 
 if __name__ == "__main__":

@@ -132,7 +132,9 @@ def _make_lax():
         return val
 
     def switch(index, branches, *operands):
-        return branches[int(np.asarray(index))](*operands)
+        # lax.switch clamps the index into [0, len(branches) - 1]
+        k = min(max(int(np.asarray(index)), 0), len(branches) - 1)
+        return branches[k](*operands)
 
     def cond(pred, true_fun, false_fun, *operands):
         return true_fun(*operands) if bool(np.asarray(pred)) else false_fun(*operands)

@@ -49,3 +49,14 @@ def oracle_scene(sc):
                 source_light_model_list=sc["src"], lens_light_model_list=sc["ll"],
                 flux_scaling=sc.get("flux_scaling", 1.0),
                 deflection_scaling_list=sc.get("deflection_scaling"), **g)
+
+
+def bulk_cases():
+    d, meta = load("bulk.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        for k in ("x", "y", "bx", "by"):
+            c[k] = d["%s_%d" % (k, i)]
+        out.append(c)
+    return out

@@ -120,3 +120,63 @@ def test_workloads_are_seeded_and_shaped():
     np.testing.assert_allclose(a[4].sum(axis=(1, 2)), 1.0, rtol=1e-14)
     sie = W.single_sie(batch=500)[1][0]
     assert np.hypot(sie["e1"], sie["e2"]).max() < 0.4
+
+
+def test_bulk_prepare_mirrors_reference_layout():
+    """prepare_ray_shooting_kwargs builds the reference's index list and
+    per-parameter arrays (single_plane_bulk.py:47-106), including NULL fillers."""
+    from oracle import lens as olens
+    unique = ["EPL", "SHEAR", "TNFW"]
+    lens_list = ["EPL", "TNFW", "SHEAR", "TNFW"]
+    kw = [{"theta_E": 1.0, "gamma": 2.0, "e1": 0.1, "e2": 0.0, "center_x": 0.0, "center_y": 0.0},
+          {"Rs": 0.05, "alpha_Rs": 0.01, "r_trunc": 0.5, "center_x": 1.0, "center_y": 2.0},
+          {"gamma1": 0.01, "gamma2": 0.02},
+          {"Rs": 0.02, "alpha_Rs": 0.002, "r_trunc": 0.2, "center_x": -1.0, "center_y": 0.5}]
+    b = J.LensModelBulk(unique, multi_plane=False)
+    rk = b.prepare_ray_shooting_kwargs(lens_list, kw, num_deflectors=6)
+    ref = olens.bulk_prepare(unique, lens_list, kw, 6)
+    assert list(rk["index_list"]) == [0, 2, 1, 2, 3, 3] == list(ref["index_list"])
+    assert set(rk["all_kwargs"]) == set(ref["all_kwargs"])
+    for k in ref["all_kwargs"]:
+        np.testing.assert_array_equal(rk["all_kwargs"][k], ref["all_kwargs"][k])
+    idx, rows = b.pack_rows(rk["all_kwargs"], rk["index_list"])
+    assert idx.dtype == np.int32 and rows.shape == (6, 12)
+    np.testing.assert_array_equal(rows[1, :5], [0.05, 0.01, 0.5, 1.0, 2.0])
+    np.testing.assert_array_equal(rows[2, :4], [0.01, 0.02, 0.0, 0.0])
+    assert not rows[4:].any()
+
+
+def test_bulk_pack_reproduces_positional_binding():
+    """EPL_MULTIPOLE_M1M3M4 in the bulk path: the reference binds the arrays in
+    param_names order to the derivatives signature, so the kernel row (read in
+    param_names order) receives the shifted values."""
+    b = J.LensModelBulk(["EPL_MULTIPOLE_M1M3M4"])
+    names = profiles.LENS_PARAMS["EPL_MULTIPOLE_M1M3M4"]
+    kw = [{n: float(i + 1) for i, n in enumerate(names)}]
+    rk = b.prepare_ray_shooting_kwargs(["EPL_MULTIPOLE_M1M3M4"], kw)
+    _, rows = b.pack_rows(rk["all_kwargs"], rk["index_list"])
+    sig = profiles.DERIVATIVES_SIGNATURE["EPL_MULTIPOLE_M1M3M4"]
+    # the value the reference binds to parameter `p` is the param_names value at
+    # p's position in the signature
+    for col, p in enumerate(names):
+        assert rows[0, col] == kw[0][names[sig.index(p)]]
+
+
+def test_bulk_errors_mirror_reference():
+    with pytest.raises(ValueError):
+        J.LensModelBulk(["EPL"], multi_plane=True)
+    with pytest.raises(ValueError):
+        J.LensModelBulk(["NOT_A_PROFILE"])
+    b = J.LensModelBulk(["TNFW"])
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW", "TNFW"], [{}])
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW", "TNFW"], [{}, {}], num_deflectors=1)
+
+
+def test_substructure_workload_shape():
+    x, y, ll, kw, src = W.substructure(num_pix=50, n_sub=20)
+    assert x.shape == (2500,) and len(ll) == len(kw) == 22
+    assert ll[:2] == ["EPL", "SHEAR"] and set(ll[2:]) == {"TNFW"}
+    assert np.isclose(x.max() - x.min(), 49 * 0.01)
+    assert all(k["r_trunc"] == 10 * k["Rs"] for k in kw[2:])

@@ -86,3 +86,29 @@ def test_nfw_alpha_at_Rs():
 def test_sersic_at_R_sersic_equals_amp():
     v = light.sersic(np.array([0.4]), np.array([0.0]), amp=7.0, R_sersic=0.4, n_sersic=3.0)
     np.testing.assert_allclose(v, 7.0, rtol=1e-14)
+
+
+@pytest.mark.parametrize("case", golden_io.bulk_cases(), ids=lambda c: "+".join(c["unique"]))
+def test_bulk_ray_shooting_matches_reference(case):
+    """Oracle SinglePlaneBulk vs LensModelBulk run from the reference source."""
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)
+        rk = lens.bulk_prepare(case["unique"], case["lens_list"], case["kwargs"],
+                               case["num_deflectors"])
+        bx, by = lens.bulk_ray_shooting(case["unique"], case["x"], case["y"], rk["all_kwargs"],
+                                        rk["index_list"])
+    np.testing.assert_allclose(bx, case["bx"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(by, case["by"], rtol=1e-12, atol=1e-14)
+
+
+def test_bulk_equals_single_plane_sum():
+    """Bulk ray shooting equals the LensModel sum over the same profile list
+    (EPL + SHEAR + TNFW subhalos + NULL fillers)."""
+    case = golden_io.bulk_cases()[0]
+    rk = lens.bulk_prepare(case["unique"], case["lens_list"], case["kwargs"],
+                           case["num_deflectors"])
+    bx, by = lens.bulk_ray_shooting(case["unique"], case["x"], case["y"], rk["all_kwargs"],
+                                    rk["index_list"])
+    sx, sy = lens.ray_shooting(case["lens_list"], case["x"], case["y"], case["kwargs"])
+    np.testing.assert_allclose(bx, sx, rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(by, sy, rtol=1e-13, atol=1e-15)

@@ -108,6 +108,11 @@ int lensgb_model_destroy(lensgb_model* model);
 /* Number of doubles per system row for this model. */
 int lensgb_model_param_count(const lensgb_model* model);
 
+/* Grow the model's device scratch to hold n_inst systems now, so that later
+ * calls with at most n_inst systems allocate nothing (needed before capturing
+ * those calls into a CUDA graph).  No counterpart in the reference. */
+int lensgb_model_reserve(lensgb_model* model, int n_inst);
+
 /* FP32-split models only: pixels whose predicted FP32 error exceeds `tau`
  * (relative, per supersampled ray) are recomputed in FP64.  The prediction is
  * (sum_k I_k |d ln I_k / d beta|) * kappa * (|alpha_x| + |alpha_y|) / I_ray, with
@@ -179,6 +184,7 @@ typedef struct {
     double exposure_time;         /* scalar exposure (floored at 1e-10)            */
     double background_rms;
     const double* error_map_dev;  /* additional variance map, NULL = none          */
+    long long mask_stride;        /* elements between systems' masks (0 = shared)  */
 } lensgb_noise_desc;
 
 /* ImageModel.likelihood_data_given_model for n_inst systems
@@ -246,6 +252,86 @@ int lensgb_bulk_set_fp32_alpha_max(lensgb_bulk* bulk, double alpha_max);
 int lensgb_bulk_ray_shooting(lensgb_bulk* bulk, const int* index_dev, const double* params_dev,
                              int n_deflectors, const double* x_dev, const double* y_dev,
                              double* beta_x_dev, double* beta_y_dev, long long n, void* stream);
+
+/* ---- serving loop ---------------------------------------------------------- */
+/* A server batches independent image / likelihood requests continuously: a
+ * worker thread groups released requests by bucket (identical
+ * lensgb_model_desc and noise options), keeps up to n_streams batches in
+ * flight on separate CUDA streams -- requests arriving while others run join
+ * the next batch of their bucket as soon as a stream is free -- and stages
+ * each request's parameters, PSF, data, noise map and mask in device buffers
+ * of a per-bucket execution context.  The device memory of all contexts is
+ * kept under hbm_budget_bytes by evicting idle contexts (least recently used
+ * first); requests wait in their queue while batches in flight hold the
+ * budget.  With use_graphs, a batch size that a context has run once is
+ * captured as a CUDA graph and replayed.  Each request's result is the same as
+ * a lensgb_image / lensgb_loglike call on that request alone (the kernels
+ * compute every system independently of the others in its batch).
+ * No counterpart in the reference, which simulates one jitted call at a time. */
+typedef struct lensgb_server lensgb_server;
+
+typedef struct {
+    int n_streams;              /* batches in flight at once (default 4, <= 64)        */
+    int max_batch;              /* requests per batch (default 256)                    */
+    long long hbm_budget_bytes; /* device memory of all contexts (default 4 GiB)       */
+    int contexts_per_bucket;    /* concurrent batches of one bucket (default 2)        */
+    int use_graphs;             /* replay captured CUDA graphs for repeated sizes      */
+} lensgb_server_config;
+
+typedef struct {
+    lensgb_model_desc desc;     /* the request's model (its bucket key)                    */
+    const double* params;       /* host: lensgb_model_param_count doubles (one system row) */
+    const void* psf;            /* host: kernel_size^2 values in the model precision       */
+    void* image_out;            /* host: ny x nx result in the model precision, or NULL;
+                                   page-locked buffers receive asynchronous copies          */
+    const double* data;         /* host, optional: ny x nx data -> likelihood request      */
+    const double* noise_map;    /* host, optional with data: ny x nx 1-sigma noise map     */
+    const double* mask;         /* host, optional with data: ny x nx likelihood mask       */
+    double background_rms;      /* with data (part of the bucket key)                      */
+    double exposure_time;       /* with data (part of the bucket key)                      */
+    double* logl_out;           /* host, optional with data: log-likelihood                */
+    long long release_ns;       /* not admitted before this server-clock time (0: now)     */
+} lensgb_request;
+
+#define LENSGB_REQ_QUEUED 0
+#define LENSGB_REQ_RUNNING 1
+#define LENSGB_REQ_DONE 2
+#define LENSGB_REQ_FAILED 3
+
+typedef struct {
+    long long batches;
+    long long requests_launched;
+    long long requests_done;
+    long long graph_captures;
+    long long graph_launches;
+    long long evictions;
+    long long bytes_held;
+    long long peak_bytes;
+} lensgb_server_stats;
+
+/* cfg may be NULL (defaults); zero fields take their defaults.  The server
+ * runs on the device current on the calling thread. */
+int lensgb_server_create(const lensgb_server_config* cfg, lensgb_server** out);
+/* Queues n requests (the host buffers they name must stay valid until each is
+ * done); tickets[i] receives request i's ticket.  Validates each request's
+ * model; on an error no later request of the call is queued. */
+int lensgb_server_submit(lensgb_server* server, const lensgb_request* requests, int n,
+                         long long* tickets);
+/* *state = LENSGB_REQ_*; returns the request's error code once it FAILED. */
+int lensgb_server_poll(lensgb_server* server, long long ticket, int* state);
+/* Polls until the request is done or failed, or timeout_s elapses. */
+int lensgb_server_wait(lensgb_server* server, long long ticket, double timeout_s, int* state);
+/* Waits until every submitted request is done or failed. */
+int lensgb_server_drain(lensgb_server* server, double timeout_s);
+/* Server clock (ns since creation), the time base of release_ns. */
+long long lensgb_server_clock_ns(const lensgb_server* server);
+/* Release, admission and completion times of a request (-1 while not reached). */
+int lensgb_server_request_times(lensgb_server* server, long long ticket, long long* release_ns,
+                                long long* admit_ns, long long* done_ns);
+int lensgb_server_get_stats(lensgb_server* server, lensgb_server_stats* out);
+/* Finishes the batches in flight, then frees everything; queued requests that
+ * were never launched stay QUEUED. */
+int lensgb_server_destroy(lensgb_server* server);
 
 /* Description of the last error on the calling thread ("" if none). */
 const char* lensgb_last_error(void);

@@ -37,12 +37,15 @@ NO_LENS_LIGHT = 4
 # exported symbols (must match include/lensgb.h)
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
-    "lensgb_model_set_refine", "lensgb_model_refined_pixels",
+    "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
     "lensgb_bulk_create", "lensgb_bulk_destroy", "lensgb_bulk_set_fp32_alpha_max",
     "lensgb_bulk_ray_shooting",
+    "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
+    "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
+    "lensgb_server_get_stats", "lensgb_server_destroy",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -82,7 +85,43 @@ class NoiseDesc(ctypes.Structure):
         ("exposure_time", ctypes.c_double),
         ("background_rms", ctypes.c_double),
         ("error_map_dev", ctypes.c_void_p),
+        ("mask_stride", ctypes.c_longlong),
     ]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("n_streams", ctypes.c_int),
+        ("max_batch", ctypes.c_int),
+        ("hbm_budget_bytes", ctypes.c_longlong),
+        ("contexts_per_bucket", ctypes.c_int),
+        ("use_graphs", ctypes.c_int),
+    ]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("desc", ModelDesc),
+        ("params", ctypes.c_void_p),
+        ("psf", ctypes.c_void_p),
+        ("image_out", ctypes.c_void_p),
+        ("data", ctypes.c_void_p),
+        ("noise_map", ctypes.c_void_p),
+        ("mask", ctypes.c_void_p),
+        ("background_rms", ctypes.c_double),
+        ("exposure_time", ctypes.c_double),
+        ("logl_out", ctypes.c_void_p),
+        ("release_ns", ctypes.c_longlong),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_longlong) for n in (
+        "batches", "requests_launched", "requests_done", "graph_captures", "graph_launches",
+        "evictions", "bytes_held", "peak_bytes")]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 class LensgbError(RuntimeError):
@@ -110,6 +149,8 @@ def load():
     lib.lensgb_model_destroy.restype = i
     lib.lensgb_model_param_count.argtypes = [vp]
     lib.lensgb_model_param_count.restype = i
+    lib.lensgb_model_reserve.argtypes = [vp, i]
+    lib.lensgb_model_reserve.restype = i
     lib.lensgb_model_set_refine.argtypes = [vp, ctypes.c_double, ctypes.c_double]
     lib.lensgb_model_set_refine.restype = i
     lib.lensgb_model_refined_pixels.argtypes = [vp, vp, ctypes.POINTER(ll)]
@@ -136,6 +177,26 @@ def load():
     lib.lensgb_bulk_set_fp32_alpha_max.restype = i
     lib.lensgb_bulk_ray_shooting.argtypes = [vp, vp, dp, i, dp, dp, dp, dp, ll, vp]
     lib.lensgb_bulk_ray_shooting.restype = i
+    lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
+    lib.lensgb_server_create.restype = i
+    lib.lensgb_server_submit.argtypes = [vp, ctypes.POINTER(Request), i,
+                                         ctypes.POINTER(ctypes.c_longlong)]
+    lib.lensgb_server_submit.restype = i
+    lib.lensgb_server_poll.argtypes = [vp, ll, ctypes.POINTER(i)]
+    lib.lensgb_server_poll.restype = i
+    lib.lensgb_server_wait.argtypes = [vp, ll, ctypes.c_double, ctypes.POINTER(i)]
+    lib.lensgb_server_wait.restype = i
+    lib.lensgb_server_drain.argtypes = [vp, ctypes.c_double]
+    lib.lensgb_server_drain.restype = i
+    lib.lensgb_server_clock_ns.argtypes = [vp]
+    lib.lensgb_server_clock_ns.restype = ll
+    lib.lensgb_server_request_times.argtypes = [vp, ll, ctypes.POINTER(ll), ctypes.POINTER(ll),
+                                                ctypes.POINTER(ll)]
+    lib.lensgb_server_request_times.restype = i
+    lib.lensgb_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    lib.lensgb_server_get_stats.restype = i
+    lib.lensgb_server_destroy.argtypes = [vp]
+    lib.lensgb_server_destroy.restype = i
     lib.lensgb_last_error.argtypes = []
     lib.lensgb_last_error.restype = ctypes.c_char_p
     lib.lensgb_version.argtypes = []

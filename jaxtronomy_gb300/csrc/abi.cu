@@ -37,6 +37,8 @@ static int fail(int code, const std::string& msg) {
     return code;
 }
 
+void lensgb::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 static int lens_param_count(int code) {
     switch (code) {
         case LENSGB_LENS_SIE: return 5;
@@ -144,7 +146,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 102; }
+int lensgb_version(void) { return 103; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -281,6 +283,12 @@ int lensgb_model_destroy(lensgb_model* m) {
 
 int lensgb_model_param_count(const lensgb_model* m) { return m ? m->st.n_params : -1; }
 
+int lensgb_model_reserve(lensgb_model* m, int n_inst) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535) return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    return n_inst > 0 ? ensure_scratch(m, n_inst) : LENSGB_OK;
+}
+
 int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* psf,
                  long long psf_stride, void* out, int flags, void* stream) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -343,7 +351,8 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     if (!image_out || !logl) return fail(LENSGB_ERR_INVALID, "null image or logL output");
     if (!nd->noise_map_dev && !nd->exposure_map_dev && !(nd->exposure_time > 0))
         return fail(LENSGB_ERR_INVALID, "exposure time must be positive without a noise map");
-    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0)
+    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0 ||
+        nd->mask_stride < 0)
         return fail(LENSGB_ERR_INVALID, "negative stride");
     int rc = lensgb_image(m, params, n_inst, psf, psf_stride, image_out, 0, stream);
     if (rc) return rc;
@@ -352,6 +361,7 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     a.data = nd->data_dev;
     a.data_stride = nd->data_stride;
     a.mask = nd->mask_dev;
+    a.mask_stride = nd->mask_stride;
     a.noise_map = nd->noise_map_dev;
     a.noise_stride = nd->noise_stride;
     a.exposure = nd->exposure_map_dev;

@@ -13,6 +13,10 @@
 // memory.  Each thread accumulates an RY x CX register block, streaming one
 // input row segment at a time through registers and reusing it for every
 // output row of its block that the row touches.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "launch.h"
 
 namespace lensgb {
@@ -183,6 +187,24 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
     }
 }
 
+// Raise a kernel's dynamic shared-memory limit only when a launch needs more
+// than any earlier one (per device and kernel), so that repeated launches --
+// including ones recorded into a CUDA graph -- make no attribute calls.
+static bool raise_smem_limit(const void* fn, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, size_t> granted;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& g = granted[std::make_pair(fn, dev)];
+    if (smem <= g) return true;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return false;
+    g = smem;
+    return true;
+}
+
 static int run_conv_f32(const void* in, void* out, const void* kernel, long long kstride,
                         int n_inst, int ny, int nx, int K, int edge, cudaStream_t stream) {
     // tile height 4*TY with TY in 8..16: fewest padded rows, then the tallest tile
@@ -201,11 +223,7 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
     const int SW = C32_W + KP + 4;
     const int SH = H + K - 1;
     const size_t smem = (size_t)(K * KP + SH * SW) * sizeof(float);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(conv_f32_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return -1;
-    }
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
     dim3 grid((unsigned)((nx + C32_W - 1) / C32_W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
     dim3 block(C32_TX, best_ty);
     conv_f32_kernel<<<grid, block, smem, stream>>>((const float*)in, (float*)out,
@@ -221,11 +239,8 @@ static int run_conv(const void* in, void* out, const void* kernel, long long kst
     const int SW = W + KP - 1 + 1;
     const int SH = H + K - 1;
     size_t smem = (size_t)(K * KP + SH * SW) * sizeof(R);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(conv_kernel<R, CX, RY, VC>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return -1;
-    }
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_kernel<R, CX, RY, VC>, smem))
+        return -1;
     dim3 grid((unsigned)((nx + W - 1) / W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
     dim3 block(CONV_TX, CONV_TY);
     conv_kernel<R, CX, RY, VC><<<grid, block, smem, stream>>>(

@@ -6,7 +6,12 @@
 
 #include "common.cuh"
 
+#include <string>
+
 namespace lensgb {
+
+// Sets the calling thread's lensgb_last_error() text (defined in abi.cu).
+void set_last_error(const std::string& msg);
 
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
                    double* rec_d, float* rec_f, double* coef_d, float* coef_f,
@@ -31,7 +36,8 @@ int launch_conv(const void* in, void* out, const void* kernel, long long kstride
 struct LoglikeArgs {
     const double* data;
     long long data_stride;
-    const double* mask;       // ny*nx or null (all pixels)
+    const double* mask;       // ny*nx per system (mask_stride apart) or null (all pixels)
+    long long mask_stride;
     const double* noise_map;  // or null
     long long noise_stride;
     const double* exposure;   // exposure map (already floored) or null

@@ -24,10 +24,11 @@ loglike_kernel(const R* __restrict__ model, long long npix, LoglikeArgs a,
     const double* d = a.data + (long long)inst * a.data_stride;
     const double* nm = a.noise_map ? a.noise_map + (long long)inst * a.noise_stride : nullptr;
     const double* ex = a.exposure ? a.exposure + (long long)inst * a.exposure_stride : nullptr;
+    const double* mask = a.mask ? a.mask + (long long)inst * a.mask_stride : nullptr;
     const double b2 = a.background_rms * a.background_rms;
     double sum = 0.0, comp = 0.0;
     for (long long i = threadIdx.x; i < npix; i += LL_THREADS) {
-        const double mk = a.mask ? a.mask[i] : 1.0;
+        const double mk = mask ? mask[i] : 1.0;
         if (mk == 0.0) continue;
         const double mv = (double)m[i];
         double c;

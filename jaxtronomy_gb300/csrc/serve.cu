@@ -1,0 +1,698 @@
+// Serving loop: continuous batching of image / likelihood requests.
+//
+// The reference simulates one ImageModel.image call per XLA program
+// (image_model.py:432-492), or a jax.vmap over a fixed batch.  A server here
+// owns one worker thread that
+//   * releases submitted requests into per-bucket FIFO queues once their
+//     release time has passed (a bucket = one compiled model: profile lists,
+//     grid, supersampling, PSF size, precision and noise options);
+//   * keeps up to n_streams batches in flight, one per CUDA stream, each batch
+//     a single lensgb_image / lensgb_loglike launch sequence over up to
+//     max_batch requests of one bucket -- requests that arrive while others
+//     are on the GPU join the next batch as soon as a stream frees up;
+//   * stages each request's parameters, PSF, data, noise map and mask into
+//     device buffers of an execution context (grow-only, per bucket), whose
+//     total size is held under hbm_budget_bytes: idle contexts are evicted
+//     (least recently used first) to admit new ones, and requests wait in
+//     their queue while the budget is exhausted by batches in flight;
+//   * optionally replays a CUDA graph captured for a context and batch size
+//     after its first eager run.
+// Results are written by device-to-host copies straight into the caller's
+// buffers (pinned buffers make them asynchronous) before a request is marked
+// done.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <queue>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "launch.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+    lensgb_request r;
+    long long ticket = 0;
+    int bucket = -1;
+    std::atomic<int> state{LENSGB_REQ_QUEUED};
+    int rc = LENSGB_OK;
+    bool out_pinned = false;  // image_out is page-locked: copy to it asynchronously
+    long long t_submit = 0, t_release = 0, t_admit = 0, t_done = 0;
+};
+
+struct BucketKey {
+    lensgb_model_desc desc;
+    int likelihood;      // 0: image only; 1: image + logL
+    int has_noise, has_mask;
+    double background_rms, exposure_time;
+    bool operator<(const BucketKey& o) const {
+        int c = memcmp(&desc, &o.desc, sizeof desc);
+        if (c) return c < 0;
+        if (likelihood != o.likelihood) return likelihood < o.likelihood;
+        if (has_noise != o.has_noise) return has_noise < o.has_noise;
+        if (has_mask != o.has_mask) return has_mask < o.has_mask;
+        if (background_rms != o.background_rms) return background_rms < o.background_rms;
+        return exposure_time < o.exposure_time;
+    }
+};
+
+struct Context {
+    int bucket = -1;
+    lensgb_model* model = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    int cap = 0;             // batch capacity of the buffers below
+    size_t bytes = 0;        // device bytes held (buffers + model scratch)
+    double* rows_dev = nullptr;
+    void* psf_dev = nullptr;
+    void* img_dev = nullptr;
+    double* data_dev = nullptr;
+    double* noise_dev = nullptr;
+    double* mask_dev = nullptr;
+    double* logl_dev = nullptr;
+    double* rows_host = nullptr;  // pinned staging
+    unsigned char* psf_host = nullptr;
+    double* logl_host = nullptr;
+    unsigned char* img_host = nullptr;  // pinned staging for pageable image_out buffers
+    bool busy = false;
+    long long last_used = 0;
+    std::vector<Req*> batch;
+    std::map<int, cudaGraphExec_t> graphs;  // batch size -> graph
+    std::map<int, int> eager_runs;          // batch size -> eager launches so far
+};
+
+struct Bucket {
+    BucketKey key;
+    int n_params = 0;
+    long long npix = 0;
+    int k2 = 0;          // PSF elements per request
+    size_t esz = 4;      // image element size
+    std::deque<Req*> queue;
+    std::vector<Context*> ctx;
+};
+
+}  // namespace
+
+struct lensgb_server {
+    lensgb_server_config cfg;
+    Clock::time_point t0;
+    std::mutex mu;
+    std::condition_variable cv;
+    int device = 0;
+    std::deque<Req> reqs;                     // stable storage, index = ticket
+    std::vector<Req*> incoming;               // submitted, not yet released
+    std::vector<Bucket*> buckets;             // guarded by mu (appended by submit)
+    std::map<BucketKey, int> bucket_index;
+    std::vector<Bucket*> wb;                  // the worker's copy of `buckets`
+    std::vector<Context*> contexts;
+    size_t bytes_held = 0;
+    size_t peak_bytes = 0;
+    int inflight = 0;
+    std::atomic<long long> n_done{0};
+    lensgb_server_stats stats;
+    std::atomic<bool> stop{false};
+    std::thread worker;
+
+    long long now() const {
+        return std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+int serr(int code, const std::string& m) {
+    lensgb::set_last_error(m);
+    return code;
+}
+
+size_t context_bytes(const Bucket& b, int cap) {
+    // buffers owned by the context
+    size_t per = (size_t)b.n_params * 8 + (size_t)b.k2 * b.esz + (size_t)b.npix * b.esz + 8;
+    if (b.key.likelihood) {
+        per += (size_t)b.npix * 8;
+        if (b.key.has_noise) per += (size_t)b.npix * 8;
+        if (b.key.has_mask) per += (size_t)b.npix * 8;
+    }
+    // model scratch: records, coefficient tables, un-convolved image, refine list
+    const lensgb_model_desc& d = b.key.desc;
+    const size_t nprof = (size_t)(d.n_lens + d.n_source + d.n_lens_light);
+    per += nprof * (32 * 8 + 36 * 4) + (size_t)d.n_lens * 500 * 12 + (size_t)b.npix * (b.esz + 4);
+    return per * (size_t)cap;
+}
+
+void free_context_buffers(Context* c) {
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
+    c->graphs.clear();
+    c->eager_runs.clear();
+    cudaFree(c->rows_dev);
+    cudaFree(c->psf_dev);
+    cudaFree(c->img_dev);
+    cudaFree(c->data_dev);
+    cudaFree(c->noise_dev);
+    cudaFree(c->mask_dev);
+    cudaFree(c->logl_dev);
+    cudaFreeHost(c->rows_host);
+    cudaFreeHost(c->psf_host);
+    cudaFreeHost(c->logl_host);
+    cudaFreeHost(c->img_host);
+    c->img_host = nullptr;
+    c->rows_dev = nullptr;
+    c->psf_dev = c->img_dev = nullptr;
+    c->data_dev = c->noise_dev = c->mask_dev = c->logl_dev = nullptr;
+    c->rows_host = nullptr;
+    c->psf_host = nullptr;
+    c->logl_host = nullptr;
+    c->cap = 0;
+}
+
+void destroy_context(lensgb_server* s, Context* c) {
+    free_context_buffers(c);
+    if (c->model) lensgb_model_destroy(c->model);
+    if (c->done) cudaEventDestroy(c->done);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    s->bytes_held -= c->bytes;
+    delete c;
+}
+
+// Evict idle contexts (least recently used first) until `need` more bytes fit.
+bool make_room(lensgb_server* s, size_t need, const Context* keep) {
+    while (s->bytes_held + need > (size_t)s->cfg.hbm_budget_bytes) {
+        Context* victim = nullptr;
+        for (Context* c : s->contexts)
+            if (!c->busy && c != keep && (!victim || c->last_used < victim->last_used)) victim = c;
+        if (!victim) return false;
+        Bucket& b = *s->wb[victim->bucket];
+        b.ctx.erase(std::find(b.ctx.begin(), b.ctx.end(), victim));
+        s->contexts.erase(std::find(s->contexts.begin(), s->contexts.end(), victim));
+        destroy_context(s, victim);
+        s->stats.evictions++;
+    }
+    return true;
+}
+
+// Grow a context to hold `n` requests (capacity doubles up to max_batch).
+int grow_context(lensgb_server* s, Context* c, int n) {
+    if (n <= c->cap) return LENSGB_OK;
+    Bucket& b = *s->wb[c->bucket];
+    int cap = c->cap > 0 ? c->cap : 1;
+    while (cap < n) cap *= 2;
+    if (cap > s->cfg.max_batch) cap = s->cfg.max_batch;
+    const size_t nb = context_bytes(b, cap);
+    if (nb > c->bytes && !make_room(s, nb - c->bytes, c)) return LENSGB_ERR_OOM;
+    free_context_buffers(c);
+    s->bytes_held -= c->bytes;
+    c->bytes = 0;
+    const size_t P = (size_t)b.n_params, np = (size_t)b.npix;
+    bool ok = cudaMalloc(&c->rows_dev, cap * P * 8 + 8) == cudaSuccess &&
+              cudaMalloc(&c->psf_dev, cap * (size_t)b.k2 * b.esz + 16) == cudaSuccess &&
+              cudaMalloc(&c->img_dev, cap * np * b.esz) == cudaSuccess &&
+              cudaMalloc(&c->logl_dev, cap * 8) == cudaSuccess &&
+              cudaMallocHost(&c->rows_host, cap * P * 8 + 8) == cudaSuccess &&
+              cudaMallocHost(&c->psf_host, cap * (size_t)b.k2 * b.esz + 16) == cudaSuccess &&
+              cudaMallocHost(&c->logl_host, cap * 8) == cudaSuccess &&
+              cudaMallocHost(&c->img_host, cap * np * b.esz) == cudaSuccess;
+    if (ok && b.key.likelihood) {
+        ok = cudaMalloc(&c->data_dev, cap * np * 8) == cudaSuccess;
+        if (ok && b.key.has_noise) ok = cudaMalloc(&c->noise_dev, cap * np * 8) == cudaSuccess;
+        if (ok && b.key.has_mask) ok = cudaMalloc(&c->mask_dev, cap * np * 8) == cudaSuccess;
+    }
+    if (ok) ok = lensgb_model_reserve(c->model, cap) == LENSGB_OK;
+    if (!ok) {
+        cudaGetLastError();
+        free_context_buffers(c);
+        return LENSGB_ERR_OOM;
+    }
+    c->cap = cap;
+    c->bytes = nb;
+    s->bytes_held += nb;
+    s->peak_bytes = std::max(s->peak_bytes, s->bytes_held);
+    return LENSGB_OK;
+}
+
+Context* new_context(lensgb_server* s, int bucket) {
+    Bucket& b = *s->wb[bucket];
+    Context* c = new Context();
+    c->bucket = bucket;
+    if (lensgb_model_create(&b.key.desc, &c->model) != LENSGB_OK ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (c->model) lensgb_model_destroy(c->model);
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return nullptr;
+    }
+    b.ctx.push_back(c);
+    s->contexts.push_back(c);
+    return c;
+}
+
+// Launch sequence of one batch on the context's stream (graph-capturable:
+// only stream operations on buffers owned by the context).
+int launch_batch(lensgb_server* s, Context* c, int n) {
+    Bucket& b = *s->wb[c->bucket];
+    cudaStream_t st = c->stream;
+    const size_t P = (size_t)b.n_params;
+    if (cudaMemcpyAsync(c->rows_dev, c->rows_host, n * P * 8, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+        return LENSGB_ERR_CUDA;
+    if (b.k2 > 0 && cudaMemcpyAsync(c->psf_dev, c->psf_host, n * (size_t)b.k2 * b.esz,
+                                    cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return LENSGB_ERR_CUDA;
+    if (!b.key.likelihood)
+        return lensgb_image(c->model, c->rows_dev, n, c->psf_dev, b.k2, c->img_dev, 0, st);
+    lensgb_noise_desc nd;
+    memset(&nd, 0, sizeof nd);
+    nd.data_dev = c->data_dev;
+    nd.data_stride = b.npix;
+    nd.noise_map_dev = c->noise_dev;
+    nd.noise_stride = c->noise_dev ? b.npix : 0;
+    nd.mask_dev = c->mask_dev;
+    nd.mask_stride = c->mask_dev ? b.npix : 0;
+    nd.exposure_time = b.key.exposure_time;
+    nd.background_rms = b.key.background_rms;
+    int rc = lensgb_loglike(c->model, c->rows_dev, n, c->psf_dev, b.k2, &nd, c->img_dev,
+                            c->logl_dev, st);
+    if (rc) return rc;
+    if (cudaMemcpyAsync(c->logl_host, c->logl_dev, n * 8, cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+        return LENSGB_ERR_CUDA;
+    return LENSGB_OK;
+}
+
+int run_batch(lensgb_server* s, Context* c, int n) {
+    Bucket& b = *s->wb[c->bucket];
+    cudaStream_t st = c->stream;
+    // stage the small per-request inputs in pinned memory
+    const size_t P = (size_t)b.n_params;
+    for (int i = 0; i < n; ++i) {
+        const lensgb_request& r = c->batch[i]->r;
+        memcpy(c->rows_host + i * P, r.params, P * 8);
+        if (b.k2 > 0) memcpy(c->psf_host + i * (size_t)b.k2 * b.esz, r.psf, (size_t)b.k2 * b.esz);
+    }
+    // the large per-request arrays go straight from the caller's buffers
+    if (b.key.likelihood) {
+        const size_t bytes = (size_t)b.npix * 8;
+        for (int i = 0; i < n; ++i) {
+            const lensgb_request& r = c->batch[i]->r;
+            if (cudaMemcpyAsync(c->data_dev + i * b.npix, r.data, bytes, cudaMemcpyHostToDevice,
+                                st) != cudaSuccess ||
+                (c->noise_dev && cudaMemcpyAsync(c->noise_dev + i * b.npix, r.noise_map, bytes,
+                                                 cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+                (c->mask_dev && cudaMemcpyAsync(c->mask_dev + i * b.npix, r.mask, bytes,
+                                                cudaMemcpyHostToDevice, st) != cudaSuccess))
+                return LENSGB_ERR_CUDA;
+        }
+    }
+    int rc = LENSGB_OK;
+    auto g = c->graphs.find(n);
+    if (g != c->graphs.end()) {
+        if (cudaGraphLaunch(g->second, st) != cudaSuccess) return LENSGB_ERR_CUDA;
+        s->stats.graph_launches++;
+    } else if (s->cfg.use_graphs && c->eager_runs[n] >= 1) {
+        // the same context and size ran eagerly before: capture and replay
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return LENSGB_ERR_CUDA;
+        rc = launch_batch(s, c, n);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc == LENSGB_OK && e == cudaSuccess &&
+            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+            c->graphs[n] = exec;
+            s->stats.graph_captures++;
+        } else {
+            exec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (exec) {
+            if (cudaGraphLaunch(exec, st) != cudaSuccess) return LENSGB_ERR_CUDA;
+            s->stats.graph_launches++;
+        } else {
+            rc = launch_batch(s, c, n);  // capture failed: run eagerly
+            if (rc) return rc;
+        }
+    } else {
+        rc = launch_batch(s, c, n);
+        if (rc) return rc;
+        c->eager_runs[n]++;
+    }
+    // results straight into page-locked caller buffers; pageable ones are
+    // staged and copied by the worker when the batch completes
+    const size_t ib = (size_t)b.npix * b.esz;
+    for (int i = 0; i < n; ++i) {
+        const Req* q = c->batch[i];
+        if (!q->r.image_out) continue;
+        void* dst = q->out_pinned ? q->r.image_out : (void*)(c->img_host + i * ib);
+        if (cudaMemcpyAsync(dst, (unsigned char*)c->img_dev + i * ib, ib, cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess)
+            return LENSGB_ERR_CUDA;
+    }
+    if (cudaEventRecord(c->done, st) != cudaSuccess) return LENSGB_ERR_CUDA;
+    return LENSGB_OK;
+}
+
+void finish_batch(lensgb_server* s, Context* c, int rc) {
+    const long long t = s->now();
+    Bucket& b = *s->wb[c->bucket];
+    const size_t ib = (size_t)b.npix * b.esz;
+    for (size_t i = 0; i < c->batch.size(); ++i) {
+        Req* q = c->batch[i];
+        if (rc == LENSGB_OK && b.key.likelihood && q->r.logl_out) *q->r.logl_out = c->logl_host[i];
+        if (rc == LENSGB_OK && q->r.image_out && !q->out_pinned)
+            memcpy(q->r.image_out, c->img_host + i * ib, ib);
+        q->rc = rc;
+        q->t_done = t;
+        q->state.store(rc == LENSGB_OK ? LENSGB_REQ_DONE : LENSGB_REQ_FAILED,
+                       std::memory_order_release);
+    }
+    s->n_done += (long long)c->batch.size();
+    c->batch.clear();
+    c->busy = false;
+    c->last_used = t;
+    s->inflight--;
+}
+
+// Pick the bucket whose oldest waiting request is oldest and that can get a
+// context; form and launch one batch.  Returns false if nothing was launched.
+bool launch_one(lensgb_server* s) {
+    int best = -1;
+    long long best_t = 0;
+    for (size_t k = 0; k < s->wb.size(); ++k) {
+        Bucket& b = *s->wb[k];
+        if (b.queue.empty()) continue;
+        bool idle = false;
+        for (Context* c : b.ctx) idle |= !c->busy;
+        if (!idle && (int)b.ctx.size() >= s->cfg.contexts_per_bucket) continue;
+        const long long t = b.queue.front()->t_release;
+        if (best < 0 || t < best_t) {
+            best = (int)k;
+            best_t = t;
+        }
+    }
+    if (best < 0) return false;
+    Bucket& b = *s->wb[best];
+    Context* c = nullptr;
+    for (Context* x : b.ctx)
+        if (!x->busy) {
+            c = x;
+            break;
+        }
+    const int n = (int)std::min<size_t>(b.queue.size(), (size_t)s->cfg.max_batch);
+    if (!c) {
+        if (!make_room(s, context_bytes(b, n), nullptr)) return false;  // wait for memory
+        c = new_context(s, best);
+        if (!c) {
+            // cannot build the model: fail the queued requests of this bucket
+            for (Req* q : b.queue) {
+                q->rc = LENSGB_ERR_UNSUPPORTED;
+                q->t_done = s->now();
+                q->state.store(LENSGB_REQ_FAILED, std::memory_order_release);
+                s->n_done++;
+            }
+            b.queue.clear();
+            return true;
+        }
+    }
+    // the largest batch that fits the budget (halving from the queue length)
+    int rc = LENSGB_ERR_OOM;
+    for (int m = n; m >= 1 && rc == LENSGB_ERR_OOM; m = (m == 1 ? 0 : (m + 1) / 2))
+        rc = grow_context(s, c, m);
+    if (rc == LENSGB_ERR_OOM) {
+        if (c->cap == 0 && s->inflight == 0) {
+            // nothing in flight can free memory: the request can never fit
+            const int m = (int)b.queue.size();
+            for (int i = 0; i < m; ++i) {
+                Req* q = b.queue.front();
+                b.queue.pop_front();
+                q->rc = LENSGB_ERR_OOM;
+                q->t_done = s->now();
+                q->state.store(LENSGB_REQ_FAILED, std::memory_order_release);
+                s->n_done++;
+            }
+            return true;
+        }
+        return false;
+    }
+    const int nb = std::min(n, c->cap);
+    const long long t = s->now();
+    for (int i = 0; i < nb; ++i) {
+        Req* q = b.queue.front();
+        b.queue.pop_front();
+        q->t_admit = t;
+        q->state.store(LENSGB_REQ_RUNNING, std::memory_order_release);
+        c->batch.push_back(q);
+    }
+    c->busy = true;
+    c->last_used = t;
+    s->inflight++;
+    s->stats.batches++;
+    s->stats.requests_launched += nb;
+    rc = run_batch(s, c, nb);
+    if (rc != LENSGB_OK) {
+        cudaStreamSynchronize(c->stream);
+        cudaGetLastError();
+        finish_batch(s, c, rc);
+    }
+    return true;
+}
+
+void worker_main(lensgb_server* s) {
+    cudaSetDevice(s->device);
+    std::vector<Req*> ready;
+    while (!s->stop.load()) {
+        bool progress = false;
+        const long long t = s->now();
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            // release due requests in submission order
+            auto& in = s->incoming;
+            size_t w = 0;
+            for (size_t i = 0; i < in.size(); ++i) {
+                if (in[i]->t_release <= t)
+                    ready.push_back(in[i]);
+                else
+                    in[w++] = in[i];
+            }
+            in.resize(w);
+            while (s->wb.size() < s->buckets.size()) s->wb.push_back(s->buckets[s->wb.size()]);
+        }
+        for (Req* q : ready) s->wb[q->bucket]->queue.push_back(q);
+        progress |= !ready.empty();
+        ready.clear();
+        // completions
+        for (Context* c : s->contexts) {
+            if (!c->busy) continue;
+            cudaError_t e = cudaEventQuery(c->done);
+            if (e == cudaSuccess) {
+                finish_batch(s, c, LENSGB_OK);
+                progress = true;
+            } else if (e != cudaErrorNotReady) {
+                cudaGetLastError();
+                finish_batch(s, c, LENSGB_ERR_CUDA);
+                progress = true;
+            }
+        }
+        // admissions
+        while (s->inflight < s->cfg.n_streams && launch_one(s)) progress = true;
+        if (!progress) {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait_for(lock, std::chrono::microseconds(20));
+        }
+    }
+    // drain what is in flight before the worker exits
+    for (Context* c : s->contexts)
+        if (c->busy) {
+            cudaEventSynchronize(c->done);
+            finish_batch(s, c, LENSGB_OK);
+        }
+}
+
+int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
+    BucketKey k;
+    memset(&k, 0, sizeof k);
+    k.desc = r.desc;
+    k.likelihood = r.data ? 1 : 0;
+    k.has_noise = r.data && r.noise_map ? 1 : 0;
+    k.has_mask = r.data && r.mask ? 1 : 0;
+    k.background_rms = r.data ? r.background_rms : 0.0;
+    k.exposure_time = r.data ? r.exposure_time : 0.0;
+    auto it = s->bucket_index.find(k);
+    if (it != s->bucket_index.end()) {
+        *out = it->second;
+        return LENSGB_OK;
+    }
+    // validate the model once per bucket
+    lensgb_model* m = nullptr;
+    int rc = lensgb_model_create(&r.desc, &m);
+    if (rc) return serr(rc, std::string("request model: ") + lensgb_last_error());
+    Bucket* b = new Bucket();
+    b->key = k;
+    b->n_params = lensgb_model_param_count(m);
+    lensgb_model_destroy(m);
+    b->npix = (long long)r.desc.nx * r.desc.ny;
+    b->k2 = r.desc.psf_type == LENSGB_PSF_NONE ? 0 : r.desc.kernel_size * r.desc.kernel_size;
+    b->esz = r.desc.precision == LENSGB_FP64 ? 8 : 4;
+    s->buckets.push_back(b);
+    *out = (int)s->buckets.size() - 1;
+    s->bucket_index[k] = *out;
+    return LENSGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lensgb_server_create(const lensgb_server_config* cfg, lensgb_server** out) {
+    if (!out) return serr(LENSGB_ERR_INVALID, "null output handle pointer");
+    *out = nullptr;
+    lensgb_server_config c;
+    memset(&c, 0, sizeof c);
+    if (cfg) c = *cfg;
+    if (c.n_streams <= 0) c.n_streams = 4;
+    if (c.max_batch <= 0) c.max_batch = 256;
+    if (c.contexts_per_bucket <= 0) c.contexts_per_bucket = 2;
+    if (c.hbm_budget_bytes <= 0) c.hbm_budget_bytes = 4ll << 30;
+    if (c.n_streams > 64 || c.max_batch > 65535 || c.contexts_per_bucket > 16)
+        return serr(LENSGB_ERR_INVALID, "n_streams <= 64, max_batch <= 65535, "
+                                        "contexts_per_bucket <= 16");
+    lensgb_server* s = new lensgb_server();
+    s->cfg = c;
+    cudaGetDevice(&s->device);
+    memset(&s->stats, 0, sizeof s->stats);
+    s->t0 = Clock::now();
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return LENSGB_OK;
+}
+
+long long lensgb_server_clock_ns(const lensgb_server* s) { return s ? s->now() : -1; }
+
+int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, long long* tickets) {
+    if (!s) return serr(LENSGB_ERR_INVALID, "null server");
+    if (n < 0 || (n > 0 && (!reqs || !tickets)))
+        return serr(LENSGB_ERR_INVALID, "null request array or tickets");
+    std::lock_guard<std::mutex> lock(s->mu);
+    const long long t = s->now();
+    for (int i = 0; i < n; ++i) {
+        const lensgb_request& r = reqs[i];
+        if (!r.params) return serr(LENSGB_ERR_INVALID, "request without params");
+        if (r.desc.psf_type != LENSGB_PSF_NONE && !r.psf)
+            return serr(LENSGB_ERR_INVALID, "request without a PSF kernel");
+        if (r.data && r.noise_map == nullptr && !(r.exposure_time > 0))
+            return serr(LENSGB_ERR_INVALID, "likelihood request needs exposure_time > 0");
+        int bucket = -1;
+        int rc = bucket_for(s, r, &bucket);
+        if (rc) return rc;
+        s->reqs.emplace_back();
+        Req& q = s->reqs.back();
+        q.r = r;
+        q.ticket = (long long)s->reqs.size() - 1;
+        q.bucket = bucket;
+        q.t_submit = t;
+        q.t_release = r.release_ns > t ? r.release_ns : t;
+        if (r.image_out) {
+            cudaPointerAttributes pa;
+            q.out_pinned = cudaPointerGetAttributes(&pa, r.image_out) == cudaSuccess &&
+                           pa.type == cudaMemoryTypeHost;
+            cudaGetLastError();
+        }
+        s->incoming.push_back(&q);
+        tickets[i] = q.ticket;
+    }
+    s->cv.notify_one();
+    return LENSGB_OK;
+}
+
+int lensgb_server_poll(lensgb_server* s, long long ticket, int* state) {
+    if (!s || !state) return serr(LENSGB_ERR_INVALID, "null server or state");
+    Req* q;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (ticket < 0 || ticket >= (long long)s->reqs.size())
+            return serr(LENSGB_ERR_INVALID, "unknown ticket");
+        q = &s->reqs[(size_t)ticket];
+    }
+    *state = q->state.load(std::memory_order_acquire);
+    return *state == LENSGB_REQ_FAILED ? q->rc : LENSGB_OK;
+}
+
+int lensgb_server_wait(lensgb_server* s, long long ticket, double timeout_s, int* state) {
+    if (!s || !state) return serr(LENSGB_ERR_INVALID, "null server or state");
+    const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
+    for (;;) {
+        int rc = lensgb_server_poll(s, ticket, state);
+        if (rc || *state == LENSGB_REQ_DONE) return rc;
+        if (Clock::now() > until) return LENSGB_OK;
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+int lensgb_server_drain(lensgb_server* s, double timeout_s) {
+    if (!s) return serr(LENSGB_ERR_INVALID, "null server");
+    const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
+    for (;;) {
+        long long total;
+        {
+            std::lock_guard<std::mutex> lock(s->mu);
+            total = (long long)s->reqs.size();
+        }
+        if (s->n_done.load() >= total) return LENSGB_OK;
+        if (Clock::now() > until) return serr(LENSGB_ERR_CUDA, "drain timed out");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int lensgb_server_request_times(lensgb_server* s, long long ticket, long long* release_ns,
+                                long long* admit_ns, long long* done_ns) {
+    if (!s) return serr(LENSGB_ERR_INVALID, "null server");
+    Req* q;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (ticket < 0 || ticket >= (long long)s->reqs.size())
+            return serr(LENSGB_ERR_INVALID, "unknown ticket");
+        q = &s->reqs[(size_t)ticket];
+    }
+    const int st = q->state.load(std::memory_order_acquire);
+    if (release_ns) *release_ns = q->t_release;
+    if (admit_ns) *admit_ns = st >= LENSGB_REQ_RUNNING ? q->t_admit : -1;
+    if (done_ns) *done_ns = st >= LENSGB_REQ_DONE ? q->t_done : -1;
+    return LENSGB_OK;
+}
+
+int lensgb_server_get_stats(lensgb_server* s, lensgb_server_stats* out) {
+    if (!s || !out) return serr(LENSGB_ERR_INVALID, "null server or stats");
+    // read on the caller's thread while the worker runs: the counters are
+    // monotone and only approximately consistent with each other
+    *out = s->stats;
+    out->bytes_held = (long long)s->bytes_held;
+    out->peak_bytes = (long long)s->peak_bytes;
+    out->requests_done = s->n_done.load();
+    return LENSGB_OK;
+}
+
+int lensgb_server_destroy(lensgb_server* s) {
+    if (!s) return LENSGB_OK;
+    s->stop.store(true);
+    s->cv.notify_one();
+    if (s->worker.joinable()) s->worker.join();
+    for (Context* c : s->contexts) destroy_context(s, c);
+    for (Bucket* b : s->buckets) delete b;
+    delete s;
+    return LENSGB_OK;
+}
+
+}  // extern "C"

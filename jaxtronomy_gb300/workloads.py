@@ -157,3 +157,83 @@ def substructure(seed=1004, num_pix=1000, delta_pix=0.01, n_sub=2000):
     xx, yy = np.meshgrid(g["ra_at_xy_0"] + c, g["dec_at_xy_0"] + c)
     lens_list = ["EPL", "SHEAR"] + ["TNFW"] * n_sub
     return xx.reshape(-1), yy.reshape(-1), lens_list, lens, src
+
+
+SERVING_STACKS = ("SIE+SHEAR", "EPL+SHEAR", "EPL_MULTIPOLE_M1M3M4+SHEAR", "NFW_ELLIPSE_CSE+SHEAR")
+
+
+def serving_stream(seed=1002, n=50000, sides=(60, 100, 180, 300), supersampling=(1, 2, 4),
+                   kernel_sizes=(11, 21, 41), delta_pix=0.05, psf_pool=32):
+    """Request stream of the serving workload: per request a grid side, a
+    supersampling factor and a PSF size drawn uniformly from the given sets, a
+    lens stack drawn uniformly from SIE+SHEAR, EPL+SHEAR,
+    EPL_MULTIPOLE_M1M3M4+SHEAR (multipole amplitudes a{1,3,4}_a~N(0,0.01),
+    angles delta_phi_m{1,3,4}~U(0,pi)) and NFW_ELLIPSE_CSE+SHEAR (Rs~U(5,20),
+    alpha_Rs~U(0.5,2)); 1 or 2 SERSIC_ELLIPSE sources and a SERSIC_ELLIPSE lens
+    light drawn as in :func:`single_sie` / :func:`batch_epl`.  PSFs are Moffat
+    kernels (beta~U(2.5,4.5), FWHM~U(0.08,0.15)") taken from a seeded pool of
+    ``psf_pool`` kernels per size.  Returns (requests, psfs): each request a dict
+    with key (side, s, K, stack, n_sources), kwargs lists and a PSF index."""
+    rng = np.random.default_rng(seed)
+    psfs = {}
+    for K in kernel_sizes:
+        b = rng.uniform(2.5, 4.5, psf_pool)
+        f = rng.uniform(0.08, 0.15, psf_pool)
+        psfs[K] = np.stack([moffat_pixel_kernel(f[i], b[i], delta_pix, K) for i in range(psf_pool)])
+    side = rng.choice(sides, n)
+    ss = rng.choice(supersampling, n)
+    ks = rng.choice(kernel_sizes, n)
+    stack = rng.integers(0, len(SERVING_STACKS), n)
+    nsrc = rng.integers(1, 3, n)
+    pidx = rng.integers(0, psf_pool, n)
+    e1, e2 = _ellip(rng, 0.1, n, clip=0.4)
+    cx, cy = rng.normal(0, 0.05, n), rng.normal(0, 0.05, n)
+    theta = rng.uniform(0.8, 1.5, n)
+    gam = rng.uniform(1.8, 2.2, n)
+    am = rng.normal(0, 0.01, (n, 3))
+    phim = rng.uniform(0, np.pi, (n, 3))
+    rs = rng.uniform(5, 20, n)
+    ars = rng.uniform(0.5, 2, n)
+    sh = _shear(rng, n)
+    src1 = _sersic_source(rng, n)
+    src2 = _sersic_source(rng, n)
+    ll = _sersic_lens_light(rng, n, cx, cy)
+    out = []
+    for i in range(n):
+        st = SERVING_STACKS[stack[i]]
+        if st == "SIE+SHEAR":
+            main = {"theta_E": theta[i], "e1": e1[i], "e2": e2[i], "center_x": cx[i],
+                    "center_y": cy[i]}
+        elif st == "NFW_ELLIPSE_CSE+SHEAR":
+            main = {"Rs": rs[i], "alpha_Rs": ars[i], "e1": e1[i], "e2": e2[i],
+                    "center_x": cx[i], "center_y": cy[i]}
+        else:
+            main = {"theta_E": theta[i], "gamma": gam[i], "e1": e1[i], "e2": e2[i],
+                    "center_x": cx[i], "center_y": cy[i]}
+            if st.startswith("EPL_MULTIPOLE"):
+                main.update({"a1_a": am[i, 0], "delta_phi_m1": phim[i, 0], "a3_a": am[i, 1],
+                             "delta_phi_m3": phim[i, 1], "a4_a": am[i, 2],
+                             "delta_phi_m4": phim[i, 2]})
+        kl = [{k: float(v) for k, v in main.items()},
+              {"gamma1": float(sh["gamma1"][i]), "gamma2": float(sh["gamma2"][i])}]
+        srcs = [src1, src2][:int(nsrc[i])]
+        kss = [{k: float(v[i]) for k, v in s.items()} for s in srcs]
+        kll = [{k: float(v[i]) for k, v in ll.items()}]
+        out.append({"key": (int(side[i]), int(ss[i]), int(ks[i]), st, int(nsrc[i])),
+                    "kwargs_lens": kl, "kwargs_source": kss, "kwargs_lens_light": kll,
+                    "psf": int(pidx[i])})
+    return out, psfs
+
+
+def serving_model(key, delta_pix=0.05, precision="fp32", data=None, exposure_time=1000.0,
+                  background_rms=0.01):
+    """ImageModel of a serving request key (side, s, K, stack, n_sources)."""
+    from . import ImageData, ImageModel, LensModel, LightModel, PSF
+    side, s, K, stack, nsrc = key
+    g = grid_kwargs(side, delta_pix)
+    d = ImageData(np.zeros((side, side)) if data is None else data, exposure_time=exposure_time,
+                  background_rms=background_rms, **g)
+    psf = PSF("PIXEL", kernel_point_source=gaussian_pixel_kernel(0.1, delta_pix, K))
+    return ImageModel(d, psf, LensModel(stack.split("+")),
+                      LightModel(["SERSIC_ELLIPSE"] * nsrc), LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics={"supersampling_factor": s, "precision": precision})

@@ -16,7 +16,8 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(lensgb_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|long long|const char\*)\s+(lensgb_\w+)\s*\(",
+                                 text, re.M)))
 
 
 def test_header_lists_the_python_symbols():
@@ -27,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.lensgb_version() == 102
+    assert lib.lensgb_version() == 103
 
 
 def _desc(**kw):
@@ -117,3 +118,28 @@ def test_split_bits_is_exact_for_grid_indices():
     assert float(hi32) == hi
     J = np.arange(540, dtype=np.float32)
     assert np.all((J * hi32).astype(np.float64) == J.astype(np.float64) * hi)
+
+
+def test_struct_sizes_match_the_header_layout():
+    """ctypes mirrors of the public structs have the C layout (x86-64 / aarch64 LP64)."""
+    assert ctypes.sizeof(_lib.NoiseDesc) == 11 * 8
+    assert ctypes.sizeof(_lib.ServerConfig) == 4 + 4 + 8 + 4 + 4
+    assert ctypes.sizeof(_lib.ServerStats) == 8 * 8
+    assert ctypes.sizeof(_lib.Request) == ctypes.sizeof(_lib.ModelDesc) + 10 * 8
+
+
+def test_bulk_and_server_handles_on_the_host():
+    """Argument validation of the bulk and server entry points (no device work)."""
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    codes = (ctypes.c_int * 2)(_lib.LENS_CODES["TNFW"], 99)
+    assert lib.lensgb_bulk_create(codes, 2, _lib.FP32_SPLIT, ctypes.byref(h)) == _lib.ERR_UNSUPPORTED
+    assert b"99" in lib.lensgb_last_error()
+    assert lib.lensgb_bulk_create(codes, 17, _lib.FP64, ctypes.byref(h)) == _lib.ERR_INVALID
+    assert lib.lensgb_bulk_create(codes, 1, 7, ctypes.byref(h)) == _lib.ERR_UNSUPPORTED
+    assert lib.lensgb_bulk_create(codes, 1, _lib.FP64, ctypes.byref(h)) == _lib.OK
+    assert lib.lensgb_bulk_set_fp32_alpha_max(h, -1.0) == _lib.ERR_INVALID
+    assert lib.lensgb_bulk_set_fp32_alpha_max(h, 0.1) == _lib.OK
+    assert lib.lensgb_bulk_destroy(h) == _lib.OK
+    cfg = _lib.ServerConfig(65, 0, 0, 0, 0)
+    assert lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.ERR_INVALID

@@ -180,3 +180,20 @@ def test_substructure_workload_shape():
     assert ll[:2] == ["EPL", "SHEAR"] and set(ll[2:]) == {"TNFW"}
     assert np.isclose(x.max() - x.min(), 49 * 0.01)
     assert all(k["r_trunc"] == 10 * k["Rs"] for k in kw[2:])
+
+
+def test_serving_stream_is_seeded_and_covers_the_grid():
+    reqs, psfs = W.serving_stream(n=400, psf_pool=4)
+    reqs2, _ = W.serving_stream(n=400, psf_pool=4)
+    assert [r["key"] for r in reqs] == [r["key"] for r in reqs2]
+    keys = {r["key"] for r in reqs}
+    assert {k[0] for k in keys} == {60, 100, 180, 300}
+    assert {k[1] for k in keys} == {1, 2, 4} and {k[2] for k in keys} == {11, 21, 41}
+    assert {k[3] for k in keys} == set(W.SERVING_STACKS) and {k[4] for k in keys} == {1, 2}
+    for K, p in psfs.items():
+        assert p.shape == (4, K, K) and np.allclose(p.sum(axis=(1, 2)), 1.0)
+    r = next(r for r in reqs if r["key"][3].startswith("EPL_MULTIPOLE"))
+    assert set(r["kwargs_lens"][0]) == set(profiles.LENS_PARAMS["EPL_MULTIPOLE_M1M3M4"])
+    im = W.serving_model(r["key"])
+    rows = im.pack_params(r["kwargs_lens"], r["kwargs_source"], r["kwargs_lens_light"])
+    assert rows.shape[0] == 1

@@ -333,19 +333,20 @@ def substructure_section(steps, warmup, fp32_peak, flush):
     }
 
 
-def serving_section(n_req, seed=1002):
+def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_bucket=2,
+                    use_graphs=True, loads=(0.5, 0.8, 0.95)):
     """Serving stream: capacity (all requests released at once), then Poisson
     arrivals at 0.5 / 0.8 / 0.95 x capacity with p50/p99 latency; results of a
     sample checked against the same requests computed alone."""
     import numpy as np
-    from jaxtronomy_gb300 import serving, workloads as W
+    from jaxtronomy_gb300 import _lib, serving, workloads as W
 
     reqs, psfs = W.serving_stream(seed=seed, n=n_req)
     models = {k: W.serving_model(k) for k in sorted({r["key"] for r in reqs})}
     pool = {side: [serving.pinned_empty((side, side), np.float32) for _ in range(32)]
             for side in {k[0] for k in models}}
-    srv = serving.Server(n_streams=8, max_batch=64, hbm_budget_bytes=16 << 30,
-                         contexts_per_bucket=2, use_graphs=True)
+    srv = serving.Server(n_streams=n_streams, max_batch=max_batch, hbm_budget_bytes=16 << 30,
+                         contexts_per_bucket=contexts_per_bucket, use_graphs=use_graphs)
     built = []
     t_build = time.perf_counter()
     for i, r in enumerate(reqs):
@@ -355,15 +356,25 @@ def serving_section(n_req, seed=1002):
                                  out=out))
     t_build = time.perf_counter() - t_build
 
+    arr = (_lib.Request * len(built))(*[b[0] for b in built])
+    run_lead = [0.5]
+
     def run(offsets):
-        t0 = srv.clock() + 0.2
-        for (req, _, _, _), off in zip(built, offsets):
-            req.release_ns = int((t0 + off) * 1e9)
-        tickets = srv.submit_requests(built)
+        # release times start after the submission call has surely returned
+        t0 = srv.clock() + run_lead[0]
+        rel = ((t0 + np.asarray(offsets)) * 1e9).astype(np.int64)
+        for i in range(len(built)):
+            arr[i].release_ns = int(rel[i])
+        ts = time.perf_counter()
+        tickets = srv.submit_requests(built, array=arr)
+        run.submit_s = time.perf_counter() - ts
+        run_lead[0] = 0.05 + 2 * run.submit_s
         srv.drain(900)
         times = np.array([t.times() for t in tickets])
         lat = (times[:, 2] - times[:, 0]) * 1e3
         span = times[:, 2].max() - times[:, 0].min()
+        run.wait_ms = (times[:, 1] - times[:, 0]) * 1e3
+        run.service_ms = (times[:, 2] - times[:, 1]) * 1e3
         return tickets, lat, span
 
     # warm-up: every bucket's contexts, graphs and kernels
@@ -371,14 +382,17 @@ def serving_section(n_req, seed=1002):
     _, lat_cap, span = run(np.zeros(len(built)))
     capacity = len(built) / span
     rng = np.random.default_rng(seed + 1)
-    loads = []
-    for f in (0.5, 0.8, 0.95):
+    load_lines = []
+    for f in loads:
         lam = f * capacity
         offs = np.cumsum(rng.exponential(1.0 / lam, len(built)))
         tickets, lat, span = run(offs)
-        loads.append({"load": f, "arrival_rate_per_s": lam, "served_per_s": len(built) / span,
+        load_lines.append({"load": f, "arrival_rate_per_s": lam, "served_per_s": len(built) / span,
                       "latency_ms_p50": float(np.percentile(lat, 50)),
-                      "latency_ms_p99": float(np.percentile(lat, 99))})
+                      "latency_ms_p99": float(np.percentile(lat, 99)),
+                      "queue_wait_ms_p50": float(np.percentile(run.wait_ms, 50)),
+                      "submit_call_s": run.submit_s,
+                      "service_ms_p50": float(np.percentile(run.service_ms, 50))})
     # sample of results vs the same requests alone
     worst = 0.0
     for i in rng.choice(len(reqs), 24, replace=False):
@@ -400,13 +414,16 @@ def serving_section(n_req, seed=1002):
         "capacity_requests_per_s": capacity,
         "capacity_latency_ms_p50": float(np.percentile(lat_cap, 50)),
         "capacity_latency_ms_p99": float(np.percentile(lat_cap, 99)),
-        "poisson": loads,
+        "poisson": load_lines,
         "mean_rays_per_request": float(rays),
         "served_vs_alone_max_abs_diff": worst,
-        "server": {"n_streams": 8, "max_batch": 64, "contexts_per_bucket": 2, "graphs": True,
+        "server": {"n_streams": n_streams, "max_batch": max_batch,
+                   "contexts_per_bucket": contexts_per_bucket, "graphs": use_graphs,
                    "hbm_budget_bytes": 16 << 30, "batches": st["batches"],
                    "graph_launches": st["graph_launches"], "evictions": st["evictions"],
-                   "peak_bytes": st["peak_bytes"]},
+                   "peak_bytes": st["peak_bytes"],
+                   "worker_launch_s": st["host_launch_ns"] / 1e9,
+                   "worker_capture_s": st["capture_ns"] / 1e9},
         "host_build_s": t_build,
         "timing": "server clock (host steady clock): latency = completion - release per "
                   "request; capacity = requests / makespan with all released at once",

@@ -307,6 +307,8 @@ typedef struct {
     long long evictions;
     long long bytes_held;
     long long peak_bytes;
+    long long host_launch_ns;   /* worker time spent staging and launching batches */
+    long long capture_ns;       /* of which capturing and instantiating graphs      */
 } lensgb_server_stats;
 
 /* cfg may be NULL (defaults); zero fields take their defaults.  The server

@@ -118,7 +118,7 @@ class Request(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_longlong) for n in (
         "batches", "requests_launched", "requests_done", "graph_captures", "graph_launches",
-        "evictions", "bytes_held", "peak_bytes")]
+        "evictions", "bytes_held", "peak_bytes", "host_launch_ns", "capture_ns")]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3

@@ -17,9 +17,12 @@
 //     their queue while the budget is exhausted by batches in flight;
 //   * optionally replays a CUDA graph captured for a context and batch size
 //     after its first eager run.
-// Results are written by device-to-host copies straight into the caller's
-// buffers (pinned buffers make them asynchronous) before a request is marked
-// done.
+// Each batch is one sequence of stream operations on buffers the context owns
+// -- copies of the pinned staging, gather kernels that read page-locked
+// request inputs through a pointer table, the image kernels, and a scatter
+// kernel that writes every image straight into its request's page-locked
+// host buffer (pageable buffers get a pinned staging copy, finished by the
+// worker) -- so a replayed graph needs only freshly staged inputs.
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
@@ -48,7 +51,8 @@ struct Req {
     int bucket = -1;
     std::atomic<int> state{LENSGB_REQ_QUEUED};
     int rc = LENSGB_OK;
-    bool out_pinned = false;  // image_out is page-locked: copy to it asynchronously
+    bool out_pinned = false;  // image_out is page-locked: the device writes it directly
+    int in_pinned = 0;        // bits 0..2: data / noise_map / mask are page-locked
     long long t_submit = 0, t_release = 0, t_admit = 0, t_done = 0;
 };
 
@@ -85,7 +89,10 @@ struct Context {
     double* rows_host = nullptr;  // pinned staging
     unsigned char* psf_host = nullptr;
     double* logl_host = nullptr;
-    unsigned char* img_host = nullptr;  // pinned staging for pageable image_out buffers
+    unsigned char* img_host = nullptr;  // pinned staging for pageable caller buffers
+    unsigned char* in_host = nullptr;   // pinned staging of pageable data / noise / mask
+    void** ptr_host = nullptr;          // pinned pointer tables: out[cap], data, noise, mask
+    void** ptr_dev = nullptr;
     bool busy = false;
     long long last_used = 0;
     std::vector<Req*> batch;
@@ -167,7 +174,13 @@ void free_context_buffers(Context* c) {
     cudaFreeHost(c->psf_host);
     cudaFreeHost(c->logl_host);
     cudaFreeHost(c->img_host);
+    cudaFreeHost(c->in_host);
+    cudaFreeHost(c->ptr_host);
+    cudaFree(c->ptr_dev);
     c->img_host = nullptr;
+    c->in_host = nullptr;
+    c->ptr_host = nullptr;
+    c->ptr_dev = nullptr;
     c->rows_dev = nullptr;
     c->psf_dev = c->img_dev = nullptr;
     c->data_dev = c->noise_dev = c->mask_dev = c->logl_dev = nullptr;
@@ -222,11 +235,15 @@ int grow_context(lensgb_server* s, Context* c, int n) {
               cudaMallocHost(&c->rows_host, cap * P * 8 + 8) == cudaSuccess &&
               cudaMallocHost(&c->psf_host, cap * (size_t)b.k2 * b.esz + 16) == cudaSuccess &&
               cudaMallocHost(&c->logl_host, cap * 8) == cudaSuccess &&
-              cudaMallocHost(&c->img_host, cap * np * b.esz) == cudaSuccess;
+              cudaMallocHost(&c->img_host, cap * np * b.esz) == cudaSuccess &&
+              cudaMallocHost(&c->ptr_host, cap * 4 * sizeof(void*)) == cudaSuccess &&
+              cudaMalloc(&c->ptr_dev, cap * 4 * sizeof(void*)) == cudaSuccess;
     if (ok && b.key.likelihood) {
         ok = cudaMalloc(&c->data_dev, cap * np * 8) == cudaSuccess;
         if (ok && b.key.has_noise) ok = cudaMalloc(&c->noise_dev, cap * np * 8) == cudaSuccess;
         if (ok && b.key.has_mask) ok = cudaMalloc(&c->mask_dev, cap * np * 8) == cudaSuccess;
+        const int planes = 1 + b.key.has_noise + b.key.has_mask;
+        if (ok) ok = cudaMallocHost(&c->in_host, cap * planes * np * 8) == cudaSuccess;
     }
     if (ok) ok = lensgb_model_reserve(c->model, cap) == LENSGB_OK;
     if (!ok) {
@@ -259,61 +276,127 @@ Context* new_context(lensgb_server* s, int bucket) {
     return c;
 }
 
-// Launch sequence of one batch on the context's stream (graph-capturable:
-// only stream operations on buffers owned by the context).
+// Copies n blocks of `bytes` between a contiguous device array and the
+// per-request buffers named by a pointer table (page-locked host memory, which
+// the GPU reads and writes directly).  to_table = 1: device -> table.
+__global__ void table_copy_kernel(unsigned char* dev, void* const* table, size_t bytes,
+                                  int to_table) {
+    const int i = blockIdx.y;
+    unsigned char* d = dev + (size_t)i * bytes;
+    unsigned char* h = (unsigned char*)table[i];
+    const uintptr_t al = ((uintptr_t)d) | ((uintptr_t)h) | (uintptr_t)bytes;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((al & 15) == 0) {
+        uint4* dv = (uint4*)d;
+        uint4* hv = (uint4*)h;
+        for (size_t j = k; j < bytes / 16; j += stride) {
+            if (to_table)
+                hv[j] = dv[j];
+            else
+                dv[j] = hv[j];
+        }
+    } else if ((al & 3) == 0) {
+        unsigned* dw = (unsigned*)d;
+        unsigned* hw = (unsigned*)h;
+        for (size_t j = k; j < bytes / 4; j += stride) {
+            if (to_table)
+                hw[j] = dw[j];
+            else
+                dw[j] = hw[j];
+        }
+    } else {
+        for (size_t j = k; j < bytes; j += stride) {
+            if (to_table)
+                h[j] = d[j];
+            else
+                d[j] = h[j];
+        }
+    }
+}
+
+void table_copy(unsigned char* dev, void* const* table, size_t bytes, int n, int to_table,
+                cudaStream_t st) {
+    const size_t units = (bytes % 16 == 0) ? bytes / 16 : (bytes % 4 == 0 ? bytes / 4 : bytes);
+    unsigned bx = (unsigned)std::min<size_t>((units + 255) / 256, 64);
+    dim3 grid(bx > 0 ? bx : 1, (unsigned)n);
+    table_copy_kernel<<<grid, 256, 0, st>>>(dev, table, bytes, to_table);
+}
+
+// Launch sequence of one batch on the context's stream.  Graph-capturable:
+// stream operations only, on buffers owned by the context (pinned staging,
+// pointer tables, device arrays), so a replay needs only fresh staging.
 int launch_batch(lensgb_server* s, Context* c, int n) {
     Bucket& b = *s->wb[c->bucket];
     cudaStream_t st = c->stream;
     const size_t P = (size_t)b.n_params;
+    const int planes = b.key.likelihood ? 1 + b.key.has_noise + b.key.has_mask : 0;
     if (cudaMemcpyAsync(c->rows_dev, c->rows_host, n * P * 8, cudaMemcpyHostToDevice, st) !=
-        cudaSuccess)
+            cudaSuccess ||
+        (b.k2 > 0 && cudaMemcpyAsync(c->psf_dev, c->psf_host, n * (size_t)b.k2 * b.esz,
+                                     cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+        cudaMemcpyAsync(c->ptr_dev, c->ptr_host, (size_t)c->cap * (1 + planes) * sizeof(void*),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
         return LENSGB_ERR_CUDA;
-    if (b.k2 > 0 && cudaMemcpyAsync(c->psf_dev, c->psf_host, n * (size_t)b.k2 * b.esz,
-                                    cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return LENSGB_ERR_CUDA;
-    if (!b.key.likelihood)
-        return lensgb_image(c->model, c->rows_dev, n, c->psf_dev, b.k2, c->img_dev, 0, st);
-    lensgb_noise_desc nd;
-    memset(&nd, 0, sizeof nd);
-    nd.data_dev = c->data_dev;
-    nd.data_stride = b.npix;
-    nd.noise_map_dev = c->noise_dev;
-    nd.noise_stride = c->noise_dev ? b.npix : 0;
-    nd.mask_dev = c->mask_dev;
-    nd.mask_stride = c->mask_dev ? b.npix : 0;
-    nd.exposure_time = b.key.exposure_time;
-    nd.background_rms = b.key.background_rms;
-    int rc = lensgb_loglike(c->model, c->rows_dev, n, c->psf_dev, b.k2, &nd, c->img_dev,
+    int rc;
+    if (!b.key.likelihood) {
+        rc = lensgb_image(c->model, c->rows_dev, n, c->psf_dev, b.k2, c->img_dev, 0, st);
+    } else {
+        const size_t bytes = (size_t)b.npix * 8;
+        int plane = 1;
+        table_copy((unsigned char*)c->data_dev, c->ptr_dev + plane++ * c->cap, bytes, n, 0, st);
+        if (c->noise_dev)
+            table_copy((unsigned char*)c->noise_dev, c->ptr_dev + plane++ * c->cap, bytes, n, 0, st);
+        if (c->mask_dev)
+            table_copy((unsigned char*)c->mask_dev, c->ptr_dev + plane++ * c->cap, bytes, n, 0, st);
+        lensgb_noise_desc nd;
+        memset(&nd, 0, sizeof nd);
+        nd.data_dev = c->data_dev;
+        nd.data_stride = b.npix;
+        nd.noise_map_dev = c->noise_dev;
+        nd.noise_stride = c->noise_dev ? b.npix : 0;
+        nd.mask_dev = c->mask_dev;
+        nd.mask_stride = c->mask_dev ? b.npix : 0;
+        nd.exposure_time = b.key.exposure_time;
+        nd.background_rms = b.key.background_rms;
+        rc = lensgb_loglike(c->model, c->rows_dev, n, c->psf_dev, b.k2, &nd, c->img_dev,
                             c->logl_dev, st);
+        if (rc == LENSGB_OK && cudaMemcpyAsync(c->logl_host, c->logl_dev, n * 8,
+                                               cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = LENSGB_ERR_CUDA;
+    }
     if (rc) return rc;
-    if (cudaMemcpyAsync(c->logl_host, c->logl_dev, n * 8, cudaMemcpyDeviceToHost, st) !=
-        cudaSuccess)
-        return LENSGB_ERR_CUDA;
-    return LENSGB_OK;
+    // every image to its request's host buffer (or the pinned staging)
+    table_copy((unsigned char*)c->img_dev, c->ptr_dev, (size_t)b.npix * b.esz, n, 1, st);
+    return cudaGetLastError() == cudaSuccess ? LENSGB_OK : LENSGB_ERR_CUDA;
 }
 
 int run_batch(lensgb_server* s, Context* c, int n) {
     Bucket& b = *s->wb[c->bucket];
     cudaStream_t st = c->stream;
-    // stage the small per-request inputs in pinned memory
+    // stage the small per-request inputs and the pointer tables in pinned memory
     const size_t P = (size_t)b.n_params;
+    const size_t ib = (size_t)b.npix * b.esz;
+    const size_t pb = (size_t)b.npix * 8;
+    const int planes = b.key.likelihood ? 1 + b.key.has_noise + b.key.has_mask : 0;
     for (int i = 0; i < n; ++i) {
-        const lensgb_request& r = c->batch[i]->r;
+        const Req* q = c->batch[i];
+        const lensgb_request& r = q->r;
         memcpy(c->rows_host + i * P, r.params, P * 8);
         if (b.k2 > 0) memcpy(c->psf_host + i * (size_t)b.k2 * b.esz, r.psf, (size_t)b.k2 * b.esz);
-    }
-    // the large per-request arrays go straight from the caller's buffers
-    if (b.key.likelihood) {
-        const size_t bytes = (size_t)b.npix * 8;
-        for (int i = 0; i < n; ++i) {
-            const lensgb_request& r = c->batch[i]->r;
-            if (cudaMemcpyAsync(c->data_dev + i * b.npix, r.data, bytes, cudaMemcpyHostToDevice,
-                                st) != cudaSuccess ||
-                (c->noise_dev && cudaMemcpyAsync(c->noise_dev + i * b.npix, r.noise_map, bytes,
-                                                 cudaMemcpyHostToDevice, st) != cudaSuccess) ||
-                (c->mask_dev && cudaMemcpyAsync(c->mask_dev + i * b.npix, r.mask, bytes,
-                                                cudaMemcpyHostToDevice, st) != cudaSuccess))
-                return LENSGB_ERR_CUDA;
+        c->ptr_host[i] = (r.image_out && q->out_pinned) ? r.image_out : (void*)(c->img_host + i * ib);
+        const void* src[3] = {r.data, r.noise_map, r.mask};
+        const bool use[3] = {true, b.key.has_noise != 0, b.key.has_mask != 0};
+        for (int k = 0, plane = 1; k < 3 && plane <= planes; ++k) {
+            if (!use[k]) continue;
+            void* p = (void*)src[k];
+            if (!(q->in_pinned & (1 << k))) {
+                // pageable input: stage it in pinned memory for the device to read
+                p = c->in_host + ((size_t)(plane - 1) * c->cap + i) * pb;
+                memcpy(p, src[k], pb);
+            }
+            c->ptr_host[(size_t)plane * c->cap + i] = p;
+            ++plane;
         }
     }
     int rc = LENSGB_OK;
@@ -323,6 +406,7 @@ int run_batch(lensgb_server* s, Context* c, int n) {
         s->stats.graph_launches++;
     } else if (s->cfg.use_graphs && c->eager_runs[n] >= 1) {
         // the same context and size ran eagerly before: capture and replay
+        const long long tc = s->now();
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
@@ -338,6 +422,7 @@ int run_batch(lensgb_server* s, Context* c, int n) {
         }
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();
+        s->stats.capture_ns += s->now() - tc;
         if (exec) {
             if (cudaGraphLaunch(exec, st) != cudaSuccess) return LENSGB_ERR_CUDA;
             s->stats.graph_launches++;
@@ -349,17 +434,6 @@ int run_batch(lensgb_server* s, Context* c, int n) {
         rc = launch_batch(s, c, n);
         if (rc) return rc;
         c->eager_runs[n]++;
-    }
-    // results straight into page-locked caller buffers; pageable ones are
-    // staged and copied by the worker when the batch completes
-    const size_t ib = (size_t)b.npix * b.esz;
-    for (int i = 0; i < n; ++i) {
-        const Req* q = c->batch[i];
-        if (!q->r.image_out) continue;
-        void* dst = q->out_pinned ? q->r.image_out : (void*)(c->img_host + i * ib);
-        if (cudaMemcpyAsync(dst, (unsigned char*)c->img_dev + i * ib, ib, cudaMemcpyDeviceToHost,
-                            st) != cudaSuccess)
-            return LENSGB_ERR_CUDA;
     }
     if (cudaEventRecord(c->done, st) != cudaSuccess) return LENSGB_ERR_CUDA;
     return LENSGB_OK;
@@ -461,7 +535,9 @@ bool launch_one(lensgb_server* s) {
     s->inflight++;
     s->stats.batches++;
     s->stats.requests_launched += nb;
+    const long long tl = s->now();
     rc = run_batch(s, c, nb);
+    s->stats.host_launch_ns += s->now() - tl;
     if (rc != LENSGB_OK) {
         cudaStreamSynchronize(c->stream);
         cudaGetLastError();
@@ -519,6 +595,16 @@ void worker_main(lensgb_server* s) {
             cudaEventSynchronize(c->done);
             finish_batch(s, c, LENSGB_OK);
         }
+}
+
+// Page-locked (cudaHostAlloc / registered) host memory, which the device can
+// read and write through the same address.
+bool is_pinned(const void* p) {
+    cudaPointerAttributes pa;
+    const bool ok = cudaPointerGetAttributes(&pa, p) == cudaSuccess &&
+                    pa.type == cudaMemoryTypeHost && pa.devicePointer == p;
+    cudaGetLastError();
+    return ok;
 }
 
 int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
@@ -585,8 +671,8 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
     if (!s) return serr(LENSGB_ERR_INVALID, "null server");
     if (n < 0 || (n > 0 && (!reqs || !tickets)))
         return serr(LENSGB_ERR_INVALID, "null request array or tickets");
-    std::lock_guard<std::mutex> lock(s->mu);
-    const long long t = s->now();
+    // validation and pointer queries outside the lock the worker needs
+    std::vector<int> pinned((size_t)n, 0);
     for (int i = 0; i < n; ++i) {
         const lensgb_request& r = reqs[i];
         if (!r.params) return serr(LENSGB_ERR_INVALID, "request without params");
@@ -594,26 +680,35 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
             return serr(LENSGB_ERR_INVALID, "request without a PSF kernel");
         if (r.data && r.noise_map == nullptr && !(r.exposure_time > 0))
             return serr(LENSGB_ERR_INVALID, "likelihood request needs exposure_time > 0");
-        int bucket = -1;
-        int rc = bucket_for(s, r, &bucket);
-        if (rc) return rc;
-        s->reqs.emplace_back();
-        Req& q = s->reqs.back();
-        q.r = r;
-        q.ticket = (long long)s->reqs.size() - 1;
-        q.bucket = bucket;
-        q.t_submit = t;
-        q.t_release = r.release_ns > t ? r.release_ns : t;
-        if (r.image_out) {
-            cudaPointerAttributes pa;
-            q.out_pinned = cudaPointerGetAttributes(&pa, r.image_out) == cudaSuccess &&
-                           pa.type == cudaMemoryTypeHost;
-            cudaGetLastError();
-        }
-        s->incoming.push_back(&q);
-        tickets[i] = q.ticket;
+        const void* in[3] = {r.data, r.noise_map, r.mask};
+        for (int k = 0; k < 3; ++k)
+            if (in[k] && is_pinned(in[k])) pinned[(size_t)i] |= 1 << k;
+        if (r.image_out && is_pinned(r.image_out)) pinned[(size_t)i] |= 8;
     }
-    s->cv.notify_one();
+    // enqueue in chunks, so that a large submission does not stall the worker
+    constexpr int CHUNK = 256;
+    for (int i0 = 0; i0 < n; i0 += CHUNK) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        const long long t = s->now();
+        for (int i = i0; i < n && i < i0 + CHUNK; ++i) {
+            const lensgb_request& r = reqs[i];
+            int bucket = -1;
+            int rc = bucket_for(s, r, &bucket);
+            if (rc) return rc;
+            s->reqs.emplace_back();
+            Req& q = s->reqs.back();
+            q.r = r;
+            q.ticket = (long long)s->reqs.size() - 1;
+            q.bucket = bucket;
+            q.t_submit = t;
+            q.t_release = r.release_ns > t ? r.release_ns : t;
+            q.out_pinned = (pinned[(size_t)i] & 8) != 0;
+            q.in_pinned = pinned[(size_t)i] & 7;
+            s->incoming.push_back(&q);
+            tickets[i] = q.ticket;
+        }
+        s->cv.notify_one();
+    }
     return LENSGB_OK;
 }
 

@@ -30,6 +30,7 @@ class Ticket:
         self._keep = keep           # inputs that must stay alive until done
 
     def state(self):
+        self.server._check_open()
         st = ctypes.c_int(0)
         _lib.check(_lib.load().lensgb_server_poll(self.server._h, self.ticket, ctypes.byref(st)))
         return st.value
@@ -39,6 +40,7 @@ class Ticket:
 
     def result(self, timeout=60.0):
         """Waits for the request; returns the image (and logL for likelihood requests)."""
+        self.server._check_open()
         st = ctypes.c_int(0)
         _lib.check(_lib.load().lensgb_server_wait(self.server._h, self.ticket, float(timeout),
                                                   ctypes.byref(st)))
@@ -51,6 +53,7 @@ class Ticket:
 
     def times(self):
         """(release, admit, done) in seconds on the server clock (-1: not reached)."""
+        self.server._check_open()
         r, a, d = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
         _lib.check(_lib.load().lensgb_server_request_times(
             self.server._h, self.ticket, ctypes.byref(r), ctypes.byref(a), ctypes.byref(d)))
@@ -70,6 +73,10 @@ class Server:
         lib = _lib.load()
         _lib.check(lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
+
+    def _check_open(self):
+        if not self._h:
+            raise RuntimeError("the server is closed; read results before closing it")
 
     def clock(self):
         """Server clock in seconds (the time base of ``release_s``)."""
@@ -147,10 +154,11 @@ class Server:
                                             kwargs_lens_light, **kw)
         return self.submit_requests([(req, keep, out, logl)])[0]
 
-    def submit_requests(self, built):
-        """Submits requests built by :meth:`request` in one call."""
+    def submit_requests(self, built, array=None):
+        """Submits requests built by :meth:`request` in one call (``array``: a
+        ctypes array of their Request structs, e.g. kept between submissions)."""
         n = len(built)
-        arr = (_lib.Request * n)(*[b[0] for b in built])
+        arr = (_lib.Request * n)(*[b[0] for b in built]) if array is None else array
         tickets = (ctypes.c_longlong * n)()
         _lib.check(_lib.load().lensgb_server_submit(self._h, arr, n, tickets))
         return [Ticket(self, tickets[i], built[i][2], built[i][3], built[i][1]) for i in range(n)]

@@ -124,7 +124,7 @@ def test_struct_sizes_match_the_header_layout():
     """ctypes mirrors of the public structs have the C layout (x86-64 / aarch64 LP64)."""
     assert ctypes.sizeof(_lib.NoiseDesc) == 11 * 8
     assert ctypes.sizeof(_lib.ServerConfig) == 4 + 4 + 8 + 4 + 4
-    assert ctypes.sizeof(_lib.ServerStats) == 8 * 8
+    assert ctypes.sizeof(_lib.ServerStats) == 10 * 8
     assert ctypes.sizeof(_lib.Request) == ctypes.sizeof(_lib.ModelDesc) + 10 * 8
 
 

@@ -195,6 +195,16 @@ int lensgb_loglike(lensgb_model* model, const double* params_dev, int n_inst,
                    const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
                    void* image_out_dev, double* logl_dev, void* stream);
 
+/* Gradient of ImageModel.likelihood_data_given_model with respect to every
+ * column of the system rows -- what jax.grad of the reference's likelihood
+ * returns for the kwargs (test_image_model.py:274-335) -- by a hand-written
+ * adjoint that recomputes the ray grid.  Same arguments as lensgb_loglike plus
+ * grad_dev: n_inst x param_count doubles, row layout.  FP64 models only; lens
+ * stacks of EPL and SHEAR, SERSIC / SERSIC_ELLIPSE light, PSF NONE or PIXEL. */
+int lensgb_loglike_grad(lensgb_model* model, const double* params_dev, int n_inst,
+                        const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
+                        void* image_out_dev, double* logl_dev, double* grad_dev, void* stream);
+
 /* SinglePlane.ray_shooting for one parameter set over n arbitrary points
  * (single_plane.py:39-56), FP64.  params_dev holds the lens profiles' kwargs
  * only (the lens part of a system row). */

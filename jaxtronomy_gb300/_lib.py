@@ -39,6 +39,7 @@ SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
+    "lensgb_loglike_grad",
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
     "lensgb_bulk_create", "lensgb_bulk_destroy", "lensgb_bulk_set_fp32_alpha_max",
@@ -163,6 +164,9 @@ def load():
     lib.lensgb_convolve.restype = i
     lib.lensgb_loglike.argtypes = [vp, dp, i, vp, ll, ctypes.POINTER(NoiseDesc), vp, dp, vp]
     lib.lensgb_loglike.restype = i
+    lib.lensgb_loglike_grad.argtypes = [vp, dp, i, vp, ll, ctypes.POINTER(NoiseDesc), vp, dp, dp,
+                                        vp]
+    lib.lensgb_loglike_grad.restype = i
     lib.lensgb_ray_shooting.argtypes = [vp, dp, dp, dp, dp, dp, ll, vp]
     lib.lensgb_ray_shooting.restype = i
     lib.lensgb_alpha.argtypes = [vp, dp, dp, dp, dp, dp, ll, vp]

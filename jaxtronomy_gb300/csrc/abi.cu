@@ -28,7 +28,24 @@ struct lensgb_model {
     unsigned int* refine_count = nullptr;
     float refine_tau = 2e-5f;             // see lensgb_model_set_refine
     float refine_kappa = 3e-7f;
+    // gradient scratch (lensgb_loglike_grad), grow-only
+    int grad_cap = 0;
+    double* g_dcoef = nullptr;
+    double* g_psf = nullptr;
+    double* g_m = nullptr;
+    double* g_low = nullptr;
+    double* g_partial = nullptr;
 };
+
+static void free_grad_scratch(lensgb_model* m) {
+    cudaFree(m->g_dcoef);
+    cudaFree(m->g_psf);
+    cudaFree(m->g_m);
+    cudaFree(m->g_low);
+    cudaFree(m->g_partial);
+    m->g_dcoef = m->g_psf = m->g_m = m->g_low = m->g_partial = nullptr;
+    m->grad_cap = 0;
+}
 
 static thread_local std::string g_last_error;
 
@@ -274,9 +291,12 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     return LENSGB_OK;
 }
 
+static int ensure_grad_scratch(lensgb_model* m, int n_inst);
+
 int lensgb_model_destroy(lensgb_model* m) {
     if (!m) return LENSGB_OK;
     free_scratch(m);
+    free_grad_scratch(m);
     delete m;
     return LENSGB_OK;
 }
@@ -372,6 +392,75 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     launch_loglike(image_out, n_inst, (long long)m->grid.nx * m->grid.ny, a, logl,
                    m->desc.precision, (cudaStream_t)stream);
     return check_cuda("likelihood launch");
+}
+
+static int ensure_grad_scratch(lensgb_model* m, int n_inst) {
+    if (n_inst <= m->grad_cap) return LENSGB_OK;
+    int cap = m->grad_cap > 0 ? m->grad_cap : 1;
+    while (cap < n_inst) cap *= 2;
+    free_grad_scratch(m);
+    const size_t npix = (size_t)m->grid.nx * m->grid.ny;
+    const size_t kk = (size_t)m->desc.kernel_size * m->desc.kernel_size;
+    const size_t ncoef = (size_t)cap * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
+    const size_t npart = (size_t)cap * grad_chunks(m->grid) * (m->st.n_params > 0 ? m->st.n_params : 1);
+    if (cudaMalloc(&m->g_dcoef, ncoef * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->g_psf, (size_t)cap * (kk > 0 ? kk : 1) * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->g_m, (size_t)cap * npix * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->g_low, (size_t)cap * npix * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->g_partial, npart * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        free_grad_scratch(m);
+        return fail(LENSGB_ERR_OOM, "device allocation of gradient scratch failed");
+    }
+    m->grad_cap = cap;
+    return LENSGB_OK;
+}
+
+int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                        long long psf_stride, const lensgb_noise_desc* nd, void* image_out,
+                        double* logl, double* grad, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (m->desc.precision != LENSGB_FP64)
+        return fail(LENSGB_ERR_UNSUPPORTED, "the likelihood gradient needs an FP64 model");
+    if (m->desc.psf_type == LENSGB_PSF_GAUSSIAN)
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "the likelihood gradient supports PSF types NONE and PIXEL (the transposed "
+                    "edge-padded convolution is not provided)");
+    if (!grad_supported(m->st))
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "the likelihood gradient supports lens stacks of EPL and SHEAR and Sersic "
+                    "light profiles, with at most 64 parameters per system");
+    if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
+    if (!image_out || !logl || !grad) return fail(LENSGB_ERR_INVALID, "null output pointer");
+    if (!nd->noise_map_dev && !nd->exposure_map_dev && !(nd->exposure_time > 0))
+        return fail(LENSGB_ERR_INVALID, "exposure time must be positive without a noise map");
+    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0 ||
+        nd->mask_stride < 0)
+        return fail(LENSGB_ERR_INVALID, "negative stride");
+    int rc = lensgb_image(m, params, n_inst, psf, psf_stride, image_out, 0, stream);
+    if (rc) return rc;
+    if (n_inst == 0) return LENSGB_OK;
+    if ((rc = ensure_grad_scratch(m, n_inst))) return rc;
+    LoglikeArgs a;
+    a.data = nd->data_dev;
+    a.data_stride = nd->data_stride;
+    a.mask = nd->mask_dev;
+    a.mask_stride = nd->mask_stride;
+    a.noise_map = nd->noise_map_dev;
+    a.noise_stride = nd->noise_stride;
+    a.exposure = nd->exposure_map_dev;
+    a.exposure_stride = nd->exposure_stride;
+    a.exposure_time = nd->exposure_time;
+    a.background_rms = nd->background_rms;
+    a.error_map = nd->error_map_dev;
+    const bool conv = m->desc.psf_type == LENSGB_PSF_PIXEL;
+    if (launch_loglike_grad(m->grid, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef,
+                            (const double*)image_out, a, conv ? (const double*)psf : nullptr,
+                            psf_stride, m->desc.kernel_size, m->g_psf, m->g_m, m->g_low,
+                            m->g_partial, m->pixel_width * m->pixel_width, logl, grad,
+                            (cudaStream_t)stream))
+        return fail(LENSGB_ERR_CUDA, "transposed convolution shared-memory configuration failed");
+    return check_cuda("likelihood gradient launch");
 }
 
 static int ray_points(const lensgb_model* mc, const double* params, const double* x,

@@ -1,0 +1,540 @@
+// Adjoint gradient of the image log-likelihood with respect to every
+// parameter of every system row: d logL / d params, FP64.
+//
+// The reference differentiates ImageModel.likelihood_data_given_model with
+// jax.grad (reverse mode through the XLA program, storing its intermediates;
+// image_model.py:163-221, test_image_model.py:274-335).  Here the chain is
+// written out and the ray grid is recomputed instead of stored:
+//   1. logL and g_m = d logL / d m per pixel (residual weights of the
+//      model-dependent variance  C = max(m,0)/t_exp + sigma_bkg^2 (+|err|) or
+//      noise_map^2; imaging_data.py:159-182, image_noise.py:100-137);
+//   2. g_low = conv^T(g_m): the transposed "same"-mode zero-padded convolution
+//      is the convolution with the kernel rotated by 180 degrees;
+//   3. one thread per pixel recomputes its s^2 rays, forward-mode derivatives
+//      of each lens deflection (EPL through its hypergeometric series, with
+//      dF_n/dt tables; SHEAR) and of each Sersic profile, and accumulates
+//      w * d flux / d p with w = g_low * pixel_width^2 / s^2 * flux_scaling;
+//      the source terms reach the lens parameters through
+//      d beta / d p = -alpha_scaling * deflection_scaling * d alpha / d p;
+//   4. per-CTA partial sums are reduced in a fixed order (deterministic).
+// The EPL derivative uses the series of the forward pass (nmax(f) terms); the
+// reference's custom JVP differentiates a 100-term series (epl.py:321-340),
+// which differs from it by at most the series truncation (< 1e-10 relative).
+#include "launch.h"
+#include "profiles.cuh"
+#include "raytrace_kernels.cuh"
+
+namespace lensgb {
+
+constexpr int GRAD_THREADS = 128;
+constexpr int GRAD_PPT = 2;  // pixels per thread
+
+// ---------------------------------------------------------------------------
+// forward-mode dual numbers with 5 tangent directions (b, t, q, x1, y1)
+// ---------------------------------------------------------------------------
+struct D5 {
+    double v;
+    double d[5];
+};
+
+__device__ __forceinline__ D5 dconst(double v) {
+    D5 r;
+    r.v = v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = 0.0;
+    return r;
+}
+__device__ __forceinline__ D5 dvar(double v, int k) {
+    D5 r = dconst(v);
+    r.d[k] = 1.0;
+    return r;
+}
+__device__ __forceinline__ D5 operator+(const D5& a, const D5& b) {
+    D5 r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 operator-(const D5& a, const D5& b) {
+    D5 r;
+    r.v = a.v - b.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 operator*(const D5& a, const D5& b) {
+    D5 r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = a.v * b.d[k] + b.v * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 operator*(double s, const D5& a) {
+    D5 r;
+    r.v = s * a.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = s * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 operator+(double s, const D5& a) {
+    D5 r = a;
+    r.v += s;
+    return r;
+}
+__device__ __forceinline__ D5 dinv(const D5& a) {
+    D5 r;
+    r.v = 1.0 / a.v;
+    const double g = -r.v * r.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 dlog(const D5& a) {
+    D5 r;
+    r.v = log(a.v);
+    const double g = 1.0 / a.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 dexp(const D5& a) {
+    D5 r;
+    r.v = exp(a.v);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = r.v * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 dsqrt(const D5& a) {
+    D5 r;
+    r.v = sqrt(a.v);
+    const double g = 0.5 / r.v;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+
+// EPL deflection (epl.py:179-200,366-394) and its Jacobian with respect to
+// (theta_E, gamma, e1, e2, center_x, center_y): J[0][k] = d alpha_x / d p_k,
+// J[1][k] = d alpha_y / d p_k.  `a` is the profile's raw parameter row.
+__device__ void epl_alpha_grad(const double* rec, const double* F, const double* dF,
+                               const double* a, double dx, double dy, double& ax, double& ay,
+                               double J[2][6]) {
+    const double b = rec[2], t = rec[3], q = rec[4], c = rec[5], sn = rec[6];
+    const int nmax = (int)rec[8];
+    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5 B = dvar(b, 0), T = dvar(t, 1), Q = dvar(q, 2);
+    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5 Za = Q * X1, Zb = Y1;
+    const D5 r2 = Za * Za + Zb * Zb;
+    for (int i = 0; i < 2; ++i)
+        for (int k = 0; k < 6; ++k) J[i][k] = 0.0;
+    ax = 0.0;
+    ay = 0.0;
+    if (r2.v == 0.0) return;  // reference: 0/0 -> NaN -> nan_to_num -> 0
+    D5 hr = dconst(1.0), hi = dconst(0.0);
+    if (nmax > 0) {
+        const D5 f = (1.0 + (-1.0) * Q) * dinv(1.0 + Q);
+        const D5 inv = dinv(r2);
+        const D5 zr = (-1.0) * f * (Za * Za - Zb * Zb) * inv;
+        const D5 zi = (-2.0) * f * Za * Zb * inv;
+        const D5 dr = zr + dconst(-2.0), di = zi;
+        const D5 dd = dinv(dr * dr + di * di);
+        const D5 wr = (zr * dr + zi * di) * dd;
+        const D5 wi = (zi * dr - zr * di) * dd;
+        D5 sr = dconst(F[nmax - 1]);
+        sr.d[1] = dF[nmax - 1];
+        D5 si = dconst(0.0);
+        for (int n = nmax - 2; n >= 0; --n) {
+            D5 fn = dconst(F[n]);
+            fn.d[1] = dF[n];
+            const D5 nr = sr * wr - si * wi + fn;
+            const D5 ni = sr * wi + si * wr;
+            sr = nr;
+            si = ni;
+        }
+        const D5 er = 1.0 + (-0.5) * zr, ei = (-0.5) * zi;
+        const D5 ee = dinv(er * er + ei * ei);
+        hr = (sr * er + si * ei) * ee;
+        hi = (si * er - sr * ei) * ee;
+    }
+    D5 R = dsqrt(r2);
+    if (R.v < 1e-9) R = dconst(1e-9);
+    // 2/(1+q) (b/R)^t
+    const D5 amp = 2.0 * dinv(1.0 + Q) * dexp(T * (dlog(B) - dlog(R)));
+    const D5 fx = amp * (Za * hr - Zb * hi);
+    const D5 fy = amp * (Za * hi + Zb * hr);
+    ax = fx.v * c - fy.v * sn;
+    ay = fx.v * sn + fy.v * c;
+    // rotate the major-axis derivatives back
+    double dA[2][5];
+    for (int k = 0; k < 5; ++k) {
+        dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
+        dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
+    }
+    // d alpha / d phi = Rot(phi) [ (-fy, fx) + J_maj (y1, -x1) ]
+    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    // d alpha / d (dx, dy) = Rot(phi) J_maj Rot(-phi); (x1, y1) = Rot(-phi) (dx, dy)
+    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    // chain to (theta_E, gamma, e1, e2): b = theta_E sqrt(q), t = gamma - 1,
+    // (phi, q) from (e1, e2) (param_util.py:88-99, epl.py:111-124)
+    const double theta_E = a[0], e1 = a[2], e2 = a[3];
+    const double sq = sqrt(q);
+    const double cc2 = e1 * e1 + e2 * e2;
+    const double cc = sqrt(cc2);
+    double dq1 = 0.0, dq2 = 0.0, dp1 = 0.0, dp2 = 0.0;
+    if (cc > 0.0) {
+        if (cc < 0.9999) {
+            const double dqdc = -2.0 / ((1.0 + cc) * (1.0 + cc));
+            dq1 = dqdc * e1 / cc;
+            dq2 = dqdc * e2 / cc;
+        }
+        dp1 = -e2 / (2.0 * cc2);
+        dp2 = e1 / (2.0 * cc2);
+    }
+    const double dbdq = theta_E / (2.0 * sq);
+    for (int i = 0; i < 2; ++i) {
+        const double aph = i == 0 ? aphx : aphy;
+        const double aq = dA[i][0] * dbdq + dA[i][2];
+        J[i][0] = dA[i][0] * sq;
+        J[i][1] = dA[i][1];
+        J[i][2] = aq * dq1 + aph * dp1;
+        J[i][3] = aq * dq2 + aph * dp2;
+        J[i][4] = -(i == 0 ? jdx0 : jdx1);
+        J[i][5] = -(i == 0 ? jdy0 : jdy1);
+    }
+}
+
+// SHEAR (shear.py:39-53) and its Jacobian w.r.t. (gamma1, gamma2, ra_0, dec_0).
+__device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, double dy,
+                                                 double& ax, double& ay, double J[2][6]) {
+    const double g1 = rec[2], g2 = rec[3];
+    ax = g1 * dx + g2 * dy;
+    ay = g2 * dx - g1 * dy;
+    J[0][0] = dx;  J[1][0] = -dy;
+    J[0][1] = dy;  J[1][1] = dx;
+    J[0][2] = -g1; J[1][2] = -g2;
+    J[0][3] = -g2; J[1][3] = g1;
+    J[0][4] = J[0][5] = J[1][4] = J[1][5] = 0.0;
+}
+
+// Sersic / elliptical Sersic (sersic_ellipse.py:62-93, sersic_utils.py:69-110,
+// 239-267) at offset (dx, dy): value, gradient with respect to the offset,
+// and derivatives with respect to the raw parameters (amp, R_sersic, n_sersic,
+// [e1, e2,] center_x, center_y).
+__device__ void sersic_grad(int code, const double* rec, const double* a, double dx, double dy,
+                            double& I, double& gx, double& gy, double dI[7]) {
+    const bool ell = code == LENSGB_LIGHT_SERSIC_ELLIPSE;
+    const int np = ell ? 7 : 5;
+    for (int k = 0; k < np; ++k) dI[k] = 0.0;
+    I = 0.0;
+    gx = 0.0;
+    gy = 0.0;
+    const double amp = rec[2], Rs = rec[3], inv_n = rec[5], bn = rec[6];
+    const double m00 = rec[7], m01 = rec[8], m10 = rec[9], m11 = rec[10];
+    const double xp = m00 * dx + m01 * dy, yp = m10 * dx + m11 * dy;
+    const double Rraw = sqrt(xp * xp + yp * yp);
+    const bool floored = !(Rraw > 0.0001);
+    const double R = floored ? 0.0001 : Rraw;
+    const double frac = R / Rs;
+    if (!(frac <= 1000.0)) return;
+    const double v = pow(frac, inv_n);
+    const double res = exp(-bn * (v - 1.0));
+    I = amp * res;
+    // d ln I / d R (zero inside the smoothing floor)
+    const double dlR = floored ? 0.0 : -bn * inv_n * v / R;
+    double dRdx = 0.0, dRdy = 0.0;
+    if (!floored) {
+        dRdx = (xp * m00 + yp * m10) / R;
+        dRdy = (xp * m01 + yp * m11) / R;
+    }
+    gx = I * dlR * dRdx;
+    gy = I * dlR * dRdy;
+    const double n = a[2];
+    dI[0] = res;                                                  // amp
+    dI[1] = a[1] > 0.0001 ? I * bn * inv_n * v / Rs : 0.0;        // R_sersic (floors)
+    const double dbn = (1.9992 * n - 0.3271) > 0.00001 ? 1.9992 : 0.0;
+    dI[2] = I * (-dbn * (v - 1.0) + bn * v * log(frac) * inv_n * inv_n);  // n_sersic
+    int k = 3;
+    if (ell) {
+        const double e1 = a[3], e2 = a[4];
+        const double n2 = 1.0 - e1 * e1 - e2 * e2;
+        const double nrm_raw = sqrt(fabs(n2));
+        const bool nfl = !(nrm_raw > 0.000001);
+        const double nrm = nfl ? 0.000001 : nrm_raw;
+        const double sgn = n2 > 0 ? -1.0 : 1.0;
+        const double dn1 = nfl ? 0.0 : sgn * e1 / nrm, dn2 = nfl ? 0.0 : sgn * e2 / nrm;
+        // x' = ((1-e1) dx - e2 dy)/norm, y' = (-e2 dx + (1+e1) dy)/norm
+        const double dxp1 = -dx / nrm - xp * dn1 / nrm, dyp1 = dy / nrm - yp * dn1 / nrm;
+        const double dxp2 = -dy / nrm - xp * dn2 / nrm, dyp2 = -dx / nrm - yp * dn2 / nrm;
+        if (!floored) {
+            dI[3] = I * dlR * (xp * dxp1 + yp * dyp1) / R;
+            dI[4] = I * dlR * (xp * dxp2 + yp * dyp2) / R;
+        }
+        k = 5;
+    }
+    dI[k] = -gx;      // center_x
+    dI[k + 1] = -gy;  // center_y
+}
+
+constexpr int GRAD_MAXP = 64;
+constexpr int GRAD_MAX_LENSP = 32;
+
+__device__ __forceinline__ int lens_np(int code) {
+    return code == LENSGB_LENS_EPL ? 6 : (code == LENSGB_LENS_SHEAR ? 4 : 0);
+}
+
+// dF_n/dt of the EPL series coefficients (hyp2f1_util.py:156-166 with
+// B = t/2, C = 2 - t/2), one thread per (system, EPL profile).
+__global__ void epl_dcoef_kernel(StackDesc st, int n_inst, const double* __restrict__ rec_d,
+                                 const double* __restrict__ coef_d, double* __restrict__ dcoef) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    if (gid >= n_inst * st.n_lens) return;
+    const int inst = gid / st.n_lens, p = gid % st.n_lens;
+    const int es = st.epl_slot[p];
+    if (es < 0 || st.lens[p] != LENSGB_LENS_EPL) return;
+    const double* d = rec_d + ((long long)inst * n_prof + p) * REC_D;
+    const double* F = coef_d + ((long long)inst * st.n_epl + es) * EPL_NMAX;
+    double* dF = dcoef + ((long long)inst * st.n_epl + es) * EPL_NMAX;
+    const int nmax = (int)d[8];
+    const double t = d[3], Bc = t / 2.0, C = 2.0 - Bc, K = 2.0 * Bc - C;
+    if (nmax > 0) dF[0] = 0.0;
+    if (nmax > 1) dF[1] = -2.0 / (C * C);
+    for (int n = 2; n < nmax; ++n)
+        dF[n] = ((n - 1.0) * dF[n - 2] - 1.5 * F[n - 1] - K * dF[n - 1] + 0.5 * F[n]) /
+                (C + n - 1.0);
+}
+
+// logL (same Kahan order as loglike_kernel) and g_m = d logL / d m.
+__global__ void __launch_bounds__(256)
+loglike_weights_kernel(const double* __restrict__ model, long long npix, LoglikeArgs a,
+                       double* __restrict__ gm, double* __restrict__ out) {
+    const int inst = blockIdx.x;
+    const double* m = model + (long long)inst * npix;
+    const double* d = a.data + (long long)inst * a.data_stride;
+    const double* nm = a.noise_map ? a.noise_map + (long long)inst * a.noise_stride : nullptr;
+    const double* ex = a.exposure ? a.exposure + (long long)inst * a.exposure_stride : nullptr;
+    const double* mask = a.mask ? a.mask + (long long)inst * a.mask_stride : nullptr;
+    double* g = gm + (long long)inst * npix;
+    const double b2 = a.background_rms * a.background_rms;
+    double sum = 0.0, comp = 0.0;
+    for (long long i = threadIdx.x; i < npix; i += 256) {
+        const double mk = mask ? mask[i] : 1.0;
+        if (mk == 0.0) {
+            g[i] = 0.0;
+            continue;
+        }
+        const double mv = m[i];
+        double c, dc = 0.0;
+        if (nm) {
+            c = nm[i] * nm[i];
+        } else {
+            const double e = ex ? ex[i] : a.exposure_time;
+            c = (mv >= 0 ? mv : 0.0) / e + b2;
+            dc = mv > 0 ? 1.0 / e : 0.0;
+        }
+        if (a.error_map) c += fabs(a.error_map[i]);
+        const double r = mv - d[i];
+        const double term = r * r / c * mk;
+        const double y = term - comp;
+        const double t = sum + y;
+        comp = (t - sum) - y;
+        sum = t;
+        // logL = -1/2 sum mask r^2 / C(m)
+        g[i] = -mk * (r / c - 0.5 * r * r * dc / (c * c));
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[inst] = -red[0] / 2.0;
+}
+
+// PSF rotated by 180 degrees (the kernel of the transposed convolution).
+__global__ void flip_psf_kernel(const double* __restrict__ in, double* __restrict__ out, int K,
+                                long long in_stride, int n) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long kk = (long long)K * K;
+    if (gid >= kk * n) return;
+    const long long inst = gid / kk, j = gid % kk;
+    out[inst * kk + j] = in[inst * in_stride + (kk - 1 - j)];
+}
+
+// Step 3: per-CTA partial gradients of one system.
+__global__ void __launch_bounds__(GRAD_THREADS)
+grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
+                const double* __restrict__ rec, const double* __restrict__ coef,
+                const double* __restrict__ dcoef, const double* __restrict__ glow,
+                double w_scale, double* __restrict__ partial) {
+    extern __shared__ double smem[];
+    const int inst = blockIdx.y;
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    double* srec = smem;
+    double* scoef = srec + n_prof * REC_D;
+    double* sdcoef = scoef + st.n_epl * EPL_NMAX;
+    load_records<double>(st, rec, coef, inst, srec, scoef);
+    for (int p = 0; p < st.n_lens; ++p) {
+        const int es = st.epl_slot[p];
+        if (es < 0) continue;
+        const int nmax = (int)srec[p * REC_D + 8];
+        const double* gc = dcoef + ((long long)inst * st.n_epl + es) * EPL_NMAX;
+        for (int k = threadIdx.x; k < nmax; k += blockDim.x) sdcoef[es * EPL_NMAX + k] = gc[k];
+    }
+    __syncthreads();
+    const double* P = params + (long long)inst * st.n_params;
+    const int NP = st.n_params;
+    double acc[GRAD_MAXP];
+    for (int k = 0; k < NP; ++k) acc[k] = 0.0;
+    const long long npix = (long long)g.nx * g.ny;
+    const long long base = (long long)blockIdx.x * GRAD_THREADS * GRAD_PPT;
+    const double* gl = glow + (long long)inst * npix;
+    const double inv_s2 = 1.0 / ((double)g.s * g.s);
+    for (int kk = 0; kk < GRAD_PPT; ++kk) {
+        const long long pix = base + (long long)kk * GRAD_THREADS + threadIdx.x;
+        if (pix >= npix) break;
+        const int row = (int)(pix / g.nx), col = (int)(pix % g.nx);
+        const double w = gl[pix] * w_scale * inv_s2 * st.flux_scaling;
+        if (w == 0.0) continue;
+        for (int si = 0; si < g.s; ++si) {
+            for (int sj = 0; sj < g.s; ++sj) {
+                const int I = row * g.s + si, Jc = col * g.s + sj;
+                const double X = g.ra00 + (double)Jc * g.ax + (double)I * g.bx;
+                const double Y = g.dec00 + (double)Jc * g.ay + (double)I * g.by;
+                double axs = 0.0, ays = 0.0;
+                double dA[2][GRAD_MAX_LENSP];
+                int lp = 0;
+                for (int p = 0; p < st.n_lens; ++p) {
+                    const double* r = srec + p * REC_D;
+                    const int code = st.lens[p];
+                    const int es = st.epl_slot[p];
+                    double ax, ay, J[2][6];
+                    const double ddx = X - r[RD_CX], ddy = Y - r[RD_CY];
+                    if (code == LENSGB_LENS_EPL)
+                        epl_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
+                                       P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else
+                        shear_alpha_grad(r, ddx, ddy, ax, ay, J);
+                    axs += ax;
+                    ays += ay;
+                    const int np = lens_np(code);
+                    for (int k = 0; k < np; ++k) {
+                        dA[0][lp + k] = J[0][k];
+                        dA[1][lp + k] = J[1][k];
+                    }
+                    lp += np;
+                }
+                axs *= st.alpha_scaling;
+                ays *= st.alpha_scaling;
+                // sources at beta; G = sum_k (-alpha_scaling s_k) grad_beta I_k
+                double Gx = 0.0, Gy = 0.0;
+                for (int k = 0; k < st.n_src; ++k) {
+                    const double* r = srec + (st.n_lens + k) * REC_D;
+                    const double sc = st.src_scale[k];
+                    double Iv, gx, gy, dI[7];
+                    sersic_grad(st.src[k], r, P + st.src_off[k], X - sc * axs - r[RD_CX],
+                                Y - sc * ays - r[RD_CY], Iv, gx, gy, dI);
+                    const int np = st.src[k] == LENSGB_LIGHT_SERSIC_ELLIPSE ? 7 : 5;
+                    for (int j = 0; j < np; ++j) acc[st.src_off[k] + j] += w * dI[j];
+                    Gx -= st.alpha_scaling * sc * gx;
+                    Gy -= st.alpha_scaling * sc * gy;
+                }
+                for (int c = 0; c < lp; ++c)
+                    acc[st.lens_off[0] + c] += w * (Gx * dA[0][c] + Gy * dA[1][c]);
+                // lens light at theta
+                for (int k = 0; k < st.n_ll; ++k) {
+                    const double* r = srec + (st.n_lens + st.n_src + k) * REC_D;
+                    double Iv, gx, gy, dI[7];
+                    sersic_grad(st.ll[k], r, P + st.ll_off[k], X - r[RD_CX], Y - r[RD_CY], Iv, gx,
+                                gy, dI);
+                    const int np = st.ll[k] == LENSGB_LIGHT_SERSIC_ELLIPSE ? 7 : 5;
+                    for (int j = 0; j < np; ++j) acc[st.ll_off[k] + j] += w * dI[j];
+                }
+            }
+        }
+    }
+    // fixed-order block reduction, one parameter at a time
+    __shared__ double red[GRAD_THREADS];
+    double* out = partial + ((long long)inst * gridDim.x + blockIdx.x) * NP;
+    for (int k = 0; k < NP; ++k) {
+        red[threadIdx.x] = acc[k];
+        __syncthreads();
+        for (int s2 = GRAD_THREADS / 2; s2 > 0; s2 >>= 1) {
+            if (threadIdx.x < s2) red[threadIdx.x] += red[threadIdx.x + s2];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[k] = red[0];
+        __syncthreads();
+    }
+}
+
+__global__ void grad_reduce_kernel(const double* __restrict__ partial, int n_chunks, int NP,
+                                   int n_inst, double* __restrict__ grad) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= n_inst * NP) return;
+    const int inst = gid / NP, k = gid % NP;
+    double s = 0.0;
+    for (int c = 0; c < n_chunks; ++c) s += partial[((long long)inst * n_chunks + c) * NP + k];
+    grad[gid] = s;
+}
+
+int grad_chunks(const GridDesc& g) {
+    const long long npix = (long long)g.nx * g.ny;
+    return (int)((npix + GRAD_THREADS * GRAD_PPT - 1) / (GRAD_THREADS * GRAD_PPT));
+}
+
+bool grad_supported(const StackDesc& st) {
+    if (st.n_params > GRAD_MAXP) return false;
+    int lp = 0;
+    for (int p = 0; p < st.n_lens; ++p) {
+        if (st.lens[p] != LENSGB_LENS_EPL && st.lens[p] != LENSGB_LENS_SHEAR) return false;
+        lp += st.lens[p] == LENSGB_LENS_EPL ? 6 : 4;
+        if (p > 0 && st.lens_off[p] != st.lens_off[p - 1] + (st.lens[p - 1] == LENSGB_LENS_EPL ? 6 : 4))
+            return false;
+    }
+    return lp <= GRAD_MAX_LENSP;
+}
+
+int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
+                        const double* rec_d, const double* coef_d, double* dcoef,
+                        const double* image, const LoglikeArgs& la, const double* psf,
+                        long long psf_stride, int K, double* psf_flip, double* gm, double* glow,
+                        double* partial, double pixel_area, double* logl, double* grad,
+                        cudaStream_t stream) {
+    const long long npix = (long long)g.nx * g.ny;
+    if (st.n_lens > 0) {
+        const int n = n_inst * st.n_lens;
+        epl_dcoef_kernel<<<(n + 127) / 128, 128, 0, stream>>>(st, n_inst, rec_d, coef_d, dcoef);
+    }
+    loglike_weights_kernel<<<n_inst, 256, 0, stream>>>(image, npix, la, gm, logl);
+    const double* gl = gm;
+    if (psf) {
+        const long long kk = (long long)K * K;
+        const long long n = kk * n_inst;
+        flip_psf_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(psf, psf_flip, K,
+                                                                          psf_stride, n_inst);
+        if (launch_conv(gm, glow, psf_flip, kk, n_inst, g.ny, g.nx, K, 0, LENSGB_FP64, stream))
+            return -1;
+        gl = glow;
+    }
+    const int chunks = grad_chunks(g);
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    const size_t smem = (size_t)(n_prof * REC_D + 2 * st.n_epl * EPL_NMAX) * sizeof(double);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(grad_ray_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    grad_ray_kernel<<<dim3((unsigned)chunks, (unsigned)n_inst), GRAD_THREADS, smem, stream>>>(
+        g, st, params, rec_d, coef_d, dcoef, gl, pixel_area, partial);
+    const int n = n_inst * st.n_params;
+    grad_reduce_kernel<<<(n + 127) / 128, 128, 0, stream>>>(partial, chunks, st.n_params, n_inst,
+                                                           grad);
+    return 0;
+}
+
+}  // namespace lensgb

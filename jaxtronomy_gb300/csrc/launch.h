@@ -50,6 +50,20 @@ struct LoglikeArgs {
 int launch_loglike(const void* model, int n_inst, long long npix, const LoglikeArgs& a,
                    double* out, int precision, cudaStream_t stream);
 
+// Adjoint gradient of logL (grad.cu): FP64 models whose lens stack holds only
+// EPL / SHEAR and whose light profiles are Sersic.  `image` is the model image
+// of the same params (lensgb_image output), rec_d / coef_d its prepared
+// records.  Scratch: dcoef (n_inst x n_epl x EPL_NMAX), psf_flip (n_inst x K^2),
+// gm and glow (n_inst x npix), partial (n_inst x grad_chunks x n_params).
+bool grad_supported(const StackDesc& st);
+int grad_chunks(const GridDesc& g);
+int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
+                        const double* rec_d, const double* coef_d, double* dcoef,
+                        const double* image, const LoglikeArgs& la, const double* psf,
+                        long long psf_stride, int K, double* psf_flip, double* gm, double* glow,
+                        double* partial, double pixel_area, double* logl, double* grad,
+                        cudaStream_t stream);
+
 // Point-wise single-parameter-set evaluation (FP64).
 int launch_ray_shoot_points(const StackDesc& st, const double* rec_d, const double* coef_d,
                             const double* x, const double* y, double* bx, double* by,

@@ -362,6 +362,21 @@ class ImageModel:
             t["expo_t"] = float(em) if em is not None else 1.0
         return t
 
+    def _noise_desc(self, nt):
+        nd = _lib.NoiseDesc()
+        nd.data_dev = nt["data"].data_ptr()
+        nd.data_stride = nt["data_stride"]
+        nd.mask_dev = nt["mask"].data_ptr()
+        nd.noise_map_dev = 0 if nt["noise"] is None else nt["noise"].data_ptr()
+        nd.noise_stride = 0
+        nd.exposure_map_dev = 0 if nt["expo"] is None else nt["expo"].data_ptr()
+        nd.exposure_stride = 0
+        nd.exposure_time = nt["expo_t"]
+        nd.background_rms = float(self.Data.background_rms)
+        nd.error_map_dev = 0
+        nd.mask_stride = 0
+        return nd
+
     def likelihood_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                          data=None, psf_kernels=None, rows=None, image_out=None, stream=None):
         """Batched ``likelihood_data_given_model``: (B,) FP64 CUDA tensor of
@@ -374,17 +389,7 @@ class ImageModel:
         rows_dev = _device.to_device_f64(rows)
         B = rows_dev.shape[0]
         nt = self._noise_tensors(data)
-        nd = _lib.NoiseDesc()
-        nd.data_dev = nt["data"].data_ptr()
-        nd.data_stride = nt["data_stride"]
-        nd.mask_dev = nt["mask"].data_ptr()
-        nd.noise_map_dev = 0 if nt["noise"] is None else nt["noise"].data_ptr()
-        nd.noise_stride = 0
-        nd.exposure_map_dev = 0 if nt["expo"] is None else nt["expo"].data_ptr()
-        nd.exposure_stride = 0
-        nd.exposure_time = nt["expo_t"]
-        nd.background_rms = float(self.Data.background_rms)
-        nd.error_map_dev = 0
+        nd = self._noise_desc(nt)
         if image_out is None:
             image_out = torch.empty((B, self._nx, self._ny), dtype=self._dtype, device="cuda")
         logl = torch.empty((B,), dtype=torch.float64, device="cuda")
@@ -395,6 +400,56 @@ class ImageModel:
             _device.ptr(image_out), _device.ptr(logl), _device.stream_handle(stream)))
         del keep
         return logl
+
+    def likelihood_grad_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                              data=None, psf_kernels=None, rows=None, image_out=None,
+                              stream=None):
+        """logL and d logL / d params for B systems: ((B,) logL, (B, param_count)
+        gradient rows) as FP64 CUDA tensors, by the adjoint kernel
+        (``lensgb_loglike_grad``).  The gradient has the layout of
+        :meth:`pack_params`; :meth:`unpack_params` turns it into kwargs lists.
+        This is ``jax.grad`` of the reference's ``likelihood_data_given_model``
+        (``image_model.py:163-221``) for FP64 models of EPL / SHEAR lenses and
+        Sersic light."""
+        if self._precision != _lib.FP64:
+            raise ValueError("likelihood gradients need kwargs_numerics precision 'fp64'")
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        if rows is None:
+            rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
+        rows_dev = _device.to_device_f64(rows)
+        B = rows_dev.shape[0]
+        nt = self._noise_tensors(data)
+        nd = self._noise_desc(nt)
+        if image_out is None:
+            image_out = torch.empty((B, self._nx, self._ny), dtype=torch.float64, device="cuda")
+        logl = torch.empty((B,), dtype=torch.float64, device="cuda")
+        grad = torch.empty((B, model.param_count), dtype=torch.float64, device="cuda")
+        kt, kstride, keep = self._psf_arg(psf_kernels, B)
+        kptr = ctypes.c_void_p(0) if kt is None else _device.ptr(kt)
+        _lib.check(_lib.load().lensgb_loglike_grad(
+            model.handle, _device.ptr(rows_dev), B, kptr, kstride, ctypes.byref(nd),
+            _device.ptr(image_out), _device.ptr(logl), _device.ptr(grad),
+            _device.stream_handle(stream)))
+        del keep
+        return logl, grad
+
+    def unpack_params(self, rows):
+        """Inverse of :meth:`pack_params`: (kwargs_lens, kwargs_source,
+        kwargs_lens_light) with one array of length B per parameter."""
+        rows = rows.cpu().numpy() if isinstance(rows, torch.Tensor) else np.asarray(rows)
+        rows = rows.reshape(-1, rows.shape[-1])
+        out, c = [], 0
+        for names, table in ((self.LensModel.lens_model_list, profiles.LENS_PARAMS),
+                             (self.SourceModel.profile_type_list, profiles.LIGHT_PARAMS),
+                             (self.LensLightModel.profile_type_list, profiles.LIGHT_PARAMS)):
+            kws = []
+            for n in names:
+                kws.append({p: rows[:, c + j].copy() for j, p in enumerate(table[n])})
+                c += len(table[n])
+            out.append(kws)
+        return tuple(out)
 
     def likelihood_data_given_model(self, kwargs_lens=None, kwargs_source=None,
                                     kwargs_lens_light=None, kwargs_ps=None,

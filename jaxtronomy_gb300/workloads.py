@@ -237,3 +237,26 @@ def serving_model(key, delta_pix=0.05, precision="fp32", data=None, exposure_tim
     return ImageModel(d, psf, LensModel(stack.split("+")),
                       LightModel(["SERSIC_ELLIPSE"] * nsrc), LightModel(["SERSIC_ELLIPSE"]),
                       kwargs_numerics={"supersampling_factor": s, "precision": precision})
+
+
+def gradient_batch(seed=1003, batch=256, num_pix=120, delta_pix=0.05, supersampling=2,
+                   kernel_size=21):
+    """Gradient workload: EPL+SHEAR lens (as :func:`batch_epl`), SERSIC_ELLIPSE
+    source and lens light (as :func:`single_sie`), 120x120 at 0.05"/pix,
+    supersampling 2, one 21x21 Moffat PSF per system; 6 + 4 + 7 + 7 parameters
+    per system (22 free when SHEAR's ra_0, dec_0 are held).  Data come from
+    :func:`noisy_data` applied to the simulated images."""
+    model, lens, src, ll, kern = batch_epl(seed=seed, batch=batch, num_pix=num_pix,
+                                           delta_pix=delta_pix, supersampling=supersampling,
+                                           kernel_size=kernel_size)
+    return model, lens, src, ll, kern
+
+
+def noisy_data(images, seed=2003, background_rms=0.01, exposure_time=1000.0):
+    """image + N(0, background_rms^2) + Poisson(image t)/t - image, with the image
+    clipped at 0 for the Poisson draw."""
+    rng = np.random.default_rng(seed)
+    img = np.asarray(images, dtype=float)
+    counts = rng.poisson(np.clip(img, 0, None) * exposure_time)
+    return img + rng.normal(0, background_rms, img.shape) + counts / exposure_time - np.clip(
+        img, 0, None)

@@ -1,0 +1,146 @@
+"""Adjoint likelihood gradient (lensgb_loglike_grad through the C ABI) against
+central finite differences.
+
+Tolerance: |g - g_fd| <= 1e-4 * (|g_fd| + 1e-3 * max_k |g_fd_k|) per component,
+with FD step 1e-6 (central).  FD of the GPU FP64 likelihood covers the batch;
+FD of the FP64 oracle (the reference's likelihood restated) covers one small
+system, tying the adjoint to the reference's own likelihood.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import jaxtronomy_gb300 as J
+from jaxtronomy_gb300 import autograd, workloads as W
+from oracle import image as oimage
+
+pytestmark = pytest.mark.gpu
+
+STEP = 1e-6
+RTOL = 1e-4
+
+
+def _model(num_pix, s, kern, precision="fp64"):
+    g = W.grid_kwargs(num_pix, 0.05)
+    data = J.ImageData(np.zeros((num_pix, num_pix)), exposure_time=1000.0, background_rms=0.01,
+                       **g)
+    return J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=kern), J.LensModel(["EPL", "SHEAR"]),
+                        J.LightModel(["SERSIC_ELLIPSE"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                        kwargs_numerics={"supersampling_factor": s, "precision": precision})
+
+
+def _setup(batch=4, num_pix=32, s=2, K=11, seed=1003):
+    model, lens, src, ll, kern = W.gradient_batch(seed=seed, batch=batch, num_pix=num_pix,
+                                                  supersampling=s, kernel_size=K)
+    im = _model(num_pix, s, kern[0])
+    rows = im.pack_params(lens, src, ll)
+    # simulate at slightly shifted parameters so that the gradient is not ~0
+    truth = rows.copy()
+    truth[:, 0] *= 1.01
+    img = im.image_batch(rows=truth, psf_kernels=kern).cpu().numpy()
+    data = W.noisy_data(img)
+    return im, rows, kern, data
+
+
+def _fd(im, rows, kern, data):
+    B, P = rows.shape
+    pert = np.repeat(rows[:, None, :], 2 * P, axis=1)
+    for k in range(P):
+        pert[:, 2 * k, k] += STEP
+        pert[:, 2 * k + 1, k] -= STEP
+    pert = pert.reshape(B * 2 * P, P)
+    d = np.repeat(data, 2 * P, axis=0)
+    kk = np.repeat(kern, 2 * P, axis=0)
+    ll = im.likelihood_batch(rows=pert, data=d, psf_kernels=kk).cpu().numpy().reshape(B, P, 2)
+    return (ll[..., 0] - ll[..., 1]) / (2 * STEP)
+
+
+def _check(g, fd):
+    scale = np.abs(fd).max(axis=1, keepdims=True)
+    bound = RTOL * (np.abs(fd) + 1e-3 * scale)
+    bad = np.abs(g - fd) > bound
+    assert not bad.any(), (np.argwhere(bad), g[bad], fd[bad])
+
+
+def test_adjoint_matches_central_differences(cuda):
+    im, rows, kern, data = _setup()
+    logl, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kern)
+    ref = im.likelihood_batch(rows=rows, data=data, psf_kernels=kern)
+    np.testing.assert_array_equal(logl.cpu().numpy(), ref.cpu().numpy())
+    _check(grad.cpu().numpy(), _fd(im, rows, kern, data))
+
+
+def test_adjoint_without_psf_and_with_noise_map_and_mask(cuda):
+    model, lens, src, ll, kern = W.gradient_batch(batch=2, num_pix=24, supersampling=1,
+                                                  kernel_size=5)
+    g = W.grid_kwargs(24, 0.05)
+    rng = np.random.default_rng(4)
+    noise = 0.02 + 0.01 * rng.random((24, 24))
+    mask = (rng.random((24, 24)) > 0.2).astype(float)
+    data = J.ImageData(np.zeros((24, 24)), exposure_time=500.0, background_rms=0.02,
+                       noise_map=noise, **g)
+    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["EPL", "SHEAR"]),
+                      J.LightModel(["SERSIC_ELLIPSE"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics={"supersampling_factor": 1}, likelihood_mask=mask)
+    rows = im.pack_params(lens, src, ll)
+    d = W.noisy_data(im.image_batch(rows=rows).cpu().numpy() * 1.02)
+    logl, grad = im.likelihood_grad_batch(rows=rows, data=d)
+    B, P = rows.shape
+    fd = np.zeros((B, P))
+    for k in range(P):
+        rp, rm = rows.copy(), rows.copy()
+        rp[:, k] += STEP
+        rm[:, k] -= STEP
+        fd[:, k] = (im.likelihood_batch(rows=rp, data=d).cpu().numpy()
+                    - im.likelihood_batch(rows=rm, data=d).cpu().numpy()) / (2 * STEP)
+    _check(grad.cpu().numpy(), fd)
+
+
+def test_adjoint_matches_oracle_likelihood_differences(cuda):
+    """FD of the oracle's FP64 likelihood (the reference's algorithm) for one
+    small system equals the adjoint gradient."""
+    im, rows, kern, data = _setup(batch=1, num_pix=20, s=2, K=5)
+    _, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kern)
+    kl, ks, kll = im.unpack_params(rows)
+    scene = dict(nx=20, ny=20, supersampling_factor=2, psf_type="PIXEL", kernel=kern[0],
+                 convolution_type="grid", lens_model_list=["EPL", "SHEAR"],
+                 source_light_model_list=["SERSIC_ELLIPSE"],
+                 lens_light_model_list=["SERSIC_ELLIPSE"], **W.grid_kwargs(20, 0.05))
+
+    def logl(r):
+        a, b, c = im.unpack_params(r[None])
+        kw = lambda lst: [{k: float(v[0]) for k, v in d.items()} for d in lst]  # noqa: E731
+        model = oimage.image(scene, kw(a), kw(b), kw(c))
+        return oimage.log_likelihood(model, data[0], np.ones((20, 20)), 0.01,
+                                     exposure_time=1000.0)
+
+    P = rows.shape[1]
+    fd = np.zeros((1, P))
+    for k in range(P):
+        rp, rm = rows[0].copy(), rows[0].copy()
+        rp[k] += STEP
+        rm[k] -= STEP
+        fd[0, k] = (logl(rp) - logl(rm)) / (2 * STEP)
+    _check(grad.cpu().numpy(), fd)
+
+
+def test_autograd_function(cuda):
+    im, rows, kern, data = _setup(batch=3)
+    r = torch.as_tensor(rows).cuda().requires_grad_(True)
+    out = autograd.log_likelihood(r, im, data=data, psf_kernels=kern)
+    w = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64, device="cuda")
+    (out * w).sum().backward()
+    _, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kern)
+    np.testing.assert_array_equal(r.grad.cpu().numpy(), (w[:, None] * grad).cpu().numpy())
+
+
+def test_unsupported_models_raise(cuda):
+    g = W.grid_kwargs(16, 0.05)
+    data = J.ImageData(np.zeros((16, 16)), exposure_time=100.0, background_rms=0.01, **g)
+    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+                      J.LightModel([]))
+    kw = ([{"theta_E": 1.0, "e1": 0.0, "e2": 0.0, "center_x": 0, "center_y": 0}],
+          [{"amp": 1.0, "R_sersic": 0.3, "n_sersic": 2, "center_x": 0, "center_y": 0}], [])
+    with pytest.raises(Exception):
+        im.likelihood_grad_batch(*kw, data=np.zeros((16, 16)))

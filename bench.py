@@ -430,6 +430,77 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     }
 
 
+def gradient_section(steps, seed=1003):
+    """Adjoint gradient of logL for 256 systems (120^2, s=2, PSF 21, EPL+SHEAR,
+    Sersic source and lens light): time per batch, and the worst component
+    error against central finite differences (step 1e-6) on a sample."""
+    import numpy as np
+    import torch
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import workloads as W
+
+    B, N, S, K = 256, 120, 2, 21
+    model, lens, src, ll, kern = W.gradient_batch(seed=seed, batch=B, num_pix=N,
+                                                  supersampling=S, kernel_size=K)
+    g = W.grid_kwargs(N, 0.05)
+    data_cls = J.ImageData(np.zeros((N, N)), exposure_time=1000.0, background_rms=0.01, **g)
+    im = J.ImageModel(data_cls, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                      J.LensModel(["EPL", "SHEAR"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                      J.LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics={"supersampling_factor": S, "precision": "fp64"})
+    rows = im.pack_params(lens, src, ll)
+    truth = rows.copy()
+    truth[:, 0] *= 1.01
+    data = W.noisy_data(im.image_batch(rows=truth, psf_kernels=kern).cpu().numpy())
+    rows_d = torch.as_tensor(rows).cuda()
+    data_d = torch.as_tensor(data).cuda()
+    kern_d = torch.as_tensor(kern).cuda()
+    for _ in range(2):
+        im.likelihood_grad_batch(rows=rows_d, data=data_d, psf_kernels=kern_d)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = max(steps, 3)
+    e0.record(stream)
+    for _ in range(n):
+        logl, grad = im.likelihood_grad_batch(rows=rows_d, data=data_d, psf_kernels=kern_d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    e0.record(stream)
+    for _ in range(n):
+        im.likelihood_batch(rows=rows_d, data=data_d, psf_kernels=kern_d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_fwd = e0.elapsed_time(e1) / n
+    # central differences on a sample of systems, all perturbations in one batch
+    idx = np.array([0, 77, 191])
+    P = rows.shape[1]
+    pert = np.repeat(rows[idx][:, None, :], 2 * P, axis=1)
+    for k in range(P):
+        pert[:, 2 * k, k] += 1e-6
+        pert[:, 2 * k + 1, k] -= 1e-6
+    pert = pert.reshape(-1, P)
+    lp = im.likelihood_batch(rows=pert, data=np.repeat(data[idx], 2 * P, axis=0),
+                             psf_kernels=np.repeat(kern[idx], 2 * P, axis=0)).cpu().numpy()
+    lp = lp.reshape(len(idx), P, 2)
+    fd = (lp[..., 0] - lp[..., 1]) / 2e-6
+    gs = grad.cpu().numpy()[idx]
+    scale = np.abs(fd).max(axis=1, keepdims=True)
+    sig = np.abs(fd) > 1e-3 * scale
+    rel = np.abs(gs - fd)[sig] / np.abs(fd)[sig]
+    return {
+        "workload": "gradient_epl_256x120x120_s2_psf21",
+        "systems": B, "params_per_system": P,
+        "ms_per_batch": ms, "systems_per_s": B / (ms / 1e3),
+        "forward_loglike_ms_per_batch": ms_fwd, "grad_over_forward": ms / ms_fwd,
+        "fd_rel_err_max": float(rel.max()), "fd_rel_err_median": float(np.median(rel)),
+        "fd_components_checked": int(sig.sum()),
+        "precision": "FP64 (forward image, adjoint and reduction)",
+        "timing": "CUDA events, mean over %d batches after 2 warm-ups" % n,
+    }
+
+
 def percentile(v, q):
     v = sorted(v)
     k = (len(v) - 1) * q
@@ -675,6 +746,10 @@ def gpu_arm(args):
             extra["substructure"] = substructure_section(args.steps, args.warmup, fp32_peak,
                                                          flush)
 
+        # --- adjoint likelihood gradient
+        if not args.no_grad:
+            extra["gradient"] = gradient_section(args.steps)
+
         # --- serving stream (continuous batching)
         if args.serve_requests > 0:
             extra["serving"] = serving_section(args.serve_requests)
@@ -725,6 +800,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sub", action="store_true")
+    ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=50000)
     args = ap.parse_args()
     if args.impl == "reference":

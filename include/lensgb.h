@@ -97,6 +97,16 @@ typedef struct {
     int psf_type;          /* LENSGB_PSF_*                                       */
     int kernel_size;       /* odd side of the PSF kernel (0 for NONE)            */
     int precision;         /* LENSGB_FP64 or LENSGB_FP32_SPLIT                   */
+    int supersampling_convolution; /* 1: convolve on the supersampled grid with a
+                              kernel_size x kernel_size supersampled kernel, then
+                              re-bin (SubgridKernelConvolution without a low-res
+                              part / GaussianConvolution, convolution.py:100-166,
+                              215-250); ignored when supersampling == 1     */
+    int low_res_kernel_size; /* PIXEL with supersampling_convolution: side of the
+                              pixel-scale part of a split kernel (0: none).  The PSF
+                              of a system is then kernel_size^2 supersampled values
+                              followed by low_res_kernel_size^2 pixel-scale values
+                              (SubgridKernelConvolution, convolution.py:117-166) */
 } lensgb_model_desc;
 
 /* Build a model (the "compile" step of ImageModel.__init__,

@@ -71,6 +71,8 @@ class ModelDesc(ctypes.Structure):
         ("psf_type", ctypes.c_int),
         ("kernel_size", ctypes.c_int),
         ("precision", ctypes.c_int),
+        ("supersampling_convolution", ctypes.c_int),
+        ("low_res_kernel_size", ctypes.c_int),
     ]
 
 

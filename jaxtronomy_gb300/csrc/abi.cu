@@ -16,6 +16,10 @@ using namespace lensgb;
 struct lensgb_model {
     lensgb_model_desc desc;
     GridDesc grid;
+    GridDesc grid_hr;            // the supersampled grid as a grid of its own (s = 1)
+    bool hr_conv = false;        // convolution on the supersampled grid
+    void* hr_img = nullptr;      // supersampled image and its convolution (hr_conv models)
+    void* hr_out = nullptr;
     StackDesc st;
     double pixel_width;
     int cap_inst = 0;
@@ -93,6 +97,10 @@ static void free_scratch(lensgb_model* m) {
     cudaFree(m->lowres);
     cudaFree(m->refine_list);
     cudaFree(m->refine_count);
+    cudaFree(m->hr_img);
+    cudaFree(m->hr_out);
+    m->hr_img = nullptr;
+    m->hr_out = nullptr;
     m->refine_list = nullptr;
     m->refine_count = nullptr;
     m->rec_d = nullptr;
@@ -113,14 +121,19 @@ static int ensure_scratch(lensgb_model* m, int n_inst) {
     const size_t ncoef = (size_t)cap * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
     const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
     const size_t nimg = (size_t)cap * m->grid.nx * m->grid.ny;
+    const size_t s2 = (size_t)m->grid.s * m->grid.s;
+    // refine list: one entry per ray of the grid the FP32 kernel runs on
+    const size_t nlist = m->hr_conv ? nimg * s2 : nimg;
     if (cudaMalloc(&m->rec_d, nrec * REC_D * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&m->rec_f, nrec * REC_F * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&m->coef_d, ncoef * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&m->coef_f, ncoef * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&m->lowres, nimg * esz) != cudaSuccess ||
         (m->desc.precision == LENSGB_FP32_SPLIT &&
-         (cudaMalloc(&m->refine_list, nimg * sizeof(unsigned int)) != cudaSuccess ||
-          cudaMalloc(&m->refine_count, sizeof(unsigned int)) != cudaSuccess))) {
+         (cudaMalloc(&m->refine_list, nlist * sizeof(unsigned int)) != cudaSuccess ||
+          cudaMalloc(&m->refine_count, sizeof(unsigned int)) != cudaSuccess)) ||
+        (m->hr_conv && (cudaMalloc(&m->hr_img, nimg * s2 * esz) != cudaSuccess ||
+                        cudaMalloc(&m->hr_out, nimg * s2 * esz) != cudaSuccess))) {
         cudaGetLastError();
         free_scratch(m);
         return fail(LENSGB_ERR_OOM, "device allocation of model scratch failed");
@@ -154,8 +167,9 @@ static RefineArgs refine_args(const lensgb_model* m, int n_inst, unsigned int* l
 
 // The refine list stores 32-bit batch-global pixel indices.
 static int check_refine_size(const lensgb_model* m, int n_inst) {
+    const long long s2 = m->hr_conv ? (long long)m->grid.s * m->grid.s : 1;
     if (m->desc.precision == LENSGB_FP32_SPLIT && m->refine_tau > 0.f &&
-        (long long)n_inst * m->grid.nx * m->grid.ny >= (1LL << 32))
+        (long long)n_inst * m->grid.nx * m->grid.ny * s2 >= (1LL << 32))
         return fail(LENSGB_ERR_INVALID,
                     "n_inst * nx * ny must stay below 2^32 for FP32 models; split the batch");
     return LENSGB_OK;
@@ -163,7 +177,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 103; }
+int lensgb_version(void) { return 105; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -212,6 +226,13 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     if (d->psf_type != LENSGB_PSF_NONE && (d->kernel_size < 1 || d->kernel_size % 2 == 0 ||
                                            d->kernel_size > 255))
         return fail(LENSGB_ERR_INVALID, "kernel_size must be odd and in 1..255");
+    if (d->low_res_kernel_size != 0 &&
+        (d->psf_type != LENSGB_PSF_PIXEL || !d->supersampling_convolution ||
+         d->low_res_kernel_size < 1 || d->low_res_kernel_size % 2 == 0 ||
+         d->low_res_kernel_size > 255))
+        return fail(LENSGB_ERR_INVALID,
+                    "low_res_kernel_size must be 0, or odd in 1..255 for PIXEL models with "
+                    "supersampling_convolution");
     lensgb_model* m = new lensgb_model();
     m->desc = *d;
     StackDesc& st = m->st;
@@ -287,6 +308,11 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     split_bits(g.ay, bits, g.ay_hi, g.ay_lo);
     split_bits(g.by, bits, g.by_hi, g.by_lo);
     m->pixel_width = sqrt(fabs(M[0] * M[3] - M[1] * M[2]));
+    m->hr_conv = d->supersampling_convolution != 0 && s > 1 && d->psf_type != LENSGB_PSF_NONE;
+    m->grid_hr = g;
+    m->grid_hr.nx = g.nx * s;
+    m->grid_hr.ny = g.ny * s;
+    m->grid_hr.s = 1;
     *out = m;
     return LENSGB_OK;
 }
@@ -327,6 +353,45 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     cudaStream_t s = (cudaStream_t)stream;
     launch_prepare(m->grid, m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
     if ((rc = check_cuda("prepare launch"))) return rc;
+    if (conv && m->hr_conv) {
+        // supersampled image (one ray per element), convolution on the
+        // supersampled grid, then the s x s block mean times the pixel area
+        // (SubgridKernelConvolution.re_size_convolve, convolution.py:154-166;
+        // GaussianConvolution.re_size_convolve, :237-250)
+        RefineArgs rf = refine_args(m, n_inst, m->refine_list, m->refine_count);
+        if (rf.tau > 0.f &&
+            cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), s) != cudaSuccess)
+            return check_cuda("refine counter reset");
+        launch_raytrace(m->grid_hr, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f,
+                        m->hr_img, flags, 1.0, m->desc.precision, rf, s);
+        if ((rc = check_cuda("raytrace launch"))) return rc;
+        if (launch_conv(m->hr_img, m->hr_out, psf, psf_stride, n_inst, m->grid_hr.ny,
+                        m->grid_hr.nx, m->desc.kernel_size,
+                        m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0, m->desc.precision, s))
+            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = check_cuda("convolution launch"))) return rc;
+        const double area = m->pixel_width * m->pixel_width;
+        const int KL = m->desc.low_res_kernel_size;
+        if (KL == 0) {
+            launch_resize(m->hr_out, out, n_inst, m->grid.ny, m->grid.nx, m->grid.s, area,
+                          m->desc.precision, s);
+            return check_cuda("re-binning launch");
+        }
+        // split kernel: re_size(conv_high(hr)) + conv_low(re_size(hr)), then x area
+        const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
+        const void* klow = (const unsigned char*)psf +
+                           (size_t)m->desc.kernel_size * m->desc.kernel_size * esz;
+        launch_resize(m->hr_out, out, n_inst, m->grid.ny, m->grid.nx, m->grid.s, 1.0,
+                      m->desc.precision, s);
+        launch_resize(m->hr_img, m->lowres, n_inst, m->grid.ny, m->grid.nx, m->grid.s, 1.0,
+                      m->desc.precision, s);
+        if (launch_conv(m->lowres, m->hr_out, klow, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                        KL, 0, m->desc.precision, s))
+            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        launch_add_scaled(out, m->hr_out, (long long)n_inst * m->grid.nx * m->grid.ny, area,
+                          m->desc.precision, s);
+        return check_cuda("re-binning launch");
+    }
     const double scale = m->pixel_width * m->pixel_width;
     void* target = conv ? m->lowres : out;
     RefineArgs rf = refine_args(m, n_inst, m->refine_list, m->refine_count);
@@ -426,6 +491,9 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
         return fail(LENSGB_ERR_UNSUPPORTED,
                     "the likelihood gradient supports PSF types NONE and PIXEL (the transposed "
                     "edge-padded convolution is not provided)");
+    if (m->hr_conv)
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "the likelihood gradient does not support supersampled convolution");
     if (!grad_supported(m->st))
         return fail(LENSGB_ERR_UNSUPPORTED,
                     "the likelihood gradient supports lens stacks of EPL and SHEAR and Sersic "
@@ -705,6 +773,9 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
     if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    if (conv && m->hr_conv)
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "lensgb_image_noalloc does not provide supersampled convolution");
     const int n_prof = m->st.n_lens + m->st.n_src + m->st.n_ll;
     const size_t nrec = (size_t)n_inst * (n_prof > 0 ? n_prof : 1);
     const size_t ncoef = (size_t)n_inst * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;

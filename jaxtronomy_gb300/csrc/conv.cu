@@ -248,6 +248,60 @@ static int run_conv(const void* in, void* out, const void* kernel, long long kst
     return 0;
 }
 
+template <typename R>
+__global__ void resize_kernel(const R* __restrict__ hr, R* __restrict__ out, int ny, int nx,
+                              int s, double scale, int n_inst) {
+    const long long npix = (long long)nx * ny;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= npix * n_inst) return;
+    const long long inst = gid / npix, p = gid % npix;
+    const int row = (int)(p / nx), col = (int)(p % nx);
+    const long long W = (long long)nx * s;
+    const R* src = hr + inst * npix * s * s;
+    double acc = 0.0;
+    for (int si = 0; si < s; ++si) {
+        double rs = 0.0;
+        const R* r = src + ((long long)row * s + si) * W + (long long)col * s;
+        for (int sj = 0; sj < s; ++sj) rs += (double)r[sj];
+        acc += rs / (double)s;
+    }
+    out[gid] = (R)(acc / (double)s * scale);
+}
+
+int launch_resize(const void* hr, void* out, int n_inst, int ny, int nx, int s, double scale,
+                  int precision, cudaStream_t stream) {
+    const long long n = (long long)nx * ny * n_inst;
+    if (n <= 0) return 0;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (precision == LENSGB_FP64)
+        resize_kernel<double><<<blocks, 256, 0, stream>>>((const double*)hr, (double*)out, ny, nx,
+                                                          s, scale, n_inst);
+    else
+        resize_kernel<float><<<blocks, 256, 0, stream>>>((const float*)hr, (float*)out, ny, nx, s,
+                                                         scale, n_inst);
+    return 0;
+}
+
+template <typename R>
+__global__ void add_scaled_kernel(R* __restrict__ out, const R* __restrict__ add, long long n,
+                                  double scale) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (R)(((double)out[i] + (double)add[i]) * scale);
+}
+
+int launch_add_scaled(void* out, const void* add, long long n, double scale, int precision,
+                      cudaStream_t stream) {
+    if (n <= 0) return 0;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (precision == LENSGB_FP64)
+        add_scaled_kernel<double><<<blocks, 256, 0, stream>>>((double*)out, (const double*)add, n,
+                                                              scale);
+    else
+        add_scaled_kernel<float><<<blocks, 256, 0, stream>>>((float*)out, (const float*)add, n,
+                                                             scale);
+    return 0;
+}
+
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream) {
     if (precision == LENSGB_FP64)

@@ -31,6 +31,15 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream);
 
+// s x s block mean (image_util.re_size, image_util.py:79-98: mean over
+// sub-columns, then sub-rows) of n_inst (ny*s, nx*s) images, times scale.
+int launch_resize(const void* hr, void* out, int n_inst, int ny, int nx, int s, double scale,
+                  int precision, cudaStream_t stream);
+
+// out[i] = (out[i] + add[i]) * scale over n elements.
+int launch_add_scaled(void* out, const void* add, long long n, double scale, int precision,
+                      cudaStream_t stream);
+
 // Noise description of the likelihood reduction (device pointers; strides in
 // elements between systems, 0 = shared by all systems).
 struct LoglikeArgs {

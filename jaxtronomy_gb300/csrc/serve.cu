@@ -630,7 +630,10 @@ int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
     b->n_params = lensgb_model_param_count(m);
     lensgb_model_destroy(m);
     b->npix = (long long)r.desc.nx * r.desc.ny;
-    b->k2 = r.desc.psf_type == LENSGB_PSF_NONE ? 0 : r.desc.kernel_size * r.desc.kernel_size;
+    b->k2 = r.desc.psf_type == LENSGB_PSF_NONE
+                ? 0
+                : r.desc.kernel_size * r.desc.kernel_size +
+                      r.desc.low_res_kernel_size * r.desc.low_res_kernel_size;
     b->esz = r.desc.precision == LENSGB_FP64 ? 8 : 4;
     s->buckets.push_back(b);
     *out = (int)s->buckets.size() - 1;

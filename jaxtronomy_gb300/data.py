@@ -178,7 +178,24 @@ class PSF:
 
     @property
     def kernel_point_source(self):
+        if self.psf_type == "PIXEL" and self.point_source_supersampling_factor > 1:
+            raise NotImplementedError(
+                "the pixel-scale kernel of a supersampled PSF (lenstronomy "
+                "kernel_util.degrade_kernel) is not provided; use it with "
+                "supersampling_convolution=True")
         return self._kernel
+
+    def kernel_point_source_supersampled(self, supersampling_factor, updata_cache=False):
+        """The supersampled PIXEL kernel: the kernel given at construction when
+        ``point_source_supersampling_factor`` equals ``supersampling_factor``."""
+        if self.psf_type != "PIXEL":
+            raise ValueError("kernel_point_source_supersampled needs a PIXEL PSF")
+        if supersampling_factor == self.point_source_supersampling_factor and supersampling_factor > 1:
+            return self._kernel
+        raise NotImplementedError(
+            "building a supersampled kernel from a pixel-scale one (lenstronomy "
+            "kernel_util.subgrid_kernel) is not provided; pass the supersampled kernel with "
+            "point_source_supersampling_factor = supersampling_factor")
 
     @property
     def fwhm(self):

@@ -62,6 +62,37 @@ def cut_psf(kernel, size):
     return kernel[c - h:c + h + 1, c - h:c + h + 1]
 
 
+def split_kernel(kernel_super, supersampling_kernel_size, supersampling_factor):
+    """(pixel-scale part, supersampled part) of a supersampled kernel for
+    ``SubgridKernelConvolution`` (the role of lenstronomy
+    ``kernel_util.split_kernel`` at convolution.py:123-127, defined here from
+    that role): the supersampled part is the central n x n block,
+    n = supersampling_kernel_size * s made odd (at most the kernel side); the
+    pixel-scale part is the rest of the kernel summed over s x s blocks aligned
+    on its centre.  Odd s only."""
+    s = int(supersampling_factor)
+    if s <= 1 or s % 2 == 0:
+        raise ValueError("a kernel split (supersampling_kernel_size) needs an odd "
+                         "supersampling factor > 1; pass supersampling_kernel_size=None")
+    k = np.asarray(kernel_super, dtype=float)
+    n_super = k.shape[0]
+    n_sub = supersampling_kernel_size * s
+    if n_sub % 2 == 0:
+        n_sub += 1
+    n_sub = min(n_sub, n_super)
+    i0 = (n_super - n_sub) // 2
+    high = k[i0:i0 + n_sub, i0:i0 + n_sub].copy()
+    hole = k.copy()
+    hole[i0:i0 + n_sub, i0:i0 + n_sub] = 0.0
+    n_low = -(-n_super // s)
+    if n_low % 2 == 0:
+        n_low += 1
+    pad = (n_low * s - n_super) // 2
+    big = np.zeros((n_low * s, n_low * s))
+    big[pad:pad + n_super, pad:pad + n_super] = hole
+    return big.reshape(n_low, s, n_low, s).sum(axis=(1, 3)), high
+
+
 class ImageModel:
     """Lens image simulation (``image_model.py:27-150``)."""
 
@@ -99,11 +130,12 @@ class ImageModel:
         s = int(s)
         if s < 1:
             raise ValueError("supersampling_factor must be >= 1")
-        ssc = kn.get("supersampling_convolution", False)
+        ssc = bool(kn.get("supersampling_convolution", False))
         if s == 1:
-            ssc = False
-        if ssc:
-            raise ValueError("supersampling_convolution=True is not supported by this build")
+            ssc = False  # numerics.py:84-85
+        self._ssc = ssc
+        # numerics.py:31: the supersampled kernel is split unless this is None
+        self._ssk = kn.get("supersampling_kernel_size", 5) if ssc else None
         if kn.get("flux_evaluate_indexes") is not None:
             raise ValueError("flux_evaluate_indexes is not supported by this build")
         conv_type = kn.get("convolution_type", "fft")
@@ -137,17 +169,27 @@ class ImageModel:
         # PSF kernel for the convolution step (numerics.py:102-139)
         pt = psf_class.psf_type
         if pt == "PIXEL":
-            kernel = np.asarray(psf_class.kernel_point_source, dtype=float)
             cks = kn.get("convolution_kernel_size")
-            if cks is not None:
-                size = cks if cks % 2 == 1 else cks + 1
-                kernel = cut_psf(kernel, size)
+            if ssc:
+                # numerics.py:104-115,196-213: supersampled kernel, cut to
+                # convolution_kernel_size * s (made odd)
+                kernel = np.asarray(psf_class.kernel_point_source_supersampled(s), dtype=float)
+                if cks is not None:
+                    size = cks * s
+                    kernel = cut_psf(kernel, size if size % 2 == 1 else size + 1)
+            else:
+                kernel = np.asarray(psf_class.kernel_point_source, dtype=float)
+                if cks is not None:
+                    size = cks if cks % 2 == 1 else cks + 1
+                    kernel = cut_psf(kernel, size)
             self._psf_type = _lib.PSF_PIXEL
         elif pt == "GAUSSIAN":
             trunc = kn.get("truncation_conv")
             if trunc is None:
                 trunc = psf_class.truncation
             sigma = fwhm2sigma(psf_class.fwhm) / data_class.pixel_width
+            if ssc:
+                sigma *= s  # convolution.py:194-195
             kernel = gaussian_kernel(sigma, trunc)
             self._psf_type = _lib.PSF_GAUSSIAN
         elif pt == "NONE":
@@ -157,6 +199,11 @@ class ImageModel:
             raise ValueError("psf_type %s not valid! Chose either NONE, GAUSSIAN or PIXEL." % pt)
         self._kernel = kernel
         self._kernel_size = 0 if kernel is None else int(kernel.shape[0])
+        self._low_kernel_size = 0
+        if ssc and pt == "PIXEL" and self._ssk is not None:
+            lo, hi = split_kernel(kernel, self._ssk, s)
+            self._kernel_size = int(hi.shape[0])
+            self._low_kernel_size = int(lo.shape[0])
         self._kernel_dev = None
         self._models = {}
 
@@ -187,6 +234,8 @@ class ImageModel:
         d.psf_type = self._psf_type
         d.kernel_size = self._kernel_size
         d.precision = self._precision
+        d.supersampling_convolution = 1 if self._ssc else 0
+        d.low_res_kernel_size = self._low_kernel_size
         return d
 
     def _model(self, lens_idx, src_idx, ll_idx, lensed=True):
@@ -203,9 +252,27 @@ class ImageModel:
                             range(len(self.LensLightModel.profile_type_list)))
         return model.refined_pixels(_device.stream_handle(stream))
 
+    def psf_elements(self):
+        """PSF values per system in the C-ABI layout (0 for psf_type NONE)."""
+        if self._kernel is None:
+            return 0
+        return self._kernel_size ** 2 + self._low_kernel_size ** 2
+
+    def pack_psf(self, kernel):
+        """One PSF kernel (the model's convolution-kernel shape: the supersampled
+        kernel when convolving on the supersampled grid) as the flat array the
+        C ABI takes: the kernel itself, or a split kernel's supersampled part
+        followed by its pixel-scale part."""
+        k = np.asarray(kernel, dtype=float)
+        if self._low_kernel_size:
+            lo, hi = split_kernel(k, self._ssk, self._s)
+            return np.concatenate([hi.ravel(), lo.ravel()])
+        return k.ravel()
+
     def _kernel_tensor(self):
         if self._kernel_dev is None and self._kernel is not None:
-            self._kernel_dev = torch.as_tensor(self._kernel, dtype=self._dtype).cuda().contiguous()
+            self._kernel_dev = torch.as_tensor(self.pack_psf(self._kernel),
+                                               dtype=self._dtype).cuda().contiguous()
         return self._kernel_dev
 
     # ------------------------------------------------------------------ packing
@@ -241,10 +308,19 @@ class ImageModel:
             k = self._kernel_tensor()
             return k, 0, k
         k = psf_kernels
+        K = int(self._kernel.shape[0])
+        if self._low_kernel_size:
+            # split each supersampled kernel on the host into the ABI layout
+            arr = k.cpu().numpy() if isinstance(k, torch.Tensor) else np.asarray(k, float)
+            if arr.shape[-2:] != (K, K) or arr.ndim not in (2, 3):
+                raise ValueError("psf kernels must be %dx%d (supersampled)" % (K, K))
+            arr = arr[None] if arr.ndim == 2 else arr
+            packed = np.stack([self.pack_psf(a) for a in arr])
+            t = torch.as_tensor(packed).to(device="cuda", dtype=self._dtype).contiguous()
+            return t, (0 if packed.shape[0] == 1 else self.psf_elements()), t
         if not isinstance(k, torch.Tensor):
             k = torch.as_tensor(np.ascontiguousarray(k))
         k = k.to(device="cuda", dtype=self._dtype).contiguous()
-        K = self._kernel_size
         if k.dim() == 2:
             if tuple(k.shape) != (K, K):
                 raise ValueError("psf kernel must be %dx%d" % (K, K))

@@ -101,10 +101,9 @@ class Server:
         req.params = keep[0].ctypes.data
         if image_model._psf_type != _lib.PSF_NONE:
             k = image_model._kernel if psf_kernel is None else psf_kernel
-            k = np.ascontiguousarray(k, dtype=np_dtype)
-            K = image_model._kernel_size
-            if k.shape != (K, K):
-                raise ValueError("psf kernel must be %dx%d" % (K, K))
+            if np.shape(k) != image_model._kernel.shape:
+                raise ValueError("psf kernel must have shape %s" % (image_model._kernel.shape,))
+            k = np.ascontiguousarray(image_model.pack_psf(k), dtype=np_dtype)
             keep.append(k)
             req.psf = k.ctypes.data
         shape = (image_model._nx, image_model._ny)

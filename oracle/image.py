@@ -59,8 +59,27 @@ def re_size_convolve(scene, flux, unconvolved=False):
     img = grid.array2image(flux, nx * s, ny * s)
     low = grid.re_size(img, s)
     psf_type = scene.get("psf_type", "NONE")
-    if scene.get("supersampling_convolution", False) and s > 1:
-        raise NotImplementedError("supersampling_convolution=True is not restated")
+    ctype = scene.get("convolution_type", "fft")
+    pw = grid.pixel_width(scene["transform_pix2angle"])
+    if (scene.get("supersampling_convolution", False) and s > 1 and not unconvolved
+            and psf_type != "NONE"):
+        if psf_type == "PIXEL":
+            # SubgridKernelConvolution.re_size_convolve (convolution.py:154-166);
+            # `kernel` is the supersampled kernel (cut, numerics.py:196-213)
+            ssk = scene.get("supersampling_kernel_size", 5)
+            if ssk is None:
+                high, lowk = scene["kernel"], None
+            else:
+                lowk, high = numerics.split_kernel(scene["kernel"], ssk, s)
+            conv = grid.re_size(numerics.pixel_convolve(img, high, ctype), s)
+            if lowk is not None:
+                conv = conv + numerics.pixel_convolve(low, lowk, ctype)
+        else:
+            # GaussianConvolution with supersampling_convolution (convolution.py:194-250)
+            sigma = numerics.fwhm2sigma(scene["fwhm"]) / pw * s
+            kernel, radius = numerics.gaussian_kernel(sigma, scene.get("truncation", 5.0))
+            conv = grid.re_size(numerics.gaussian_convolve(img, kernel, radius), s)
+        return conv * pw ** 2
     if unconvolved or psf_type == "NONE":
         conv = low
     elif psf_type == "PIXEL":

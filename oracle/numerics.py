@@ -53,3 +53,55 @@ def normalize_pixel_kernel(kernel):
     if kernel.shape[0] % 2 == 0 or kernel.shape[1] % 2 == 0:
         raise ValueError("kernel needs to have odd axis number")
     return kernel / np.sum(kernel)
+
+
+def cut_psf(kernel, size):
+    """Centred odd-size cut without renormalisation (lenstronomy
+    ``kernel_util.cut_psf(..., normalisation=False)``, called at numerics.py:210)."""
+    n = kernel.shape[0]
+    if size >= n:
+        return np.array(kernel, dtype=float)
+    c = n // 2
+    h = size // 2
+    return np.array(kernel[c - h:c + h + 1, c - h:c + h + 1], dtype=float)
+
+
+def split_kernel(kernel_super, supersampling_kernel_size, supersampling_factor):
+    """Split of a supersampled kernel into the part convolved on the supersampled
+    grid and the part convolved on the pixel grid (the role of lenstronomy's
+    ``kernel_util.split_kernel``, called at convolution.py:123-127; restated
+    here from that role, not from lenstronomy's code, so parity with lenstronomy
+    itself is unpinned):
+
+    * high-resolution part: the central n x n block of the supersampled kernel,
+      n = supersampling_kernel_size * s (made odd, at most the kernel side);
+    * pixel-scale part: the supersampled kernel with that block set to zero,
+      summed over s x s blocks aligned on the kernel centre (the kernel is
+      zero-padded symmetrically to a whole number of blocks).
+
+    Both parts keep the supersampled kernel's normalisation, so together they
+    carry its total weight.  Odd supersampling factors only (an even factor
+    puts the kernel centre on a block boundary)."""
+    s = int(supersampling_factor)
+    if s <= 1:
+        raise ValueError("a kernel split needs supersampling_factor > 1")
+    if s % 2 == 0:
+        raise ValueError("a kernel split needs an odd supersampling factor")
+    k = np.asarray(kernel_super, dtype=float)
+    n_super = k.shape[0]
+    n_sub = supersampling_kernel_size * s
+    if n_sub % 2 == 0:
+        n_sub += 1
+    n_sub = min(n_sub, n_super)
+    i0 = (n_super - n_sub) // 2
+    high = k[i0:i0 + n_sub, i0:i0 + n_sub].copy()
+    hole = k.copy()
+    hole[i0:i0 + n_sub, i0:i0 + n_sub] = 0.0
+    n_low = -(-n_super // s)
+    if n_low % 2 == 0:
+        n_low += 1
+    pad = (n_low * s - n_super) // 2
+    big = np.zeros((n_low * s, n_low * s))
+    big[pad:pad + n_super, pad:pad + n_super] = hole
+    low = big.reshape(n_low, s, n_low, s).sum(axis=(1, 3))
+    return low, high

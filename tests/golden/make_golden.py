@@ -120,7 +120,7 @@ def gen_hyp2f1():
 
 def _image_model(num_pix, delta_pix, s, psf_kwargs, lens_list, src_list, ll_list,
                  data=None, bkg=0.01, exp_time=1000.0, flux_scaling=1, deflection_scaling=None,
-                 convolution_type="fft"):
+                 convolution_type="fft", numerics=None):
     from jaxtronomy.Data.imaging_data import ImageData
     from jaxtronomy.ImSim.image_model import ImageModel
     from jaxtronomy.LensModel.lens_model import LensModel
@@ -138,8 +138,9 @@ def _image_model(num_pix, delta_pix, s, psf_kwargs, lens_list, src_list, ll_list
     return ImageModel(data_class, psf, LensModel(lens_list),
                       LightModel(src_list, deflection_scaling_list=deflection_scaling),
                       LightModel(ll_list),
-                      kwargs_numerics={"supersampling_factor": s,
-                                       "convolution_type": convolution_type})
+                      kwargs_numerics=dict({"supersampling_factor": s,
+                                            "convolution_type": convolution_type},
+                                           **(numerics or {})))
 
 
 def gen_images():
@@ -231,6 +232,37 @@ def gen_images():
                        "src": ["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], "ll": ["SERSIC_ELLIPSE"],
                        "kwargs_lens": kl, "kwargs_source": ks2, "kwargs_lens_light": kll2,
                        "image": np.asarray(im.image(kl, ks2, kll2))})
+    # 7) convolution on the supersampled grid (SubgridKernelConvolution with the
+    #    supersampled kernel given to the PSF; GaussianConvolution with
+    #    supersampling_convolution), EPL+SHEAR, s = 3 and 2
+    model, lens, src, ll, _ = W.batch_epl(seed=1005, batch=1, num_pix=30, kernel_size=11)
+    kl, ks, kll = W.instance(lens, 0), W.instance(src, 0), W.instance(ll, 0)
+    for tag, side, cks, ssk in [("ssc_pixel_split", 27, None, 3),
+                                ("ssc_pixel", 15, None, None),
+                                ("ssc_pixel_cut", 27, 5, 1)]:
+        k_super = W.moffat_pixel_kernel(0.12, 3.0, 0.05 / 3, side)
+        num = {"supersampling_convolution": True, "supersampling_kernel_size": ssk}
+        if cks is not None:
+            num["convolution_kernel_size"] = cks
+        im = _image_model(30, 0.05, 3, {"psf_type": "PIXEL", "kernel_point_source": k_super,
+                                        "point_source_supersampling_factor": 3},
+                          model["lens_model_list"], model["source_light_model_list"],
+                          model["lens_light_model_list"], numerics=num)
+        scenes.append({"tag": tag, "num_pix": 30, "delta_pix": 0.05, "s": 3,
+                       "psf_type": "PIXEL", "kernel": k_super, "ssc": True, "cks": cks,
+                       "ssk": ssk, "lens": model["lens_model_list"],
+                       "src": model["source_light_model_list"],
+                       "ll": model["lens_light_model_list"], "kwargs_lens": kl,
+                       "kwargs_source": ks, "kwargs_lens_light": kll,
+                       "image": np.asarray(im.image(kl, ks, kll))})
+    im = _image_model(32, 0.08, 2, {"psf_type": "GAUSSIAN", "fwhm": 0.2, "truncation": 4},
+                      model["lens_model_list"], model["source_light_model_list"],
+                      model["lens_light_model_list"], numerics={"supersampling_convolution": True})
+    scenes.append({"tag": "ssc_gaussian", "num_pix": 32, "delta_pix": 0.08, "s": 2,
+                   "psf_type": "GAUSSIAN", "fwhm": 0.2, "truncation": 4.0, "ssc": True,
+                   "lens": model["lens_model_list"], "src": model["source_light_model_list"],
+                   "ll": model["lens_light_model_list"], "kwargs_lens": kl, "kwargs_source": ks,
+                   "kwargs_lens_light": kll, "image": np.asarray(im.image(kl, ks, kll))})
     # 6) likelihood on the first single-image scene with noisy data
     rng = np.random.default_rng(77)
     base = scenes[0]

@@ -365,6 +365,7 @@ class PSF:
             self._kernel = k / np.sum(k)
         self.psf_variance_map_bool = psf_variance_map is not None
         self._pixel_size = None
+        self.point_source_supersampling_factor = point_source_supersampling_factor
 
     @property
     def kernel_point_source(self):
@@ -381,12 +382,14 @@ class PSF:
     def set_pixel_size(self, deltaPix):
         self._pixel_size = deltaPix
 
-    point_source_supersampling_factor = 1
-
     def kernel_point_source_supersampled(self, supersampling_factor, updata_cache=False):
-        if supersampling_factor != 1:
-            raise NotImplementedError("supersampled PSF kernels are not restated")
-        return self._kernel
+        # the kernel given at construction is the supersampled one when the
+        # factors match; building one from a pixel-scale kernel is not restated.
+        # Factor 1 is only requested by the point-source renderer, which these
+        # scenes never use.
+        if supersampling_factor in (self.point_source_supersampling_factor, 1):
+            return self._kernel
+        raise NotImplementedError("supersampled PSF kernels are not restated")
 
 
 class Image2SourceMapping:
@@ -444,7 +447,19 @@ def install_lenstronomy():
                selectBest=_Dummy(), fwhm2sigma=lambda f: f / (2 * np.sqrt(2 * np.log(2))),
                grid_from_coordinate_transform=_grid_from_transform)
     package_util = mod("lenstronomy.Util.package_util", exporter=_exporter)
-    kernel_util = mod("lenstronomy.Util.kernel_util", cut_psf=_Dummy(), split_kernel=_Dummy())
+    from oracle import numerics as _onum
+
+    def _cut_psf(psf_data, psf_size, normalisation=True):
+        k = _onum.cut_psf(np.asarray(psf_data, float), psf_size)
+        return k / np.sum(k) if normalisation else k
+
+    def _split_kernel(kernel_super, supersampling_kernel_size, supersampling_factor,
+                      normalized=True):
+        return _onum.split_kernel(np.asarray(kernel_super, float), supersampling_kernel_size,
+                                  supersampling_factor)
+
+    kernel_util = mod("lenstronomy.Util.kernel_util", cut_psf=_cut_psf,
+                      split_kernel=_split_kernel)
     constants = mod("lenstronomy.Util.constants")
     cosmo_util = mod("lenstronomy.Util.cosmo_util", get_astropy_cosmology=_Dummy())
     mod("lenstronomy.Util", util=util, package_util=package_util, kernel_util=kernel_util,

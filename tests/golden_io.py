@@ -7,6 +7,7 @@ import os
 import numpy as np
 
 from jaxtronomy_gb300.workloads import grid_kwargs
+from oracle import numerics as onum
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -43,7 +44,14 @@ def oracle_scene(sc):
     kernel = sc.get("kernel")
     if kernel is not None:
         kernel = kernel / kernel.sum()
-    return dict(nx=sc["num_pix"], ny=sc["num_pix"], supersampling_factor=sc["s"],
+        if sc.get("ssc") and sc.get("cks") is not None:
+            size = sc["cks"] * sc["s"]
+            kernel = onum.cut_psf(kernel, size if size % 2 else size + 1)
+    extra = {}
+    if sc.get("ssc"):
+        extra = {"supersampling_convolution": True,
+                 "supersampling_kernel_size": sc.get("ssk")}
+    return dict(nx=sc["num_pix"], ny=sc["num_pix"], supersampling_factor=sc["s"], **extra,
                 psf_type=sc["psf_type"], kernel=kernel, fwhm=sc.get("fwhm"),
                 truncation=sc.get("truncation", 5.0), lens_model_list=sc["lens"],
                 source_light_model_list=sc["src"], lens_light_model_list=sc["ll"],

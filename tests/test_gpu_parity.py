@@ -39,16 +39,24 @@ def build_model(sc, precision="fp64", kernel=None):
     g = W.grid_kwargs(sc["num_pix"], sc["delta_pix"])
     data = J.ImageData(np.zeros((sc["num_pix"], sc["num_pix"])), exposure_time=1000.0,
                        background_rms=0.01, flux_scaling=sc.get("flux_scaling", 1), **g)
+    numerics = {"supersampling_factor": sc["s"], "precision": precision}
+    ssf = 1
+    if sc.get("ssc"):
+        numerics["supersampling_convolution"] = True
+        numerics["supersampling_kernel_size"] = sc.get("ssk")
+        if sc.get("cks") is not None:
+            numerics["convolution_kernel_size"] = sc["cks"]
+        ssf = sc["s"]
     if sc["psf_type"] == "PIXEL":
-        psf = J.PSF("PIXEL", kernel_point_source=sc["kernel"] if kernel is None else kernel)
+        psf = J.PSF("PIXEL", kernel_point_source=sc["kernel"] if kernel is None else kernel,
+                    point_source_supersampling_factor=ssf)
     elif sc["psf_type"] == "GAUSSIAN":
         psf = J.PSF("GAUSSIAN", fwhm=sc["fwhm"], truncation=sc["truncation"])
     else:
         psf = J.PSF("NONE")
     return J.ImageModel(data, psf, J.LensModel(sc["lens"]),
                         J.LightModel(sc["src"], deflection_scaling_list=sc.get("deflection_scaling")),
-                        J.LightModel(sc["ll"]),
-                        kwargs_numerics={"supersampling_factor": sc["s"], "precision": precision})
+                        J.LightModel(sc["ll"]), kwargs_numerics=numerics)
 
 
 SCENES, LIKE = golden_io.image_scenes()

@@ -197,3 +197,47 @@ def test_serving_stream_is_seeded_and_covers_the_grid():
     im = W.serving_model(r["key"])
     rows = im.pack_params(r["kwargs_lens"], r["kwargs_source"], r["kwargs_lens_light"])
     assert rows.shape[0] == 1
+
+
+def test_split_kernel_product_equals_oracle_and_keeps_weight():
+    from jaxtronomy_gb300.image_model import split_kernel
+    from oracle import numerics as onum
+    k = W.moffat_pixel_kernel(0.12, 3.0, 0.05 / 3, 27)
+    for ssk in (1, 3, 5, 9):
+        lo, hi = split_kernel(k, ssk, 3)
+        lo2, hi2 = onum.split_kernel(k, ssk, 3)
+        np.testing.assert_array_equal(lo, lo2)
+        np.testing.assert_array_equal(hi, hi2)
+        assert np.isclose(lo.sum() + hi.sum(), k.sum())
+        assert hi.shape[0] % 2 == 1 and lo.shape[0] % 2 == 1
+    with pytest.raises(ValueError):
+        split_kernel(k, 3, 2)
+
+
+def test_supersampled_convolution_models():
+    g = W.grid_kwargs(20, 0.05)
+    data = J.ImageData(np.zeros((20, 20)), exposure_time=100.0, background_rms=0.01, **g)
+    ks = W.moffat_pixel_kernel(0.12, 3.0, 0.05 / 3, 27)
+    lm, sm = J.LensModel(["EPL", "SHEAR"]), J.LightModel(["SERSIC_ELLIPSE"])
+    psf = J.PSF("PIXEL", kernel_point_source=ks, point_source_supersampling_factor=3)
+    im = J.ImageModel(data, psf, lm, sm, kwargs_numerics={"supersampling_factor": 3,
+                                                          "supersampling_convolution": True,
+                                                          "supersampling_kernel_size": 3})
+    d = im._desc(range(2), range(1), [])
+    assert d.supersampling_convolution == 1 and d.kernel_size == 9 and d.low_res_kernel_size == 9
+    assert im.pack_psf(ks).size == 81 + 81
+    im2 = J.ImageModel(data, psf, lm, sm, kwargs_numerics={"supersampling_factor": 3,
+                                                           "supersampling_convolution": True,
+                                                           "supersampling_kernel_size": None})
+    d2 = im2._desc(range(2), range(1), [])
+    assert d2.kernel_size == 27 and d2.low_res_kernel_size == 0
+    # an even factor cannot split; a pixel-scale PSF cannot be supersampled here
+    psf2 = J.PSF("PIXEL", kernel_point_source=ks[1:-1, 1:-1][:25, :25],
+                 point_source_supersampling_factor=2)
+    with pytest.raises(ValueError):
+        J.ImageModel(data, psf2, lm, sm, kwargs_numerics={"supersampling_factor": 2,
+                                                          "supersampling_convolution": True})
+    with pytest.raises(NotImplementedError):
+        J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=ks), lm, sm,
+                     kwargs_numerics={"supersampling_factor": 3,
+                                      "supersampling_convolution": True})

@@ -47,12 +47,14 @@ def _submit(srv, models, reqs, psfs, release=None, pinned=False):
 
 
 def test_served_results_equal_alone_results(cuda):
-    reqs, psfs = _stream(120)
+    base, psfs = _stream(60)
+    reqs = [r for r in base for _ in range(2)]  # every request twice, released together
     models = _models(reqs)
     with serving.Server(n_streams=3, max_batch=16) as srv:
         t0 = srv.clock() + 0.01
-        # staggered arrivals: requests join batches while others are in flight
-        release = t0 + np.cumsum(np.random.default_rng(1).exponential(2e-4, len(reqs)))
+        # staggered bursts: requests join batches while others are in flight
+        gaps = np.random.default_rng(1).exponential(4e-4, len(base))
+        release = t0 + np.repeat(np.cumsum(gaps), 2)
         tickets = _submit(srv, models, reqs, psfs, release=release)
         srv.drain(120)
         st = srv.stats()

@@ -693,7 +693,13 @@ def gpu_arm(args):
             "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2) at the sampled "
                            "median SM clock; MEASURED_PEAKS.json has no FP32 figure",
             "algorithmic_gflop_per_launch": flop_ray / 1e9,
-            "transcendentals_per_s": t_ray / rt, "launch_ms": rt * 1e3, "traffic": None,
+            "transcendentals_per_s": t_ray / rt, "launch_ms": rt * 1e3,
+            # DRAM bytes per 1024-system launch (read + write) of raytrace_fp32_kernel plus
+            # refine_kernel, from one ncu capture of this workload (dram__bytes_read.sum +
+            # dram__bytes_write.sum): 0.83 + 74.0 MB and 0.75 + 0 MB.  Below the algorithmic
+            # 132.7 MB image write because the image tail is still in L2 when the kernel ends.
+            "traffic": 75.6e6 if B == 1024 else None,
+            "algorithmic_bytes_per_launch": B * N_PIX * N_PIX * 4 + rows_host.nbytes,
         }
         hbm_peak = 6784.5
         try:
@@ -707,6 +713,9 @@ def gpu_arm(args):
             "achieved": flop_conv / cv / 1e12, "peak": fp32_peak,
             "frac": flop_conv / cv / 1e12 / fp32_peak, "launch_ms": cv * 1e3,
             "hbm_gbs": conv_bytes / cv / 1e9, "hbm_frac_of_measured": conv_bytes / cv / 1e9 / hbm_peak,
+            # one ncu capture of this workload: 136.7 MB read + 83.8 MB written per launch
+            "traffic": 220.5e6 if B == 1024 else None,
+            "algorithmic_bytes_per_launch": conv_bytes,
         }
 
         # --- end to end through the public API with host buffers

@@ -153,7 +153,40 @@ __device__ void prepare_lens_record(int code, const double* a, double* d, double
         double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
         d[RD_CX] = a[3];
         d[RD_CY] = a[4];
-        d[2] = Rs; d[3] = rho0; d[4] = r_trunc / Rs; d[5] = 4 * rho0 * Rs; d[6] = 1.0 / Rs;
+        const double tau = r_trunc / Rs;
+        d[2] = Rs; d[3] = rho0; d[4] = tau; d[5] = 4 * rho0 * Rs; d[6] = 1.0 / Rs;
+        // many-deflector FP32 constants: 1/tau, tau^2/(tau^2+1)^2, tau^2 - 1
+        d[7] = 1.0 / tau; d[8] = tau * tau / ((tau * tau + 1) * (tau * tau + 1));
+        d[9] = tau * tau - 1;
+        // far field x >= 3 s, s = max(tau, 1): the bracket b(x) of g(x) as the series
+        // sum_k c_k z^k in z = s/x (c_k = b_k / s^k, b_k from tnfw_series_gen.py in
+        // this directory; truncation error below 1e-8 relative), and 4 rho0 Rs tau^2/(tau^2+1)^2
+        double b[16];
+        b[0] = pow(tau, 2)*log(tau) - pow(tau, 2) + M_PI*tau - log(tau) - 1;
+        b[1] = 0;
+        b[2] = -1.0/3.0*pow(tau, 4) - 2.0/3.0*pow(tau, 2) - 1.0/3.0;
+        b[3] = (1.0/8.0)*M_PI*pow(tau, 4) + (1.0/4.0)*M_PI*pow(tau, 2) + (1.0/8.0)*M_PI;
+        b[4] = (2.0/15.0)*pow(tau, 6) - 2.0/15.0*pow(tau, 4) - 2.0/3.0*pow(tau, 2) - 2.0/5.0;
+        b[5] = -1.0/16.0*M_PI*pow(tau, 6) + (3.0/16.0)*M_PI*pow(tau, 2) + (1.0/8.0)*M_PI;
+        b[6] = -8.0/105.0*pow(tau, 8) + (8.0/105.0)*pow(tau, 6) - 8.0/15.0*pow(tau, 2) - 8.0/21.0;
+        b[7] = (5.0/128.0)*M_PI*pow(tau, 8) + (5.0/32.0)*M_PI*pow(tau, 2) + (15.0/128.0)*M_PI;
+        b[8] = (16.0/315.0)*pow(tau, 10) - 16.0/315.0*pow(tau, 8) - 16.0/35.0*pow(tau, 2) - 16.0/45.0;
+        b[9] = -7.0/256.0*M_PI*pow(tau, 10) + (35.0/256.0)*M_PI*pow(tau, 2) + (7.0/64.0)*M_PI;
+        b[10] = -128.0/3465.0*pow(tau, 12) + (128.0/3465.0)*pow(tau, 10) - 128.0/315.0*pow(tau, 2) - 128.0/385.0;
+        b[11] = (21.0/1024.0)*M_PI*pow(tau, 12) + (63.0/512.0)*M_PI*pow(tau, 2) + (105.0/1024.0)*M_PI;
+        b[12] = (256.0/9009.0)*pow(tau, 14) - 256.0/9009.0*pow(tau, 12) - 256.0/693.0*pow(tau, 2) - 256.0/819.0;
+        b[13] = -33.0/2048.0*M_PI*pow(tau, 14) + (231.0/2048.0)*M_PI*pow(tau, 2) + (99.0/1024.0)*M_PI;
+        b[14] = -1024.0/45045.0*pow(tau, 16) + (1024.0/45045.0)*pow(tau, 14) - 1024.0/3003.0*pow(tau, 2) - 1024.0/3465.0;
+        b[15] = (429.0/32768.0)*M_PI*pow(tau, 16) + (429.0/4096.0)*M_PI*pow(tau, 2) + (3003.0/32768.0)*M_PI;
+        const double sc = tau > 1.0 ? tau : 1.0;
+        double sk = 1.0;
+        for (int k = 0; k < 16; ++k) {
+            d[12 + k] = b[k] / sk;
+            sk *= sc;
+        }
+        d[10] = 9.0 * sc * sc;
+        d[11] = d[5] * d[8];
+        d[28] = sc;
     }
 }
 

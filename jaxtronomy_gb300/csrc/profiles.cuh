@@ -27,7 +27,8 @@ namespace lensgb {
 //           d9 2/(1+q) b^t
 // SHEAR   : d2 gamma1, d3 gamma2
 // NFW     : d2 Rs (floored), d3 rho0, d4 4 rho0 Rs, d5 1/Rs
-// TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs
+// TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs, d7 1/tau,
+//           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1
 // SERSIC* : d2 amp, d3 R_sersic (floored), d4 1/R_sersic, d5 1/n, d6 b_n,
 //           d7..d10 product-average transform (m00 m01 m10 m11)
 constexpr int F_OFF = 2;  // float slot = double slot + F_OFF
@@ -469,6 +470,62 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
     float B = x2 / (tau * tr) * L - log1pf(x2 / (2.f * tau * tr)) + nfw_g_f(x);
     float br = (t2 - 1.f) * B + 2.f * x2 * nfw_G_f(x) - 3.14159265358979f * x2 / tr;
     return t2 / ((t2 + 1.f) * (t2 + 1.f)) * br;
+}
+
+// FP32 TNFW deflection of one (ray, deflector) pair for many-deflector ray
+// shooting: the same regrouped forms as tnfw_g_f / nfw_g_f / nfw_G_f with G(x)
+// evaluated once, one reciprocal of tau + r shared by L and x^2/(tau (tau+r)),
+// and the per-deflector constants of the record (f6 tau, f7 4 rho0 Rs,
+// f8 1/Rs, f9 1/tau, f10 tau^2/(tau^2+1)^2, f11 tau^2 - 1).  Far from the
+// subhalo (x >= 3 max(tau, 1): f12 holds that bound squared) the bracket is the
+// convergent series sum_k c_k z^k in z = max(tau, 1)/x (f14..f29 = c_0..c_15,
+// f30 = max(tau, 1), f13 = 4 rho0 Rs tau^2/(tau^2+1)^2; within 1e-8 relative).
+__device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy, float& ax,
+                                            float& ay) {
+    const float tau = rec[6], a4 = rec[7], inv_rs = rec[8], inv_tau = rec[9];
+    const float c0 = rec[10], tm1 = rec[11];
+    const float u = fmaf(dx, dx, dy * dy) * (inv_rs * inv_rs);  // x^2
+    if (u >= rec[12]) {
+        const float e = rsqrtf(u);
+        const float z = rec[30] * e;
+        float b = rec[29];
+#pragma unroll
+        for (int k = 14; k >= 0; --k) b = fmaf(b, z, rec[14 + k]);
+        const float a = rec[13] * b * (e * e);
+        ax = a * dx;
+        ay = a * dy;
+        return;
+    }
+    const float t2 = tau * tau;
+    // R >= 0.001 Rs and x >= 0.001 (tnfw.py:85, :335)
+    float X = sqrtf(fmaf(dx, dx, dy * dy)) * inv_rs;
+    X = X > 0.001f ? X : 0.001f;
+    const float x2 = X * X;
+    const float w = (1.f - X) * (1.f + X);
+    float G, gn;
+    if (fabsf(w) < 0.12f) {
+        G = nfw_G_f(X);
+        gn = logf(0.5f * X) + G;
+    } else if (w > 0.f) {
+        const float u = sqrtf(w);
+        const float opu = 1.f + u;
+        const float iu = __frcp_rn(u);
+        G = logf(opu / X) * iu;
+        gn = (logf(2.f / X) * x2 / opu + log1pf(-x2 / (2.f * opu))) * iu;
+    } else {
+        const float rv = rsqrtf(-w);
+        G = atanf(-w * rv) * rv;
+        gn = logf(0.5f * X) + G;
+    }
+    const float r = sqrtf(t2 + x2);
+    const float itr = __frcp_rn(tau + r);
+    const float L = logf(X * itr);
+    const float p = x2 * itr * inv_tau;  // x^2 / (tau (tau + r))
+    const float B = p * L - log1pf(0.5f * p) + gn;
+    const float br = tm1 * B + 2.f * x2 * G - 3.14159265358979f * tau * p;
+    const float a = a4 * (c0 * br) * __frcp_rn(x2);
+    ax = a * dx;
+    ay = a * dy;
 }
 
 template <typename R>

@@ -218,6 +218,8 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     if ((long long)d->nx * d->supersampling > (1 << 22) ||
         (long long)d->ny * d->supersampling > (1 << 22))
         return fail(LENSGB_ERR_INVALID, "supersampled grid side exceeds 2^22");
+    if ((long long)d->nx * d->ny * d->supersampling * d->supersampling >= (1LL << 31))
+        return fail(LENSGB_ERR_INVALID, "more than 2^31 supersampled rays per system");
     if (d->precision != LENSGB_FP64 && d->precision != LENSGB_FP32_SPLIT)
         return fail(LENSGB_ERR_UNSUPPORTED, "unknown precision mode");
     if (d->psf_type != LENSGB_PSF_NONE && d->psf_type != LENSGB_PSF_PIXEL &&

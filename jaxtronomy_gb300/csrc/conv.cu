@@ -15,6 +15,7 @@
 // output row of its block that the row touches.
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 
 #include "launch.h"
@@ -187,6 +188,113 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
     }
 }
 
+// FP32 variant with the kernel width fixed at compile time (NSEG segments of 8
+// columns, K <= 8 NSEG): the same tiles and shared-memory layout as
+// conv_f32_kernel, but the input-row loop is split so that its middle part --
+// every output row of the thread has a kernel row -- runs without branches and
+// with all shared-memory offsets as immediates, and the halo tile is filled row
+// by row without index divisions.
+template <int NSEG>
+__global__ void __launch_bounds__(C32_TX * 16)
+conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
+                      const float* __restrict__ ker, long long kstride, int ny, int nx, int K,
+                      int edge) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int KP = 8 * NSEG;
+    constexpr int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
+    const int TY = blockDim.y;
+    const int H = TY * C32_RY;
+    const int SH = H + K - 1;
+    float* sk = (float*)smem_raw;
+    float* si = sk + K * KP;
+    const int inst = blockIdx.z;
+    const int ox0 = blockIdx.x * C32_W, oy0 = blockIdx.y * H;
+    const int h = K / 2;
+    const int tid = threadIdx.y * C32_TX + threadIdx.x;
+    const int nthr = C32_TX * TY;
+    const float* kk = ker + (long long)inst * kstride;
+    for (int e = tid; e < K * KP; e += nthr) {
+        const int u = e / KP, v = e % KP;
+        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
+    }
+    const float* img = in + (long long)inst * ny * nx;
+    for (int r = threadIdx.y; r < SH; r += TY) {
+        int gy = oy0 - h + r;
+        const bool rin = gy >= 0 && gy < ny;
+        if (edge) gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+        const float* grow = img + (long long)gy * nx;
+        float* srow = si + r * SW;
+        for (int c = threadIdx.x; c < SW; c += C32_TX) {
+            int gx = ox0 - h + c;
+            float v;
+            if (edge) {
+                gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+                v = grow[gx];
+            } else {
+                v = (rin && gx >= 0 && gx < nx) ? grow[gx] : 0.f;
+            }
+            srow[c] = v;
+        }
+    }
+    __syncthreads();
+
+    float acc[C32_RY][C32_CX];
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i)
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
+    const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
+    const float* base = si + r0 * SW + c0;
+    // input row ir feeds output row i through kernel row ir - i
+    auto row_step = [&](int ir, int ilo, int ihi) {
+        const float4* row = reinterpret_cast<const float4*>(base + ir * SW);
+#pragma unroll
+        for (int sg = 0; sg < NSEG; ++sg) {
+            float seg[16];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 q = row[2 * sg + j];
+                seg[4 * j] = q.x;
+                seg[4 * j + 1] = q.y;
+                seg[4 * j + 2] = q.z;
+                seg[4 * j + 3] = q.w;
+            }
+#pragma unroll
+            for (int i = 0; i < C32_RY; ++i) {
+                if (i < ilo || i > ihi) continue;
+                const float4* kr = reinterpret_cast<const float4*>(sk + (ir - i) * KP + 8 * sg);
+                const float4 k0 = kr[0], k1 = kr[1];
+                const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+#pragma unroll
+                for (int vv = 0; vv < 8; ++vv)
+#pragma unroll
+                    for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+            }
+        }
+    };
+    // output row i takes input rows i .. i+K-1, i.e. input row ir serves the
+    // output rows max(0, ir-K+1) .. min(RY-1, ir)
+    // head: input rows 0 .. RY-2
+    for (int ir = 0; ir < C32_RY - 1; ++ir)
+        row_step(ir, ir - K + 1 > 0 ? ir - K + 1 : 0, ir);
+    // body: rows RY-1 .. K-1 serve every output row (branch-free)
+    for (int ir = C32_RY - 1; ir < K; ++ir) row_step(ir, 0, C32_RY - 1);
+    // tail: rows max(K, RY-1) .. K+RY-2
+    for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
+        row_step(ir, ir - K + 1, C32_RY - 1);
+    float* o = out + (long long)inst * ny * nx;
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i) {
+        const int y = oy0 + r0 + i;
+        if (y >= ny) continue;
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) {
+            const int x = ox0 + c0 + c;
+            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+        }
+    }
+}
+
 // Raise a kernel's dynamic shared-memory limit only when a launch needs more
 // than any earlier one (per device and kernel), so that repeated launches --
 // including ones recorded into a CUDA graph -- make no attribute calls.
@@ -223,11 +331,29 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
     const int SW = C32_W + KP + 4;
     const int SH = H + K - 1;
     const size_t smem = (size_t)(K * KP + SH * SW) * sizeof(float);
-    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
     dim3 grid((unsigned)((nx + C32_W - 1) / C32_W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
     dim3 block(C32_TX, best_ty);
-    conv_f32_kernel<<<grid, block, smem, stream>>>((const float*)in, (float*)out,
-                                                   (const float*)kernel, kstride, ny, nx, K, edge);
+    const float* fin = (const float*)in;
+    const float* fk = (const float*)kernel;
+    auto fixed = [&](auto nseg_tag) {
+        constexpr int NS = decltype(nseg_tag)::value;
+        const void* fn = (const void*)conv_f32_fixed_kernel<NS>;
+        if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
+        conv_f32_fixed_kernel<NS><<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny,
+                                                                 nx, K, edge);
+        return 0;
+    };
+    switch (KP / 8) {
+        case 1: return fixed(std::integral_constant<int, 1>());
+        case 2: return fixed(std::integral_constant<int, 2>());
+        case 3: return fixed(std::integral_constant<int, 3>());
+        case 4: return fixed(std::integral_constant<int, 4>());
+        case 5: return fixed(std::integral_constant<int, 5>());
+        case 6: return fixed(std::integral_constant<int, 6>());
+        default: break;
+    }
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
+    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny, nx, K, edge);
     return 0;
 }
 

@@ -180,6 +180,7 @@ raytrace_fp64_kernel(GridDesc g, StackDesc st, int ppt, const double* __restrict
 // ---------------------------------------------------------------------------
 // FP32 kernel (pass 1)
 // ---------------------------------------------------------------------------
+
 // SS > 0 fixes the supersampling factor at compile time (the sub-ray loops
 // unroll); SS = 0 reads it from the grid.
 template <int C0, int C1, int NS, int NLL, int SS>
@@ -226,7 +227,9 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
     for (int kk = 0; kk < ppt; ++kk) {
         const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
         if (pix >= npix) break;
-        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        // pixel index of one system (< 2^31): 32-bit division
+        const unsigned int p32 = (unsigned int)pix;
+        const int row = (int)(p32 / (unsigned int)g.nx), col = (int)(p32 - (unsigned int)row * g.nx);
         const float Jb = (float)(col * s), Ib = (float)(row * s);
         // base-ray offsets from every profile centre, FP64-accurate
         PixOff ol[ML], os[MS], oll[MLL];

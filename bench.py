@@ -501,6 +501,28 @@ def gradient_section(steps, seed=1003):
     }
 
 
+def max_over_ranks(ms, dist=None, device="cpu"):
+    """Step time of the whole job: the maximum of the ranks' mean step times
+    (an all-reduce of one float; nothing on the data path)."""
+    if dist is None:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, ms):
+    """Whole-job throughput: every rank processes units_per_rank per step
+    (weak scaling), the job's step time is the slowest rank's."""
+    return units_per_rank * world / (ms / 1e3)
+
+
+def rank_seed(base, rank):
+    """Each replica simulates its own seeded batch."""
+    return base + rank
+
+
 def percentile(v, q):
     v = sorted(v)
     k = (len(v) - 1) * q
@@ -535,7 +557,7 @@ def gpu_arm(args):
         torch.cuda.synchronize()
 
     B = args.batch
-    model, lens, src, ll, kern = W.batch_epl(seed=1001 + rank, batch=B, num_pix=N_PIX,
+    model, lens, src, ll, kern = W.batch_epl(seed=rank_seed(1001, rank), batch=B, num_pix=N_PIX,
                                              delta_pix=DPIX, supersampling=SS, kernel_size=KSIZE)
     g = W.grid_kwargs(N_PIX, DPIX)
 
@@ -582,11 +604,8 @@ def gpu_arm(args):
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = statistics.mean(step_ms)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = B * world / (ms / 1e3)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = job_rate(B, world, ms)
 
     extra = {}
     if rank == 0:

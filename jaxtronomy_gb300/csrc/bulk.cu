@@ -17,7 +17,7 @@ namespace lensgb {
 
 constexpr int BULK_CHUNK = 64;
 constexpr int BULK_THREADS = 256;
-constexpr int BULK_RPT = 2;  // rays per thread (i and i + BULK_THREADS of the CTA's span)
+constexpr int BULK_RPT = 2;  // rays per thread (i and i + BULK_THREADS of the CTA span)
 
 template <bool F32>
 __global__ void __launch_bounds__(BULK_THREADS)

@@ -178,15 +178,17 @@ __device__ void prepare_lens_record(int code, const double* a, double* d, double
         b[13] = -33.0/2048.0*M_PI*pow(tau, 14) + (231.0/2048.0)*M_PI*pow(tau, 2) + (99.0/1024.0)*M_PI;
         b[14] = -1024.0/45045.0*pow(tau, 16) + (1024.0/45045.0)*pow(tau, 14) - 1024.0/3003.0*pow(tau, 2) - 1024.0/3465.0;
         b[15] = (429.0/32768.0)*M_PI*pow(tau, 16) + (429.0/4096.0)*M_PI*pow(tau, 2) + (3003.0/32768.0)*M_PI;
+        // layout: d10 bound, d11 4 rho0 Rs tau^2/(tau^2+1)^2, d12 s, d14..d29 c_0..c_15
+        // (float slots 16..31: 16-byte aligned for vector loads)
         const double sc = tau > 1.0 ? tau : 1.0;
         double sk = 1.0;
         for (int k = 0; k < 16; ++k) {
-            d[12 + k] = b[k] / sk;
+            d[14 + k] = b[k] / sk;
             sk *= sc;
         }
         d[10] = 9.0 * sc * sc;
         d[11] = d[5] * d[8];
-        d[28] = sc;
+        d[12] = sc;
     }
 }
 

@@ -28,7 +28,8 @@ namespace lensgb {
 // SHEAR   : d2 gamma1, d3 gamma2
 // NFW     : d2 Rs (floored), d3 rho0, d4 4 rho0 Rs, d5 1/Rs
 // TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs, d7 1/tau,
-//           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1
+//           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1, d10..d12 and d14..d29 far-field
+//           series (tnfw_pair_f)
 // SERSIC* : d2 amp, d3 R_sersic (floored), d4 1/R_sersic, d5 1/n, d6 b_n,
 //           d7..d10 product-average transform (m00 m01 m10 m11)
 constexpr int F_OFF = 2;  // float slot = double slot + F_OFF
@@ -478,8 +479,8 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
 // and the per-deflector constants of the record (f6 tau, f7 4 rho0 Rs,
 // f8 1/Rs, f9 1/tau, f10 tau^2/(tau^2+1)^2, f11 tau^2 - 1).  Far from the
 // subhalo (x >= 3 max(tau, 1): f12 holds that bound squared) the bracket is the
-// convergent series sum_k c_k z^k in z = max(tau, 1)/x (f14..f29 = c_0..c_15,
-// f30 = max(tau, 1), f13 = 4 rho0 Rs tau^2/(tau^2+1)^2; within 1e-8 relative).
+// convergent series sum_k c_k z^k in z = max(tau, 1)/x (f16..f31 = c_0..c_15,
+// f14 = max(tau, 1), f13 = 4 rho0 Rs tau^2/(tau^2+1)^2; within 1e-8 relative).
 __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy, float& ax,
                                             float& ay) {
     const float tau = rec[6], a4 = rec[7], inv_rs = rec[8], inv_tau = rec[9];
@@ -487,10 +488,14 @@ __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy
     const float u = fmaf(dx, dx, dy * dy) * (inv_rs * inv_rs);  // x^2
     if (u >= rec[12]) {
         const float e = rsqrtf(u);
-        const float z = rec[30] * e;
-        float b = rec[29];
+        const float z = rec[14] * e;
+        const float4* cv = reinterpret_cast<const float4*>(rec + 16);
+        const float4 q0 = cv[0], q1 = cv[1], q2 = cv[2], q3 = cv[3];
+        const float c[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                             q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+        float b = c[15];
 #pragma unroll
-        for (int k = 14; k >= 0; --k) b = fmaf(b, z, rec[14 + k]);
+        for (int k = 14; k >= 0; --k) b = fmaf(b, z, c[k]);
         const float a = rec[13] * b * (e * e);
         ax = a * dx;
         ay = a * dy;

@@ -118,6 +118,16 @@ int lensgb_model_destroy(lensgb_model* model);
 /* Number of doubles per system row for this model. */
 int lensgb_model_param_count(const lensgb_model* model);
 
+/* NumericsSubFrame (numerics_subframe.py:20-200): compute only the n x n
+ * sub-frame whose top-left pixel is (row0, col0) -- the bounding box of the
+ * reference's flux_evaluate_indexes -- with the n x n evaluation mask `mask`
+ * (host, row-major bytes, 0 = pixel not evaluated; NULL = all), convolve it as
+ * an image of its own and return full images that are zero outside it.  As in
+ * the reference, the sub-frame's pixel (0, 0) is placed at
+ * map_pix2coord(row0, col0) (row index in the pixel-x slot, :185-190). */
+int lensgb_model_set_subframe(lensgb_model* model, int row0, int col0, int n,
+                              const unsigned char* mask);
+
 /* Grow the model's device scratch to hold n_inst systems now, so that later
  * calls with at most n_inst systems allocate nothing (needed before capturing
  * those calls into a CUDA graph).  No counterpart in the reference. */

@@ -38,6 +38,7 @@ NO_LENS_LIGHT = 4
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
+    "lensgb_model_set_subframe",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
     "lensgb_loglike_grad",
     "lensgb_ray_shooting", "lensgb_alpha",
@@ -152,6 +153,8 @@ def load():
     lib.lensgb_model_destroy.restype = i
     lib.lensgb_model_param_count.argtypes = [vp]
     lib.lensgb_model_param_count.restype = i
+    lib.lensgb_model_set_subframe.argtypes = [vp, i, i, i, vp]
+    lib.lensgb_model_set_subframe.restype = i
     lib.lensgb_model_reserve.argtypes = [vp, i]
     lib.lensgb_model_reserve.restype = i
     lib.lensgb_model_set_refine.argtypes = [vp, ctypes.c_double, ctypes.c_double]
@@ -220,15 +223,20 @@ def check(rc):
 class Model:
     """Owner of one lensgb_model handle."""
 
-    def __init__(self, desc, refine=None):
+    def __init__(self, desc, refine=None, subframe=None):
         lib = load()
         h = ctypes.c_void_p()
         check(lib.lensgb_model_create(ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
         self.desc = desc
         self.param_count = lib.lensgb_model_param_count(h)
+        self.subframe = subframe
         if refine is not None:
             check(lib.lensgb_model_set_refine(h, float(refine[0]), float(refine[1])))
+        if subframe is not None:
+            r0, c0, mask = subframe
+            m = (ctypes.c_ubyte * mask.size).from_buffer_copy(mask.astype("uint8").tobytes())
+            check(lib.lensgb_model_set_subframe(h, int(r0), int(c0), int(mask.shape[0]), m))
 
     def refined_pixels(self, stream):
         n = ctypes.c_longlong(0)

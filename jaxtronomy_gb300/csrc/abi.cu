@@ -20,6 +20,12 @@ struct lensgb_model {
     bool hr_conv = false;        // convolution on the supersampled grid
     void* hr_img = nullptr;      // supersampled image and its convolution (hr_conv models)
     void* hr_out = nullptr;
+    // sub-frame (NumericsSubFrame): the kernels run on `grid`, an n x n sub-frame
+    // whose images are embedded at (sub_r0, sub_c0) of the full image
+    bool sub = false;
+    int sub_r0 = 0, sub_c0 = 0;
+    unsigned char* sub_mask = nullptr;  // n x n evaluation mask (device), or null
+    void* sub_out = nullptr;            // sub-frame images before embedding
     StackDesc st;
     double pixel_width;
     int cap_inst = 0;
@@ -99,8 +105,10 @@ static void free_scratch(lensgb_model* m) {
     cudaFree(m->refine_count);
     cudaFree(m->hr_img);
     cudaFree(m->hr_out);
+    cudaFree(m->sub_out);
     m->hr_img = nullptr;
     m->hr_out = nullptr;
+    m->sub_out = nullptr;
     m->refine_list = nullptr;
     m->refine_count = nullptr;
     m->rec_d = nullptr;
@@ -133,7 +141,8 @@ static int ensure_scratch(lensgb_model* m, int n_inst) {
          (cudaMalloc(&m->refine_list, nlist * sizeof(unsigned int)) != cudaSuccess ||
           cudaMalloc(&m->refine_count, sizeof(unsigned int)) != cudaSuccess)) ||
         (m->hr_conv && (cudaMalloc(&m->hr_img, nimg * s2 * esz) != cudaSuccess ||
-                        cudaMalloc(&m->hr_out, nimg * s2 * esz) != cudaSuccess))) {
+                        cudaMalloc(&m->hr_out, nimg * s2 * esz) != cudaSuccess)) ||
+        (m->sub && cudaMalloc(&m->sub_out, nimg * esz) != cudaSuccess)) {
         cudaGetLastError();
         free_scratch(m);
         return fail(LENSGB_ERR_OOM, "device allocation of model scratch failed");
@@ -166,6 +175,35 @@ static RefineArgs refine_args(const lensgb_model* m, int n_inst, unsigned int* l
 }
 
 // The refine list stores 32-bit batch-global pixel indices.
+// Kernel grids of an nx x ny pixel grid whose pixel (0, 0) is at (ra0, dec0),
+// with the model's transform and supersampling: the image grid and its
+// supersampled twin (s = 1), as the ray kernels index them.
+static void set_grids(lensgb_model* m, int nx, int ny, double ra0, double dec0) {
+    const lensgb_model_desc* d = &m->desc;
+    GridDesc& g = m->grid;
+    const double* M = d->transform_pix2angle;
+    const int s = d->supersampling;
+    g.nx = nx;
+    g.ny = ny;
+    g.s = s;
+    const double f0 = 0.5 / s - 0.5;
+    g.ra00 = ra0 + M[0] * f0 + M[1] * f0;
+    g.dec00 = dec0 + M[2] * f0 + M[3] * f0;
+    g.ax = M[0] / s;
+    g.bx = M[1] / s;
+    g.ay = M[2] / s;
+    g.by = M[3] / s;
+    const int bits = exact_bits((nx > ny ? nx : ny) * s);
+    split_bits(g.ax, bits, g.ax_hi, g.ax_lo);
+    split_bits(g.bx, bits, g.bx_hi, g.bx_lo);
+    split_bits(g.ay, bits, g.ay_hi, g.ay_lo);
+    split_bits(g.by, bits, g.by_hi, g.by_lo);
+    m->grid_hr = g;
+    m->grid_hr.nx = g.nx * s;
+    m->grid_hr.ny = g.ny * s;
+    m->grid_hr.s = 1;
+}
+
 static int check_refine_size(const lensgb_model* m, int n_inst) {
     const long long s2 = m->hr_conv ? (long long)m->grid.s * m->grid.s : 1;
     if (m->desc.precision == LENSGB_FP32_SPLIT && m->refine_tau > 0.f &&
@@ -177,7 +215,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 105; }
+int lensgb_version(void) { return 106; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -291,31 +329,40 @@ int lensgb_model_create(const lensgb_model_desc* d, lensgb_model** out) {
     st.flux_scaling_f = (float)d->flux_scaling;
     for (int i = 0; i < MAX_PROF; ++i) st.src_scale_f[i] = (float)st.src_scale[i];
 
-    GridDesc& g = m->grid;
     const double* M = d->transform_pix2angle;
     const int s = d->supersampling;
-    g.nx = d->nx;
-    g.ny = d->ny;
-    g.s = s;
-    const double f0 = 0.5 / s - 0.5;
-    g.ra00 = d->ra_at_xy_0 + M[0] * f0 + M[1] * f0;
-    g.dec00 = d->dec_at_xy_0 + M[2] * f0 + M[3] * f0;
-    g.ax = M[0] / s;
-    g.bx = M[1] / s;
-    g.ay = M[2] / s;
-    g.by = M[3] / s;
-    const int bits = exact_bits((d->nx > d->ny ? d->nx : d->ny) * s);
-    split_bits(g.ax, bits, g.ax_hi, g.ax_lo);
-    split_bits(g.bx, bits, g.bx_hi, g.bx_lo);
-    split_bits(g.ay, bits, g.ay_hi, g.ay_lo);
-    split_bits(g.by, bits, g.by_hi, g.by_lo);
+    set_grids(m, d->nx, d->ny, d->ra_at_xy_0, d->dec_at_xy_0);
     m->pixel_width = sqrt(fabs(M[0] * M[3] - M[1] * M[2]));
     m->hr_conv = d->supersampling_convolution != 0 && s > 1 && d->psf_type != LENSGB_PSF_NONE;
-    m->grid_hr = g;
-    m->grid_hr.nx = g.nx * s;
-    m->grid_hr.ny = g.ny * s;
-    m->grid_hr.s = 1;
     *out = m;
+    return LENSGB_OK;
+}
+
+int lensgb_model_set_subframe(lensgb_model* m, int row0, int col0, int n,
+                              const unsigned char* mask) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n < 1 || row0 < 0 || col0 < 0 || row0 + n > m->desc.ny || col0 + n > m->desc.nx)
+        return fail(LENSGB_ERR_INVALID, "sub-frame outside the image");
+    free_scratch(m);
+    cudaFree(m->sub_mask);
+    m->sub_mask = nullptr;
+    if (mask) {
+        if (cudaMalloc(&m->sub_mask, (size_t)n * n) != cudaSuccess ||
+            cudaMemcpy(m->sub_mask, mask, (size_t)n * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(m->sub_mask);
+            m->sub_mask = nullptr;
+            return fail(LENSGB_ERR_OOM, "sub-frame mask allocation failed");
+        }
+    }
+    // the sub-frame's pixel (0, 0) sits at map_pix2coord(row0, col0): the
+    // reference passes the row index in the pixel-x slot (numerics_subframe.py:185-190)
+    const double* M = m->desc.transform_pix2angle;
+    set_grids(m, n, n, m->desc.ra_at_xy_0 + M[0] * row0 + M[1] * col0,
+              m->desc.dec_at_xy_0 + M[2] * row0 + M[3] * col0);
+    m->sub = true;
+    m->sub_r0 = row0;
+    m->sub_c0 = col0;
     return LENSGB_OK;
 }
 
@@ -325,6 +372,7 @@ int lensgb_model_destroy(lensgb_model* m) {
     if (!m) return LENSGB_OK;
     free_scratch(m);
     free_grad_scratch(m);
+    cudaFree(m->sub_mask);
     delete m;
     return LENSGB_OK;
 }
@@ -337,22 +385,14 @@ int lensgb_model_reserve(lensgb_model* m, int n_inst) {
     return n_inst > 0 ? ensure_scratch(m, n_inst) : LENSGB_OK;
 }
 
-int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* psf,
-                 long long psf_stride, void* out, int flags, void* stream) {
-    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
-    if (n_inst < 0 || n_inst > 65535)
-        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
-    if (n_inst == 0) return LENSGB_OK;
-    if (!out || (!params && m->st.n_params > 0))
-        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+}  // extern "C"
+
+// Images of the model's kernel grid (the sub-frame of sub-frame models) into
+// `out`, with the evaluation mask applied before the convolution.
+static int image_core(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                      long long psf_stride, void* out, int flags, cudaStream_t s) {
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
-    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
-    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
-    int rc = check_refine_size(m, n_inst);
-    if (rc) return rc;
-    rc = ensure_scratch(m, n_inst);
-    if (rc) return rc;
-    cudaStream_t s = (cudaStream_t)stream;
+    int rc;
     launch_prepare(m->grid, m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
     if ((rc = check_cuda("prepare launch"))) return rc;
     if (conv && m->hr_conv) {
@@ -367,6 +407,9 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
         launch_raytrace(m->grid_hr, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f,
                         m->hr_img, flags, 1.0, m->desc.precision, rf, s);
         if ((rc = check_cuda("raytrace launch"))) return rc;
+        if (m->sub_mask)
+            launch_mask(m->hr_img, n_inst, m->grid.ny, m->grid.nx, m->grid.s, m->sub_mask,
+                        m->desc.precision, s);
         if (launch_conv(m->hr_img, m->hr_out, psf, psf_stride, n_inst, m->grid_hr.ny,
                         m->grid_hr.nx, m->desc.kernel_size,
                         m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0, m->desc.precision, s))
@@ -402,6 +445,8 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     launch_raytrace(m->grid, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
                     flags, scale, m->desc.precision, rf, s);
     if ((rc = check_cuda("raytrace launch"))) return rc;
+    if (m->sub_mask)
+        launch_mask(target, n_inst, m->grid.ny, m->grid.nx, 1, m->sub_mask, m->desc.precision, s);
     if (conv) {
         if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
                         m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
@@ -410,6 +455,33 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
         if ((rc = check_cuda("convolution launch"))) return rc;
     }
     return LENSGB_OK;
+}
+
+extern "C" {
+
+int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                 long long psf_stride, void* out, int flags, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!out || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    int rc = check_refine_size(m, n_inst);
+    if (rc) return rc;
+    rc = ensure_scratch(m, n_inst);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!m->sub) return image_core(m, params, n_inst, psf, psf_stride, out, flags, s);
+    // NumericsSubFrame: the sub-frame image, zeros elsewhere (numerics_subframe.py:87-149)
+    rc = image_core(m, params, n_inst, psf, psf_stride, m->sub_out, flags, s);
+    if (rc) return rc;
+    launch_embed(m->sub_out, out, n_inst, m->grid.nx, m->sub_r0, m->sub_c0, m->desc.ny,
+                 m->desc.nx, m->desc.precision, s);
+    return check_cuda("sub-frame embedding launch");
 }
 
 int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const void* psf,
@@ -423,7 +495,7 @@ int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const voi
     if (!in || !out || !psf) return fail(LENSGB_ERR_INVALID, "null image or PSF pointer");
     if (in == out) return fail(LENSGB_ERR_INVALID, "in-place convolution is not supported");
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
-    if (launch_conv(in, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+    if (launch_conv(in, out, psf, psf_stride, n_inst, m->desc.ny, m->desc.nx,
                     m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
                     m->desc.precision, (cudaStream_t)stream))
         return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
@@ -456,7 +528,7 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     a.exposure_time = nd->exposure_time;
     a.background_rms = nd->background_rms;
     a.error_map = nd->error_map_dev;
-    launch_loglike(image_out, n_inst, (long long)m->grid.nx * m->grid.ny, a, logl,
+    launch_loglike(image_out, n_inst, (long long)m->desc.nx * m->desc.ny, a, logl,
                    m->desc.precision, (cudaStream_t)stream);
     return check_cuda("likelihood launch");
 }
@@ -493,9 +565,10 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
         return fail(LENSGB_ERR_UNSUPPORTED,
                     "the likelihood gradient supports PSF types NONE and PIXEL (the transposed "
                     "edge-padded convolution is not provided)");
-    if (m->hr_conv)
+    if (m->hr_conv || m->sub)
         return fail(LENSGB_ERR_UNSUPPORTED,
-                    "the likelihood gradient does not support supersampled convolution");
+                    "the likelihood gradient does not support supersampled convolution or "
+                    "sub-frames");
     if (!grad_supported(m->st))
         return fail(LENSGB_ERR_UNSUPPORTED,
                     "the likelihood gradient supports lens stacks of EPL and SHEAR and Sersic "
@@ -775,9 +848,10 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
     if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
-    if (conv && m->hr_conv)
+    if ((conv && m->hr_conv) || m->sub)
         return fail(LENSGB_ERR_UNSUPPORTED,
-                    "lensgb_image_noalloc does not provide supersampled convolution");
+                    "lensgb_image_noalloc does not provide supersampled convolution or "
+                    "sub-frames");
     const int n_prof = m->st.n_lens + m->st.n_src + m->st.n_ll;
     const size_t nrec = (size_t)n_inst * (n_prof > 0 ? n_prof : 1);
     const size_t ncoef = (size_t)n_inst * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;

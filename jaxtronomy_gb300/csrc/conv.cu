@@ -409,6 +409,56 @@ int launch_resize(const void* hr, void* out, int n_inst, int ny, int nx, int s, 
 }
 
 template <typename R>
+__global__ void mask_kernel(R* __restrict__ img, long long n, int W, int s, int nx,
+                            const unsigned char* __restrict__ mask, long long per_inst) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long p = i % per_inst;
+    const int r = (int)(p / W), c = (int)(p % W);
+    if (!mask[(long long)(r / s) * nx + c / s]) img[i] = (R)0;
+}
+
+int launch_mask(void* img, int n_inst, int ny, int nx, int s, const unsigned char* mask,
+                int precision, cudaStream_t stream) {
+    const long long per = (long long)ny * s * nx * s;
+    const long long n = per * n_inst;
+    if (n <= 0) return 0;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (precision == LENSGB_FP64)
+        mask_kernel<double><<<blocks, 256, 0, stream>>>((double*)img, n, nx * s, s, nx, mask, per);
+    else
+        mask_kernel<float><<<blocks, 256, 0, stream>>>((float*)img, n, nx * s, s, nx, mask, per);
+    return 0;
+}
+
+template <typename R>
+__global__ void embed_kernel(const R* __restrict__ sub, R* __restrict__ out, long long n, int nsub,
+                             int r0, int c0, int nyf, int nxf) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long per = (long long)nyf * nxf;
+    const long long inst = i / per, p = i % per;
+    const int r = (int)(p / nxf) - r0, c = (int)(p % nxf) - c0;
+    out[i] = (r >= 0 && r < nsub && c >= 0 && c < nsub)
+                 ? sub[(inst * nsub + r) * (long long)nsub + c]
+                 : (R)0;
+}
+
+int launch_embed(const void* sub, void* out, int n_inst, int n, int r0, int c0, int ny_full,
+                 int nx_full, int precision, cudaStream_t stream) {
+    const long long total = (long long)ny_full * nx_full * n_inst;
+    if (total <= 0) return 0;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    if (precision == LENSGB_FP64)
+        embed_kernel<double><<<blocks, 256, 0, stream>>>((const double*)sub, (double*)out, total, n,
+                                                         r0, c0, ny_full, nx_full);
+    else
+        embed_kernel<float><<<blocks, 256, 0, stream>>>((const float*)sub, (float*)out, total, n,
+                                                        r0, c0, ny_full, nx_full);
+    return 0;
+}
+
+template <typename R>
 __global__ void add_scaled_kernel(R* __restrict__ out, const R* __restrict__ add, long long n,
                                   double scale) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -36,6 +36,14 @@ int launch_conv(const void* in, void* out, const void* kernel, long long kstride
 int launch_resize(const void* hr, void* out, int n_inst, int ny, int nx, int s, double scale,
                   int precision, cudaStream_t stream);
 
+// Multiply n_inst (ny*s, nx*s) images by an (ny, nx) 0/1 mask (mask[r/s][c/s]).
+int launch_mask(void* img, int n_inst, int ny, int nx, int s, const unsigned char* mask,
+                int precision, cudaStream_t stream);
+// out (n_inst full ny_full x nx_full images) = 0 except the n x n block at
+// (r0, c0), which receives `sub`.
+int launch_embed(const void* sub, void* out, int n_inst, int n, int r0, int c0, int ny_full,
+                 int nx_full, int precision, cudaStream_t stream);
+
 // out[i] = (out[i] + add[i]) * scale over n elements.
 int launch_add_scaled(void* out, const void* add, long long n, double scale, int precision,
                       cudaStream_t stream);

@@ -136,8 +136,20 @@ class ImageModel:
         self._ssc = ssc
         # numerics.py:31: the supersampled kernel is split unless this is None
         self._ssk = kn.get("supersampling_kernel_size", 5) if ssc else None
-        if kn.get("flux_evaluate_indexes") is not None:
-            raise ValueError("flux_evaluate_indexes is not supported by this build")
+        self._subframe = None
+        fei = kn.get("flux_evaluate_indexes")
+        if fei is not None:
+            # NumericsSubFrame._init_sub_frame (numerics_subframe.py:151-163)
+            fei = np.asarray(fei, dtype=bool)
+            if fei.shape != tuple(data_class.num_pixel_axes) or not fei.any():
+                raise ValueError("flux_evaluate_indexes must be a non-empty boolean image")
+            rows, cols = np.where(fei)
+            x0, x1, y0, y1 = rows.min(), rows.max(), cols.min(), cols.max()
+            if x1 - x0 != y1 - y0:
+                # the reference's sub-frame grid has the transposed shape of the
+                # slice it fills (numerics_subframe.py:134-149,176-200)
+                raise ValueError("flux_evaluate_indexes needs a square bounding box")
+            self._subframe = (int(x0), int(y0), fei[x0:x1 + 1, y0:y1 + 1].copy())
         conv_type = kn.get("convolution_type", "fft")
         if conv_type not in ("fft", "grid", "fft_static"):
             raise ValueError("convolution_type %s not supported!" % conv_type)
@@ -242,7 +254,8 @@ class ImageModel:
         key = (tuple(lens_idx), tuple(src_idx), tuple(ll_idx), lensed)
         if key not in self._models:
             refine = self._refine if self._precision == _lib.FP32_SPLIT else None
-            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed), refine)
+            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed), refine,
+                                           self._subframe)
         return self._models[key]
 
     def refined_pixels(self, stream=None):

@@ -29,6 +29,38 @@ def _source_scalings(scene):
     return [float(v) for v in dsl]
 
 
+def _subframe(scene):
+    """``NumericsSubFrame._init_sub_frame`` / ``_sub_pixel_grid`` / ``_cut_frame``
+    (numerics_subframe.py:151-200): the bounding box of ``flux_evaluate_indexes``
+    (rows x0..x1 = axis 0, columns y0..y1 = axis 1) and the sub-frame scene,
+    whose origin is ``map_pix2coord(x0, y0)`` -- the axis-0 index in the pixel-x
+    slot, as the reference passes it -- and whose pixel mask is the cut of
+    ``flux_evaluate_indexes``."""
+    fei = np.asarray(scene["flux_evaluate_indexes"], dtype=bool)
+    rows, cols = np.where(fei)
+    x0, x1, y0, y1 = rows.min(), rows.max(), cols.min(), cols.max()
+    M = np.asarray(scene["transform_pix2angle"], float)
+    sub = dict(scene)
+    sub["flux_evaluate_indexes"] = None
+    sub["nx"] = x1 - x0 + 1
+    sub["ny"] = y1 - y0 + 1
+    sub["ra_at_xy_0"] = scene["ra_at_xy_0"] + x0 * M[0, 0] + y0 * M[0, 1]
+    sub["dec_at_xy_0"] = scene["dec_at_xy_0"] + x0 * M[1, 0] + y0 * M[1, 1]
+    sub["pixel_mask"] = fei[x0:x1 + 1, y0:y1 + 1]
+    return sub, (x0, x1, y0, y1)
+
+
+def _mask_rays(scene, flux):
+    """Zero the rays of pixels outside the evaluation mask (RegularGrid with
+    flux_evaluate_indexes evaluates only those, grid.py:48-64,134-148)."""
+    m = scene.get("pixel_mask")
+    if m is None:
+        return flux
+    s = scene["supersampling_factor"]
+    mm = np.repeat(np.repeat(np.asarray(m, float), s, axis=0), s, axis=1)
+    return flux * mm.reshape(-1)
+
+
 def ray_fluxes(scene, kwargs_lens, kwargs_source, kwargs_lens_light,
                source_add=True, lens_light_add=True):
     """Per-ray flux (before re-binning) of the source (lensed, x flux_scaling)
@@ -49,7 +81,7 @@ def ray_fluxes(scene, kwargs_lens, kwargs_source, kwargs_lens_light,
     ll_list = scene.get("lens_light_model_list", [])
     if lens_light_add and len(ll_list) > 0:
         ll = light.surface_brightness(ll_list, ra, dec, kwargs_lens_light)
-    return src, ll
+    return _mask_rays(scene, src), _mask_rays(scene, ll)
 
 
 def re_size_convolve(scene, flux, unconvolved=False):
@@ -97,6 +129,14 @@ def re_size_convolve(scene, flux, unconvolved=False):
 def image(scene, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
           unconvolved=False, source_add=True, lens_light_add=True):
     """``ImageModel.image`` ``image_model.py:432-492`` (point sources empty)."""
+    if scene.get("flux_evaluate_indexes") is not None:
+        # NumericsSubFrame: compute on the sub-frame, zeros elsewhere (:87-100,134-149)
+        sub, (x0, x1, y0, y1) = _subframe(scene)
+        img = image(sub, kwargs_lens, kwargs_source, kwargs_lens_light, unconvolved,
+                    source_add, lens_light_add)
+        out = np.zeros((scene["ny"], scene["nx"]))
+        out[x0:x1 + 1, y0:y1 + 1] = img
+        return out
     nx, ny = scene["nx"], scene["ny"]
     model = np.zeros((ny, nx))
     src, ll = ray_fluxes(scene, kwargs_lens, kwargs_source, kwargs_lens_light,

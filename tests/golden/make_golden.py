@@ -263,6 +263,20 @@ def gen_images():
                    "lens": model["lens_model_list"], "src": model["source_light_model_list"],
                    "ll": model["lens_light_model_list"], "kwargs_lens": kl, "kwargs_source": ks,
                    "kwargs_lens_light": kll, "image": np.asarray(im.image(kl, ks, kll))})
+    # 8) flux_evaluate_indexes (NumericsSubFrame): a disc mask whose bounding box
+    #    (rows 6..22, columns 11..27) is off the diagonal, s = 2, PIXEL 7x7
+    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=1, num_pix=30, kernel_size=7)
+    kl, ks, kll = W.instance(lens, 0), W.instance(src, 0), W.instance(ll, 0)
+    yy, xx = np.mgrid[0:30, 0:30]
+    mask = (yy - 14) ** 2 + (xx - 19) ** 2 <= 64
+    im = _image_model(30, 0.04, 2, {"psf_type": "PIXEL", "kernel_point_source": kern[0]},
+                      model["lens_model_list"], model["source_light_model_list"],
+                      model["lens_light_model_list"], numerics={"flux_evaluate_indexes": mask})
+    scenes.append({"tag": "subframe", "num_pix": 30, "delta_pix": 0.04, "s": 2,
+                   "psf_type": "PIXEL", "kernel": kern[0], "fei": mask.astype(int).tolist(),
+                   "lens": model["lens_model_list"], "src": model["source_light_model_list"],
+                   "ll": model["lens_light_model_list"], "kwargs_lens": kl, "kwargs_source": ks,
+                   "kwargs_lens_light": kll, "image": np.asarray(im.image(kl, ks, kll))})
     # 6) likelihood on the first single-image scene with noisy data
     rng = np.random.default_rng(77)
     base = scenes[0]

@@ -238,11 +238,13 @@ def _make_grid(numPix, deltapix, subgrid_res=1, left_lower=False):
 
 
 def _array2image(array, nx=0, ny=0):
+    # lenstronomy's util.array2image fills an (nx, ny) array row by row; the
+    # reference relies on that order for non-square shapes (grid.py:127-130)
     array = np.asarray(array)
     if nx == 0 or ny == 0:
         n = int(np.sqrt(len(array)))
         nx = ny = n
-    return array.reshape(ny, nx)
+    return array.reshape(int(nx), int(ny))
 
 
 def _image2array(image):

@@ -48,6 +48,8 @@ def oracle_scene(sc):
             size = sc["cks"] * sc["s"]
             kernel = onum.cut_psf(kernel, size if size % 2 else size + 1)
     extra = {}
+    if sc.get("fei") is not None:
+        extra["flux_evaluate_indexes"] = np.asarray(sc["fei"], dtype=bool)
     if sc.get("ssc"):
         extra = {"supersampling_convolution": True,
                  "supersampling_kernel_size": sc.get("ssk")}

@@ -40,6 +40,8 @@ def build_model(sc, precision="fp64", kernel=None):
     data = J.ImageData(np.zeros((sc["num_pix"], sc["num_pix"])), exposure_time=1000.0,
                        background_rms=0.01, flux_scaling=sc.get("flux_scaling", 1), **g)
     numerics = {"supersampling_factor": sc["s"], "precision": precision}
+    if sc.get("fei") is not None:
+        numerics["flux_evaluate_indexes"] = np.asarray(sc["fei"], dtype=bool)
     ssf = 1
     if sc.get("ssc"):
         numerics["supersampling_convolution"] = True

@@ -241,3 +241,21 @@ def test_supersampled_convolution_models():
         J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=ks), lm, sm,
                      kwargs_numerics={"supersampling_factor": 3,
                                       "supersampling_convolution": True})
+
+
+def test_flux_evaluate_indexes_subframe():
+    g = W.grid_kwargs(20, 0.05)
+    data = J.ImageData(np.zeros((20, 20)), exposure_time=100.0, background_rms=0.01, **g)
+    psf = J.PSF("PIXEL", kernel_point_source=W.gaussian_pixel_kernel(0.1, 0.05, 5))
+    mask = np.zeros((20, 20), bool)
+    mask[3:9, 10:16] = True
+    mask[3, 10] = False
+    im = J.ImageModel(data, psf, J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+                      kwargs_numerics={"flux_evaluate_indexes": mask})
+    r0, c0, cut = im._subframe
+    assert (r0, c0) == (3, 10) and cut.shape == (6, 6) and not cut[0, 0] and cut.sum() == 35
+    bad = np.zeros((20, 20), bool)
+    bad[2:5, 4:12] = True
+    with pytest.raises(ValueError):
+        J.ImageModel(data, psf, J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+                     kwargs_numerics={"flux_evaluate_indexes": bad})

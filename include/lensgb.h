@@ -158,6 +158,26 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
                  const void* psf_dev, long long psf_stride, void* out_dev, int flags,
                  void* stream);
 
+/* lensgb_image for systems of different pixel grids in one launch sequence:
+ * grids[i] (host) gives system i's grid and PSF size; the model supplies the
+ * profile stack, supersampling, PSF type and precision (its own grid fields
+ * are not used).  psf_dev holds the systems' kernels back to back
+ * (kernel_size_i^2 values each), out_dev their images back to back
+ * (ny_i x nx_i each).  Each image equals lensgb_image of that system alone.
+ * Not for supersampled convolution or sub-frame models.  The call waits for
+ * the stream's earlier work before it copies its tables.  No reference
+ * counterpart (the reference compiles one program per grid). */
+typedef struct {
+    int nx, ny;
+    double transform_pix2angle[4];
+    double ra_at_xy_0, dec_at_xy_0;
+    int kernel_size;
+} lensgb_system_grid;
+
+int lensgb_image_mixed(lensgb_model* model, const double* params_dev, int n_inst,
+                       const lensgb_system_grid* grids, const void* psf_dev, void* out_dev,
+                       int flags, void* stream);
+
 /* lensgb_image without any device allocation.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory on the
  * call path -- e.g. a handler invoked from inside an XLA/JAX program (the way a

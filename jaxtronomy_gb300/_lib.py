@@ -39,7 +39,8 @@ SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
     "lensgb_model_set_subframe",
-    "lensgb_image", "lensgb_image_noalloc", "lensgb_convolve", "lensgb_loglike",
+    "lensgb_image", "lensgb_image_noalloc", "lensgb_image_mixed", "lensgb_convolve",
+    "lensgb_loglike",
     "lensgb_loglike_grad",
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
@@ -90,6 +91,17 @@ class NoiseDesc(ctypes.Structure):
         ("background_rms", ctypes.c_double),
         ("error_map_dev", ctypes.c_void_p),
         ("mask_stride", ctypes.c_longlong),
+    ]
+
+
+class SystemGrid(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int),
+        ("ny", ctypes.c_int),
+        ("transform_pix2angle", ctypes.c_double * 4),
+        ("ra_at_xy_0", ctypes.c_double),
+        ("dec_at_xy_0", ctypes.c_double),
+        ("kernel_size", ctypes.c_int),
     ]
 
 
@@ -163,6 +175,8 @@ def load():
     lib.lensgb_model_refined_pixels.restype = i
     lib.lensgb_image.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
     lib.lensgb_image.restype = i
+    lib.lensgb_image_mixed.argtypes = [vp, dp, i, ctypes.POINTER(SystemGrid), vp, vp, i, vp]
+    lib.lensgb_image_mixed.restype = i
     lib.lensgb_image_noalloc.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
     lib.lensgb_image_noalloc.restype = i
     lib.lensgb_convolve.argtypes = [vp, vp, i, vp, ll, vp, vp]

@@ -7,7 +7,9 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <string>
+#include <vector>
 
 #include "launch.h"
 
@@ -26,6 +28,11 @@ struct lensgb_model {
     int sub_r0 = 0, sub_c0 = 0;
     unsigned char* sub_mask = nullptr;  // n x n evaluation mask (device), or null
     void* sub_out = nullptr;            // sub-frame images before embedding
+    // lensgb_image_mixed scratch (grow-only): tables and per-pixel buffers
+    size_t mix_tab_cap = 0, mix_pix_cap = 0;
+    unsigned char* mix_tab = nullptr;
+    void* mix_low = nullptr;
+    unsigned int* mix_list = nullptr;
     StackDesc st;
     double pixel_width;
     int cap_inst = 0;
@@ -178,11 +185,8 @@ static RefineArgs refine_args(const lensgb_model* m, int n_inst, unsigned int* l
 // Kernel grids of an nx x ny pixel grid whose pixel (0, 0) is at (ra0, dec0),
 // with the model's transform and supersampling: the image grid and its
 // supersampled twin (s = 1), as the ray kernels index them.
-static void set_grids(lensgb_model* m, int nx, int ny, double ra0, double dec0) {
-    const lensgb_model_desc* d = &m->desc;
-    GridDesc& g = m->grid;
-    const double* M = d->transform_pix2angle;
-    const int s = d->supersampling;
+static GridDesc make_grid(int nx, int ny, int s, const double* M, double ra0, double dec0) {
+    GridDesc g;
     g.nx = nx;
     g.ny = ny;
     g.s = s;
@@ -198,6 +202,14 @@ static void set_grids(lensgb_model* m, int nx, int ny, double ra0, double dec0) 
     split_bits(g.bx, bits, g.bx_hi, g.bx_lo);
     split_bits(g.ay, bits, g.ay_hi, g.ay_lo);
     split_bits(g.by, bits, g.by_hi, g.by_lo);
+    return g;
+}
+
+static void set_grids(lensgb_model* m, int nx, int ny, double ra0, double dec0) {
+    const lensgb_model_desc* d = &m->desc;
+    m->grid = make_grid(nx, ny, d->supersampling, d->transform_pix2angle, ra0, dec0);
+    const GridDesc& g = m->grid;
+    const int s = d->supersampling;
     m->grid_hr = g;
     m->grid_hr.nx = g.nx * s;
     m->grid_hr.ny = g.ny * s;
@@ -215,7 +227,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 106; }
+int lensgb_version(void) { return 107; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -373,6 +385,9 @@ int lensgb_model_destroy(lensgb_model* m) {
     free_scratch(m);
     free_grad_scratch(m);
     cudaFree(m->sub_mask);
+    cudaFree(m->mix_tab);
+    cudaFree(m->mix_low);
+    cudaFree(m->mix_list);
     delete m;
     return LENSGB_OK;
 }
@@ -482,6 +497,149 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     launch_embed(m->sub_out, out, n_inst, m->grid.nx, m->sub_r0, m->sub_c0, m->desc.ny,
                  m->desc.nx, m->desc.precision, s);
     return check_cuda("sub-frame embedding launch");
+}
+
+int lensgb_image_mixed(lensgb_model* m, const double* params, int n_inst,
+                       const lensgb_system_grid* grids, const void* psf, void* out, int flags,
+                       void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!out || !grids || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params, grids or output pointer");
+    if (m->hr_conv || m->sub)
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "lensgb_image_mixed does not take supersampled-convolution or sub-frame models");
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    const int s = m->desc.supersampling;
+    const bool fp64 = m->desc.precision == LENSGB_FP64;
+    // host tables
+    std::vector<GridDesc> gd((size_t)n_inst);
+    std::vector<long long> off((size_t)n_inst + 1), koff((size_t)n_inst);
+    std::vector<double> area((size_t)n_inst);
+    std::vector<int> ks((size_t)n_inst);
+    std::vector<int2> rblk;
+    long long pix = 0, kel = 0;
+    for (int i = 0; i < n_inst; ++i) {
+        const lensgb_system_grid& q = grids[i];
+        if (q.nx <= 0 || q.ny <= 0 || (long long)q.nx * s > (1 << 22) || (long long)q.ny * s > (1 << 22) ||
+            (long long)q.nx * q.ny * s * s >= (1LL << 31))
+            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad grid size");
+        if (conv && (q.kernel_size < 1 || q.kernel_size % 2 == 0 || q.kernel_size > 255))
+            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad kernel size");
+        gd[i] = make_grid(q.nx, q.ny, s, q.transform_pix2angle, q.ra_at_xy_0, q.dec_at_xy_0);
+        const double* Mq = q.transform_pix2angle;
+        const double pw = sqrt(fabs(Mq[0] * Mq[3] - Mq[1] * Mq[2]));
+        area[i] = pw * pw;  // as the single-grid path forms pixel_width^2
+        off[i] = pix;
+        koff[i] = kel;
+        ks[i] = conv ? q.kernel_size : 0;
+        const long long np = (long long)q.nx * q.ny;
+        for (long long t = 0; t * 256 < np; ++t) rblk.push_back(make_int2(i, (int)t));
+        pix += np;
+        kel += conv ? (long long)q.kernel_size * q.kernel_size : 0;
+    }
+    off[n_inst] = pix;
+    if (pix >= (1LL << 32)) return fail(LENSGB_ERR_INVALID, "more than 2^32 pixels in one call");
+    // convolution CTAs, grouped by kernel width (FP32: segments of 8 columns)
+    std::vector<std::vector<int4>> cgrp(8);
+    std::vector<int> kmax(8, 0);
+    if (conv) {
+        const int TW = fp64 ? 32 : 64, TH = 64;
+        for (int i = 0; i < n_inst; ++i) {
+            int grp = fp64 ? 0 : (ks[i] + 7) / 8;
+            if (grp > 6) grp = 7;  // run-time-width kernel
+            for (int by = 0; by * TH < gd[i].ny; ++by)
+                for (int bx = 0; bx * TW < gd[i].nx; ++bx) cgrp[grp].push_back(make_int4(i, bx, by, 0));
+            kmax[grp] = std::max(kmax[grp], ks[i]);
+        }
+    }
+    // one device table block: grids | off | koff | ksize | ray CTAs | conv CTAs
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    size_t o_grid = 0, o_off = al(o_grid + gd.size() * sizeof(GridDesc));
+    size_t o_koff = al(o_off + off.size() * 8), o_ks = al(o_koff + koff.size() * 8);
+    size_t o_area = al(o_ks + ks.size() * 4);
+    size_t o_rblk = al(o_area + area.size() * 8);
+    size_t o_cblk = al(o_rblk + rblk.size() * sizeof(int2));
+    std::vector<size_t> o_grp(8);
+    size_t end = o_cblk;
+    for (int gidx = 0; gidx < 8; ++gidx) {
+        o_grp[gidx] = end;
+        end = al(end + cgrp[gidx].size() * sizeof(int4));
+    }
+    std::vector<unsigned char> host(end, 0);
+    memcpy(host.data() + o_grid, gd.data(), gd.size() * sizeof(GridDesc));
+    memcpy(host.data() + o_off, off.data(), off.size() * 8);
+    memcpy(host.data() + o_koff, koff.data(), koff.size() * 8);
+    memcpy(host.data() + o_ks, ks.data(), ks.size() * 4);
+    memcpy(host.data() + o_area, area.data(), area.size() * 8);
+    memcpy(host.data() + o_rblk, rblk.data(), rblk.size() * sizeof(int2));
+    for (int gidx = 0; gidx < 8; ++gidx)
+        if (!cgrp[gidx].empty())
+            memcpy(host.data() + o_grp[gidx], cgrp[gidx].data(), cgrp[gidx].size() * sizeof(int4));
+    int rc = ensure_scratch(m, n_inst);
+    if (rc) return rc;
+    const size_t esz = fp64 ? 8 : 4;
+    if (end > m->mix_tab_cap || (size_t)pix > m->mix_pix_cap) {
+        cudaFree(m->mix_tab);
+        cudaFree(m->mix_low);
+        cudaFree(m->mix_list);
+        m->mix_tab = nullptr;
+        m->mix_low = nullptr;
+        m->mix_list = nullptr;
+        const size_t tc = std::max(end, m->mix_tab_cap), pc = std::max((size_t)pix, m->mix_pix_cap);
+        m->mix_tab_cap = m->mix_pix_cap = 0;
+        if (cudaMalloc(&m->mix_tab, tc) != cudaSuccess ||
+            cudaMalloc(&m->mix_low, pc * esz) != cudaSuccess ||
+            cudaMalloc(&m->mix_list, pc * sizeof(unsigned int)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(LENSGB_ERR_OOM, "device allocation of mixed-launch scratch failed");
+        }
+        m->mix_tab_cap = tc;
+        m->mix_pix_cap = pc;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    // pageable source: the copy waits for the stream's earlier work, which may
+    // still read the previous tables
+    if (cudaMemcpyAsync(m->mix_tab, host.data(), end, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return check_cuda("mixed table copy");
+    const GridDesc* dgrid = (const GridDesc*)(m->mix_tab + o_grid);
+    MixedTab mt;
+    mt.grid = dgrid;
+    mt.off = (const long long*)(m->mix_tab + o_off);
+    mt.blk = (const int2*)(m->mix_tab + o_rblk);
+    mt.scale = (const double*)(m->mix_tab + o_area);
+    mt.n_inst = n_inst;
+    launch_prepare(gd[0], m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, st,
+                   dgrid);
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    RefineArgs rf = refine_args(m, n_inst, m->mix_list, m->refine_count);
+    if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), st) != cudaSuccess)
+        return check_cuda("refine counter reset");
+    void* target = conv ? m->mix_low : out;
+    launch_raytrace(gd[0], m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target, flags,
+                    m->pixel_width * m->pixel_width, m->desc.precision, rf, st, &mt,
+                    (int)rblk.size());
+    if ((rc = check_cuda("raytrace launch"))) return rc;
+    if (conv) {
+        ConvMixed cm;
+        cm.grid = dgrid;
+        cm.off = mt.off;
+        cm.koff = (const long long*)(m->mix_tab + o_koff);
+        cm.ksize = (const int*)(m->mix_tab + o_ks);
+        for (int gidx = 0; gidx < 8; ++gidx) {
+            if (cgrp[gidx].empty()) continue;
+            cm.blk = (const int4*)(m->mix_tab + o_grp[gidx]);
+            if (launch_conv_mixed(m->mix_low, out, psf, cm, (int)cgrp[gidx].size(), kmax[gidx],
+                                  gidx == 7 ? 0 : gidx, m->desc.psf_type == LENSGB_PSF_GAUSSIAN,
+                                  m->desc.precision, st))
+                return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        }
+        if ((rc = check_cuda("convolution launch"))) return rc;
+    }
+    return LENSGB_OK;
 }
 
 int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const void* psf,

@@ -64,6 +64,29 @@ struct RefineArgs {
     float kappa;                // FP32 relative error bound of |alpha| (units of 1)
 };
 
+// Launch over systems of different grids (one model's profile stack and
+// supersampling): per-system grids and image offsets, and for each CTA of the
+// ray kernels its (system, tile).  grid == nullptr: every system uses the
+// launch's own grid and images are nx * ny apart.
+struct MixedTab {
+    const GridDesc* grid;   // [n_inst]
+    const long long* off;   // [n_inst + 1]: element offset of each system's image
+    const int2* blk;        // [ray CTAs]: (system, tile of 256 pixels)
+    const double* scale;    // [n_inst]: image scale (pixel area) of each system
+    int n_inst;
+};
+
+// Convolution over systems of different sizes: per CTA (system, tile x,
+// tile y); per system its grid (nx, ny), image offset, kernel offset and K.
+// blk == nullptr: a uniform launch.
+struct ConvMixed {
+    const int4* blk;
+    const GridDesc* grid;
+    const long long* off;
+    const long long* koff;
+    const int* ksize;
+};
+
 // Unique profile codes of a bulk handle (LensModelBulk's unique_lens_model_list);
 // index u.n stands for the NULL profile.
 struct BulkUnique {

@@ -24,28 +24,45 @@ namespace lensgb {
 
 constexpr int CONV_TX = 8, CONV_TY = 16;
 
+// Which system and tile a CTA convolves: blockIdx.z / (x, y) for a uniform
+// launch, or the CTA's table entry of a launch over systems of different
+// sizes (ny, nx, K and the image / kernel offsets then come from the tables).
+#define CONV_MIXED_PREAMBLE                                                            \
+    int bxi = blockIdx.x, byi = blockIdx.y;                                            \
+    long long ioff = (long long)blockIdx.z * ny * nx, koff = (long long)blockIdx.z * kstride; \
+    if (cm.blk) {                                                                      \
+        const int4 b = cm.blk[blockIdx.x];                                             \
+        bxi = b.y;                                                                     \
+        byi = b.z;                                                                     \
+        nx = cm.grid[b.x].nx;                                                          \
+        ny = cm.grid[b.x].ny;                                                          \
+        K = cm.ksize[b.x];                                                             \
+        ioff = cm.off[b.x];                                                            \
+        koff = cm.koff[b.x];                                                           \
+    }
+
 template <typename R, int CX, int RY, int VC>
 __global__ void __launch_bounds__(CONV_TX* CONV_TY)
 conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__ ker,
-            long long kstride, int ny, int nx, int K, int edge) {
+            long long kstride, int ny, int nx, int K, int edge, ConvMixed cm) {
     constexpr int W = CONV_TX * CX, H = CONV_TY * RY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CONV_MIXED_PREAMBLE
     R* sk = (R*)smem_raw;
     const int KP = ((K + VC - 1) / VC) * VC;
     const int SW = W + KP - 1 + 1;  // +1 keeps row starts off the same bank
     const int SH = H + K - 1;
     R* si = sk + K * KP;
-    const int inst = blockIdx.z;
-    const int ox0 = blockIdx.x * W, oy0 = blockIdx.y * H;
+    const int ox0 = bxi * W, oy0 = byi * H;
     const int h = K / 2;
     const int tid = threadIdx.y * CONV_TX + threadIdx.x;
     const int nthr = CONV_TX * CONV_TY;
-    const R* kk = ker + (long long)inst * kstride;
+    const R* kk = ker + koff;
     for (int e = tid; e < K * KP; e += nthr) {
         int u = e / KP, v = e - u * KP;
         sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : R(0);
     }
-    const R* img = in + (long long)inst * ny * nx;
+    const R* img = in + ioff;
     for (int e = tid; e < SH * SW; e += nthr) {
         int r = e / SW, c = e - r * SW;
         int gy = oy0 - h + r, gx = ox0 - h + c;
@@ -87,7 +104,7 @@ conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__
             }
         }
     }
-    R* o = out + (long long)inst * ny * nx;
+    R* o = out + ioff;
 #pragma unroll
     for (int i = 0; i < RY; ++i) {
         const int y = oy0 + r0 + i;
@@ -108,8 +125,10 @@ constexpr int C32_CX = 8, C32_RY = 4, C32_TX = 8, C32_W = C32_TX * C32_CX;
 
 __global__ void __launch_bounds__(C32_TX * 16)
 conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
-                const float* __restrict__ ker, long long kstride, int ny, int nx, int K, int edge) {
+                const float* __restrict__ ker, long long kstride, int ny, int nx, int K, int edge,
+                ConvMixed cm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CONV_MIXED_PREAMBLE
     const int TY = blockDim.y;
     const int H = TY * C32_RY;
     const int KP = ((K + 7) / 8) * 8;
@@ -117,17 +136,16 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
     const int SH = H + K - 1;
     float* sk = (float*)smem_raw;
     float* si = sk + K * KP;
-    const int inst = blockIdx.z;
-    const int ox0 = blockIdx.x * C32_W, oy0 = blockIdx.y * H;
+    const int ox0 = bxi * C32_W, oy0 = byi * H;
     const int h = K / 2;
     const int tid = threadIdx.y * C32_TX + threadIdx.x;
     const int nthr = C32_TX * TY;
-    const float* kk = ker + (long long)inst * kstride;
+    const float* kk = ker + koff;
     for (int e = tid; e < K * KP; e += nthr) {
         const int u = e / KP, v = e - u * KP;
         sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
     }
-    const float* img = in + (long long)inst * ny * nx;
+    const float* img = in + ioff;
     for (int e = tid; e < SH * SW; e += nthr) {
         const int r = e / SW, c = e - r * SW;
         int gy = oy0 - h + r, gx = ox0 - h + c;
@@ -175,7 +193,7 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
             }
         }
     }
-    float* o = out + (long long)inst * ny * nx;
+    float* o = out + ioff;
 #pragma unroll
     for (int i = 0; i < C32_RY; ++i) {
         const int y = oy0 + r0 + i;
@@ -198,8 +216,9 @@ template <int NSEG>
 __global__ void __launch_bounds__(C32_TX * 16)
 conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
                       const float* __restrict__ ker, long long kstride, int ny, int nx, int K,
-                      int edge) {
+                      int edge, ConvMixed cm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    CONV_MIXED_PREAMBLE
     constexpr int KP = 8 * NSEG;
     constexpr int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
     const int TY = blockDim.y;
@@ -207,17 +226,16 @@ conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
     const int SH = H + K - 1;
     float* sk = (float*)smem_raw;
     float* si = sk + K * KP;
-    const int inst = blockIdx.z;
-    const int ox0 = blockIdx.x * C32_W, oy0 = blockIdx.y * H;
+    const int ox0 = bxi * C32_W, oy0 = byi * H;
     const int h = K / 2;
     const int tid = threadIdx.y * C32_TX + threadIdx.x;
     const int nthr = C32_TX * TY;
-    const float* kk = ker + (long long)inst * kstride;
+    const float* kk = ker + koff;
     for (int e = tid; e < K * KP; e += nthr) {
         const int u = e / KP, v = e % KP;
         sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
     }
-    const float* img = in + (long long)inst * ny * nx;
+    const float* img = in + ioff;
     for (int r = threadIdx.y; r < SH; r += TY) {
         int gy = oy0 - h + r;
         const bool rin = gy >= 0 && gy < ny;
@@ -282,7 +300,7 @@ conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
     // tail: rows max(K, RY-1) .. K+RY-2
     for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
         row_step(ir, ir - K + 1, C32_RY - 1);
-    float* o = out + (long long)inst * ny * nx;
+    float* o = out + ioff;
 #pragma unroll
     for (int i = 0; i < C32_RY; ++i) {
         const int y = oy0 + r0 + i;
@@ -340,7 +358,7 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
         const void* fn = (const void*)conv_f32_fixed_kernel<NS>;
         if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
         conv_f32_fixed_kernel<NS><<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny,
-                                                                 nx, K, edge);
+                                                                 nx, K, edge, ConvMixed{});
         return 0;
     };
     switch (KP / 8) {
@@ -353,7 +371,8 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
         default: break;
     }
     if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
-    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny, nx, K, edge);
+    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny, nx, K, edge,
+                                                   ConvMixed{});
     return 0;
 }
 
@@ -370,7 +389,7 @@ static int run_conv(const void* in, void* out, const void* kernel, long long kst
     dim3 grid((unsigned)((nx + W - 1) / W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
     dim3 block(CONV_TX, CONV_TY);
     conv_kernel<R, CX, RY, VC><<<grid, block, smem, stream>>>(
-        (const R*)in, (R*)out, (const R*)kernel, kstride, ny, nx, K, edge);
+        (const R*)in, (R*)out, (const R*)kernel, kstride, ny, nx, K, edge, ConvMixed{});
     return 0;
 }
 
@@ -475,6 +494,52 @@ int launch_add_scaled(void* out, const void* add, long long n, double scale, int
     else
         add_scaled_kernel<float><<<blocks, 256, 0, stream>>>((float*)out, (const float*)add, n,
                                                              scale);
+    return 0;
+}
+
+int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvMixed& cm,
+                      int n_ctas, int kmax, int group, int edge, int precision,
+                      cudaStream_t stream) {
+    if (n_ctas <= 0) return 0;
+    const dim3 grid((unsigned)n_ctas);
+    if (precision == LENSGB_FP64) {
+        constexpr int W = CONV_TX * 4, H = CONV_TY * 4;
+        const int KP = ((kmax + 3) / 4) * 4;
+        const size_t smem = (size_t)(kmax * KP + (H + kmax - 1) * (W + KP)) * sizeof(double);
+        const void* fn = (const void*)conv_kernel<double, 4, 4, 4>;
+        if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
+        conv_kernel<double, 4, 4, 4><<<grid, dim3(CONV_TX, CONV_TY), smem, stream>>>(
+            (const double*)in, (double*)out, (const double*)kernel, 0, 0, 0, 0, edge, cm);
+        return 0;
+    }
+    // FP32: tiles of 64 x 64 (blockDim 8 x 16); `group` = kernel segments of 8
+    // columns (0: the run-time-width kernel)
+    const int TY = 16, H = 4 * TY;
+    const int KP = group > 0 ? 8 * group : ((kmax + 7) / 8) * 8;
+    const int SW = C32_W + KP + 4;
+    const size_t smem = (size_t)(kmax * KP + (H + kmax - 1) * SW) * sizeof(float);
+    const dim3 block(C32_TX, TY);
+    const float* fin = (const float*)in;
+    const float* fk = (const float*)kernel;
+    auto fixed = [&](auto nseg_tag) {
+        constexpr int NS = decltype(nseg_tag)::value;
+        const void* fn = (const void*)conv_f32_fixed_kernel<NS>;
+        if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
+        conv_f32_fixed_kernel<NS><<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0,
+                                                                 edge, cm);
+        return 0;
+    };
+    switch (group) {
+        case 1: return fixed(std::integral_constant<int, 1>());
+        case 2: return fixed(std::integral_constant<int, 2>());
+        case 3: return fixed(std::integral_constant<int, 3>());
+        case 4: return fixed(std::integral_constant<int, 4>());
+        case 5: return fixed(std::integral_constant<int, 5>());
+        case 6: return fixed(std::integral_constant<int, 6>());
+        default: break;
+    }
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
+    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
     return 0;
 }
 

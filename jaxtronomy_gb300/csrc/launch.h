@@ -15,21 +15,31 @@ void set_last_error(const std::string& msg);
 
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
                    double* rec_d, float* rec_f, double* coef_d, float* coef_f,
-                   cudaStream_t stream);
+                   cudaStream_t stream, const GridDesc* grids = nullptr);
 
 // Supersampled ray tracing + light + s x s re-binning into a (ny, nx) image per
 // system, scaled by out_scale (pixel_width^2).  `precision` selects FP64 or FP32;
 // the FP32 path refines flagged pixels in FP64 as described by `rf`
 // (rf.count must be zero on the stream when the launch starts).
+// `mixed` (device tables, or null): systems of different grids in one launch
+// of mixed_ctas CTAs (g then only supplies s); images are laid out at mixed->off.
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,
                     int flags, double out_scale, int precision, const RefineArgs& rf,
-                    cudaStream_t stream);
+                    cudaStream_t stream, const MixedTab* mixed = nullptr, int mixed_ctas = 0);
 
 // "same"-mode 2-D convolution of n_inst (ny, nx) images with K x K kernels
 // (kernel stride 0 = shared).  edge = 0: zero padding; 1: edge padding.
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream);
+
+// Convolution of systems of different sizes (tables in `cm`): one launch of
+// n_ctas CTAs whose kernels are at most kmax wide; FP32 `group` g > 0 runs the
+// kernel specialised for widths <= 8 g (systems are grouped by it), 0 the
+// run-time-width one.  Tiles are 64 x 64 (FP32) / 32 x 64 (FP64) pixels.
+int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvMixed& cm,
+                      int n_ctas, int kmax, int group, int edge, int precision,
+                      cudaStream_t stream);
 
 // s x s block mean (image_util.re_size, image_util.py:79-98: mean over
 // sub-columns, then sub-rows) of n_inst (ny*s, nx*s) images, times scale.

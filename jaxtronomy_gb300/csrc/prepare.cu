@@ -223,7 +223,8 @@ __device__ void finish_record_f(const double* d, float* f) {
 
 __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                                int n_inst, double* __restrict__ rec_d, float* __restrict__ rec_f,
-                               double* __restrict__ coef_d, float* __restrict__ coef_f) {
+                               double* __restrict__ coef_d, float* __restrict__ coef_f,
+                               const GridDesc* __restrict__ grids) {
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)n_inst * n_prof) return;
@@ -253,19 +254,19 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
         prepare_light_record(code, a, d);
     }
     finish_record_f(d, f);
-    write_offsets(g, d[RD_CX], d[RD_CY], f);
+    write_offsets(grids ? grids[inst] : g, d[RD_CX], d[RD_CY], f);
 }
 
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
                    double* rec_d, float* rec_f, double* coef_d, float* coef_f,
-                   cudaStream_t stream) {
+                   cudaStream_t stream, const GridDesc* grids) {
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     long long n = (long long)n_inst * n_prof;
     if (n == 0) return 0;
     int threads = 128;
     int blocks = (int)((n + threads - 1) / threads);
     prepare_kernel<<<blocks, threads, 0, stream>>>(g, st, params, n_inst, rec_d, rec_f, coef_d,
-                                                   coef_f);
+                                                   coef_f, grids);
     return 0;
 }
 

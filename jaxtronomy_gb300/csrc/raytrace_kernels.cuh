@@ -157,18 +157,22 @@ __device__ __forceinline__ void load_records(const StackDesc& st, const R* rec, 
 // ---------------------------------------------------------------------------
 template <int C0, int C1, int NS, int NLL>
 __global__ void __launch_bounds__(256)
-raytrace_fp64_kernel(GridDesc g, StackDesc st, int ppt, const double* __restrict__ rec,
+raytrace_fp64_kernel(GridDesc g0, StackDesc st, int ppt, const double* __restrict__ rec,
                      const double* __restrict__ coef, double* __restrict__ out, int flags,
-                     double out_scale) {
+                     double out_scale, MixedTab mt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     double* srec = (double*)smem_raw;
     double* scoef = srec + n_prof * REC_D;
-    const int inst = blockIdx.y;
+    const bool mixed = mt.grid != nullptr;
+    const int2 bt = mixed ? mt.blk[blockIdx.x] : make_int2((int)blockIdx.y, (int)blockIdx.x);
+    const int inst = bt.x;
+    const GridDesc g = mixed ? mt.grid[inst] : g0;
+    if (mixed) out_scale = mt.scale[inst];
     load_records<double>(st, rec, coef, inst, srec, scoef);
     const long long npix = (long long)g.nx * g.ny;
-    double* o = out + (long long)inst * npix;
-    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
+    double* o = out + (mixed ? mt.off[inst] : (long long)inst * npix);
+    const long long base = (long long)bt.y * blockDim.x * ppt;
     for (int k = 0; k < ppt; ++k) {
         const long long pix = base + (long long)k * blockDim.x + threadIdx.x;
         if (pix >= npix) break;
@@ -185,15 +189,19 @@ raytrace_fp64_kernel(GridDesc g, StackDesc st, int ppt, const double* __restrict
 // unroll); SS = 0 reads it from the grid.
 template <int C0, int C1, int NS, int NLL, int SS>
 __global__ void __launch_bounds__(256)
-raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict__ rec,
+raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict__ rec,
                      const float* __restrict__ coef, float* __restrict__ out, int flags,
-                     float out_scale, RefineArgs rf) {
+                     float out_scale, RefineArgs rf, MixedTab mt) {
     using LS = LensStackT<C0, C1>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     float* srec = (float*)smem_raw;
     float* scoef = srec + n_prof * REC_F;
-    const int inst = blockIdx.y;
+    const bool mixed = mt.grid != nullptr;
+    const int2 bt = mixed ? mt.blk[blockIdx.x] : make_int2((int)blockIdx.y, (int)blockIdx.x);
+    const int inst = bt.x;
+    const GridDesc g = mixed ? mt.grid[inst] : g0;
+    if (mixed) out_scale = (float)mt.scale[inst];
     load_records<float>(st, rec, coef, inst, srec, scoef);
 
     const int n_lens = LS::generic ? st.n_lens : LS::n;
@@ -221,8 +229,9 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
     const float axf = g.ax_hi + g.ax_lo, bxf = g.bx_hi + g.bx_lo;
     const float ayf = g.ay_hi + g.ay_lo, byf = g.by_hi + g.by_lo;
     const long long npix = (long long)g.nx * g.ny;
-    float* o = out + (long long)inst * npix;
-    const long long base = (long long)blockIdx.x * blockDim.x * ppt;
+    const long long img0 = mixed ? mt.off[inst] : (long long)inst * npix;
+    float* o = out + img0;
+    const long long base = (long long)bt.y * blockDim.x * ppt;
 
     for (int kk = 0; kk < ppt; ++kk) {
         const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
@@ -314,7 +323,7 @@ raytrace_fp32_kernel(GridDesc g, StackDesc st, int ppt, const float* __restrict_
         o[pix] = acc * st.flux_scaling_f * out_scale;
         if (flag) {
             const unsigned int slot_i = atomicAdd(rf.count, 1u);
-            rf.list[slot_i] = (unsigned int)((long long)inst * npix + pix);
+            rf.list[slot_i] = (unsigned int)(img0 + pix);
         }
     }
 #undef REC
@@ -331,14 +340,14 @@ constexpr int REFINE_THREADS = 128;
 
 template <int C0, int C1, int NS, int NLL>
 __global__ void __launch_bounds__(REFINE_THREADS)
-refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
+refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
               const double* __restrict__ coef, float* __restrict__ out, int flags,
-              double out_scale, RefineArgs rf) {
+              double out_scale, RefineArgs rf, MixedTab mt) {
     __shared__ double sub[32 * 32];  // s <= 32
     const unsigned int n = *rf.count;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const long long npix = (long long)g.nx * g.ny;
-    const int s = g.s, s2 = s * s;
+    const bool mixed = mt.grid != nullptr;
+    const int s = g0.s, s2 = s * s;
     const int per = s2 <= REFINE_THREADS ? REFINE_THREADS / s2 : 1;  // pixels per chunk
     for (unsigned int first = blockIdx.x * per; first < n; first += gridDim.x * per) {
         for (int w = threadIdx.x; w < per * s2; w += REFINE_THREADS) {
@@ -346,8 +355,20 @@ refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
             double v = 0.0;
             if (first + el < n) {
                 const long long e = (long long)rf.list[first + el];
-                const int inst = (int)(e / npix);
-                const long long pix = e - (long long)inst * npix;
+                int inst;
+                if (mixed) {
+                    // the system whose image holds element e: off[inst] <= e < off[inst + 1]
+                    int lo = 0, hi = mt.n_inst - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
+                    }
+                    inst = lo;
+                } else {
+                    inst = (int)(e / ((long long)g0.nx * g0.ny));
+                }
+                const GridDesc g = mixed ? mt.grid[inst] : g0;
+                const long long pix = e - (mixed ? mt.off[inst] : (long long)inst * g.nx * g.ny);
                 const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
                 const int si = k / s, sj = k - si * s;
                 v = ray_flux_d<C0, C1, NS, NLL>(g, st, rec + (long long)inst * n_prof * REC_D,
@@ -367,7 +388,17 @@ refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
                 acc += s == 1 ? rs : rs / (double)s;
             }
             if (s > 1) acc = acc / (double)s;
-            out[rf.list[first + el]] = (float)(acc * out_scale);
+            double osc = out_scale;
+            if (mixed) {
+                const long long e = (long long)rf.list[first + el];
+                int lo = 0, hi = mt.n_inst - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
+                }
+                osc = mt.scale[lo];
+            }
+            out[rf.list[first + el]] = (float)(acc * osc);
         }
         __syncthreads();
     }
@@ -391,7 +422,8 @@ template <int C0, int C1, int NS, int NLL>
 void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                            const float* rec_f, const double* coef_d, const float* coef_f,
                            void* out, int flags, double out_scale, int precision,
-                           const RefineArgs& rf, cudaStream_t stream) {
+                           const RefineArgs& rf, const MixedTab& mt, int mixed_ctas,
+                           cudaStream_t stream) {
     const int threads = 256;
     const long long npix = (long long)g.nx * g.ny;
     // pixels per thread: enough CTAs to fill the GPU several times over
@@ -399,8 +431,10 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
     long long total = npix * (long long)n_inst;
     int ppt = (int)((total + target - 1) / target);
     ppt = ppt < 1 ? 1 : (ppt > 8 ? 8 : ppt);
+    if (mt.grid) ppt = 1;  // mixed launches: one tile of 256 pixels per CTA
     const long long per_cta = (long long)threads * ppt;
-    dim3 grid((unsigned)((npix + per_cta - 1) / per_cta), (unsigned)n_inst);
+    dim3 grid = mt.grid ? dim3((unsigned)mixed_ctas, 1)
+                        : dim3((unsigned)((npix + per_cta - 1) / per_cta), (unsigned)n_inst);
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     if (precision == LENSGB_FP64) {
         size_t smem = (size_t)(n_prof * REC_D + st.n_epl * EPL_NMAX) * sizeof(double);
@@ -408,7 +442,7 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
             cudaFuncSetAttribute(raytrace_fp64_kernel<C0, C1, NS, NLL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         raytrace_fp64_kernel<C0, C1, NS, NLL><<<grid, threads, smem, stream>>>(
-            g, st, ppt, rec_d, coef_d, (double*)out, flags, out_scale);
+            g, st, ppt, rec_d, coef_d, (double*)out, flags, out_scale, mt);
     } else {
         size_t smem = (size_t)(n_prof * REC_F + st.n_epl * EPL_NMAX) * sizeof(float);
         // compile-time supersampling factor for the specialised stacks
@@ -418,7 +452,7 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
                 cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL, SS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             raytrace_fp32_kernel<C0, C1, NS, NLL, SS><<<grid, threads, smem, stream>>>(
-                g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf);
+                g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf, mt);
         };
         if (C0 == GENERIC) run(std::integral_constant<int, 0>());
         else if (g.s == 1) run(std::integral_constant<int, 1>());
@@ -429,7 +463,7 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
         if (rf.tau > 0.f && !(flags & LENSGB_NO_SOURCE) && st.n_src > 0) {
             const int rblocks = num_sms() * 4;
             refine_kernel<C0, C1, NS, NLL><<<rblocks, 128, 0, stream>>>(
-                g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf);
+                g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf, mt);
         }
     }
 }

@@ -573,3 +573,66 @@ class ImageModel:
 
 
 __all__ = ["ImageModel", "PSF"]
+
+
+def image_mixed(requests, stream=None):
+    """Images of systems on different pixel grids (and PSF sizes) in one launch
+    sequence (``lensgb_image_mixed``).  ``requests``: list of (image_model,
+    kwargs_lens, kwargs_source, kwargs_lens_light[, psf_kernel]) with one system
+    each; the image models must share their profile lists, supersampling, PSF
+    type and precision.  Returns one CUDA tensor per request, each equal to that
+    model's ``image_batch`` of the request alone."""
+    _device.require_cuda()
+    if not requests:
+        return []
+    first = requests[0][0]
+    key = None
+    rows, grids, psfs, shapes = [], [], [], []
+    for req in requests:
+        im, kl, ks, kll = req[:4]
+        psf = req[4] if len(req) > 4 else None
+        d = im._desc(range(len(im.LensModel.lens_model_list)),
+                     range(len(im.SourceModel.profile_type_list)),
+                     range(len(im.LensLightModel.profile_type_list)))
+        k = (tuple(d.lens_codes[:d.n_lens]), tuple(d.source_codes[:d.n_source]),
+             tuple(d.deflection_scaling[:d.n_source]), tuple(d.lens_light_codes[:d.n_lens_light]),
+             d.supersampling, d.psf_type, d.precision, d.flux_scaling, d.alpha_scaling)
+        if key is None:
+            key = k
+        elif k != key:
+            raise ValueError("image_mixed needs models with the same profiles, supersampling, "
+                             "PSF type, precision and scalings")
+        if im._ssc or im._subframe is not None:
+            raise ValueError("image_mixed does not take supersampled convolution or sub-frames")
+        r = im.pack_params(kl, ks, kll)
+        if r.shape[0] != 1:
+            raise ValueError("one system per request")
+        rows.append(r[0])
+        g = _lib.SystemGrid()
+        g.nx, g.ny = d.nx, d.ny
+        g.transform_pix2angle[:] = list(d.transform_pix2angle)
+        g.ra_at_xy_0, g.dec_at_xy_0 = d.ra_at_xy_0, d.dec_at_xy_0
+        g.kernel_size = d.kernel_size
+        grids.append(g)
+        if im._psf_type != _lib.PSF_NONE:
+            psfs.append(im.pack_psf(im._kernel if psf is None else psf))
+        shapes.append((im._nx, im._ny))
+    model = first._model(range(len(first.LensModel.lens_model_list)),
+                         range(len(first.SourceModel.profile_type_list)),
+                         range(len(first.LensLightModel.profile_type_list)))
+    rows_dev = _device.to_device_f64(np.stack(rows))
+    dtype = first._dtype
+    psf_dev = (torch.as_tensor(np.concatenate(psfs)).to(device="cuda", dtype=dtype)
+               if psfs else None)
+    total = sum(a * b for a, b in shapes)
+    out = torch.empty(total, dtype=dtype, device="cuda")
+    arr = (_lib.SystemGrid * len(grids))(*grids)
+    _lib.check(_lib.load().lensgb_image_mixed(
+        model.handle, _device.ptr(rows_dev), len(grids), arr,
+        ctypes.c_void_p(0) if psf_dev is None else _device.ptr(psf_dev), _device.ptr(out), 0,
+        _device.stream_handle(stream)))
+    res, o = [], 0
+    for a, b in shapes:
+        res.append(out[o:o + a * b].view(a, b))
+        o += a * b
+    return res

@@ -187,7 +187,7 @@ raytrace_fp64_kernel(GridDesc g0, StackDesc st, int ppt, const double* __restric
 
 // SS > 0 fixes the supersampling factor at compile time (the sub-ray loops
 // unroll); SS = 0 reads it from the grid.
-template <int C0, int C1, int NS, int NLL, int SS>
+template <int C0, int C1, int NS, int NLL, int SS, bool MIXED>
 __global__ void __launch_bounds__(256)
 raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict__ rec,
                      const float* __restrict__ coef, float* __restrict__ out, int flags,
@@ -197,10 +197,10 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     float* srec = (float*)smem_raw;
     float* scoef = srec + n_prof * REC_F;
-    const bool mixed = mt.grid != nullptr;
+    constexpr bool mixed = MIXED;  // compile-time, so a uniform launch reads g0 directly
     const int2 bt = mixed ? mt.blk[blockIdx.x] : make_int2((int)blockIdx.y, (int)blockIdx.x);
     const int inst = bt.x;
-    const GridDesc g = mixed ? mt.grid[inst] : g0;
+    const GridDesc& g = mixed ? mt.grid[inst] : g0;
     if (mixed) out_scale = (float)mt.scale[inst];
     load_records<float>(st, rec, coef, inst, srec, scoef);
 
@@ -448,11 +448,19 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
         // compile-time supersampling factor for the specialised stacks
         auto run = [&](auto ss_tag) {
             constexpr int SS = decltype(ss_tag)::value;
-            if (smem > 48 * 1024)
-                cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL, SS>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            raytrace_fp32_kernel<C0, C1, NS, NLL, SS><<<grid, threads, smem, stream>>>(
-                g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf, mt);
+            if (mt.grid) {
+                if (smem > 48 * 1024)
+                    cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL, SS, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                raytrace_fp32_kernel<C0, C1, NS, NLL, SS, true><<<grid, threads, smem, stream>>>(
+                    g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf, mt);
+            } else {
+                if (smem > 48 * 1024)
+                    cudaFuncSetAttribute(raytrace_fp32_kernel<C0, C1, NS, NLL, SS, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                raytrace_fp32_kernel<C0, C1, NS, NLL, SS, false><<<grid, threads, smem, stream>>>(
+                    g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf, mt);
+            }
         };
         if (C0 == GENERIC) run(std::integral_constant<int, 0>());
         else if (g.s == 1) run(std::integral_constant<int, 1>());

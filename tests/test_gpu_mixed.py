@@ -1,7 +1,9 @@
 """Systems on different pixel grids and PSF sizes in one launch sequence
 (lensgb_image_mixed through the C ABI): every image must equal that system
-computed alone by its own ImageModel (bit for bit: the kernels evaluate each
-pixel with the same arithmetic whatever else shares the launch)."""
+computed alone by its own ImageModel -- bit for bit in FP64, and in FP32 within
+1e-6 relative (the mixed launch runs its own compiled instantiation of the FP32
+ray kernel, whose instruction selection may differ by an ulp; the FP32 bar is
+1e-5)."""
 
 import numpy as np
 import pytest
@@ -48,7 +50,11 @@ def test_mixed_batch_equals_alone(cuda, precision, psf_type):
     assert len(got) == len(shapes)
     for g, a, (n, _, _) in zip(got, alone, shapes):
         assert g.shape == (n, n)
-        np.testing.assert_array_equal(g.cpu().numpy(), a)
+        g = g.cpu().numpy()
+        if precision == "fp64":
+            np.testing.assert_array_equal(g, a)
+        else:
+            np.testing.assert_allclose(g, a, rtol=1e-6, atol=1e-6 * np.abs(a).max())
 
 
 def test_mixed_rejects_different_stacks(cuda):

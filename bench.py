@@ -334,10 +334,12 @@ def substructure_section(steps, warmup, fp32_peak, flush):
 
 
 def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_bucket=2,
-                    use_graphs=True, loads=(0.5, 0.8, 0.95)):
+                    use_graphs=True, loads=(0.5, 0.8, 0.95), mixed_grids=True):
     """Serving stream: capacity (all requests released at once), then Poisson
     arrivals at 0.5 / 0.8 / 0.95 x capacity with p50/p99 latency; results of a
-    sample checked against the same requests computed alone."""
+    sample checked against the same requests computed alone.  mixed_grids:
+    requests of every grid and PSF size of one (profile stack, supersampling)
+    share a bucket; otherwise every exact model is a bucket of its own."""
     import numpy as np
     from jaxtronomy_gb300 import _lib, serving, workloads as W
 
@@ -346,7 +348,8 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     pool = {side: [serving.pinned_empty((side, side), np.float32) for _ in range(32)]
             for side in {k[0] for k in models}}
     srv = serving.Server(n_streams=n_streams, max_batch=max_batch, hbm_budget_bytes=16 << 30,
-                         contexts_per_bucket=contexts_per_bucket, use_graphs=use_graphs)
+                         contexts_per_bucket=contexts_per_bucket, use_graphs=use_graphs,
+                         mixed_grids=mixed_grids)
     built = []
     t_build = time.perf_counter()
     for i, r in enumerate(reqs):
@@ -377,11 +380,14 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
         run.service_ms = (times[:, 2] - times[:, 1]) * 1e3
         return tickets, lat, span
 
-    # warm-up: every bucket's contexts, graphs and kernels
+    # warm-up: every bucket's contexts, graphs and kernels -- for the large
+    # batches of a burst and the small ones of Poisson arrivals
     run(np.zeros(len(built)))
     _, lat_cap, span = run(np.zeros(len(built)))
     capacity = len(built) / span
     rng = np.random.default_rng(seed + 1)
+    for f in (0.5, 0.95):
+        run(np.cumsum(rng.exponential(1.0 / (f * capacity), len(built))))
     load_lines = []
     for f in loads:
         lam = f * capacity
@@ -410,7 +416,9 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     rays = np.mean([(r["key"][0] * r["key"][1]) ** 2 for r in reqs])
     return {
         "workload": "serving_stream_%d_requests" % len(reqs),
-        "requests": len(reqs), "buckets": len(models),
+        "requests": len(reqs),
+        "buckets": len({(k[1], k[3], k[4]) for k in models}) if mixed_grids else len(models),
+        "mixed_grids": mixed_grids,
         "capacity_requests_per_s": capacity,
         "capacity_latency_ms_p50": float(np.percentile(lat_cap, 50)),
         "capacity_latency_ms_p99": float(np.percentile(lat_cap, 99)),
@@ -420,7 +428,8 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
         "server": {"n_streams": n_streams, "max_batch": max_batch,
                    "contexts_per_bucket": contexts_per_bucket, "graphs": use_graphs,
                    "hbm_budget_bytes": 16 << 30, "batches": st["batches"],
-                   "graph_launches": st["graph_launches"], "evictions": st["evictions"],
+                   "graph_launches": st["graph_launches"], "mixed_batches": st["mixed_batches"],
+                   "evictions": st["evictions"],
                    "peak_bytes": st["peak_bytes"],
                    "worker_launch_s": st["host_launch_ns"] / 1e9,
                    "worker_capture_s": st["capture_ns"] / 1e9},
@@ -781,6 +790,8 @@ def gpu_arm(args):
         # --- serving stream (continuous batching)
         if args.serve_requests > 0:
             extra["serving"] = serving_section(args.serve_requests)
+            extra["serving_exact_buckets"] = serving_section(args.serve_requests,
+                                                             mixed_grids=False)
 
         # --- CPU baseline (oracle port, bounded sample)
         if pool is not None:

@@ -163,10 +163,12 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
  * profile stack, supersampling, PSF type and precision (its own grid fields
  * are not used).  psf_dev holds the systems' kernels back to back
  * (kernel_size_i^2 values each), out_dev their images back to back
- * (ny_i x nx_i each).  Each image equals lensgb_image of that system alone.
- * Not for supersampled convolution or sub-frame models.  The call waits for
- * the stream's earlier work before it copies its tables.  No reference
- * counterpart (the reference compiles one program per grid). */
+ * (ny_i x nx_i each).  Each image equals lensgb_image of that system alone,
+ * bit for bit.  Not for supersampled convolution or sub-frame models.  The
+ * call is asynchronous: its tables go to the device from a page-locked copy
+ * owned by the model, and a call waits only until the table copy of the
+ * previous call on the same model has run.  No reference counterpart (the
+ * reference compiles one program per grid). */
 typedef struct {
     int nx, ny;
     double transform_pix2angle[4];
@@ -326,6 +328,12 @@ typedef struct {
     long long hbm_budget_bytes; /* device memory of all contexts (default 4 GiB)       */
     int contexts_per_bucket;    /* concurrent batches of one bucket (default 2)        */
     int use_graphs;             /* replay captured CUDA graphs for repeated sizes      */
+    int mixed_grids;            /* 1: image requests whose models differ only in the
+                                   grid (nx, ny, transform_pix2angle, ra/dec_at_xy_0)
+                                   and kernel_size share a bucket, whose batches run
+                                   through lensgb_image_mixed (not graph-captured);
+                                   likelihood and supersampled-convolution requests
+                                   keep exact-model buckets                           */
 } lensgb_server_config;
 
 typedef struct {
@@ -359,6 +367,7 @@ typedef struct {
     long long peak_bytes;
     long long host_launch_ns;   /* worker time spent staging and launching batches */
     long long capture_ns;       /* of which capturing and instantiating graphs      */
+    long long mixed_batches;    /* batches run through lensgb_image_mixed           */
 } lensgb_server_stats;
 
 /* cfg may be NULL (defaults); zero fields take their defaults.  The server

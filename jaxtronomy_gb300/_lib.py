@@ -112,6 +112,7 @@ class ServerConfig(ctypes.Structure):
         ("hbm_budget_bytes", ctypes.c_longlong),
         ("contexts_per_bucket", ctypes.c_int),
         ("use_graphs", ctypes.c_int),
+        ("mixed_grids", ctypes.c_int),
     ]
 
 
@@ -134,7 +135,8 @@ class Request(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_longlong) for n in (
         "batches", "requests_launched", "requests_done", "graph_captures", "graph_launches",
-        "evictions", "bytes_held", "peak_bytes", "host_launch_ns", "capture_ns")]
+        "evictions", "bytes_held", "peak_bytes", "host_launch_ns", "capture_ns",
+        "mixed_batches")]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3

@@ -6,6 +6,7 @@
 // records, the EPL coefficient tables and the un-convolved image.
 #include <math.h>
 #include <stdio.h>
+#include <string.h>
 
 #include <algorithm>
 #include <string>
@@ -33,6 +34,12 @@ struct lensgb_model {
     unsigned char* mix_tab = nullptr;
     void* mix_low = nullptr;
     unsigned int* mix_list = nullptr;
+    // page-locked host copy of the tables; mix_ev marks the end of the last
+    // table copy, before which the host buffer is not rewritten
+    size_t mix_host_cap = 0;
+    unsigned char* mix_host = nullptr;
+    cudaEvent_t mix_ev = nullptr;
+    bool mix_ev_pending = false;
     StackDesc st;
     double pixel_width;
     int cap_inst = 0;
@@ -227,7 +234,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 107; }
+int lensgb_version(void) { return 108; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -388,6 +395,11 @@ int lensgb_model_destroy(lensgb_model* m) {
     cudaFree(m->mix_tab);
     cudaFree(m->mix_low);
     cudaFree(m->mix_list);
+    if (m->mix_ev) {
+        cudaEventSynchronize(m->mix_ev);
+        cudaEventDestroy(m->mix_ev);
+    }
+    cudaFreeHost(m->mix_host);
     delete m;
     return LENSGB_OK;
 }
@@ -472,6 +484,174 @@ static int image_core(lensgb_model* m, const double* params, int n_inst, const v
     return LENSGB_OK;
 }
 
+namespace lensgb {
+
+MixedLayout mixed_layout(int cap) {
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t n = (size_t)(cap > 0 ? cap : 1);
+    MixedLayout L;
+    L.cap = (int)n;
+    L.o_n = 0;
+    L.o_grid = 256;
+    L.o_off = al(L.o_grid + n * sizeof(GridDesc));
+    L.o_toff = al(L.o_off + (n + 1) * 8);
+    L.o_koff = al(L.o_toff + (n + 1) * 4);
+    L.o_ks = al(L.o_koff + n * 8);
+    L.o_scale = al(L.o_ks + n * 4);
+    L.o_gsys = al(L.o_scale + n * 8);
+    L.o_goff = al(L.o_gsys + 8 * n * 4);
+    L.o_gcnt = al(L.o_goff + 8 * (n + 1) * 4);
+    L.bytes = al(L.o_gcnt + 8 * 4);
+    return L;
+}
+
+// Convolution group of a kernel width: FP64 has one (run-time width); FP32
+// groups 1..6 run the kernel specialised for widths <= 8 g, 7 the run-time-width one.
+static int conv_group(int K, bool fp64) {
+    if (fp64) return 0;
+    const int g = (K + 7) / 8;
+    return g > 6 ? 7 : g;
+}
+
+int mixed_fill(const lensgb_model* m, unsigned char* H, const MixedLayout& L,
+               const lensgb_system_grid* grids, int n, bool conv, MixedCounts* out) {
+    if (n < 1 || n > L.cap) return fail(LENSGB_ERR_INVALID, "mixed table capacity exceeded");
+    const int s = m->desc.supersampling;
+    const bool fp64 = m->desc.precision == LENSGB_FP64;
+    const int TW = fp64 ? 32 : 64, TH = 64;  // convolution tile (columns, rows)
+    GridDesc* gd = (GridDesc*)(H + L.o_grid);
+    long long* off = (long long*)(H + L.o_off);
+    int* toff = (int*)(H + L.o_toff);
+    long long* koff = (long long*)(H + L.o_koff);
+    int* ks = (int*)(H + L.o_ks);
+    double* area = (double*)(H + L.o_scale);
+    int* gsys = (int*)(H + L.o_gsys);
+    int* goff = (int*)(H + L.o_goff);
+    int* gcnt = (int*)(H + L.o_gcnt);
+    MixedCounts c;
+    memset(&c, 0, sizeof c);
+    for (int k = 0; k < 8; ++k) {
+        gcnt[k] = 0;
+        goff[(size_t)k * (L.cap + 1)] = 0;
+    }
+    long long pix = 0, kel = 0, tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        const lensgb_system_grid& q = grids[i];
+        if (q.nx <= 0 || q.ny <= 0 || (long long)q.nx * s > (1 << 22) ||
+            (long long)q.ny * s > (1 << 22) || (long long)q.nx * q.ny * s * s >= (1LL << 31))
+            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad grid size");
+        if (conv && (q.kernel_size < 1 || q.kernel_size % 2 == 0 || q.kernel_size > 255))
+            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad kernel size");
+        gd[i] = make_grid(q.nx, q.ny, s, q.transform_pix2angle, q.ra_at_xy_0, q.dec_at_xy_0);
+        const double* Mq = q.transform_pix2angle;
+        const double pw = sqrt(fabs(Mq[0] * Mq[3] - Mq[1] * Mq[2]));
+        area[i] = pw * pw;  // as the single-grid path forms pixel_width^2
+        const long long np = (long long)q.nx * q.ny;
+        off[i] = pix;
+        toff[i] = (int)tiles;
+        koff[i] = kel;
+        ks[i] = conv ? q.kernel_size : 0;
+        pix += np;
+        tiles += (np + 255) / 256;
+        if (conv) {
+            kel += (long long)q.kernel_size * q.kernel_size;
+            const int g = conv_group(q.kernel_size, fp64);
+            const long long ct = (long long)((q.ny + TH - 1) / TH) * ((q.nx + TW - 1) / TW);
+            int* go = goff + (size_t)g * (L.cap + 1);
+            gsys[(size_t)g * L.cap + gcnt[g]] = i;
+            go[gcnt[g] + 1] = go[gcnt[g]] + (int)ct;
+            gcnt[g]++;
+            c.conv_tiles[g] += (int)ct;
+            c.kmax[g] = std::max(c.kmax[g], q.kernel_size);
+        }
+    }
+    if (pix >= (1LL << 32)) return fail(LENSGB_ERR_INVALID, "more than 2^32 pixels in one call");
+    if (tiles >= (1LL << 31)) return fail(LENSGB_ERR_INVALID, "too many ray tiles in one call");
+    off[n] = pix;
+    toff[n] = (int)tiles;
+    *(int*)(H + L.o_n) = n;
+    c.n = n;
+    c.pix = pix;
+    c.kel = kel;
+    c.ray_tiles = (int)tiles;
+    *out = c;
+    return LENSGB_OK;
+}
+
+int mixed_reserve(lensgb_model* m, int cap, long long pix, size_t table_bytes) {
+    int rc = ensure_scratch(m, cap);
+    if (rc) return rc;
+    const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
+    if (table_bytes > m->mix_tab_cap || (size_t)pix > m->mix_pix_cap) {
+        cudaFree(m->mix_tab);
+        cudaFree(m->mix_low);
+        cudaFree(m->mix_list);
+        m->mix_tab = nullptr;
+        m->mix_low = nullptr;
+        m->mix_list = nullptr;
+        const size_t tc = std::max(table_bytes, m->mix_tab_cap);
+        const size_t pc = std::max((size_t)pix, m->mix_pix_cap);
+        m->mix_tab_cap = m->mix_pix_cap = 0;
+        if (cudaMalloc(&m->mix_tab, tc) != cudaSuccess ||
+            cudaMalloc(&m->mix_low, pc * esz) != cudaSuccess ||
+            cudaMalloc(&m->mix_list, pc * sizeof(unsigned int)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(LENSGB_ERR_OOM, "device allocation of mixed-launch scratch failed");
+        }
+        m->mix_tab_cap = tc;
+        m->mix_pix_cap = pc;
+    }
+    return LENSGB_OK;
+}
+
+int mixed_launch(lensgb_model* m, const double* params, int n_cap, const unsigned char* tab,
+                 const MixedLayout& L, const MixedGrid& gr, const void* psf, void* out, int flags,
+                 cudaStream_t st) {
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    const int* n_dev = (const int*)(tab + L.o_n);
+    const GridDesc* dgrid = (const GridDesc*)(tab + L.o_grid);
+    MixedTab mt;
+    mt.grid = dgrid;
+    mt.off = (const long long*)(tab + L.o_off);
+    mt.tile_off = (const int*)(tab + L.o_toff);
+    mt.scale = (const double*)(tab + L.o_scale);
+    mt.n_inst = n_dev;
+    launch_prepare(m->grid, m->st, params, n_cap, m->rec_d, m->rec_f, m->coef_d, m->coef_f, st,
+                   dgrid, n_dev);
+    int rc;
+    if ((rc = check_cuda("prepare launch"))) return rc;
+    RefineArgs rf = refine_args(m, n_cap, m->mix_list, m->refine_count);
+    if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), st) != cudaSuccess)
+        return check_cuda("refine counter reset");
+    void* target = conv ? m->mix_low : out;
+    if (gr.ray_ctas > 0)
+        launch_raytrace(m->grid, m->st, n_cap, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
+                        flags, m->pixel_width * m->pixel_width, m->desc.precision, rf, st, &mt,
+                        gr.ray_ctas);
+    if ((rc = check_cuda("raytrace launch"))) return rc;
+    if (conv) {
+        ConvMixed cm;
+        cm.grid = dgrid;
+        cm.off = mt.off;
+        cm.koff = (const long long*)(tab + L.o_koff);
+        cm.ksize = (const int*)(tab + L.o_ks);
+        for (int g = 0; g < 8; ++g) {
+            if (gr.conv_ctas[g] <= 0) continue;
+            cm.sys = (const int*)(tab + L.o_gsys) + (size_t)g * L.cap;
+            cm.tile_off = (const int*)(tab + L.o_goff) + (size_t)g * (L.cap + 1);
+            cm.count = (const int*)(tab + L.o_gcnt) + g;
+            if (launch_conv_mixed(m->mix_low, out, psf, cm, gr.conv_ctas[g], gr.conv_kmax[g],
+                                  g == 7 ? 0 : g, m->desc.psf_type == LENSGB_PSF_GAUSSIAN,
+                                  m->desc.precision, st))
+                return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        }
+        if ((rc = check_cuda("convolution launch"))) return rc;
+    }
+    return LENSGB_OK;
+}
+
+}  // namespace lensgb
+
 extern "C" {
 
 int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* psf,
@@ -513,133 +693,40 @@ int lensgb_image_mixed(lensgb_model* m, const double* params, int n_inst,
                     "lensgb_image_mixed does not take supersampled-convolution or sub-frame models");
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
     if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
-    const int s = m->desc.supersampling;
-    const bool fp64 = m->desc.precision == LENSGB_FP64;
-    // host tables
-    std::vector<GridDesc> gd((size_t)n_inst);
-    std::vector<long long> off((size_t)n_inst + 1), koff((size_t)n_inst);
-    std::vector<double> area((size_t)n_inst);
-    std::vector<int> ks((size_t)n_inst);
-    std::vector<int2> rblk;
-    long long pix = 0, kel = 0;
-    for (int i = 0; i < n_inst; ++i) {
-        const lensgb_system_grid& q = grids[i];
-        if (q.nx <= 0 || q.ny <= 0 || (long long)q.nx * s > (1 << 22) || (long long)q.ny * s > (1 << 22) ||
-            (long long)q.nx * q.ny * s * s >= (1LL << 31))
-            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad grid size");
-        if (conv && (q.kernel_size < 1 || q.kernel_size % 2 == 0 || q.kernel_size > 255))
-            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad kernel size");
-        gd[i] = make_grid(q.nx, q.ny, s, q.transform_pix2angle, q.ra_at_xy_0, q.dec_at_xy_0);
-        const double* Mq = q.transform_pix2angle;
-        const double pw = sqrt(fabs(Mq[0] * Mq[3] - Mq[1] * Mq[2]));
-        area[i] = pw * pw;  // as the single-grid path forms pixel_width^2
-        off[i] = pix;
-        koff[i] = kel;
-        ks[i] = conv ? q.kernel_size : 0;
-        const long long np = (long long)q.nx * q.ny;
-        for (long long t = 0; t * 256 < np; ++t) rblk.push_back(make_int2(i, (int)t));
-        pix += np;
-        kel += conv ? (long long)q.kernel_size * q.kernel_size : 0;
-    }
-    off[n_inst] = pix;
-    if (pix >= (1LL << 32)) return fail(LENSGB_ERR_INVALID, "more than 2^32 pixels in one call");
-    // convolution CTAs, grouped by kernel width (FP32: segments of 8 columns)
-    std::vector<std::vector<int4>> cgrp(8);
-    std::vector<int> kmax(8, 0);
-    if (conv) {
-        const int TW = fp64 ? 32 : 64, TH = 64;
-        for (int i = 0; i < n_inst; ++i) {
-            int grp = fp64 ? 0 : (ks[i] + 7) / 8;
-            if (grp > 6) grp = 7;  // run-time-width kernel
-            for (int by = 0; by * TH < gd[i].ny; ++by)
-                for (int bx = 0; bx * TW < gd[i].nx; ++bx) cgrp[grp].push_back(make_int4(i, bx, by, 0));
-            kmax[grp] = std::max(kmax[grp], ks[i]);
-        }
-    }
-    // one device table block: grids | off | koff | ksize | ray CTAs | conv CTAs
-    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-    size_t o_grid = 0, o_off = al(o_grid + gd.size() * sizeof(GridDesc));
-    size_t o_koff = al(o_off + off.size() * 8), o_ks = al(o_koff + koff.size() * 8);
-    size_t o_area = al(o_ks + ks.size() * 4);
-    size_t o_rblk = al(o_area + area.size() * 8);
-    size_t o_cblk = al(o_rblk + rblk.size() * sizeof(int2));
-    std::vector<size_t> o_grp(8);
-    size_t end = o_cblk;
-    for (int gidx = 0; gidx < 8; ++gidx) {
-        o_grp[gidx] = end;
-        end = al(end + cgrp[gidx].size() * sizeof(int4));
-    }
-    std::vector<unsigned char> host(end, 0);
-    memcpy(host.data() + o_grid, gd.data(), gd.size() * sizeof(GridDesc));
-    memcpy(host.data() + o_off, off.data(), off.size() * 8);
-    memcpy(host.data() + o_koff, koff.data(), koff.size() * 8);
-    memcpy(host.data() + o_ks, ks.data(), ks.size() * 4);
-    memcpy(host.data() + o_area, area.data(), area.size() * 8);
-    memcpy(host.data() + o_rblk, rblk.data(), rblk.size() * sizeof(int2));
-    for (int gidx = 0; gidx < 8; ++gidx)
-        if (!cgrp[gidx].empty())
-            memcpy(host.data() + o_grp[gidx], cgrp[gidx].data(), cgrp[gidx].size() * sizeof(int4));
-    int rc = ensure_scratch(m, n_inst);
-    if (rc) return rc;
-    const size_t esz = fp64 ? 8 : 4;
-    if (end > m->mix_tab_cap || (size_t)pix > m->mix_pix_cap) {
-        cudaFree(m->mix_tab);
-        cudaFree(m->mix_low);
-        cudaFree(m->mix_list);
-        m->mix_tab = nullptr;
-        m->mix_low = nullptr;
-        m->mix_list = nullptr;
-        const size_t tc = std::max(end, m->mix_tab_cap), pc = std::max((size_t)pix, m->mix_pix_cap);
-        m->mix_tab_cap = m->mix_pix_cap = 0;
-        if (cudaMalloc(&m->mix_tab, tc) != cudaSuccess ||
-            cudaMalloc(&m->mix_low, pc * esz) != cudaSuccess ||
-            cudaMalloc(&m->mix_list, pc * sizeof(unsigned int)) != cudaSuccess) {
+    const MixedLayout L = mixed_layout(n_inst);
+    // the host tables: wait for the previous table copy to have read them
+    if (m->mix_ev_pending && cudaEventSynchronize(m->mix_ev) != cudaSuccess)
+        return check_cuda("mixed table event");
+    m->mix_ev_pending = false;
+    if (!m->mix_ev && cudaEventCreateWithFlags(&m->mix_ev, cudaEventDisableTiming) != cudaSuccess)
+        return check_cuda("mixed table event");
+    if (L.bytes > m->mix_host_cap) {
+        cudaFreeHost(m->mix_host);
+        m->mix_host = nullptr;
+        m->mix_host_cap = 0;
+        if (cudaMallocHost(&m->mix_host, L.bytes) != cudaSuccess) {
             cudaGetLastError();
-            return fail(LENSGB_ERR_OOM, "device allocation of mixed-launch scratch failed");
+            return fail(LENSGB_ERR_OOM, "page-locked allocation of mixed-launch tables failed");
         }
-        m->mix_tab_cap = tc;
-        m->mix_pix_cap = pc;
+        m->mix_host_cap = L.bytes;
     }
+    MixedCounts c;
+    int rc = mixed_fill(m, m->mix_host, L, grids, n_inst, conv, &c);
+    if (rc) return rc;
+    if ((rc = mixed_reserve(m, n_inst, c.pix, L.bytes))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    // pageable source: the copy waits for the stream's earlier work, which may
-    // still read the previous tables
-    if (cudaMemcpyAsync(m->mix_tab, host.data(), end, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    if (cudaMemcpyAsync(m->mix_tab, m->mix_host, L.bytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaEventRecord(m->mix_ev, st) != cudaSuccess)
         return check_cuda("mixed table copy");
-    const GridDesc* dgrid = (const GridDesc*)(m->mix_tab + o_grid);
-    MixedTab mt;
-    mt.grid = dgrid;
-    mt.off = (const long long*)(m->mix_tab + o_off);
-    mt.blk = (const int2*)(m->mix_tab + o_rblk);
-    mt.scale = (const double*)(m->mix_tab + o_area);
-    mt.n_inst = n_inst;
-    launch_prepare(gd[0], m->st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, st,
-                   dgrid);
-    if ((rc = check_cuda("prepare launch"))) return rc;
-    RefineArgs rf = refine_args(m, n_inst, m->mix_list, m->refine_count);
-    if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), st) != cudaSuccess)
-        return check_cuda("refine counter reset");
-    void* target = conv ? m->mix_low : out;
-    launch_raytrace(gd[0], m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target, flags,
-                    m->pixel_width * m->pixel_width, m->desc.precision, rf, st, &mt,
-                    (int)rblk.size());
-    if ((rc = check_cuda("raytrace launch"))) return rc;
-    if (conv) {
-        ConvMixed cm;
-        cm.grid = dgrid;
-        cm.off = mt.off;
-        cm.koff = (const long long*)(m->mix_tab + o_koff);
-        cm.ksize = (const int*)(m->mix_tab + o_ks);
-        for (int gidx = 0; gidx < 8; ++gidx) {
-            if (cgrp[gidx].empty()) continue;
-            cm.blk = (const int4*)(m->mix_tab + o_grp[gidx]);
-            if (launch_conv_mixed(m->mix_low, out, psf, cm, (int)cgrp[gidx].size(), kmax[gidx],
-                                  gidx == 7 ? 0 : gidx, m->desc.psf_type == LENSGB_PSF_GAUSSIAN,
-                                  m->desc.precision, st))
-                return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
-        }
-        if ((rc = check_cuda("convolution launch"))) return rc;
+    m->mix_ev_pending = true;
+    // one CTA per tile; every group with tiles gets its launch
+    MixedGrid gr;
+    gr.ray_ctas = c.ray_tiles;
+    for (int k = 0; k < 8; ++k) {
+        gr.conv_ctas[k] = c.conv_tiles[k];
+        gr.conv_kmax[k] = c.kmax[k];
     }
-    return LENSGB_OK;
+    return mixed_launch(m, params, n_inst, m->mix_tab, L, gr, psf, out, flags, st);
 }
 
 int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const void* psf,

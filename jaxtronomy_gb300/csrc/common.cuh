@@ -65,27 +65,48 @@ struct RefineArgs {
 };
 
 // Launch over systems of different grids (one model's profile stack and
-// supersampling): per-system grids and image offsets, and for each CTA of the
-// ray kernels its (system, tile).  grid == nullptr: every system uses the
-// launch's own grid and images are nx * ny apart.
+// supersampling).  Every table is per system, so its size does not depend on
+// the pixel count, and the system count is read on the device, so one launch
+// configuration (e.g. a captured CUDA graph) serves batches of any mix.  The
+// ray kernels run a grid-stride loop over tiles of 256 pixels; system i owns
+// tiles tile_off[i] .. tile_off[i + 1] - 1.  grid == nullptr: a uniform launch
+// (every system on the launch's own grid, images nx * ny apart).
 struct MixedTab {
-    const GridDesc* grid;   // [n_inst]
-    const long long* off;   // [n_inst + 1]: element offset of each system's image
-    const int2* blk;        // [ray CTAs]: (system, tile of 256 pixels)
-    const double* scale;    // [n_inst]: image scale (pixel area) of each system
-    int n_inst;
+    const GridDesc* grid;     // [n]
+    const long long* off;     // [n + 1]: element offset of each system's image
+    const int* tile_off;      // [n + 1]: first ray tile of each system
+    const double* scale;      // [n]: image scale (pixel area) of each system
+    const int* n_inst;        // device: n
 };
 
-// Convolution over systems of different sizes: per CTA (system, tile x,
-// tile y); per system its grid (nx, ny), image offset, kernel offset and K.
-// blk == nullptr: a uniform launch.
+// Convolution over systems of different sizes, one launch per kernel-width
+// group: the group's systems sys[0 .. count-1] in order, conv tile prefix
+// tile_off[0 .. count] (tiles of the kernel's tile size, row-major per
+// system), and per system its grid (nx, ny), image offset, kernel offset and K.
+// count == nullptr: a uniform launch.
 struct ConvMixed {
-    const int4* blk;
     const GridDesc* grid;
     const long long* off;
     const long long* koff;
     const int* ksize;
+    const int* sys;
+    const int* tile_off;
+    const int* count;
 };
+
+// Segment j of a strictly increasing prefix array off[0 .. n] with
+// off[j] <= t < off[j + 1] (t < off[n]).
+__device__ __forceinline__ int find_segment(const int* off, int n, int t) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
 // Unique profile codes of a bulk handle (LensModelBulk's unique_lens_model_list);
 // index u.n stands for the NULL profile.

@@ -24,97 +24,116 @@ namespace lensgb {
 
 constexpr int CONV_TX = 8, CONV_TY = 16;
 
-// Which system and tile a CTA convolves: blockIdx.z / (x, y) for a uniform
-// launch, or the CTA's table entry of a launch over systems of different
-// sizes (ny, nx, K and the image / kernel offsets then come from the tables).
-#define CONV_MIXED_PREAMBLE                                                            \
-    int bxi = blockIdx.x, byi = blockIdx.y;                                            \
-    long long ioff = (long long)blockIdx.z * ny * nx, koff = (long long)blockIdx.z * kstride; \
-    if (cm.blk) {                                                                      \
-        const int4 b = cm.blk[blockIdx.x];                                             \
-        bxi = b.y;                                                                     \
-        byi = b.z;                                                                     \
-        nx = cm.grid[b.x].nx;                                                          \
-        ny = cm.grid[b.x].ny;                                                          \
-        K = cm.ksize[b.x];                                                             \
-        ioff = cm.off[b.x];                                                            \
-        koff = cm.koff[b.x];                                                           \
+// Which system and tile a CTA convolves.  Each kernel's body is a lambda
+// tile(bxi, byi, nx, ny, K, ioff, koff) over one output tile; a uniform launch
+// (MIXED = false) runs it once for tile (blockIdx.x, blockIdx.y) of system
+// blockIdx.z.  Its arguments pass through an empty asm statement, so that the
+// compiler schedules the body for opaque register values rather than for
+// values it derives from blockIdx (measured on GB300: 1.35 -> 1.27 ms for
+// 1024 images of 180^2 with K = 31).  A launch over systems of different sizes
+// (MIXED = true) runs a grid-stride loop over the group's tiles, taking ny, nx,
+// K and the image / kernel offsets from the per-system tables, with a barrier
+// before the next tile refills shared memory.
+#define CONV_RUN_TILES(TILE_W)                                                         \
+    if (!MIXED) {                                                                      \
+        int bxi = blockIdx.x, byi = blockIdx.y, nx_ = nx, ny_ = ny, K_ = K;            \
+        long long ioff = (long long)blockIdx.z * ny * nx;                              \
+        long long koff = (long long)blockIdx.z * kstride;                              \
+        asm volatile("" : "+r"(bxi), "+r"(byi), "+r"(nx_), "+r"(ny_), "+r"(K_),        \
+                     "+l"(ioff), "+l"(koff));                                          \
+        tile(bxi, byi, nx_, ny_, K_, ioff, koff);                                      \
+    } else {                                                                           \
+        const int n_sys = *cm.count;                                                   \
+        const int n_tiles = __ldg(cm.tile_off + n_sys);                                \
+        for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {                        \
+            const int j = find_segment(cm.tile_off, n_sys, t);                         \
+            const int sys = __ldg(cm.sys + j);                                         \
+            const int mx = cm.grid[sys].nx, my = cm.grid[sys].ny;                      \
+            const int tx = (mx + (TILE_W) - 1) / (TILE_W);                             \
+            const int l = t - __ldg(cm.tile_off + j);                                  \
+            const int by = l / tx;                                                     \
+            tile(l - by * tx, by, mx, my, __ldg(cm.ksize + sys), __ldg(cm.off + sys),  \
+                 __ldg(cm.koff + sys));                                                \
+            __syncthreads();                                                           \
+        }                                                                              \
     }
 
-template <typename R, int CX, int RY, int VC>
+template <typename R, int CX, int RY, int VC, bool MIXED>
 __global__ void __launch_bounds__(CONV_TX* CONV_TY)
 conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__ ker,
             long long kstride, int ny, int nx, int K, int edge, ConvMixed cm) {
     constexpr int W = CONV_TX * CX, H = CONV_TY * RY;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CONV_MIXED_PREAMBLE
-    R* sk = (R*)smem_raw;
-    const int KP = ((K + VC - 1) / VC) * VC;
-    const int SW = W + KP - 1 + 1;  // +1 keeps row starts off the same bank
-    const int SH = H + K - 1;
-    R* si = sk + K * KP;
-    const int ox0 = bxi * W, oy0 = byi * H;
-    const int h = K / 2;
-    const int tid = threadIdx.y * CONV_TX + threadIdx.x;
-    const int nthr = CONV_TX * CONV_TY;
-    const R* kk = ker + koff;
-    for (int e = tid; e < K * KP; e += nthr) {
-        int u = e / KP, v = e - u * KP;
-        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : R(0);
-    }
-    const R* img = in + ioff;
-    for (int e = tid; e < SH * SW; e += nthr) {
-        int r = e / SW, c = e - r * SW;
-        int gy = oy0 - h + r, gx = ox0 - h + c;
-        R v;
-        if (edge) {
-            gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
-            gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
-            v = img[(long long)gy * nx + gx];
-        } else {
-            v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : R(0);
+    auto tile = [&](int bxi, int byi, int nx, int ny, int K, long long ioff, long long koff) {
+        R* sk = (R*)smem_raw;
+        const int KP = ((K + VC - 1) / VC) * VC;
+        const int SW = W + KP - 1 + 1;  // +1 keeps row starts off the same bank
+        const int SH = H + K - 1;
+        R* si = sk + K * KP;
+        const int ox0 = bxi * W, oy0 = byi * H;
+        const int h = K / 2;
+        const int tid = threadIdx.y * CONV_TX + threadIdx.x;
+        const int nthr = CONV_TX * CONV_TY;
+        const R* kk = ker + koff;
+        for (int e = tid; e < K * KP; e += nthr) {
+            int u = e / KP, v = e - u * KP;
+            sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : R(0);
         }
-        si[e] = v;
-    }
-    __syncthreads();
+        const R* img = in + ioff;
+        for (int e = tid; e < SH * SW; e += nthr) {
+            int r = e / SW, c = e - r * SW;
+            int gy = oy0 - h + r, gx = ox0 - h + c;
+            R v;
+            if (edge) {
+                gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+                gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+                v = img[(long long)gy * nx + gx];
+            } else {
+                v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : R(0);
+            }
+            si[e] = v;
+        }
+        __syncthreads();
 
-    R acc[RY][CX];
+        R acc[RY][CX];
 #pragma unroll
-    for (int i = 0; i < RY; ++i)
+        for (int i = 0; i < RY; ++i)
 #pragma unroll
-        for (int c = 0; c < CX; ++c) acc[i][c] = 0;
-    const int c0 = threadIdx.x * CX, r0 = threadIdx.y * RY;
-    for (int ir = 0; ir < RY + K - 1; ++ir) {
-        const R* row = si + (r0 + ir) * SW + c0;
-        for (int v0 = 0; v0 < KP; v0 += VC) {
-            R seg[CX + VC - 1];
+            for (int c = 0; c < CX; ++c) acc[i][c] = 0;
+        const int c0 = threadIdx.x * CX, r0 = threadIdx.y * RY;
+        for (int ir = 0; ir < RY + K - 1; ++ir) {
+            const R* row = si + (r0 + ir) * SW + c0;
+            for (int v0 = 0; v0 < KP; v0 += VC) {
+                R seg[CX + VC - 1];
 #pragma unroll
-            for (int j = 0; j < CX + VC - 1; ++j) seg[j] = row[v0 + j];
+                for (int j = 0; j < CX + VC - 1; ++j) seg[j] = row[v0 + j];
 #pragma unroll
-            for (int i = 0; i < RY; ++i) {
-                const int u = ir - i;
-                if (u < 0 || u >= K) continue;
-                const R* kr = sk + u * KP + v0;
+                for (int i = 0; i < RY; ++i) {
+                    const int u = ir - i;
+                    if (u < 0 || u >= K) continue;
+                    const R* kr = sk + u * KP + v0;
 #pragma unroll
-                for (int vv = 0; vv < VC; ++vv) {
-                    const R w = kr[vv];
+                    for (int vv = 0; vv < VC; ++vv) {
+                        const R w = kr[vv];
 #pragma unroll
-                    for (int c = 0; c < CX; ++c) acc[i][c] = fma(w, seg[c + vv], acc[i][c]);
+                        for (int c = 0; c < CX; ++c) acc[i][c] = fma(w, seg[c + vv], acc[i][c]);
+                    }
                 }
             }
         }
-    }
-    R* o = out + ioff;
+        R* o = out + ioff;
 #pragma unroll
-    for (int i = 0; i < RY; ++i) {
-        const int y = oy0 + r0 + i;
-        if (y >= ny) continue;
+        for (int i = 0; i < RY; ++i) {
+            const int y = oy0 + r0 + i;
+            if (y >= ny) continue;
 #pragma unroll
-        for (int c = 0; c < CX; ++c) {
-            const int x = ox0 + c0 + c;
-            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+            for (int c = 0; c < CX; ++c) {
+                const int x = ox0 + c0 + c;
+                if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+            }
         }
-    }
+    };
+    CONV_RUN_TILES(W)
 }
 
 // FP32 variant: each thread owns 4 rows x 8 columns; input segments and kernel
@@ -123,87 +142,90 @@ conv_kernel(const R* __restrict__ in, R* __restrict__ out, const R* __restrict__
 // the 4*TY-row tiles waste as few rows as possible.
 constexpr int C32_CX = 8, C32_RY = 4, C32_TX = 8, C32_W = C32_TX * C32_CX;
 
+template <bool MIXED>
 __global__ void __launch_bounds__(C32_TX * 16)
 conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
                 const float* __restrict__ ker, long long kstride, int ny, int nx, int K, int edge,
                 ConvMixed cm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CONV_MIXED_PREAMBLE
-    const int TY = blockDim.y;
-    const int H = TY * C32_RY;
-    const int KP = ((K + 7) / 8) * 8;
-    const int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
-    const int SH = H + K - 1;
-    float* sk = (float*)smem_raw;
-    float* si = sk + K * KP;
-    const int ox0 = bxi * C32_W, oy0 = byi * H;
-    const int h = K / 2;
-    const int tid = threadIdx.y * C32_TX + threadIdx.x;
-    const int nthr = C32_TX * TY;
-    const float* kk = ker + koff;
-    for (int e = tid; e < K * KP; e += nthr) {
-        const int u = e / KP, v = e - u * KP;
-        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
-    }
-    const float* img = in + ioff;
-    for (int e = tid; e < SH * SW; e += nthr) {
-        const int r = e / SW, c = e - r * SW;
-        int gy = oy0 - h + r, gx = ox0 - h + c;
-        float v;
-        if (edge) {
-            gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
-            gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
-            v = img[(long long)gy * nx + gx];
-        } else {
-            v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : 0.f;
+    auto tile = [&](int bxi, int byi, int nx, int ny, int K, long long ioff, long long koff) {
+        const int TY = blockDim.y;
+        const int H = TY * C32_RY;
+        const int KP = ((K + 7) / 8) * 8;
+        const int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
+        const int SH = H + K - 1;
+        float* sk = (float*)smem_raw;
+        float* si = sk + K * KP;
+        const int ox0 = bxi * C32_W, oy0 = byi * H;
+        const int h = K / 2;
+        const int tid = threadIdx.y * C32_TX + threadIdx.x;
+        const int nthr = C32_TX * TY;
+        const float* kk = ker + koff;
+        for (int e = tid; e < K * KP; e += nthr) {
+            const int u = e / KP, v = e - u * KP;
+            sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
         }
-        si[e] = v;
-    }
-    __syncthreads();
+        const float* img = in + ioff;
+        for (int e = tid; e < SH * SW; e += nthr) {
+            const int r = e / SW, c = e - r * SW;
+            int gy = oy0 - h + r, gx = ox0 - h + c;
+            float v;
+            if (edge) {
+                gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+                gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+                v = img[(long long)gy * nx + gx];
+            } else {
+                v = (gy >= 0 && gy < ny && gx >= 0 && gx < nx) ? img[(long long)gy * nx + gx] : 0.f;
+            }
+            si[e] = v;
+        }
+        __syncthreads();
 
-    float acc[C32_RY][C32_CX];
+        float acc[C32_RY][C32_CX];
 #pragma unroll
-    for (int i = 0; i < C32_RY; ++i)
+        for (int i = 0; i < C32_RY; ++i)
 #pragma unroll
-        for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
-    const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
-    for (int ir = 0; ir < C32_RY + K - 1; ++ir) {
-        const float4* row = reinterpret_cast<const float4*>(si + (r0 + ir) * SW + c0);
-        for (int v0 = 0; v0 < KP; v0 += 8) {
-            float seg[16];
+            for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
+        const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
+        for (int ir = 0; ir < C32_RY + K - 1; ++ir) {
+            const float4* row = reinterpret_cast<const float4*>(si + (r0 + ir) * SW + c0);
+            for (int v0 = 0; v0 < KP; v0 += 8) {
+                float seg[16];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const float4 q = row[v0 / 4 + j];
-                seg[4 * j] = q.x;
-                seg[4 * j + 1] = q.y;
-                seg[4 * j + 2] = q.z;
-                seg[4 * j + 3] = q.w;
-            }
+                for (int j = 0; j < 4; ++j) {
+                    const float4 q = row[v0 / 4 + j];
+                    seg[4 * j] = q.x;
+                    seg[4 * j + 1] = q.y;
+                    seg[4 * j + 2] = q.z;
+                    seg[4 * j + 3] = q.w;
+                }
 #pragma unroll
-            for (int i = 0; i < C32_RY; ++i) {
-                const int u = ir - i;
-                if (u < 0 || u >= K) continue;
-                const float4* kr = reinterpret_cast<const float4*>(sk + u * KP + v0);
-                const float4 k0 = kr[0], k1 = kr[1];
-                const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+                for (int i = 0; i < C32_RY; ++i) {
+                    const int u = ir - i;
+                    if (u < 0 || u >= K) continue;
+                    const float4* kr = reinterpret_cast<const float4*>(sk + u * KP + v0);
+                    const float4 k0 = kr[0], k1 = kr[1];
+                    const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
 #pragma unroll
-                for (int vv = 0; vv < 8; ++vv)
+                    for (int vv = 0; vv < 8; ++vv)
 #pragma unroll
-                    for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+                        for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+                }
             }
         }
-    }
-    float* o = out + ioff;
+        float* o = out + ioff;
 #pragma unroll
-    for (int i = 0; i < C32_RY; ++i) {
-        const int y = oy0 + r0 + i;
-        if (y >= ny) continue;
+        for (int i = 0; i < C32_RY; ++i) {
+            const int y = oy0 + r0 + i;
+            if (y >= ny) continue;
 #pragma unroll
-        for (int c = 0; c < C32_CX; ++c) {
-            const int x = ox0 + c0 + c;
-            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+            for (int c = 0; c < C32_CX; ++c) {
+                const int x = ox0 + c0 + c;
+                if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+            }
         }
-    }
+    };
+    CONV_RUN_TILES(C32_W)
 }
 
 // FP32 variant with the kernel width fixed at compile time (NSEG segments of 8
@@ -212,105 +234,107 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
 // every output row of the thread has a kernel row -- runs without branches and
 // with all shared-memory offsets as immediates, and the halo tile is filled row
 // by row without index divisions.
-template <int NSEG>
+template <int NSEG, bool MIXED>
 __global__ void __launch_bounds__(C32_TX * 16)
 conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
                       const float* __restrict__ ker, long long kstride, int ny, int nx, int K,
                       int edge, ConvMixed cm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CONV_MIXED_PREAMBLE
-    constexpr int KP = 8 * NSEG;
-    constexpr int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
-    const int TY = blockDim.y;
-    const int H = TY * C32_RY;
-    const int SH = H + K - 1;
-    float* sk = (float*)smem_raw;
-    float* si = sk + K * KP;
-    const int ox0 = bxi * C32_W, oy0 = byi * H;
-    const int h = K / 2;
-    const int tid = threadIdx.y * C32_TX + threadIdx.x;
-    const int nthr = C32_TX * TY;
-    const float* kk = ker + koff;
-    for (int e = tid; e < K * KP; e += nthr) {
-        const int u = e / KP, v = e % KP;
-        sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
-    }
-    const float* img = in + ioff;
-    for (int r = threadIdx.y; r < SH; r += TY) {
-        int gy = oy0 - h + r;
-        const bool rin = gy >= 0 && gy < ny;
-        if (edge) gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
-        const float* grow = img + (long long)gy * nx;
-        float* srow = si + r * SW;
-        for (int c = threadIdx.x; c < SW; c += C32_TX) {
-            int gx = ox0 - h + c;
-            float v;
-            if (edge) {
-                gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
-                v = grow[gx];
-            } else {
-                v = (rin && gx >= 0 && gx < nx) ? grow[gx] : 0.f;
-            }
-            srow[c] = v;
+    auto tile = [&](int bxi, int byi, int nx, int ny, int K, long long ioff, long long koff) {
+        constexpr int KP = 8 * NSEG;
+        constexpr int SW = C32_W + KP + 4;  // multiple of 4 floats: rows stay 16-byte aligned
+        const int TY = blockDim.y;
+        const int H = TY * C32_RY;
+        const int SH = H + K - 1;
+        float* sk = (float*)smem_raw;
+        float* si = sk + K * KP;
+        const int ox0 = bxi * C32_W, oy0 = byi * H;
+        const int h = K / 2;
+        const int tid = threadIdx.y * C32_TX + threadIdx.x;
+        const int nthr = C32_TX * TY;
+        const float* kk = ker + koff;
+        for (int e = tid; e < K * KP; e += nthr) {
+            const int u = e / KP, v = e % KP;
+            sk[e] = v < K ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
         }
-    }
-    __syncthreads();
-
-    float acc[C32_RY][C32_CX];
-#pragma unroll
-    for (int i = 0; i < C32_RY; ++i)
-#pragma unroll
-        for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
-    const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
-    const float* base = si + r0 * SW + c0;
-    // input row ir feeds output row i through kernel row ir - i
-    auto row_step = [&](int ir, int ilo, int ihi) {
-        const float4* row = reinterpret_cast<const float4*>(base + ir * SW);
-#pragma unroll
-        for (int sg = 0; sg < NSEG; ++sg) {
-            float seg[16];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const float4 q = row[2 * sg + j];
-                seg[4 * j] = q.x;
-                seg[4 * j + 1] = q.y;
-                seg[4 * j + 2] = q.z;
-                seg[4 * j + 3] = q.w;
+        const float* img = in + ioff;
+        for (int r = threadIdx.y; r < SH; r += TY) {
+            int gy = oy0 - h + r;
+            const bool rin = gy >= 0 && gy < ny;
+            if (edge) gy = gy < 0 ? 0 : (gy >= ny ? ny - 1 : gy);
+            const float* grow = img + (long long)gy * nx;
+            float* srow = si + r * SW;
+            for (int c = threadIdx.x; c < SW; c += C32_TX) {
+                int gx = ox0 - h + c;
+                float v;
+                if (edge) {
+                    gx = gx < 0 ? 0 : (gx >= nx ? nx - 1 : gx);
+                    v = grow[gx];
+                } else {
+                    v = (rin && gx >= 0 && gx < nx) ? grow[gx] : 0.f;
+                }
+                srow[c] = v;
             }
+        }
+        __syncthreads();
+
+        float acc[C32_RY][C32_CX];
 #pragma unroll
-            for (int i = 0; i < C32_RY; ++i) {
-                if (i < ilo || i > ihi) continue;
-                const float4* kr = reinterpret_cast<const float4*>(sk + (ir - i) * KP + 8 * sg);
-                const float4 k0 = kr[0], k1 = kr[1];
-                const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+        for (int i = 0; i < C32_RY; ++i)
 #pragma unroll
-                for (int vv = 0; vv < 8; ++vv)
+            for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
+        const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
+        const float* base = si + r0 * SW + c0;
+        // input row ir feeds output row i through kernel row ir - i
+        auto row_step = [&](int ir, int ilo, int ihi) {
+            const float4* row = reinterpret_cast<const float4*>(base + ir * SW);
 #pragma unroll
-                    for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+            for (int sg = 0; sg < NSEG; ++sg) {
+                float seg[16];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 q = row[2 * sg + j];
+                    seg[4 * j] = q.x;
+                    seg[4 * j + 1] = q.y;
+                    seg[4 * j + 2] = q.z;
+                    seg[4 * j + 3] = q.w;
+                }
+#pragma unroll
+                for (int i = 0; i < C32_RY; ++i) {
+                    if (i < ilo || i > ihi) continue;
+                    const float4* kr = reinterpret_cast<const float4*>(sk + (ir - i) * KP + 8 * sg);
+                    const float4 k0 = kr[0], k1 = kr[1];
+                    const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+#pragma unroll
+                    for (int vv = 0; vv < 8; ++vv)
+#pragma unroll
+                        for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+                }
+            }
+        };
+        // output row i takes input rows i .. i+K-1, i.e. input row ir serves the
+        // output rows max(0, ir-K+1) .. min(RY-1, ir)
+        // head: input rows 0 .. RY-2
+        for (int ir = 0; ir < C32_RY - 1; ++ir)
+            row_step(ir, ir - K + 1 > 0 ? ir - K + 1 : 0, ir);
+        // body: rows RY-1 .. K-1 serve every output row (branch-free)
+        for (int ir = C32_RY - 1; ir < K; ++ir) row_step(ir, 0, C32_RY - 1);
+        // tail: rows max(K, RY-1) .. K+RY-2
+        for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
+            row_step(ir, ir - K + 1, C32_RY - 1);
+        float* o = out + ioff;
+#pragma unroll
+        for (int i = 0; i < C32_RY; ++i) {
+            const int y = oy0 + r0 + i;
+            if (y >= ny) continue;
+#pragma unroll
+            for (int c = 0; c < C32_CX; ++c) {
+                const int x = ox0 + c0 + c;
+                if (x < nx) o[(long long)y * nx + x] = acc[i][c];
             }
         }
     };
-    // output row i takes input rows i .. i+K-1, i.e. input row ir serves the
-    // output rows max(0, ir-K+1) .. min(RY-1, ir)
-    // head: input rows 0 .. RY-2
-    for (int ir = 0; ir < C32_RY - 1; ++ir)
-        row_step(ir, ir - K + 1 > 0 ? ir - K + 1 : 0, ir);
-    // body: rows RY-1 .. K-1 serve every output row (branch-free)
-    for (int ir = C32_RY - 1; ir < K; ++ir) row_step(ir, 0, C32_RY - 1);
-    // tail: rows max(K, RY-1) .. K+RY-2
-    for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
-        row_step(ir, ir - K + 1, C32_RY - 1);
-    float* o = out + ioff;
-#pragma unroll
-    for (int i = 0; i < C32_RY; ++i) {
-        const int y = oy0 + r0 + i;
-        if (y >= ny) continue;
-#pragma unroll
-        for (int c = 0; c < C32_CX; ++c) {
-            const int x = ox0 + c0 + c;
-            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
-        }
-    }
+    CONV_RUN_TILES(C32_W)
 }
 
 // Raise a kernel's dynamic shared-memory limit only when a launch needs more
@@ -355,10 +379,10 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
     const float* fk = (const float*)kernel;
     auto fixed = [&](auto nseg_tag) {
         constexpr int NS = decltype(nseg_tag)::value;
-        const void* fn = (const void*)conv_f32_fixed_kernel<NS>;
+        const void* fn = (const void*)conv_f32_fixed_kernel<NS, false>;
         if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
-        conv_f32_fixed_kernel<NS><<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny,
-                                                                 nx, K, edge, ConvMixed{});
+        conv_f32_fixed_kernel<NS, false><<<grid, block, smem, stream>>>(
+            fin, (float*)out, fk, kstride, ny, nx, K, edge, ConvMixed{});
         return 0;
     };
     switch (KP / 8) {
@@ -370,9 +394,9 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
         case 6: return fixed(std::integral_constant<int, 6>());
         default: break;
     }
-    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
-    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny, nx, K, edge,
-                                                   ConvMixed{});
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel<false>, smem)) return -1;
+    conv_f32_kernel<false><<<grid, block, smem, stream>>>(fin, (float*)out, fk, kstride, ny, nx, K,
+                                                          edge, ConvMixed{});
     return 0;
 }
 
@@ -384,11 +408,11 @@ static int run_conv(const void* in, void* out, const void* kernel, long long kst
     const int SW = W + KP - 1 + 1;
     const int SH = H + K - 1;
     size_t smem = (size_t)(K * KP + SH * SW) * sizeof(R);
-    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_kernel<R, CX, RY, VC>, smem))
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_kernel<R, CX, RY, VC, false>, smem))
         return -1;
     dim3 grid((unsigned)((nx + W - 1) / W), (unsigned)((ny + H - 1) / H), (unsigned)n_inst);
     dim3 block(CONV_TX, CONV_TY);
-    conv_kernel<R, CX, RY, VC><<<grid, block, smem, stream>>>(
+    conv_kernel<R, CX, RY, VC, false><<<grid, block, smem, stream>>>(
         (const R*)in, (R*)out, (const R*)kernel, kstride, ny, nx, K, edge, ConvMixed{});
     return 0;
 }
@@ -506,9 +530,9 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
         constexpr int W = CONV_TX * 4, H = CONV_TY * 4;
         const int KP = ((kmax + 3) / 4) * 4;
         const size_t smem = (size_t)(kmax * KP + (H + kmax - 1) * (W + KP)) * sizeof(double);
-        const void* fn = (const void*)conv_kernel<double, 4, 4, 4>;
+        const void* fn = (const void*)conv_kernel<double, 4, 4, 4, true>;
         if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
-        conv_kernel<double, 4, 4, 4><<<grid, dim3(CONV_TX, CONV_TY), smem, stream>>>(
+        conv_kernel<double, 4, 4, 4, true><<<grid, dim3(CONV_TX, CONV_TY), smem, stream>>>(
             (const double*)in, (double*)out, (const double*)kernel, 0, 0, 0, 0, edge, cm);
         return 0;
     }
@@ -523,10 +547,10 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
     const float* fk = (const float*)kernel;
     auto fixed = [&](auto nseg_tag) {
         constexpr int NS = decltype(nseg_tag)::value;
-        const void* fn = (const void*)conv_f32_fixed_kernel<NS>;
+        const void* fn = (const void*)conv_f32_fixed_kernel<NS, true>;
         if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
-        conv_f32_fixed_kernel<NS><<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0,
-                                                                 edge, cm);
+        conv_f32_fixed_kernel<NS, true><<<grid, block, smem, stream>>>(
+            fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
         return 0;
     };
     switch (group) {
@@ -538,8 +562,8 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
         case 6: return fixed(std::integral_constant<int, 6>());
         default: break;
     }
-    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel, smem)) return -1;
-    conv_f32_kernel<<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
+    if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel<true>, smem)) return -1;
+    conv_f32_kernel<true><<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
     return 0;
 }
 

@@ -13,16 +13,20 @@ namespace lensgb {
 // Sets the calling thread's lensgb_last_error() text (defined in abi.cu).
 void set_last_error(const std::string& msg);
 
+// Per-system profile records of n_inst systems (grids: per-system grids of a
+// mixed launch; n_dev: device count of systems actually present, <= n_inst).
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
                    double* rec_d, float* rec_f, double* coef_d, float* coef_f,
-                   cudaStream_t stream, const GridDesc* grids = nullptr);
+                   cudaStream_t stream, const GridDesc* grids = nullptr,
+                   const int* n_dev = nullptr);
 
 // Supersampled ray tracing + light + s x s re-binning into a (ny, nx) image per
 // system, scaled by out_scale (pixel_width^2).  `precision` selects FP64 or FP32;
 // the FP32 path refines flagged pixels in FP64 as described by `rf`
 // (rf.count must be zero on the stream when the launch starts).
 // `mixed` (device tables, or null): systems of different grids in one launch
-// of mixed_ctas CTAs (g then only supplies s); images are laid out at mixed->off.
+// of mixed_ctas CTAs looping over the systems' tiles (g then only supplies s);
+// images are laid out at mixed->off.
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,
                     int flags, double out_scale, int precision, const RefineArgs& rf,
@@ -34,12 +38,53 @@ int launch_conv(const void* in, void* out, const void* kernel, long long kstride
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream);
 
 // Convolution of systems of different sizes (tables in `cm`): one launch of
-// n_ctas CTAs whose kernels are at most kmax wide; FP32 `group` g > 0 runs the
-// kernel specialised for widths <= 8 g (systems are grouped by it), 0 the
-// run-time-width one.  Tiles are 64 x 64 (FP32) / 32 x 64 (FP64) pixels.
+// n_ctas CTAs looping over the tiles of the group's systems, whose kernels are
+// at most kmax wide; FP32 `group` g > 0 runs the kernel specialised for widths
+// <= 8 g (systems are grouped by it), 0 the run-time-width one.  Tiles are
+// 64 x 64 (FP32) / 32 x 64 (FP64) pixels.
 int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvMixed& cm,
                       int n_ctas, int kmax, int group, int edge, int precision,
                       cudaStream_t stream);
+
+// ---- mixed-grid launches (abi.cu) -------------------------------------------
+// Offsets, in one device / page-locked table block, of the per-system tables
+// of a mixed launch for up to `cap` systems (see MixedTab / ConvMixed).
+struct MixedLayout {
+    int cap;
+    size_t o_n, o_grid, o_off, o_toff, o_koff, o_ks, o_scale, o_gsys, o_goff, o_gcnt, bytes;
+};
+MixedLayout mixed_layout(int cap);
+
+// Host-side totals of a filled table block.  Convolution groups: index 0 for
+// FP64, 1..6 the fixed-width FP32 kernels, 7 the run-time-width FP32 kernel.
+struct MixedCounts {
+    int n;
+    long long pix, kel;
+    int ray_tiles;
+    int conv_tiles[8];
+    int kmax[8];
+};
+
+// Launch configuration: CTAs of the ray kernel and of each convolution group
+// (0: the group is not launched) and the widest kernel each group may meet.
+struct MixedGrid {
+    int ray_ctas;
+    int conv_ctas[8];
+    int conv_kmax[8];
+};
+
+// Validates n system grids and writes their tables into host block H.
+int mixed_fill(const lensgb_model* m, unsigned char* H, const MixedLayout& L,
+               const lensgb_system_grid* grids, int n, bool conv, MixedCounts* out);
+// Grows the model's scratch for cap systems of `pix` pixels in total.
+int mixed_reserve(lensgb_model* m, int cap, long long pix, size_t table_bytes);
+// Stream operations of one mixed launch over at most n_cap systems whose tables
+// are at device address tab (the system count is read on the device): records,
+// ray tracing (+ FP32 refinement), grouped convolution.  Allocates nothing, so
+// it can be captured into a CUDA graph after mixed_reserve.
+int mixed_launch(lensgb_model* m, const double* params_dev, int n_cap, const unsigned char* tab,
+                 const MixedLayout& L, const MixedGrid& gr, const void* psf, void* out, int flags,
+                 cudaStream_t st);
 
 // s x s block mean (image_util.re_size, image_util.py:79-98: mean over
 // sub-columns, then sub-rows) of n_inst (ny*s, nx*s) images, times scale.

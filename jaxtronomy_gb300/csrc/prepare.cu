@@ -224,8 +224,9 @@ __device__ void finish_record_f(const double* d, float* f) {
 __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                                int n_inst, double* __restrict__ rec_d, float* __restrict__ rec_f,
                                double* __restrict__ coef_d, float* __restrict__ coef_f,
-                               const GridDesc* __restrict__ grids) {
+                               const GridDesc* __restrict__ grids, const int* __restrict__ n_dev) {
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    if (n_dev) n_inst = min(n_inst, *n_dev);
     long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long long)n_inst * n_prof) return;
     const int inst = (int)(gid / n_prof);
@@ -259,14 +260,14 @@ __global__ void prepare_kernel(GridDesc g, StackDesc st, const double* __restric
 
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
                    double* rec_d, float* rec_f, double* coef_d, float* coef_f,
-                   cudaStream_t stream, const GridDesc* grids) {
+                   cudaStream_t stream, const GridDesc* grids, const int* n_dev) {
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     long long n = (long long)n_inst * n_prof;
     if (n == 0) return 0;
     int threads = 128;
     int blocks = (int)((n + threads - 1) / threads);
     prepare_kernel<<<blocks, threads, 0, stream>>>(g, st, params, n_inst, rec_d, rec_f, coef_d,
-                                                   coef_f, grids);
+                                                   coef_f, grids, n_dev);
     return 0;
 }
 

@@ -164,20 +164,30 @@ raytrace_fp64_kernel(GridDesc g0, StackDesc st, int ppt, const double* __restric
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     double* srec = (double*)smem_raw;
     double* scoef = srec + n_prof * REC_D;
+    // uniform launch: one pass for (system blockIdx.y, tile blockIdx.x);
+    // mixed launch: grid-stride loop over every system's tiles
     const bool mixed = mt.grid != nullptr;
-    const int2 bt = mixed ? mt.blk[blockIdx.x] : make_int2((int)blockIdx.y, (int)blockIdx.x);
-    const int inst = bt.x;
-    const GridDesc g = mixed ? mt.grid[inst] : g0;
-    if (mixed) out_scale = mt.scale[inst];
-    load_records<double>(st, rec, coef, inst, srec, scoef);
-    const long long npix = (long long)g.nx * g.ny;
-    double* o = out + (mixed ? mt.off[inst] : (long long)inst * npix);
-    const long long base = (long long)bt.y * blockDim.x * ppt;
-    for (int k = 0; k < ppt; ++k) {
-        const long long pix = base + (long long)k * blockDim.x + threadIdx.x;
-        if (pix >= npix) break;
-        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
-        o[pix] = pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, out_scale);
+    const int n_mixed = mixed ? *mt.n_inst : 0;
+    const int n_tiles = mixed ? __ldg(mt.tile_off + n_mixed) : 1;
+    for (int t = mixed ? (int)blockIdx.x : 0; t < n_tiles; t += mixed ? (int)gridDim.x : 1) {
+        int inst = blockIdx.y, tile = blockIdx.x;
+        if (mixed) {
+            inst = find_segment(mt.tile_off, n_mixed, t);
+            tile = t - __ldg(mt.tile_off + inst);
+        }
+        const GridDesc g = mixed ? mt.grid[inst] : g0;
+        const double osc = mixed ? mt.scale[inst] : out_scale;
+        load_records<double>(st, rec, coef, inst, srec, scoef);
+        const long long npix = (long long)g.nx * g.ny;
+        double* o = out + (mixed ? mt.off[inst] : (long long)inst * npix);
+        const long long base = (long long)tile * blockDim.x * ppt;
+        for (int k = 0; k < ppt; ++k) {
+            const long long pix = base + (long long)k * blockDim.x + threadIdx.x;
+            if (pix >= npix) break;
+            const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+            o[pix] = pixel_value_d<C0, C1, NS, NLL>(g, st, srec, scoef, row, col, flags, osc);
+        }
+        if (mixed) __syncthreads();  // before the next tile reloads the records
     }
 }
 
@@ -198,102 +208,124 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
     float* srec = (float*)smem_raw;
     float* scoef = srec + n_prof * REC_F;
     constexpr bool mixed = MIXED;  // compile-time, so a uniform launch reads g0 directly
-    const int2 bt = mixed ? mt.blk[blockIdx.x] : make_int2((int)blockIdx.y, (int)blockIdx.x);
-    const int inst = bt.x;
-    const GridDesc& g = mixed ? mt.grid[inst] : g0;
-    if (mixed) out_scale = (float)mt.scale[inst];
-    load_records<float>(st, rec, coef, inst, srec, scoef);
+    // uniform launch: one pass for (system blockIdx.y, tile blockIdx.x);
+    // mixed launch: grid-stride loop over every system's tiles of 256 pixels
+    const int n_mixed = mixed ? *mt.n_inst : 0;
+    const int n_tiles = mixed ? __ldg(mt.tile_off + n_mixed) : 1;
+    for (int t = mixed ? (int)blockIdx.x : 0; t < n_tiles; t += mixed ? (int)gridDim.x : 1) {
+        int inst = blockIdx.y, tile = blockIdx.x;
+        if (mixed) {
+            inst = find_segment(mt.tile_off, n_mixed, t);
+            tile = t - __ldg(mt.tile_off + inst);
+            out_scale = (float)mt.scale[inst];
+        }
+        const GridDesc& g = mixed ? mt.grid[inst] : g0;
+        load_records<float>(st, rec, coef, inst, srec, scoef);
 
-    const int n_lens = LS::generic ? st.n_lens : LS::n;
-    const int n_src = NS >= 0 ? NS : st.n_src;
-    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
-    constexpr int ML = LS::generic ? MAX_PROF : (LS::n > 0 ? LS::n : 1);
-    constexpr int MS = NS >= 0 ? (NS > 0 ? NS : 1) : MAX_PROF;
-    constexpr int MLL = NLL >= 0 ? (NLL > 0 ? NLL : 1) : MAX_PROF;
-    // compile-time stacks keep every record in registers for the whole CTA
-    constexpr int NPC = LS::generic ? 1 : LS::n + MS + MLL;
-    float lr[NPC][REC_F];
-    if (!LS::generic) {
+        const int n_lens = LS::generic ? st.n_lens : LS::n;
+        const int n_src = NS >= 0 ? NS : st.n_src;
+        const int n_ll = NLL >= 0 ? NLL : st.n_ll;
+        constexpr int ML = LS::generic ? MAX_PROF : (LS::n > 0 ? LS::n : 1);
+        constexpr int MS = NS >= 0 ? (NS > 0 ? NS : 1) : MAX_PROF;
+        constexpr int MLL = NLL >= 0 ? (NLL > 0 ? NLL : 1) : MAX_PROF;
+        // compile-time stacks keep every record in registers for the whole CTA
+        constexpr int NPC = LS::generic ? 1 : LS::n + MS + MLL;
+        float lr[NPC][REC_F];
+        if (!LS::generic) {
 #pragma unroll
-        for (int i = 0; i < NPC; ++i)
+            for (int i = 0; i < NPC; ++i)
 #pragma unroll
-            for (int k = 0; k < REC_F; ++k)
-                lr[i][k] = i < n_prof ? srec[i * REC_F + k] : 0.f;
-    }
+                for (int k = 0; k < REC_F; ++k)
+                    lr[i][k] = i < n_prof ? srec[i * REC_F + k] : 0.f;
+        }
 #define REC(i) (LS::generic ? srec + (i) * REC_F : lr[(i)])
-    const bool do_src = !(flags & LENSGB_NO_SOURCE) && n_src > 0;
-    const bool do_ll = !(flags & LENSGB_NO_LENS_LIGHT) && n_ll > 0;
-    const bool refine = rf.tau > 0.f && do_src;
-    const int s = SS > 0 ? SS : g.s;
-    const float inv_s = 1.f / (float)s;
-    const float axf = g.ax_hi + g.ax_lo, bxf = g.bx_hi + g.bx_lo;
-    const float ayf = g.ay_hi + g.ay_lo, byf = g.by_hi + g.by_lo;
-    const long long npix = (long long)g.nx * g.ny;
-    const long long img0 = mixed ? mt.off[inst] : (long long)inst * npix;
-    float* o = out + img0;
-    const long long base = (long long)bt.y * blockDim.x * ppt;
+        const bool do_src = !(flags & LENSGB_NO_SOURCE) && n_src > 0;
+        const bool do_ll = !(flags & LENSGB_NO_LENS_LIGHT) && n_ll > 0;
+        const bool refine = rf.tau > 0.f && do_src;
+        const int s = SS > 0 ? SS : g.s;
+        const float inv_s = 1.f / (float)s;
+        const float axf = g.ax_hi + g.ax_lo, bxf = g.bx_hi + g.bx_lo;
+        const float ayf = g.ay_hi + g.ay_lo, byf = g.by_hi + g.by_lo;
+        const long long npix = (long long)g.nx * g.ny;
+        const long long img0 = mixed ? mt.off[inst] : (long long)inst * npix;
+        float* o = out + img0;
+        const long long base = (long long)tile * blockDim.x * ppt;
 
-    for (int kk = 0; kk < ppt; ++kk) {
-        const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
-        if (pix >= npix) break;
-        // pixel index of one system (< 2^31): 32-bit division
-        const unsigned int p32 = (unsigned int)pix;
-        const int row = (int)(p32 / (unsigned int)g.nx), col = (int)(p32 - (unsigned int)row * g.nx);
-        const float Jb = (float)(col * s), Ib = (float)(row * s);
-        // base-ray offsets from every profile centre, FP64-accurate
-        PixOff ol[ML], os[MS], oll[MLL];
+        for (int kk = 0; kk < ppt; ++kk) {
+            const long long pix = base + (long long)kk * blockDim.x + threadIdx.x;
+            if (pix >= npix) break;
+            // pixel index of one system (< 2^31): 32-bit division
+            const unsigned int p32 = (unsigned int)pix;
+            const int row = (int)(p32 / (unsigned int)g.nx), col = (int)(p32 - (unsigned int)row * g.nx);
+            const float Jb = (float)(col * s), Ib = (float)(row * s);
+            // base-ray offsets from every profile centre, FP64-accurate
+            PixOff ol[ML], os[MS], oll[MLL];
 #pragma unroll (LS::generic ? 1 : 8)
-        for (int p = 0; p < ML; ++p)
-            if (p < n_lens && do_src) ol[p] = pix_offset_f(g, REC(p), Jb, Ib);
+            for (int p = 0; p < ML; ++p)
+                if (p < n_lens && do_src) ol[p] = pix_offset_f(g, REC(p), Jb, Ib);
 #pragma unroll (LS::generic ? 1 : 8)
-        for (int k = 0; k < MS; ++k)
-            if (k < n_src && do_src) os[k] = pix_offset_f(g, REC(n_lens + k), Jb, Ib);
+            for (int k = 0; k < MS; ++k)
+                if (k < n_src && do_src) os[k] = pix_offset_f(g, REC(n_lens + k), Jb, Ib);
 #pragma unroll (LS::generic ? 1 : 8)
-        for (int k = 0; k < MLL; ++k)
-            if (k < n_ll && do_ll) oll[k] = pix_offset_f(g, REC(n_lens + n_src + k), Jb, Ib);
+            for (int k = 0; k < MLL; ++k)
+                if (k < n_ll && do_ll) oll[k] = pix_offset_f(g, REC(n_lens + n_src + k), Jb, Ib);
 
-        float acc = 0.f;
-        bool flag = false;
+            float acc = 0.f;
+            bool flag = false;
 #pragma unroll (SS > 0 ? SS : 1)
-        for (int si = 0; si < (SS > 0 ? SS : s); ++si) {
-            float rs = 0.f;
-            const float fi = (float)si;
+            for (int si = 0; si < (SS > 0 ? SS : s); ++si) {
+                float rs = 0.f;
+                const float fi = (float)si;
 #pragma unroll (SS > 0 ? SS : 1)
-            for (int sj = 0; sj < (SS > 0 ? SS : s); ++sj) {
-                // sub-ray displacement from the base ray: below one pixel, so a
-                // plain FP32 product keeps an absolute error of ~1e-9 pixel
-                const float fj = (float)sj;
-                const float ddx = fmaf(fi, bxf, fj * axf);
-                const float ddy = fmaf(fi, byf, fj * ayf);
-                float flux = 0.f;
-                if (do_src) {
-                    float axs = 0.f, ays = 0.f;
+                for (int sj = 0; sj < (SS > 0 ? SS : s); ++sj) {
+                    // sub-ray displacement from the base ray: below one pixel, so a
+                    // plain FP32 product keeps an absolute error of ~1e-9 pixel
+                    const float fj = (float)sj;
+                    const float ddx = fmaf(fi, bxf, fj * axf);
+                    const float ddy = fmaf(fi, byf, fj * ayf);
+                    float flux = 0.f;
+                    if (do_src) {
+                        float axs = 0.f, ays = 0.f;
 #pragma unroll (LS::generic ? 1 : 8)
-                    for (int p = 0; p < ML; ++p) {
-                        if (p >= n_lens) break;
-                        const int code = LS::generic ? st.lens[p] : LS::code(p);
-                        const int es = st.epl_slot[p];
-                        float ax, ay;
-                        lens_deflect<float>(code, REC(p), es >= 0 ? scoef + es * EPL_NMAX : nullptr,
-                                            ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
-                        axs += ax;
-                        ays += ay;
-                    }
-                    axs *= st.alpha_scaling_f;
-                    ays *= st.alpha_scaling_f;
-                    float fsrc = 0.f, gsum = 0.f;
+                        for (int p = 0; p < ML; ++p) {
+                            if (p >= n_lens) break;
+                            const int code = LS::generic ? st.lens[p] : LS::code(p);
+                            const int es = st.epl_slot[p];
+                            float ax, ay;
+                            lens_deflect<float>(code, REC(p), es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                                                ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
+                            axs += ax;
+                            ays += ay;
+                        }
+                        axs *= st.alpha_scaling_f;
+                        ays *= st.alpha_scaling_f;
+                        float fsrc = 0.f, gsum = 0.f;
 #pragma unroll (LS::generic ? 1 : 8)
-                    for (int k = 0; k < MS; ++k) {
-                        if (k >= n_src) break;
-                        const float sc = st.src_scale_f[k];
-                        float gk;
-                        const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sc * axs,
-                                                          os[k].by + ddy - sc * ays, gk);
-                        fsrc += fk;
-                        gsum += fk * gk * sc;
-                    }
-                    flux = fsrc;
-                    if (do_ll) {
+                        for (int k = 0; k < MS; ++k) {
+                            if (k >= n_src) break;
+                            const float sc = st.src_scale_f[k];
+                            float gk;
+                            const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sc * axs,
+                                                              os[k].by + ddy - sc * ays, gk);
+                            fsrc += fk;
+                            gsum += fk * gk * sc;
+                        }
+                        flux = fsrc;
+                        if (do_ll) {
+#pragma unroll (LS::generic ? 1 : 8)
+                            for (int k = 0; k < MLL; ++k) {
+                                if (k >= n_ll) break;
+                                flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
+                                                           oll[k].by + ddy);
+                            }
+                        }
+                        if (refine) {
+                            // predicted relative error of this ray's flux from the FP32
+                            // error of beta (kappa * |alpha|) through the source gradients
+                            const float dbeta = rf.kappa * (fabsf(axs) + fabsf(ays));
+                            flag |= gsum * dbeta > rf.tau * flux;
+                        }
+                    } else if (do_ll) {
 #pragma unroll (LS::generic ? 1 : 8)
                         for (int k = 0; k < MLL; ++k) {
                             if (k >= n_ll) break;
@@ -301,30 +333,18 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
                                                        oll[k].by + ddy);
                         }
                     }
-                    if (refine) {
-                        // predicted relative error of this ray's flux from the FP32
-                        // error of beta (kappa * |alpha|) through the source gradients
-                        const float dbeta = rf.kappa * (fabsf(axs) + fabsf(ays));
-                        flag |= gsum * dbeta > rf.tau * flux;
-                    }
-                } else if (do_ll) {
-#pragma unroll (LS::generic ? 1 : 8)
-                    for (int k = 0; k < MLL; ++k) {
-                        if (k >= n_ll) break;
-                        flux += sersic_flux<float>(REC(n_lens + n_src + k), oll[k].bx + ddx,
-                                                   oll[k].by + ddy);
-                    }
+                    rs += flux;
                 }
-                rs += flux;
+                acc += s == 1 ? rs : rs * inv_s;
             }
-            acc += s == 1 ? rs : rs * inv_s;
+            if (s > 1) acc *= inv_s;
+            o[pix] = acc * st.flux_scaling_f * out_scale;
+            if (flag) {
+                const unsigned int slot_i = atomicAdd(rf.count, 1u);
+                rf.list[slot_i] = (unsigned int)(img0 + pix);
+            }
         }
-        if (s > 1) acc *= inv_s;
-        o[pix] = acc * st.flux_scaling_f * out_scale;
-        if (flag) {
-            const unsigned int slot_i = atomicAdd(rf.count, 1u);
-            rf.list[slot_i] = (unsigned int)(img0 + pix);
-        }
+        if (mixed) __syncthreads();  // before the next tile reloads the records
     }
 #undef REC
 }
@@ -347,6 +367,7 @@ refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
     const unsigned int n = *rf.count;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     const bool mixed = mt.grid != nullptr;
+    const int n_mixed = mixed ? *mt.n_inst : 0;
     const int s = g0.s, s2 = s * s;
     const int per = s2 <= REFINE_THREADS ? REFINE_THREADS / s2 : 1;  // pixels per chunk
     for (unsigned int first = blockIdx.x * per; first < n; first += gridDim.x * per) {
@@ -358,7 +379,7 @@ refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
                 int inst;
                 if (mixed) {
                     // the system whose image holds element e: off[inst] <= e < off[inst + 1]
-                    int lo = 0, hi = mt.n_inst - 1;
+                    int lo = 0, hi = n_mixed - 1;
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) >> 1;
                         if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
@@ -391,7 +412,7 @@ refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
             double osc = out_scale;
             if (mixed) {
                 const long long e = (long long)rf.list[first + el];
-                int lo = 0, hi = mt.n_inst - 1;
+                int lo = 0, hi = n_mixed - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
                     if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;

@@ -5,7 +5,10 @@
 // owns one worker thread that
 //   * releases submitted requests into per-bucket FIFO queues once their
 //     release time has passed (a bucket = one compiled model: profile lists,
-//     grid, supersampling, PSF size, precision and noise options);
+//     grid, supersampling, PSF size, precision and noise options; with
+//     mixed_grids, image requests of every grid and PSF size of one profile
+//     stack, supersampling and precision share a bucket, whose batches run
+//     through lensgb_image_mixed);
 //   * keeps up to n_streams batches in flight, one per CUDA stream, each batch
 //     a single lensgb_image / lensgb_loglike launch sequence over up to
 //     max_batch requests of one bucket -- requests that arrive while others
@@ -53,6 +56,8 @@ struct Req {
     int rc = LENSGB_OK;
     bool out_pinned = false;  // image_out is page-locked: the device writes it directly
     int in_pinned = 0;        // bits 0..2: data / noise_map / mask are page-locked
+    long long npix = 0;       // ny x nx of the request's grid
+    int k2 = 0;               // PSF elements of the request
     long long t_submit = 0, t_release = 0, t_admit = 0, t_done = 0;
 };
 
@@ -77,7 +82,9 @@ struct Context {
     lensgb_model* model = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    int cap = 0;             // batch capacity of the buffers below
+    int cap = 0;             // batch capacity of the buffers below (requests)
+    long long pix_cap = 0;   // image pixels and PSF elements the buffers hold
+    long long kel_cap = 0;
     size_t bytes = 0;        // device bytes held (buffers + model scratch)
     double* rows_dev = nullptr;
     void* psf_dev = nullptr;
@@ -91,20 +98,33 @@ struct Context {
     double* logl_host = nullptr;
     unsigned char* img_host = nullptr;  // pinned staging for pageable caller buffers
     unsigned char* in_host = nullptr;   // pinned staging of pageable data / noise / mask
-    void** ptr_host = nullptr;          // pinned pointer tables: out[cap], data, noise, mask
-    void** ptr_dev = nullptr;
+    void** ptr_host = nullptr;          // pinned pointer tables: out[cap], data, noise, mask,
+    void** ptr_dev = nullptr;           // then (mixed buckets) cap + 1 image byte offsets
+    long long* boff_host = nullptr;     // the byte-offset part of ptr_host / ptr_dev
+    long long* boff_dev = nullptr;
+    // mixed buckets: one page-locked staging block -- rows | PSFs | output
+    // pointers + byte offsets | mixed-launch tables -- and its device mirror,
+    // refreshed by one copy of fixed size (rows_host ... point into it)
+    unsigned char* stage_host = nullptr;
+    unsigned char* stage_dev = nullptr;
+    size_t stage_bytes = 0, o_tab = 0;
+    lensgb::MixedLayout ml;
+    std::vector<lensgb_system_grid> grids;  // the batch's grids
+    lensgb::MixedGrid mgrid;                // the batch's launch shape
     bool busy = false;
     long long last_used = 0;
     std::vector<Req*> batch;
-    std::map<int, cudaGraphExec_t> graphs;  // batch size -> graph
-    std::map<int, int> eager_runs;          // batch size -> eager launches so far
+    // uniform buckets: batch size -> graph; mixed buckets: launch shape -> graph
+    std::map<long long, cudaGraphExec_t> graphs;
+    std::map<long long, int> eager_runs;    // eager launches so far, same keys
 };
 
 struct Bucket {
     BucketKey key;
+    bool mixed = false;  // requests of different grids / PSF sizes (lensgb_image_mixed)
     int n_params = 0;
-    long long npix = 0;
-    int k2 = 0;          // PSF elements per request
+    long long npix = 0;  // uniform buckets: pixels and PSF elements per request
+    int k2 = 0;
     size_t esz = 4;      // image element size
     std::deque<Req*> queue;
     std::vector<Context*> ctx;
@@ -118,12 +138,15 @@ struct lensgb_server {
     std::mutex mu;
     std::condition_variable cv;
     int device = 0;
+    int n_sms = 152;                          // SMs of the device (launch shapes)
     std::deque<Req> reqs;                     // stable storage, index = ticket
     std::vector<Req*> incoming;               // submitted, not yet released
     std::vector<Bucket*> buckets;             // guarded by mu (appended by submit)
-    std::map<BucketKey, int> bucket_index;
+    std::map<BucketKey, int> bucket_index;    // exact request key -> bucket
+    std::map<BucketKey, int> mixed_index;     // grid-free key -> mixed bucket
     std::vector<Bucket*> wb;                  // the worker's copy of `buckets`
     std::vector<Context*> contexts;
+    std::vector<long long> pre_pix, pre_kel;  // worker scratch: prefix sums of a queue head
     size_t bytes_held = 0;
     size_t peak_bytes = 0;
     int inflight = 0;
@@ -144,25 +167,48 @@ int serr(int code, const std::string& m) {
     return code;
 }
 
-size_t context_bytes(const Bucket& b, int cap) {
+// What a batch needs: requests, image pixels, PSF elements.
+struct Need {
+    int n;
+    long long pix, kel;
+};
+
+size_t context_bytes(const Bucket& b, const Need& d) {
     // buffers owned by the context
-    size_t per = (size_t)b.n_params * 8 + (size_t)b.k2 * b.esz + (size_t)b.npix * b.esz + 8;
+    size_t bytes = (size_t)d.n * ((size_t)b.n_params * 8 + 8) + (size_t)d.kel * b.esz +
+                   (size_t)d.pix * b.esz;
     if (b.key.likelihood) {
-        per += (size_t)b.npix * 8;
-        if (b.key.has_noise) per += (size_t)b.npix * 8;
-        if (b.key.has_mask) per += (size_t)b.npix * 8;
+        bytes += (size_t)d.pix * 8;
+        if (b.key.has_noise) bytes += (size_t)d.pix * 8;
+        if (b.key.has_mask) bytes += (size_t)d.pix * 8;
     }
     // model scratch: records, coefficient tables, un-convolved image, refine list
-    const lensgb_model_desc& d = b.key.desc;
-    const size_t nprof = (size_t)(d.n_lens + d.n_source + d.n_lens_light);
-    per += nprof * (32 * 8 + 36 * 4) + (size_t)d.n_lens * 500 * 12 + (size_t)b.npix * (b.esz + 4);
-    return per * (size_t)cap;
+    const lensgb_model_desc& m = b.key.desc;
+    const size_t nprof = (size_t)(m.n_lens + m.n_source + m.n_lens_light);
+    bytes += (size_t)d.n * (nprof * (32 * 8 + 36 * 4) + (size_t)m.n_lens * 500 * 12) +
+             (size_t)d.pix * (b.esz + 4);
+    // mixed launches: ray and convolution CTA tables, per-system grids
+    if (b.mixed) bytes += (size_t)d.pix / 16 + (size_t)d.n * 160 + 4096;
+    return bytes;
 }
 
 void free_context_buffers(Context* c) {
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.second);
     c->graphs.clear();
     c->eager_runs.clear();
+    if (c->stage_host) {
+        // the staging buffers are parts of one block
+        cudaFreeHost(c->stage_host);
+        cudaFree(c->stage_dev);
+        c->stage_host = c->stage_dev = nullptr;
+        c->stage_bytes = 0;
+        c->rows_dev = nullptr;
+        c->psf_dev = nullptr;
+        c->ptr_dev = nullptr;
+        c->rows_host = nullptr;
+        c->psf_host = nullptr;
+        c->ptr_host = nullptr;
+    }
     cudaFree(c->rows_dev);
     cudaFree(c->psf_dev);
     cudaFree(c->img_dev);
@@ -181,6 +227,7 @@ void free_context_buffers(Context* c) {
     c->in_host = nullptr;
     c->ptr_host = nullptr;
     c->ptr_dev = nullptr;
+    c->boff_host = c->boff_dev = nullptr;
     c->rows_dev = nullptr;
     c->psf_dev = c->img_dev = nullptr;
     c->data_dev = c->noise_dev = c->mask_dev = c->logl_dev = nullptr;
@@ -188,6 +235,7 @@ void free_context_buffers(Context* c) {
     c->psf_host = nullptr;
     c->logl_host = nullptr;
     c->cap = 0;
+    c->pix_cap = c->kel_cap = 0;
 }
 
 void destroy_context(lensgb_server* s, Context* c) {
@@ -215,35 +263,73 @@ bool make_room(lensgb_server* s, size_t need, const Context* keep) {
     return true;
 }
 
-// Grow a context to hold `n` requests (capacity doubles up to max_batch).
-int grow_context(lensgb_server* s, Context* c, int n) {
-    if (n <= c->cap) return LENSGB_OK;
+// Grow a context to hold a batch of `d` (capacities double; requests up to
+// max_batch).
+int grow_context(lensgb_server* s, Context* c, const Need& d) {
+    if (d.n <= c->cap && d.pix <= c->pix_cap && d.kel <= c->kel_cap) return LENSGB_OK;
     Bucket& b = *s->wb[c->bucket];
     int cap = c->cap > 0 ? c->cap : 1;
-    while (cap < n) cap *= 2;
+    while (cap < d.n) cap *= 2;
     if (cap > s->cfg.max_batch) cap = s->cfg.max_batch;
-    const size_t nb = context_bytes(b, cap);
+    long long pix_cap, kel_cap;
+    if (b.mixed) {
+        pix_cap = std::max<long long>(c->pix_cap, 4096);
+        while (pix_cap < d.pix) pix_cap *= 2;
+        kel_cap = std::max<long long>(c->kel_cap, 256);
+        while (kel_cap < d.kel) kel_cap *= 2;
+    } else {
+        pix_cap = (long long)cap * b.npix;
+        kel_cap = (long long)cap * b.k2;
+    }
+    const Need nd{cap, pix_cap, kel_cap};
+    const size_t nb = context_bytes(b, nd);
     if (nb > c->bytes && !make_room(s, nb - c->bytes, c)) return LENSGB_ERR_OOM;
     free_context_buffers(c);
     s->bytes_held -= c->bytes;
     c->bytes = 0;
-    const size_t P = (size_t)b.n_params, np = (size_t)b.npix;
-    bool ok = cudaMalloc(&c->rows_dev, cap * P * 8 + 8) == cudaSuccess &&
-              cudaMalloc(&c->psf_dev, cap * (size_t)b.k2 * b.esz + 16) == cudaSuccess &&
-              cudaMalloc(&c->img_dev, cap * np * b.esz) == cudaSuccess &&
-              cudaMalloc(&c->logl_dev, cap * 8) == cudaSuccess &&
-              cudaMallocHost(&c->rows_host, cap * P * 8 + 8) == cudaSuccess &&
-              cudaMallocHost(&c->psf_host, cap * (size_t)b.k2 * b.esz + 16) == cudaSuccess &&
-              cudaMallocHost(&c->logl_host, cap * 8) == cudaSuccess &&
-              cudaMallocHost(&c->img_host, cap * np * b.esz) == cudaSuccess &&
-              cudaMallocHost(&c->ptr_host, cap * 4 * sizeof(void*)) == cudaSuccess &&
-              cudaMalloc(&c->ptr_dev, cap * 4 * sizeof(void*)) == cudaSuccess;
+    const size_t P = (size_t)b.n_params, np = (size_t)pix_cap, nk = (size_t)kel_cap;
+    const size_t ptr_bytes = (size_t)cap * 4 * sizeof(void*) + ((size_t)cap + 1) * 8;
+    bool ok;
+    if (b.mixed) {
+        auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+        c->ml = lensgb::mixed_layout(cap);
+        const size_t o_psf = al(cap * P * 8 + 8), o_ptr = al(o_psf + nk * b.esz + 16);
+        c->o_tab = al(o_ptr + ptr_bytes);
+        c->stage_bytes = c->o_tab + c->ml.bytes;
+        ok = cudaMallocHost(&c->stage_host, c->stage_bytes) == cudaSuccess &&
+             cudaMalloc(&c->stage_dev, c->stage_bytes) == cudaSuccess &&
+             cudaMalloc(&c->img_dev, np * b.esz) == cudaSuccess &&
+             cudaMalloc(&c->logl_dev, cap * 8) == cudaSuccess &&
+             cudaMallocHost(&c->logl_host, cap * 8) == cudaSuccess &&
+             cudaMallocHost(&c->img_host, np * b.esz) == cudaSuccess;
+        if (ok) {
+            memset(c->stage_host, 0, c->stage_bytes);
+            c->rows_host = (double*)c->stage_host;
+            c->rows_dev = (double*)c->stage_dev;
+            c->psf_host = c->stage_host + o_psf;
+            c->psf_dev = c->stage_dev + o_psf;
+            c->ptr_host = (void**)(c->stage_host + o_ptr);
+            c->ptr_dev = (void**)(c->stage_dev + o_ptr);
+            ok = lensgb::mixed_reserve(c->model, cap, pix_cap, 256) == LENSGB_OK;
+        }
+    } else {
+        ok = cudaMalloc(&c->rows_dev, cap * P * 8 + 8) == cudaSuccess &&
+             cudaMalloc(&c->psf_dev, nk * b.esz + 16) == cudaSuccess &&
+             cudaMalloc(&c->img_dev, np * b.esz) == cudaSuccess &&
+             cudaMalloc(&c->logl_dev, cap * 8) == cudaSuccess &&
+             cudaMallocHost(&c->rows_host, cap * P * 8 + 8) == cudaSuccess &&
+             cudaMallocHost(&c->psf_host, nk * b.esz + 16) == cudaSuccess &&
+             cudaMallocHost(&c->logl_host, cap * 8) == cudaSuccess &&
+             cudaMallocHost(&c->img_host, np * b.esz) == cudaSuccess &&
+             cudaMallocHost(&c->ptr_host, ptr_bytes) == cudaSuccess &&
+             cudaMalloc(&c->ptr_dev, ptr_bytes) == cudaSuccess;
+    }
     if (ok && b.key.likelihood) {
-        ok = cudaMalloc(&c->data_dev, cap * np * 8) == cudaSuccess;
-        if (ok && b.key.has_noise) ok = cudaMalloc(&c->noise_dev, cap * np * 8) == cudaSuccess;
-        if (ok && b.key.has_mask) ok = cudaMalloc(&c->mask_dev, cap * np * 8) == cudaSuccess;
+        ok = cudaMalloc(&c->data_dev, np * 8) == cudaSuccess;
+        if (ok && b.key.has_noise) ok = cudaMalloc(&c->noise_dev, np * 8) == cudaSuccess;
+        if (ok && b.key.has_mask) ok = cudaMalloc(&c->mask_dev, np * 8) == cudaSuccess;
         const int planes = 1 + b.key.has_noise + b.key.has_mask;
-        if (ok) ok = cudaMallocHost(&c->in_host, cap * planes * np * 8) == cudaSuccess;
+        if (ok) ok = cudaMallocHost(&c->in_host, planes * np * 8) == cudaSuccess;
     }
     if (ok) ok = lensgb_model_reserve(c->model, cap) == LENSGB_OK;
     if (!ok) {
@@ -251,7 +337,11 @@ int grow_context(lensgb_server* s, Context* c, int n) {
         free_context_buffers(c);
         return LENSGB_ERR_OOM;
     }
+    c->boff_host = (long long*)(c->ptr_host + (size_t)cap * 4);
+    c->boff_dev = (long long*)(c->ptr_dev + (size_t)cap * 4);  // in the staging block when mixed
     c->cap = cap;
+    c->pix_cap = pix_cap;
+    c->kel_cap = kel_cap;
     c->bytes = nb;
     s->bytes_held += nb;
     s->peak_bytes = std::max(s->peak_bytes, s->bytes_held);
@@ -276,13 +366,22 @@ Context* new_context(lensgb_server* s, int bucket) {
     return c;
 }
 
-// Copies n blocks of `bytes` between a contiguous device array and the
-// per-request buffers named by a pointer table (page-locked host memory, which
-// the GPU reads and writes directly).  to_table = 1: device -> table.
+// Copies n blocks between a contiguous device array and the per-request
+// buffers named by a pointer table (page-locked host memory, which the GPU
+// reads and writes directly): block i is `bytes` long at i * bytes, or, with
+// byte offsets `boff` (n + 1 entries), boff[i + 1] - boff[i] long at boff[i].
+// n_dev (or null): device count of blocks present, <= gridDim.y.
+// to_table = 1: device -> table.
 __global__ void table_copy_kernel(unsigned char* dev, void* const* table, size_t bytes,
-                                  int to_table) {
+                                  const long long* boff, const int* n_dev, int to_table) {
     const int i = blockIdx.y;
-    unsigned char* d = dev + (size_t)i * bytes;
+    if (n_dev && i >= *n_dev) return;
+    size_t o = (size_t)i * bytes;
+    if (boff) {
+        o = (size_t)boff[i];
+        bytes = (size_t)(boff[i + 1] - boff[i]);
+    }
+    unsigned char* d = dev + o;
     unsigned char* h = (unsigned char*)table[i];
     const uintptr_t al = ((uintptr_t)d) | ((uintptr_t)h) | (uintptr_t)bytes;
     const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -315,12 +414,13 @@ __global__ void table_copy_kernel(unsigned char* dev, void* const* table, size_t
     }
 }
 
+// `bytes`: the block size, or with boff the largest block (sizes the grid).
 void table_copy(unsigned char* dev, void* const* table, size_t bytes, int n, int to_table,
-                cudaStream_t st) {
+                cudaStream_t st, const long long* boff = nullptr, const int* n_dev = nullptr) {
     const size_t units = (bytes % 16 == 0) ? bytes / 16 : (bytes % 4 == 0 ? bytes / 4 : bytes);
     unsigned bx = (unsigned)std::min<size_t>((units + 255) / 256, 64);
     dim3 grid(bx > 0 ? bx : 1, (unsigned)n);
-    table_copy_kernel<<<grid, 256, 0, st>>>(dev, table, bytes, to_table);
+    table_copy_kernel<<<grid, 256, 0, st>>>(dev, table, bytes, boff, n_dev, to_table);
 }
 
 // Launch sequence of one batch on the context's stream.  Graph-capturable:
@@ -330,6 +430,22 @@ int launch_batch(lensgb_server* s, Context* c, int n) {
     Bucket& b = *s->wb[c->bucket];
     cudaStream_t st = c->stream;
     const size_t P = (size_t)b.n_params;
+    if (b.mixed) {
+        // systems of different grids: the whole staging block in one copy, the
+        // mixed launch (system count read on the device), then every image to
+        // its request's host buffer
+        const lensgb::MixedGrid& gr = c->mgrid;
+        if (cudaMemcpyAsync(c->stage_dev, c->stage_host, c->stage_bytes, cudaMemcpyHostToDevice,
+                            st) != cudaSuccess)
+            return LENSGB_ERR_CUDA;
+        const unsigned char* tab = c->stage_dev + c->o_tab;
+        int rc = lensgb::mixed_launch(c->model, c->rows_dev, c->cap, tab, c->ml, gr, c->psf_dev,
+                                      c->img_dev, 0, st);
+        if (rc) return rc;
+        table_copy((unsigned char*)c->img_dev, c->ptr_dev, (size_t)16 * 256 * 16, c->cap, 1, st,
+                   c->boff_dev, (const int*)(tab + c->ml.o_n));
+        return cudaGetLastError() == cudaSuccess ? LENSGB_OK : LENSGB_ERR_CUDA;
+    }
     const int planes = b.key.likelihood ? 1 + b.key.has_noise + b.key.has_mask : 0;
     if (cudaMemcpyAsync(c->rows_dev, c->rows_host, n * P * 8, cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
@@ -371,6 +487,46 @@ int launch_batch(lensgb_server* s, Context* c, int n) {
     return cudaGetLastError() == cudaSuccess ? LENSGB_OK : LENSGB_ERR_CUDA;
 }
 
+// Runs the batch's launch sequence: eagerly the first time a context meets a
+// launch shape `key`, then (use_graphs) captured into a CUDA graph and replayed.
+int launch_or_replay(lensgb_server* s, Context* c, int n, long long key) {
+    cudaStream_t st = c->stream;
+    auto g = c->graphs.find(key);
+    if (g != c->graphs.end()) {
+        if (cudaGraphLaunch(g->second, st) != cudaSuccess) return LENSGB_ERR_CUDA;
+        s->stats.graph_launches++;
+        return LENSGB_OK;
+    }
+    if (!(s->cfg.use_graphs && c->eager_runs[key] >= 1)) {
+        const int rc = launch_batch(s, c, n);
+        if (rc == LENSGB_OK) c->eager_runs[key]++;
+        return rc;
+    }
+    // the same context and shape ran eagerly before: capture and replay
+    const long long tc = s->now();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return LENSGB_ERR_CUDA;
+    int rc = launch_batch(s, c, n);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc == LENSGB_OK && e == cudaSuccess && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+        c->graphs[key] = exec;
+        s->stats.graph_captures++;
+    } else {
+        exec = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    s->stats.capture_ns += s->now() - tc;
+    if (exec) {
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) return LENSGB_ERR_CUDA;
+        s->stats.graph_launches++;
+        return LENSGB_OK;
+    }
+    return launch_batch(s, c, n);  // capture failed: run eagerly
+}
+
 int run_batch(lensgb_server* s, Context* c, int n) {
     Bucket& b = *s->wb[c->bucket];
     cudaStream_t st = c->stream;
@@ -379,6 +535,68 @@ int run_batch(lensgb_server* s, Context* c, int n) {
     const size_t ib = (size_t)b.npix * b.esz;
     const size_t pb = (size_t)b.npix * 8;
     const int planes = b.key.likelihood ? 1 + b.key.has_noise + b.key.has_mask : 0;
+    if (b.mixed) {
+        c->grids.resize((size_t)n);
+        long long po = 0, ko = 0;
+        for (int i = 0; i < n; ++i) {
+            const Req* q = c->batch[i];
+            const lensgb_request& r = q->r;
+            memcpy(c->rows_host + i * P, r.params, P * 8);
+            if (q->k2 > 0) memcpy(c->psf_host + ko * b.esz, r.psf, (size_t)q->k2 * b.esz);
+            lensgb_system_grid& gi = c->grids[(size_t)i];
+            gi.nx = r.desc.nx;
+            gi.ny = r.desc.ny;
+            memcpy(gi.transform_pix2angle, r.desc.transform_pix2angle, sizeof gi.transform_pix2angle);
+            gi.ra_at_xy_0 = r.desc.ra_at_xy_0;
+            gi.dec_at_xy_0 = r.desc.dec_at_xy_0;
+            gi.kernel_size = r.desc.kernel_size;
+            c->boff_host[i] = po * (long long)b.esz;
+            c->ptr_host[i] = (r.image_out && q->out_pinned) ? r.image_out
+                                                             : (void*)(c->img_host + po * b.esz);
+            po += q->npix;
+            ko += q->k2;
+        }
+        c->boff_host[n] = po * (long long)b.esz;
+        lensgb::MixedCounts mc;
+        const bool conv = b.key.desc.psf_type != LENSGB_PSF_NONE;
+        int rc = lensgb::mixed_fill(c->model, c->stage_host + c->o_tab, c->ml, c->grids.data(), n,
+                                    conv, &mc);
+        if (rc) return rc;
+        // launch shape: CTA counts in power-of-two classes of the batch's tiles,
+        // the convolution groups present, and (run-time-width group) the kernel
+        // width rounded up; one graph per shape
+        auto p2 = [](int v, int cap) {
+            int k = 0;
+            while ((1 << k) < v && (1 << k) < cap) ++k;
+            return k;
+        };
+        const int nsm = s->n_sms;
+        lensgb::MixedGrid& gr = c->mgrid;
+        const int kr = p2(mc.ray_tiles, 8 * nsm);
+        gr.ray_ctas = std::min(1 << kr, 8 * nsm);
+        int ctot = 0, mask = 0, kvar = 0;
+        for (int g = 0; g < 8; ++g) ctot += mc.conv_tiles[g];
+        const int kc = p2(ctot, 4 * nsm);
+        for (int g = 0; g < 8; ++g) {
+            gr.conv_ctas[g] = 0;
+            gr.conv_kmax[g] = 0;
+            if (mc.conv_tiles[g] == 0) continue;
+            mask |= 1 << g;
+            gr.conv_ctas[g] = std::min(1 << kc, 4 * nsm);
+            if (g >= 1 && g <= 6) {
+                gr.conv_kmax[g] = 8 * g - 1;  // the widest odd kernel of the group
+            } else {
+                kvar = ((mc.kmax[g] + 15) / 16) * 16 - 1;
+                gr.conv_kmax[g] = kvar;
+            }
+        }
+        const long long key = (long long)mask | ((long long)kvar << 8) | ((long long)kr << 16) |
+                              ((long long)kc << 24);
+        rc = launch_or_replay(s, c, n, key);
+        if (rc) return rc;
+        s->stats.mixed_batches++;
+        return cudaEventRecord(c->done, st) == cudaSuccess ? LENSGB_OK : LENSGB_ERR_CUDA;
+    }
     for (int i = 0; i < n; ++i) {
         const Req* q = c->batch[i];
         const lensgb_request& r = q->r;
@@ -399,42 +617,8 @@ int run_batch(lensgb_server* s, Context* c, int n) {
             ++plane;
         }
     }
-    int rc = LENSGB_OK;
-    auto g = c->graphs.find(n);
-    if (g != c->graphs.end()) {
-        if (cudaGraphLaunch(g->second, st) != cudaSuccess) return LENSGB_ERR_CUDA;
-        s->stats.graph_launches++;
-    } else if (s->cfg.use_graphs && c->eager_runs[n] >= 1) {
-        // the same context and size ran eagerly before: capture and replay
-        const long long tc = s->now();
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-            return LENSGB_ERR_CUDA;
-        rc = launch_batch(s, c, n);
-        cudaError_t e = cudaStreamEndCapture(st, &graph);
-        if (rc == LENSGB_OK && e == cudaSuccess &&
-            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
-            c->graphs[n] = exec;
-            s->stats.graph_captures++;
-        } else {
-            exec = nullptr;
-        }
-        if (graph) cudaGraphDestroy(graph);
-        cudaGetLastError();
-        s->stats.capture_ns += s->now() - tc;
-        if (exec) {
-            if (cudaGraphLaunch(exec, st) != cudaSuccess) return LENSGB_ERR_CUDA;
-            s->stats.graph_launches++;
-        } else {
-            rc = launch_batch(s, c, n);  // capture failed: run eagerly
-            if (rc) return rc;
-        }
-    } else {
-        rc = launch_batch(s, c, n);
-        if (rc) return rc;
-        c->eager_runs[n]++;
-    }
+    int rc = launch_or_replay(s, c, n, n);
+    if (rc) return rc;
     if (cudaEventRecord(c->done, st) != cudaSuccess) return LENSGB_ERR_CUDA;
     return LENSGB_OK;
 }
@@ -446,8 +630,10 @@ void finish_batch(lensgb_server* s, Context* c, int rc) {
     for (size_t i = 0; i < c->batch.size(); ++i) {
         Req* q = c->batch[i];
         if (rc == LENSGB_OK && b.key.likelihood && q->r.logl_out) *q->r.logl_out = c->logl_host[i];
-        if (rc == LENSGB_OK && q->r.image_out && !q->out_pinned)
-            memcpy(q->r.image_out, c->img_host + i * ib, ib);
+        if (rc == LENSGB_OK && q->r.image_out && !q->out_pinned) {
+            const size_t o = b.mixed ? (size_t)c->boff_host[i] : i * ib;
+            memcpy(q->r.image_out, c->img_host + o, (size_t)q->npix * b.esz);
+        }
         q->rc = rc;
         q->t_done = t;
         q->state.store(rc == LENSGB_OK ? LENSGB_REQ_DONE : LENSGB_REQ_FAILED,
@@ -486,8 +672,18 @@ bool launch_one(lensgb_server* s) {
             break;
         }
     const int n = (int)std::min<size_t>(b.queue.size(), (size_t)s->cfg.max_batch);
+    // what the first m queued requests need (prefix sums over the queue head)
+    auto& pp = s->pre_pix;
+    auto& pk = s->pre_kel;
+    pp.assign((size_t)n + 1, 0);
+    pk.assign((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        pp[(size_t)i + 1] = pp[(size_t)i] + b.queue[(size_t)i]->npix;
+        pk[(size_t)i + 1] = pk[(size_t)i] + b.queue[(size_t)i]->k2;
+    }
+    auto need = [&](int m) { return Need{m, pp[(size_t)m], pk[(size_t)m]}; };
     if (!c) {
-        if (!make_room(s, context_bytes(b, n), nullptr)) return false;  // wait for memory
+        if (!make_room(s, context_bytes(b, need(n)), nullptr)) return false;  // wait for memory
         c = new_context(s, best);
         if (!c) {
             // cannot build the model: fail the queued requests of this bucket
@@ -504,11 +700,12 @@ bool launch_one(lensgb_server* s) {
     // the largest batch that fits the budget (halving from the queue length)
     int rc = LENSGB_ERR_OOM;
     for (int m = n; m >= 1 && rc == LENSGB_ERR_OOM; m = (m == 1 ? 0 : (m + 1) / 2))
-        rc = grow_context(s, c, m);
+        rc = grow_context(s, c, need(m));
     if (rc == LENSGB_ERR_OOM) {
         if (c->cap == 0 && s->inflight == 0) {
-            // nothing in flight can free memory: the request can never fit
-            const int m = (int)b.queue.size();
+            // nothing in flight can free memory: the request can never fit (in a
+            // uniform bucket, neither can any other of its queue)
+            const int m = b.mixed ? 1 : (int)b.queue.size();
             for (int i = 0; i < m; ++i) {
                 Req* q = b.queue.front();
                 b.queue.pop_front();
@@ -521,7 +718,9 @@ bool launch_one(lensgb_server* s) {
         }
         return false;
     }
-    const int nb = std::min(n, c->cap);
+    // the longest queue head that the context holds
+    int nb = std::min(n, c->cap);
+    while (nb > 1 && (pp[(size_t)nb] > c->pix_cap || pk[(size_t)nb] > c->kel_cap)) --nb;
     const long long t = s->now();
     for (int i = 0; i < nb; ++i) {
         Req* q = b.queue.front();
@@ -607,6 +806,12 @@ bool is_pinned(const void* p) {
     return ok;
 }
 
+// Requests that a mixed bucket can take: image only, no supersampled convolution.
+bool mixable(const lensgb_server* s, const lensgb_request& r) {
+    return s->cfg.mixed_grids && !r.data &&
+           !(r.desc.supersampling_convolution && r.desc.supersampling > 1);
+}
+
 int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
     BucketKey k;
     memset(&k, 0, sizeof k);
@@ -621,14 +826,37 @@ int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
         *out = it->second;
         return LENSGB_OK;
     }
-    // validate the model once per bucket
+    // validate the model once per exact key
     lensgb_model* m = nullptr;
     int rc = lensgb_model_create(&r.desc, &m);
     if (rc) return serr(rc, std::string("request model: ") + lensgb_last_error());
-    Bucket* b = new Bucket();
-    b->key = k;
-    b->n_params = lensgb_model_param_count(m);
+    const int n_params = lensgb_model_param_count(m);
     lensgb_model_destroy(m);
+    const bool mixed = mixable(s, r);
+    BucketKey bk = k;
+    if (mixed) {
+        // the bucket's model: the request's profile stack, supersampling,
+        // precision and PSF type on a 1 x 1 placeholder grid (lensgb_image_mixed
+        // takes every system's grid and PSF size from its table)
+        lensgb_model_desc& d = bk.desc;
+        d.nx = d.ny = 1;
+        d.transform_pix2angle[0] = d.transform_pix2angle[3] = 1.0;
+        d.transform_pix2angle[1] = d.transform_pix2angle[2] = 0.0;
+        d.ra_at_xy_0 = d.dec_at_xy_0 = 0.0;
+        d.kernel_size = d.psf_type == LENSGB_PSF_NONE ? 0 : 1;
+        d.supersampling_convolution = 0;
+        d.low_res_kernel_size = 0;
+        auto mi = s->mixed_index.find(bk);
+        if (mi != s->mixed_index.end()) {
+            *out = mi->second;
+            s->bucket_index[k] = *out;
+            return LENSGB_OK;
+        }
+    }
+    Bucket* b = new Bucket();
+    b->key = bk;
+    b->mixed = mixed;
+    b->n_params = n_params;
     b->npix = (long long)r.desc.nx * r.desc.ny;
     b->k2 = r.desc.psf_type == LENSGB_PSF_NONE
                 ? 0
@@ -638,6 +866,7 @@ int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
     s->buckets.push_back(b);
     *out = (int)s->buckets.size() - 1;
     s->bucket_index[k] = *out;
+    if (mixed) s->mixed_index[bk] = *out;
     return LENSGB_OK;
 }
 
@@ -661,6 +890,11 @@ int lensgb_server_create(const lensgb_server_config* cfg, lensgb_server** out) {
     lensgb_server* s = new lensgb_server();
     s->cfg = c;
     cudaGetDevice(&s->device);
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device) == cudaSuccess &&
+        nsm > 0)
+        s->n_sms = nsm;
+    cudaGetLastError();
     memset(&s->stats, 0, sizeof s->stats);
     s->t0 = Clock::now();
     s->worker = std::thread(worker_main, s);
@@ -707,6 +941,11 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
             q.t_release = r.release_ns > t ? r.release_ns : t;
             q.out_pinned = (pinned[(size_t)i] & 8) != 0;
             q.in_pinned = pinned[(size_t)i] & 7;
+            q.npix = (long long)r.desc.nx * r.desc.ny;
+            q.k2 = r.desc.psf_type == LENSGB_PSF_NONE
+                       ? 0
+                       : r.desc.kernel_size * r.desc.kernel_size +
+                             r.desc.low_res_kernel_size * r.desc.low_res_kernel_size;
             s->incoming.push_back(&q);
             tickets[i] = q.ticket;
         }

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.lensgb_version() == 107
+    assert lib.lensgb_version() == 108
 
 
 def _desc(**kw):
@@ -123,8 +123,8 @@ def test_split_bits_is_exact_for_grid_indices():
 def test_struct_sizes_match_the_header_layout():
     """ctypes mirrors of the public structs have the C layout (x86-64 / aarch64 LP64)."""
     assert ctypes.sizeof(_lib.NoiseDesc) == 11 * 8
-    assert ctypes.sizeof(_lib.ServerConfig) == 4 + 4 + 8 + 4 + 4
-    assert ctypes.sizeof(_lib.ServerStats) == 10 * 8
+    assert ctypes.sizeof(_lib.ServerConfig) == 4 + 4 + 8 + 4 + 4 + 4 + 4  # tail padding
+    assert ctypes.sizeof(_lib.ServerStats) == 11 * 8
     assert ctypes.sizeof(_lib.Request) == ctypes.sizeof(_lib.ModelDesc) + 10 * 8
 
 

@@ -1,9 +1,12 @@
 """Systems on different pixel grids and PSF sizes in one launch sequence
 (lensgb_image_mixed through the C ABI): every image must equal that system
-computed alone by its own ImageModel -- bit for bit in FP64, and in FP32 within
-1e-6 relative (the mixed launch runs its own compiled instantiation of the FP32
-ray kernel, whose instruction selection may differ by an ulp; the FP32 bar is
-1e-5)."""
+computed alone by its own ImageModel: bit for bit in FP64; in FP32 within the
+FP32 bar, 1e-5 of the image maximum, because the mixed launch runs its own
+compiled instantiation of the FP32 ray kernel, whose FMA contractions may round
+a few pixels differently by an ulp or two (and so flip a pixel's FP64
+refinement).  Within the mixed path a
+system's image does not depend on what else shares the launch: bit for bit in
+both precisions."""
 
 import numpy as np
 import pytest
@@ -54,7 +57,10 @@ def test_mixed_batch_equals_alone(cuda, precision, psf_type):
         if precision == "fp64":
             np.testing.assert_array_equal(g, a)
         else:
-            np.testing.assert_allclose(g, a, rtol=1e-6, atol=1e-6 * np.abs(a).max())
+            np.testing.assert_allclose(g, a, rtol=0, atol=1e-5 * np.abs(a).max())
+    # each system alone through the mixed path: the same bits as in the mix
+    for req, g in zip(reqs, got):
+        np.testing.assert_array_equal(image_mixed([req])[0].cpu().numpy(), g.cpu().numpy())
 
 
 def test_mixed_rejects_different_stacks(cuda):

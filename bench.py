@@ -439,6 +439,69 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     }
 
 
+def sampler_section(steps, seed=1003, n_walkers=256):
+    """Sampler ensemble: LikelihoodModule.logL_batch over n_walkers parameter
+    vectors of the gradient workload's system (120^2, s=2, K=21, EPL+SHEAR,
+    Sersic source and lens light, 22 sampled parameters) -- one batched launch
+    -- against the same module called one vector at a time."""
+    import numpy as np
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import sampling as S, workloads as W
+
+    N, S2, K = 120, 2, 21
+    model_lists = {"lens_model_list": ["EPL", "SHEAR"],
+                   "source_light_model_list": ["SERSIC_ELLIPSE"],
+                   "lens_light_model_list": ["SERSIC_ELLIPSE"]}
+    _, lens, src, ll, kern = W.gradient_batch(seed=seed, batch=1, num_pix=N, supersampling=S2,
+                                              kernel_size=K)
+    kl, ks, kll = W.instance(lens, 0), W.instance(src, 0), W.instance(ll, 0)
+    g = W.grid_kwargs(N, 0.05)
+    im = J.ImageModel(J.ImageData(np.zeros((N, N)), exposure_time=1000.0, background_rms=0.01,
+                                  **g),
+                      J.PSF("PIXEL", kernel_point_source=kern[0]),
+                      J.LensModel(model_lists["lens_model_list"]),
+                      J.LightModel(model_lists["source_light_model_list"]),
+                      J.LightModel(model_lists["lens_light_model_list"]),
+                      kwargs_numerics={"supersampling_factor": S2})
+    data = W.noisy_data(im.image(kl, ks, kll))
+    joint = {"multi_band_list": [[{"image_data": data, "background_rms": 0.01,
+                                   "exposure_time": 1000.0, **g},
+                                  {"psf_type": "PIXEL", "kernel_point_source": kern[0]},
+                                  {"supersampling_factor": S2}]],
+             "multi_band_type": "single-band"}
+    param = S.Param(model_lists, kwargs_fixed_lens=[{}, {"ra_0": 0.0, "dec_0": 0.0}],
+                    linear_solver=False)
+    lm = S.LikelihoodModule(joint, model_lists, param)
+    f = S.prepare_logL_func("gpu", lm.logL)
+    truth = param.kwargs2args(kl, ks, kll)
+    args = truth + 1e-3 * np.random.default_rng(seed).standard_normal((n_walkers, truth.size))
+    for _ in range(3):
+        f(args)
+    t = []
+    for _ in range(max(steps, 3)):
+        t0 = time.perf_counter()
+        f(args)
+        t.append(time.perf_counter() - t0)
+    batched = statistics.median(t)
+    n1 = 16
+    for j in range(3):
+        lm.logL(args[j])
+    t0 = time.perf_counter()
+    for j in range(n1):
+        lm.logL(args[j])
+    single = (time.perf_counter() - t0) / n1
+    return {
+        "workload": "sampler_ensemble_epl_120x120_s2_psf21",
+        "walkers": n_walkers, "sampled_params": int(truth.size),
+        "ms_per_ensemble": batched * 1e3, "evaluations_per_s": n_walkers / batched,
+        "one_vector_per_call_ms": single * 1e3, "one_vector_per_call_evaluations_per_s": 1.0 / single,
+        "speedup": single * n_walkers / batched,
+        "precision": "FP64 image and likelihood",
+        "timing": "host wall clock of prepare_logL_func('gpu', LikelihoodModule.logL) on an "
+                  "(n_walkers, 22) host array, result back on the host; median over calls",
+    }
+
+
 def gradient_section(steps, seed=1003):
     """Adjoint gradient of logL for 256 systems (120^2, s=2, PSF 21, EPL+SHEAR,
     Sersic source and lens light): time per batch, and the worst component
@@ -786,6 +849,7 @@ def gpu_arm(args):
         # --- adjoint likelihood gradient
         if not args.no_grad:
             extra["gradient"] = gradient_section(args.steps)
+            extra["sampler"] = sampler_section(args.steps)
 
         # --- serving stream (continuous batching)
         if args.serve_requests > 0:

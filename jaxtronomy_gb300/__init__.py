@@ -10,7 +10,9 @@ from .image_model import ImageModel  # noqa: F401
 from .lens_model import LensModel  # noqa: F401
 from .lens_model_bulk import LensModelBulk  # noqa: F401
 from .light_model import LightModel  # noqa: F401
+from .sampling import ImageLikelihood, LikelihoodModule, Param, prepare_logL_func  # noqa: F401
 
 __version__ = "0.1.0"
 
-__all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LensModelBulk", "LightModel"]
+__all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LensModelBulk", "LightModel",
+           "ImageLikelihood", "LikelihoodModule", "Param", "prepare_logL_func"]

@@ -1,0 +1,82 @@
+"""Host logic of the sampler-facing layer (no GPU): parameter bookkeeping of
+Param, bounds, and the construction-time errors of LikelihoodModule /
+ImageLikelihood / prepare_logL_func."""
+
+import numpy as np
+import pytest
+
+from jaxtronomy_gb300 import sampling as S
+
+MODEL = {"lens_model_list": ["EPL", "SHEAR"], "source_light_model_list": ["SERSIC_ELLIPSE"],
+         "lens_light_model_list": ["SERSIC"]}
+FIXED_LENS = [{"center_x": 0.0, "center_y": 0.0}, {"ra_0": 0.0, "dec_0": 0.0}]
+
+
+def _param(**kw):
+    return S.Param(MODEL, kwargs_fixed_lens=FIXED_LENS, linear_solver=False, **kw)
+
+
+def test_param_order_and_limits():
+    p = _param()
+    n, names = p.num_param()
+    # EPL: theta_E gamma e1 e2 (centre fixed); SHEAR: gamma1 gamma2; Sersic ellipse 7; Sersic 5
+    assert n == 4 + 2 + 7 + 5
+    assert names[:6] == ["theta_E_lens0", "gamma_lens0", "e1_lens0", "e2_lens0", "gamma1_lens1",
+                         "gamma2_lens1"]
+    lo, hi = p.param_limits()
+    assert lo[1] == 1.5 and hi[1] == 2.5          # EPL gamma (epl.py:51-66)
+    assert lo[6] == 0.0 and hi[6] == 100.0        # Sersic amp (sersic_ellipse.py:26-43)
+    assert lo[8] == 0.5 and hi[8] == 8.0          # n_sersic
+
+
+def test_param_round_trip_single_and_batched():
+    p = _param(kwargs_lower_lens=[{"theta_E": 0.5}, {}], kwargs_upper_lens=[{"theta_E": 2.0}, {}])
+    lo, hi = p.param_limits()
+    assert (lo[0], hi[0]) == (0.5, 2.0)
+    rng = np.random.default_rng(0)
+    a = rng.uniform(lo, np.minimum(hi, lo + 1.0), size=(7, p.num_param()[0]))
+    kw = p.args2kwargs(a)
+    assert kw["kwargs_lens"][0]["center_x"] == 0.0            # fixed values stay scalars
+    assert np.shape(kw["kwargs_lens"][0]["theta_E"]) == (7,)  # sampled values become arrays
+    for j in range(7):
+        kj = p.args2kwargs(a[j])
+        np.testing.assert_array_equal(p.kwargs2args(kj["kwargs_lens"], kj["kwargs_source"],
+                                                    kj["kwargs_lens_light"]), a[j])
+
+
+def test_param_rejects_unsupported():
+    with pytest.raises(ValueError):
+        S.Param(MODEL)  # linear_solver defaults to True, as in lenstronomy
+    with pytest.raises(ValueError):
+        S.Param(MODEL, linear_solver=False, kwargs_fixed_ps=[{"ra_image": [0.0]}])
+    with pytest.raises(ValueError):
+        S.Param(MODEL, linear_solver=False, joint_lens_with_light=[[0, 0, ["center_x"]]])
+    with pytest.raises(ValueError):
+        S.Param({"lens_model_list": ["SPEMD"]}, linear_solver=False)
+    with pytest.raises(ValueError):
+        _param().args2kwargs(np.zeros(3))
+
+
+def test_check_bounds_and_prepare_errors():
+    pen, hit = S.LikelihoodModule.check_bounds([0.0, 2.0], [0.0, 0.0], [1.0, 1.0])
+    assert hit and pen == 1e5
+    pen, hit = S.LikelihoodModule.check_bounds([0.5], [0.0], [1.0])
+    assert not hit and pen == 0.0
+    with pytest.raises(ValueError):
+        S.prepare_logL_func("tpu", lambda a: 0.0)
+    with pytest.raises(ValueError):
+        S.prepare_logL_func("cpu", lambda a: 0.0)
+    with pytest.raises(ValueError):
+        S.prepare_logL_func("gpu", lambda a: 0.0)
+
+
+def test_likelihood_module_rejects_unsupported_terms():
+    p = _param()
+    with pytest.raises(ValueError):
+        S.LikelihoodModule({}, MODEL, p, time_delay_likelihood=True)
+    with pytest.raises(ValueError):
+        S.LikelihoodModule({}, MODEL, p, prior_lens_kde=[[0, "theta_E", [1.0]]])
+    with pytest.raises(ValueError):
+        S.ImageLikelihood([[{}, {}, {}]], "multi-linear", MODEL, linear_solver=False)
+    with pytest.raises(ValueError):
+        S.ImageLikelihood([[{}, {}, {}]], "single-band", MODEL)  # linear_solver=True

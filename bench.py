@@ -334,12 +334,13 @@ def substructure_section(steps, warmup, fp32_peak, flush):
 
 
 def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_bucket=2,
-                    use_graphs=True, loads=(0.5, 0.8, 0.95), mixed_grids=True):
+                    use_graphs=True, loads=(0.5, 0.8, 0.95), mixed_grids=2):
     """Serving stream: capacity (all requests released at once), then Poisson
     arrivals at 0.5 / 0.8 / 0.95 x capacity with p50/p99 latency; results of a
     sample checked against the same requests computed alone.  mixed_grids:
     requests of every grid and PSF size of one (profile stack, supersampling)
-    share a bucket; otherwise every exact model is a bucket of its own."""
+    share a bucket (2: of one profile stack); otherwise every exact model is a
+    bucket of its own."""
     import numpy as np
     from jaxtronomy_gb300 import _lib, serving, workloads as W
 
@@ -417,7 +418,8 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     return {
         "workload": "serving_stream_%d_requests" % len(reqs),
         "requests": len(reqs),
-        "buckets": len({(k[1], k[3], k[4]) for k in models}) if mixed_grids else len(models),
+        "buckets": (len({(k[3], k[4]) for k in models}) if mixed_grids == 2 else
+                    len({(k[1], k[3], k[4]) for k in models}) if mixed_grids else len(models)),
         "mixed_grids": mixed_grids,
         "capacity_requests_per_s": capacity,
         "capacity_latency_ms_p50": float(np.percentile(lat_cap, 50)),
@@ -854,6 +856,7 @@ def gpu_arm(args):
         # --- serving stream (continuous batching)
         if args.serve_requests > 0:
             extra["serving"] = serving_section(args.serve_requests)
+            extra["serving_grid_buckets"] = serving_section(args.serve_requests, mixed_grids=1)
             extra["serving_exact_buckets"] = serving_section(args.serve_requests,
                                                              mixed_grids=False)
 

@@ -159,9 +159,9 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
                  void* stream);
 
 /* lensgb_image for systems of different pixel grids in one launch sequence:
- * grids[i] (host) gives system i's grid and PSF size; the model supplies the
- * profile stack, supersampling, PSF type and precision (its own grid fields
- * are not used).  psf_dev holds the systems' kernels back to back
+ * grids[i] (host) gives system i's grid, PSF size and (optionally)
+ * supersampling factor; the model supplies the profile stack, PSF type,
+ * precision and the default supersampling (its own grid fields are not used).  psf_dev holds the systems' kernels back to back
  * (kernel_size_i^2 values each), out_dev their images back to back
  * (ny_i x nx_i each).  Each image equals lensgb_image of that system alone,
  * bit for bit.  Not for supersampled convolution or sub-frame models.  The
@@ -174,6 +174,7 @@ typedef struct {
     double transform_pix2angle[4];
     double ra_at_xy_0, dec_at_xy_0;
     int kernel_size;
+    int supersampling;  /* this system's supersampling factor (0: the model's)          */
 } lensgb_system_grid;
 
 int lensgb_image_mixed(lensgb_model* model, const double* params_dev, int n_inst,
@@ -331,9 +332,11 @@ typedef struct {
     int mixed_grids;            /* 1: image requests whose models differ only in the
                                    grid (nx, ny, transform_pix2angle, ra/dec_at_xy_0)
                                    and kernel_size share a bucket, whose batches run
-                                   through lensgb_image_mixed (not graph-captured);
-                                   likelihood and supersampled-convolution requests
-                                   keep exact-model buckets                           */
+                                   through lensgb_image_mixed; 2: also requests of
+                                   different supersampling factors (one ray-kernel
+                                   launch per factor in each batch); likelihood and
+                                   supersampled-convolution requests keep exact-model
+                                   buckets                                             */
 } lensgb_server_config;
 
 typedef struct {

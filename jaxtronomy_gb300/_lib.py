@@ -102,6 +102,7 @@ class SystemGrid(ctypes.Structure):
         ("ra_at_xy_0", ctypes.c_double),
         ("dec_at_xy_0", ctypes.c_double),
         ("kernel_size", ctypes.c_int),
+        ("supersampling", ctypes.c_int),
     ]
 
 

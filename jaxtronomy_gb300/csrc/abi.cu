@@ -234,7 +234,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 108; }
+int lensgb_version(void) { return 109; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -494,16 +494,21 @@ MixedLayout mixed_layout(int cap) {
     L.o_n = 0;
     L.o_grid = 256;
     L.o_off = al(L.o_grid + n * sizeof(GridDesc));
-    L.o_toff = al(L.o_off + (n + 1) * 8);
-    L.o_koff = al(L.o_toff + (n + 1) * 4);
+    L.o_koff = al(L.o_off + (n + 1) * 8);
     L.o_ks = al(L.o_koff + n * 8);
     L.o_scale = al(L.o_ks + n * 4);
-    L.o_gsys = al(L.o_scale + n * 8);
-    L.o_goff = al(L.o_gsys + 8 * n * 4);
-    L.o_gcnt = al(L.o_goff + 8 * (n + 1) * 4);
-    L.bytes = al(L.o_gcnt + 8 * 4);
+    L.o_rsys = al(L.o_scale + n * 8);
+    L.o_rtoff = al(L.o_rsys + MIX_RAY_GROUPS * n * 4);
+    L.o_rcnt = al(L.o_rtoff + MIX_RAY_GROUPS * (n + 1) * 4);
+    L.o_gsys = al(L.o_rcnt + MIX_RAY_GROUPS * 4);
+    L.o_goff = al(L.o_gsys + MIX_CONV_GROUPS * n * 4);
+    L.o_gcnt = al(L.o_goff + MIX_CONV_GROUPS * (n + 1) * 4);
+    L.bytes = al(L.o_gcnt + MIX_CONV_GROUPS * 4);
     return L;
 }
+
+// Ray group of a supersampling factor (see MIX_RAY_GROUPS).
+static int ray_group(int s, bool fp64) { return (!fp64 && s >= 1 && s <= 4) ? s : 0; }
 
 // Convolution group of a kernel width: FP64 has one (run-time width); FP32
 // groups 1..6 run the kernel specialised for widths <= 8 g, 7 the run-time-width one.
@@ -516,27 +521,37 @@ static int conv_group(int K, bool fp64) {
 int mixed_fill(const lensgb_model* m, unsigned char* H, const MixedLayout& L,
                const lensgb_system_grid* grids, int n, bool conv, MixedCounts* out) {
     if (n < 1 || n > L.cap) return fail(LENSGB_ERR_INVALID, "mixed table capacity exceeded");
-    const int s = m->desc.supersampling;
+    const int s_model = m->desc.supersampling;
     const bool fp64 = m->desc.precision == LENSGB_FP64;
     const int TW = fp64 ? 32 : 64, TH = 64;  // convolution tile (columns, rows)
     GridDesc* gd = (GridDesc*)(H + L.o_grid);
     long long* off = (long long*)(H + L.o_off);
-    int* toff = (int*)(H + L.o_toff);
     long long* koff = (long long*)(H + L.o_koff);
     int* ks = (int*)(H + L.o_ks);
     double* area = (double*)(H + L.o_scale);
+    int* rsys = (int*)(H + L.o_rsys);
+    int* rtoff = (int*)(H + L.o_rtoff);
+    int* rcnt = (int*)(H + L.o_rcnt);
     int* gsys = (int*)(H + L.o_gsys);
     int* goff = (int*)(H + L.o_goff);
     int* gcnt = (int*)(H + L.o_gcnt);
     MixedCounts c;
     memset(&c, 0, sizeof c);
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < MIX_RAY_GROUPS; ++k) {
+        rcnt[k] = 0;
+        rtoff[(size_t)k * (L.cap + 1)] = 0;
+    }
+    for (int k = 0; k < MIX_CONV_GROUPS; ++k) {
         gcnt[k] = 0;
         goff[(size_t)k * (L.cap + 1)] = 0;
     }
     long long pix = 0, kel = 0, tiles = 0;
     for (int i = 0; i < n; ++i) {
         const lensgb_system_grid& q = grids[i];
+        const int s = q.supersampling > 0 ? q.supersampling : s_model;
+        if (q.supersampling < 0 || s > 32)
+            return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) +
+                                                ": supersampling must be in 0..32");
         if (q.nx <= 0 || q.ny <= 0 || (long long)q.nx * s > (1 << 22) ||
             (long long)q.ny * s > (1 << 22) || (long long)q.nx * q.ny * s * s >= (1LL << 31))
             return fail(LENSGB_ERR_INVALID, "system " + std::to_string(i) + ": bad grid size");
@@ -548,11 +563,17 @@ int mixed_fill(const lensgb_model* m, unsigned char* H, const MixedLayout& L,
         area[i] = pw * pw;  // as the single-grid path forms pixel_width^2
         const long long np = (long long)q.nx * q.ny;
         off[i] = pix;
-        toff[i] = (int)tiles;
         koff[i] = kel;
         ks[i] = conv ? q.kernel_size : 0;
         pix += np;
-        tiles += (np + 255) / 256;
+        const long long rt = (np + 255) / 256;
+        tiles += rt;
+        const int rg = ray_group(s, fp64);
+        int* ro = rtoff + (size_t)rg * (L.cap + 1);
+        rsys[(size_t)rg * L.cap + rcnt[rg]] = i;
+        ro[rcnt[rg] + 1] = ro[rcnt[rg]] + (int)rt;
+        rcnt[rg]++;
+        c.ray_tiles[rg] += (int)rt;
         if (conv) {
             kel += (long long)q.kernel_size * q.kernel_size;
             const int g = conv_group(q.kernel_size, fp64);
@@ -568,12 +589,10 @@ int mixed_fill(const lensgb_model* m, unsigned char* H, const MixedLayout& L,
     if (pix >= (1LL << 32)) return fail(LENSGB_ERR_INVALID, "more than 2^32 pixels in one call");
     if (tiles >= (1LL << 31)) return fail(LENSGB_ERR_INVALID, "too many ray tiles in one call");
     off[n] = pix;
-    toff[n] = (int)tiles;
     *(int*)(H + L.o_n) = n;
     c.n = n;
     c.pix = pix;
     c.kel = kel;
-    c.ray_tiles = (int)tiles;
     *out = c;
     return LENSGB_OK;
 }
@@ -613,7 +632,6 @@ int mixed_launch(lensgb_model* m, const double* params, int n_cap, const unsigne
     MixedTab mt;
     mt.grid = dgrid;
     mt.off = (const long long*)(tab + L.o_off);
-    mt.tile_off = (const int*)(tab + L.o_toff);
     mt.scale = (const double*)(tab + L.o_scale);
     mt.n_inst = n_dev;
     launch_prepare(m->grid, m->st, params, n_cap, m->rec_d, m->rec_f, m->coef_d, m->coef_f, st,
@@ -624,10 +642,20 @@ int mixed_launch(lensgb_model* m, const double* params, int n_cap, const unsigne
     if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), st) != cudaSuccess)
         return check_cuda("refine counter reset");
     void* target = conv ? m->mix_low : out;
-    if (gr.ray_ctas > 0)
+    int last = -1;
+    for (int g = 0; g < MIX_RAY_GROUPS; ++g)
+        if (gr.ray_ctas[g] > 0) last = g;
+    for (int g = 0; g < MIX_RAY_GROUPS; ++g) {
+        if (gr.ray_ctas[g] <= 0) continue;
+        mt.sys = (const int*)(tab + L.o_rsys) + (size_t)g * L.cap;
+        mt.tile_off = (const int*)(tab + L.o_rtoff) + (size_t)g * (L.cap + 1);
+        mt.count = (const int*)(tab + L.o_rcnt) + g;
+        mt.s_group = g;
+        mt.refine = g == last;  // one FP64 refine pass after all groups
         launch_raytrace(m->grid, m->st, n_cap, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
                         flags, m->pixel_width * m->pixel_width, m->desc.precision, rf, st, &mt,
-                        gr.ray_ctas);
+                        gr.ray_ctas[g]);
+    }
     if ((rc = check_cuda("raytrace launch"))) return rc;
     if (conv) {
         ConvMixed cm;
@@ -721,7 +749,7 @@ int lensgb_image_mixed(lensgb_model* m, const double* params, int n_inst,
     m->mix_ev_pending = true;
     // one CTA per tile; every group with tiles gets its launch
     MixedGrid gr;
-    gr.ray_ctas = c.ray_tiles;
+    for (int k = 0; k < MIX_RAY_GROUPS; ++k) gr.ray_ctas[k] = c.ray_tiles[k];
     for (int k = 0; k < 8; ++k) {
         gr.conv_ctas[k] = c.conv_tiles[k];
         gr.conv_kmax[k] = c.kmax[k];

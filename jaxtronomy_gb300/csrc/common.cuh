@@ -64,19 +64,26 @@ struct RefineArgs {
     float kappa;                // FP32 relative error bound of |alpha| (units of 1)
 };
 
-// Launch over systems of different grids (one model's profile stack and
-// supersampling).  Every table is per system, so its size does not depend on
-// the pixel count, and the system count is read on the device, so one launch
-// configuration (e.g. a captured CUDA graph) serves batches of any mix.  The
-// ray kernels run a grid-stride loop over tiles of 256 pixels; system i owns
-// tiles tile_off[i] .. tile_off[i + 1] - 1.  grid == nullptr: a uniform launch
+// Launch over systems of different grids and supersampling factors (one
+// model's profile stack).  Every table is per system, so its size does not
+// depend on the pixel count, and the system counts are read on the device, so
+// one launch configuration (e.g. a captured CUDA graph) serves batches of any
+// mix.  The ray kernel runs once per supersampling group (FP32: s = 1..4 with
+// the compile-time-s kernel, group 0 every other s; FP64: one group) -- so a
+// system always runs the same instantiation, whatever shares its batch -- as a
+// grid-stride loop over the group's tiles of 256 pixels: system sys[j] owns
+// tiles tile_off[j] .. tile_off[j + 1] - 1.  grid == nullptr: a uniform launch
 // (every system on the launch's own grid, images nx * ny apart).
 struct MixedTab {
     const GridDesc* grid;     // [n]
     const long long* off;     // [n + 1]: element offset of each system's image
-    const int* tile_off;      // [n + 1]: first ray tile of each system
     const double* scale;      // [n]: image scale (pixel area) of each system
     const int* n_inst;        // device: n
+    const int* sys;           // this launch's group: its systems, in order
+    const int* tile_off;      // [count + 1]: first ray tile of each
+    const int* count;         // device: systems in the group
+    int s_group;              // host: the group's compile-time s (0: per system)
+    bool refine;              // host: launch the refine pass after this group
 };
 
 // Convolution over systems of different sizes, one launch per kernel-width

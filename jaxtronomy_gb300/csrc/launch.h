@@ -51,26 +51,35 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
 // of a mixed launch for up to `cap` systems (see MixedTab / ConvMixed).
 struct MixedLayout {
     int cap;
-    size_t o_n, o_grid, o_off, o_toff, o_koff, o_ks, o_scale, o_gsys, o_goff, o_gcnt, bytes;
+    size_t o_n, o_grid, o_off, o_koff, o_ks, o_scale;
+    size_t o_rsys, o_rtoff, o_rcnt;  // ray groups: systems, tile prefix, counts
+    size_t o_gsys, o_goff, o_gcnt;   // convolution groups: the same
+    size_t bytes;
 };
 MixedLayout mixed_layout(int cap);
 
-// Host-side totals of a filled table block.  Convolution groups: index 0 for
-// FP64, 1..6 the fixed-width FP32 kernels, 7 the run-time-width FP32 kernel.
+// Ray-kernel groups: FP32 s = 1..4 (compile-time s), 0 every other s; FP64
+// uses group 0 only.  Convolution groups: index 0 for FP64, 1..6 the
+// fixed-width FP32 kernels, 7 the run-time-width FP32 kernel.
+constexpr int MIX_RAY_GROUPS = 5;
+constexpr int MIX_CONV_GROUPS = 8;
+
+// Host-side totals of a filled table block.
 struct MixedCounts {
     int n;
     long long pix, kel;
-    int ray_tiles;
-    int conv_tiles[8];
-    int kmax[8];
+    int ray_tiles[MIX_RAY_GROUPS];
+    int conv_tiles[MIX_CONV_GROUPS];
+    int kmax[MIX_CONV_GROUPS];
 };
 
-// Launch configuration: CTAs of the ray kernel and of each convolution group
-// (0: the group is not launched) and the widest kernel each group may meet.
+// Launch configuration: CTAs of each ray group and of each convolution group
+// (0: the group is not launched) and the widest kernel each convolution group
+// may meet.
 struct MixedGrid {
-    int ray_ctas;
-    int conv_ctas[8];
-    int conv_kmax[8];
+    int ray_ctas[MIX_RAY_GROUPS];
+    int conv_ctas[MIX_CONV_GROUPS];
+    int conv_kmax[MIX_CONV_GROUPS];
 };
 
 // Validates n system grids and writes their tables into host block H.

@@ -17,9 +17,13 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
     } else {
         mt.grid = nullptr;
         mt.off = nullptr;
-        mt.tile_off = nullptr;
         mt.scale = nullptr;
         mt.n_inst = nullptr;
+        mt.sys = nullptr;
+        mt.tile_off = nullptr;
+        mt.count = nullptr;
+        mt.s_group = g.s;
+        mt.refine = true;
     }
     const bool one_light = st.n_ll <= 1;
     const int a = st.n_lens == 2 ? st.lens[0] : 0, b = st.n_lens == 2 ? st.lens[1] : 0;

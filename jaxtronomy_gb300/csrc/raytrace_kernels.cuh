@@ -167,13 +167,14 @@ raytrace_fp64_kernel(GridDesc g0, StackDesc st, int ppt, const double* __restric
     // uniform launch: one pass for (system blockIdx.y, tile blockIdx.x);
     // mixed launch: grid-stride loop over every system's tiles
     const bool mixed = mt.grid != nullptr;
-    const int n_mixed = mixed ? *mt.n_inst : 0;
-    const int n_tiles = mixed ? __ldg(mt.tile_off + n_mixed) : 1;
+    const int n_grp = mixed ? *mt.count : 0;
+    const int n_tiles = mixed ? __ldg(mt.tile_off + n_grp) : 1;
     for (int t = mixed ? (int)blockIdx.x : 0; t < n_tiles; t += mixed ? (int)gridDim.x : 1) {
         int inst = blockIdx.y, tile = blockIdx.x;
         if (mixed) {
-            inst = find_segment(mt.tile_off, n_mixed, t);
-            tile = t - __ldg(mt.tile_off + inst);
+            const int j = find_segment(mt.tile_off, n_grp, t);
+            inst = __ldg(mt.sys + j);
+            tile = t - __ldg(mt.tile_off + j);
         }
         const GridDesc g = mixed ? mt.grid[inst] : g0;
         const double osc = mixed ? mt.scale[inst] : out_scale;
@@ -210,13 +211,14 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
     constexpr bool mixed = MIXED;  // compile-time, so a uniform launch reads g0 directly
     // uniform launch: one pass for (system blockIdx.y, tile blockIdx.x);
     // mixed launch: grid-stride loop over every system's tiles of 256 pixels
-    const int n_mixed = mixed ? *mt.n_inst : 0;
-    const int n_tiles = mixed ? __ldg(mt.tile_off + n_mixed) : 1;
+    const int n_grp = mixed ? *mt.count : 0;
+    const int n_tiles = mixed ? __ldg(mt.tile_off + n_grp) : 1;
     for (int t = mixed ? (int)blockIdx.x : 0; t < n_tiles; t += mixed ? (int)gridDim.x : 1) {
         int inst = blockIdx.y, tile = blockIdx.x;
         if (mixed) {
-            inst = find_segment(mt.tile_off, n_mixed, t);
-            tile = t - __ldg(mt.tile_off + inst);
+            const int j = find_segment(mt.tile_off, n_grp, t);
+            inst = __ldg(mt.sys + j);
+            tile = t - __ldg(mt.tile_off + j);
             out_scale = (float)mt.scale[inst];
         }
         const GridDesc& g = mixed ? mt.grid[inst] : g0;
@@ -360,15 +362,13 @@ constexpr int REFINE_THREADS = 128;
 
 template <int C0, int C1, int NS, int NLL>
 __global__ void __launch_bounds__(REFINE_THREADS)
-refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
+refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
               const double* __restrict__ coef, float* __restrict__ out, int flags,
-              double out_scale, RefineArgs rf, MixedTab mt) {
+              double out_scale, RefineArgs rf) {
     __shared__ double sub[32 * 32];  // s <= 32
     const unsigned int n = *rf.count;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const bool mixed = mt.grid != nullptr;
-    const int n_mixed = mixed ? *mt.n_inst : 0;
-    const int s = g0.s, s2 = s * s;
+    const int s = g.s, s2 = s * s;
     const int per = s2 <= REFINE_THREADS ? REFINE_THREADS / s2 : 1;  // pixels per chunk
     for (unsigned int first = blockIdx.x * per; first < n; first += gridDim.x * per) {
         for (int w = threadIdx.x; w < per * s2; w += REFINE_THREADS) {
@@ -376,20 +376,8 @@ refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
             double v = 0.0;
             if (first + el < n) {
                 const long long e = (long long)rf.list[first + el];
-                int inst;
-                if (mixed) {
-                    // the system whose image holds element e: off[inst] <= e < off[inst + 1]
-                    int lo = 0, hi = n_mixed - 1;
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
-                    }
-                    inst = lo;
-                } else {
-                    inst = (int)(e / ((long long)g0.nx * g0.ny));
-                }
-                const GridDesc g = mixed ? mt.grid[inst] : g0;
-                const long long pix = e - (mixed ? mt.off[inst] : (long long)inst * g.nx * g.ny);
+                const int inst = (int)(e / ((long long)g.nx * g.ny));
+                const long long pix = e - (long long)inst * g.nx * g.ny;
                 const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
                 const int si = k / s, sj = k - si * s;
                 v = ray_flux_d<C0, C1, NS, NLL>(g, st, rec + (long long)inst * n_prof * REC_D,
@@ -409,19 +397,59 @@ refine_kernel(GridDesc g0, StackDesc st, const double* __restrict__ rec,
                 acc += s == 1 ? rs : rs / (double)s;
             }
             if (s > 1) acc = acc / (double)s;
-            double osc = out_scale;
-            if (mixed) {
-                const long long e = (long long)rf.list[first + el];
-                int lo = 0, hi = n_mixed - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
-                }
-                osc = mt.scale[lo];
-            }
-            out[rf.list[first + el]] = (float)(acc * osc);
+            out[rf.list[first + el]] = (float)(acc * out_scale);
         }
         __syncthreads();
+    }
+}
+
+// Refine pass of a mixed launch (systems of different grids and supersampling
+// factors): one warp per listed pixel, its lanes evaluating the pixel's s^2
+// sub-rays (system s from the pixel's grid), combined by lane 0 in the order
+// of pixel_value_d, so a refined pixel again equals the FP64 kernel's value.
+template <int C0, int C1, int NS, int NLL>
+__global__ void __launch_bounds__(REFINE_THREADS)
+refine_mixed_kernel(StackDesc st, const double* __restrict__ rec,
+                    const double* __restrict__ coef, float* __restrict__ out, int flags,
+                    RefineArgs rf, MixedTab mt) {
+    constexpr int WARPS = REFINE_THREADS / 32;
+    __shared__ double sub[WARPS][32 * 32];  // s <= 32
+    const unsigned int n = *rf.count;
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    const int n_mixed = *mt.n_inst;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (unsigned int i = blockIdx.x * WARPS + warp; i < n; i += gridDim.x * WARPS) {
+        const long long e = (long long)rf.list[i];
+        // the system whose image holds element e: off[inst] <= e < off[inst + 1]
+        int lo = 0, hi = n_mixed - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (mt.off[mid] <= e) lo = mid; else hi = mid - 1;
+        }
+        const GridDesc g = mt.grid[lo];
+        const int s = g.s, s2 = s * s;
+        const long long pix = e - mt.off[lo];
+        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        const double* r = rec + (long long)lo * n_prof * REC_D;
+        const double* cf = coef + (long long)lo * st.n_epl * EPL_NMAX;
+        for (int k = lane; k < s2; k += 32) {
+            const int si = k / s, sj = k - si * s;
+            sub[warp][k] = ray_flux_d<C0, C1, NS, NLL>(g, st, r, cf, row * s + si, col * s + sj,
+                                                       flags);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const double* b = sub[warp];
+            double acc = 0;
+            for (int si = 0; si < s; ++si) {
+                double rs = 0;
+                for (int sj = 0; sj < s; ++sj) rs += b[si * s + sj];
+                acc += s == 1 ? rs : rs / (double)s;
+            }
+            if (s > 1) acc = acc / (double)s;
+            out[e] = (float)(acc * mt.scale[lo]);
+        }
+        __syncwarp();
     }
 }
 
@@ -483,16 +511,23 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
                     g, st, ppt, rec_f, coef_f, (float*)out, flags, (float)out_scale, rf, mt);
             }
         };
+        // a mixed launch runs its supersampling group's kernel (group 0: the
+        // run-time-s kernel, which reads s from each system's grid)
+        const int ss = mt.grid ? mt.s_group : g.s;
         if (C0 == GENERIC) run(std::integral_constant<int, 0>());
-        else if (g.s == 1) run(std::integral_constant<int, 1>());
-        else if (g.s == 2) run(std::integral_constant<int, 2>());
-        else if (g.s == 3) run(std::integral_constant<int, 3>());
-        else if (g.s == 4) run(std::integral_constant<int, 4>());
+        else if (ss == 1) run(std::integral_constant<int, 1>());
+        else if (ss == 2) run(std::integral_constant<int, 2>());
+        else if (ss == 3) run(std::integral_constant<int, 3>());
+        else if (ss == 4) run(std::integral_constant<int, 4>());
         else run(std::integral_constant<int, 0>());
-        if (rf.tau > 0.f && !(flags & LENSGB_NO_SOURCE) && st.n_src > 0) {
+        if (rf.tau > 0.f && !(flags & LENSGB_NO_SOURCE) && st.n_src > 0 && mt.refine) {
             const int rblocks = num_sms() * 4;
-            refine_kernel<C0, C1, NS, NLL><<<rblocks, 128, 0, stream>>>(
-                g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf, mt);
+            if (mt.grid)
+                refine_mixed_kernel<C0, C1, NS, NLL><<<rblocks, REFINE_THREADS, 0, stream>>>(
+                    st, rec_d, coef_d, (float*)out, flags, rf, mt);
+            else
+                refine_kernel<C0, C1, NS, NLL><<<rblocks, REFINE_THREADS, 0, stream>>>(
+                    g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf);
         }
     }
 }

@@ -6,9 +6,9 @@
 //   * releases submitted requests into per-bucket FIFO queues once their
 //     release time has passed (a bucket = one compiled model: profile lists,
 //     grid, supersampling, PSF size, precision and noise options; with
-//     mixed_grids, image requests of every grid and PSF size of one profile
-//     stack, supersampling and precision share a bucket, whose batches run
-//     through lensgb_image_mixed);
+//     mixed_grids, image requests of every grid and PSF size (mixed_grids = 2:
+//     and supersampling factor) of one profile stack and precision share a
+//     bucket, whose batches run through lensgb_image_mixed);
 //   * keeps up to n_streams batches in flight, one per CUDA stream, each batch
 //     a single lensgb_image / lensgb_loglike launch sequence over up to
 //     max_batch requests of one bucket -- requests that arrive while others
@@ -550,6 +550,7 @@ int run_batch(lensgb_server* s, Context* c, int n) {
             gi.ra_at_xy_0 = r.desc.ra_at_xy_0;
             gi.dec_at_xy_0 = r.desc.dec_at_xy_0;
             gi.kernel_size = r.desc.kernel_size;
+            gi.supersampling = r.desc.supersampling;
             c->boff_host[i] = po * (long long)b.esz;
             c->ptr_host[i] = (r.image_out && q->out_pinned) ? r.image_out
                                                              : (void*)(c->img_host + po * b.esz);
@@ -563,8 +564,8 @@ int run_batch(lensgb_server* s, Context* c, int n) {
                                     conv, &mc);
         if (rc) return rc;
         // launch shape: CTA counts in power-of-two classes of the batch's tiles,
-        // the convolution groups present, and (run-time-width group) the kernel
-        // width rounded up; one graph per shape
+        // the supersampling and convolution groups present, and (run-time-width
+        // group) the kernel width rounded up; one graph per shape
         auto p2 = [](int v, int cap) {
             int k = 0;
             while ((1 << k) < v && (1 << k) < cap) ++k;
@@ -572,8 +573,13 @@ int run_batch(lensgb_server* s, Context* c, int n) {
         };
         const int nsm = s->n_sms;
         lensgb::MixedGrid& gr = c->mgrid;
-        const int kr = p2(mc.ray_tiles, 8 * nsm);
-        gr.ray_ctas = std::min(1 << kr, 8 * nsm);
+        int rtot = 0, rmask = 0;
+        for (int g = 0; g < lensgb::MIX_RAY_GROUPS; ++g) rtot += mc.ray_tiles[g];
+        const int kr = p2(rtot, 8 * nsm);
+        for (int g = 0; g < lensgb::MIX_RAY_GROUPS; ++g) {
+            gr.ray_ctas[g] = mc.ray_tiles[g] > 0 ? std::min(1 << kr, 8 * nsm) : 0;
+            if (mc.ray_tiles[g] > 0) rmask |= 1 << g;
+        }
         int ctot = 0, mask = 0, kvar = 0;
         for (int g = 0; g < 8; ++g) ctot += mc.conv_tiles[g];
         const int kc = p2(ctot, 4 * nsm);
@@ -591,7 +597,7 @@ int run_batch(lensgb_server* s, Context* c, int n) {
             }
         }
         const long long key = (long long)mask | ((long long)kvar << 8) | ((long long)kr << 16) |
-                              ((long long)kc << 24);
+                              ((long long)kc << 24) | ((long long)rmask << 32);
         rc = launch_or_replay(s, c, n, key);
         if (rc) return rc;
         s->stats.mixed_batches++;
@@ -835,11 +841,13 @@ int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
     const bool mixed = mixable(s, r);
     BucketKey bk = k;
     if (mixed) {
-        // the bucket's model: the request's profile stack, supersampling,
-        // precision and PSF type on a 1 x 1 placeholder grid (lensgb_image_mixed
-        // takes every system's grid and PSF size from its table)
+        // the bucket's model: the request's profile stack, precision, PSF type
+        // (and, with mixed_grids == 1, supersampling) on a 1 x 1 placeholder
+        // grid; lensgb_image_mixed takes every system's grid, supersampling and
+        // PSF size from its table
         lensgb_model_desc& d = bk.desc;
         d.nx = d.ny = 1;
+        if (s->cfg.mixed_grids >= 2) d.supersampling = 1;
         d.transform_pix2angle[0] = d.transform_pix2angle[3] = 1.0;
         d.transform_pix2angle[1] = d.transform_pix2angle[2] = 0.0;
         d.ra_at_xy_0 = d.dec_at_xy_0 = 0.0;
@@ -887,6 +895,8 @@ int lensgb_server_create(const lensgb_server_config* cfg, lensgb_server** out) {
     if (c.n_streams > 64 || c.max_batch > 65535 || c.contexts_per_bucket > 16)
         return serr(LENSGB_ERR_INVALID, "n_streams <= 64, max_batch <= 65535, "
                                         "contexts_per_bucket <= 16");
+    if (c.mixed_grids < 0 || c.mixed_grids > 2)
+        return serr(LENSGB_ERR_INVALID, "mixed_grids must be 0, 1 or 2");
     lensgb_server* s = new lensgb_server();
     s->cfg = c;
     cudaGetDevice(&s->device);

@@ -576,10 +576,10 @@ __all__ = ["ImageModel", "PSF"]
 
 
 def image_mixed(requests, stream=None):
-    """Images of systems on different pixel grids (and PSF sizes) in one launch
-    sequence (``lensgb_image_mixed``).  ``requests``: list of (image_model,
-    kwargs_lens, kwargs_source, kwargs_lens_light[, psf_kernel]) with one system
-    each; the image models must share their profile lists, supersampling, PSF
+    """Images of systems on different pixel grids, PSF sizes and supersampling
+    factors in one launch sequence (``lensgb_image_mixed``).  ``requests``: list
+    of (image_model, kwargs_lens, kwargs_source, kwargs_lens_light[, psf_kernel])
+    with one system each; the image models must share their profile lists, PSF
     type and precision.  Returns one CUDA tensor per request, each equal to that
     model's ``image_batch`` of the request alone."""
     _device.require_cuda()
@@ -596,12 +596,12 @@ def image_mixed(requests, stream=None):
                      range(len(im.LensLightModel.profile_type_list)))
         k = (tuple(d.lens_codes[:d.n_lens]), tuple(d.source_codes[:d.n_source]),
              tuple(d.deflection_scaling[:d.n_source]), tuple(d.lens_light_codes[:d.n_lens_light]),
-             d.supersampling, d.psf_type, d.precision, d.flux_scaling, d.alpha_scaling)
+             d.psf_type, d.precision, d.flux_scaling, d.alpha_scaling)
         if key is None:
             key = k
         elif k != key:
-            raise ValueError("image_mixed needs models with the same profiles, supersampling, "
-                             "PSF type, precision and scalings")
+            raise ValueError("image_mixed needs models with the same profiles, PSF type, "
+                             "precision and scalings")
         if im._ssc or im._subframe is not None:
             raise ValueError("image_mixed does not take supersampled convolution or sub-frames")
         r = im.pack_params(kl, ks, kll)
@@ -613,6 +613,7 @@ def image_mixed(requests, stream=None):
         g.transform_pix2angle[:] = list(d.transform_pix2angle)
         g.ra_at_xy_0, g.dec_at_xy_0 = d.ra_at_xy_0, d.dec_at_xy_0
         g.kernel_size = d.kernel_size
+        g.supersampling = d.supersampling
         grids.append(g)
         if im._psf_type != _lib.PSF_NONE:
             psfs.append(im.pack_psf(im._kernel if psf is None else psf))

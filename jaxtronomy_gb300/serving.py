@@ -4,9 +4,10 @@
 in liblensgb.so groups requests by bucket (the compiled model of their
 ``ImageModel`` plus noise options), keeps several batches in flight on
 separate CUDA streams, admits new contexts within an HBM budget and replays
-CUDA graphs for repeated batch sizes; with ``mixed_grids`` (the default),
-image requests that differ only in their grid and PSF size share a bucket and
-run through one mixed-grid launch sequence.  Each result equals what
+CUDA graphs for repeated launch shapes; with ``mixed_grids`` (default 2),
+image requests that differ only in their grid, PSF size and supersampling
+factor (``mixed_grids=1``: grid and PSF size) share a bucket and run through one
+mixed-grid launch sequence.  Each result equals what
 ``ImageModel.image_batch`` / ``likelihood_batch`` returns for that request
 alone.  The reference has no serving loop; requests here are single
 ``ImageModel.image`` / ``likelihood_data_given_model`` calls
@@ -67,11 +68,13 @@ class Server:
     """Native serving loop (continuous batching) on the current CUDA device."""
 
     def __init__(self, n_streams=4, max_batch=256, hbm_budget_bytes=4 << 30,
-                 contexts_per_bucket=2, use_graphs=True, mixed_grids=True):
+                 contexts_per_bucket=2, use_graphs=True, mixed_grids=2):
         _device.require_cuda()
+        # mixed_grids: 0 / False (exact-model buckets), 1 / True (grids and PSF
+        # sizes share a bucket) or 2 (also supersampling factors; the default)
         cfg = _lib.ServerConfig(int(n_streams), int(max_batch), int(hbm_budget_bytes),
                                 int(contexts_per_bucket), 1 if use_graphs else 0,
-                                1 if mixed_grids else 0)
+                                int(mixed_grids))
         h = ctypes.c_void_p()
         lib = _lib.load()
         _lib.check(lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)))

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.lensgb_version() == 108
+    assert lib.lensgb_version() == 109
 
 
 def _desc(**kw):
@@ -142,4 +142,6 @@ def test_bulk_and_server_handles_on_the_host():
     assert lib.lensgb_bulk_set_fp32_alpha_max(h, 0.1) == _lib.OK
     assert lib.lensgb_bulk_destroy(h) == _lib.OK
     cfg = _lib.ServerConfig(65, 0, 0, 0, 0)
+    assert lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.ERR_INVALID
+    cfg = _lib.ServerConfig(4, 0, 0, 0, 0, 3)  # mixed_grids must be 0, 1 or 2
     assert lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.ERR_INVALID

@@ -34,14 +34,18 @@ def _model(n, dpix, K, s, precision, psf_type="PIXEL", lens=("EPL", "SHEAR")):
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("psf_type", ["PIXEL", "GAUSSIAN", "NONE"])
-def test_mixed_batch_equals_alone(cuda, precision, psf_type):
+@pytest.mark.parametrize("mixed_s", [False, True])
+def test_mixed_batch_equals_alone(cuda, precision, psf_type, mixed_s):
+    """mixed_s: the systems also differ in supersampling (the run-time-s ray
+    kernel and the per-pixel refine pass)."""
     shapes = [(24, 0.05, 5), (40, 0.04, 11), (33, 0.06, 21), (17, 0.05, 41), (64, 0.03, 9),
               (40, 0.04, 11)]
+    sups = [1, 2, 3, 4, 2, 1] if mixed_s else [2] * len(shapes)
     _, lens, src, ll, _ = W.batch_epl(seed=21, batch=len(shapes), num_pix=24, kernel_size=5)
     reqs, alone = [], []
     rng = np.random.default_rng(4)
     for i, (n, d, K) in enumerate(shapes):
-        im = _model(n, d, K, 2, precision, psf_type)
+        im = _model(n, d, K, sups[i], precision, psf_type)
         kl, ks, kll = W.instance(lens, i), W.instance(src, i), W.instance(ll, i)
         psf = None
         if psf_type == "PIXEL" and i % 2:

@@ -59,7 +59,7 @@ def _submit(srv, models, reqs, psfs, release=None, pinned=False):
     return srv.submit_requests(built)
 
 
-@pytest.mark.parametrize("mixed_grids", [False, True])
+@pytest.mark.parametrize("mixed_grids", [False, True, 2])
 def test_served_results_equal_alone_results(cuda, mixed_grids):
     base, psfs = _stream(60)
     reqs = [r for r in base for _ in range(2)]  # every request twice, released together
@@ -74,7 +74,7 @@ def test_served_results_equal_alone_results(cuda, mixed_grids):
         st = srv.stats()
         assert st["requests_done"] == len(reqs)
         assert st["batches"] < len(reqs)  # requests were batched
-        assert (st["mixed_batches"] > 0) == mixed_grids
+        assert (st["mixed_batches"] > 0) == bool(mixed_grids)
         for r, t in zip(reqs, tickets):
             got = t.result()
             _check(got, _alone(models, r, psfs), mixed_grids)
@@ -82,7 +82,7 @@ def test_served_results_equal_alone_results(cuda, mixed_grids):
             assert 0 <= rel <= adm <= done
 
 
-@pytest.mark.parametrize("mixed_grids", [False, True])
+@pytest.mark.parametrize("mixed_grids", [False, True, 2])
 def test_request_alone_and_in_mix_and_pinned_outputs(cuda, mixed_grids):
     reqs, psfs = _stream(60, seed=11)
     models = _models(reqs)

@@ -657,6 +657,8 @@ def gpu_arm(args):
     def step():
         im32.image_batch(rows=rows_dev, psf_kernels=psf32, out=out32)
 
+    # launch shapes from the autotuner (timed on this workload before the run)
+    tune = im32.autotune(rows=rows_dev, psf_kernels=psf32)
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -743,6 +745,7 @@ def gpu_arm(args):
             s1.record(stream)
             s1.synchronize()
             lat.append(s0.elapsed_time(s1))
+        extra["autotune"] = tune
         extra["fp32_single_request_latency_ms_p50"] = percentile(lat, 0.5)
         extra["fp32_single_request_latency_ms_p99"] = percentile(lat, 0.99)
 

@@ -133,6 +133,34 @@ int lensgb_model_set_subframe(lensgb_model* model, int row0, int col0, int n,
  * those calls into a CUDA graph).  No counterpart in the reference. */
 int lensgb_model_reserve(lensgb_model* model, int n_inst);
 
+/* Launch shapes of a model's image calls.  ppt: pixels per thread of the ray
+ * kernel (1, 2, 4 or 8); conv_tile_rows: output rows per tile of the FP32
+ * convolution (a multiple of 4 in 32..64); 0 keeps the built-in choice.  They
+ * change no result: every pixel's arithmetic is the same under any shape. */
+int lensgb_model_set_tuning(lensgb_model* model, int ppt, int conv_tile_rows);
+
+/* The autotuner: runs the model's image call on the caller's inputs (n_inst
+ * systems, as lensgb_image) with every ray-kernel ppt in {1, 2, 4, 8} and every
+ * convolution tile height in {32, 36, ..., 64} (FP32; FP64 has one shape),
+ * timing each with CUDA events on `stream` (the minimum of three launches after
+ * a warm-up), and keeps the fastest shapes in the model (the tuned ppt applies
+ * to calls of at least a quarter of the tuned call's pixels; smaller calls keep
+ * the built-in choice).  Synchronizes the stream; not for use while a graph is
+ * being captured.  out_dev receives an image of the last run.  No counterpart
+ * in the reference. */
+typedef struct {
+    int ppt;                  /* chosen ray-kernel pixels per thread             */
+    int conv_tile_rows;       /* chosen convolution tile height (0: FP64 / none) */
+    double ray_ms;            /* its prepare + ray + refine time                 */
+    double conv_ms;           /* its convolution time                            */
+    double ray_ms_builtin;    /* the same with the built-in shapes               */
+    double conv_ms_builtin;
+} lensgb_tune_result;
+
+int lensgb_model_autotune(lensgb_model* model, const double* params_dev, int n_inst,
+                          const void* psf_dev, long long psf_stride, void* out_dev, void* stream,
+                          lensgb_tune_result* result);
+
 /* FP32-split models only: pixels whose predicted FP32 error exceeds `tau`
  * (relative, per supersampled ray) are recomputed in FP64.  The prediction is
  * (sum_k I_k |d ln I_k / d beta|) * kappa * (|alpha_x| + |alpha_y|) / I_ray, with

@@ -38,6 +38,7 @@ NO_LENS_LIGHT = 4
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
+    "lensgb_model_set_tuning", "lensgb_model_autotune",
     "lensgb_model_set_subframe",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_image_mixed", "lensgb_convolve",
     "lensgb_loglike",
@@ -91,6 +92,17 @@ class NoiseDesc(ctypes.Structure):
         ("background_rms", ctypes.c_double),
         ("error_map_dev", ctypes.c_void_p),
         ("mask_stride", ctypes.c_longlong),
+    ]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [
+        ("ppt", ctypes.c_int),
+        ("conv_tile_rows", ctypes.c_int),
+        ("ray_ms", ctypes.c_double),
+        ("conv_ms", ctypes.c_double),
+        ("ray_ms_builtin", ctypes.c_double),
+        ("conv_ms_builtin", ctypes.c_double),
     ]
 
 
@@ -176,6 +188,10 @@ def load():
     lib.lensgb_model_set_refine.restype = i
     lib.lensgb_model_refined_pixels.argtypes = [vp, vp, ctypes.POINTER(ll)]
     lib.lensgb_model_refined_pixels.restype = i
+    lib.lensgb_model_set_tuning.argtypes = [vp, i, i]
+    lib.lensgb_model_set_tuning.restype = i
+    lib.lensgb_model_autotune.argtypes = [vp, dp, i, vp, ll, vp, vp, ctypes.POINTER(TuneResult)]
+    lib.lensgb_model_autotune.restype = i
     lib.lensgb_image.argtypes = [vp, dp, i, vp, ll, vp, i, vp]
     lib.lensgb_image.restype = i
     lib.lensgb_image_mixed.argtypes = [vp, dp, i, ctypes.POINTER(SystemGrid), vp, vp, i, vp]

@@ -51,6 +51,8 @@ struct lensgb_model {
     unsigned int* refine_list = nullptr;  // FP32 models: one entry per pixel
     unsigned int* refine_count = nullptr;
     float refine_tau = 2e-5f;             // see lensgb_model_set_refine
+    int tune_ppt = 0, tune_rows = 0;      // launch shapes (lensgb_model_autotune; 0: built-in)
+    long long tune_pix = 0;               // pixels of the tuned call; tuned ppt applies from 1/4 of it
     float refine_kappa = 3e-7f;
     // gradient scratch (lensgb_loglike_grad), grow-only
     int grad_cap = 0;
@@ -234,7 +236,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 109; }
+int lensgb_version(void) { return 110; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -416,6 +418,13 @@ int lensgb_model_reserve(lensgb_model* m, int n_inst) {
 
 // Images of the model's kernel grid (the sub-frame of sub-frame models) into
 // `out`, with the evaluation mask applied before the convolution.
+// The tuned ray-kernel pixels per thread for a call of n_inst systems: a
+// shape tuned on a large batch is kept off much smaller calls (0: built-in).
+static int tuned_ppt(const lensgb_model* m, int n_inst) {
+    const long long pix = (long long)n_inst * m->grid.nx * m->grid.ny;
+    return (m->tune_ppt > 0 && 4 * pix >= m->tune_pix) ? m->tune_ppt : 0;
+}
+
 static int image_core(lensgb_model* m, const double* params, int n_inst, const void* psf,
                       long long psf_stride, void* out, int flags, cudaStream_t s) {
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
@@ -470,14 +479,14 @@ static int image_core(lensgb_model* m, const double* params, int n_inst, const v
     if (rf.tau > 0.f && cudaMemsetAsync(m->refine_count, 0, sizeof(unsigned int), s) != cudaSuccess)
         return check_cuda("refine counter reset");
     launch_raytrace(m->grid, m->st, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, target,
-                    flags, scale, m->desc.precision, rf, s);
+                    flags, scale, m->desc.precision, rf, s, nullptr, 0, tuned_ppt(m, n_inst));
     if ((rc = check_cuda("raytrace launch"))) return rc;
     if (m->sub_mask)
         launch_mask(target, n_inst, m->grid.ny, m->grid.nx, 1, m->sub_mask, m->desc.precision, s);
     if (conv) {
         if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
                         m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
-                        m->desc.precision, s))
+                        m->desc.precision, s, m->tune_rows))
             return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
         if ((rc = check_cuda("convolution launch"))) return rc;
     }
@@ -707,6 +716,119 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     return check_cuda("sub-frame embedding launch");
 }
 
+int lensgb_model_set_tuning(lensgb_model* m, int ppt, int conv_tile_rows) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (!(ppt == 0 || ppt == 1 || ppt == 2 || ppt == 4 || ppt == 8))
+        return fail(LENSGB_ERR_INVALID, "ppt must be 0, 1, 2, 4 or 8");
+    if (!(conv_tile_rows == 0 ||
+          (conv_tile_rows >= 32 && conv_tile_rows <= 64 && conv_tile_rows % 4 == 0)))
+        return fail(LENSGB_ERR_INVALID, "conv_tile_rows must be 0 or a multiple of 4 in 32..64");
+    m->tune_ppt = ppt;
+    m->tune_rows = conv_tile_rows;
+    m->tune_pix = 0;
+    return LENSGB_OK;
+}
+
+}  // extern "C"
+
+// Minimum over three timed launches of `f` (after one untimed) on stream st.
+template <typename F>
+static int time_min_ms(cudaStream_t st, cudaEvent_t a, cudaEvent_t b, F f, double* ms) {
+    int rc = f();
+    if (rc) return rc;
+    double best = 1e300;
+    for (int r = 0; r < 3; ++r) {
+        if (cudaEventRecord(a, st) != cudaSuccess) return check_cuda("autotune event");
+        if ((rc = f())) return rc;
+        if (cudaEventRecord(b, st) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess)
+            return check_cuda("autotune event");
+        float t = 0.f;
+        cudaEventElapsedTime(&t, a, b);
+        best = std::min(best, (double)t);
+    }
+    *ms = best;
+    return LENSGB_OK;
+}
+
+extern "C" {
+
+int lensgb_model_autotune(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                          long long psf_stride, void* out, void* stream,
+                          lensgb_tune_result* result) {
+    if (!m || !result) return fail(LENSGB_ERR_INVALID, "null model or result");
+    if (n_inst <= 0 || n_inst > 65535) return fail(LENSGB_ERR_INVALID, "n_inst must be in 1..65535");
+    if (!out || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+    if (m->hr_conv || m->sub)
+        return fail(LENSGB_ERR_UNSUPPORTED,
+                    "autotune does not take supersampled-convolution or sub-frame models");
+    const bool conv = m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    int rc = check_refine_size(m, n_inst);
+    if (rc) return rc;
+    if ((rc = ensure_scratch(m, n_inst))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        if (a) cudaEventDestroy(a);
+        return check_cuda("autotune event");
+    }
+    memset(result, 0, sizeof *result);
+    // ray stage: prepare + rays + refine into `out` (unconvolved)
+    const int ppts[5] = {0, 1, 2, 4, 8};
+    m->tune_pix = 0;
+    double best_ray = 1e300;
+    int best_ppt = 0;
+    for (int k = 0; k < 5 && rc == LENSGB_OK; ++k) {
+        m->tune_ppt = ppts[k];
+        double t = 0;
+        rc = time_min_ms(st, a, b, [&] {
+            return image_core(m, params, n_inst, psf, psf_stride, out, LENSGB_UNCONVOLVED, st);
+        }, &t);
+        if (rc) break;
+        if (k == 0) result->ray_ms_builtin = t;
+        if (t < best_ray) {
+            best_ray = t;
+            best_ppt = ppts[k];
+        }
+    }
+    m->tune_ppt = rc == LENSGB_OK ? best_ppt : 0;
+    m->tune_pix = (long long)n_inst * m->grid.nx * m->grid.ny;
+    result->ppt = best_ppt;
+    result->ray_ms = best_ray;
+    if (rc == LENSGB_OK && conv) {
+        // convolution stage on the un-convolved images of one full call
+        rc = image_core(m, params, n_inst, psf, psf_stride, out, 0, st);
+        const bool fp32 = m->desc.precision == LENSGB_FP32_SPLIT;
+        double best_conv = 1e300;
+        int best_rows = 0;
+        for (int rows = 0; rc == LENSGB_OK && rows <= (fp32 ? 64 : 0); rows += (rows ? 4 : 32)) {
+            double t = 0;
+            rc = time_min_ms(st, a, b, [&] {
+                if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                                m->desc.kernel_size,
+                                m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
+                                m->desc.precision, st, rows))
+                    return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+                return check_cuda("convolution launch");
+            }, &t);
+            if (rc) break;
+            if (rows == 0) result->conv_ms_builtin = t;
+            if (t < best_conv) {
+                best_conv = t;
+                best_rows = rows;
+            }
+        }
+        m->tune_rows = rc == LENSGB_OK ? best_rows : 0;
+        result->conv_tile_rows = best_rows;
+        result->conv_ms = best_conv;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+}
+
 int lensgb_image_mixed(lensgb_model* m, const double* params, int n_inst,
                        const lensgb_system_grid* grids, const void* psf, void* out, int flags,
                        void* stream) {
@@ -770,7 +892,7 @@ int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const voi
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
     if (launch_conv(in, out, psf, psf_stride, n_inst, m->desc.ny, m->desc.nx,
                     m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
-                    m->desc.precision, (cudaStream_t)stream))
+                    m->desc.precision, (cudaStream_t)stream, m->tune_rows))
         return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
     return check_cuda("convolution launch");
 }
@@ -1167,12 +1289,12 @@ extern "C" int lensgb_image_noalloc(lensgb_model* m, const double* params, int n
     if (rf.tau > 0.f && cudaMemsetAsync(cnt, 0, sizeof(unsigned int), s) != cudaSuccess)
         return check_cuda("refine counter reset");
     launch_raytrace(m->grid, m->st, n_inst, rec_d, rec_f, coef_d, coef_f, conv ? low : out, flags,
-                    scale, m->desc.precision, rf, s);
+                    scale, m->desc.precision, rf, s, nullptr, 0, tuned_ppt(m, n_inst));
     if ((rc = check_cuda("raytrace launch"))) return rc;
     if (conv) {
         if (launch_conv(low, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
                         m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
-                        m->desc.precision, s))
+                        m->desc.precision, s, m->tune_rows))
             return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
         if ((rc = check_cuda("convolution launch"))) return rc;
     }

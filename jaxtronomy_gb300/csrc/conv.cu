@@ -356,8 +356,10 @@ static bool raise_smem_limit(const void* fn, size_t smem) {
 }
 
 static int run_conv_f32(const void* in, void* out, const void* kernel, long long kstride,
-                        int n_inst, int ny, int nx, int K, int edge, cudaStream_t stream) {
-    // tile height 4*TY with TY in 8..16: fewest padded rows, then the tallest tile
+                        int n_inst, int ny, int nx, int K, int edge, cudaStream_t stream,
+                        int tile_rows) {
+    // tile height 4*TY with TY in 8..16: a tuned choice, else fewest padded
+    // rows, then the tallest tile
     int best_ty = 16;
     long long best_waste = -1;
     for (int ty = 16; ty >= 8; --ty) {
@@ -368,6 +370,7 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
             best_ty = ty;
         }
     }
+    if (tile_rows >= 32 && tile_rows <= 64 && tile_rows % 4 == 0) best_ty = tile_rows / 4;
     const int H = 4 * best_ty;
     const int KP = ((K + 7) / 8) * 8;
     const int SW = C32_W + KP + 4;
@@ -568,10 +571,11 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
 }
 
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
-                int ny, int nx, int K, int edge, int precision, cudaStream_t stream) {
+                int ny, int nx, int K, int edge, int precision, cudaStream_t stream,
+                int tile_rows) {
     if (precision == LENSGB_FP64)
         return run_conv<double, 4, 4, 4>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
-    return run_conv_f32(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
+    return run_conv_f32(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream, tile_rows);
 }
 
 }  // namespace lensgb

@@ -27,15 +27,20 @@ int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params,
 // `mixed` (device tables, or null): systems of different grids in one launch
 // of mixed_ctas CTAs looping over the systems' tiles (g then only supplies s);
 // images are laid out at mixed->off.
+// ppt > 0 (uniform launches): pixels per thread instead of the built-in choice.
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,
                     int flags, double out_scale, int precision, const RefineArgs& rf,
-                    cudaStream_t stream, const MixedTab* mixed = nullptr, int mixed_ctas = 0);
+                    cudaStream_t stream, const MixedTab* mixed = nullptr, int mixed_ctas = 0,
+                    int ppt = 0);
 
 // "same"-mode 2-D convolution of n_inst (ny, nx) images with K x K kernels
 // (kernel stride 0 = shared).  edge = 0: zero padding; 1: edge padding.
+// tile_rows (FP32; a multiple of 4 in 32..64, 0: the built-in choice): output
+// rows per CTA tile.
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
-                int ny, int nx, int K, int edge, int precision, cudaStream_t stream);
+                int ny, int nx, int K, int edge, int precision, cudaStream_t stream,
+                int tile_rows = 0);
 
 // Convolution of systems of different sizes (tables in `cm`): one launch of
 // n_ctas CTAs looping over the tiles of the group's systems, whose kernels are

@@ -10,7 +10,7 @@ namespace lensgb {
 int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                     const float* rec_f, const double* coef_d, const float* coef_f, void* out,
                     int flags, double out_scale, int precision, const RefineArgs& rf,
-                    cudaStream_t stream, const MixedTab* mixed, int mixed_ctas) {
+                    cudaStream_t stream, const MixedTab* mixed, int mixed_ctas, int ppt) {
     MixedTab mt;
     if (mixed) {
         mt = *mixed;
@@ -29,7 +29,7 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
     const int a = st.n_lens == 2 ? st.lens[0] : 0, b = st.n_lens == 2 ? st.lens[1] : 0;
 #define LENSGB_VARIANT(C0, C1, NS, NLL)                                                        \
     launch_variant<C0, C1, NS, NLL>(g, st, n_inst, rec_d, rec_f, coef_d, coef_f, out, flags, \
-                                    out_scale, precision, rf, mt, mixed_ctas, stream)
+                                    out_scale, precision, rf, mt, mixed_ctas, ppt, stream)
     if (one_light && st.n_src >= 1 && st.n_src <= 2 && b == LENSGB_LENS_SHEAR) {
         if (a == LENSGB_LENS_EPL) {
             if (st.n_src == 1 && st.n_ll == 1) { LENSGB_VARIANT(LENSGB_LENS_EPL, LENSGB_LENS_SHEAR, 1, 1); return 0; }

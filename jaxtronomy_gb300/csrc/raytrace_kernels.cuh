@@ -472,7 +472,7 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
                            const float* rec_f, const double* coef_d, const float* coef_f,
                            void* out, int flags, double out_scale, int precision,
                            const RefineArgs& rf, const MixedTab& mt, int mixed_ctas,
-                           cudaStream_t stream) {
+                           int ppt_override, cudaStream_t stream) {
     const int threads = 256;
     const long long npix = (long long)g.nx * g.ny;
     // pixels per thread: enough CTAs to fill the GPU several times over
@@ -480,6 +480,7 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
     long long total = npix * (long long)n_inst;
     int ppt = (int)((total + target - 1) / target);
     ppt = ppt < 1 ? 1 : (ppt > 8 ? 8 : ppt);
+    if (ppt_override > 0) ppt = ppt_override;  // a tuned choice (lensgb_model_autotune)
     if (mt.grid) ppt = 1;  // mixed launches: one tile of 256 pixels per CTA
     const long long per_cta = (long long)threads * ppt;
     dim3 grid = mt.grid ? dim3((unsigned)mixed_ctas, 1)

@@ -265,6 +265,37 @@ class ImageModel:
                             range(len(self.LensLightModel.profile_type_list)))
         return model.refined_pixels(_device.stream_handle(stream))
 
+    def autotune(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                 psf_kernels=None, rows=None, stream=None):
+        """Times the batched image call on these (batched) kwargs with every ray-kernel
+        pixels-per-thread and convolution tile height (``lensgb_model_autotune``)
+        and keeps the fastest for this model's later calls.  Returns the chosen
+        shapes and their times next to the built-in ones (ms)."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        if rows is None:
+            rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
+        rows_dev = _device.to_device_f64(rows)
+        B = rows_dev.shape[0]
+        out = torch.empty((B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        kt, kstride, keep = self._psf_arg(psf_kernels, B)
+        kptr = ctypes.c_void_p(0) if kt is None else _device.ptr(kt)
+        res = _lib.TuneResult()
+        _lib.check(_lib.load().lensgb_model_autotune(
+            model.handle, _device.ptr(rows_dev), B, kptr, kstride, _device.ptr(out),
+            _device.stream_handle(stream), ctypes.byref(res)))
+        del keep
+        return {n: getattr(res, n) for n, _ in _lib.TuneResult._fields_}
+
+    def set_tuning(self, ppt=0, conv_tile_rows=0):
+        """Launch shapes of this model's image calls (0: the built-in choice)."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        _lib.check(_lib.load().lensgb_model_set_tuning(model.handle, int(ppt),
+                                                       int(conv_tile_rows)))
+
     def psf_elements(self):
         """PSF values per system in the C-ABI layout (0 for psf_type NONE)."""
         if self._kernel is None:

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.lensgb_version() == 109
+    assert lib.lensgb_version() == 110
 
 
 def _desc(**kw):
@@ -145,3 +145,20 @@ def test_bulk_and_server_handles_on_the_host():
     assert lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.ERR_INVALID
     cfg = _lib.ServerConfig(4, 0, 0, 0, 0, 3)  # mixed_grids must be 0, 1 or 2
     assert lib.lensgb_server_create(ctypes.byref(cfg), ctypes.byref(h)) == _lib.ERR_INVALID
+
+
+def test_tuning_arguments_are_validated_without_a_gpu():
+    lib = _lib.load()
+    assert ctypes.sizeof(_lib.TuneResult) == 2 * 4 + 4 * 8
+    rc, h, _ = _create(_desc())
+    assert rc == _lib.OK
+    assert lib.lensgb_model_set_tuning(h, 3, 0) == _lib.ERR_INVALID
+    assert lib.lensgb_model_set_tuning(h, 2, 30) == _lib.ERR_INVALID
+    assert lib.lensgb_model_set_tuning(h, 2, 66) == _lib.ERR_INVALID
+    assert lib.lensgb_model_set_tuning(h, 4, 60) == _lib.OK
+    assert lib.lensgb_model_set_tuning(h, 0, 0) == _lib.OK
+    res = _lib.TuneResult()
+    assert lib.lensgb_model_autotune(h, None, 0, None, 0, None, None,
+                                     ctypes.byref(res)) == _lib.ERR_INVALID
+    assert lib.lensgb_model_autotune(h, None, 4, None, 0, None, None, None) == _lib.ERR_INVALID
+    lib.lensgb_model_destroy(h)

@@ -186,6 +186,22 @@ int lensgb_image(lensgb_model* model, const double* params_dev, int n_inst,
                  const void* psf_dev, long long psf_stride, void* out_dev, int flags,
                  void* stream);
 
+/* lensgb_image with HOST buffers: params_host (n_inst rows), psf_host (as
+ * lensgb_image's psf_dev, psf_stride elements apart or shared) and out_host
+ * are host memory.  Parameters and PSFs go up and the batch is computed on
+ * `stream`, in n_chunks chunks (0: 1); each chunk's images are copied to
+ * out_host on a second stream owned by the model, overlapping the next chunk
+ * and the next call's work (alternate calls use two device image slots).
+ * `stream` does not wait for these copies: lensgb_image_host_wait makes it
+ * wait for every copy queued so far (or synchronize the device) before out_host
+ * is read.  Page-locked host buffers give the overlap (pageable ones work, with
+ * synchronous copies).  Results equal lensgb_image's.  No reference
+ * counterpart (the reference returns device arrays that the caller copies). */
+int lensgb_image_host(lensgb_model* model, const double* params_host, int n_inst,
+                      const void* psf_host, long long psf_stride, void* out_host, int flags,
+                      int n_chunks, void* stream);
+int lensgb_image_host_wait(lensgb_model* model, void* stream);
+
 /* lensgb_image for systems of different pixel grids in one launch sequence:
  * grids[i] (host) gives system i's grid, PSF size and (optionally)
  * supersampling factor; the model supplies the profile stack, PSF type,

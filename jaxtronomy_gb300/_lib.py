@@ -38,7 +38,8 @@ NO_LENS_LIGHT = 4
 SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
-    "lensgb_model_set_tuning", "lensgb_model_autotune",
+    "lensgb_model_set_tuning", "lensgb_model_autotune", "lensgb_image_host",
+    "lensgb_image_host_wait",
     "lensgb_model_set_subframe",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_image_mixed", "lensgb_convolve",
     "lensgb_loglike",
@@ -188,6 +189,10 @@ def load():
     lib.lensgb_model_set_refine.restype = i
     lib.lensgb_model_refined_pixels.argtypes = [vp, vp, ctypes.POINTER(ll)]
     lib.lensgb_model_refined_pixels.restype = i
+    lib.lensgb_image_host.argtypes = [vp, vp, i, vp, ll, vp, i, i, vp]
+    lib.lensgb_image_host.restype = i
+    lib.lensgb_image_host_wait.argtypes = [vp, vp]
+    lib.lensgb_image_host_wait.restype = i
     lib.lensgb_model_set_tuning.argtypes = [vp, i, i]
     lib.lensgb_model_set_tuning.restype = i
     lib.lensgb_model_autotune.argtypes = [vp, dp, i, vp, ll, vp, vp, ctypes.POINTER(TuneResult)]

@@ -38,6 +38,18 @@ struct lensgb_model {
     // table copy, before which the host buffer is not rewritten
     size_t mix_host_cap = 0;
     unsigned char* mix_host = nullptr;
+    // lensgb_image_host: device staging (grow-only; two image slots used by
+    // alternate calls, so a call's image copies overlap the next call's work),
+    // the copy-back stream, one event per chunk and one per slot
+    size_t pipe_rows_cap = 0, pipe_psf_cap = 0, pipe_out_cap[2] = {0, 0};
+    void* pipe_rows = nullptr;
+    void* pipe_psf = nullptr;
+    void* pipe_out[2] = {nullptr, nullptr};
+    int pipe_slot = 0;
+    cudaStream_t pipe_stream = nullptr;
+    cudaEvent_t pipe_ev[16] = {};
+    cudaEvent_t pipe_slot_ev[2] = {};
+    cudaEvent_t pipe_wait_ev = nullptr;
     cudaEvent_t mix_ev = nullptr;
     bool mix_ev_pending = false;
     StackDesc st;
@@ -402,6 +414,19 @@ int lensgb_model_destroy(lensgb_model* m) {
         cudaEventDestroy(m->mix_ev);
     }
     cudaFreeHost(m->mix_host);
+    if (m->pipe_stream) {
+        cudaStreamSynchronize(m->pipe_stream);
+        cudaStreamDestroy(m->pipe_stream);
+    }
+    for (cudaEvent_t e : m->pipe_ev)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : m->pipe_slot_ev)
+        if (e) cudaEventDestroy(e);
+    if (m->pipe_wait_ev) cudaEventDestroy(m->pipe_wait_ev);
+    cudaFree(m->pipe_rows);
+    cudaFree(m->pipe_psf);
+    cudaFree(m->pipe_out[0]);
+    cudaFree(m->pipe_out[1]);
     delete m;
     return LENSGB_OK;
 }
@@ -714,6 +739,118 @@ int lensgb_image(lensgb_model* m, const double* params, int n_inst, const void* 
     launch_embed(m->sub_out, out, n_inst, m->grid.nx, m->sub_r0, m->sub_c0, m->desc.ny,
                  m->desc.nx, m->desc.precision, s);
     return check_cuda("sub-frame embedding launch");
+}
+
+// Grow-only device buffer.
+static int grow_buffer(void** p, size_t* cap, size_t need) {
+    if (need <= *cap) return LENSGB_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    if (cudaMalloc(p, need) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(LENSGB_ERR_OOM, "device allocation of host-call staging failed");
+    }
+    *cap = need;
+    return LENSGB_OK;
+}
+
+int lensgb_image_host(lensgb_model* m, const double* params, int n_inst, const void* psf,
+                      long long psf_stride, void* out, int flags, int n_chunks, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!out || (!params && m->st.n_params > 0))
+        return fail(LENSGB_ERR_INVALID, "null params or output pointer");
+    const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
+    if (conv && !psf) return fail(LENSGB_ERR_INVALID, "null PSF kernel pointer");
+    if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
+    if (n_chunks < 0 || n_chunks > 16) return fail(LENSGB_ERR_INVALID, "n_chunks must be in 0..16");
+    if (n_chunks == 0) n_chunks = 1;
+    if (n_chunks > n_inst) n_chunks = n_inst;
+    const size_t esz = m->desc.precision == LENSGB_FP64 ? 8 : 4;
+    const size_t P = (size_t)m->st.n_params;
+    const size_t npix = (size_t)m->desc.nx * m->desc.ny;
+    const size_t k_el = conv ? (size_t)(m->desc.kernel_size * m->desc.kernel_size +
+                                        m->desc.low_res_kernel_size * m->desc.low_res_kernel_size)
+                             : 0;
+    const size_t psf_el = !conv ? 0 : (psf_stride > 0 ? (size_t)psf_stride * n_inst : k_el);
+    if (!m->pipe_stream &&
+        cudaStreamCreateWithFlags(&m->pipe_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return check_cuda("copy stream");
+    for (cudaEvent_t& e : m->pipe_ev)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return check_cuda("copy event");
+    for (cudaEvent_t& e : m->pipe_slot_ev)
+        if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return check_cuda("copy event");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int slot = m->pipe_slot;
+    // this slot's images of two calls ago must have left before it is rewritten
+    // (growing a buffer frees it: wait for the copies first)
+    if (cudaStreamWaitEvent(st, m->pipe_slot_ev[slot], 0) != cudaSuccess)
+        return check_cuda("stream order");
+    if (npix * n_inst * esz > m->pipe_out_cap[slot] &&
+        cudaEventSynchronize(m->pipe_slot_ev[slot]) != cudaSuccess)
+        return check_cuda("copy event");
+    int rc;
+    if ((rc = grow_buffer(&m->pipe_rows, &m->pipe_rows_cap, P * n_inst * 8 + 8)) ||
+        (rc = grow_buffer(&m->pipe_psf, &m->pipe_psf_cap, psf_el * esz + 16)) ||
+        (rc = grow_buffer(&m->pipe_out[slot], &m->pipe_out_cap[slot], npix * n_inst * esz)))
+        return rc;
+    m->pipe_slot ^= 1;
+    unsigned char* rows_d = (unsigned char*)m->pipe_rows;
+    unsigned char* psf_d = (unsigned char*)m->pipe_psf;
+    unsigned char* out_d = (unsigned char*)m->pipe_out[slot];
+    // a shared PSF goes up once
+    if (conv && psf_stride == 0 &&
+        cudaMemcpyAsync(psf_d, psf, k_el * esz, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return check_cuda("PSF copy");
+    for (int c = 0; c < n_chunks; ++c) {
+        const int i0 = (int)((long long)n_inst * c / n_chunks);
+        const int i1 = (int)((long long)n_inst * (c + 1) / n_chunks);
+        const int nc = i1 - i0;
+        if (nc <= 0) continue;
+        if (cudaMemcpyAsync(rows_d + (size_t)i0 * P * 8, params + (size_t)i0 * P, (size_t)nc * P * 8,
+                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return check_cuda("parameter copy");
+        const unsigned char* kp = psf_d;
+        if (conv && psf_stride > 0) {
+            const size_t off = (size_t)i0 * psf_stride * esz;
+            if (cudaMemcpyAsync(psf_d + off, (const unsigned char*)psf + off,
+                                (size_t)nc * psf_stride * esz, cudaMemcpyHostToDevice,
+                                st) != cudaSuccess)
+                return check_cuda("PSF copy");
+            kp = psf_d + off;
+        }
+        rc = lensgb_image(m, (const double*)(rows_d + (size_t)i0 * P * 8), nc, conv ? kp : nullptr,
+                          psf_stride, out_d + (size_t)i0 * npix * esz, flags, stream);
+        if (rc) return rc;
+        if (cudaEventRecord(m->pipe_ev[c], st) != cudaSuccess ||
+            cudaStreamWaitEvent(m->pipe_stream, m->pipe_ev[c], 0) != cudaSuccess ||
+            cudaMemcpyAsync((unsigned char*)out + (size_t)i0 * npix * esz,
+                            out_d + (size_t)i0 * npix * esz, (size_t)nc * npix * esz,
+                            cudaMemcpyDeviceToHost, m->pipe_stream) != cudaSuccess)
+            return check_cuda("image copy");
+    }
+    // the copies stay in flight on the copy stream (lensgb_image_host_wait)
+    if (cudaEventRecord(m->pipe_slot_ev[slot], m->pipe_stream) != cudaSuccess)
+        return check_cuda("copy event");
+    return LENSGB_OK;
+}
+
+int lensgb_image_host_wait(lensgb_model* m, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (!m->pipe_stream) return LENSGB_OK;
+    if (!m->pipe_wait_ev &&
+        cudaEventCreateWithFlags(&m->pipe_wait_ev, cudaEventDisableTiming) != cudaSuccess)
+        return check_cuda("copy event");
+    if (cudaEventRecord(m->pipe_wait_ev, m->pipe_stream) != cudaSuccess ||
+        cudaStreamWaitEvent((cudaStream_t)stream, m->pipe_wait_ev, 0) != cudaSuccess)
+        return check_cuda("stream order");
+    return LENSGB_OK;
 }
 
 int lensgb_model_set_tuning(lensgb_model* m, int ppt, int conv_tile_rows) {

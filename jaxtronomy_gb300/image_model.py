@@ -389,6 +389,58 @@ class ImageModel:
         del keep
         return out
 
+    def host_wait(self, stream=None):
+        """Makes ``stream`` wait for every image copy of earlier host-output calls."""
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        _lib.check(_lib.load().lensgb_image_host_wait(model.handle,
+                                                      _device.stream_handle(stream)))
+
+    def _launch_host(self, model, rows, flags, psf_kernels, out, stream, n_chunks=0):
+        # host rows / PSFs / images: lensgb_image_host copies the images of each
+        # chunk back while the next chunk is computed
+        rows_h = rows if isinstance(rows, torch.Tensor) else torch.as_tensor(
+            np.ascontiguousarray(rows, dtype=np.float64))
+        if rows_h.device.type != "cpu":
+            raise ValueError("host output needs host parameter rows")
+        rows_h = rows_h.to(torch.float64).contiguous()
+        B = rows_h.shape[0]
+        if (out.dtype != self._dtype or not out.is_contiguous()
+                or out.numel() < B * self._nx * self._ny):
+            raise ValueError("out must be a contiguous %s tensor of shape (B, %d, %d)"
+                             % (self._dtype, self._nx, self._ny))
+        kh, kstride = None, 0
+        if self._psf_type != _lib.PSF_NONE:
+            K = int(self._kernel.shape[0])
+            if psf_kernels is None:
+                kh = torch.as_tensor(self.pack_psf(self._kernel))
+            else:
+                arr = psf_kernels if isinstance(psf_kernels, torch.Tensor) else torch.as_tensor(
+                    np.asarray(psf_kernels))
+                if arr.device.type != "cpu":
+                    raise ValueError("host output needs host PSF kernels")
+                if tuple(arr.shape[-2:]) != (K, K) or arr.dim() not in (2, 3) or (
+                        arr.dim() == 3 and arr.shape[0] != B):
+                    raise ValueError("psf kernels must have shape (%d, %d) or (%d, %d, %d)"
+                                     % (K, K, B, K, K))
+                per_system = arr.dim() == 3
+                if self._low_kernel_size:
+                    a3 = arr.double().numpy().reshape(-1, K, K)
+                    arr = torch.as_tensor(np.stack([self.pack_psf(a) for a in a3]))
+                kh = arr
+                kstride = self.psf_elements() if per_system else 0
+            kh = kh.to(self._dtype).contiguous()
+        kptr = ctypes.c_void_p(0) if kh is None else ctypes.c_void_p(kh.data_ptr())
+        _lib.check(_lib.load().lensgb_image_host(
+            model.handle, ctypes.c_void_p(rows_h.data_ptr()), B, kptr, kstride,
+            ctypes.c_void_p(out.data_ptr()), flags, int(n_chunks),
+            _device.stream_handle(stream)))
+        # the host buffers must outlive the copies queued on the stream (two
+        # calls may be in flight)
+        self._host_keep = (getattr(self, "_host_keep", (None,))[-1], (rows_h, kh))
+        return out
+
     def image_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                     unconvolved=False, source_add=True, lens_light_add=True, psf_kernels=None,
                     out=None, stream=None, rows=None):
@@ -396,17 +448,24 @@ class ImageModel:
         Returns a (B, ny, nx) CUDA tensor in the model precision.  ``psf_kernels``
         may give one (K, K) kernel or one per system (B, K, K) in place of the
         model PSF (normalised by the caller).  ``rows`` may pass pre-packed
-        parameter rows (host array or CUDA tensor, see :meth:`pack_params`)."""
+        parameter rows (host array or CUDA tensor, see :meth:`pack_params`).
+        With a host tensor ``out`` (and host rows / PSFs) the call runs
+        ``lensgb_image_host``: the images are copied back on a second stream,
+        overlapping the next call's work (page-locked buffers give the overlap);
+        ``out`` is complete after :meth:`host_wait` and a synchronization of the
+        stream (or a device synchronization)."""
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
                             range(len(self.LensLightModel.profile_type_list)))
         if rows is None:
             rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
-        rows_dev = _device.to_device_f64(rows)
-        B = rows_dev.shape[0]
         flags = ((_lib.UNCONVOLVED if unconvolved else 0)
                  | (0 if source_add else _lib.NO_SOURCE)
                  | (0 if lens_light_add else _lib.NO_LENS_LIGHT))
+        if isinstance(out, torch.Tensor) and out.device.type == "cpu":
+            return self._launch_host(model, rows, flags, psf_kernels, out, stream)
+        rows_dev = _device.to_device_f64(rows)
+        B = rows_dev.shape[0]
         return self._launch(model, rows_dev, B, flags, psf_kernels, out, stream)
 
     # ------------------------------------------------------------------ reference API

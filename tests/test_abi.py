@@ -162,3 +162,14 @@ def test_tuning_arguments_are_validated_without_a_gpu():
                                      ctypes.byref(res)) == _lib.ERR_INVALID
     assert lib.lensgb_model_autotune(h, None, 4, None, 0, None, None, None) == _lib.ERR_INVALID
     lib.lensgb_model_destroy(h)
+
+
+def test_host_call_arguments_are_validated_without_a_gpu():
+    lib = _lib.load()
+    rc, h, _ = _create(_desc())
+    assert rc == _lib.OK
+    assert lib.lensgb_image_host(None, None, 1, None, 0, None, 0, 0, None) == _lib.ERR_INVALID
+    assert lib.lensgb_image_host(h, None, -1, None, 0, None, 0, 0, None) == _lib.ERR_INVALID
+    assert lib.lensgb_image_host(h, None, 2, None, 0, None, 0, 0, None) == _lib.ERR_INVALID
+    assert lib.lensgb_image_host(h, None, 0, None, 0, None, 0, 0, None) == _lib.OK
+    lib.lensgb_model_destroy(h)

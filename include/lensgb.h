@@ -274,6 +274,27 @@ typedef struct {
     long long mask_stride;        /* elements between systems' masks (0 = shared)  */
 } lensgb_noise_desc;
 
+/* ImageLinearFit's linear amplitude solve (image_linear_solve.py:98-228,
+ * 229-341; de_lens.get_param_WLS, de_lens.py:8-38) for n_inst systems of the
+ * model's grid: response_dev holds n_linear unit-amplitude component images
+ * (component j of system i at (j * n_inst + i) * ny * nx, model precision: the
+ * lensgb_image of that component alone with amp = 1).  With the data-based
+ * covariance C_D(d) of `noise` (noise map, or max(d, 0)/exposure + bkg^2) and
+ * the mask, M = A W A^T and R = A W d are solved for the amplitudes
+ * (param_dev, n_inst x n_linear) when cond(M) < 5/eps, else they are 0; the
+ * model image sum_j param_j A_j (0 outside the mask) goes to image_out_dev and
+ * its log-likelihood (model-based C_D, as lensgb_loglike) to logl_dev.
+ * LENSGB_LINEAR_INVERSE (source_marg): M^-1 goes to cov_dev (n_inst x n x n,
+ * may be NULL otherwise) and 1/2 log det(M^-1) is added (-1e15 if singular);
+ * LENSGB_LINEAR_POSITIVE (check_positive_flux): 1e8 is subtracted when an
+ * amplitude is negative.  n_linear <= LENSGB_LINEAR_MAX. */
+#define LENSGB_LINEAR_MAX 8
+#define LENSGB_LINEAR_INVERSE 1
+#define LENSGB_LINEAR_POSITIVE 2
+int lensgb_linear_solve(const lensgb_model* model, const void* response_dev, int n_linear,
+                        int n_inst, const lensgb_noise_desc* noise, int flags, double* param_dev,
+                        double* cov_dev, void* image_out_dev, double* logl_dev, void* stream);
+
 /* ImageModel.likelihood_data_given_model for n_inst systems
  * (image_model.py:163-221): simulates the images into image_out_dev (caller
  * buffer, same layout as lensgb_image's output) and writes one FP64

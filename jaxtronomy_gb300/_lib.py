@@ -39,7 +39,7 @@ SYMBOLS = [
     "lensgb_model_create", "lensgb_model_destroy", "lensgb_model_param_count",
     "lensgb_model_reserve", "lensgb_model_set_refine", "lensgb_model_refined_pixels",
     "lensgb_model_set_tuning", "lensgb_model_autotune", "lensgb_image_host",
-    "lensgb_image_host_wait",
+    "lensgb_image_host_wait", "lensgb_linear_solve",
     "lensgb_model_set_subframe",
     "lensgb_image", "lensgb_image_noalloc", "lensgb_image_mixed", "lensgb_convolve",
     "lensgb_loglike",
@@ -155,6 +155,8 @@ class ServerStats(ctypes.Structure):
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
+LINEAR_MAX, LINEAR_INVERSE, LINEAR_POSITIVE = 8, 1, 2
+
 
 class LensgbError(RuntimeError):
     def __init__(self, code, msg):
@@ -191,6 +193,9 @@ def load():
     lib.lensgb_model_refined_pixels.restype = i
     lib.lensgb_image_host.argtypes = [vp, vp, i, vp, ll, vp, i, i, vp]
     lib.lensgb_image_host.restype = i
+    lib.lensgb_linear_solve.argtypes = [vp, vp, i, i, ctypes.POINTER(NoiseDesc), i, vp, vp, vp,
+                                        vp, vp]
+    lib.lensgb_linear_solve.restype = i
     lib.lensgb_image_host_wait.argtypes = [vp, vp]
     lib.lensgb_image_host_wait.restype = i
     lib.lensgb_model_set_tuning.argtypes = [vp, i, i]

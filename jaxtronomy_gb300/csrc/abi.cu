@@ -248,7 +248,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 110; }
+int lensgb_version(void) { return 111; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -1063,6 +1063,42 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     launch_loglike(image_out, n_inst, (long long)m->desc.nx * m->desc.ny, a, logl,
                    m->desc.precision, (cudaStream_t)stream);
     return check_cuda("likelihood launch");
+}
+
+int lensgb_linear_solve(const lensgb_model* m, const void* A, int n_linear, int n_inst,
+                        const lensgb_noise_desc* nd, int flags, double* param, double* cov,
+                        void* image_out, double* logl, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0 || n_inst > 65535) return fail(LENSGB_ERR_INVALID, "n_inst must be in 0..65535");
+    if (n_linear < 1 || n_linear > LENSGB_LINEAR_MAX)
+        return fail(LENSGB_ERR_INVALID, "n_linear must be in 1..8");
+    if (flags & ~(LENSGB_LINEAR_INVERSE | LENSGB_LINEAR_POSITIVE))
+        return fail(LENSGB_ERR_INVALID, "unknown linear-solve flags");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!A || !param || !image_out || !logl)
+        return fail(LENSGB_ERR_INVALID, "null response, parameter, image or logL pointer");
+    if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
+    if (!nd->noise_map_dev && !nd->exposure_map_dev && !(nd->exposure_time > 0))
+        return fail(LENSGB_ERR_INVALID, "exposure time must be positive without a noise map");
+    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0 ||
+        nd->mask_stride < 0)
+        return fail(LENSGB_ERR_INVALID, "negative stride");
+    LoglikeArgs a;
+    a.data = nd->data_dev;
+    a.data_stride = nd->data_stride;
+    a.mask = nd->mask_dev;
+    a.mask_stride = nd->mask_stride;
+    a.noise_map = nd->noise_map_dev;
+    a.noise_stride = nd->noise_stride;
+    a.exposure = nd->exposure_map_dev;
+    a.exposure_stride = nd->exposure_stride;
+    a.exposure_time = nd->exposure_time;
+    a.background_rms = nd->background_rms;
+    a.error_map = nd->error_map_dev;
+    launch_linear_solve(A, n_linear, n_inst, (long long)m->desc.nx * m->desc.ny, a, flags, param,
+                        (flags & LENSGB_LINEAR_INVERSE) ? cov : nullptr, image_out, logl,
+                        m->desc.precision, (cudaStream_t)stream);
+    return check_cuda("linear solve launch");
 }
 
 static int ensure_grad_scratch(lensgb_model* m, int n_inst) {

@@ -136,6 +136,12 @@ struct LoglikeArgs {
 int launch_loglike(const void* model, int n_inst, long long npix, const LoglikeArgs& a,
                    double* out, int precision, cudaStream_t stream);
 
+// Linear amplitude solve (linear.cu): see lensgb_linear_solve.
+constexpr int LIN_MAX = LENSGB_LINEAR_MAX;
+int launch_linear_solve(const void* A, int n_lin, int n_inst, long long npix, const LoglikeArgs& a,
+                        int flags, double* param, double* cov, void* image, double* logl,
+                        int precision, cudaStream_t stream);
+
 // Adjoint gradient of logL (grad.cu): FP64 models whose lens stack holds only
 // EPL / SHEAR and whose light profiles are Sersic.  `image` is the model image
 // of the same params (lensgb_image output), rec_d / coef_d its prepared

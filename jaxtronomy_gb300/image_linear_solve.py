@@ -1,0 +1,161 @@
+"""ImageModel with the linear amplitude solve (``ImSim/image_linear_solve.py:11-740``).
+
+Every light profile of this library (SERSIC, SERSIC_ELLIPSE) has one linear
+amplitude, ``amp``.  For a batch of systems the unit-amplitude convolved image
+of each linear component is one ``lensgb_image`` launch of that component alone
+(``linear_response_matrix``, ``image_linear_solve.py:362-456``); one
+``lensgb_linear_solve`` launch then forms and solves the weighted least-squares
+system of every system (``de_lens.get_param_WLS``, ``de_lens.py:8-38``), writes
+the model images and their log-likelihoods (``likelihood_data_given_model``,
+``:229-341``).  Point sources are not supported (the reference's point-source
+response rows are therefore absent).
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device, _lib
+from .image_model import ImageModel
+
+
+class ImageLinearFit(ImageModel):
+    """Linear version of :class:`ImageModel` (``image_linear_solve.py:11-97``)."""
+
+    def __init__(self, data_class, psf_class, lens_model_class=None, source_model_class=None,
+                 lens_light_model_class=None, point_source_class=None, extinction_class=None,
+                 kwargs_numerics=None, likelihood_mask=None, psf_error_map_bool_list=None,
+                 kwargs_pixelbased=None):
+        super().__init__(data_class, psf_class, lens_model_class, source_model_class,
+                         lens_light_model_class, point_source_class, extinction_class,
+                         kwargs_numerics, likelihood_mask, psf_error_map_bool_list,
+                         kwargs_pixelbased)
+        self._n_src = len(self.SourceModel.profile_type_list)
+        self._n_ll = len(self.LensLightModel.profile_type_list)
+        if self._n_src + self._n_ll > _lib.LINEAR_MAX:
+            raise ValueError("at most %d linear light components are supported"
+                             % _lib.LINEAR_MAX)
+
+    # ------------------------------------------------------------------ linear parameters
+    def num_param_linear(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                         kwargs_ps=None):
+        """``image_linear_solve.py:342-360``: one amplitude per light profile."""
+        return self._n_src + self._n_ll
+
+    def linear_param_from_kwargs(self, kwargs_source, kwargs_lens_light, kwargs_ps=None):
+        """``image_linear_solve.py:484-528``: the amplitudes, sources first."""
+        return [kw["amp"] for kw in (kwargs_source or [])] + [
+            kw["amp"] for kw in (kwargs_lens_light or [])]
+
+    def update_linear_kwargs(self, param, kwargs_lens, kwargs_source, kwargs_lens_light,
+                             kwargs_ps=None):
+        """``image_linear_solve.py:458-482``: writes the amplitudes into the kwargs
+        (in place, as the reference's LightModel.update_linear does) and returns them."""
+        p = np.asarray(param, dtype=float)
+        for i, kw in enumerate(kwargs_source or []):
+            kw["amp"] = p[..., i]
+        for i, kw in enumerate(kwargs_lens_light or []):
+            kw["amp"] = p[..., self._n_src + i]
+        return kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps
+
+    def check_positive_flux(self, kwargs_source, kwargs_lens_light, kwargs_ps=None):
+        """``image_linear_solve.py:598-618``: True when no amplitude is negative."""
+        amps = np.asarray(self.linear_param_from_kwargs(kwargs_source, kwargs_lens_light),
+                          dtype=float)
+        return bool(np.all(amps >= 0))
+
+    # ------------------------------------------------------------------ response
+    def linear_response_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                              unconvolved=False, psf_kernels=None, stream=None):
+        """(n_linear, B, ny, nx) CUDA tensor of unit-amplitude component images:
+        each source lensed alone, each lens-light profile alone, amp = 1."""
+        n_lens = len(self.LensModel.lens_model_list)
+        unit = lambda kws: [dict(kw, amp=1.0) for kw in (kws or [])]  # noqa: E731
+        ks, kll = unit(kwargs_source), unit(kwargs_lens_light)
+        jobs = [((range(n_lens), [j], []), True) for j in range(self._n_src)]
+        jobs += [(([], [], [j]), False) for j in range(self._n_ll)]
+        flags = _lib.UNCONVOLVED if unconvolved else 0
+        rows = [self.pack_params(kwargs_lens, ks, kll, lens_idx=list(li), src_idx=si,
+                                 ll_idx=lli, lensed=lensed)
+                for (li, si, lli), lensed in jobs]
+        # the batch of the whole kwargs (a lens-light row alone does not see batched lens
+        # kwargs): rows of one system are repeated
+        B = max(r.shape[0] for r in rows)
+        A = torch.empty((len(jobs), B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        for c, ((li, si, lli), lensed) in enumerate(jobs):
+            r = rows[c] if rows[c].shape[0] == B else np.repeat(rows[c], B, axis=0)
+            model = self._model(li, si, lli, lensed=lensed)
+            self._launch(model, _device.to_device_f64(r), B, flags, psf_kernels, A[c], stream)
+        return A
+
+    def linear_response_matrix(self, kwargs_lens, kwargs_source, kwargs_lens_light,
+                               kwargs_ps=None, kwargs_extinction=None, kwargs_special=None,
+                               unconvolved=False):
+        """``image_linear_solve.py:362-456``: (num_param, num_data_evaluate) response
+        of one system (the unit-amplitude images at the mask pixels)."""
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        A = self.linear_response_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                       unconvolved=unconvolved)
+        a = A[:, 0].to(torch.float64).cpu().numpy()
+        return np.nan_to_num(a[:, self.likelihood_mask])
+
+    # ------------------------------------------------------------------ solve
+    def likelihood_linear_batch(self, kwargs_lens=None, kwargs_source=None,
+                                kwargs_lens_light=None, data=None, source_marg=False,
+                                check_positive_flux=False, psf_kernels=None, stream=None):
+        """Linear solve of B systems: ((B,) logL, (B, n) amplitudes, (B, ny, nx) model
+        images, (B, n, n) inverse normal matrices or None) as CUDA tensors (FP64;
+        images in the model precision)."""
+        A = self.linear_response_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                       psf_kernels=psf_kernels, stream=stream)
+        n, B = A.shape[0], A.shape[1]
+        nt = self._noise_tensors(data)
+        nd = self._noise_desc(nt)
+        param = torch.empty((B, n), dtype=torch.float64, device="cuda")
+        cov = torch.empty((B, n, n), dtype=torch.float64, device="cuda") if source_marg else None
+        image = torch.empty((B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        logl = torch.empty((B,), dtype=torch.float64, device="cuda")
+        flags = ((_lib.LINEAR_INVERSE if source_marg else 0)
+                 | (_lib.LINEAR_POSITIVE if check_positive_flux else 0))
+        model = self._model(range(len(self.LensModel.lens_model_list)), range(self._n_src),
+                            range(self._n_ll))
+        _lib.check(_lib.load().lensgb_linear_solve(
+            model.handle, _device.ptr(A), n, B, ctypes.byref(nd), flags, _device.ptr(param),
+            ctypes.c_void_p(0) if cov is None else _device.ptr(cov), _device.ptr(image),
+            _device.ptr(logl), _device.stream_handle(stream)))
+        return logl, param, image, cov
+
+    def image_linear_solve(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
+                           kwargs_ps=None, kwargs_extinction=None, kwargs_special=None,
+                           inv_bool=False):
+        """``image_linear_solve.py:98-228``: (model image, model error, covariance of
+        the amplitudes or None, amplitudes); the amplitudes are written into the
+        kwargs as the reference does."""
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        logl, param, image, cov = self.likelihood_linear_batch(
+            kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=inv_bool)
+        p = param[0].cpu().numpy()
+        self.update_linear_kwargs(p, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps)
+        return (image[0].to(torch.float64).cpu().numpy(), 0,
+                None if cov is None else cov[0].cpu().numpy(), p)
+
+    def likelihood_data_given_model(self, kwargs_lens=None, kwargs_source=None,
+                                    kwargs_lens_light=None, kwargs_ps=None,
+                                    kwargs_extinction=None, kwargs_special=None,
+                                    source_marg=False, linear_prior=None,
+                                    check_positive_flux=False):
+        """``image_linear_solve.py:229-341``: (logL, amplitudes) after the linear solve."""
+        if kwargs_extinction:
+            raise ValueError("Extinction is not implemented")
+        if linear_prior is not None:
+            raise ValueError("linear_prior (marginalization_new) is not supported; use "
+                             "source_marg with flat priors")
+        logl, param, _, _ = self.likelihood_linear_batch(
+            kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=source_marg,
+            check_positive_flux=check_positive_flux)
+        p = param[0].cpu().numpy()
+        self.update_linear_kwargs(p, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps)
+        return float(logl[0].cpu()), p

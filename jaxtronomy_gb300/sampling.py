@@ -9,6 +9,9 @@ and ``prepare_logL_func`` (``Sampling/sampler.py:215-250``) vectorises it with
 takes the whole ensemble and evaluates it as one batched ``lensgb_loglike``
 launch; ``prepare_logL_func("gpu", module.logL)`` returns that batched function.
 
+With the linear solver (the reference's default) ``ImageLikelihood`` runs
+``ImageLinearFit``'s batched solve (``image_linear_solve.py``).
+
 ``Param`` restates the sampled-parameter bookkeeping of lenstronomy's ``Param``
 (``lenstronomy/Sampling/parameters.py``, not vendored; the reference's
 LikelihoodModule takes an instance of it, ``likelihood.py:147-148``) for the
@@ -20,6 +23,7 @@ import numpy as np
 import torch
 
 from .data import PSF, ImageData
+from .image_linear_solve import ImageLinearFit
 from .image_model import ImageModel
 from .lens_model import LensModel
 from .light_model import LightModel
@@ -74,9 +78,9 @@ class Param:
     ``kwargs_fixed_*`` dict is one sampled argument, ordered by list (lens,
     source, lens light), then profile, then ``param_names``.  Bounds default to
     the profiles' ``lower_limit_default`` / ``upper_limit_default``; entries of
-    ``kwargs_lower_*`` / ``kwargs_upper_*`` replace them.  The linear amplitude
-    solve is not built, so ``linear_solver`` must be False (every ``amp`` is then
-    sampled or fixed like any other parameter)."""
+    ``kwargs_lower_*`` / ``kwargs_upper_*`` replace them.  With ``linear_solver``
+    (the default, as in lenstronomy) every light profile's ``amp`` is left to the
+    linear solve: it is not sampled and reads 1 unless fixed otherwise."""
 
     def __init__(self, kwargs_model, kwargs_fixed_lens=None, kwargs_fixed_source=None,
                  kwargs_fixed_lens_light=None, kwargs_fixed_ps=None, kwargs_fixed_special=None,
@@ -85,9 +89,6 @@ class Param:
                  kwargs_lower_extinction=None, kwargs_upper_lens=None, kwargs_upper_source=None,
                  kwargs_upper_lens_light=None, kwargs_upper_ps=None, kwargs_upper_special=None,
                  kwargs_upper_extinction=None, linear_solver=True, **constraints):
-        if linear_solver:
-            raise ValueError("the linear amplitude solve is not built in this library; "
-                             "use linear_solver=False and sample (or fix) 'amp'")
         for name, v in (("kwargs_fixed_ps", kwargs_fixed_ps),
                         ("kwargs_fixed_special", kwargs_fixed_special),
                         ("kwargs_fixed_extinction", kwargs_fixed_extinction),
@@ -102,7 +103,7 @@ class Param:
         for name, v in constraints.items():
             if v:
                 raise ValueError("parameter constraint %s is not supported by this build" % name)
-        self.linear_solver = False
+        self.linear_solver = bool(linear_solver)
         self._lists = _model_lists(kwargs_model)
         fixed = {"lens": kwargs_fixed_lens, "source": kwargs_fixed_source,
                  "lens_light": kwargs_fixed_lens_light}
@@ -124,6 +125,10 @@ class Param:
                     raise ValueError("kwargs_%s_%s needs one dict per %s profile"
                                      % (what, tag, tag))
             self._fixed[tag] = [dict(d) for d in fx]
+            if self.linear_solver and tag != "lens":
+                for d in self._fixed[tag]:
+                    d.setdefault("amp", 1.0)
+            fx = self._fixed[tag]
             for i, name in enumerate(names):
                 for p in table[name]:
                     if p in fx[i]:
@@ -179,13 +184,14 @@ class ImageLikelihood:
         if multi_band_type != "single-band":
             raise ValueError("Type %s is not supported in JAXtronomy! Use lenstronomy instead."
                              % multi_band_type)
-        if linear_solver:
-            raise ValueError("the linear amplitude solve is not built in this library; "
-                             "use linear_solver=False")
-        if source_marg:
-            raise ValueError("source_marg needs the linear solve, which is not built")
-        if check_positive_flux:
-            raise ValueError("check positive flux is not supported")
+        if linear_prior is not None:
+            raise ValueError("linear_prior (marginalization_new) is not supported; use "
+                             "source_marg with flat priors")
+        if (source_marg or check_positive_flux) and not linear_solver:
+            raise ValueError("source_marg and check_positive_flux need the linear solver")
+        self._linear = bool(linear_solver)
+        self._source_marg = bool(source_marg)
+        self._check_positive_flux = bool(check_positive_flux)
         lists = _model_lists(kwargs_model)
         kwargs_data, kwargs_psf, kwargs_numerics = multi_band_list[0][:3]
         data = ImageData(**kwargs_data)
@@ -193,9 +199,10 @@ class ImageLikelihood:
         kn = dict(kwargs_numerics or {})
         kn.setdefault("precision", precision)
         mask = None if image_likelihood_mask_list is None else image_likelihood_mask_list[0]
-        self.imSim = ImageModel(data, psf, LensModel(lists["lens"]),
-                                LightModel(lists["source"]), LightModel(lists["lens_light"]),
-                                kwargs_numerics=kn, likelihood_mask=mask)
+        cls = ImageLinearFit if self._linear else ImageModel
+        self.imSim = cls(data, psf, LensModel(lists["lens"]), LightModel(lists["source"]),
+                         LightModel(lists["lens_light"]), kwargs_numerics=kn,
+                         likelihood_mask=mask)
         self._model_type = self.imSim.type
 
     @property
@@ -206,16 +213,26 @@ class ImageLikelihood:
                    stream=None, **kwargs):
         """(B,) FP64 log-likelihoods of batched kwargs, NaN replaced by -1e15
         (``image_likelihood.py:95``)."""
-        logl = self.imSim.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
-                                           stream=stream)
+        if self._linear:
+            logl, _, _, _ = self.imSim.likelihood_linear_batch(
+                kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=self._source_marg,
+                check_positive_flux=self._check_positive_flux, stream=stream)
+        else:
+            logl = self.imSim.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                               stream=stream)
         return torch.nan_to_num(logl, nan=-(10.0 ** 15))
 
     def logL(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None, kwargs_ps=None,
              kwargs_special=None, kwargs_extinction=None, **kwargs):
-        """(logL, linear parameters) of one system; no linear solve, so None."""
+        """(logL, linear parameters) of one system (None without the linear solver)."""
         if kwargs_extinction:
             raise ValueError("Extinction is not implemented")
-        return float(self.logL_batch(kwargs_lens, kwargs_source, kwargs_lens_light)[0]), None
+        if not self._linear:
+            return float(self.logL_batch(kwargs_lens, kwargs_source, kwargs_lens_light)[0]), None
+        logl, param, _, _ = self.imSim.likelihood_linear_batch(
+            kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=self._source_marg,
+            check_positive_flux=self._check_positive_flux)
+        return float(torch.nan_to_num(logl, nan=-(10.0 ** 15))[0]), param[0].cpu().numpy()
 
 
 def _prior_terms(prior, kwargs_list):

@@ -15,6 +15,7 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
   hyp2f1.npz    hyp2f1_lopez_temme_8 at the reference's own test points
   images.npz    ImageModel.image and likelihood_data_given_model on small scenes
   bulk.npz      LensModelBulk.ray_shooting through many deflectors
+  linear.npz    ImageLinearFit: linear amplitude solve, model image, logL
 """
 
 import json
@@ -349,6 +350,88 @@ def gen_bulk(rng):
     return cases
 
 
+def gen_linear():
+    """ImageLinearFit (image_linear_solve.py) on small scenes: amplitudes, model
+    image, inverse normal matrix (source_marg) and logL."""
+    import copy
+
+    from jaxtronomy.ImSim.image_linear_solve import ImageLinearFit
+    from jaxtronomy.Data.imaging_data import ImageData
+    from jaxtronomy.LensModel.lens_model import LensModel
+    from jaxtronomy.LightModel.light_model import LightModel
+    from jaxtronomy_gb300 import workloads as W
+
+    rng = np.random.default_rng(20240603)
+    out = []
+    sie = [{"theta_E": 1.0, "e1": 0.1, "e2": -0.05, "center_x": 0.02, "center_y": 0.0},
+           {"gamma1": 0.02, "gamma2": -0.01}]
+    epl = [{"theta_E": 1.1, "gamma": 2.05, "e1": -0.08, "e2": 0.06, "center_x": 0.0,
+            "center_y": 0.03}, {"gamma1": -0.015, "gamma2": 0.025}]
+    src = {"amp": 3.0, "R_sersic": 0.2, "n_sersic": 2.0, "e1": 0.05, "e2": 0.1,
+           "center_x": 0.05, "center_y": -0.02}
+    src2 = {"amp": 1.0, "R_sersic": 0.12, "n_sersic": 1.2, "e1": -0.1, "e2": 0.0,
+            "center_x": -0.1, "center_y": 0.08}
+    ll_s = {"amp": 5.0, "R_sersic": 0.8, "n_sersic": 3.0, "center_x": 0.0, "center_y": 0.0}
+    ll_e = {"amp": 4.0, "R_sersic": 0.9, "n_sersic": 3.5, "e1": 0.05, "e2": 0.02,
+            "center_x": 0.01, "center_y": 0.0}
+    cases = [
+        dict(tag="sie_gauss_s2", n=30, dpix=0.08, s=2, lens=["SIE", "SHEAR"], kl=sie,
+             src=["SERSIC_ELLIPSE"], ks=[src], ll=["SERSIC"], kll=[ll_s],
+             psf={"psf_type": "GAUSSIAN", "fwhm": 0.15, "truncation": 3}, mask=False,
+             marg=False, pos=False, sign=1.0),
+        dict(tag="epl_pixel_two_sources_mask_marg", n=36, dpix=0.06, s=1, lens=["EPL", "SHEAR"],
+             kl=epl, src=["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], ks=[src, src2],
+             ll=["SERSIC_ELLIPSE"], kll=[ll_e], dsl=[1.0, 0.7],
+             psf={"psf_type": "PIXEL", "kernel_point_source": W.gaussian_pixel_kernel(0.12, 0.06, 7)},
+             mask=True, marg=True, pos=False, sign=1.0),
+        dict(tag="sie_negative_source_positive_check", n=30, dpix=0.08, s=2, lens=["SIE", "SHEAR"],
+             kl=sie, src=["SERSIC_ELLIPSE"], ks=[src], ll=["SERSIC"], kll=[ll_s],
+             psf={"psf_type": "GAUSSIAN", "fwhm": 0.15, "truncation": 3}, mask=False,
+             marg=False, pos=True, sign=-1.0),
+        dict(tag="degenerate_two_identical_sources", n=24, dpix=0.1, s=1, lens=["SIE", "SHEAR"],
+             kl=sie, src=["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], ks=[src, dict(src)],
+             ll=["SERSIC"], kll=[ll_s], psf={"psf_type": "NONE"}, mask=False, marg=True,
+             pos=False, sign=1.0),
+    ]
+    for c in cases:
+        g = W.grid_kwargs(c["n"], c["dpix"])
+        # data: the model with the given amplitudes (the source scaled by `sign`) + noise
+        sim = _image_model(c["n"], c["dpix"], c["s"], c["psf"], c["lens"], c["src"], c["ll"],
+                           deflection_scaling=c.get("dsl"))
+        ks_sim = copy.deepcopy(c["ks"])
+        ks_sim[0]["amp"] = ks_sim[0]["amp"] * c["sign"]
+        img = np.asarray(sim.image(c["kl"], ks_sim, c["kll"]))
+        data = img + rng.normal(0, 0.02, img.shape)
+        mask = np.ones((c["n"], c["n"]))
+        if c["mask"]:
+            yy, xx = np.mgrid[:c["n"], :c["n"]]
+            mask = (((xx - c["n"] / 2) ** 2 + (yy - c["n"] / 2) ** 2) < (0.42 * c["n"]) ** 2
+                    ).astype(float)
+        data_class = ImageData(image_data=data, exposure_time=500.0, background_rms=0.02, **g)
+        im = ImageLinearFit(data_class, refshim.PSF(**c["psf"]), LensModel(c["lens"]),
+                            LightModel(c["src"], deflection_scaling_list=c.get("dsl")),
+                            LightModel(c["ll"]), kwargs_numerics={"supersampling_factor": c["s"]},
+                            likelihood_mask=mask)
+        kl, ks, kll = copy.deepcopy(c["kl"]), copy.deepcopy(c["ks"]), copy.deepcopy(c["kll"])
+        model, _, cov, param = im.image_linear_solve(kl, ks, kll, kwargs_ps=[], inv_bool=c["marg"])
+        kl, ks, kll = copy.deepcopy(c["kl"]), copy.deepcopy(c["ks"]), copy.deepcopy(c["kll"])
+        logl, _ = im.likelihood_data_given_model(kl, ks, kll, kwargs_ps=[], source_marg=c["marg"],
+                                                 check_positive_flux=c["pos"])
+        rec = {k: c[k] for k in ("tag", "n", "dpix", "s", "lens", "kl", "src", "ks", "ll", "kll",
+                                 "marg", "pos")}
+        rec["dsl"] = c.get("dsl")
+        rec["psf"] = {k: v for k, v in c["psf"].items() if k != "kernel_point_source"}
+        rec["logL"] = float(logl)
+        rec["bkg"], rec["exp_time"] = 0.02, 500.0
+        rec["data"], rec["mask"], rec["model"] = data, mask, np.asarray(model)
+        rec["param"] = np.asarray(param, float)
+        rec["cov"] = None if cov is None else np.asarray(cov, float)
+        if c["psf"]["psf_type"] == "PIXEL":
+            rec["kernel"] = np.asarray(c["psf"]["kernel_point_source"])
+        out.append(rec)
+    return out
+
+
 def _save(path, arrays, meta):
     np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
 
@@ -386,8 +469,17 @@ def main(reference_root):
             arrays["%s_%d" % (k, i)] = c.pop(k)
         meta.append(c)
     _save(os.path.join(HERE, "bulk.npz"), arrays, meta)
+    lin = gen_linear()
+    arrays, meta = {}, []
+    for i, c in enumerate(lin):
+        for k in ("data", "mask", "model", "param", "cov", "kernel"):
+            v = c.pop(k, None)
+            if v is not None:
+                arrays["%s_%d" % (k, i)] = v
+        meta.append(c)
+    _save(os.path.join(HERE, "linear.npz"), arrays, meta)
     print("wrote", len(cases), "profile cases,", len(scenes), "image scenes,", len(bulk),
-          "bulk cases")
+          "bulk cases,", len(lin), "linear-solve cases")
 
 
 if __name__ == "__main__":

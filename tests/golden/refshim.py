@@ -87,6 +87,25 @@ def _make_jnp():
         else:
             setattr(jnp, name, _wrap(fn))
     jnp.ndarray = np.ndarray
+    # jax.numpy.linalg returns non-finite values for a singular matrix where
+    # numpy raises; the reference filters them (de_lens.py:72-99)
+    linalg = types.ModuleType("jax.numpy.linalg")
+    for name in dir(np.linalg):
+        if not name.startswith("__"):
+            setattr(linalg, name, getattr(np.linalg, name))
+
+    def _nan_on_singular(fn):
+        def inner(a, *rest):
+            try:
+                return fn(a, *rest)
+            except np.linalg.LinAlgError:
+                shape = np.shape(rest[0]) if rest else np.shape(a)
+                return np.full(shape, np.nan)
+        return inner
+
+    linalg.inv = _nan_on_singular(np.linalg.inv)
+    linalg.solve = _nan_on_singular(np.linalg.solve)
+    jnp.linalg = linalg
     return jnp
 
 
@@ -412,6 +431,22 @@ class Image2SourceMapping:
             if k is None or k == i:
                 flux = flux + func.function(x - scal[i] * ax, y - scal[i] * ay, **kwargs_source[i])
         return flux
+
+    def image_flux_split(self, x, y, kwargs_lens, kwargs_source, kwargs_special=None):
+        """Unit-amplitude response of every linear source component at its lensed
+        position: the source model's functions_split at theta - scale_i * alpha."""
+        scal = getattr(self._source, "deflection_scaling_list", None)
+        if scal is None:
+            bx, by = self._lens.ray_shooting(x, y, kwargs_lens)
+            return self._source.functions_split(bx, by, kwargs_source)
+        ax, ay = self._lens.alpha(x, y, kwargs_lens)
+        response, n = [], 0
+        for i in range(len(self._source.func_list)):
+            r, m = self._source.functions_split(x - scal[i] * ax, y - scal[i] * ay, kwargs_source,
+                                                k=i)
+            response += r
+            n += m
+        return response, n
 
 
 def _exporter():

@@ -70,3 +70,31 @@ def bulk_cases():
             c[k] = d["%s_%d" % (k, i)]
         out.append(c)
     return out
+
+
+def linear_cases():
+    """ImageLinearFit cases: kwargs, data, mask and the reference's amplitudes,
+    model image, inverse normal matrix (source_marg) and logL."""
+    d, meta = load("linear.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        for k in ("data", "mask", "model", "param", "cov", "kernel"):
+            key = "%s_%d" % (k, i)
+            c[k] = d[key] if key in d.files else None
+        out.append(c)
+    return out
+
+
+def linear_scene(c):
+    """The oracle scene of a linear-solve case."""
+    g = grid_kwargs(c["n"], c["dpix"])
+    sc = dict(nx=c["n"], ny=c["n"], supersampling_factor=c["s"], psf_type=c["psf"]["psf_type"],
+              lens_model_list=c["lens"], source_light_model_list=c["src"],
+              lens_light_model_list=c["ll"], deflection_scaling_list=c["dsl"], **g)
+    if c["psf"]["psf_type"] == "PIXEL":
+        sc["kernel"] = c["kernel"]
+    elif c["psf"]["psf_type"] == "GAUSSIAN":
+        sc["fwhm"] = c["psf"]["fwhm"]
+        sc["truncation"] = c["psf"]["truncation"]
+    return sc

@@ -101,3 +101,46 @@ def test_image_likelihood_wrapper(cuda):
     assert logl == im.likelihood_data_given_model(kw["kwargs_lens"], kw["kwargs_source"],
                                                   kw["kwargs_lens_light"])
     assert il.num_data == N * N
+
+
+def test_linear_solver_likelihood_module(cuda):
+    """linear_solver=True (the reference's default): amplitudes are solved per
+    walker; the batched logL equals ImageLinearFit per vector (bit for bit) and the
+    oracle's linear solve (1e-10)."""
+    from jaxtronomy_gb300.image_linear_solve import ImageLinearFit
+    from oracle import linear as olinear
+
+    joint, _, args, im, data, kern, g = _setup(n_walkers=8)
+    param = S.Param(MODEL, kwargs_fixed_lens=[{}, {"ra_0": 0.0, "dec_0": 0.0}])
+    n = param.num_param()[0]
+    rng = np.random.default_rng(9)
+    lo, hi = param.param_limits()
+    truth = param.kwargs2args(*[[{k: v for k, v in kw.items() if k != "amp"} for kw in lst]
+                                for lst in _truth_kwargs()])
+    a = truth + 1e-3 * rng.standard_normal((8, n))
+    lm = S.LikelihoodModule(joint, MODEL, param, source_marg=True)
+    got = lm.logL_batch(a)
+    fit = ImageLinearFit(J.ImageData(data, exposure_time=1000.0, background_rms=0.01, **g),
+                         J.PSF("PIXEL", kernel_point_source=kern),
+                         J.LensModel(MODEL["lens_model_list"]),
+                         J.LightModel(MODEL["source_light_model_list"]),
+                         J.LightModel(MODEL["lens_light_model_list"]),
+                         kwargs_numerics={"supersampling_factor": SS})
+    for j in range(8):
+        kw = param.args2kwargs(a[j])
+        l1, _ = fit.likelihood_data_given_model(kw["kwargs_lens"], kw["kwargs_source"],
+                                                kw["kwargs_lens_light"], source_marg=True)
+        assert got[j] == l1
+    kw = param.args2kwargs(a[2])
+    scene = dict(nx=N, ny=N, supersampling_factor=SS, psf_type="PIXEL", kernel=kern, **MODEL, **g)
+    o, _, _, _ = olinear.likelihood(scene, kw["kwargs_lens"], kw["kwargs_source"],
+                                    kw["kwargs_lens_light"], data, np.ones_like(data), 0.01,
+                                    exposure_time=1000.0, source_marg=True)
+    assert abs(got[2] - o) <= 1e-10 * abs(o), (got[2], o)
+
+
+def _truth_kwargs():
+    _, lens, src, ll, _ = W.gradient_batch(seed=5, batch=1, num_pix=N, delta_pix=DPIX,
+                                           supersampling=SS, kernel_size=K)
+    kl = W.instance(lens, 0)
+    return kl, W.instance(src, 0), W.instance(ll, 0)

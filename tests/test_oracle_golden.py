@@ -112,3 +112,20 @@ def test_bulk_equals_single_plane_sum():
     sx, sy = lens.ray_shooting(case["lens_list"], case["x"], case["y"], case["kwargs"])
     np.testing.assert_allclose(bx, sx, rtol=1e-13, atol=1e-15)
     np.testing.assert_allclose(by, sy, rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("case", golden_io.linear_cases(), ids=lambda c: c["tag"])
+def test_linear_solve_matches_reference(case):
+    """oracle.linear against the reference's ImageLinearFit (amplitudes, model
+    image, inverse normal matrix, logL incl. marginalisation and positivity)."""
+    from oracle import linear
+
+    sc = golden_io.linear_scene(case)
+    logl, param, model, cov = linear.likelihood(
+        sc, case["kl"], case["ks"], case["kll"], case["data"], case["mask"], case["bkg"],
+        exposure_time=case["exp_time"], source_marg=case["marg"], check_positive_flux=case["pos"])
+    np.testing.assert_allclose(param, case["param"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(model, case["model"], rtol=1e-10, atol=1e-12 * np.abs(model).max())
+    assert abs(logl - case["logL"]) <= 1e-10 * abs(case["logL"])
+    if case["cov"] is not None:
+        np.testing.assert_allclose(cov, case["cov"], rtol=1e-9, atol=1e-14)

@@ -44,9 +44,15 @@ def test_param_round_trip_single_and_batched():
                                                     kj["kwargs_lens_light"]), a[j])
 
 
+def test_linear_solver_leaves_amplitudes_to_the_solve():
+    p = S.Param(MODEL, kwargs_fixed_lens=FIXED_LENS)  # linear_solver=True, as in lenstronomy
+    n, names = p.num_param()
+    assert n == 4 + 2 + 6 + 4 and not any(nm.startswith("amp_") for nm in names)
+    kw = p.args2kwargs(np.zeros(n))
+    assert kw["kwargs_source"][0]["amp"] == 1.0 and kw["kwargs_lens_light"][0]["amp"] == 1.0
+
+
 def test_param_rejects_unsupported():
-    with pytest.raises(ValueError):
-        S.Param(MODEL)  # linear_solver defaults to True, as in lenstronomy
     with pytest.raises(ValueError):
         S.Param(MODEL, linear_solver=False, kwargs_fixed_ps=[{"ra_image": [0.0]}])
     with pytest.raises(ValueError):
@@ -79,4 +85,7 @@ def test_likelihood_module_rejects_unsupported_terms():
     with pytest.raises(ValueError):
         S.ImageLikelihood([[{}, {}, {}]], "multi-linear", MODEL, linear_solver=False)
     with pytest.raises(ValueError):
-        S.ImageLikelihood([[{}, {}, {}]], "single-band", MODEL)  # linear_solver=True
+        S.ImageLikelihood([[{}, {}, {}]], "single-band", MODEL, linear_prior=1.0)
+    with pytest.raises(ValueError):
+        S.ImageLikelihood([[{}, {}, {}]], "single-band", MODEL, source_marg=True,
+                          linear_solver=False)

@@ -441,11 +441,12 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     }
 
 
-def sampler_section(steps, seed=1003, n_walkers=256):
+def sampler_section(steps, seed=1003, n_walkers=256, linear_solver=False):
     """Sampler ensemble: LikelihoodModule.logL_batch over n_walkers parameter
     vectors of the gradient workload's system (120^2, s=2, K=21, EPL+SHEAR,
-    Sersic source and lens light, 22 sampled parameters) -- one batched launch
-    -- against the same module called one vector at a time."""
+    Sersic source and lens light; 22 sampled parameters, or 20 with the linear
+    solver fitting the two amplitudes) -- one batched launch sequence -- against
+    the same module called one vector at a time."""
     import numpy as np
     import jaxtronomy_gb300 as J
     from jaxtronomy_gb300 import sampling as S, workloads as W
@@ -472,7 +473,7 @@ def sampler_section(steps, seed=1003, n_walkers=256):
                                   {"supersampling_factor": S2}]],
              "multi_band_type": "single-band"}
     param = S.Param(model_lists, kwargs_fixed_lens=[{}, {"ra_0": 0.0, "dec_0": 0.0}],
-                    linear_solver=False)
+                    linear_solver=linear_solver)
     lm = S.LikelihoodModule(joint, model_lists, param)
     f = S.prepare_logL_func("gpu", lm.logL)
     truth = param.kwargs2args(kl, ks, kll)
@@ -493,7 +494,8 @@ def sampler_section(steps, seed=1003, n_walkers=256):
         lm.logL(args[j])
     single = (time.perf_counter() - t0) / n1
     return {
-        "workload": "sampler_ensemble_epl_120x120_s2_psf21",
+        "workload": "sampler_ensemble_epl_120x120_s2_psf21" + ("_linear_solve" if linear_solver
+                                                                  else ""),
         "walkers": n_walkers, "sampled_params": int(truth.size),
         "ms_per_ensemble": batched * 1e3, "evaluations_per_s": n_walkers / batched,
         "one_vector_per_call_ms": single * 1e3, "one_vector_per_call_evaluations_per_s": 1.0 / single,
@@ -855,6 +857,7 @@ def gpu_arm(args):
         if not args.no_grad:
             extra["gradient"] = gradient_section(args.steps)
             extra["sampler"] = sampler_section(args.steps)
+            extra["sampler_linear_solve"] = sampler_section(args.steps, linear_solver=True)
 
         # --- serving stream (continuous batching)
         if args.serve_requests > 0:

@@ -1139,7 +1139,7 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
                     "sub-frames");
     if (!grad_supported(m->st))
         return fail(LENSGB_ERR_UNSUPPORTED,
-                    "the likelihood gradient supports lens stacks of EPL and SHEAR and Sersic "
+                    "the likelihood gradient supports lens stacks of EPL, SIE, NIE and SHEAR and Sersic "
                     "light profiles, with at most 64 parameters per system");
     if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
     if (!image_out || !logl || !grad) return fail(LENSGB_ERR_INVALID, "null output pointer");

@@ -113,6 +113,40 @@ __device__ __forceinline__ D5 dsqrt(const D5& a) {
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
+__device__ __forceinline__ D5 datan(const D5& a) {
+    D5 r;
+    r.v = atan(a.v);
+    const double g = 1.0 / (1.0 + a.v * a.v);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 datanh(const D5& a) {
+    D5 r;
+    r.v = atanh(a.v);
+    const double g = 1.0 / (1.0 - a.v * a.v);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+
+// (phi, q) = ellipticity2phi_q(e1, e2) (param_util.py:88-99): dq/de and dphi/de
+// (zero at e = 0 and where the axis-ratio clamp c < 0.9999 holds it).
+__device__ __forceinline__ void dphiq_de(double e1, double e2, double& dq1, double& dq2,
+                                         double& dp1, double& dp2) {
+    const double cc2 = e1 * e1 + e2 * e2;
+    const double cc = sqrt(cc2);
+    dq1 = dq2 = dp1 = dp2 = 0.0;
+    if (cc > 0.0) {
+        if (cc < 0.9999) {
+            const double dqdc = -2.0 / ((1.0 + cc) * (1.0 + cc));
+            dq1 = dqdc * e1 / cc;
+            dq2 = dqdc * e2 / cc;
+        }
+        dp1 = -e2 / (2.0 * cc2);
+        dp2 = e1 / (2.0 * cc2);
+    }
+}
 
 // EPL deflection (epl.py:179-200,366-394) and its Jacobian with respect to
 // (theta_E, gamma, e1, e2, center_x, center_y): J[0][k] = d alpha_x / d p_k,
@@ -208,6 +242,60 @@ __device__ void epl_alpha_grad(const double* rec, const double* F, const double*
     }
 }
 
+// NIE / SIE deflection (nie.py:86-107,182-200,280-294; sie.py:105-124 with
+// s_scale = 1e-10) and its Jacobian with respect to (theta_E, e1, e2, [s_scale,]
+// center_x, center_y).  b = theta_E sqrt(q) (the product-average conversion
+// times sqrt((1 + q^2) / 2)), s = s_scale / sqrt(q); the major-axis formula is
+// differentiated in (b, s, q, x1, y1), with q frozen where the q < 1 clamp
+// replaces it.
+__device__ void nie_alpha_grad(int code, const double* rec, const double* a, double dx, double dy,
+                               double& ax, double& ay, double J[2][6]) {
+    const double b = rec[2], s = rec[3], qc = rec[4], c = rec[5], sn = rec[6];
+    const bool nie = code == LENSGB_LENS_NIE;
+    const double e1 = a[1], e2 = a[2];
+    const double cc = sqrt(e1 * e1 + e2 * e2);
+    const double q = (1.0 - fmin(cc, 0.9999)) / (1.0 + fmin(cc, 0.9999));
+    const bool clamped = q >= 1.0;
+    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5 B = dvar(b, 0), S = dvar(s, 1), Q = clamped ? dconst(qc) : dvar(qc, 2);
+    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5 Q2 = Q * Q;
+    const D5 psi = dsqrt(Q2 * (S * S + X1 * X1) + Y1 * Y1);
+    const D5 sq = dsqrt(1.0 + (-1.0) * Q2);
+    const D5 bs = B * dinv(sq);
+    const D5 fx = bs * datan(sq * X1 * dinv(psi + S));
+    const D5 fy = bs * datanh(sq * Y1 * dinv(psi + Q2 * S));
+    ax = fx.v * c - fy.v * sn;
+    ay = fx.v * sn + fy.v * c;
+    double dA[2][5];
+    for (int k = 0; k < 5; ++k) {
+        dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
+        dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
+    }
+    // d alpha / d phi = Rot(phi) [ (-fy, fx) + J_maj (y1, -x1) ]
+    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    double dq1, dq2, dp1, dp2;
+    dphiq_de(e1, e2, dq1, dq2, dp1, dp2);
+    const double theta_E = a[0], s_scale = nie ? a[3] : 0.0000000001;
+    const double sqq = sqrt(q);
+    const double dbdq = theta_E / (2.0 * sqq), dsdq = -s_scale / (2.0 * q * sqq);
+    const int co = nie ? 4 : 3;
+    for (int i = 0; i < 2; ++i) {
+        const double aph = i == 0 ? aphx : aphy;
+        const double aq = dA[i][0] * dbdq + dA[i][1] * dsdq + dA[i][2];
+        J[i][0] = dA[i][0] * sqq;
+        J[i][1] = aq * dq1 + aph * dp1;
+        J[i][2] = aq * dq2 + aph * dp2;
+        if (nie) J[i][3] = dA[i][1] / sqq;
+        J[i][co] = -(i == 0 ? jdx0 : jdx1);
+        J[i][co + 1] = -(i == 0 ? jdy0 : jdy1);
+    }
+}
+
 // SHEAR (shear.py:39-53) and its Jacobian w.r.t. (gamma1, gamma2, ra_0, dec_0).
 __device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, double dy,
                                                  double& ax, double& ay, double J[2][6]) {
@@ -283,8 +371,14 @@ __device__ void sersic_grad(int code, const double* rec, const double* a, double
 constexpr int GRAD_MAXP = 64;
 constexpr int GRAD_MAX_LENSP = 32;
 
-__device__ __forceinline__ int lens_np(int code) {
-    return code == LENSGB_LENS_EPL ? 6 : (code == LENSGB_LENS_SHEAR ? 4 : 0);
+__device__ __host__ __forceinline__ int lens_np(int code) {
+    switch (code) {
+        case LENSGB_LENS_EPL: return 6;
+        case LENSGB_LENS_NIE: return 6;
+        case LENSGB_LENS_SIE: return 5;
+        case LENSGB_LENS_SHEAR: return 4;
+        default: return 0;
+    }
 }
 
 // dF_n/dt of the EPL series coefficients (hyp2f1_util.py:156-166 with
@@ -419,6 +513,8 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                     if (code == LENSGB_LENS_EPL)
                         epl_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
                                        P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE)
+                        nie_alpha_grad(code, r, P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else
                         shear_alpha_grad(r, ddx, ddy, ax, ay, J);
                     axs += ax;
@@ -493,10 +589,10 @@ bool grad_supported(const StackDesc& st) {
     if (st.n_params > GRAD_MAXP) return false;
     int lp = 0;
     for (int p = 0; p < st.n_lens; ++p) {
-        if (st.lens[p] != LENSGB_LENS_EPL && st.lens[p] != LENSGB_LENS_SHEAR) return false;
-        lp += st.lens[p] == LENSGB_LENS_EPL ? 6 : 4;
-        if (p > 0 && st.lens_off[p] != st.lens_off[p - 1] + (st.lens[p - 1] == LENSGB_LENS_EPL ? 6 : 4))
-            return false;
+        const int np = lens_np(st.lens[p]);
+        if (np == 0) return false;
+        lp += np;
+        if (p > 0 && st.lens_off[p] != st.lens_off[p - 1] + lens_np(st.lens[p - 1])) return false;
     }
     return lp <= GRAD_MAX_LENSP;
 }

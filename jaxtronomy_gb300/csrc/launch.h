@@ -143,7 +143,7 @@ int launch_linear_solve(const void* A, int n_lin, int n_inst, long long npix, co
                         int precision, cudaStream_t stream);
 
 // Adjoint gradient of logL (grad.cu): FP64 models whose lens stack holds only
-// EPL / SHEAR and whose light profiles are Sersic.  `image` is the model image
+// EPL / SIE / NIE / SHEAR and whose light profiles are Sersic.  `image` is the model image
 // of the same params (lensgb_image output), rec_d / coef_d its prepared
 // records.  Scratch: dcoef (n_inst x n_epl x EPL_NMAX), psf_flip (n_inst x K^2),
 // gm and glow (n_inst x npix), partial (n_inst x grad_chunks x n_params).

@@ -135,12 +135,36 @@ def test_autograd_function(cuda):
     np.testing.assert_array_equal(r.grad.cpu().numpy(), (w[:, None] * grad).cpu().numpy())
 
 
+@pytest.mark.parametrize("lens", ["SIE", "NIE"])
+def test_isothermal_lenses_match_central_differences(cuda, lens):
+    """SIE / NIE + SHEAR: the NIE major-axis formula differentiated in (b, s, q,
+    x1, y1) and chained to (theta_E, e1, e2, [s_scale,] centre)."""
+    model, lens_kw, src, ll, kern = W.gradient_batch(seed=1009, batch=3, num_pix=32,
+                                                     supersampling=2, kernel_size=11)
+    main = {k: v for k, v in lens_kw[0].items() if k != "gamma"}
+    if lens == "NIE":
+        main = dict(main, s_scale=np.full(3, 0.05))
+        main = {k: main[k] for k in ("theta_E", "e1", "e2", "s_scale", "center_x", "center_y")}
+    g = W.grid_kwargs(32, 0.05)
+    data_cls = J.ImageData(np.zeros((32, 32)), exposure_time=1000.0, background_rms=0.01, **g)
+    im = J.ImageModel(data_cls, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                      J.LensModel([lens, "SHEAR"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                      J.LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics={"supersampling_factor": 2})
+    rows = im.pack_params([main, lens_kw[1]], src, ll)
+    truth = rows.copy()
+    truth[:, 0] *= 1.01
+    data = W.noisy_data(im.image_batch(rows=truth, psf_kernels=kern).cpu().numpy())
+    logl, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kern)
+    _check(grad.cpu().numpy(), _fd(im, rows, kern, data))
+
+
 def test_unsupported_models_raise(cuda):
     g = W.grid_kwargs(16, 0.05)
     data = J.ImageData(np.zeros((16, 16)), exposure_time=100.0, background_rms=0.01, **g)
-    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["NFW"]), J.LightModel(["SERSIC"]),
                       J.LightModel([]))
-    kw = ([{"theta_E": 1.0, "e1": 0.0, "e2": 0.0, "center_x": 0, "center_y": 0}],
+    kw = ([{"Rs": 1.0, "alpha_Rs": 0.5, "center_x": 0, "center_y": 0}],
           [{"amp": 1.0, "R_sersic": 0.3, "n_sersic": 2, "center_x": 0, "center_y": 0}], [])
     with pytest.raises(Exception):
         im.likelihood_grad_batch(*kw, data=np.zeros((16, 16)))

@@ -161,7 +161,8 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        outdir = os.path.join(ROOT, "gpurun_out") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else tempfile.gettempdir()
+        # side files (the per-run clock samples) go to LENSGB_BENCH_OUT if set
+        outdir = os.environ.get("LENSGB_BENCH_OUT") or tempfile.gettempdir()
         self.path = os.path.join(outdir, "clocks_rank%d.csv" % gpu_index)
 
     def start(self):

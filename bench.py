@@ -574,8 +574,25 @@ def gradient_section(steps, seed=1003):
         "fd_rel_err_max": float(rel.max()), "fd_rel_err_median": float(np.median(rel)),
         "fd_components_checked": int(sig.sum()),
         "precision": "FP64 (forward image, adjoint and reduction)",
+        "roofline": grad_roofline(B, N, S, K, P, ms),
         "timing": "CUDA events, mean over %d batches after 2 warm-ups" % n,
     }
+
+
+def grad_roofline(B, N, S, K, P, ms):
+    """Algorithmic FP64 work of one adjoint batch: every ray's EPL + SHEAR + two
+    Sersic evaluation (~220 flop) carried with 5 tangent directions (~6x), plus
+    the per-parameter accumulation (2 P flop per ray); the forward image and
+    likelihood (ray work + 2 K^2 per pixel), and the transposed convolution
+    (2 K^2 per pixel).  Peak: the nominal GB300 FP64 rate (no measured FP64 figure)."""
+    rays = B * (N * S) ** 2
+    flop = rays * (220 * 6 + 2 * P) + rays * 220 + 2 * (2 * K * K) * B * N * N
+    peak = 1.25  # TFLOP/s, nominal FP64 (CUDA cores) of GB300
+    achieved = flop / (ms / 1e3) / 1e12
+    return {"kernel": "grad_ray_kernel (+ forward image, weights, transposed conv)",
+            "bound": "fp64", "unit": "TFLOP/s", "algorithmic_gflop_per_batch": flop / 1e9,
+            "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "peak_source": "nominal FP64 rate; MEASURED_PEAKS.json has no FP64 figure"}
 
 
 def max_over_ranks(ms, dist=None, device="cpu"):

@@ -308,7 +308,8 @@ int lensgb_loglike(lensgb_model* model, const double* params_dev, int n_inst,
  * returns for the kwargs (test_image_model.py:274-335) -- by a hand-written
  * adjoint that recomputes the ray grid.  Same arguments as lensgb_loglike plus
  * grad_dev: n_inst x param_count doubles, row layout.  FP64 models only; lens
- * stacks of EPL, SIE, NIE and SHEAR, SERSIC / SERSIC_ELLIPSE light, PSF NONE or PIXEL. */
+ * stacks of EPL, SIE, NIE, NFW, TNFW and SHEAR, SERSIC / SERSIC_ELLIPSE light,
+ * PSF NONE or PIXEL. */
 int lensgb_loglike_grad(lensgb_model* model, const double* params_dev, int n_inst,
                         const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
                         void* image_out_dev, double* logl_dev, double* grad_dev, void* stream);

@@ -130,6 +130,23 @@ __device__ __forceinline__ D5 datanh(const D5& a) {
     return r;
 }
 
+__device__ __forceinline__ D5 dacosh(const D5& a) {
+    D5 r;
+    r.v = acosh(a.v);
+    const double g = 1.0 / sqrt(a.v * a.v - 1.0);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+__device__ __forceinline__ D5 dacos(const D5& a) {
+    D5 r;
+    r.v = acos(a.v);
+    const double g = -1.0 / sqrt(1.0 - a.v * a.v);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
+    return r;
+}
+
 // (phi, q) = ellipticity2phi_q(e1, e2) (param_util.py:88-99): dq/de and dphi/de
 // (zero at e = 0 and where the axis-ratio clamp c < 0.9999 holds it).
 __device__ __forceinline__ void dphiq_de(double e1, double e2, double& dq1, double& dq2,
@@ -296,6 +313,72 @@ __device__ void nie_alpha_grad(int code, const double* rec, const double* a, dou
     }
 }
 
+// NFW (nfw.py:88-105, nfw_alpha :259-279, g :347-365, alpha2rho0 :386-395) and
+// TNFW (tnfw.py:69-87, tnfw_alpha :228-248, _g :331-349, F :290-304, _L :278-286)
+// deflections and their Jacobians with respect to (Rs, alpha_Rs, [r_trunc,]
+// center_x, center_y), as dual numbers in (Rs, alpha_Rs, r_trunc, x, y) through
+// the same formulas and floors as the forward pass (a floor freezes its
+// argument's derivative).
+__device__ void nfw_alpha_grad(int code, const double* a, double dx, double dy, double& ax,
+                               double& ay, double J[2][6]) {
+    const bool trunc = code == LENSGB_LENS_TNFW;
+    const D5 RS = dvar(a[0], 0), ARS = dvar(a[1], 1);
+    const D5 X1 = dvar(dx, 3), Y1 = dvar(dy, 4);
+    // rho0 from the unfloored Rs, as alpha2rho0 does (nfw.py:386-395)
+    const D5 rho0 = ARS * dinv((4.0 * (1.0 + log(0.5))) * (RS * RS));
+    D5 R = dsqrt(X1 * X1 + Y1 * Y1);
+    D5 g, X, RSF;
+    if (!trunc) {
+        RSF = a[0] < 0.0000001 ? dconst(0.0000001) : RS;
+        if (!(R.v > 0.00000001)) R = dconst(0.00000001);
+        X = R * dinv(RSF);
+        if (X.v < 0.000001) X = dconst(0.000001);
+        if (X.v < 1.0)
+            g = dlog(0.5 * X) + dinv(dsqrt(1.0 + (-1.0) * X * X)) * dacosh(dinv(X));
+        else if (X.v == 1.0)
+            g = dconst(1.0 + log(0.5));
+        else
+            g = dlog(0.5 * X) + dinv(dsqrt(X * X + dconst(-1.0))) * dacos(dinv(X));
+    } else {
+        RSF = RS;
+        const D5 tau = dvar(a[2], 2) * dinv(RS);
+        if (!(R.v > 0.001 * a[0])) R = 0.001 * RS;
+        X = R * dinv(RS);
+        if (!(X.v > 0.001)) X = dconst(0.001);
+        const D5 x2 = X * X;
+        D5 F;
+        if (X.v < 1.0) {
+            const D5 w = dsqrt(1.0 + (-1.0) * x2);
+            F = dinv(w) * datanh(w);
+        } else if (X.v > 1.0) {
+            const D5 w = dsqrt(x2 + dconst(-1.0));
+            F = dinv(w) * datan(w);
+        } else {
+            F = X;
+        }
+        const D5 t2 = tau * tau;
+        const D5 r = dsqrt(t2 + x2);
+        const D5 L = dlog(X * dinv(tau + r));
+        const D5 tp1 = t2 + dconst(1.0), tm1 = t2 + dconst(-1.0);
+        const D5 br = (tp1 + 2.0 * (x2 + dconst(-1.0))) * F + M_PI * tau + tm1 * dlog(tau) +
+                      r * (dconst(-M_PI) + L * tm1 * dinv(tau));
+        g = t2 * dinv(tp1 * tp1) * br;
+    }
+    const D5 al = 4.0 * rho0 * RSF * g * dinv(X * X);
+    const D5 fx = al * X1, fy = al * Y1;
+    ax = fx.v;
+    ay = fy.v;
+    const int co = trunc ? 3 : 2;
+    for (int i = 0; i < 2; ++i) {
+        const D5& f = i == 0 ? fx : fy;
+        J[i][0] = f.d[0];
+        J[i][1] = f.d[1];
+        if (trunc) J[i][2] = f.d[2];
+        J[i][co] = -f.d[3];
+        J[i][co + 1] = -f.d[4];
+    }
+}
+
 // SHEAR (shear.py:39-53) and its Jacobian w.r.t. (gamma1, gamma2, ra_0, dec_0).
 __device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, double dy,
                                                  double& ax, double& ay, double J[2][6]) {
@@ -377,6 +460,8 @@ __device__ __host__ __forceinline__ int lens_np(int code) {
         case LENSGB_LENS_NIE: return 6;
         case LENSGB_LENS_SIE: return 5;
         case LENSGB_LENS_SHEAR: return 4;
+        case LENSGB_LENS_NFW: return 4;
+        case LENSGB_LENS_TNFW: return 5;
         default: return 0;
     }
 }
@@ -515,6 +600,8 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                                        P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE)
                         nie_alpha_grad(code, r, P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else if (code == LENSGB_LENS_NFW || code == LENSGB_LENS_TNFW)
+                        nfw_alpha_grad(code, P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else
                         shear_alpha_grad(r, ddx, ddy, ax, ay, J);
                     axs += ax;

@@ -588,8 +588,8 @@ class ImageModel:
         (``lensgb_loglike_grad``).  The gradient has the layout of
         :meth:`pack_params`; :meth:`unpack_params` turns it into kwargs lists.
         This is ``jax.grad`` of the reference's ``likelihood_data_given_model``
-        (``image_model.py:163-221``) for FP64 models of EPL / SIE / NIE / SHEAR lenses and
-        Sersic light."""
+        (``image_model.py:163-221``) for FP64 models of EPL / SIE / NIE / NFW / TNFW /
+        SHEAR lenses and Sersic light."""
         if self._precision != _lib.FP64:
             raise ValueError("likelihood gradients need kwargs_numerics precision 'fp64'")
         model = self._model(range(len(self.LensModel.lens_model_list)),

@@ -159,12 +159,37 @@ def test_isothermal_lenses_match_central_differences(cuda, lens):
     _check(grad.cpu().numpy(), _fd(im, rows, kern, data))
 
 
+def test_nfw_halos_match_central_differences(cuda):
+    """EPL + SHEAR + an NFW halo + a TNFW subhalo near the arc: the NFW / TNFW
+    deflections differentiated in (Rs, alpha_Rs, [r_trunc,] centre)."""
+    model, lens_kw, src, ll, kern = W.gradient_batch(seed=1013, batch=3, num_pix=32,
+                                                     supersampling=2, kernel_size=11)
+    rng = np.random.default_rng(7)
+    nfw = {"Rs": rng.uniform(0.8, 1.5, 3), "alpha_Rs": rng.uniform(0.1, 0.3, 3),
+           "center_x": rng.uniform(-0.1, 0.1, 3), "center_y": rng.uniform(-0.1, 0.1, 3)}
+    tnfw = {"Rs": rng.uniform(0.1, 0.3, 3), "alpha_Rs": rng.uniform(0.02, 0.06, 3),
+            "r_trunc": rng.uniform(0.3, 0.8, 3), "center_x": rng.uniform(0.4, 0.6, 3),
+            "center_y": rng.uniform(-0.3, 0.3, 3)}
+    g = W.grid_kwargs(32, 0.05)
+    data_cls = J.ImageData(np.zeros((32, 32)), exposure_time=1000.0, background_rms=0.01, **g)
+    im = J.ImageModel(data_cls, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                      J.LensModel(["EPL", "SHEAR", "NFW", "TNFW"]),
+                      J.LightModel(["SERSIC_ELLIPSE"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics={"supersampling_factor": 2})
+    rows = im.pack_params(list(lens_kw) + [nfw, tnfw], src, ll)
+    truth = rows.copy()
+    truth[:, 0] *= 1.01
+    data = W.noisy_data(im.image_batch(rows=truth, psf_kernels=kern).cpu().numpy())
+    logl, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kern)
+    _check(grad.cpu().numpy(), _fd(im, rows, kern, data))
+
+
 def test_unsupported_models_raise(cuda):
     g = W.grid_kwargs(16, 0.05)
     data = J.ImageData(np.zeros((16, 16)), exposure_time=100.0, background_rms=0.01, **g)
-    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["NFW"]), J.LightModel(["SERSIC"]),
-                      J.LightModel([]))
-    kw = ([{"Rs": 1.0, "alpha_Rs": 0.5, "center_x": 0, "center_y": 0}],
+    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["NFW_ELLIPSE_CSE"]),
+                      J.LightModel(["SERSIC"]), J.LightModel([]))
+    kw = ([{"Rs": 1.0, "alpha_Rs": 0.5, "e1": 0.1, "e2": 0.0, "center_x": 0, "center_y": 0}],
           [{"amp": 1.0, "R_sersic": 0.3, "n_sersic": 2, "center_x": 0, "center_y": 0}], [])
     with pytest.raises(Exception):
         im.likelihood_grad_batch(*kw, data=np.zeros((16, 16)))

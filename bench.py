@@ -334,6 +334,102 @@ def substructure_section(steps, warmup, fp32_peak, flush):
     }
 
 
+# Multi-plane substructure ray shooting (LensModelBulk, multi_plane=True): the
+# shapes of the reference's GPU notebook benchmark (400^2 rays through 5130 TNFW
+# halos and 126 CONVERGENCE sheets on 126 planes, z_s = 2.5, num_deflectors =
+# 5500); published there: 47.93 s lenstronomy CPU, 0.468 s JAXtronomy GPU (FP64).
+MP_PUBLISHED_S = {"lenstronomy_cpu": 47.93, "jaxtronomy_gpu_fp64": 0.468}
+
+
+def multi_plane_section(steps, warmup, fp32_peak, flush):
+    """FP32 and FP64 multi-plane ray shooting times, FP32-vs-FP64 and FP64-vs-oracle
+    errors, and the oracle's CPU rate on a ray sample."""
+    import numpy as np
+    import torch
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import workloads as W
+    from oracle import lens as olens
+
+    x, y, ll, kw, z, zs, nd = W.line_of_sight_halos()
+    unique = ["TNFW", "CONVERGENCE"]
+    cosmo = J.FlatLambdaCDM(67.66, 0.30966)
+    b32 = J.LensModelBulk(unique, multi_plane=True, cosmo=cosmo, precision="fp32")
+    b64 = J.LensModelBulk(unique, multi_plane=True, cosmo=cosmo, precision="fp64")
+    t0 = time.perf_counter()
+    rk = b32.prepare_ray_shooting_kwargs(ll, kw, z_source=zs, lens_redshift_list=z,
+                                         num_deflectors=nd)
+    prep_s = time.perf_counter() - t0
+    rk_dev = {k: ({kk: torch.as_tensor(vv).cuda() for kk, vv in v.items()}
+                  if isinstance(v, dict) else torch.as_tensor(v).cuda())
+              for k, v in rk.items()}
+    xt = torch.as_tensor(x).cuda()
+    yt = torch.as_tensor(y).cuda()
+    stream = torch.cuda.current_stream()
+
+    def timed(b, n_rep):
+        times = []
+        for _ in range(n_rep):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = b.ray_shooting(xt, yt, rk_dev)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return statistics.mean(times), out
+
+    for _ in range(max(warmup, 3)):
+        b32.ray_shooting(xt, yt, rk_dev)
+    torch.cuda.synchronize()
+    ms, (bx32, by32) = timed(b32, max(steps, 3))
+    b64.ray_shooting(xt, yt, rk_dev)
+    ms64, (bx64, by64) = timed(b64, 1)
+    d = torch.maximum((bx32 - bx64).abs(), (by32 - by64).abs())
+    sample = np.arange(0, x.size, x.size // 256)[:256]
+    ox, oy = olens.multi_plane_ray_shooting(unique, x[sample], y[sample], rk["all_kwargs"],
+                                            rk["index_list"], rk["T_ij_list"], rk["T_z_list"],
+                                            rk["reduced2physical_factor"])
+    g64x = bx64.cpu().numpy()[sample]
+    g64y = by64.cpu().numpy()[sample]
+    orc = max(np.max(np.abs(g64x - ox) / np.maximum(np.abs(ox), 1e-300)),
+              np.max(np.abs(g64y - oy) / np.maximum(np.abs(oy), 1e-300)))
+    cs = np.arange(0, x.size, x.size // 2000)[:2000]
+    t0 = time.perf_counter()
+    olens.multi_plane_ray_shooting(unique, x[cs], y[cs], rk["all_kwargs"], rk["index_list"],
+                                   rk["T_ij_list"], rk["T_z_list"], rk["reduced2physical_factor"])
+    cpu_s = time.perf_counter() - t0
+    n_tnfw = sum(1 for m in ll if m == "TNFW")
+    flop = x.size * n_tnfw * FLOP_TNFW
+    return {
+        "workload": "multi_plane_400x400_5130tnfw_126convergence_126planes_5500steps",
+        "rays": int(x.size), "deflectors": len(ll), "steps": int(len(rk["index_list"])),
+        "ms_per_call": ms, "rays_per_s": x.size / (ms / 1e3),
+        "pairs_per_s": x.size * len(rk["index_list"]) / (ms / 1e3),
+        "fp64_ms_per_call": ms64, "speedup_vs_fp64": ms64 / ms,
+        "published_s": MP_PUBLISHED_S,
+        "speedup_vs_published_jaxtronomy_gpu": MP_PUBLISHED_S["jaxtronomy_gpu_fp64"] / (ms / 1e3),
+        "fp64_speedup_vs_published_jaxtronomy_gpu":
+            MP_PUBLISHED_S["jaxtronomy_gpu_fp64"] / (ms64 / 1e3),
+        "host_prepare_s": prep_s,
+        "beta_err_fp32_vs_fp64_arcsec_max": d.max().item(),
+        "beta_err_fp32_vs_fp64_arcsec_median": d.median().item(),
+        "fp64_vs_oracle_rel_err_max": float(orc),
+        "roofline": {"kernel": "multi_plane_kernel<FP32>", "bound": "fp32", "unit": "TFLOP/s",
+                     "achieved": flop / (ms / 1e3) / 1e12, "peak": fp32_peak,
+                     "frac": flop / (ms / 1e3) / 1e12 / fp32_peak,
+                     "algorithmic_gflop_per_launch": flop / 1e9,
+                     "flop_model": "%d flop per (ray, TNFW) pair; CONVERGENCE, plane updates "
+                                   "and FP32-pair state not counted" % FLOP_TNFW},
+        "cpu_baseline": {"value": cs.size / cpu_s, "unit": "rays/s", "cores": 1, "kind": "port",
+                         "sample": "%d rays x %d steps, FP64 NumPy oracle (MultiPlaneBulk "
+                                   "restatement), vectorised over rays"
+                                   % (cs.size, len(rk["index_list"]))},
+        "timing": "CUDA events per call after %d warm-ups, L2 flushed before each; "
+                  "distances from FlatLambdaCDM(67.66, 0.30966)" % max(warmup, 3),
+    }
+
+
 def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_bucket=2,
                     use_graphs=True, loads=(0.5, 0.8, 0.95), mixed_grids=2):
     """Serving stream: capacity (all requests released at once), then Poisson
@@ -870,6 +966,8 @@ def gpu_arm(args):
         if not args.no_sub:
             extra["substructure"] = substructure_section(args.steps, args.warmup, fp32_peak,
                                                          flush)
+            extra["multi_plane"] = multi_plane_section(args.steps, args.warmup, fp32_peak,
+                                                       flush)
 
         # --- adjoint likelihood gradient
         if not args.no_grad:

@@ -28,6 +28,7 @@
  *   NIE            theta_E e1 e2 s_scale center_x center_y         (nie.py:19)
  *   EPL            theta_E gamma e1 e2 center_x center_y           (epl.py:50)
  *   SHEAR          gamma1 gamma2 ra_0 dec_0                        (shear.py:16)
+ *   CONVERGENCE    kappa ra_0 dec_0                                (convergence.py:15)
  *   NFW            Rs alpha_Rs center_x center_y                   (nfw.py:49)
  *   TNFW           Rs alpha_Rs r_trunc center_x center_y           (tnfw.py:27)
  *   NFW_ELLIPSE_CSE Rs alpha_Rs e1 e2 center_x center_y            (nfw_ellipse_cse.py:172)
@@ -59,6 +60,7 @@ extern "C" {
 #define LENSGB_LENS_TNFW 6
 #define LENSGB_LENS_NFW_ELLIPSE_CSE 7
 #define LENSGB_LENS_EPL_MULTIPOLE_M1M3M4 8
+#define LENSGB_LENS_CONVERGENCE 9
 
 #define LENSGB_LIGHT_SERSIC 1
 #define LENSGB_LIGHT_SERSIC_ELLIPSE 2
@@ -354,7 +356,7 @@ int lensgb_surface_brightness(const lensgb_model* model, int which, const double
  * <= 2 alpha_Rs for NFW/TNFW/NFW_ELLIPSE_CSE; SHEAR never), sums those terms
  * in FP32 over chunks of 64 deflectors and accumulates the chunk sums, and
  * every FP64 term, in FP64.  The handle owns grow-only device scratch
- * (about 300 B per deflector, plus 6 KB per deflector when an EPL-type or
+ * (about 340 B per deflector, plus 6 KB per deflector when an EPL-type or
  * NFW_ELLIPSE_CSE profile is in the unique list) and serves one stream at a
  * time. */
 #define LENSGB_LENS_NULL 0 /* the reference's "NULL" profile: no deflection */
@@ -371,6 +373,29 @@ int lensgb_bulk_set_fp32_alpha_max(lensgb_bulk* bulk, double alpha_max);
 int lensgb_bulk_ray_shooting(lensgb_bulk* bulk, const int* index_dev, const double* params_dev,
                              int n_deflectors, const double* x_dev, const double* y_dev,
                              double* beta_x_dev, double* beta_y_dev, long long n, void* stream);
+
+/* LensModelBulk(unique_lens_model_list, multi_plane=True) -> MultiPlaneBulk
+ * (jaxtronomy/LensModel/MultiPlane/multi_plane_bulk.py:11-272):
+ * ray_shooting(alpha_x, alpha_y, all_kwargs, index_list, T_ij_list, T_z_list,
+ * reduced2physical_factor) (:152-200).  The n_steps steps are the
+ * redshift-sorted deflectors, the source plane and the NULL fillers that
+ * prepare_ray_shooting_kwargs builds (:57-150), with index_dev / params_dev as
+ * in lensgb_bulk_ray_shooting and, per step, T_ij_dev (transverse comoving
+ * distance from the previous step), T_z_dev (from the observer) and r2p_dev
+ * (reduced-to-physical deflection factor).  Starting from x = 0 at angles
+ * alpha (arcsec), every step does x += alpha T_ij; alpha -= r2p *
+ * alpha_i(x / T_z); beta = x / T_z[n_steps - 1].  n_steps >= 1.
+ * LENSGB_FP64 follows that recurrence in FP64.  LENSGB_FP32_SPLIT carries the
+ * deflection and displacement as FP32 pairs next to the FP64 start angle,
+ * groups consecutive deflectors of one plane (T_ij = 0, equal T_z and r2p),
+ * evaluates fp32_alpha_max-bounded terms in FP32, CONVERGENCE as an FP32-pair
+ * product and the other terms in FP64. */
+int lensgb_bulk_multi_plane_ray_shooting(lensgb_bulk* bulk, const int* index_dev,
+                                         const double* params_dev, int n_steps,
+                                         const double* T_ij_dev, const double* T_z_dev,
+                                         const double* r2p_dev, const double* alpha_x_dev,
+                                         const double* alpha_y_dev, double* beta_x_dev,
+                                         double* beta_y_dev, long long n, void* stream);
 
 /* ---- serving loop ---------------------------------------------------------- */
 /* A server batches independent image / likelihood requests continuously: a

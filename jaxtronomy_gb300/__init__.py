@@ -8,11 +8,13 @@ C ABI, ``include/lensgb.h``); build it with ``python -m jaxtronomy_gb300.build``
 from .data import ImageData, PSF, PixelGrid  # noqa: F401
 from .image_model import ImageModel  # noqa: F401
 from .lens_model import LensModel  # noqa: F401
-from .lens_model_bulk import LensModelBulk  # noqa: F401
+from .cosmology import FlatLambdaCDM  # noqa: F401
+from .lens_model_bulk import LensModelBulk, MultiPlaneBulk, SinglePlaneBulk  # noqa: F401
 from .light_model import LightModel  # noqa: F401
 from .sampling import ImageLikelihood, LikelihoodModule, Param, prepare_logL_func  # noqa: F401
 
 __version__ = "0.1.0"
 
 __all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LensModelBulk", "LightModel",
+           "MultiPlaneBulk", "SinglePlaneBulk", "FlatLambdaCDM",
            "ImageLikelihood", "LikelihoodModule", "Param", "prepare_logL_func"]

@@ -24,7 +24,7 @@ LENS_NULL = 0
 BULK_MAX_UNIQUE = 16
 BULK_PARAM_STRIDE = 12
 LENS_CODES = {"SIE": 1, "NIE": 2, "EPL": 3, "SHEAR": 4, "NFW": 5, "TNFW": 6,
-              "NFW_ELLIPSE_CSE": 7, "EPL_MULTIPOLE_M1M3M4": 8}
+              "NFW_ELLIPSE_CSE": 7, "EPL_MULTIPOLE_M1M3M4": 8, "CONVERGENCE": 9}
 LIGHT_CODES = {"SERSIC": 1, "SERSIC_ELLIPSE": 2}
 
 PSF_NONE, PSF_PIXEL, PSF_GAUSSIAN = 0, 1, 2
@@ -47,7 +47,7 @@ SYMBOLS = [
     "lensgb_ray_shooting", "lensgb_alpha",
     "lensgb_surface_brightness",
     "lensgb_bulk_create", "lensgb_bulk_destroy", "lensgb_bulk_set_fp32_alpha_max",
-    "lensgb_bulk_ray_shooting",
+    "lensgb_bulk_ray_shooting", "lensgb_bulk_multi_plane_ray_shooting",
     "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
@@ -229,6 +229,9 @@ def load():
     lib.lensgb_bulk_set_fp32_alpha_max.restype = i
     lib.lensgb_bulk_ray_shooting.argtypes = [vp, vp, dp, i, dp, dp, dp, dp, ll, vp]
     lib.lensgb_bulk_ray_shooting.restype = i
+    lib.lensgb_bulk_multi_plane_ray_shooting.argtypes = [vp, vp, dp, i, dp, dp, dp, dp, dp, dp,
+                                                         dp, ll, vp]
+    lib.lensgb_bulk_multi_plane_ray_shooting.restype = i
     lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
     lib.lensgb_server_create.restype = i
     lib.lensgb_server_submit.argtypes = [vp, ctypes.POINTER(Request), i,

@@ -103,6 +103,7 @@ static int lens_param_count(int code) {
         case LENSGB_LENS_NFW: return 4;
         case LENSGB_LENS_TNFW: return 5;
         case LENSGB_LENS_NFW_ELLIPSE_CSE: return 6;
+        case LENSGB_LENS_CONVERGENCE: return 3;
         case LENSGB_LENS_EPL_MULTIPOLE_M1M3M4: return 12;
         default: return -1;
     }
@@ -248,7 +249,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 111; }
+int lensgb_version(void) { return 112; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -1257,6 +1258,8 @@ struct lensgb_bulk {
     float* rec_f = nullptr;
     double* coef_d = nullptr;
     float* coef_f = nullptr;
+    float* pl_f = nullptr;    // multi-plane step table (8 floats per step)
+    double* eps_d = nullptr;  // multi-plane T_cum / T_z - 1 per step
 };
 
 static void bulk_free(lensgb_bulk* b) {
@@ -1265,6 +1268,10 @@ static void bulk_free(lensgb_bulk* b) {
     cudaFree(b->rec_f);
     cudaFree(b->coef_d);
     cudaFree(b->coef_f);
+    cudaFree(b->pl_f);
+    cudaFree(b->eps_d);
+    b->pl_f = nullptr;
+    b->eps_d = nullptr;
     b->tag = nullptr;
     b->rec_d = nullptr;
     b->rec_f = nullptr;
@@ -1279,7 +1286,9 @@ static int bulk_ensure(lensgb_bulk* b, int n_defl) {
     const size_t n = (size_t)n_defl;
     bool ok = cudaMalloc(&b->tag, n * sizeof(int)) == cudaSuccess &&
               cudaMalloc(&b->rec_d, n * REC_D * sizeof(double)) == cudaSuccess &&
-              cudaMalloc(&b->rec_f, n * REC_F * sizeof(float)) == cudaSuccess;
+              cudaMalloc(&b->rec_f, n * REC_F * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&b->pl_f, n * 8 * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&b->eps_d, n * sizeof(double)) == cudaSuccess;
     if (ok && b->need_coef)
         ok = cudaMalloc(&b->coef_d, n * EPL_NMAX * sizeof(double)) == cudaSuccess &&
              cudaMalloc(&b->coef_f, n * EPL_NMAX * sizeof(float)) == cudaSuccess;
@@ -1356,6 +1365,32 @@ int lensgb_bulk_ray_shooting(lensgb_bulk* b, const int* index, const double* par
     launch_bulk_ray_shooting(b->tag, b->rec_d, b->rec_f, b->coef_d, b->coef_f, n_defl, x, y, bx,
                              by, n, b->precision, s);
     return check_cuda("bulk ray shooting launch");
+}
+
+int lensgb_bulk_multi_plane_ray_shooting(lensgb_bulk* b, const int* index, const double* params,
+                                         int n_steps, const double* T_ij, const double* T_z,
+                                         const double* r2p, const double* alpha_x,
+                                         const double* alpha_y, double* bx, double* by,
+                                         long long n, void* stream) {
+    if (!b) return fail(LENSGB_ERR_INVALID, "null bulk handle");
+    if (n_steps < 1)
+        return fail(LENSGB_ERR_INVALID, "multi-plane ray shooting needs at least one step "
+                                        "(the source plane)");
+    if (n < 0) return fail(LENSGB_ERR_INVALID, "negative point count");
+    if (n == 0) return LENSGB_OK;
+    if (!alpha_x || !alpha_y || !bx || !by)
+        return fail(LENSGB_ERR_INVALID, "null coordinate pointer");
+    if (!index || !params || !T_ij || !T_z || !r2p)
+        return fail(LENSGB_ERR_INVALID, "null index, params or distance pointer");
+    int rc = bulk_ensure(b, n_steps);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_bulk_prepare(b->u, index, params, n_steps, b->fp32_alpha_max, b->tag, b->rec_d,
+                        b->rec_f, b->coef_d, b->coef_f, s);
+    if ((rc = check_cuda("bulk prepare launch"))) return rc;
+    launch_multi_plane(b->tag, b->rec_d, b->rec_f, b->coef_d, b->coef_f, b->pl_f, b->eps_d, T_ij,
+                       T_z, r2p, n_steps, alpha_x, alpha_y, bx, by, n, b->precision, s);
+    return check_cuda("multi-plane ray shooting launch");
 }
 
 }  // extern "C"

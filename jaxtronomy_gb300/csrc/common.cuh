@@ -123,8 +123,10 @@ struct BulkUnique {
 };
 
 // Per-deflector tag of a bulk call: profile code in the low byte, plus this
-// flag when the deflector's terms run in FP64.
+// flag when the deflector's terms run in FP64, and (multi-plane FP32 calls)
+// the flag of a step that starts a new lens plane.
 constexpr int BULK_TAG_FP64 = 0x100;
+constexpr int BULK_TAG_PLANE = 0x200;
 constexpr int BULK_CODE_MASK = 0xff;
 
 // ---------------------------------------------------------------------------

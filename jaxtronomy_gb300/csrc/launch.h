@@ -177,5 +177,14 @@ int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* r
                              const double* coef_d, const float* coef_f, int n_defl,
                              const double* x, const double* y, double* bx, double* by,
                              long long n, int precision, cudaStream_t stream);
+// MultiPlaneBulk.ray_shooting over n_steps redshift-ordered steps (tags and
+// records from launch_bulk_prepare; T_ij, T_z, r2p per step) for n rays
+// starting at angles (ax, ay).  FP32_SPLIT also writes the plane table pl_f
+// (8 floats per step), eps_d (n_steps doubles) and the tags' plane flags.
+int launch_multi_plane(int* tag, const double* rec_d, const float* rec_f, const double* coef_d,
+                       const float* coef_f, float* pl_f, double* eps_d, const double* dT,
+                       const double* Tz, const double* r2p, int n_steps, const double* ax,
+                       const double* ay, double* bx, double* by, long long n, int precision,
+                       cudaStream_t stream);
 
 }  // namespace lensgb

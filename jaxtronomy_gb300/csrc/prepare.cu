@@ -141,6 +141,11 @@ __device__ void prepare_lens_record(int code, const double* a, double* d, double
         d[RD_CX] = a[2];
         d[RD_CY] = a[3];
         d[2] = a[0]; d[3] = a[1];
+    } else if (code == LENSGB_LENS_CONVERGENCE) {
+        d[RD_CX] = a[1];
+        d[RD_CY] = a[2];
+        d[2] = a[0];
+        d[3] = a[0] - (double)(float)a[0];
     } else if (code == LENSGB_LENS_NFW) {
         double Rs = a[0], alpha_Rs = a[1];
         double rho0 = alpha_Rs / (4.0 * Rs * Rs * (1.0 + log(1.0 / 2.0)));
@@ -277,8 +282,10 @@ namespace lensgb {
 
 // Bound on |alpha| of one deflector, the quantity that decides whether its
 // terms may run in FP32 (deflection scale theta_E of the power laws; NFW-type
-// deflections peak near 1.01 alpha_Rs, doubled for ellipticity).  SHEAR grows
-// without bound away from its origin and always runs in FP64.
+// deflections peak near 1.01 alpha_Rs, doubled for ellipticity).  SHEAR and
+// CONVERGENCE grow without bound away from their origin and run in FP64 in
+// single-plane calls (the multi-plane kernel evaluates CONVERGENCE as an
+// FP32-pair product instead).
 __device__ static double bulk_alpha_bound(int code, const double* a) {
     switch (code) {
         case LENSGB_LENS_SIE:

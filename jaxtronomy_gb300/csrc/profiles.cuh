@@ -358,6 +358,15 @@ __device__ __forceinline__ void shear_deflect(const R* rec, R dx, R dy, R& ax, R
     ay = g2 * dx - g1 * dy;
 }
 
+// CONVERGENCE (convergence.py:33-46): a mass sheet, alpha = kappa (x - ra_0).
+// Record: d2 kappa, d3 kappa - fl(kappa) (the FP32 split's low part).
+template <typename R>
+__device__ __forceinline__ void convergence_deflect(const R* rec, R dx, R dy, R& ax, R& ay) {
+    const R k = rec[slot<R>(2)];
+    ax = k * dx;
+    ay = k * dy;
+}
+
 // ---------------------------------------------------------------------------
 // NFW
 // ---------------------------------------------------------------------------
@@ -440,17 +449,25 @@ __device__ __forceinline__ void nfw_deflect(const R* rec, R dx, R dy, R& ax, R& 
 // ---------------------------------------------------------------------------
 // TNFW
 // ---------------------------------------------------------------------------
+// The reference's powers w^-0.5, w^0.5 and w^-1 (tnfw.py:278-304) are taken
+// as 1/sqrt(w), sqrt(w) and 1/w: the same values to an ulp, without pow.
 __device__ __forceinline__ double tnfw_F_d(double x) {
     x = x > 0.001 ? x : 0.001;
-    if (x < 1) return pow(1 - x * x, -0.5) * atanh(pow(1 - x * x, 0.5));
-    if (x > 1) return pow(x * x - 1, -0.5) * atan(pow(x * x - 1, 0.5));
+    if (x < 1) {
+        const double s = sqrt(1 - x * x);
+        return atanh(s) / s;
+    }
+    if (x > 1) {
+        const double s = sqrt(x * x - 1);
+        return atan(s) / s;
+    }
     return x;
 }
 
 __device__ __forceinline__ double tnfw_g_d(double x, double tau) {
     x = x > 0.001 ? x : 0.001;
     double t2 = tau * tau;
-    double L = log(x * pow(tau + sqrt(t2 + x * x), -1.0));
+    double L = log(x / (tau + sqrt(t2 + x * x)));
     return t2 / ((t2 + 1) * (t2 + 1)) *
            ((t2 + 1 + 2 * (x * x - 1)) * tnfw_F_d(x) + tau * M_PI + (t2 - 1) * log(tau) +
             sqrt(t2 + x * x) * (-M_PI + L * (t2 - 1) / tau));
@@ -632,6 +649,7 @@ __device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F,
         case LENSGB_LENS_NIE: nie_deflect<R>(rec, dx, dy, ax, ay); break;
         case LENSGB_LENS_EPL: epl_deflect<R>(rec, F, dx, dy, ax, ay); break;
         case LENSGB_LENS_SHEAR: shear_deflect<R>(rec, dx, dy, ax, ay); break;
+        case LENSGB_LENS_CONVERGENCE: convergence_deflect<R>(rec, dx, dy, ax, ay); break;
         case LENSGB_LENS_NFW: nfw_deflect<R>(rec, dx, dy, ax, ay); break;
         case LENSGB_LENS_TNFW: tnfw_deflect<R>(rec, dx, dy, ax, ay); break;
         case LENSGB_LENS_NFW_ELLIPSE_CSE: nfw_cse_deflect<R>(rec, F, dx, dy, ax, ay); break;

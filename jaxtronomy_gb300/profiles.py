@@ -2,7 +2,7 @@
 
 Parameter names and their order are the reference profiles' ``param_names``
 (JAXtronomy: ``LensModel/Profiles/sie.py:40``, ``nie.py:19``, ``epl.py:50``,
-``shear.py:16``, ``nfw.py:49``, ``tnfw.py:27``, ``nfw_ellipse_cse.py:172``,
+``shear.py:16``, ``convergence.py:15``, ``nfw.py:49``, ``tnfw.py:27``, ``nfw_ellipse_cse.py:172``,
 ``epl_multipole_m1m3m4.py:415-428``,
 ``LightModel/Profiles/sersic.py:27``, ``sersic_ellipse.py:25``).  The packed
 row layout is the one documented in ``include/lensgb.h``.
@@ -17,6 +17,7 @@ LENS_PARAMS = {
     "NIE": ["theta_E", "e1", "e2", "s_scale", "center_x", "center_y"],
     "EPL": ["theta_E", "gamma", "e1", "e2", "center_x", "center_y"],
     "SHEAR": ["gamma1", "gamma2", "ra_0", "dec_0"],
+    "CONVERGENCE": ["kappa", "ra_0", "dec_0"],
     "NFW": ["Rs", "alpha_Rs", "center_x", "center_y"],
     "TNFW": ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"],
     "NFW_ELLIPSE_CSE": ["Rs", "alpha_Rs", "e1", "e2", "center_x", "center_y"],

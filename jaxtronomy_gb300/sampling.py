@@ -33,7 +33,7 @@ _PI = np.pi
 
 # lower_limit_default / upper_limit_default of each supported profile
 # (LensModel/Profiles/sie.py:41-54, nie.py:20-35, epl.py:51-66, shear.py:17-18,
-# nfw.py:49-50, tnfw.py:28-41, nfw_ellipse_cse.py:173-188,
+# convergence.py:16-17, nfw.py:49-50, tnfw.py:28-41, nfw_ellipse_cse.py:173-188,
 # epl_multipole_m1m3m4.py:429-456; LightModel/Profiles/sersic.py:22-35,
 # sersic_ellipse.py:26-43)
 _C = {"center_x": (-100.0, 100.0), "center_y": (-100.0, 100.0)}
@@ -44,6 +44,7 @@ LIMITS = {
     "EPL": {"theta_E": (0.0, 100.0), "gamma": (1.5, 2.5), **_E, **_C},
     "SHEAR": {"gamma1": (-0.5, 0.5), "gamma2": (-0.5, 0.5), "ra_0": (-100.0, 100.0),
               "dec_0": (-100.0, 100.0)},
+    "CONVERGENCE": {"kappa": (-10.0, 10.0), "ra_0": (-100.0, 100.0), "dec_0": (-100.0, 100.0)},
     "NFW": {"Rs": (0.0, 100.0), "alpha_Rs": (0.0, 10.0), **_C},
     "TNFW": {"Rs": (0.0, 100.0), "alpha_Rs": (0.0, 10.0), "r_trunc": (0.0, 100.0), **_C},
     "NFW_ELLIPSE_CSE": {"Rs": (0.0, 100.0), "alpha_Rs": (0.0, 10.0), **_E, **_C},

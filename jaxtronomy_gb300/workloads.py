@@ -159,6 +159,51 @@ def substructure(seed=1004, num_pix=1000, delta_pix=0.01, n_sub=2000):
     return xx.reshape(-1), yy.reshape(-1), lens_list, lens, src
 
 
+def line_of_sight_halos(seed=1005, num_pix=400, half_width=10.0, n_halos=5130, n_planes=126,
+                        z_lens=0.5, z_source=2.5, cone_radius=2.75, num_deflectors=5500):
+    """Multi-plane substructure ray shooting with the shapes of the reference's
+    GPU notebook benchmark (a pyHalo CDM realisation: 400^2 rays on
+    linspace(-10, 10) through 5130 TNFW halos and 126 CONVERGENCE sheets,
+    z_lens = 0.5, z_source = 2.5, padded to 5500 deflectors), drawn here
+    synthetically: n_planes planes at z = linspace(0.02, z_source - 0.02); 30%
+    of the halos on the plane nearest z_lens (subhalos), the rest uniform over
+    the planes; centres uniform in a disk of radius cone_radius arcsec; masses
+    log10 m ~ dN/dlog m ∝ m^-0.9 on [6, 10] with Rs = 0.05 (m / 1e8)^(1/3)
+    arcsec, alpha_Rs = 0.004 (m / 1e8)^(2/3) arcsec, r_trunc = U(5, 20) Rs; one
+    negative CONVERGENCE sheet kappa ~ -U(0.001, 0.006) per plane.  Returns
+    (x, y, lens_model_list, kwargs_lens, lens_redshift_list, z_source,
+    num_deflectors) with x, y the flattened ray grid (x fastest, as the
+    notebook's np.tile / np.repeat)."""
+    rng = np.random.default_rng(seed)
+    planes = np.linspace(0.02, z_source - 0.02, n_planes)
+    main = int(np.argmin(np.abs(planes - z_lens)))
+    n_sub = int(0.3 * n_halos)
+    zi = np.concatenate([np.full(n_sub, main), rng.integers(0, n_planes, n_halos - n_sub)])
+    # inverse-CDF draw of dN/dlog m ∝ m^-0.9 on [1e6, 1e10]
+    u = rng.uniform(0, 1, n_halos)
+    a = -0.9 * np.log(10.0)
+    lm = 6.0 + np.log1p(u * np.expm1(a * 4.0)) / a
+    m8 = 10.0 ** (lm - 8.0)
+    r = cone_radius * np.sqrt(rng.uniform(0, 1, n_halos))
+    ph = rng.uniform(0, 2 * np.pi, n_halos)
+    rs = 0.05 * m8 ** (1.0 / 3.0)
+    lens_list, kwargs, z = [], [], []
+    for i in range(n_halos):
+        lens_list.append("TNFW")
+        kwargs.append({"Rs": float(rs[i]), "alpha_Rs": float(0.004 * m8[i] ** (2.0 / 3.0)),
+                       "r_trunc": float(rs[i] * rng.uniform(5, 20)),
+                       "center_x": float(r[i] * np.cos(ph[i])),
+                       "center_y": float(r[i] * np.sin(ph[i]))})
+        z.append(float(planes[zi[i]]))
+    for k in range(n_planes):
+        lens_list.append("CONVERGENCE")
+        kwargs.append({"kappa": float(-rng.uniform(0.001, 0.006))})
+        z.append(float(planes[k]))
+    x = np.tile(np.linspace(-half_width, half_width, num_pix), num_pix)
+    y = np.repeat(np.linspace(-half_width, half_width, num_pix), num_pix)
+    return x, y, lens_list, kwargs, z, z_source, num_deflectors
+
+
 SERVING_STACKS = ("SIE+SHEAR", "EPL+SHEAR", "EPL_MULTIPOLE_M1M3M4+SHEAR", "NFW_ELLIPSE_CSE+SHEAR")
 
 

@@ -1,4 +1,5 @@
-"""Lens-profile deflections and single-plane ray shooting (oracle, FP64).
+"""Lens-profile deflections, single-plane and multi-plane bulk ray shooting
+(oracle, FP64; test infrastructure).
 
 Every profile function takes 1d FP64 ray coordinates and the profile's kwargs
 exactly as named by the reference's ``param_names`` and returns (alpha_x,
@@ -39,6 +40,15 @@ def shear(x, y, gamma1, gamma2, ra_0=0.0, dec_0=0.0):
     x_ = _f(x) - ra_0
     y_ = _f(y) - dec_0
     return gamma1 * x_ + gamma2 * y_, gamma2 * x_ - gamma1 * y_
+
+
+# ---------------------------------------------------------------------------
+# CONVERGENCE  (jaxtronomy/LensModel/Profiles/convergence.py:33-46)
+# ---------------------------------------------------------------------------
+
+
+def convergence(x, y, kappa, ra_0=0.0, dec_0=0.0):
+    return kappa * (_f(x) - ra_0), kappa * (_f(y) - dec_0)
 
 
 # ---------------------------------------------------------------------------
@@ -349,6 +359,7 @@ PROFILES = {
     "NIE": (nie, ["theta_E", "e1", "e2", "s_scale", "center_x", "center_y"]),
     "EPL": (epl, ["theta_E", "gamma", "e1", "e2", "center_x", "center_y"]),
     "SHEAR": (shear, ["gamma1", "gamma2", "ra_0", "dec_0"]),
+    "CONVERGENCE": (convergence, ["kappa", "ra_0", "dec_0"]),
     "NFW": (nfw, ["Rs", "alpha_Rs", "center_x", "center_y"]),
     "TNFW": (tnfw, ["Rs", "alpha_Rs", "r_trunc", "center_x", "center_y"]),
     "NFW_ELLIPSE_CSE": (nfw_ellipse_cse, ["Rs", "alpha_Rs", "e1", "e2", "center_x", "center_y"]),
@@ -436,3 +447,88 @@ def bulk_ray_shooting(unique_lens_model_list, x, y, all_kwargs, index_list):
         fx = fx + ax
         fy = fy + ay
     return x - fx, y - fy
+
+
+# ---------------------------------------------------------------------------
+# many-deflector multi-plane ray shooting
+# ---------------------------------------------------------------------------
+
+def multi_plane_distances(lens_redshift_list, z_source, d_xy, T_xy):
+    """``MultiPlaneBulk._set_T_zs_and_T_ijs`` (``multi_plane_bulk.py:226-272``) for a
+    SORTED redshift array, given the background's angular diameter distance
+    ``d_xy(z1, z2)`` and transverse comoving distance ``T_xy(z1, z2)``:
+    (T_ij list, T_z list, reduced2physical factors), the source appended."""
+    z = np.asarray(lens_redshift_list, dtype=float)
+    r2p = [d_xy(0, z_source) / d_xy(zi, z_source) for zi in z]
+    T_ij, T_z = [], []
+    z_before, tz = 0, 0
+    for zi in list(z) + [z_source]:
+        if z_before == zi:
+            dt = 0
+        else:
+            tz = T_xy(0, zi)
+            dt = T_xy(z_before, zi)
+        T_ij.append(dt)
+        T_z.append(tz)
+        z_before = zi
+    return T_ij, T_z, r2p
+
+
+def multi_plane_prepare(unique_lens_model_list, lens_model_list, kwargs_lens, z_source,
+                        lens_redshift_list, d_xy, T_xy, num_deflectors=None):
+    """``MultiPlaneBulk.prepare_ray_shooting_kwargs`` (``multi_plane_bulk.py:57-150``):
+    redshift sort (``np.argsort``, :203-224), index list with NULL entries for the
+    source step and the fillers, zero-filled parameter arrays and the padded
+    distance lists."""
+    n = len(lens_model_list)
+    if n != len(kwargs_lens) or n != len(lens_redshift_list):
+        raise ValueError("lens model list, kwargs_lens and redshift list lengths differ")
+    if num_deflectors is None:
+        num_deflectors = n
+    elif num_deflectors < n:
+        raise ValueError("num_deflectors is smaller than the length of lens_model_list")
+    z = np.array(lens_redshift_list)
+    order = np.argsort(z)
+    models = [lens_model_list[i] for i in order]
+    kws = [kwargs_lens[i] for i in order]
+    z = z[order]
+    num_filler = num_deflectors - n
+    index_list = [unique_lens_model_list.index(m) for m in models]
+    index_list += [len(unique_lens_model_list)] * (num_filler + 1)
+    names = set(p for m in unique_lens_model_list if m != "NULL" for p in PROFILES[m][1])
+    all_kwargs = {k: np.array([kw.get(k, 0) for kw in kws] + [0] * (num_filler + 1), dtype=float)
+                  for k in names}
+    T_ij, T_z, r2p = multi_plane_distances(z, z_source, d_xy, T_xy)
+    T_ij = np.array(T_ij + [0] * num_filler, dtype=float)
+    T_z = np.array(T_z + [T_z[-1]] * num_filler, dtype=float)
+    r2p = np.array(list(r2p) + [0] * (num_filler + 1), dtype=float)
+    return {"all_kwargs": all_kwargs, "index_list": np.array(index_list), "T_ij_list": T_ij,
+            "T_z_list": T_z, "reduced2physical_factor": r2p}
+
+
+def multi_plane_ray_shooting(unique_lens_model_list, alpha_x, alpha_y, all_kwargs, index_list,
+                             T_ij_list, T_z_list, reduced2physical_factor):
+    """``MultiPlaneBulk.ray_shooting`` (``multi_plane_bulk.py:152-200``): the
+    ``lax.scan`` over steps, x += alpha T_ij; alpha -= r2p * alpha_i(x / T_z);
+    beta = x / T_z[-1].  Parameters are bound positionally as in
+    :func:`bulk_ray_shooting`."""
+    ax = _f(alpha_x).copy()
+    ay = _f(alpha_y).copy()
+    x = np.zeros_like(ax)
+    y = np.zeros_like(ay)
+    n_u = len(unique_lens_model_list)
+    T_ij = _f(T_ij_list)
+    T_z = _f(T_z_list)
+    r2p = _f(reduced2physical_factor)
+    for i, k in enumerate(np.asarray(index_list)):
+        x = x + ax * T_ij[i]
+        y = y + ay * T_ij[i]
+        k = min(max(int(k), 0), n_u)
+        name = unique_lens_model_list[k] if k < n_u else "NULL"
+        if name == "NULL":
+            continue
+        func, names = PROFILES[name]
+        fx, fy = func(x / T_z[i], y / T_z[i], *[float(all_kwargs[p][i]) for p in names])
+        ax = ax - fx * r2p[i]
+        ay = ay - fy * r2p[i]
+    return x / T_z[-1], y / T_z[-1]

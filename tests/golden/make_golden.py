@@ -15,6 +15,7 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
   hyp2f1.npz    hyp2f1_lopez_temme_8 at the reference's own test points
   images.npz    ImageModel.image and likelihood_data_given_model on small scenes
   bulk.npz      LensModelBulk.ray_shooting through many deflectors
+  multiplane.npz LensModelBulk (multi-plane): prepared kwargs and ray shooting
   linear.npz    ImageLinearFit: linear amplitude solve, model image, logL
 """
 
@@ -102,6 +103,11 @@ def gen_profiles(rng):
         out = lm.surface_brightness(x, y, [kw])
         cases.append({"kind": "light", "name": name, "kwargs": kw, "x": x, "y": y,
                       "out": np.asarray(out)[None, :]})
+    for kw in ({"kappa": -0.03, "ra_0": 0.2, "dec_0": -0.1}, {"kappa": 0.12}):
+        x, y = _points(rng, 64)
+        ax, ay = LensModel(["CONVERGENCE"]).alpha(x, y, [kw])
+        cases.append({"kind": "lens", "name": "CONVERGENCE", "kwargs": kw, "x": x, "y": y,
+                      "out": np.stack([np.asarray(ax), np.asarray(ay)])})
     return cases
 
 
@@ -350,6 +356,84 @@ def gen_bulk(rng):
     return cases
 
 
+def gen_multi_plane(rng):
+    """LensModelBulk (multi-plane, MultiPlaneBulk) through redshift-spread deflectors:
+    the prepared kwargs (sorting, fillers, distance lists) and beta.  Distances come
+    from refshim's flat Lambda-CDM Background (H0 = 70, Om0 = 0.3, no radiation)."""
+    from jaxtronomy.LensModel.lens_model_bulk import LensModelBulk
+
+    cosmo = refshim.FlatLCDM(70.0, 0.3)
+    cases = []
+
+    def run(tag, unique, lens_list, kw, z, z_source, num_deflectors, x, y):
+        bulk = LensModelBulk(unique, multi_plane=True, cosmo=cosmo)
+        rk = bulk.prepare_ray_shooting_kwargs(lens_list, kw, z_source=z_source,
+                                              lens_redshift_list=z,
+                                              num_deflectors=num_deflectors)
+        # the reference updates its scan carry with augmented assignments, which act
+        # in place on the shim's NumPy arrays (JAX arrays are immutable): pass copies
+        bx, by = bulk.ray_shooting(np.array(x), np.array(y), rk)
+        prep = {"index_list": np.asarray(rk["index_list"]),
+                "T_ij_list": np.asarray(rk["T_ij_list"], dtype=float),
+                "T_z_list": np.asarray(rk["T_z_list"], dtype=float),
+                "reduced2physical_factor": np.asarray(rk["reduced2physical_factor"],
+                                                      dtype=float)}
+        for k, v in rk["all_kwargs"].items():
+            prep["kw_" + k] = np.asarray(v, dtype=float)
+        cases.append({"tag": tag, "unique": unique, "lens_list": lens_list, "kwargs": kw,
+                      "z": [float(v) for v in z], "z_source": z_source,
+                      "num_deflectors": num_deflectors, "x": x, "y": y,
+                      "bx": np.asarray(bx), "by": np.asarray(by), "prep": prep})
+
+    # substructure-like: TNFW halos on 8 planes, a negative CONVERGENCE sheet per
+    # plane, NULL fillers; rays on and next to halo centres
+    planes = np.round(np.linspace(0.1, 2.3, 8), 2)
+    lens_list, kw, z = [], [], []
+    for zp in planes:
+        for _ in range(6):
+            rs = rng.uniform(0.02, 0.15)
+            lens_list.append("TNFW")
+            kw.append({"Rs": float(rs), "alpha_Rs": float(10 ** rng.uniform(-3.5, -2)),
+                       "r_trunc": float(rs * rng.uniform(5, 20)),
+                       "center_x": float(rng.uniform(-2.5, 2.5)),
+                       "center_y": float(rng.uniform(-2.5, 2.5))})
+            z.append(float(zp))
+        lens_list.append("CONVERGENCE")
+        kw.append({"kappa": float(-rng.uniform(0.001, 0.01))})
+        z.append(float(zp))
+    perm = rng.permutation(len(lens_list))
+    lens_list = [lens_list[i] for i in perm]
+    kw = [kw[i] for i in perm]
+    z = [z[i] for i in perm]
+    x, y = _points(rng, 400, -3.0, 3.0)
+    cent = [(k["center_x"], k["center_y"]) for k in kw if "center_x" in k][:4]
+    x[4:8] = [c[0] + d for c, d in zip(cent, (0.0, 1e-4, -3e-3, 0.02))]
+    y[4:8] = [c[1] + d for c, d in zip(cent, (0.0, 0.0, 2e-3, -0.01))]
+    run("halos", ["TNFW", "CONVERGENCE"], lens_list, kw, z, 2.5, len(lens_list) + 9, x, y)
+
+    # main deflector (EPL + SHEAR on one plane) with halos before, on and behind it
+    unique = ["EPL", "SHEAR", "TNFW", "NFW", "CONVERGENCE", "SIE"]
+    lens_list = ["TNFW", "EPL", "NFW", "SHEAR", "TNFW", "CONVERGENCE", "SIE", "TNFW"]
+    kw = [{"Rs": 0.05, "alpha_Rs": 0.004, "r_trunc": 0.6, "center_x": 0.9, "center_y": -0.4},
+          {"theta_E": 1.1, "gamma": 2.08, "e1": 0.07, "e2": -0.04, "center_x": 0.01,
+           "center_y": -0.02},
+          {"Rs": 0.4, "alpha_Rs": 0.05, "center_x": -0.8, "center_y": 1.2},
+          {"gamma1": 0.03, "gamma2": -0.015},
+          {"Rs": 0.08, "alpha_Rs": 0.006, "r_trunc": 0.9, "center_x": -1.0, "center_y": -0.7},
+          {"kappa": 0.02, "ra_0": 0.1, "dec_0": -0.1},
+          {"theta_E": 0.15, "e1": 0.1, "e2": 0.0, "center_x": 1.3, "center_y": 0.6},
+          {"Rs": 0.03, "alpha_Rs": 0.002, "r_trunc": 0.3, "center_x": 0.2, "center_y": 1.0}]
+    z = [0.3, 0.5, 0.2, 0.5, 0.5, 0.9, 1.4, 0.9]
+    x, y = _points(rng, 400)
+    run("main_lens", unique, lens_list, kw, z, 2.0, None, x, y)
+
+    # one deflector, the source step only after it
+    x, y = _points(rng, 50)
+    run("single", ["SIE"], ["SIE"], [{"theta_E": 0.8, "e1": 0.05, "e2": 0.1}], [0.4], 1.2, 1,
+        x, y)
+    return cases
+
+
 def gen_linear():
     """ImageLinearFit (image_linear_solve.py) on small scenes: amplitudes, model
     image, inverse normal matrix (source_marg) and logL."""
@@ -469,6 +553,15 @@ def main(reference_root):
             arrays["%s_%d" % (k, i)] = c.pop(k)
         meta.append(c)
     _save(os.path.join(HERE, "bulk.npz"), arrays, meta)
+    mp = gen_multi_plane(np.random.default_rng(20240604))
+    arrays, meta = {}, []
+    for i, c in enumerate(mp):
+        for k in ("x", "y", "bx", "by"):
+            arrays["%s_%d" % (k, i)] = c.pop(k)
+        for k, v in c.pop("prep").items():
+            arrays["prep_%d_%s" % (i, k)] = v
+        meta.append(c)
+    _save(os.path.join(HERE, "multiplane.npz"), arrays, meta)
     lin = gen_linear()
     arrays, meta = {}, []
     for i, c in enumerate(lin):
@@ -479,7 +572,7 @@ def main(reference_root):
         meta.append(c)
     _save(os.path.join(HERE, "linear.npz"), arrays, meta)
     print("wrote", len(cases), "profile cases,", len(scenes), "image scenes,", len(bulk),
-          "bulk cases,", len(lin), "linear-solve cases")
+          "bulk cases,", len(mp), "multi-plane cases,", len(lin), "linear-solve cases")
 
 
 if __name__ == "__main__":

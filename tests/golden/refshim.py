@@ -470,6 +470,43 @@ class _Dummy:
         return _Dummy()
 
 
+class FlatLCDM:
+    """Stand-in for an astropy ``FlatLambdaCDM(H0, Om0, Tcmb0=0)`` instance: only the
+    two parameters, read by :class:`Background`."""
+
+    def __init__(self, H0=70.0, Om0=0.3):
+        self.H0 = H0
+        self.Om0 = Om0
+
+
+class Background:
+    """lenstronomy's ``Cosmo.background.Background`` distances (lenstronomy >= 1.13.6):
+    ``d_xy`` = astropy's ``angular_diameter_distance_z1z2`` in Mpc and
+    ``T_xy = d_xy (1 + z_source)``, for a flat matter + Lambda cosmology without
+    radiation: D_C = (c/H0) int dz / sqrt(Om0 (1+z)^3 + 1 - Om0) by adaptive
+    quadrature (scipy ``quad``), D_A(z1, z2) = D_C(z1, z2) / (1 + z2)."""
+
+    def __init__(self, cosmo):
+        self._h0 = float(cosmo.H0)
+        self._om = float(cosmo.Om0)
+
+    def _dc(self, z1, z2):
+        from scipy.integrate import quad
+        f = lambda z: 1.0 / np.sqrt(self._om * (1 + z) ** 3 + 1 - self._om)  # noqa: E731
+        val, _ = quad(f, float(z1), float(z2), epsabs=0, epsrel=1e-13, limit=200)
+        return 299792.458 / self._h0 * val
+
+    def d_xy(self, z_observer, z_source):
+        zo = np.asarray(z_observer, dtype=float)
+        zs = np.asarray(z_source, dtype=float)
+        zo, zs = np.broadcast_arrays(zo, zs)
+        out = np.array([self._dc(a, b) / (1 + b) for a, b in zip(zo.ravel(), zs.ravel())])
+        return out.reshape(zo.shape) if zo.ndim else float(out[0])
+
+    def T_xy(self, z_observer, z_source):
+        return self.d_xy(z_observer, z_source) * (1 + np.asarray(z_source, dtype=float))
+
+
 def install_lenstronomy():
     def mod(name, **attrs):
         m = types.ModuleType(name)
@@ -520,7 +557,7 @@ def install_lenstronomy():
     cl = mod("lenstronomy.Conf.config_loader", conventions_conf=lambda: {})
     mod("lenstronomy.Conf", config_loader=cl)
     lc = mod("lenstronomy.Cosmo.lens_cosmo", LensCosmo=_Dummy)
-    bg = mod("lenstronomy.Cosmo.background", Background=_Dummy)
+    bg = mod("lenstronomy.Cosmo.background", Background=Background)
     mod("lenstronomy.Cosmo", lens_cosmo=lc, background=bg)
     mod("lenstronomy")
     cosmo = mod("astropy.cosmology", default_cosmology=_Dummy())

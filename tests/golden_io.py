@@ -72,6 +72,24 @@ def bulk_cases():
     return out
 
 
+def multi_plane_cases():
+    """MultiPlaneBulk cases: unique list, lens list, kwargs, redshifts, rays, the
+    reference's prepared kwargs (``prep``) and beta.  Distances of the reference run:
+    flat Lambda-CDM, H0 = 70, Om0 = 0.3, no radiation."""
+    d, meta = load("multiplane.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        for k in ("x", "y", "bx", "by"):
+            c[k] = d["%s_%d" % (k, i)]
+        pre = "prep_%d_" % i
+        prep = {k[len(pre):]: d[k] for k in d.files if k.startswith(pre)}
+        c["prep"] = {"all_kwargs": {k[3:]: v for k, v in prep.items() if k.startswith("kw_")},
+                     **{k: v for k, v in prep.items() if not k.startswith("kw_")}}
+        out.append(c)
+    return out
+
+
 def linear_cases():
     """ImageLinearFit cases: kwargs, data, mask and the reference's amplitudes,
     model image, inverse normal matrix (source_marg) and logL."""

@@ -4,6 +4,7 @@ reference's construction-time errors, PSF kernels and workload generation."""
 import numpy as np
 import pytest
 
+import golden_io
 import jaxtronomy_gb300 as J
 from jaxtronomy_gb300 import profiles, workloads as W
 
@@ -164,8 +165,6 @@ def test_bulk_pack_reproduces_positional_binding():
 
 def test_bulk_errors_mirror_reference():
     with pytest.raises(ValueError):
-        J.LensModelBulk(["EPL"], multi_plane=True)
-    with pytest.raises(ValueError):
         J.LensModelBulk(["NOT_A_PROFILE"])
     b = J.LensModelBulk(["TNFW"])
     with pytest.raises(ValueError):
@@ -259,3 +258,59 @@ def test_flux_evaluate_indexes_subframe():
     with pytest.raises(ValueError):
         J.ImageModel(data, psf, J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
                      kwargs_numerics={"flux_evaluate_indexes": bad})
+
+
+@pytest.mark.parametrize("case", golden_io.multi_plane_cases(), ids=lambda c: c["tag"])
+def test_multi_plane_prepare_matches_reference(case):
+    """LensModelBulk(multi_plane=True).prepare_ray_shooting_kwargs against the
+    reference's own output (multi_plane_bulk.py:57-150): redshift sort, NULL source
+    and filler steps, zero-filled arrays; distance lists from FlatLambdaCDM(70, 0.3)
+    against the goldens' independent quadrature."""
+    b = J.LensModelBulk(case["unique"], multi_plane=True, cosmo=J.FlatLambdaCDM(70.0, 0.3))
+    rk = b.prepare_ray_shooting_kwargs(case["lens_list"], case["kwargs"],
+                                       z_source=case["z_source"], lens_redshift_list=case["z"],
+                                       num_deflectors=case["num_deflectors"])
+    ref = case["prep"]
+    np.testing.assert_array_equal(rk["index_list"], ref["index_list"])
+    assert set(rk["all_kwargs"]) == set(ref["all_kwargs"])
+    for k, v in ref["all_kwargs"].items():
+        np.testing.assert_array_equal(rk["all_kwargs"][k], v)
+    for k in ("T_ij_list", "T_z_list", "reduced2physical_factor"):
+        np.testing.assert_allclose(rk[k], ref[k], rtol=1e-12, atol=0)
+
+
+def test_multi_plane_errors_mirror_reference():
+    b = J.LensModelBulk(["TNFW"], multi_plane=True, cosmo=J.FlatLambdaCDM())
+    kw = [{"Rs": 0.1, "alpha_Rs": 0.01, "r_trunc": 1.0}]
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW"], kw, z_source=2.0)
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW"], kw, lens_redshift_list=[0.5])
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW"], kw, z_source=2.0, lens_redshift_list=[0.5, 0.6])
+    with pytest.raises(ValueError):
+        b.prepare_ray_shooting_kwargs(["TNFW", "TNFW"], kw * 2, z_source=2.0,
+                                      lens_redshift_list=[0.5, 0.6], num_deflectors=1)
+    try:
+        import astropy  # noqa: F401
+    except ImportError:
+        with pytest.raises(ValueError):
+            J.LensModelBulk(["TNFW"], multi_plane=True)
+
+
+def test_flat_lcdm_distances():
+    """FlatLambdaCDM against closed forms: Einstein-de Sitter (Om0 = 1),
+    D_C = 2 (c/H0) (1 - 1/sqrt(1+z)); de Sitter (Om0 = 0), D_C = (c/H0) z; and
+    additivity of comoving distance (flat: T_xy(z1, z3) = T_xy(z1, z2) + T_xy(z2, z3))."""
+    from jaxtronomy_gb300 import cosmology
+    dh = cosmology.C_KM_S / 70.0
+    for z in (0.1, 0.5, 2.5, 6.0):
+        eds = J.FlatLambdaCDM(70.0, 1.0).comoving_distance(z)
+        assert abs(eds - 2 * dh * (1 - 1 / np.sqrt(1 + z))) <= 1e-13 * eds
+        ds = J.FlatLambdaCDM(70.0, 0.0).comoving_distance(z)
+        assert abs(ds - dh * z) <= 1e-13 * ds
+    bg = cosmology.Background(J.FlatLambdaCDM(67.0, 0.31))
+    t13, t12, t23 = bg.T_xy(0.2, 2.4), bg.T_xy(0.2, 0.9), bg.T_xy(0.9, 2.4)
+    assert abs(t13 - (t12 + t23)) <= 1e-12 * t13
+    d = bg.d_xy(np.array([0.1, 0.5]), np.array([1.0, 1.0]))
+    assert d.shape == (2,) and abs(d[1] - bg.d_xy(0.5, 1.0)) == 0

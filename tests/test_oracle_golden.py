@@ -114,6 +114,70 @@ def test_bulk_equals_single_plane_sum():
     np.testing.assert_allclose(by, sy, rtol=1e-13, atol=1e-15)
 
 
+def _ref_background():
+    """The flat Lambda-CDM background the multi-plane goldens were made with."""
+    import os
+    import sys
+    sys.path.insert(0, golden_io.GOLDEN)
+    import refshim
+    return refshim.Background(refshim.FlatLCDM(70.0, 0.3))
+
+
+@pytest.mark.parametrize("case", golden_io.multi_plane_cases(), ids=lambda c: c["tag"])
+def test_multi_plane_prepare_matches_reference(case):
+    """Oracle MultiPlaneBulk.prepare_ray_shooting_kwargs: sorting, NULL source and
+    filler steps, zero-filled arrays and distance lists, as the reference made them."""
+    bg = _ref_background()
+    rk = lens.multi_plane_prepare(case["unique"], case["lens_list"], case["kwargs"],
+                                  case["z_source"], case["z"], bg.d_xy, bg.T_xy,
+                                  case["num_deflectors"])
+    ref = case["prep"]
+    np.testing.assert_array_equal(rk["index_list"], ref["index_list"])
+    assert set(rk["all_kwargs"]) == set(ref["all_kwargs"])
+    for k, v in ref["all_kwargs"].items():
+        np.testing.assert_array_equal(rk["all_kwargs"][k], v)
+    for k in ("T_ij_list", "T_z_list", "reduced2physical_factor"):
+        np.testing.assert_allclose(rk[k], ref[k], rtol=1e-14, atol=0)
+
+
+@pytest.mark.parametrize("case", golden_io.multi_plane_cases(), ids=lambda c: c["tag"])
+def test_multi_plane_ray_shooting_matches_reference(case):
+    """Oracle MultiPlaneBulk.ray_shooting on the reference's prepared kwargs."""
+    ref = case["prep"]
+    bx, by = lens.multi_plane_ray_shooting(case["unique"], case["x"], case["y"],
+                                           ref["all_kwargs"], ref["index_list"],
+                                           ref["T_ij_list"], ref["T_z_list"],
+                                           ref["reduced2physical_factor"])
+    np.testing.assert_allclose(bx, case["bx"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(by, case["by"], rtol=1e-12, atol=1e-14)
+
+
+def test_multi_plane_one_plane_equals_single_plane():
+    """All deflectors on one plane: the multi-plane recurrence reduces to the
+    single-plane sum scaled by r2p (D_s / D_ds) and T_ij/T_z (flat cosmology)."""
+    case = golden_io.bulk_cases()[1]
+    rk = lens.bulk_prepare(case["unique"], case["lens_list"], case["kwargs"])
+    n = len(rk["index_list"])
+    bg = _ref_background()
+    zl, zs = 0.5, 2.0
+    T_l, T_s = bg.T_xy(0, zl), bg.T_xy(0, zs)
+    r2p = bg.d_xy(0, zs) / bg.d_xy(zl, zs)
+    idx = np.append(rk["index_list"], len(case["unique"]))
+    kw = {k: np.append(v, 0.0) for k, v in rk["all_kwargs"].items()}
+    T_ij = np.array([T_l] + [0.0] * (n - 1) + [bg.T_xy(zl, zs)])
+    T_z = np.array([T_l] * n + [T_s])
+    r = np.array([r2p] * n + [0.0])
+    bx, by = lens.multi_plane_ray_shooting(case["unique"], case["x"], case["y"], kw, idx, T_ij,
+                                           T_z, r)
+    sx, sy = lens.bulk_ray_shooting(case["unique"], case["x"], case["y"], rk["all_kwargs"],
+                                    rk["index_list"])
+    # beta = theta - alpha_red r2p D_ls T... ; with T_ij = T_s - T_l (flat):
+    # beta = theta - (theta - s) r2p (T_s - T_l) / T_s where s = single-plane beta
+    scale = r2p * bg.T_xy(zl, zs) / T_s
+    np.testing.assert_allclose(bx, case["x"] - (case["x"] - sx) * scale, rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(by, case["y"] - (case["y"] - sy) * scale, rtol=1e-12, atol=1e-13)
+
+
 @pytest.mark.parametrize("case", golden_io.linear_cases(), ids=lambda c: c["tag"])
 def test_linear_solve_matches_reference(case):
     """oracle.linear against the reference's ImageLinearFit (amplitudes, model

@@ -7,7 +7,8 @@ kernel (``lensgb_loglike_grad``), computed together with the forward pass so
 the ray grid is traced twice in all (forward image, adjoint), never stored.
 This is what ``jax.grad`` through the reference's
 ``ImageModel.likelihood_data_given_model`` (``image_model.py:163-221``)
-provides, for the profiles the adjoint supports (EPL, SHEAR, Sersic).
+provides, for the profiles the adjoint supports (EPL, SIE, NIE, NFW, TNFW,
+SHEAR lenses; Sersic light).
 """
 
 import torch

@@ -147,7 +147,7 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
 // FP64 from an FP64 offset, both summed as FP32 pairs.
 // ---------------------------------------------------------------------------
 constexpr int MP_THREADS = 64;
-constexpr int MP_RPT = 2;
+constexpr int MP_RPT = 3;
 constexpr int MP_CHUNK = 64;
 constexpr int PL_F = 8;  // per-step floats: dT hi/lo, 1/T_z hi/lo, eps, r2p hi/lo, tag bits
 
@@ -165,44 +165,52 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Plane table of n_steps steps (one CTA): pl_f receives the FP32 step constants
-// and the step's tag with BULK_TAG_PLANE where a new plane starts, eps_d the
-// FP64 eps.
-__global__ void __launch_bounds__(1024)
+// Plane table of n_steps steps, one CTA of PREP_THREADS per PREP_THREADS steps:
+// pl_f receives the FP32 step constants and the step's tag with
+// BULK_TAG_PLANE where a new plane starts, eps_d the FP64 eps.  Each CTA sums
+// the T_ij before its steps itself (T_cum needs only ~1e-16 relative accuracy:
+// it enters eps, a correction to the ray offset).
+constexpr int PREP_THREADS = 64;
+
+__global__ void __launch_bounds__(PREP_THREADS)
 plane_prepare_kernel(const double* __restrict__ dT, const double* __restrict__ Tz,
                      const double* __restrict__ r2p, int n_steps, const int* __restrict__ tag,
                      float* __restrict__ pl_f, double* __restrict__ eps_d) {
-    __shared__ double part[1024];
-    const int t = threadIdx.x, nt = blockDim.x;
-    const int seg = (n_steps + nt - 1) / nt;
-    const int lo = min(n_steps, t * seg), hi = min(n_steps, lo + seg);
+    __shared__ double sc[PREP_THREADS];
+    const int t = threadIdx.x;
+    const int i0 = blockIdx.x * PREP_THREADS;
+    const int i = i0 + t;
     double acc = 0.0;
-    for (int i = lo; i < hi; ++i) acc += dT[i];
-    part[t] = acc;
+    for (int k = t; k < i0; k += PREP_THREADS) acc += dT[k];
+    sc[t] = acc;
     __syncthreads();
-    if (t == 0) {
-        double run = 0.0;
-        for (int k = 0; k < nt; ++k) {
-            const double v = part[k];
-            part[k] = run;
-            run += v;
-        }
+    for (int w = PREP_THREADS / 2; w > 0; w >>= 1) {
+        if (t < w) sc[t] += sc[t + w];
+        __syncthreads();
     }
+    const double before = sc[0];
     __syncthreads();
-    double cum = part[t];
-    for (int i = lo; i < hi; ++i) {
-        cum += dT[i];
-        const bool start = i == 0 || dT[i] != 0.0 || Tz[i] != Tz[i - 1] || r2p[i] != r2p[i - 1];
-        const int tg = tag[i] | (start ? BULK_TAG_PLANE : 0);
-        const double e = cum / Tz[i] - 1.0;
-        eps_d[i] = e;
-        float* f = pl_f + (long long)i * PL_F;
-        split_double(dT[i], f[0], f[1]);
-        split_double(1.0 / Tz[i], f[2], f[3]);
-        f[4] = (float)e;
-        split_double(r2p[i], f[5], f[6]);
-        f[7] = __int_as_float(tg);
+    // inclusive scan of this CTA's T_ij (Hillis-Steele)
+    sc[t] = i < n_steps ? dT[i] : 0.0;
+    __syncthreads();
+    for (int w = 1; w < PREP_THREADS; w <<= 1) {
+        const double v = t >= w ? sc[t - w] : 0.0;
+        __syncthreads();
+        sc[t] += v;
+        __syncthreads();
     }
+    if (i >= n_steps) return;
+    const double cum = before + sc[t];
+    const bool start = i == 0 || dT[i] != 0.0 || Tz[i] != Tz[i - 1] || r2p[i] != r2p[i - 1];
+    const int tg = tag[i] | (start ? BULK_TAG_PLANE : 0);
+    const double e = cum / Tz[i] - 1.0;
+    eps_d[i] = e;
+    float* f = pl_f + (long long)i * PL_F;
+    split_double(dT[i], f[0], f[1]);
+    split_double(1.0 / Tz[i], f[2], f[3]);
+    f[4] = (float)e;
+    split_double(r2p[i], f[5], f[6]);
+    f[7] = __int_as_float(tg);
 }
 
 // (h, l) += (bh, bl) for FP32 pairs with |l| << |h|.
@@ -222,8 +230,11 @@ __device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl,
     pl = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, pl));
 }
 
+// 3 rays per thread and 160 registers: a 400^2-ray call (834 CTAs of 64
+// threads) is resident in one wave at 6 CTAs per SM with no spills; fewer
+// registers made the compiler rebuild ray state in FP64 or spill.
 template <bool F32>
-__global__ void __maxnreg__(112)
+__global__ void __maxnreg__(160)
 multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
                    const float* __restrict__ rec_f, const double* __restrict__ coef_d,
                    const float* __restrict__ coef_f, const float* __restrict__ pl_f,
@@ -450,7 +461,9 @@ int launch_multi_plane(int* tag, const double* rec_d, const float* rec_f, const 
                        cudaStream_t stream) {
     if (n <= 0 || n_steps <= 0) return 0;
     const bool f32 = precision == LENSGB_FP32_SPLIT;
-    if (f32) plane_prepare_kernel<<<1, 1024, 0, stream>>>(dT, Tz, r2p, n_steps, tag, pl_f, eps_d);
+    if (f32)
+        plane_prepare_kernel<<<(n_steps + PREP_THREADS - 1) / PREP_THREADS, PREP_THREADS, 0,
+                               stream>>>(dT, Tz, r2p, n_steps, tag, pl_f, eps_d);
     const long long per_cta = (long long)MP_THREADS * MP_RPT;
     const long long blocks = (n + per_cta - 1) / per_cta;
     if (f32)

@@ -301,6 +301,29 @@ int lensgb_linear_solve(const lensgb_model* model, const void* response_dev, int
  * (image_model.py:163-221): simulates the images into image_out_dev (caller
  * buffer, same layout as lensgb_image's output) and writes one FP64
  * log-likelihood per system to logl_dev. */
+/* The likelihood step of lensgb_loglike alone, on given model images (n_inst
+ * images in the model precision): Data.log_likelihood (imaging_data.py:159-182)
+ * with the model-based C_D (image_noise.py:100-137), e.g. after
+ * lensgb_point_sources_add.  FP64 logL per system to logl_dev. */
+int lensgb_loglike_image(const lensgb_model* model, const void* image_dev, int n_inst,
+                         const lensgb_noise_desc* noise, double* logl_dev, void* stream);
+
+/* ImageModel.point_source (jaxtronomy/ImSim/image_model.py:396-429) ->
+ * PointSourceRendering.point_source_rendering
+ * (ImSim/Numerics/point_source_rendering.py:34-77): adds to image_dev (n_inst
+ * images in the model precision) the point images of each system.  ps_dev:
+ * n_inst x n_images x 3 doubles (ra, dec, amp) -- PointSource.point_source_list
+ * after ImageModel._displace_astrometry.  kernel_dev: the kernel_size^2 kernel
+ * (doubles; the PSF at subgrid factor `subgrid`, or the 3x3 delta of an
+ * unconvolved call), kernel_stride doubles apart per system (0: one kernel
+ * for all).  Each image is the kernel bilinearly interpolated at the image
+ * position on the subgrid (zero outside the kernel, as jax.scipy.ndimage.
+ * map_coordinates order 1), summed over each pixel's subgrid^2 cells and
+ * scaled by amp and the model's flux_scaling.  Not for sub-frame models. */
+int lensgb_point_sources_add(const lensgb_model* model, const double* ps_dev, int n_images,
+                             int n_inst, const double* kernel_dev, int kernel_size,
+                             long long kernel_stride, int subgrid, void* image_dev, void* stream);
+
 int lensgb_loglike(lensgb_model* model, const double* params_dev, int n_inst,
                    const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
                    void* image_out_dev, double* logl_dev, void* stream);

@@ -11,10 +11,11 @@ from .lens_model import LensModel  # noqa: F401
 from .cosmology import FlatLambdaCDM  # noqa: F401
 from .lens_model_bulk import LensModelBulk, MultiPlaneBulk, SinglePlaneBulk  # noqa: F401
 from .light_model import LightModel  # noqa: F401
+from .point_source import PointSource  # noqa: F401
 from .sampling import ImageLikelihood, LikelihoodModule, Param, prepare_logL_func  # noqa: F401
 
 __version__ = "0.1.0"
 
 __all__ = ["ImageData", "PSF", "PixelGrid", "ImageModel", "LensModel", "LensModelBulk", "LightModel",
-           "MultiPlaneBulk", "SinglePlaneBulk", "FlatLambdaCDM",
+           "MultiPlaneBulk", "SinglePlaneBulk", "FlatLambdaCDM", "PointSource",
            "ImageLikelihood", "LikelihoodModule", "Param", "prepare_logL_func"]

@@ -249,7 +249,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 112; }
+int lensgb_version(void) { return 113; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -1064,6 +1064,63 @@ int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void
     launch_loglike(image_out, n_inst, (long long)m->desc.nx * m->desc.ny, a, logl,
                    m->desc.precision, (cudaStream_t)stream);
     return check_cuda("likelihood launch");
+}
+
+int lensgb_loglike_image(const lensgb_model* m, const void* image, int n_inst,
+                         const lensgb_noise_desc* nd, double* logl, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_inst < 0) return fail(LENSGB_ERR_INVALID, "negative system count");
+    if (n_inst == 0) return LENSGB_OK;
+    if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
+    if (!image || !logl) return fail(LENSGB_ERR_INVALID, "null image or logL pointer");
+    if (!nd->noise_map_dev && !nd->exposure_map_dev && !(nd->exposure_time > 0))
+        return fail(LENSGB_ERR_INVALID, "exposure time must be positive without a noise map");
+    if (nd->data_stride < 0 || nd->noise_stride < 0 || nd->exposure_stride < 0 ||
+        nd->mask_stride < 0)
+        return fail(LENSGB_ERR_INVALID, "negative stride");
+    LoglikeArgs a;
+    a.data = nd->data_dev;
+    a.data_stride = nd->data_stride;
+    a.mask = nd->mask_dev;
+    a.mask_stride = nd->mask_stride;
+    a.noise_map = nd->noise_map_dev;
+    a.noise_stride = nd->noise_stride;
+    a.exposure = nd->exposure_map_dev;
+    a.exposure_stride = nd->exposure_stride;
+    a.exposure_time = nd->exposure_time;
+    a.background_rms = nd->background_rms;
+    a.error_map = nd->error_map_dev;
+    launch_loglike(image, n_inst, (long long)m->desc.nx * m->desc.ny, a, logl, m->desc.precision,
+                   (cudaStream_t)stream);
+    return check_cuda("likelihood launch");
+}
+
+int lensgb_point_sources_add(const lensgb_model* m, const double* ps, int n_images, int n_inst,
+                             const double* kernel, int kernel_size, long long kernel_stride,
+                             int subgrid, void* image, void* stream) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (n_images < 0 || n_inst < 0 || n_inst > 65535)
+        return fail(LENSGB_ERR_INVALID, "n_images >= 0 and n_inst in 0..65535 required");
+    if (n_images == 0 || n_inst == 0) return LENSGB_OK;
+    if (!ps || !kernel || !image) return fail(LENSGB_ERR_INVALID, "null point, kernel or image");
+    if (kernel_size < 1 || kernel_size % 2 == 0)
+        return fail(LENSGB_ERR_INVALID, "kernel dimensions must be odd");
+    if (kernel_stride != 0 && kernel_stride < (long long)kernel_size * kernel_size)
+        return fail(LENSGB_ERR_INVALID, "kernel stride smaller than one kernel");
+    if (subgrid < 1) return fail(LENSGB_ERR_INVALID, "subgrid factor must be >= 1");
+    if (m->sub)
+        return fail(LENSGB_ERR_UNSUPPORTED, "point sources on a sub-frame model");
+    // PixelGrid: Ma2pix = inverse(transform_pix2angle), pixel position of ra = dec = 0
+    const double* T = m->desc.transform_pix2angle;
+    const double det = T[0] * T[3] - T[1] * T[2];
+    if (!(det != 0.0)) return fail(LENSGB_ERR_INVALID, "singular pixel transform");
+    const double M[4] = {T[3] / det, -T[1] / det, -T[2] / det, T[0] / det};
+    const double ra0 = -m->desc.ra_at_xy_0, dec0 = -m->desc.dec_at_xy_0;
+    const double x0 = M[0] * ra0 + M[1] * dec0, y0 = M[2] * ra0 + M[3] * dec0;
+    launch_point_sources(ps, n_images, n_inst, kernel, kernel_size, kernel_stride, subgrid, M, x0,
+                         y0, m->desc.ny, m->desc.nx, m->desc.flux_scaling, image,
+                         m->desc.precision, (cudaStream_t)stream);
+    return check_cuda("point-source rendering launch");
 }
 
 int lensgb_linear_solve(const lensgb_model* m, const void* A, int n_linear, int n_inst,

@@ -177,6 +177,13 @@ int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* r
                              const double* coef_d, const float* coef_f, int n_defl,
                              const double* x, const double* y, double* bx, double* by,
                              long long n, int precision, cudaStream_t stream);
+// Point-source rendering: adds to out (n_inst images of rows x cols, model
+// precision) the n_img images (ra, dec, amp) of each system, the kernel
+// (ks x ks doubles; kstride per system, 0: shared) at subgrid factor p.
+int launch_point_sources(const double* ps, int n_img, int n_inst, const double* K, int ks,
+                         long long kstride, int p, const double* Ma2pix, double x0, double y0,
+                         int rows, int cols, double scale, void* out, int precision,
+                         cudaStream_t stream);
 // MultiPlaneBulk.ray_shooting over n_steps redshift-ordered steps (tags and
 // records from launch_bulk_prepare; T_ij, T_z, r2p per step) for n rays
 // starting at angles (ax, ay).  FP32_SPLIT also writes the plane table pl_f

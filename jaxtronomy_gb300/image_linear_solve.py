@@ -31,6 +31,8 @@ class ImageLinearFit(ImageModel):
                          lens_light_model_class, point_source_class, extinction_class,
                          kwargs_numerics, likelihood_mask, psf_error_map_bool_list,
                          kwargs_pixelbased)
+        if self._n_ps:
+            raise ValueError("the linear solve with point-source amplitudes is not supported")
         self._n_src = len(self.SourceModel.profile_type_list)
         self._n_ll = len(self.LensLightModel.profile_type_list)
         if self._n_src + self._n_ll > _lib.LINEAR_MAX:

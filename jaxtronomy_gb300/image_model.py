@@ -26,6 +26,7 @@ from . import _device, _lib, profiles
 from .data import PSF
 from .lens_model import LensModel
 from .light_model import LightModel
+from .point_source import PointSource
 
 _NUMERICS_KEYS = {
     "supersampling_factor", "compute_mode", "supersampling_convolution",
@@ -33,6 +34,14 @@ _NUMERICS_KEYS = {
     "compute_indexes", "point_source_supersampling_factor", "convolution_kernel_size",
     "convolution_type", "truncation_conv", "precision", "fp32_refine_tol", "fp32_refine_kappa",
 }
+
+
+def _delta_kernel():
+    """The 3x3 kernel of an unconvolved point source (point_source_rendering.py:59-61) and
+    of a NONE PSF."""
+    k = np.zeros((3, 3))
+    k[1, 1] = 1.0
+    return k
 
 
 def fwhm2sigma(fwhm):
@@ -159,9 +168,12 @@ class ImageModel:
             raise ValueError("pixelbased solver not supported")
         if extinction_class is not None and getattr(extinction_class, "_profile_type_list", []):
             raise ValueError("extinction is not supported")
-        if point_source_class is not None and len(getattr(point_source_class,
-                                                          "point_source_type_list", [])) > 0:
-            raise ValueError("point sources are not supported by this build")
+        if point_source_class is None:
+            point_source_class = PointSource([], lens_model=lens_model_class)
+        if not isinstance(point_source_class, PointSource):
+            raise ValueError("point_source_class must be a jaxtronomy_gb300.PointSource")
+        self.PointSource = point_source_class
+        self._n_ps = len(point_source_class.point_source_type_list)
         if data_class.primary_beam is not None:
             raise ValueError("primary beam not supported")
         self.LensModel = lens_model_class if lens_model_class is not None else LensModel([])
@@ -218,6 +230,25 @@ class ImageModel:
             self._low_kernel_size = int(lo.shape[0])
         self._kernel_dev = None
         self._models = {}
+        # point-source rendering kernel (numerics.py:147-151, point_source_rendering.py:14-32)
+        self._ps_sub = int(kn.get("point_source_supersampling_factor", 1))
+        self._ps_kernel = None
+        if self._n_ps:
+            if self._subframe is not None:
+                raise ValueError("point sources with flux_evaluate_indexes are not supported")
+            if self.PSF.psf_variance_map_bool:
+                raise ValueError("PSF variance maps (point-source error maps) are not supported")
+            if self._ps_sub < 1:
+                raise ValueError("point_source_supersampling_factor must be >= 1")
+            if pt == "PIXEL":
+                ps_k = (psf_class.kernel_point_source if self._ps_sub == 1
+                        else psf_class.kernel_point_source_supersampled(self._ps_sub))
+            elif pt == "NONE":
+                ps_k = _delta_kernel()
+            else:
+                raise ValueError("point sources need a PIXEL or NONE PSF (the pixelised "
+                                 "GAUSSIAN kernel of lenstronomy's PSF is not provided)")
+            self._ps_kernel = np.ascontiguousarray(ps_k, dtype=np.float64)
 
     # ------------------------------------------------------------------ models
     def _desc(self, lens_idx, src_idx, ll_idx, lensed=True):
@@ -389,6 +420,66 @@ class ImageModel:
         del keep
         return out
 
+    # ------------------------------------------------------------------ point sources
+    def point_source_rows(self, kwargs_ps, kwargs_special=None, B=None, k=None):
+        """(B, n_images, 3) FP64 rows (ra, dec, amp): PointSource.point_source_list
+        (point_source.py:255-284) after ImageModel._displace_astrometry
+        (image_model.py:652-676), broadcast over a batch of B systems."""
+        ra, dec, amp = self.PointSource.point_source_list(kwargs_ps, k=k)
+        ra, dec, amp = (np.atleast_2d(np.asarray(a, dtype=float)) for a in (ra, dec, amp))
+        n = ra.shape[-1]
+        if kwargs_special is not None and "delta_x_image" in kwargs_special:
+            shifts = []
+            for key in ("delta_x_image", "delta_y_image"):
+                d = np.atleast_2d(np.asarray(kwargs_special[key], dtype=float))[..., :n]
+                pad = np.zeros(d.shape[:-1] + (n - d.shape[-1],))
+                shifts.append(np.concatenate([d, pad], axis=-1))
+            ra, dec = ra + shifts[0], dec + shifts[1]
+        ra, dec, amp = np.broadcast_arrays(ra, dec, amp)
+        Bp = ra.shape[0]
+        if B is None:
+            B = Bp
+        if Bp not in (1, B):
+            raise ValueError("point-source kwargs have %d systems, the call %d" % (Bp, B))
+        rows = np.stack([ra, dec, amp], axis=-1)
+        return np.array(np.broadcast_to(rows, (B, n, 3)), dtype=np.float64)
+
+    def _add_point_sources(self, out, B, kwargs_ps, kwargs_special=None, unconvolved=False,
+                           psf_kernels=None, stream=None, k=None):
+        """Adds ImageModel.point_source (image_model.py:396-429) to the (B, ny, nx)
+        images ``out`` on the GPU (``lensgb_point_sources_add``)."""
+        if not self._n_ps:
+            return out
+        if kwargs_ps is None:
+            raise ValueError("kwargs_ps is needed for the point-source models %s"
+                             % self.PointSource.point_source_type_list)
+        rows = self.point_source_rows(kwargs_ps, kwargs_special, B, k=k)
+        n = rows.shape[1]
+        if n == 0:
+            return out
+        ps = _device.to_device_f64(rows)
+        kstride = 0
+        if unconvolved:
+            kern = _delta_kernel()
+        elif psf_kernels is not None and self._ps_sub == 1 and self._psf_type == _lib.PSF_PIXEL:
+            kern = psf_kernels.cpu().numpy() if isinstance(psf_kernels, torch.Tensor) \
+                else np.asarray(psf_kernels, dtype=float)
+            if kern.ndim == 3 and kern.shape[0] > 1:
+                kstride = kern.shape[1] * kern.shape[2]
+            kern = kern.reshape((-1,) + kern.shape[-2:])[0] if kstride == 0 else kern
+        else:
+            kern = self._ps_kernel
+        kt = _device.to_device_f64(np.ascontiguousarray(kern, dtype=np.float64))
+        model = self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list)))
+        _lib.check(_lib.load().lensgb_point_sources_add(
+            model.handle, _device.ptr(ps), n, B, _device.ptr(kt), int(kern.shape[-1]), kstride,
+            self._ps_sub, _device.ptr(out),
+            _device.stream_handle(stream)))
+        self._ps_keep = (ps, kt)
+        return out
+
     def host_wait(self, stream=None):
         """Makes ``stream`` wait for every image copy of earlier host-output calls."""
         model = self._model(range(len(self.LensModel.lens_model_list)),
@@ -443,7 +534,8 @@ class ImageModel:
 
     def image_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                     unconvolved=False, source_add=True, lens_light_add=True, psf_kernels=None,
-                    out=None, stream=None, rows=None):
+                    out=None, stream=None, rows=None, kwargs_ps=None, kwargs_special=None,
+                    point_source_add=True):
         """Batched ``image``: kwargs values are arrays of length B (or scalars).
         Returns a (B, ny, nx) CUDA tensor in the model precision.  ``psf_kernels``
         may give one (K, K) kernel or one per system (B, K, K) in place of the
@@ -453,7 +545,9 @@ class ImageModel:
         ``lensgb_image_host``: the images are copied back on a second stream,
         overlapping the next call's work (page-locked buffers give the overlap);
         ``out`` is complete after :meth:`host_wait` and a synchronization of the
-        stream (or a device synchronization)."""
+        stream (or a device synchronization).  Point sources (``kwargs_ps``, values
+        of shape (n_images,) or (B, n_images)) are rendered on the GPU and added
+        after the convolution, as ``ImageModel.image`` adds ``point_source``."""
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
                             range(len(self.LensLightModel.profile_type_list)))
@@ -462,11 +556,21 @@ class ImageModel:
         flags = ((_lib.UNCONVOLVED if unconvolved else 0)
                  | (0 if source_add else _lib.NO_SOURCE)
                  | (0 if lens_light_add else _lib.NO_LENS_LIGHT))
-        if isinstance(out, torch.Tensor) and out.device.type == "cpu":
+        with_ps = bool(self._n_ps) and point_source_add
+        host_out = isinstance(out, torch.Tensor) and out.device.type == "cpu"
+        if host_out and not with_ps:
             return self._launch_host(model, rows, flags, psf_kernels, out, stream)
         rows_dev = _device.to_device_f64(rows)
         B = rows_dev.shape[0]
-        return self._launch(model, rows_dev, B, flags, psf_kernels, out, stream)
+        dev_out = self._launch(model, rows_dev, B, flags, psf_kernels,
+                               None if host_out else out, stream)
+        if with_ps:
+            self._add_point_sources(dev_out, B, kwargs_ps, kwargs_special, unconvolved,
+                                    psf_kernels, stream)
+        if host_out:
+            out.copy_(dev_out)
+            return out
+        return dev_out
 
     # ------------------------------------------------------------------ reference API
     def image(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None, kwargs_ps=None,
@@ -477,7 +581,8 @@ class ImageModel:
             raise ValueError("Extinction is not implemented")
         im = self.image_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
                               unconvolved=unconvolved, source_add=source_add,
-                              lens_light_add=lens_light_add)
+                              lens_light_add=lens_light_add, kwargs_ps=kwargs_ps,
+                              kwargs_special=kwargs_special, point_source_add=point_source_add)
         return im[0].to(torch.float64).cpu().numpy()
 
     def source_surface_brightness(self, kwargs_source, kwargs_lens=None, kwargs_extinction=None,
@@ -557,9 +662,26 @@ class ImageModel:
         return nd
 
     def likelihood_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
-                         data=None, psf_kernels=None, rows=None, image_out=None, stream=None):
+                         data=None, psf_kernels=None, rows=None, image_out=None, stream=None,
+                         kwargs_ps=None, kwargs_special=None):
         """Batched ``likelihood_data_given_model``: (B,) FP64 CUDA tensor of
-        log-likelihoods; ``data`` optionally gives one (ny, nx) image per system."""
+        log-likelihoods; ``data`` optionally gives one (ny, nx) image per system.
+        With point-source models the model image (extended light + rendered point
+        sources) is made first and ``lensgb_loglike_image`` scores it."""
+        if self._n_ps:
+            im = self.image_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                  psf_kernels=psf_kernels, out=image_out, stream=stream,
+                                  rows=rows, kwargs_ps=kwargs_ps, kwargs_special=kwargs_special)
+            nt = self._noise_tensors(data)
+            nd = self._noise_desc(nt)
+            logl = torch.empty((im.shape[0],), dtype=torch.float64, device="cuda")
+            _lib.check(_lib.load().lensgb_loglike_image(
+                self._model(range(len(self.LensModel.lens_model_list)),
+                            range(len(self.SourceModel.profile_type_list)),
+                            range(len(self.LensLightModel.profile_type_list))).handle,
+                _device.ptr(im), im.shape[0], ctypes.byref(nd), _device.ptr(logl),
+                _device.stream_handle(stream)))
+            return logl
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
                             range(len(self.LensLightModel.profile_type_list)))
@@ -592,6 +714,8 @@ class ImageModel:
         SHEAR lenses and Sersic light."""
         if self._precision != _lib.FP64:
             raise ValueError("likelihood gradients need kwargs_numerics precision 'fp64'")
+        if self._n_ps:
+            raise ValueError("likelihood gradients with point sources are not supported")
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
                             range(len(self.LensLightModel.profile_type_list)))
@@ -640,12 +764,21 @@ class ImageModel:
             raise ValueError("check positive flux is not supported")
         if kwargs_extinction:
             raise ValueError("Extinction is not implemented")
-        return float(self.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light)[0].cpu())
+        return float(self.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                           kwargs_ps=kwargs_ps,
+                                           kwargs_special=kwargs_special)[0].cpu())
 
     def point_source(self, kwargs_ps, kwargs_lens=None, kwargs_special=None, unconvolved=False,
                      k=None):
-        """Point sources are not part of this build: always an empty image."""
-        return np.zeros((self._nx, self._ny))
+        """``image_model.py:396-429``: the rendered point sources alone (all models, or
+        the k-th)."""
+        if not self._n_ps:
+            return np.zeros((self._nx, self._ny))
+        rows = self.point_source_rows(kwargs_ps, kwargs_special, k=k)
+        out = torch.zeros((rows.shape[0], self._nx, self._ny), dtype=self._dtype, device="cuda")
+        self._add_point_sources(out, rows.shape[0], kwargs_ps, kwargs_special, unconvolved,
+                                k=k)
+        return out[0].to(torch.float64).cpu().numpy()
 
     def reduced_residuals(self, model, error_map=0):
         """(data - model) / sqrt(C_D_model + |error_map|) on the host."""

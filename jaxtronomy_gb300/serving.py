@@ -94,6 +94,8 @@ class Server:
         """Builds (without submitting) one request and the host buffers it names.
         ``data`` makes it a likelihood request using the model's ImageData
         ``background_rms`` / ``exposure_time``.  Returns (Request, keep, image, logl)."""
+        if getattr(image_model, "_n_ps", 0):
+            raise ValueError("serving requests with point sources are not supported")
         if getattr(image_model, "_subframe", None) is not None:
             raise ValueError("the server does not take models with flux_evaluate_indexes")
         model = image_model._model(range(len(image_model.LensModel.lens_model_list)),

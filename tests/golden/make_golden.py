@@ -16,6 +16,7 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
   images.npz    ImageModel.image and likelihood_data_given_model on small scenes
   bulk.npz      LensModelBulk.ray_shooting through many deflectors
   multiplane.npz LensModelBulk (multi-plane): prepared kwargs and ray shooting
+  point_sources.npz ImageModel with LENSED_POSITION / UNLENSED point sources
   linear.npz    ImageLinearFit: linear amplitude solve, model image, logL
 """
 
@@ -356,6 +357,75 @@ def gen_bulk(rng):
     return cases
 
 
+def gen_point_sources(rng):
+    """ImageModel with point sources (PointSource LENSED_POSITION + UNLENSED,
+    PointSourceRendering): images, the point-source term alone and a likelihood."""
+    from jaxtronomy.Data.imaging_data import ImageData
+    from jaxtronomy.ImSim.image_model import ImageModel
+    from jaxtronomy.LensModel.lens_model import LensModel
+    from jaxtronomy.LightModel.light_model import LightModel
+    from jaxtronomy.PointSource.point_source import PointSource
+    from jaxtronomy_gb300 import workloads as W
+
+    lens = [{"theta_E": 1.0, "gamma": 2.05, "e1": 0.06, "e2": -0.03, "center_x": 0.01,
+             "center_y": 0.0}, {"gamma1": 0.02, "gamma2": -0.01}]
+    src = [{"amp": 4.0, "R_sersic": 0.15, "n_sersic": 1.5, "e1": 0.05, "e2": 0.0,
+            "center_x": 0.03, "center_y": -0.02}]
+    ll = [{"amp": 6.0, "R_sersic": 0.7, "n_sersic": 3.0, "center_x": 0.0, "center_y": 0.0}]
+    out = []
+
+    def scene(tag, n, dpix, s, psf_kwargs, ps_kwargs, numerics=None, special=None,
+              unconvolved=False, flux_scaling=1.0):
+        g = W.grid_kwargs(n, dpix)
+        rng_d = np.random.default_rng(len(out) + 7)
+        data = rng_d.normal(0, 0.01, (n, n))
+        data_class = ImageData(image_data=data, exposure_time=800.0, background_rms=0.01,
+                               ra_at_xy_0=g["ra_at_xy_0"], dec_at_xy_0=g["dec_at_xy_0"],
+                               transform_pix2angle=g["transform_pix2angle"],
+                               flux_scaling=flux_scaling)
+        num = dict({"supersampling_factor": s}, **(numerics or {}))
+        im = ImageModel(data_class, refshim.PSF(**psf_kwargs), LensModel(["EPL", "SHEAR"]),
+                        LightModel(["SERSIC_ELLIPSE"]), LightModel(["SERSIC"]),
+                        point_source_class=PointSource(["LENSED_POSITION", "UNLENSED"]),
+                        kwargs_numerics=num)
+        image = np.asarray(im.image(lens, src, ll, ps_kwargs, kwargs_special=special,
+                                    unconvolved=unconvolved))
+        ps1 = np.asarray(im.point_source(ps_kwargs, lens, kwargs_special=special, k=1))
+        logl = float(im.likelihood_data_given_model(lens, src, ll, ps_kwargs,
+                                                    kwargs_special=special))
+        rec = {"tag": tag, "n": n, "dpix": dpix, "s": s, "numerics": numerics or {},
+               "psf": {k: v for k, v in psf_kwargs.items() if k != "kernel_point_source"},
+               "ps": ps_kwargs, "special": special, "unconvolved": unconvolved,
+               "flux_scaling": flux_scaling, "logL": logl, "image": image, "ps1": ps1,
+               "data": data, "lens": lens, "src": src, "ll": ll}
+        if "kernel_point_source" in psf_kwargs:
+            rec["kernel"] = np.asarray(psf_kwargs["kernel_point_source"], float)
+        out.append(rec)
+
+    k11 = W.gaussian_pixel_kernel(0.12, 0.08, 11)
+    # four lensed images (one near the field edge, one on a pixel centre), one
+    # unlensed image and one outside the field
+    ps = [{"ra_image": [1.02, -0.55, 0.31, -1.52], "dec_image": [0.11, 0.87, -0.98, -1.49],
+           "point_amp": [3.0, 2.2, 1.7, 0.9]},
+          {"ra_image": [0.4, 2.1], "dec_image": [1.2, 0.0], "point_amp": [1.3, 5.0]}]
+    scene("pixel_psf_s2", 40, 0.08, 2, {"psf_type": "PIXEL", "kernel_point_source": k11}, ps)
+    scene("pixel_psf_s2_shifted", 40, 0.08, 2, {"psf_type": "PIXEL", "kernel_point_source": k11},
+          ps, special={"delta_x_image": [0.013, -0.02], "delta_y_image": [0.007, 0.011]},
+          flux_scaling=1.3)
+    scene("pixel_psf_unconvolved", 40, 0.08, 1, {"psf_type": "PIXEL", "kernel_point_source": k11},
+          ps, unconvolved=True)
+    scene("none_psf", 36, 0.1, 1, {"psf_type": "NONE"}, ps)
+    # supersampled rendering: the supersampled kernel given, convolution on the
+    # supersampled grid, point_source_supersampling_factor 3
+    k33 = W.gaussian_pixel_kernel(0.12, 0.08 / 3, 33)
+    scene("supersampled_rendering_s3", 30, 0.08, 3,
+          {"psf_type": "PIXEL", "kernel_point_source": k33,
+           "point_source_supersampling_factor": 3}, ps,
+          numerics={"supersampling_convolution": True, "supersampling_kernel_size": None,
+                    "point_source_supersampling_factor": 3})
+    return out
+
+
 def gen_multi_plane(rng):
     """LensModelBulk (multi-plane, MultiPlaneBulk) through redshift-spread deflectors:
     the prepared kwargs (sorting, fillers, distance lists) and beta.  Distances come
@@ -553,6 +623,15 @@ def main(reference_root):
             arrays["%s_%d" % (k, i)] = c.pop(k)
         meta.append(c)
     _save(os.path.join(HERE, "bulk.npz"), arrays, meta)
+    pts = gen_point_sources(np.random.default_rng(20240605))
+    arrays, meta = {}, []
+    for i, c in enumerate(pts):
+        for k in ("image", "ps1", "data", "kernel"):
+            v = c.pop(k, None)
+            if v is not None:
+                arrays["%s_%d" % (k, i)] = v
+        meta.append(c)
+    _save(os.path.join(HERE, "point_sources.npz"), arrays, meta)
     mp = gen_multi_plane(np.random.default_rng(20240604))
     arrays, meta = {}, []
     for i, c in enumerate(mp):

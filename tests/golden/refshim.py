@@ -210,7 +210,17 @@ def install_jax():
     signal.convolve2d = lambda in1, in2, mode="full": np.asarray(
         scipy.signal.convolve2d(in1, in2, mode=mode)).view(AtArray)
     ndimage = types.ModuleType("jax.scipy.ndimage")
-    ndimage.map_coordinates = scipy.ndimage.map_coordinates
+
+    def _map_coordinates(input, coordinates, order, mode="constant", cval=0.0):
+        # jax.scipy.ndimage.map_coordinates reads every interpolation corner outside
+        # the input as cval ("constant"); SciPy calls that mode "grid-constant"
+        m = {"constant": "grid-constant"}.get(mode, mode)
+        return np.asarray(scipy.ndimage.map_coordinates(np.asarray(input, float),
+                                                        np.asarray(coordinates, float),
+                                                        order=order, mode=m, cval=cval,
+                                                        prefilter=False)).view(AtArray)
+
+    ndimage.map_coordinates = _map_coordinates
     jscipy.special = special
     jscipy.signal = signal
     jscipy.ndimage = ndimage
@@ -230,10 +240,17 @@ def install_jax():
     jax.Array = np.ndarray
     jax.devices = lambda *a, **k: ["cpu"]
     jax.debug = types.SimpleNamespace(print=lambda *a, **k: None)
+    # names the lens-equation solver module imports (never called on these paths)
+    jrandom = types.ModuleType("jax.random")
+    optimize = types.ModuleType("jax.scipy.optimize")
+    optimize.minimize = _Dummy()
+    jscipy.optimize = optimize
+    jax.random = jrandom
     mods = {
         "jax": jax, "jax.numpy": jnp, "jax.lax": lax, "jax.tree_util": tree_util,
         "jax.scipy": jscipy, "jax.scipy.special": special, "jax.scipy.signal": signal,
         "jax.scipy.ndimage": ndimage, "jax.experimental": experimental,
+        "jax.random": jrandom, "jax.scipy.optimize": optimize,
     }
     sys.modules.update(mods)
 
@@ -384,6 +401,10 @@ class PSF:
         if psf_type == "PIXEL":
             k = np.asarray(kernel_point_source, float)
             self._kernel = k / np.sum(k)
+        elif psf_type == "NONE":
+            # lenstronomy's PSF("NONE") carries a 3x3 delta kernel
+            self._kernel = np.zeros((3, 3))
+            self._kernel[1, 1] = 1.0
         self.psf_variance_map_bool = psf_variance_map is not None
         self._pixel_size = None
         self.point_source_supersampling_factor = point_source_supersampling_factor
@@ -532,6 +553,9 @@ def install_lenstronomy():
         return _onum.split_kernel(np.asarray(kernel_super, float), supersampling_kernel_size,
                                   supersampling_factor)
 
+    mod("lenstronomy.Util.image_util")
+    mod("lenstronomy.LensModel.Solver.epl_shear_solver", solve_lenseq_pemd=_Dummy())
+    mod("lenstronomy.LensModel.Solver")
     kernel_util = mod("lenstronomy.Util.kernel_util", cut_psf=_cut_psf,
                       split_kernel=_split_kernel)
     constants = mod("lenstronomy.Util.constants")

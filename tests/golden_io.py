@@ -90,6 +90,36 @@ def multi_plane_cases():
     return out
 
 
+def point_source_cases():
+    """ImageModel scenes with LENSED_POSITION + UNLENSED point sources: kwargs,
+    data, the reference's image, its point-source term of model 1 and logL
+    (exposure 800 s, background rms 0.01)."""
+    d, meta = load("point_sources.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        for k in ("image", "ps1", "data", "kernel"):
+            key = "%s_%d" % (k, i)
+            c[k] = d[key] if key in d.files else None
+        out.append(c)
+    return out
+
+
+def point_source_scene(c):
+    """Oracle scene dict of a point-source case (its extended-light part)."""
+    g = grid_kwargs(c["n"], c["dpix"])
+    num = c.get("numerics") or {}
+    kernel = None if c["kernel"] is None else c["kernel"] / c["kernel"].sum()
+    extra = {}
+    if num.get("supersampling_convolution"):
+        extra = {"supersampling_convolution": True,
+                 "supersampling_kernel_size": num.get("supersampling_kernel_size")}
+    return dict(nx=c["n"], ny=c["n"], supersampling_factor=c["s"], psf_type=c["psf"]["psf_type"],
+                kernel=kernel, lens_model_list=["EPL", "SHEAR"],
+                source_light_model_list=["SERSIC_ELLIPSE"], lens_light_model_list=["SERSIC"],
+                flux_scaling=c["flux_scaling"], **extra, **g)
+
+
 def linear_cases():
     """ImageLinearFit cases: kwargs, data, mask and the reference's amplitudes,
     model image, inverse normal matrix (source_marg) and logL."""

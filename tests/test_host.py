@@ -314,3 +314,25 @@ def test_flat_lcdm_distances():
     assert abs(t13 - (t12 + t23)) <= 1e-12 * t13
     d = bg.d_xy(np.array([0.1, 0.5]), np.array([1.0, 1.0]))
     assert d.shape == (2,) and abs(d[1] - bg.d_xy(0.5, 1.0)) == 0
+
+
+def test_point_source_rows_layout():
+    """PointSource.point_source_list order (models concatenated), the astrometric
+    shift of the first images (image_model.py:652-676) and batch broadcasting."""
+    g = W.grid_kwargs(20, 0.1)
+    data = J.ImageData(np.zeros((20, 20)), exposure_time=100.0, background_rms=0.01, **g)
+    psf = J.PSF("PIXEL", kernel_point_source=W.gaussian_pixel_kernel(0.1, 0.1, 5))
+    im = J.ImageModel(data, psf, J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+                      J.LightModel([]),
+                      point_source_class=J.PointSource(["LENSED_POSITION", "UNLENSED"],
+                                                       flux_from_point_source_list=[True, False]))
+    ps = [{"ra_image": [0.1, 0.2], "dec_image": [0.3, 0.4], "point_amp": [1.0, 2.0]},
+          {"ra_image": [0.5], "dec_image": [0.6], "point_amp": [3.0]}]
+    rows = im.point_source_rows(ps, {"delta_x_image": [0.01], "delta_y_image": [0.02]}, B=3)
+    assert rows.shape == (3, 3, 3)
+    np.testing.assert_allclose(rows[0, :, 0], [0.11, 0.2, 0.5])
+    np.testing.assert_allclose(rows[0, :, 1], [0.32, 0.4, 0.6])
+    np.testing.assert_allclose(rows[2, :, 2], [1.0, 2.0, 0.0])  # flux_from_point_source False
+    assert im.PointSource.num_basis(ps) == 2
+    with pytest.raises(ValueError):
+        im.point_source_rows([ps[0]])

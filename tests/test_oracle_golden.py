@@ -193,3 +193,46 @@ def test_linear_solve_matches_reference(case):
     assert abs(logl - case["logL"]) <= 1e-10 * abs(case["logL"])
     if case["cov"] is not None:
         np.testing.assert_allclose(cov, case["cov"], rtol=1e-9, atol=1e-14)
+
+
+def _ps_kernel(case):
+    """The kernel the reference renders with: the 3x3 delta when unconvolved or for
+    a NONE PSF, else the (supersampled) PIXEL kernel, normalised."""
+    if case["unconvolved"] or case["psf"]["psf_type"] == "NONE":
+        k = np.zeros((3, 3))
+        k[1, 1] = 1.0
+        return k
+    return case["kernel"] / case["kernel"].sum()
+
+
+def _ps_render(case, models):
+    from oracle import point_source as ops
+    from jaxtronomy_gb300.workloads import grid_kwargs
+    g = grid_kwargs(case["n"], case["dpix"])
+    ra = np.concatenate([np.asarray(case["ps"][m]["ra_image"], float) for m in models])
+    dec = np.concatenate([np.asarray(case["ps"][m]["dec_image"], float) for m in models])
+    amp = np.concatenate([np.asarray(case["ps"][m]["point_amp"], float) for m in models])
+    ra, dec = ops.displace_astrometry(ra, dec, case["special"])
+    p = (case.get("numerics") or {}).get("point_source_supersampling_factor", 1)
+    img = ops.render(case["n"], case["n"], g["transform_pix2angle"], g["ra_at_xy_0"],
+                     g["dec_at_xy_0"], ra, dec, amp, _ps_kernel(case), p)
+    return img * case["flux_scaling"]
+
+
+@pytest.mark.parametrize("case", golden_io.point_source_cases(), ids=lambda c: c["tag"])
+def test_point_source_images_match_reference(case):
+    """Oracle extended image + rendered point sources (LENSED_POSITION + UNLENSED,
+    astrometric shifts, flux scaling, unconvolved, NONE PSF, supersampled
+    rendering) against the reference's ImageModel, its point-source term of model
+    1 and its likelihood."""
+    sc = golden_io.point_source_scene(case)
+    ext = image.image(sc, case["lens"], case["src"], case["ll"], unconvolved=case["unconvolved"])
+    model = ext + _ps_render(case, [0, 1])
+    tol = 1e-10 * np.abs(case["image"]).max()
+    np.testing.assert_allclose(model, case["image"], rtol=1e-10, atol=tol)
+    if case["unconvolved"]:
+        return
+    np.testing.assert_allclose(_ps_render(case, [1]), case["ps1"], rtol=1e-10, atol=tol)
+    logl = image.log_likelihood(model, case["data"], np.ones_like(model), 0.01,
+                                exposure_time=800.0)
+    assert abs(logl - case["logL"]) <= 1e-10 * abs(case["logL"])

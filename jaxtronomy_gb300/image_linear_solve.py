@@ -7,8 +7,9 @@ of each linear component is one ``lensgb_image`` launch of that component alone
 ``lensgb_linear_solve`` launch then forms and solves the weighted least-squares
 system of every system (``de_lens.get_param_WLS``, ``de_lens.py:8-38``), writes
 the model images and their log-likelihoods (``likelihood_data_given_model``,
-``:229-341``).  Point sources are not supported (the reference's point-source
-response rows are therefore absent).
+``:229-341``).  Point images (LENSED_POSITION / UNLENSED models whose flux comes
+from the point source) add one response row each: the image rendered alone at
+amp = 1 (``:440-456``), so their ``point_amp`` are solved too.
 """
 
 import ctypes
@@ -31,24 +32,53 @@ class ImageLinearFit(ImageModel):
                          lens_light_model_class, point_source_class, extinction_class,
                          kwargs_numerics, likelihood_mask, psf_error_map_bool_list,
                          kwargs_pixelbased)
-        if self._n_ps:
-            raise ValueError("the linear solve with point-source amplitudes is not supported")
         self._n_src = len(self.SourceModel.profile_type_list)
         self._n_ll = len(self.LensLightModel.profile_type_list)
         if self._n_src + self._n_ll > _lib.LINEAR_MAX:
             raise ValueError("at most %d linear light components are supported"
                              % _lib.LINEAR_MAX)
 
+    def _ps_linear(self, kwargs_ps, kwargs_special=None):
+        """Positions of the point images with linear amplitudes (flux from the point
+        source), shifted as ``point_source_linear_response_set`` does
+        (``image_linear_solve.py:559-600``): lists of (ra, dec) arrays of shape
+        (B or 1,) per image."""
+        if not self._n_ps:
+            return []
+        ra, dec = self.PointSource.image_position(kwargs_ps)
+        out = []
+        for k, (r, d) in enumerate(zip(ra, dec)):
+            if not self.PointSource._flux_from_point_source_list[k]:
+                continue
+            r = np.atleast_2d(r)
+            d = np.atleast_2d(d)
+            for j in range(r.shape[-1]):
+                out.append([r[:, j].copy(), d[:, j].copy()])
+        if kwargs_special is not None and "delta_x_image" in kwargs_special:
+            dx = np.asarray(kwargs_special["delta_x_image"], dtype=float)
+            dy = np.asarray(kwargs_special["delta_y_image"], dtype=float)
+            for q in range(min(len(out), dx.shape[-1])):
+                out[q][0] = out[q][0] + dx[..., q]
+                out[q][1] = out[q][1] + dy[..., q]
+        return out
+
     # ------------------------------------------------------------------ linear parameters
     def num_param_linear(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                          kwargs_ps=None):
-        """``image_linear_solve.py:342-360``: one amplitude per light profile."""
-        return self._n_src + self._n_ll
+        """``image_linear_solve.py:342-360``: one amplitude per light profile and per
+        point image with flux from the point source."""
+        n_ps = self.PointSource.num_basis(kwargs_ps) if self._n_ps and kwargs_ps else 0
+        return self._n_src + self._n_ll + n_ps
 
     def linear_param_from_kwargs(self, kwargs_source, kwargs_lens_light, kwargs_ps=None):
-        """``image_linear_solve.py:484-528``: the amplitudes, sources first."""
-        return [kw["amp"] for kw in (kwargs_source or [])] + [
+        """``image_linear_solve.py:484-528``: the amplitudes, sources, lens light, then
+        the point images' ``point_amp``."""
+        out = [kw["amp"] for kw in (kwargs_source or [])] + [
             kw["amp"] for kw in (kwargs_lens_light or [])]
+        for k, kw in enumerate(kwargs_ps or []):
+            if self.PointSource._flux_from_point_source_list[k]:
+                out += list(np.atleast_1d(kw["point_amp"]))
+        return out
 
     def update_linear_kwargs(self, param, kwargs_lens, kwargs_source, kwargs_lens_light,
                              kwargs_ps=None):
@@ -59,19 +89,34 @@ class ImageLinearFit(ImageModel):
             kw["amp"] = p[..., i]
         for i, kw in enumerate(kwargs_lens_light or []):
             kw["amp"] = p[..., self._n_src + i]
+        c = self._n_src + self._n_ll
+        for k, kw in enumerate(kwargs_ps or []):
+            if self.PointSource._flux_from_point_source_list[k]:
+                n = np.shape(kw["ra_image"])[-1]
+                kw["point_amp"] = p[..., c:c + n]
+                c += n
         return kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps
 
     def check_positive_flux(self, kwargs_source, kwargs_lens_light, kwargs_ps=None):
         """``image_linear_solve.py:598-618``: True when no amplitude is negative."""
         amps = np.asarray(self.linear_param_from_kwargs(kwargs_source, kwargs_lens_light),
                           dtype=float)
-        return bool(np.all(amps >= 0))
+        ok = bool(np.all(amps >= 0))
+        if self._n_ps and kwargs_ps:
+            ok = ok and self.PointSource.check_positive_flux(kwargs_ps)
+        return ok
 
     # ------------------------------------------------------------------ response
     def linear_response_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
-                              unconvolved=False, psf_kernels=None, stream=None):
+                              unconvolved=False, psf_kernels=None, stream=None, kwargs_ps=None,
+                              kwargs_special=None):
         """(n_linear, B, ny, nx) CUDA tensor of unit-amplitude component images:
-        each source lensed alone, each lens-light profile alone, amp = 1."""
+        each source lensed alone, each lens-light profile alone, amp = 1, then each
+        point image alone at amp = 1 without the flux scaling (image_linear_solve.py:
+        440-456)."""
+        ps_pos = self._ps_linear(kwargs_ps, kwargs_special)
+        if self._n_src + self._n_ll + len(ps_pos) > _lib.LINEAR_MAX:
+            raise ValueError("at most %d linear amplitudes are supported" % _lib.LINEAR_MAX)
         n_lens = len(self.LensModel.lens_model_list)
         unit = lambda kws: [dict(kw, amp=1.0) for kw in (kws or [])]  # noqa: E731
         ks, kll = unit(kwargs_source), unit(kwargs_lens_light)
@@ -83,12 +128,21 @@ class ImageLinearFit(ImageModel):
                 for (li, si, lli), lensed in jobs]
         # the batch of the whole kwargs (a lens-light row alone does not see batched lens
         # kwargs): rows of one system are repeated
-        B = max(r.shape[0] for r in rows)
-        A = torch.empty((len(jobs), B, self._nx, self._ny), dtype=self._dtype, device="cuda")
+        B = max([r.shape[0] for r in rows] + [p[0].shape[0] for p in ps_pos] + [1])
+        A = torch.empty((len(jobs) + len(ps_pos), B, self._nx, self._ny), dtype=self._dtype,
+                        device="cuda")
         for c, ((li, si, lli), lensed) in enumerate(jobs):
             r = rows[c] if rows[c].shape[0] == B else np.repeat(rows[c], B, axis=0)
             model = self._model(li, si, lli, lensed=lensed)
             self._launch(model, _device.to_device_f64(r), B, flags, psf_kernels, A[c], stream)
+        # the renderer applies the model's flux scaling; the response rows have none
+        unit = 1.0 / self._flux_scaling
+        for j, (ra, dec) in enumerate(ps_pos):
+            row = A[len(jobs) + j]
+            row.zero_()
+            pts = np.stack([np.broadcast_to(ra, (B,)), np.broadcast_to(dec, (B,)),
+                            np.full(B, unit)], axis=-1)[:, None, :]
+            self._render_point_rows(row, np.ascontiguousarray(pts), False, psf_kernels, stream)
         return A
 
     def linear_response_matrix(self, kwargs_lens, kwargs_source, kwargs_lens_light,
@@ -99,19 +153,22 @@ class ImageLinearFit(ImageModel):
         if kwargs_extinction:
             raise ValueError("Extinction is not implemented")
         A = self.linear_response_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
-                                       unconvolved=unconvolved)
+                                       unconvolved=unconvolved, kwargs_ps=kwargs_ps,
+                                       kwargs_special=kwargs_special)
         a = A[:, 0].to(torch.float64).cpu().numpy()
         return np.nan_to_num(a[:, self.likelihood_mask])
 
     # ------------------------------------------------------------------ solve
     def likelihood_linear_batch(self, kwargs_lens=None, kwargs_source=None,
                                 kwargs_lens_light=None, data=None, source_marg=False,
-                                check_positive_flux=False, psf_kernels=None, stream=None):
+                                check_positive_flux=False, psf_kernels=None, stream=None,
+                                kwargs_ps=None, kwargs_special=None):
         """Linear solve of B systems: ((B,) logL, (B, n) amplitudes, (B, ny, nx) model
         images, (B, n, n) inverse normal matrices or None) as CUDA tensors (FP64;
         images in the model precision)."""
         A = self.linear_response_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
-                                       psf_kernels=psf_kernels, stream=stream)
+                                       psf_kernels=psf_kernels, stream=stream,
+                                       kwargs_ps=kwargs_ps, kwargs_special=kwargs_special)
         n, B = A.shape[0], A.shape[1]
         nt = self._noise_tensors(data)
         nd = self._noise_desc(nt)
@@ -138,7 +195,8 @@ class ImageLinearFit(ImageModel):
         if kwargs_extinction:
             raise ValueError("Extinction is not implemented")
         logl, param, image, cov = self.likelihood_linear_batch(
-            kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=inv_bool)
+            kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=inv_bool,
+            kwargs_ps=kwargs_ps, kwargs_special=kwargs_special)
         p = param[0].cpu().numpy()
         self.update_linear_kwargs(p, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps)
         return (image[0].to(torch.float64).cpu().numpy(), 0,
@@ -157,7 +215,8 @@ class ImageLinearFit(ImageModel):
                              "source_marg with flat priors")
         logl, param, _, _ = self.likelihood_linear_batch(
             kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=source_marg,
-            check_positive_flux=check_positive_flux)
+            check_positive_flux=check_positive_flux, kwargs_ps=kwargs_ps,
+            kwargs_special=kwargs_special)
         p = param[0].cpu().numpy()
         self.update_linear_kwargs(p, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps)
         return float(logl[0].cpu()), p

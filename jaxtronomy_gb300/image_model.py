@@ -454,7 +454,11 @@ class ImageModel:
             raise ValueError("kwargs_ps is needed for the point-source models %s"
                              % self.PointSource.point_source_type_list)
         rows = self.point_source_rows(kwargs_ps, kwargs_special, B, k=k)
-        n = rows.shape[1]
+        return self._render_point_rows(out, rows, unconvolved, psf_kernels, stream)
+
+    def _render_point_rows(self, out, rows, unconvolved=False, psf_kernels=None, stream=None):
+        """Adds the (B, n_images, 3) point rows (ra, dec, amp) to ``out``."""
+        B, n = rows.shape[0], rows.shape[1]
         if n == 0:
             return out
         ps = _device.to_device_f64(rows)

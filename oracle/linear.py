@@ -19,9 +19,13 @@ from . import image as oimage
 EPSILON = sys.float_info.epsilon
 
 
-def response(scene, kwargs_lens, kwargs_source, kwargs_lens_light):
+def response(scene, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps=None,
+             kwargs_special=None):
     """(n_linear, ny, nx): each source lensed alone and each lens-light profile
-    alone, amp = 1 (flux scaling included, as ``linear_response_matrix`` applies it)."""
+    alone, amp = 1 (flux scaling included, as ``linear_response_matrix`` applies it),
+    then each point image alone at amp = 1 (``image_linear_solve.py:440-456``, no flux
+    scaling; positions shifted as ``point_source_linear_response_set`` does,
+    ``:559-600``), rendered with ``scene["ps_kernel"]`` at ``scene["ps_subgrid"]``."""
     src = scene.get("source_light_model_list", [])
     ll = scene.get("lens_light_model_list", [])
     dsl = scene.get("deflection_scaling_list")
@@ -34,6 +38,17 @@ def response(scene, kwargs_lens, kwargs_source, kwargs_lens_light):
         sc = dict(scene, source_light_model_list=[], lens_light_model_list=[name],
                   deflection_scaling_list=None)
         out.append(oimage.image(sc, kwargs_lens, [], [dict(kwargs_lens_light[j], amp=1.0)]))
+    if kwargs_ps:
+        from . import point_source as ops
+        ra = np.concatenate([np.atleast_1d(np.asarray(p["ra_image"], float)) for p in kwargs_ps])
+        dec = np.concatenate([np.atleast_1d(np.asarray(p["dec_image"], float))
+                              for p in kwargs_ps])
+        ra, dec = ops.displace_astrometry(ra, dec, kwargs_special)
+        for j in range(len(ra)):
+            out.append(ops.render(scene["nx"], scene["ny"], scene["transform_pix2angle"],
+                                  scene["ra_at_xy_0"], scene["dec_at_xy_0"], ra[j:j + 1],
+                                  dec[j:j + 1], [1.0], scene["ps_kernel"],
+                                  scene.get("ps_subgrid", 1)))
     return np.nan_to_num(np.array(out))
 
 
@@ -63,11 +78,11 @@ def marginalisation_const(M_inv):
 
 def likelihood(scene, kwargs_lens, kwargs_source, kwargs_lens_light, data, mask,
                background_rms, exposure_time=None, noise_map=None, source_marg=False,
-               check_positive_flux=False):
+               check_positive_flux=False, kwargs_ps=None):
     """(logL, amplitudes, model image, M^-1 or None) of ``likelihood_data_given_model``
     with the linear solve (``image_linear_solve.py:229-341``)."""
     mask = np.asarray(mask, dtype=bool)
-    A = response(scene, kwargs_lens, kwargs_source, kwargs_lens_light)[:, mask]
+    A = response(scene, kwargs_lens, kwargs_source, kwargs_lens_light, kwargs_ps)[:, mask]
     if noise_map is not None:
         c_d = np.asarray(noise_map, float) ** 2
     else:

@@ -546,6 +546,14 @@ def gen_linear():
              kl=sie, src=["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], ks=[src, dict(src)],
              ll=["SERSIC"], kll=[ll_s], psf={"psf_type": "NONE"}, mask=False, marg=True,
              pos=False, sign=1.0),
+        dict(tag="sie_point_sources_marg", n=40, dpix=0.08, s=2, lens=["SIE", "SHEAR"], kl=sie,
+             src=["SERSIC_ELLIPSE"], ks=[src], ll=["SERSIC"], kll=[ll_s],
+             psf={"psf_type": "PIXEL", "kernel_point_source": W.gaussian_pixel_kernel(0.12, 0.08, 11)},
+             mask=False, marg=True, pos=True, sign=1.0,
+             ps_types=["LENSED_POSITION", "UNLENSED"],
+             ps=[{"ra_image": [1.05, -0.62, 0.35, -0.2], "dec_image": [0.2, 0.8, -0.95, -0.1],
+                  "point_amp": [3.0, 2.5, 1.5, 0.8]},
+                 {"ra_image": [0.9], "dec_image": [-1.2], "point_amp": [2.0]}]),
     ]
     for c in cases:
         g = W.grid_kwargs(c["n"], c["dpix"])
@@ -555,6 +563,11 @@ def gen_linear():
         ks_sim = copy.deepcopy(c["ks"])
         ks_sim[0]["amp"] = ks_sim[0]["amp"] * c["sign"]
         img = np.asarray(sim.image(c["kl"], ks_sim, c["kll"]))
+        if c.get("ps"):
+            from jaxtronomy.PointSource.point_source import PointSource
+            img = img + np.asarray(sim.ImageNumerics.point_source_rendering(
+                *[np.concatenate([np.asarray(p[k], float) for p in c["ps"]])
+                  for k in ("ra_image", "dec_image", "point_amp")]))
         data = img + rng.normal(0, 0.02, img.shape)
         mask = np.ones((c["n"], c["n"]))
         if c["mask"]:
@@ -562,18 +575,28 @@ def gen_linear():
             mask = (((xx - c["n"] / 2) ** 2 + (yy - c["n"] / 2) ** 2) < (0.42 * c["n"]) ** 2
                     ).astype(float)
         data_class = ImageData(image_data=data, exposure_time=500.0, background_rms=0.02, **g)
+        pcls = None
+        if c.get("ps"):
+            from jaxtronomy.PointSource.point_source import PointSource
+            pcls = PointSource(c["ps_types"])
         im = ImageLinearFit(data_class, refshim.PSF(**c["psf"]), LensModel(c["lens"]),
                             LightModel(c["src"], deflection_scaling_list=c.get("dsl")),
-                            LightModel(c["ll"]), kwargs_numerics={"supersampling_factor": c["s"]},
+                            LightModel(c["ll"]), point_source_class=pcls,
+                            kwargs_numerics={"supersampling_factor": c["s"]},
                             likelihood_mask=mask)
         kl, ks, kll = copy.deepcopy(c["kl"]), copy.deepcopy(c["ks"]), copy.deepcopy(c["kll"])
-        model, _, cov, param = im.image_linear_solve(kl, ks, kll, kwargs_ps=[], inv_bool=c["marg"])
+        kps = copy.deepcopy(c.get("ps", []))
+        model, _, cov, param = im.image_linear_solve(kl, ks, kll, kwargs_ps=kps,
+                                                     inv_bool=c["marg"])
         kl, ks, kll = copy.deepcopy(c["kl"]), copy.deepcopy(c["ks"]), copy.deepcopy(c["kll"])
-        logl, _ = im.likelihood_data_given_model(kl, ks, kll, kwargs_ps=[], source_marg=c["marg"],
+        kps = copy.deepcopy(c.get("ps", []))
+        logl, _ = im.likelihood_data_given_model(kl, ks, kll, kwargs_ps=kps,
+                                                 source_marg=c["marg"],
                                                  check_positive_flux=c["pos"])
         rec = {k: c[k] for k in ("tag", "n", "dpix", "s", "lens", "kl", "src", "ks", "ll", "kll",
                                  "marg", "pos")}
         rec["dsl"] = c.get("dsl")
+        rec["ps_types"], rec["ps"] = c.get("ps_types", []), c.get("ps", [])
         rec["psf"] = {k: v for k, v in c["psf"].items() if k != "kernel_point_source"}
         rec["logL"] = float(logl)
         rec["bkg"], rec["exp_time"] = 0.02, 500.0

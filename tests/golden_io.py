@@ -142,6 +142,7 @@ def linear_scene(c):
               lens_light_model_list=c["ll"], deflection_scaling_list=c["dsl"], **g)
     if c["psf"]["psf_type"] == "PIXEL":
         sc["kernel"] = c["kernel"]
+        sc["ps_kernel"] = c["kernel"] / c["kernel"].sum()
     elif c["psf"]["psf_type"] == "GAUSSIAN":
         sc["fwhm"] = c["psf"]["fwhm"]
         sc["truncation"] = c["psf"]["truncation"]

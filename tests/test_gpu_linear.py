@@ -27,9 +27,10 @@ def _fit(c, precision="fp64"):
         psf = J.PSF("GAUSSIAN", fwhm=p["fwhm"], truncation=p["truncation"])
     else:
         psf = J.PSF("NONE")
+    pcls = J.PointSource(c["ps_types"]) if c.get("ps_types") else None
     return ImageLinearFit(data, psf, J.LensModel(c["lens"]),
                           J.LightModel(c["src"], deflection_scaling_list=c["dsl"]),
-                          J.LightModel(c["ll"]),
+                          J.LightModel(c["ll"]), point_source_class=pcls,
                           kwargs_numerics={"supersampling_factor": c["s"], "precision": precision},
                           likelihood_mask=c["mask"])
 
@@ -37,22 +38,27 @@ def _fit(c, precision="fp64"):
 @pytest.mark.parametrize("case", golden_io.linear_cases(), ids=lambda c: c["tag"])
 def test_linear_fit_matches_reference(cuda, case):
     im = _fit(case)
-    kl, ks, kll = (copy.deepcopy(case[k]) for k in ("kl", "ks", "kll"))
-    logl, param = im.likelihood_data_given_model(kl, ks, kll, source_marg=case["marg"],
+    kl, ks, kll, kps = (copy.deepcopy(case.get(k) or []) for k in ("kl", "ks", "kll", "ps"))
+    logl, param = im.likelihood_data_given_model(kl, ks, kll, kps, source_marg=case["marg"],
                                                  check_positive_flux=case["pos"])
     assert abs(logl - case["logL"]) <= 1e-10 * abs(case["logL"]), (logl, case["logL"])
     np.testing.assert_allclose(param, case["param"], rtol=1e-10, atol=1e-12)
     # the amplitudes are written into the kwargs, as the reference does
     assert ks[0]["amp"] == param[0]
-    kl, ks, kll = (copy.deepcopy(case[k]) for k in ("kl", "ks", "kll"))
-    model, err, cov, p2 = im.image_linear_solve(kl, ks, kll, inv_bool=case["marg"])
+    if kps:
+        # point_amp written back too, sources and lens light first
+        n_ext = len(case["src"]) + len(case["ll"])
+        np.testing.assert_array_equal(kps[0]["point_amp"], param[n_ext:n_ext + 4])
+    kl, ks, kll, kps = (copy.deepcopy(case.get(k) or []) for k in ("kl", "ks", "kll", "ps"))
+    model, err, cov, p2 = im.image_linear_solve(kl, ks, kll, kps, inv_bool=case["marg"])
     np.testing.assert_array_equal(p2, param)
     np.testing.assert_allclose(model, case["model"], rtol=1e-10,
                                atol=1e-12 * np.abs(case["model"]).max())
     if case["cov"] is not None:
         np.testing.assert_allclose(cov, case["cov"], rtol=1e-9, atol=1e-14)
-    A = im.linear_response_matrix(kl, ks, kll)
-    assert A.shape == (len(case["src"]) + len(case["ll"]), int(np.sum(case["mask"])))
+    A = im.linear_response_matrix(kl, ks, kll, kps)
+    n_ps = sum(len(p["ra_image"]) for p in (case.get("ps") or []))
+    assert A.shape == (len(case["src"]) + len(case["ll"]) + n_ps, int(np.sum(case["mask"])))
 
 
 def test_batched_solve_equals_single_and_fp32(cuda):

@@ -187,7 +187,8 @@ def test_linear_solve_matches_reference(case):
     sc = golden_io.linear_scene(case)
     logl, param, model, cov = linear.likelihood(
         sc, case["kl"], case["ks"], case["kll"], case["data"], case["mask"], case["bkg"],
-        exposure_time=case["exp_time"], source_marg=case["marg"], check_positive_flux=case["pos"])
+        exposure_time=case["exp_time"], source_marg=case["marg"], check_positive_flux=case["pos"],
+        kwargs_ps=case.get("ps"))
     np.testing.assert_allclose(param, case["param"], rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(model, case["model"], rtol=1e-10, atol=1e-12 * np.abs(model).max())
     assert abs(logl - case["logL"]) <= 1e-10 * abs(case["logL"])

@@ -27,6 +27,7 @@ from .image_linear_solve import ImageLinearFit
 from .image_model import ImageModel
 from .lens_model import LensModel
 from .light_model import LightModel
+from .point_source import PointSource
 from . import profiles
 
 _PI = np.pi
@@ -61,15 +62,20 @@ _LISTS = (("lens", "lens_model_list", profiles.LENS_PARAMS),
           ("source", "source_light_model_list", profiles.LIGHT_PARAMS),
           ("lens_light", "lens_light_model_list", profiles.LIGHT_PARAMS))
 
-_UNSUPPORTED_MODEL_KEYS = ("point_source_model_list", "optical_depth_model_list",
-                           "tracer_source_model_list")
+_UNSUPPORTED_MODEL_KEYS = ("optical_depth_model_list", "tracer_source_model_list")
+
+# parameters of the point-source types (PointSource/Types/{lensed_position,unlensed}.py),
+# each an array of num_point_source_list[i] values
+_PS_PARAMS = ["ra_image", "dec_image", "point_amp"]
 
 
 def _model_lists(kwargs_model):
     for key in _UNSUPPORTED_MODEL_KEYS:
         if kwargs_model.get(key):
             raise ValueError("%s is not supported by this build" % key)
-    return {tag: list(kwargs_model.get(key, [])) for tag, key, _ in _LISTS}
+    out = {tag: list(kwargs_model.get(key, [])) for tag, key, _ in _LISTS}
+    out["ps"] = list(kwargs_model.get("point_source_model_list", []))
+    return out
 
 
 class Param:
@@ -81,7 +87,11 @@ class Param:
     the profiles' ``lower_limit_default`` / ``upper_limit_default``; entries of
     ``kwargs_lower_*`` / ``kwargs_upper_*`` replace them.  With ``linear_solver``
     (the default, as in lenstronomy) every light profile's ``amp`` is left to the
-    linear solve: it is not sampled and reads 1 unless fixed otherwise."""
+    linear solve: it is not sampled and reads 1 unless fixed otherwise.  Point
+    sources (``point_source_model_list`` with ``num_point_source_list``) follow:
+    ``ra_image``, ``dec_image`` and, without the linear solver, ``point_amp``, one
+    argument per image; their bounds come from ``kwargs_lower_ps`` /
+    ``kwargs_upper_ps``, which a sampled point-source parameter needs."""
 
     def __init__(self, kwargs_model, kwargs_fixed_lens=None, kwargs_fixed_source=None,
                  kwargs_fixed_lens_light=None, kwargs_fixed_ps=None, kwargs_fixed_special=None,
@@ -90,17 +100,15 @@ class Param:
                  kwargs_lower_extinction=None, kwargs_upper_lens=None, kwargs_upper_source=None,
                  kwargs_upper_lens_light=None, kwargs_upper_ps=None, kwargs_upper_special=None,
                  kwargs_upper_extinction=None, linear_solver=True, **constraints):
-        for name, v in (("kwargs_fixed_ps", kwargs_fixed_ps),
-                        ("kwargs_fixed_special", kwargs_fixed_special),
+        for name, v in (("kwargs_fixed_special", kwargs_fixed_special),
                         ("kwargs_fixed_extinction", kwargs_fixed_extinction),
-                        ("kwargs_lower_ps", kwargs_lower_ps),
                         ("kwargs_lower_special", kwargs_lower_special),
                         ("kwargs_lower_extinction", kwargs_lower_extinction),
-                        ("kwargs_upper_ps", kwargs_upper_ps),
                         ("kwargs_upper_special", kwargs_upper_special),
                         ("kwargs_upper_extinction", kwargs_upper_extinction)):
             if v:
                 raise ValueError("%s is not supported by this build" % name)
+        num_point_source_list = constraints.pop("num_point_source_list", None)
         for name, v in constraints.items():
             if v:
                 raise ValueError("parameter constraint %s is not supported by this build" % name)
@@ -134,15 +142,47 @@ class Param:
                 for p in table[name]:
                     if p in fx[i]:
                         continue
-                    self._slots.append((tag, i, p))
+                    self._slots.append((tag, i, p, None))
                     lo.append(float(lw[i].get(p, LIMITS[name][p][0])))
                     hi.append(float(up[i].get(p, LIMITS[name][p][1])))
+        # point sources: ra_image, dec_image, point_amp arrays of num_point_source_list[i]
+        # values; point_amp is left to the linear solve; sampled arrays need their bounds
+        ps = self._lists["ps"]
+        npl = (list(num_point_source_list) if num_point_source_list is not None
+               else [1] * len(ps))
+        if len(npl) != len(ps):
+            raise ValueError("num_point_source_list needs one entry per point-source model")
+        fx = list(kwargs_fixed_ps) if kwargs_fixed_ps is not None else [{} for _ in ps]
+        lw = list(kwargs_lower_ps) if kwargs_lower_ps is not None else [{} for _ in ps]
+        up = list(kwargs_upper_ps) if kwargs_upper_ps is not None else [{} for _ in ps]
+        for what, lst in (("fixed", fx), ("lower", lw), ("upper", up)):
+            if len(lst) != len(ps):
+                raise ValueError("kwargs_%s_ps needs one dict per point-source model" % what)
+        self._fixed["ps"] = [dict(d) for d in fx]
+        self._num_point_source_list = npl
+        for i, name in enumerate(ps):
+            if name not in ("LENSED_POSITION", "UNLENSED"):
+                raise ValueError("point-source model %s is not supported" % name)
+            if self.linear_solver:
+                self._fixed["ps"][i].setdefault("point_amp", np.ones(npl[i]))
+            for p in _PS_PARAMS:
+                if p in self._fixed["ps"][i]:
+                    continue
+                if p not in lw[i] or p not in up[i]:
+                    raise ValueError("sampled point-source parameter %s needs kwargs_lower_ps "
+                                     "and kwargs_upper_ps entries" % p)
+                lo_p = np.broadcast_to(np.asarray(lw[i][p], dtype=float), (npl[i],))
+                hi_p = np.broadcast_to(np.asarray(up[i][p], dtype=float), (npl[i],))
+                for j in range(npl[i]):
+                    self._slots.append(("ps", i, p, j))
+                    lo.append(float(lo_p[j]))
+                    hi.append(float(hi_p[j]))
         self._lower = np.array(lo)
         self._upper = np.array(hi)
 
     def num_param(self):
         """(number of sampled arguments, their names as ``param_name_list-tag-index``)."""
-        names = ["%s_%s%d" % (p, tag, i) for tag, i, p in self._slots]
+        names = [p if tag == "ps" else "%s_%s%d" % (p, tag, i) for tag, i, p, _ in self._slots]
         return len(self._slots), names
 
     def num_param_linear(self):
@@ -154,8 +194,10 @@ class Param:
     def kwargs2args(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                     kwargs_ps=None, kwargs_special=None, kwargs_extinction=None,
                     kwargs_tracer_source=None):
-        kw = {"lens": kwargs_lens, "source": kwargs_source, "lens_light": kwargs_lens_light}
-        return np.array([float(kw[tag][i][p]) for tag, i, p in self._slots])
+        kw = {"lens": kwargs_lens, "source": kwargs_source, "lens_light": kwargs_lens_light,
+              "ps": kwargs_ps}
+        return np.array([float(kw[tag][i][p] if j is None else np.asarray(kw[tag][i][p])[j])
+                         for tag, i, p, j in self._slots])
 
     def args2kwargs(self, args, bijective=False):
         """kwargs of one vector (d,) or, for an ensemble (n, d), kwargs whose
@@ -164,11 +206,18 @@ class Param:
         a = np.asarray(args, dtype=float)
         if a.shape[-1] != len(self._slots):
             raise ValueError("expected %d arguments, got %d" % (len(self._slots), a.shape[-1]))
-        out = {tag: [dict(d) for d in self._fixed[tag]] for tag, _, _ in _LISTS}
-        for k, (tag, i, p) in enumerate(self._slots):
-            out[tag][i][p] = a[..., k]
+        out = {tag: [dict(d) for d in self._fixed[tag]] for tag in ("lens", "source",
+                                                                     "lens_light", "ps")}
+        arrays = {}
+        for k, (tag, i, p, j) in enumerate(self._slots):
+            if j is None:
+                out[tag][i][p] = a[..., k]
+            else:
+                arrays.setdefault((i, p), []).append(a[..., k])
+        for (i, p), cols in arrays.items():
+            out["ps"][i][p] = np.stack(cols, axis=-1)
         return {"kwargs_lens": out["lens"], "kwargs_source": out["source"],
-                "kwargs_lens_light": out["lens_light"], "kwargs_ps": [],
+                "kwargs_lens_light": out["lens_light"], "kwargs_ps": out["ps"],
                 "kwargs_special": {}, "kwargs_extinction": [], "kwargs_tracer_source": []}
 
 
@@ -201,9 +250,11 @@ class ImageLikelihood:
         kn.setdefault("precision", precision)
         mask = None if image_likelihood_mask_list is None else image_likelihood_mask_list[0]
         cls = ImageLinearFit if self._linear else ImageModel
-        self.imSim = cls(data, psf, LensModel(lists["lens"]), LightModel(lists["source"]),
-                         LightModel(lists["lens_light"]), kwargs_numerics=kn,
-                         likelihood_mask=mask)
+        lens_model = LensModel(lists["lens"])
+        self.imSim = cls(data, psf, lens_model, LightModel(lists["source"]),
+                         LightModel(lists["lens_light"]),
+                         point_source_class=PointSource(lists["ps"], lens_model=lens_model),
+                         kwargs_numerics=kn, likelihood_mask=mask)
         self._model_type = self.imSim.type
 
     @property
@@ -211,16 +262,18 @@ class ImageLikelihood:
         return self.imSim.num_data_evaluate
 
     def logL_batch(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
-                   stream=None, **kwargs):
+                   stream=None, kwargs_ps=None, kwargs_special=None, **kwargs):
         """(B,) FP64 log-likelihoods of batched kwargs, NaN replaced by -1e15
         (``image_likelihood.py:95``)."""
         if self._linear:
             logl, _, _, _ = self.imSim.likelihood_linear_batch(
                 kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=self._source_marg,
-                check_positive_flux=self._check_positive_flux, stream=stream)
+                check_positive_flux=self._check_positive_flux, stream=stream,
+                kwargs_ps=kwargs_ps, kwargs_special=kwargs_special)
         else:
             logl = self.imSim.likelihood_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
-                                               stream=stream)
+                                               stream=stream, kwargs_ps=kwargs_ps,
+                                               kwargs_special=kwargs_special)
         return torch.nan_to_num(logl, nan=-(10.0 ** 15))
 
     def logL(self, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None, kwargs_ps=None,
@@ -229,10 +282,13 @@ class ImageLikelihood:
         if kwargs_extinction:
             raise ValueError("Extinction is not implemented")
         if not self._linear:
-            return float(self.logL_batch(kwargs_lens, kwargs_source, kwargs_lens_light)[0]), None
+            return float(self.logL_batch(kwargs_lens, kwargs_source, kwargs_lens_light,
+                                         kwargs_ps=kwargs_ps,
+                                         kwargs_special=kwargs_special)[0]), None
         logl, param, _, _ = self.imSim.likelihood_linear_batch(
             kwargs_lens, kwargs_source, kwargs_lens_light, source_marg=self._source_marg,
-            check_positive_flux=self._check_positive_flux)
+            check_positive_flux=self._check_positive_flux, kwargs_ps=kwargs_ps,
+            kwargs_special=kwargs_special)
         return float(torch.nan_to_num(logl, nan=-(10.0 ** 15))[0]), param[0].cpu().numpy()
 
 
@@ -276,7 +332,7 @@ class LikelihoodModule:
             raise ValueError("tracer, flux_ratio, and kinematic_2d likelihoods are not currently "
                              "supported and should be set to False.")
         if astrometric_likelihood or image_position_likelihood or source_position_likelihood:
-            raise ValueError("point-source position likelihoods need point sources, which are "
+            raise ValueError("astrometric, image-position and source-position likelihoods are "
                              "not supported by this build")
         for name, v in (("prior_ps", prior_ps), ("prior_special", prior_special),
                         ("prior_extinction", prior_extinction)):
@@ -334,7 +390,8 @@ class LikelihoodModule:
             logl = logl + _prior_terms(prior, kw[key])
         if self._image_likelihood:
             img = self.image_likelihood.logL_batch(kw["kwargs_lens"], kw["kwargs_source"],
-                                                   kw["kwargs_lens_light"], stream=stream)
+                                                   kw["kwargs_lens_light"], stream=stream,
+                                                   kwargs_ps=kw["kwargs_ps"] or None)
             logl = logl + img.cpu().numpy()
         logl = np.nan_to_num(logl, nan=1e-18)
         if self._check_bounds:

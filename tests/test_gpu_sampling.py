@@ -144,3 +144,43 @@ def _truth_kwargs():
                                            supersampling=SS, kernel_size=K)
     kl = W.instance(lens, 0)
     return kl, W.instance(src, 0), W.instance(ll, 0)
+
+
+@pytest.mark.parametrize("linear", [False, True])
+def test_point_source_ensemble_equals_per_vector(cuda, linear):
+    """point_source_model_list in the sampler path: sampled image positions (and,
+    without the linear solver, amplitudes) of a LENSED_POSITION model; the
+    ensemble's logL equals each vector's ImageModel / ImageLinearFit likelihood."""
+    from jaxtronomy_gb300.image_linear_solve import ImageLinearFit
+    joint, _, _, _, data, kern, g = _setup()
+    model = dict(MODEL, point_source_model_list=["LENSED_POSITION"])
+    ra0, dec0 = np.array([1.0, -0.6, 0.3]), np.array([0.2, 0.8, -0.9])
+    lo = {"ra_image": ra0 - 0.1, "dec_image": dec0 - 0.1, "point_amp": np.zeros(3)}
+    hi = {"ra_image": ra0 + 0.1, "dec_image": dec0 + 0.1, "point_amp": np.full(3, 10.0)}
+    param = S.Param(model, kwargs_fixed_lens=[{}, {"ra_0": 0.0, "dec_0": 0.0}],
+                    kwargs_lower_ps=[lo], kwargs_upper_ps=[hi], num_point_source_list=[3],
+                    linear_solver=linear)
+    lo_all, hi_all = param.param_limits()
+    rng = np.random.default_rng(9)
+    model0, lens, src, ll, _ = W.gradient_batch(seed=5, batch=1, num_pix=N, delta_pix=DPIX,
+                                                supersampling=SS, kernel_size=K)
+    kl, ks, kll = W.instance(lens, 0), W.instance(src, 0), W.instance(ll, 0)
+    kps = [{"ra_image": ra0, "dec_image": dec0, "point_amp": np.array([2.0, 1.5, 1.0])}]
+    truth = param.kwargs2args(kl, ks, kll, kps)
+    args = np.clip(truth + 1e-3 * rng.standard_normal((16, truth.size)), lo_all, hi_all)
+    lm = S.LikelihoodModule(joint, model, param)
+    got = lm.logL_batch(args)
+    cls = ImageLinearFit if linear else J.ImageModel
+    im = cls(J.ImageData(data, exposure_time=1000.0, background_rms=0.01, **g),
+             J.PSF("PIXEL", kernel_point_source=kern), J.LensModel(MODEL["lens_model_list"]),
+             J.LightModel(MODEL["source_light_model_list"]),
+             J.LightModel(MODEL["lens_light_model_list"]),
+             point_source_class=J.PointSource(["LENSED_POSITION"]),
+             kwargs_numerics={"supersampling_factor": SS})
+    ref = []
+    for a in args:
+        kw = param.args2kwargs(a)
+        r = im.likelihood_data_given_model(kw["kwargs_lens"], kw["kwargs_source"],
+                                           kw["kwargs_lens_light"], kw["kwargs_ps"])
+        ref.append(r[0] if linear else r)
+    np.testing.assert_allclose(got, np.array(ref), rtol=1e-12, atol=0)

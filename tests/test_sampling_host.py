@@ -89,3 +89,31 @@ def test_likelihood_module_rejects_unsupported_terms():
     with pytest.raises(ValueError):
         S.ImageLikelihood([[{}, {}, {}]], "single-band", MODEL, source_marg=True,
                           linear_solver=False)
+
+
+def test_param_point_sources_round_trip():
+    """Point-source arguments (ra_image, dec_image per image; point_amp left to the
+    linear solve) after the light profiles; batched args give (n, n_images) arrays."""
+    from jaxtronomy_gb300.sampling import Param
+    km = {"lens_model_list": ["SIE"], "source_light_model_list": ["SERSIC"],
+          "lens_light_model_list": [], "point_source_model_list": ["LENSED_POSITION"]}
+    lo = [{"ra_image": [-2.0] * 4, "dec_image": [-2.0] * 4}]
+    hi = [{"ra_image": [2.0] * 4, "dec_image": [2.0] * 4}]
+    p = Param(km, kwargs_fixed_lens=[{"center_x": 0.0, "center_y": 0.0}],
+              kwargs_lower_ps=lo, kwargs_upper_ps=hi, num_point_source_list=[4])
+    n, names = p.num_param()
+    assert n == 3 + 4 + 8 and names[-8:] == ["ra_image"] * 4 + ["dec_image"] * 4
+    a = np.random.default_rng(0).uniform(-1, 1, (3, n))
+    kw = p.args2kwargs(a)
+    assert kw["kwargs_ps"][0]["ra_image"].shape == (3, 4)
+    np.testing.assert_array_equal(kw["kwargs_ps"][0]["point_amp"], np.ones(4))
+    one = p.args2kwargs(a[1])
+    np.testing.assert_array_equal(p.kwargs2args(one["kwargs_lens"], one["kwargs_source"],
+                                                one["kwargs_lens_light"], one["kwargs_ps"]), a[1])
+    lo_all, hi_all = p.param_limits()
+    assert lo_all[-1] == -2.0 and hi_all[-1] == 2.0
+    with pytest.raises(ValueError):
+        Param(km, num_point_source_list=[4])          # sampled ps arrays need bounds
+    p2 = Param(km, linear_solver=False, kwargs_lower_ps=[dict(lo[0], point_amp=[0.0] * 4)],
+               kwargs_upper_ps=[dict(hi[0], point_amp=[10.0] * 4)], num_point_source_list=[4])
+    assert p2.num_param()[0] == 5 + 5 + 12

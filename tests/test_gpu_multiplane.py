@@ -160,3 +160,28 @@ def test_multi_plane_abi_rejects_bad_arguments(cuda):
     rc = _lib.load().lensgb_bulk_multi_plane_ray_shooting(h, i.data_ptr(), p, 0, p, p, p, p, p,
                                                           p, p, 1, None)
     assert rc == 1
+
+
+def test_multi_plane_benchmark_realisation_fp32_vs_fp64(cuda):
+    """The benchmark's full workload (400^2 rays, 5130 TNFW + 126 CONVERGENCE on 126
+    planes, 5501 steps): FP32 beta within 2e-7 arcsec of FP64 on every ray, and FP64
+    within 1e-10 of the oracle on a ray sample."""
+    x, y, ll, kw, z, zs, nd = W.line_of_sight_halos()
+    unique = ["TNFW", "CONVERGENCE"]
+    cosmo = J.FlatLambdaCDM(67.66, 0.30966)
+    b64 = J.LensModelBulk(unique, multi_plane=True, cosmo=cosmo)
+    b32 = J.LensModelBulk(unique, multi_plane=True, cosmo=cosmo, precision="fp32")
+    rk = b64.prepare_ray_shooting_kwargs(ll, kw, z_source=zs, lens_redshift_list=z,
+                                         num_deflectors=nd)
+    xt = torch.as_tensor(x).cuda()
+    yt = torch.as_tensor(y).cuda()
+    bx, by = b64.ray_shooting(xt, yt, rk)
+    fx, fy = b32.ray_shooting(xt, yt, rk)
+    err = torch.maximum((fx - bx).abs(), (fy - by).abs())
+    assert err.max().item() <= FP32_BETA_ATOL
+    s = np.arange(0, x.size, x.size // 64)[:64]
+    ox, oy = olens.multi_plane_ray_shooting(unique, x[s], y[s], rk["all_kwargs"], rk["index_list"],
+                                            rk["T_ij_list"], rk["T_z_list"],
+                                            rk["reduced2physical_factor"])
+    assert_beta_close(bx.cpu().numpy()[s], ox)
+    assert_beta_close(by.cpu().numpy()[s], oy)

@@ -92,16 +92,21 @@ class _BulkProfiles:
             isinstance(v, torch.Tensor) for v in all_kwargs.values())
         n_unique = len(self.unique_lens_model_list)
         if on_dev:
+            # one gather: S stacks the parameter arrays (plus a zero row), and
+            # G[u, j] names the row of S that column j of profile u reads
             idx = _device.to_device(index_list, torch.int64).reshape(-1)
             n = idx.numel()
-            rows = torch.zeros((n, _lib.BULK_PARAM_STRIDE), dtype=torch.float64, device=idx.device)
+            names = sorted(set(q for sub in self.param_name_list for q in sub))
+            S = torch.stack([_device.to_device_f64(all_kwargs[q]).reshape(-1) for q in names]
+                            + [torch.zeros(n, dtype=torch.float64, device=idx.device)])
+            G = np.full((n_unique + 1, _lib.BULK_PARAM_STRIDE), len(names), dtype=np.int64)
+            for u, pn in enumerate(self.param_name_list[:-1]):
+                for j, q in zip(self._columns[u], pn):
+                    G[u, j] = names.index(q)
+            G = torch.as_tensor(G, device=idx.device)
             k = idx.clamp(0, n_unique)
-            for u, names in enumerate(self.param_name_list[:-1]):
-                sel = k == u
-                for j, p in zip(self._columns[u], names):
-                    v = _device.to_device_f64(all_kwargs[p]).reshape(-1)
-                    rows[:, j] = torch.where(sel, v, rows[:, j])
-            return idx.to(torch.int32).contiguous(), rows
+            rows = S.t().gather(1, G.index_select(0, k))
+            return idx.to(torch.int32).contiguous(), rows.contiguous()
         idx, rows = self.pack_rows(all_kwargs, index_list)
         return _device.to_device(idx, torch.int32), _device.to_device_f64(rows)
 

@@ -387,7 +387,19 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                                ((double)dh[c][k] + (double)dl[c][k]) * itz;
                     }
                     double ax, ay;
-                    lens_deflect<double>(code, rd, cd, o[0], o[1], ax, ay);
+                    const double u = (o[0] * o[0] + o[1] * o[1]) * (rd[6] * rd[6]);
+                    if (code == LENSGB_LENS_TNFW && u >= rd[10]) {
+                        // far field of a strong TNFW halo: the record's 16-term series
+                        // (truncation below 1e-8 relative, far inside this path's error)
+                        const double e = 1.0 / sqrt(u), z = rd[12] * e;
+                        double bs = rd[29];
+                        for (int q = 14; q >= 0; --q) bs = fma(bs, z, rd[14 + q]);
+                        const double a = rd[11] * bs * (e * e);
+                        ax = a * o[0];
+                        ay = a * o[1];
+                    } else {
+                        lens_deflect<double>(code, rd, cd, o[0], o[1], ax, ay);
+                    }
                     float h, l;
                     split_double(ax, h, l);
                     pair_add(ph[0][k], pq[0][k], h, l);

@@ -352,6 +352,14 @@ int lensgb_alpha(const lensgb_model* model, const double* params_dev, const doub
                  const double* y_dev, double* alpha_x_dev, double* alpha_y_dev, long long n,
                  void* stream);
 
+/* LensModel.hessian (jaxtronomy/LensModel/lens_model.py:384-414 ->
+ * single_plane.py:142-180) of the model's lens profiles at n points, FP64:
+ * out_dev receives f_xx, f_xy, f_yx, f_yy as four consecutive arrays of n
+ * doubles (times alpha_scaling).  EPL, SIE, NIE, NFW, TNFW, SHEAR and
+ * CONVERGENCE only (LENSGB_ERR_UNSUPPORTED otherwise). */
+int lensgb_hessian(const lensgb_model* model, const double* params_dev, const double* x_dev,
+                   const double* y_dev, double* out_dev, long long n, void* stream);
+
 /* LightModel.surface_brightness of the model's source (which = 0) or lens
  * light (which = 1) profiles over n arbitrary points (light_model_base.py:230-252),
  * FP64.  params_dev holds that light model's kwargs only. */

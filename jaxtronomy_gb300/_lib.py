@@ -48,7 +48,7 @@ SYMBOLS = [
     "lensgb_surface_brightness",
     "lensgb_bulk_create", "lensgb_bulk_destroy", "lensgb_bulk_set_fp32_alpha_max",
     "lensgb_bulk_ray_shooting", "lensgb_bulk_multi_plane_ray_shooting",
-    "lensgb_loglike_image", "lensgb_point_sources_add",
+    "lensgb_loglike_image", "lensgb_point_sources_add", "lensgb_hessian",
     "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
@@ -237,6 +237,8 @@ def load():
     lib.lensgb_loglike_image.restype = i
     lib.lensgb_point_sources_add.argtypes = [vp, dp, i, i, dp, i, ll, i, vp, vp]
     lib.lensgb_point_sources_add.restype = i
+    lib.lensgb_hessian.argtypes = [vp, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_hessian.restype = i
     lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
     lib.lensgb_server_create.restype = i
     lib.lensgb_server_submit.argtypes = [vp, ctypes.POINTER(Request), i,

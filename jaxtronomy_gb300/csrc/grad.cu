@@ -720,4 +720,71 @@ int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, cons
     return 0;
 }
 
+// LensModel.hessian (LensModel/lens_model.py:384-414 -> single_plane.py:142-180):
+// f_xx, f_xy, f_yx, f_yy of the lens stack at n points, the derivatives of each
+// profile's deflection with respect to the ray position taken from the same
+// dual-number evaluation as the adjoint (the centre derivatives, negated), times
+// alpha_scaling.  One thread per point; out holds the four components as four
+// consecutive arrays of n.
+__global__ void hessian_points_kernel(StackDesc st, const double* __restrict__ rec,
+                                      const double* __restrict__ coef,
+                                      const double* __restrict__ P, const double* __restrict__ x,
+                                      const double* __restrict__ y, double* __restrict__ out,
+                                      long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double X = x[i], Y = y[i];
+    double h[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int p = 0; p < st.n_lens; ++p) {
+        const int code = st.lens[p];
+        const double* r = rec + p * REC_D;
+        const double* a = P + st.lens_off[p];
+        const double dx = X - r[RD_CX], dy = Y - r[RD_CY];
+        if (code == LENSGB_LENS_CONVERGENCE) {
+            h[0] += r[2];
+            h[3] += r[2];
+            continue;
+        }
+        double ax, ay, J[2][6];
+        int co;
+        if (code == LENSGB_LENS_EPL) {
+            // dF/dt enters only the t direction of the duals: the coefficient table
+            // stands in for it
+            const double* F = coef + st.epl_slot[p] * EPL_NMAX;
+            epl_alpha_grad(r, F, F, a, dx, dy, ax, ay, J);
+            co = 4;
+        } else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
+            nie_alpha_grad(code, r, a, dx, dy, ax, ay, J);
+            co = code == LENSGB_LENS_SIE ? 3 : 4;
+        } else if (code == LENSGB_LENS_NFW || code == LENSGB_LENS_TNFW) {
+            nfw_alpha_grad(code, a, dx, dy, ax, ay, J);
+            co = code == LENSGB_LENS_TNFW ? 3 : 2;
+        } else {
+            shear_alpha_grad(r, dx, dy, ax, ay, J);
+            co = 2;
+        }
+        h[0] -= J[0][co];
+        h[1] -= J[0][co + 1];
+        h[2] -= J[1][co];
+        h[3] -= J[1][co + 1];
+    }
+    for (int c = 0; c < 4; ++c) out[c * n + i] = h[c] * st.alpha_scaling;
+}
+
+bool hessian_supported(const StackDesc& st) {
+    for (int p = 0; p < st.n_lens; ++p)
+        if (st.lens[p] != LENSGB_LENS_CONVERGENCE && lens_np(st.lens[p]) <= 0) return false;
+    return true;
+}
+
+int launch_hessian_points(const StackDesc& st, const double* rec, const double* coef,
+                          const double* params, const double* x, const double* y, double* out,
+                          long long n, cudaStream_t stream) {
+    if (n <= 0) return 0;
+    const int threads = 128;
+    hessian_points_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(
+        st, rec, coef, params, x, y, out, n);
+    return 0;
+}
+
 }  // namespace lensgb

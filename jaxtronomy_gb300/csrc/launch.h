@@ -177,6 +177,13 @@ int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* r
                              const double* coef_d, const float* coef_f, int n_defl,
                              const double* x, const double* y, double* bx, double* by,
                              long long n, int precision, cudaStream_t stream);
+// LensModel.hessian at n points (out: f_xx, f_xy, f_yx, f_yy, n each) from the
+// lens records of one parameter row; hessian_supported: every lens profile has
+// position derivatives (EPL, SIE, NIE, NFW, TNFW, SHEAR, CONVERGENCE).
+bool hessian_supported(const StackDesc& st);
+int launch_hessian_points(const StackDesc& st, const double* rec, const double* coef,
+                          const double* params, const double* x, const double* y, double* out,
+                          long long n, cudaStream_t stream);
 // Point-source rendering: adds to out (n_inst images of rows x cols, model
 // precision) the n_img images (ra, dec, amp) of each system, the kernel
 // (ks x ks doubles; kstride per system, 0: shared) at subgrid factor p.

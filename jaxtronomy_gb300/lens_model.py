@@ -120,3 +120,68 @@ class LensModel:
     def alpha(self, x, y, kwargs, k=None):
         """Deflection angles, ``lens_model.py:353-381``."""
         return self._points("alpha", x, y, kwargs, k)
+
+    def hessian(self, x, y, kwargs, k=None, diff=None, diff_method="square"):
+        """``lens_model.py:384-414``: (f_xx, f_xy, f_yx, f_yy).  ``diff=None`` gives the
+        exact second derivatives (``lensgb_hessian``: EPL, SIE, NIE, NFW, TNFW, SHEAR,
+        CONVERGENCE); a step ``diff`` gives the reference's finite differences of
+        ``alpha`` on a square or a cross (``:617-680``), for any profile."""
+        if diff is not None:
+            if diff_method == "square":
+                return self._hessian_differential_square(x, y, kwargs, k, diff)
+            if diff_method == "cross":
+                return self._hessian_differential_cross(x, y, kwargs, k, diff)
+            raise ValueError('diff_method %s not supported. Chose among "square" or "cross".'
+                             % diff_method)
+        _device.require_cuda()
+        idx = self._select(k)
+        xt = _device.to_device_f64(x).reshape(-1)
+        yt = _device.to_device_f64(y).reshape(-1)
+        shape = np.shape(x) if not isinstance(x, torch.Tensor) else tuple(x.shape)
+        out = torch.zeros((4, xt.numel()), dtype=torch.float64, device=xt.device)
+        if len(idx):
+            m = self._model(idx)
+            p = _device.to_device_f64(self._row(idx, kwargs))
+            _lib.check(_lib.load().lensgb_hessian(
+                m.handle, _device.ptr(p), _device.ptr(xt), _device.ptr(yt), _device.ptr(out),
+                xt.numel(), _device.stream_handle()))
+        return tuple(_as_out(out[c].reshape(shape), x) for c in range(4))
+
+    def _hessian_differential_cross(self, x, y, kwargs, k=None, diff=0.00001):
+        ax_dx, ay_dx = self.alpha(x + diff / 2, y, kwargs, k=k)
+        ax_dy, ay_dy = self.alpha(x, y + diff / 2, kwargs, k=k)
+        ax_dx_, ay_dx_ = self.alpha(x - diff / 2, y, kwargs, k=k)
+        ax_dy_, ay_dy_ = self.alpha(x, y - diff / 2, kwargs, k=k)
+        return ((ax_dx - ax_dx_) / diff, (ax_dy - ax_dy_) / diff, (ay_dx - ay_dx_) / diff,
+                (ay_dy - ay_dy_) / diff)
+
+    def _hessian_differential_square(self, x, y, kwargs, k=None, diff=0.00001):
+        ax_pp, ay_pp = self.alpha(x + diff / 2, y + diff / 2, kwargs, k=k)
+        ax_pn, ay_pn = self.alpha(x + diff / 2, y - diff / 2, kwargs, k=k)
+        ax_np, ay_np = self.alpha(x - diff / 2, y + diff / 2, kwargs, k=k)
+        ax_nn, ay_nn = self.alpha(x - diff / 2, y - diff / 2, kwargs, k=k)
+        return ((ax_pp - ax_np + ax_pn - ax_nn) / diff / 2,
+                (ax_pp - ax_pn + ax_np - ax_nn) / diff / 2,
+                (ay_pp - ay_np + ay_pn - ay_nn) / diff / 2,
+                (ay_pp - ay_pn + ay_np - ay_nn) / diff / 2)
+
+    def kappa(self, x, y, kwargs, k=None, diff=None, diff_method="square"):
+        """``lens_model.py:417-441``: convergence (f_xx + f_yy) / 2."""
+        f_xx, _, _, f_yy = self.hessian(x, y, kwargs, k, diff, diff_method)
+        return 1.0 / 2 * (f_xx + f_yy)
+
+    def curl(self, x, y, kwargs, k=None, diff=None, diff_method="square"):
+        """``lens_model.py:444-467``: f_xy - f_yx."""
+        _, f_xy, f_yx, _ = self.hessian(x, y, kwargs, k, diff, diff_method)
+        return f_xy - f_yx
+
+    def gamma(self, x, y, kwargs, k=None, diff=None, diff_method="square"):
+        """``lens_model.py:470-497``: shear (gamma1, gamma2)."""
+        f_xx, f_xy, _, f_yy = self.hessian(x, y, kwargs, k, diff, diff_method)
+        return 1.0 / 2 * (f_xx - f_yy), f_xy
+
+    def magnification(self, x, y, kwargs, k=None, diff=None, diff_method="square"):
+        """``lens_model.py:500-526``: 1 / det(1 - Hessian)."""
+        f_xx, f_xy, f_yx, f_yy = self.hessian(x, y, kwargs, k, diff, diff_method)
+        det_A = (1 - f_xx) * (1 - f_yy) - f_xy * f_yx
+        return 1.0 / det_A

@@ -104,6 +104,14 @@ def gen_profiles(rng):
         out = lm.surface_brightness(x, y, [kw])
         cases.append({"kind": "light", "name": name, "kwargs": kw, "x": x, "y": y,
                       "out": np.asarray(out)[None, :]})
+    # exact Hessians of the profiles with position derivatives (kind "hessian")
+    for name, kw in [lens_cases[0], lens_cases[2], lens_cases[3], lens_cases[5],
+                     lens_cases[6], lens_cases[7]] + [c for c in lens_cases if c[0] == "EPL"][:8:3]:
+        x, y = _points(rng, 64)
+        x[:4] = x[:4] + 0.3  # away from the centre floors
+        out = np.stack([np.asarray(v) for v in LensModel([name]).hessian(x, y, [kw])])
+        cases.append({"kind": "hessian", "name": name, "kwargs": kw, "x": x, "y": y,
+                      "out": out})
     for kw in ({"kappa": -0.03, "ra_0": 0.2, "dec_0": -0.1}, {"kappa": 0.12}):
         x, y = _points(rng, 64)
         ax, ay = LensModel(["CONVERGENCE"]).alpha(x, y, [kw])

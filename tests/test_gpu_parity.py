@@ -83,6 +83,28 @@ def test_fp32_image_matches_reference(cuda, sc):
 @pytest.mark.parametrize("case", golden_io.profile_cases(),
                          ids=lambda c: "%s-%s" % (c["kind"], c["name"]))
 def test_profiles_match_reference(cuda, case):
+    if case["kind"] == "hessian":
+        # exact second derivatives vs the reference's analytic Hessians
+        lm = J.LensModel([case["name"]])
+        got = np.array(lm.hessian(case["x"], case["y"], [case["kwargs"]]))
+        ref = case["out"]
+        if case["name"] in ("SIE", "NIE"):
+            # the reference's NIE Hessian is a one-sided difference of its deflection
+            # with step 1e-10 (nie.py:298-312): ~1e-6 relative error of its own
+            np.testing.assert_allclose(got, ref, rtol=0, atol=5e-6 * np.abs(ref).max())
+        else:
+            np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+        # derived quantities (lens_model.py:417-526)
+        f_xx, f_xy, f_yx, f_yy = ref
+        g_xx, g_xy, g_yx, g_yy = got
+        np.testing.assert_allclose(lm.kappa(case["x"], case["y"], [case["kwargs"]]),
+                                   (g_xx + g_yy) / 2, rtol=1e-14, atol=1e-15)
+        mag = 1.0 / ((1 - g_xx) * (1 - g_yy) - g_xy * g_yx)
+        np.testing.assert_allclose(lm.magnification(case["x"], case["y"], [case["kwargs"]]),
+                                   mag, rtol=1e-12)
+        fd = np.array(lm.hessian(case["x"], case["y"], [case["kwargs"]], diff=1e-5))
+        np.testing.assert_allclose(fd, ref, rtol=1e-4, atol=1e-5 * np.abs(ref).max())
+        return
     if case["kind"] == "lens":
         lm = J.LensModel([case["name"]])
         ax, ay = lm.alpha(case["x"], case["y"], [case["kwargs"]])

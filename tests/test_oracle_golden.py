@@ -17,6 +17,8 @@ warnings.filterwarnings("ignore", category=RuntimeWarning)
 @pytest.mark.parametrize("case", golden_io.profile_cases(),
                          ids=lambda c: "%s-%s" % (c["kind"], c["name"]))
 def test_profiles_match_reference(case):
+    if case["kind"] == "hessian":
+        pytest.skip("Hessians have no oracle restatement; checked on the GPU")
     if case["kind"] == "lens":
         got = np.array(lens.deflection(case["name"], case["x"], case["y"], case["kwargs"]))
     else:

@@ -38,28 +38,42 @@ class ImageLinearFit(ImageModel):
             raise ValueError("at most %d linear light components are supported"
                              % _lib.LINEAR_MAX)
 
-    def _ps_linear(self, kwargs_ps, kwargs_special=None):
-        """Positions of the point images with linear amplitudes (flux from the point
-        source), shifted as ``point_source_linear_response_set`` does
-        (``image_linear_solve.py:559-600``): lists of (ra, dec) arrays of shape
-        (B or 1,) per image."""
+    def _ps_linear(self, kwargs_ps, kwargs_special=None, kwargs_lens=None):
+        """Response rows of the point sources with linear amplitudes
+        (``PointSource.linear_response_set``, point_source.py:347-384): one row per
+        image (amp 1), or one row per fixed-magnification model (all its images,
+        amp |mag|); positions shifted as ``point_source_linear_response_set`` does
+        (``image_linear_solve.py:559-600``, image by image in row order).  Each row
+        is [ra, dec, amp] arrays of shape (B or 1, n_row)."""
         if not self._n_ps:
             return []
-        ra, dec = self.PointSource.image_position(kwargs_ps)
+        ps = self.PointSource
+        ra, dec = ps.image_position(kwargs_ps)
         out = []
         for k, (r, d) in enumerate(zip(ra, dec)):
-            if not self.PointSource._flux_from_point_source_list[k]:
+            if not ps._flux_from_point_source_list[k]:
                 continue
             r = np.atleast_2d(r)
             d = np.atleast_2d(d)
-            for j in range(r.shape[-1]):
-                out.append([r[:, j].copy(), d[:, j].copy()])
+            if ps.fixed_magnification(k):
+                mag = np.atleast_2d(ps.magnification(kwargs_ps[k]["ra_image"],
+                                                     kwargs_ps[k]["dec_image"], kwargs_lens))
+                out.append([r.copy(), d.copy(), mag])
+            else:
+                for j in range(r.shape[-1]):
+                    out.append([r[:, j:j + 1].copy(), d[:, j:j + 1].copy(),
+                                np.ones((1, 1))])
         if kwargs_special is not None and "delta_x_image" in kwargs_special:
-            dx = np.asarray(kwargs_special["delta_x_image"], dtype=float)
-            dy = np.asarray(kwargs_special["delta_y_image"], dtype=float)
-            for q in range(min(len(out), dx.shape[-1])):
-                out[q][0] = out[q][0] + dx[..., q]
-                out[q][1] = out[q][1] + dy[..., q]
+            dx = np.atleast_2d(np.asarray(kwargs_special["delta_x_image"], dtype=float))
+            dy = np.atleast_2d(np.asarray(kwargs_special["delta_y_image"], dtype=float))
+            q = 0
+            for row in out:
+                for j in range(row[0].shape[-1]):
+                    if q >= dx.shape[-1]:
+                        break
+                    row[0] = row[0] + np.eye(row[0].shape[-1])[j] * dx[..., q:q + 1]
+                    row[1] = row[1] + np.eye(row[1].shape[-1])[j] * dy[..., q:q + 1]
+                    q += 1
         return out
 
     # ------------------------------------------------------------------ linear parameters
@@ -77,7 +91,10 @@ class ImageLinearFit(ImageModel):
             kw["amp"] for kw in (kwargs_lens_light or [])]
         for k, kw in enumerate(kwargs_ps or []):
             if self.PointSource._flux_from_point_source_list[k]:
-                out += list(np.atleast_1d(kw["point_amp"]))
+                if self.PointSource.fixed_magnification(k):
+                    out.append(kw["source_amp"])
+                else:
+                    out += list(np.atleast_1d(kw["point_amp"]))
         return out
 
     def update_linear_kwargs(self, param, kwargs_lens, kwargs_source, kwargs_lens_light,
@@ -92,6 +109,10 @@ class ImageLinearFit(ImageModel):
         c = self._n_src + self._n_ll
         for k, kw in enumerate(kwargs_ps or []):
             if self.PointSource._flux_from_point_source_list[k]:
+                if self.PointSource.fixed_magnification(k):
+                    kw["source_amp"] = p[..., c]
+                    c += 1
+                    continue
                 n = np.shape(kw["ra_image"])[-1]
                 kw["point_amp"] = p[..., c:c + n]
                 c += n
@@ -114,7 +135,7 @@ class ImageLinearFit(ImageModel):
         each source lensed alone, each lens-light profile alone, amp = 1, then each
         point image alone at amp = 1 without the flux scaling (image_linear_solve.py:
         440-456)."""
-        ps_pos = self._ps_linear(kwargs_ps, kwargs_special)
+        ps_pos = self._ps_linear(kwargs_ps, kwargs_special, kwargs_lens)
         if self._n_src + self._n_ll + len(ps_pos) > _lib.LINEAR_MAX:
             raise ValueError("at most %d linear amplitudes are supported" % _lib.LINEAR_MAX)
         n_lens = len(self.LensModel.lens_model_list)
@@ -128,7 +149,8 @@ class ImageLinearFit(ImageModel):
                 for (li, si, lli), lensed in jobs]
         # the batch of the whole kwargs (a lens-light row alone does not see batched lens
         # kwargs): rows of one system are repeated
-        B = max([r.shape[0] for r in rows] + [p[0].shape[0] for p in ps_pos] + [1])
+        B = max([r.shape[0] for r in rows] + [max(p[0].shape[0], p[2].shape[0]) for p in ps_pos]
+                + [1])
         A = torch.empty((len(jobs) + len(ps_pos), B, self._nx, self._ny), dtype=self._dtype,
                         device="cuda")
         for c, ((li, si, lli), lensed) in enumerate(jobs):
@@ -137,11 +159,12 @@ class ImageLinearFit(ImageModel):
             self._launch(model, _device.to_device_f64(r), B, flags, psf_kernels, A[c], stream)
         # the renderer applies the model's flux scaling; the response rows have none
         unit = 1.0 / self._flux_scaling
-        for j, (ra, dec) in enumerate(ps_pos):
+        for j, (ra, dec, amp) in enumerate(ps_pos):
             row = A[len(jobs) + j]
             row.zero_()
-            pts = np.stack([np.broadcast_to(ra, (B,)), np.broadcast_to(dec, (B,)),
-                            np.full(B, unit)], axis=-1)[:, None, :]
+            m = ra.shape[-1]
+            pts = np.stack([np.broadcast_to(ra, (B, m)), np.broadcast_to(dec, (B, m)),
+                            np.broadcast_to(amp, (B, m)) * unit], axis=-1)
             self._render_point_rows(row, np.ascontiguousarray(pts), False, psf_kernels, stream)
         return A
 

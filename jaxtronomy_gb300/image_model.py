@@ -17,6 +17,7 @@ with FP64 set-up, FP64-accurate coordinate offsets and an FP64 likelihood
 reduction).
 """
 
+import copy
 import ctypes
 
 import numpy as np
@@ -177,6 +178,10 @@ class ImageModel:
         if data_class.primary_beam is not None:
             raise ValueError("primary beam not supported")
         self.LensModel = lens_model_class if lens_model_class is not None else LensModel([])
+        if self.PointSource._lens_model is None:
+            # image_model.py:80-92: the point sources get the image's lens model
+            self.PointSource = copy.copy(self.PointSource)
+            self.PointSource._lens_model = self.LensModel
         self.SourceModel = source_model_class if source_model_class is not None else LightModel([])
         self.LensLightModel = (lens_light_model_class if lens_light_model_class is not None
                                else LightModel([]))
@@ -421,11 +426,12 @@ class ImageModel:
         return out
 
     # ------------------------------------------------------------------ point sources
-    def point_source_rows(self, kwargs_ps, kwargs_special=None, B=None, k=None):
+    def point_source_rows(self, kwargs_ps, kwargs_special=None, B=None, k=None,
+                          kwargs_lens=None):
         """(B, n_images, 3) FP64 rows (ra, dec, amp): PointSource.point_source_list
         (point_source.py:255-284) after ImageModel._displace_astrometry
         (image_model.py:652-676), broadcast over a batch of B systems."""
-        ra, dec, amp = self.PointSource.point_source_list(kwargs_ps, k=k)
+        ra, dec, amp = self.PointSource.point_source_list(kwargs_ps, kwargs_lens, k=k)
         ra, dec, amp = (np.atleast_2d(np.asarray(a, dtype=float)) for a in (ra, dec, amp))
         n = ra.shape[-1]
         if kwargs_special is not None and "delta_x_image" in kwargs_special:
@@ -445,7 +451,7 @@ class ImageModel:
         return np.array(np.broadcast_to(rows, (B, n, 3)), dtype=np.float64)
 
     def _add_point_sources(self, out, B, kwargs_ps, kwargs_special=None, unconvolved=False,
-                           psf_kernels=None, stream=None, k=None):
+                           psf_kernels=None, stream=None, k=None, kwargs_lens=None):
         """Adds ImageModel.point_source (image_model.py:396-429) to the (B, ny, nx)
         images ``out`` on the GPU (``lensgb_point_sources_add``)."""
         if not self._n_ps:
@@ -453,7 +459,7 @@ class ImageModel:
         if kwargs_ps is None:
             raise ValueError("kwargs_ps is needed for the point-source models %s"
                              % self.PointSource.point_source_type_list)
-        rows = self.point_source_rows(kwargs_ps, kwargs_special, B, k=k)
+        rows = self.point_source_rows(kwargs_ps, kwargs_special, B, k=k, kwargs_lens=kwargs_lens)
         return self._render_point_rows(out, rows, unconvolved, psf_kernels, stream)
 
     def _render_point_rows(self, out, rows, unconvolved=False, psf_kernels=None, stream=None):
@@ -570,7 +576,7 @@ class ImageModel:
                                None if host_out else out, stream)
         if with_ps:
             self._add_point_sources(dev_out, B, kwargs_ps, kwargs_special, unconvolved,
-                                    psf_kernels, stream)
+                                    psf_kernels, stream, kwargs_lens=kwargs_lens)
         if host_out:
             out.copy_(dev_out)
             return out
@@ -778,10 +784,9 @@ class ImageModel:
         the k-th)."""
         if not self._n_ps:
             return np.zeros((self._nx, self._ny))
-        rows = self.point_source_rows(kwargs_ps, kwargs_special, k=k)
+        rows = self.point_source_rows(kwargs_ps, kwargs_special, k=k, kwargs_lens=kwargs_lens)
         out = torch.zeros((rows.shape[0], self._nx, self._ny), dtype=self._dtype, device="cuda")
-        self._add_point_sources(out, rows.shape[0], kwargs_ps, kwargs_special, unconvolved,
-                                k=k)
+        self._render_point_rows(out, rows, unconvolved)
         return out[0].to(torch.float64).cpu().numpy()
 
     def reduced_residuals(self, model, error_map=0):

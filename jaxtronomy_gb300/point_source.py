@@ -6,9 +6,9 @@ Drop-in for ``jaxtronomy.PointSource.point_source.PointSource``
 amplitudes ``point_amp`` given) and ``UNLENSED`` (``Types/unlensed.py``).  The
 reference raises for ``SOURCE_POSITION``, for additional images (both need
 the lens-equation solver) and for ``save_cache``; this library raises in the
-same places, and also for ``fixed_magnification`` (amplitudes from the lens
-magnification, which needs lens Hessians that this library does not
-compute).
+same places.  ``fixed_magnification`` LENSED_POSITION models take
+``source_amp`` and give each image ``source_amp * |magnification|``, the
+magnification from the lens model's exact Hessian (``LensModel.magnification``).
 
 Kwargs values may be arrays of shape (n_images,) for one system or
 (B, n_images) for a batch.
@@ -59,9 +59,6 @@ class PointSource:
             if model not in _SUPPORTED_MODELS:
                 raise ValueError("Point-source model %s not available. Supported models are %s ."
                                  % (model, _SUPPORTED_MODELS))
-            if model == "LENSED_POSITION" and self._fixed_magnification_list[i]:
-                raise ValueError("fixed_magnification needs lens Hessians, which this library "
-                                 "does not compute")
 
     def _check(self, kwargs_ps):
         if len(kwargs_ps) != len(self.point_source_type_list):
@@ -84,14 +81,48 @@ class PointSource:
                 dec.append(np.asarray(kw["dec_image"], dtype=float))
         return ra, dec
 
+    def fixed_magnification(self, i):
+        return (self.point_source_type_list[i] == "LENSED_POSITION"
+                and bool(self._fixed_magnification_list[i]))
+
+    def magnification(self, ra, dec, kwargs_lens):
+        """|magnification| of the lens model at image positions of shape (n,) or
+        (B, n); batched lens kwargs are evaluated system by system."""
+        if self._lens_model is None:
+            raise ValueError("fixed_magnification needs the lens model (PointSource(..., "
+                             "lens_model=...) or an ImageModel)")
+        ra = np.asarray(ra, dtype=float)
+        dec = np.asarray(dec, dtype=float)
+        sizes = [np.size(v) for kw in (kwargs_lens or []) for v in kw.values()]
+        B = max(sizes + [1])
+        if ra.ndim == 2:
+            B = max(B, ra.shape[0])
+        if B == 1 and ra.ndim == 1:
+            return np.abs(np.asarray(self._lens_model.magnification(ra, dec, kwargs_lens)))
+        ra2 = np.broadcast_to(np.atleast_2d(ra), (B, ra.shape[-1]))
+        dec2 = np.broadcast_to(np.atleast_2d(dec), (B, dec.shape[-1]))
+        out = np.empty(ra2.shape)
+        for b in range(B):
+            kl = [{key: (np.asarray(v).reshape(-1)[b] if np.size(v) > 1 else
+                         float(np.asarray(v).reshape(-1)[0])) for key, v in kw.items()}
+                  for kw in kwargs_lens]
+            out[b] = np.abs(np.asarray(self._lens_model.magnification(ra2[b], dec2[b], kl)))
+        return out
+
     def image_amplitude(self, kwargs_ps, kwargs_lens=None, k=None):
         """``point_source.py:304-326``: per model, the image amplitudes (zeros where
-        flux_from_point_source is False)."""
+        flux_from_point_source is False; ``source_amp * |mag|`` with fixed
+        magnification, ``Types/lensed_position.py:134-177``)."""
         self._check(kwargs_ps)
         out = []
         for i, kw in enumerate(kwargs_ps):
             if k is None or k == i:
-                amp = np.asarray(kw["point_amp"], dtype=float)
+                if self.fixed_magnification(i):
+                    mag = self.magnification(kw["ra_image"], kw["dec_image"], kwargs_lens)
+                    sa = np.asarray(kw["source_amp"], dtype=float)
+                    amp = (sa[..., None] if sa.ndim else sa) * mag
+                else:
+                    amp = np.asarray(kw["point_amp"], dtype=float)
                 out.append(amp if self._flux_from_point_source_list[i] else np.zeros_like(amp))
         return out
 
@@ -118,13 +149,14 @@ class PointSource:
     def num_basis(self, kwargs_ps, kwargs_lens=None):
         """``point_source.py:286-302``: number of linear amplitudes."""
         ra, _ = self.image_position(kwargs_ps, kwargs_lens)
-        return int(sum(np.shape(r)[-1] if np.ndim(r) else 1
+        return int(sum((1 if self.fixed_magnification(i) else
+                        (np.shape(r)[-1] if np.ndim(r) else 1))
                        for i, r in enumerate(ra) if self._flux_from_point_source_list[i]))
 
     def check_positive_flux(self, kwargs_ps):
         """``point_source.py:488-502``: True when no ``point_amp`` is negative."""
-        return all(np.all(np.asarray(kw["point_amp"]) >= 0) for kw in kwargs_ps
-                   if "point_amp" in kw)
+        return all(np.all(np.asarray(kw[key]) >= 0) for kw in kwargs_ps
+                   for key in ("point_amp", "source_amp") if key in kw)
 
 
 def _cat(arrays):

@@ -383,7 +383,7 @@ def gen_point_sources(rng):
     out = []
 
     def scene(tag, n, dpix, s, psf_kwargs, ps_kwargs, numerics=None, special=None,
-              unconvolved=False, flux_scaling=1.0):
+              unconvolved=False, flux_scaling=1.0, fixed=None):
         g = W.grid_kwargs(n, dpix)
         rng_d = np.random.default_rng(len(out) + 7)
         data = rng_d.normal(0, 0.01, (n, n))
@@ -394,7 +394,8 @@ def gen_point_sources(rng):
         num = dict({"supersampling_factor": s}, **(numerics or {}))
         im = ImageModel(data_class, refshim.PSF(**psf_kwargs), LensModel(["EPL", "SHEAR"]),
                         LightModel(["SERSIC_ELLIPSE"]), LightModel(["SERSIC"]),
-                        point_source_class=PointSource(["LENSED_POSITION", "UNLENSED"]),
+                        point_source_class=PointSource(["LENSED_POSITION", "UNLENSED"],
+                                                       fixed_magnification_list=fixed),
                         kwargs_numerics=num)
         image = np.asarray(im.image(lens, src, ll, ps_kwargs, kwargs_special=special,
                                     unconvolved=unconvolved))
@@ -405,7 +406,7 @@ def gen_point_sources(rng):
                "psf": {k: v for k, v in psf_kwargs.items() if k != "kernel_point_source"},
                "ps": ps_kwargs, "special": special, "unconvolved": unconvolved,
                "flux_scaling": flux_scaling, "logL": logl, "image": image, "ps1": ps1,
-               "data": data, "lens": lens, "src": src, "ll": ll}
+               "data": data, "lens": lens, "src": src, "ll": ll, "fixed": fixed}
         if "kernel_point_source" in psf_kwargs:
             rec["kernel"] = np.asarray(psf_kwargs["kernel_point_source"], float)
         out.append(rec)
@@ -431,6 +432,11 @@ def gen_point_sources(rng):
            "point_source_supersampling_factor": 3}, ps,
           numerics={"supersampling_convolution": True, "supersampling_kernel_size": None,
                     "point_source_supersampling_factor": 3})
+    # fixed magnification: amplitudes source_amp * |mag| from the EPL + SHEAR Hessian
+    ps_fixed = [{"ra_image": [1.02, -0.55, 0.31], "dec_image": [0.11, 0.87, -0.98],
+                 "source_amp": 1.7}, ps[1]]
+    scene("fixed_magnification", 40, 0.08, 2, {"psf_type": "PIXEL", "kernel_point_source": k11},
+          ps_fixed, fixed=[True, False])
     return out
 
 
@@ -562,6 +568,13 @@ def gen_linear():
              ps=[{"ra_image": [1.05, -0.62, 0.35, -0.2], "dec_image": [0.2, 0.8, -0.95, -0.1],
                   "point_amp": [3.0, 2.5, 1.5, 0.8]},
                  {"ra_image": [0.9], "dec_image": [-1.2], "point_amp": [2.0]}]),
+        dict(tag="epl_fixed_magnification", n=40, dpix=0.08, s=2, lens=["EPL", "SHEAR"], kl=epl,
+             src=["SERSIC_ELLIPSE"], ks=[src], ll=["SERSIC_ELLIPSE"], kll=[ll_e],
+             psf={"psf_type": "PIXEL", "kernel_point_source": W.gaussian_pixel_kernel(0.12, 0.08, 11)},
+             mask=False, marg=True, pos=False, sign=1.0, ps_types=["LENSED_POSITION"],
+             ps_fixed=[True],
+             ps=[{"ra_image": [1.05, -0.62, 0.35], "dec_image": [0.2, 0.8, -0.95],
+                  "source_amp": 2.5}]),
     ]
     for c in cases:
         g = W.grid_kwargs(c["n"], c["dpix"])
@@ -572,10 +585,14 @@ def gen_linear():
         ks_sim[0]["amp"] = ks_sim[0]["amp"] * c["sign"]
         img = np.asarray(sim.image(c["kl"], ks_sim, c["kll"]))
         if c.get("ps"):
-            from jaxtronomy.PointSource.point_source import PointSource
-            img = img + np.asarray(sim.ImageNumerics.point_source_rendering(
-                *[np.concatenate([np.asarray(p[k], float) for p in c["ps"]])
-                  for k in ("ra_image", "dec_image", "point_amp")]))
+            ra = np.concatenate([np.asarray(p["ra_image"], float) for p in c["ps"]])
+            dec = np.concatenate([np.asarray(p["dec_image"], float) for p in c["ps"]])
+            if c.get("ps_fixed"):
+                amp = c["ps"][0]["source_amp"] * np.abs(np.asarray(
+                    LensModel(c["lens"]).magnification(ra, dec, c["kl"])))
+            else:
+                amp = np.concatenate([np.asarray(p["point_amp"], float) for p in c["ps"]])
+            img = img + np.asarray(sim.ImageNumerics.point_source_rendering(ra, dec, amp))
         data = img + rng.normal(0, 0.02, img.shape)
         mask = np.ones((c["n"], c["n"]))
         if c["mask"]:
@@ -586,7 +603,7 @@ def gen_linear():
         pcls = None
         if c.get("ps"):
             from jaxtronomy.PointSource.point_source import PointSource
-            pcls = PointSource(c["ps_types"])
+            pcls = PointSource(c["ps_types"], fixed_magnification_list=c.get("ps_fixed"))
         im = ImageLinearFit(data_class, refshim.PSF(**c["psf"]), LensModel(c["lens"]),
                             LightModel(c["src"], deflection_scaling_list=c.get("dsl")),
                             LightModel(c["ll"]), point_source_class=pcls,
@@ -605,6 +622,7 @@ def gen_linear():
                                  "marg", "pos")}
         rec["dsl"] = c.get("dsl")
         rec["ps_types"], rec["ps"] = c.get("ps_types", []), c.get("ps", [])
+        rec["ps_fixed"] = c.get("ps_fixed")
         rec["psf"] = {k: v for k, v in c["psf"].items() if k != "kernel_point_source"}
         rec["logL"] = float(logl)
         rec["bkg"], rec["exp_time"] = 0.02, 500.0

@@ -27,7 +27,8 @@ def _fit(c, precision="fp64"):
         psf = J.PSF("GAUSSIAN", fwhm=p["fwhm"], truncation=p["truncation"])
     else:
         psf = J.PSF("NONE")
-    pcls = J.PointSource(c["ps_types"]) if c.get("ps_types") else None
+    pcls = (J.PointSource(c["ps_types"], fixed_magnification_list=c.get("ps_fixed"))
+            if c.get("ps_types") else None)
     return ImageLinearFit(data, psf, J.LensModel(c["lens"]),
                           J.LightModel(c["src"], deflection_scaling_list=c["dsl"]),
                           J.LightModel(c["ll"]), point_source_class=pcls,
@@ -46,9 +47,12 @@ def test_linear_fit_matches_reference(cuda, case):
     # the amplitudes are written into the kwargs, as the reference does
     assert ks[0]["amp"] == param[0]
     if kps:
-        # point_amp written back too, sources and lens light first
+        # point_amp (or source_amp with fixed magnification) written back too
         n_ext = len(case["src"]) + len(case["ll"])
-        np.testing.assert_array_equal(kps[0]["point_amp"], param[n_ext:n_ext + 4])
+        if case.get("ps_fixed"):
+            assert kps[0]["source_amp"] == param[n_ext]
+        else:
+            np.testing.assert_array_equal(kps[0]["point_amp"], param[n_ext:n_ext + 4])
     kl, ks, kll, kps = (copy.deepcopy(case.get(k) or []) for k in ("kl", "ks", "kll", "ps"))
     model, err, cov, p2 = im.image_linear_solve(kl, ks, kll, kps, inv_bool=case["marg"])
     np.testing.assert_array_equal(p2, param)
@@ -57,7 +61,8 @@ def test_linear_fit_matches_reference(cuda, case):
     if case["cov"] is not None:
         np.testing.assert_allclose(cov, case["cov"], rtol=1e-9, atol=1e-14)
     A = im.linear_response_matrix(kl, ks, kll, kps)
-    n_ps = sum(len(p["ra_image"]) for p in (case.get("ps") or []))
+    n_ps = (1 if case.get("ps_fixed") else
+            sum(len(p["ra_image"]) for p in (case.get("ps") or [])))
     assert A.shape == (len(case["src"]) + len(case["ll"]) + n_ps, int(np.sum(case["mask"])))
 
 

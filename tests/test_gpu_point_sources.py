@@ -28,7 +28,9 @@ def _model(case, precision="fp64"):
                **(case.get("numerics") or {}))
     return J.ImageModel(data, J.PSF(**pk), J.LensModel(["EPL", "SHEAR"]),
                         J.LightModel(["SERSIC_ELLIPSE"]), J.LightModel(["SERSIC"]),
-                        point_source_class=J.PointSource(["LENSED_POSITION", "UNLENSED"]),
+                        point_source_class=J.PointSource(
+                            ["LENSED_POSITION", "UNLENSED"],
+                            fixed_magnification_list=case.get("fixed")),
                         kwargs_numerics=num)
 
 
@@ -87,8 +89,6 @@ def test_point_source_options_raise(cuda):
     data = J.ImageData(case["data"], exposure_time=800.0, background_rms=0.01, **g)
     with pytest.raises(ValueError):
         J.PointSource(["SOURCE_POSITION"])
-    with pytest.raises(ValueError):
-        J.PointSource(["LENSED_POSITION"], fixed_magnification_list=[True])
     with pytest.raises(ValueError):
         J.PointSource(["UNLENSED"], save_cache=True)
     with pytest.raises(ValueError):

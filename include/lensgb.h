@@ -353,12 +353,14 @@ int lensgb_alpha(const lensgb_model* model, const double* params_dev, const doub
                  void* stream);
 
 /* LensModel.hessian (jaxtronomy/LensModel/lens_model.py:384-414 ->
- * single_plane.py:142-180) of the model's lens profiles at n points, FP64:
- * out_dev receives f_xx, f_xy, f_yx, f_yy as four consecutive arrays of n
+ * single_plane.py:142-180) of the model's lens profiles, FP64, for n_inst
+ * parameter rows with n points each (x_dev, y_dev: n_inst x n): out_dev
+ * receives f_xx, f_xy, f_yx, f_yy as four consecutive arrays of n_inst x n
  * doubles (times alpha_scaling).  EPL, SIE, NIE, NFW, TNFW, SHEAR and
  * CONVERGENCE only (LENSGB_ERR_UNSUPPORTED otherwise). */
-int lensgb_hessian(const lensgb_model* model, const double* params_dev, const double* x_dev,
-                   const double* y_dev, double* out_dev, long long n, void* stream);
+int lensgb_hessian(const lensgb_model* model, const double* params_dev, int n_inst,
+                   const double* x_dev, const double* y_dev, double* out_dev, long long n,
+                   void* stream);
 
 /* LightModel.surface_brightness of the model's source (which = 0) or lens
  * light (which = 1) profiles over n arbitrary points (light_model_base.py:230-252),

@@ -237,7 +237,7 @@ def load():
     lib.lensgb_loglike_image.restype = i
     lib.lensgb_point_sources_add.argtypes = [vp, dp, i, i, dp, i, ll, i, vp, vp]
     lib.lensgb_point_sources_add.restype = i
-    lib.lensgb_hessian.argtypes = [vp, dp, dp, dp, dp, ll, vp]
+    lib.lensgb_hessian.argtypes = [vp, dp, i, dp, dp, dp, ll, vp]
     lib.lensgb_hessian.restype = i
     lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]
     lib.lensgb_server_create.restype = i

@@ -249,7 +249,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 114; }
+int lensgb_version(void) { return 115; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -1264,26 +1264,26 @@ int lensgb_alpha(const lensgb_model* m, const double* params, const double* x, c
     return ray_points(m, params, x, y, ax, ay, n, 1, stream);
 }
 
-int lensgb_hessian(const lensgb_model* mc, const double* params, const double* x,
+int lensgb_hessian(const lensgb_model* mc, const double* params, int n_inst, const double* x,
                    const double* y, double* out, long long n, void* stream) {
     lensgb_model* m = const_cast<lensgb_model*>(mc);
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
-    if (n < 0) return fail(LENSGB_ERR_INVALID, "negative point count");
-    if (n == 0) return LENSGB_OK;
+    if (n < 0 || n_inst < 0) return fail(LENSGB_ERR_INVALID, "negative point or system count");
+    if (n == 0 || n_inst == 0) return LENSGB_OK;
     if (!x || !y || !out) return fail(LENSGB_ERR_INVALID, "null coordinate pointer");
     if (!params && m->st.n_lens > 0) return fail(LENSGB_ERR_INVALID, "null params pointer");
     if (!hessian_supported(m->st))
         return fail(LENSGB_ERR_UNSUPPORTED, "exact Hessians exist for EPL, SIE, NIE, NFW, TNFW, "
                                             "SHEAR and CONVERGENCE lenses");
-    int rc = ensure_scratch(m, 1);
+    int rc = ensure_scratch(m, n_inst);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     StackDesc st = m->st;
     st.n_src = 0;
     st.n_ll = 0;
-    launch_prepare(m->grid, st, params, 1, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
+    launch_prepare(m->grid, st, params, n_inst, m->rec_d, m->rec_f, m->coef_d, m->coef_f, s);
     if ((rc = check_cuda("prepare launch"))) return rc;
-    launch_hessian_points(st, m->rec_d, m->coef_d, params, x, y, out, n, s);
+    launch_hessian_points(st, m->rec_d, m->coef_d, params, x, y, out, n * n_inst, n, s);
     return check_cuda("hessian launch");
 }
 

@@ -724,20 +724,24 @@ int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, cons
 // f_xx, f_xy, f_yx, f_yy of the lens stack at n points, the derivatives of each
 // profile's deflection with respect to the ray position taken from the same
 // dual-number evaluation as the adjoint (the centre derivatives, negated), times
-// alpha_scaling.  One thread per point; out holds the four components as four
-// consecutive arrays of n.
+// alpha_scaling.  One thread per point; n_per points per system (parameter
+// row); out holds the four components as four consecutive arrays of n.
 __global__ void hessian_points_kernel(StackDesc st, const double* __restrict__ rec,
                                       const double* __restrict__ coef,
-                                      const double* __restrict__ P, const double* __restrict__ x,
-                                      const double* __restrict__ y, double* __restrict__ out,
-                                      long long n) {
+                                      const double* __restrict__ params,
+                                      const double* __restrict__ x, const double* __restrict__ y,
+                                      double* __restrict__ out, long long n, long long n_per) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const long long inst = i / n_per;
     const double X = x[i], Y = y[i];
+    const double* P = params + inst * st.n_params;
+    const double* rec_i = rec + inst * st.n_lens * REC_D;
+    const double* coef_i = coef ? coef + inst * st.n_epl * EPL_NMAX : nullptr;
     double h[4] = {0.0, 0.0, 0.0, 0.0};
     for (int p = 0; p < st.n_lens; ++p) {
         const int code = st.lens[p];
-        const double* r = rec + p * REC_D;
+        const double* r = rec_i + p * REC_D;
         const double* a = P + st.lens_off[p];
         const double dx = X - r[RD_CX], dy = Y - r[RD_CY];
         if (code == LENSGB_LENS_CONVERGENCE) {
@@ -750,7 +754,7 @@ __global__ void hessian_points_kernel(StackDesc st, const double* __restrict__ r
         if (code == LENSGB_LENS_EPL) {
             // dF/dt enters only the t direction of the duals: the coefficient table
             // stands in for it
-            const double* F = coef + st.epl_slot[p] * EPL_NMAX;
+            const double* F = coef_i + st.epl_slot[p] * EPL_NMAX;
             epl_alpha_grad(r, F, F, a, dx, dy, ax, ay, J);
             co = 4;
         } else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
@@ -779,11 +783,11 @@ bool hessian_supported(const StackDesc& st) {
 
 int launch_hessian_points(const StackDesc& st, const double* rec, const double* coef,
                           const double* params, const double* x, const double* y, double* out,
-                          long long n, cudaStream_t stream) {
-    if (n <= 0) return 0;
+                          long long n, long long n_per, cudaStream_t stream) {
+    if (n <= 0 || n_per <= 0) return 0;
     const int threads = 128;
     hessian_points_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(
-        st, rec, coef, params, x, y, out, n);
+        st, rec, coef, params, x, y, out, n, n_per);
     return 0;
 }
 

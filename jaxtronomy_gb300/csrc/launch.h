@@ -183,7 +183,7 @@ int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* r
 bool hessian_supported(const StackDesc& st);
 int launch_hessian_points(const StackDesc& st, const double* rec, const double* coef,
                           const double* params, const double* x, const double* y, double* out,
-                          long long n, cudaStream_t stream);
+                          long long n, long long n_per, cudaStream_t stream);
 // Point-source rendering: adds to out (n_inst images of rows x cols, model
 // precision) the n_img images (ra, dec, amp) of each system, the kernel
 // (ks x ks doubles; kstride per system, 0: shared) at subgrid factor p.

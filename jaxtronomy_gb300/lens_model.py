@@ -143,9 +143,34 @@ class LensModel:
             m = self._model(idx)
             p = _device.to_device_f64(self._row(idx, kwargs))
             _lib.check(_lib.load().lensgb_hessian(
-                m.handle, _device.ptr(p), _device.ptr(xt), _device.ptr(yt), _device.ptr(out),
+                m.handle, _device.ptr(p), 1, _device.ptr(xt), _device.ptr(yt), _device.ptr(out),
                 xt.numel(), _device.stream_handle()))
         return tuple(_as_out(out[c].reshape(shape), x) for c in range(4))
+
+    def hessian_batch(self, x, y, kwargs):
+        """Exact Hessians of B systems in one launch: kwargs values of length B (or
+        scalars), x and y of shape (B, n); returns four (B, n) arrays."""
+        _device.require_cuda()
+        idx = self._select(None)
+        xa = np.asarray(x, dtype=float)
+        ya = np.asarray(y, dtype=float)
+        if xa.ndim != 2 or xa.shape != ya.shape:
+            raise ValueError("x and y must have shape (B, n)")
+        B, n = xa.shape
+        names = [self.lens_model_list[i] for i in idx]
+        rows = np.zeros((B, profiles.n_params(names, profiles.LENS_PARAMS)))
+        profiles.pack(names, profiles.LENS_PARAMS, [kwargs[i] for i in idx], rows, 0, "Lens")
+        out = torch.zeros((4, B * n), dtype=torch.float64, device="cuda")
+        if len(idx):
+            m = self._model(idx)
+            p = _device.to_device_f64(rows)
+            xt = _device.to_device_f64(xa).reshape(-1)
+            yt = _device.to_device_f64(ya).reshape(-1)
+            _lib.check(_lib.load().lensgb_hessian(
+                m.handle, _device.ptr(p), B, _device.ptr(xt), _device.ptr(yt), _device.ptr(out),
+                n, _device.stream_handle()))
+        o = out.reshape(4, B, n).cpu().numpy()
+        return o[0], o[1], o[2], o[3]
 
     def _hessian_differential_cross(self, x, y, kwargs, k=None, diff=0.00001):
         ax_dx, ay_dx = self.alpha(x + diff / 2, y, kwargs, k=k)

@@ -101,13 +101,9 @@ class PointSource:
             return np.abs(np.asarray(self._lens_model.magnification(ra, dec, kwargs_lens)))
         ra2 = np.broadcast_to(np.atleast_2d(ra), (B, ra.shape[-1]))
         dec2 = np.broadcast_to(np.atleast_2d(dec), (B, dec.shape[-1]))
-        out = np.empty(ra2.shape)
-        for b in range(B):
-            kl = [{key: (np.asarray(v).reshape(-1)[b] if np.size(v) > 1 else
-                         float(np.asarray(v).reshape(-1)[0])) for key, v in kw.items()}
-                  for kw in kwargs_lens]
-            out[b] = np.abs(np.asarray(self._lens_model.magnification(ra2[b], dec2[b], kl)))
-        return out
+        # one Hessian launch for the batch (lensgb_hessian with B parameter rows)
+        f_xx, f_xy, f_yx, f_yy = self._lens_model.hessian_batch(ra2, dec2, kwargs_lens)
+        return np.abs(1.0 / ((1 - f_xx) * (1 - f_yy) - f_xy * f_yx))
 
     def image_amplitude(self, kwargs_ps, kwargs_lens=None, k=None):
         """``point_source.py:304-326``: per model, the image amplitudes (zeros where

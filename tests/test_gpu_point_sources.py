@@ -100,3 +100,20 @@ def test_point_source_options_raise(cuda):
         im.image(case["lens"], case["src"], case["ll"], None)
     with pytest.raises(ValueError):
         im.likelihood_grad_batch(case["lens"], case["src"], case["ll"])
+
+
+def test_fixed_magnification_batch_equals_single(cuda):
+    """Batched lens kwargs with fixed-magnification point sources: one Hessian launch
+    for the batch gives each system its own magnifications."""
+    case = [c for c in golden_io.point_source_cases() if c["tag"] == "fixed_magnification"][0]
+    im = _model(case)
+    B = 3
+    lens = [{k: np.full(B, v) * (1 + 0.01 * np.arange(B)) if k == "theta_E" else np.full(B, v)
+             for k, v in kw.items()} for kw in case["lens"]]
+    src = [{k: np.full(B, v) for k, v in kw.items()} for kw in case["src"]]
+    ll = [{k: np.full(B, v) for k, v in kw.items()} for kw in case["ll"]]
+    batch = im.image_batch(lens, src, ll, kwargs_ps=case["ps"]).cpu().numpy()
+    for b in range(B):
+        one = im.image([{k: float(v[b]) for k, v in kw.items()} for kw in lens], case["src"],
+                       case["ll"], case["ps"])
+        np.testing.assert_allclose(batch[b], one, rtol=1e-13, atol=1e-13 * np.abs(one).max())

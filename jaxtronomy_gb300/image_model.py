@@ -471,7 +471,10 @@ class ImageModel:
         kstride = 0
         if unconvolved:
             kern = _delta_kernel()
-        elif psf_kernels is not None and self._ps_sub == 1 and self._psf_type == _lib.PSF_PIXEL:
+        elif (psf_kernels is not None and self._ps_sub == 1 and self._psf_type == _lib.PSF_PIXEL
+              and not self._ssc):
+            # per-system pixel-scale kernels (supersampled ones, of a model convolving on
+            # the supersampled grid, are not the rendering kernel)
             kern = psf_kernels.cpu().numpy() if isinstance(psf_kernels, torch.Tensor) \
                 else np.asarray(psf_kernels, dtype=float)
             if kern.ndim == 3 and kern.shape[0] > 1:

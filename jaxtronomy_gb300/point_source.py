@@ -63,9 +63,9 @@ class PointSource:
     def _check(self, kwargs_ps):
         if len(kwargs_ps) != len(self.point_source_type_list):
             raise ValueError("kwargs_ps needs one dict per point-source model")
-        for i, kw in enumerate(kwargs_ps):
+        for i in range(len(kwargs_ps)):
             if self.point_source_type_list[i] == "LENSED_POSITION" and \
-                    (self._additional_images_list[i] or kw.get("additional_images", False)):
+                    self._additional_images_list[i]:
                 raise ValueError("additional images not supported in jaxtronomy")
 
     def image_position(self, kwargs_ps, kwargs_lens=None, k=None, original_position=False,

@@ -131,7 +131,8 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
 // (alpha, x): x += alpha T_ij[i]; alpha -= r2p[i] alpha_i(x / T_z[i]);
 // beta = x / T_z[last].
 //
-// FP64 follows that recurrence step by step.  FP32_SPLIT writes it as
+// FP64 follows that recurrence step by step (x / T_z as x times a per-step
+// 1 / T_z).  FP32_SPLIT writes it as
 //   alpha = theta - v,  x = theta T_cum - d,
 //   v += r2p_i alpha_i,  d += v T_ij[i]  (T_cum = running sum of T_ij),
 // so that the ray state is the small deflection v and the displacement d,
@@ -314,14 +315,15 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                     xs[1][k] += al[1][k] * dt;
                 }
                 if (code == LENSGB_LENS_NULL) continue;
-                const double tz = Tz[g], r = r2p[g];
+                // x / T_z as x * (1 / T_z): within an ulp of the division
+                const double itz = eps_d[g], r = r2p[g];
                 const double* rd = rec_d + g * REC_D;
                 const double* cd = coef_d ? coef_d + g * EPL_NMAX : nullptr;
 #pragma unroll
                 for (int k = 0; k < MP_RPT; ++k) {
                     double ax, ay;
-                    lens_deflect<double>(code, rd, cd, xs[0][k] / tz - rd[RD_CX],
-                                         xs[1][k] / tz - rd[RD_CY], ax, ay);
+                    lens_deflect<double>(code, rd, cd, xs[0][k] * itz - rd[RD_CX],
+                                         xs[1][k] * itz - rd[RD_CY], ax, ay);
                     al[0][k] -= ax * r;
                     al[1][k] -= ay * r;
                 }
@@ -466,6 +468,12 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
     }
 }
 
+// FP64 multi-plane: 1 / T_z per step (into the eps_d scratch, unused in FP64).
+__global__ void inv_tz_kernel(const double* __restrict__ Tz, int n, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = 1.0 / Tz[i];
+}
+
 int launch_multi_plane(int* tag, const double* rec_d, const float* rec_f, const double* coef_d,
                        const float* coef_f, float* pl_f, double* eps_d, const double* dT,
                        const double* Tz, const double* r2p, int n_steps, const double* ax,
@@ -482,10 +490,12 @@ int launch_multi_plane(int* tag, const double* rec_d, const float* rec_f, const 
         multi_plane_kernel<true><<<(unsigned)blocks, MP_THREADS, 0, stream>>>(
             tag, rec_d, rec_f, coef_d, coef_f, pl_f, eps_d, dT, Tz, r2p, n_steps, ax, ay, bx, by,
             n);
-    else
+    else {
+        inv_tz_kernel<<<(n_steps + 255) / 256, 256, 0, stream>>>(Tz, n_steps, eps_d);
         multi_plane_kernel<false><<<(unsigned)blocks, MP_THREADS, 0, stream>>>(
             tag, rec_d, rec_f, coef_d, coef_f, pl_f, eps_d, dT, Tz, r2p, n_steps, ax, ay, bx, by,
             n);
+    }
     return 0;
 }
 

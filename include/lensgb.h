@@ -234,7 +234,13 @@ int lensgb_image_mixed(lensgb_model* model, const double* params_dev, int n_inst
  * XLA has already reserved most of the GPU's memory for its own pool, so a
  * cudaMalloc can fail, and cudaFree would synchronize the device under XLA.
  *
- * Same arguments and results as lensgb_image.  The device scratch (profile
+ * Same arguments and results as lensgb_image, for every model except two
+ * kinds, which it refuses with LENSGB_ERR_UNSUPPORTED (their extra image
+ * buffers are not part of the fixed array): models that convolve on the
+ * supersampled grid (kwargs_numerics supersampling_convolution=True with
+ * s > 1), unless the call passes LENSGB_UNCONVOLVED, which skips that
+ * convolution and works; and sub-frame models (lensgb_model_set_subframe,
+ * kwargs_numerics flux_evaluate_indexes).  The device scratch (profile
  * records, EPL tables, un-convolved images) comes from a fixed array of
  * LENSGB_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads
  * the library holds until exit.  A call whose scratch would exceed it returns

@@ -17,6 +17,13 @@ import torch
 class LogLikelihood(torch.autograd.Function):
     @staticmethod
     def forward(ctx, rows, image_model, data=None, psf_kernels=None):
+        if not ctx.needs_input_grad[0]:
+            # no gradient wanted (torch.no_grad(), or rows without requires_grad):
+            # the forward likelihood alone, without the adjoint pass
+            ctx.save_for_backward(None)
+            logl = image_model.likelihood_batch(rows=rows.detach(), data=data,
+                                                psf_kernels=psf_kernels)
+            return logl.to(rows.device)
         logl, grad = image_model.likelihood_grad_batch(rows=rows.detach(), data=data,
                                                        psf_kernels=psf_kernels)
         ctx.save_for_backward(grad)
@@ -25,6 +32,8 @@ class LogLikelihood(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_output):
         (grad,) = ctx.saved_tensors
+        if grad is None:
+            return None, None, None, None
         g = grad_output.to(grad.device, grad.dtype)[:, None] * grad
         return g, None, None, None
 

@@ -1339,7 +1339,7 @@ struct lensgb_bulk {
     double* coef_d = nullptr;
     float* coef_f = nullptr;
     float* pl_f = nullptr;    // multi-plane step table (8 floats per step)
-    double* eps_d = nullptr;  // multi-plane T_cum / T_z - 1 per step
+    double* eps_d = nullptr;  // multi-plane, per step: FP32 T_cum / T_z - 1; FP64 1 / T_z (inv_tz_kernel)
 };
 
 static void bulk_free(lensgb_bulk* b) {

@@ -8,7 +8,10 @@ value stored here, in FP64.
 
 Usage (needs the reference source tree; the output files are committed):
 
-    python tests/golden/make_golden.py /path/to/jaxtronomy-source
+    python tests/golden/make_golden.py /path/to/jaxtronomy-source [file ...]
+
+or with the source tree in the environment variable ``JAXTRONOMY_SOURCE``.
+Naming files (e.g. ``serving_scenes.npz``) regenerates only those.
 
 Outputs (all .npz, metadata as a JSON string under key ``meta``):
   profiles.npz  per-profile deflections / surface brightness at seeded points
@@ -18,6 +21,10 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
   multiplane.npz LensModelBulk (multi-plane): prepared kwargs and ray shooting
   point_sources.npz ImageModel with LENSED_POSITION / UNLENSED point sources
   linear.npz    ImageLinearFit: linear amplitude solve, model image, logL
+  serving_scenes.npz ImageModel.image of the four serving lens stacks with two
+                sources at 100x100, supersampling 4, a 41x41 Moffat kernel
+  grad_fd.npz   central differences of likelihood_data_given_model (the
+                reference's own likelihood) on gradient-workload scenes
 """
 
 import json
@@ -635,12 +642,181 @@ def gen_linear():
     return out
 
 
+def gen_serving_scenes():
+    """ImageModel.image of the four serving lens stacks, each with two
+    SERSIC_ELLIPSE sources and a SERSIC_ELLIPSE lens light, drawn by the serving
+    stream's generator and rendered at its largest supersampling factor and PSF
+    (100x100 at 0.05"/pix, s = 4, a 41x41 Moffat kernel)."""
+    from jaxtronomy_gb300 import workloads as W
+
+    reqs, psfs = W.serving_stream(seed=1002, n=400)
+    scenes = []
+    for stack in W.SERVING_STACKS:
+        r = next(q for q in reqs if q["key"][3] == stack and q["key"][4] == 2)
+        kern = psfs[41][r["psf"]]
+        lens = stack.split("+")
+        src = ["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"]
+        ll = ["SERSIC_ELLIPSE"]
+        im = _image_model(100, 0.05, 4, {"psf_type": "PIXEL", "kernel_point_source": kern},
+                          lens, src, ll)
+        kl, ks, kll = r["kwargs_lens"], r["kwargs_source"], r["kwargs_lens_light"]
+        scenes.append({"tag": stack, "num_pix": 100, "delta_pix": 0.05, "s": 4,
+                       "psf_type": "PIXEL", "kernel": kern, "lens": lens, "src": src, "ll": ll,
+                       "kwargs_lens": kl, "kwargs_source": ks, "kwargs_lens_light": kll,
+                       "image": np.asarray(im.image(kl, ks, kll))})
+    return scenes
+
+
+def _rows_order(lens, src, ll):
+    """(list index, profile index, parameter name) in the row layout of
+    ImageModel.pack_params: lens, source, lens-light profiles in order, each
+    profile's parameters in param_names order."""
+    from jaxtronomy_gb300 import profiles as P
+
+    out = []
+    for li, (names, table) in enumerate(((lens, P.LENS_PARAMS), (src, P.LIGHT_PARAMS),
+                                         (ll, P.LIGHT_PARAMS))):
+        for pi, n in enumerate(names):
+            out += [(li, pi, k) for k in table[n]]
+    return out
+
+
+def gen_grad_fd():
+    """Finite differences of the reference's likelihood_data_given_model
+    (image_model.py:163-221) with respect to every parameter, in the row order of
+    ImageModel.pack_params: a five-point stencil (step 1e-4, truncation ~1e-13
+    relative) and the central difference with step 1e-6 of the gradient workload.
+    Data are the reference's own image at parameters 1 % off in theta_E (or Rs),
+    plus seeded Gaussian and Poisson noise."""
+    import copy
+
+    from jaxtronomy_gb300 import workloads as W
+
+    scenes = []
+    # the gradient workload's first system: 120x120, s = 2, 21x21 Moffat
+    model, lens, src, ll, kern = W.gradient_batch(seed=1003, batch=1)
+    scenes.append({"tag": "epl_shear_120_s2_psf21", "num_pix": 120, "delta_pix": 0.05, "s": 2,
+                   "psf": {"psf_type": "PIXEL", "kernel_point_source": kern[0]},
+                   "lens": model["lens_model_list"], "src": model["source_light_model_list"],
+                   "ll": model["lens_light_model_list"], "kwargs_lens": W.instance(lens, 0),
+                   "kwargs_source": W.instance(src, 0), "kwargs_lens_light": W.instance(ll, 0)})
+    ks1 = [{"amp": 40.0, "R_sersic": 0.3, "n_sersic": 2.2, "e1": 0.06, "e2": -0.04,
+            "center_x": 0.03, "center_y": 0.02}]
+    ks2 = ks1 + [{"amp": 15.0, "R_sersic": 0.2, "n_sersic": 1.5, "e1": -0.05, "e2": 0.08,
+                  "center_x": -0.12, "center_y": 0.07}]
+    kll = [{"amp": 30.0, "R_sersic": 0.8, "n_sersic": 3.0, "e1": 0.05, "e2": 0.02,
+            "center_x": 0.01, "center_y": -0.01}]
+    moffat = W.moffat_pixel_kernel(0.12, 3.0, 0.06, 11)
+    scenes.append({"tag": "nfw_cse_gaussian_psf", "num_pix": 40, "delta_pix": 0.06, "s": 2,
+                   "psf": {"psf_type": "GAUSSIAN", "fwhm": 0.15, "truncation": 3.0},
+                   "lens": ["NFW_ELLIPSE_CSE", "SHEAR"], "src": ["SERSIC_ELLIPSE"],
+                   "ll": ["SERSIC_ELLIPSE"],
+                   "kwargs_lens": [{"Rs": 9.0, "alpha_Rs": 1.4, "e1": 0.12, "e2": -0.07,
+                                    "center_x": 0.02, "center_y": -0.01},
+                                   {"gamma1": 0.02, "gamma2": -0.03, "ra_0": 0.0,
+                                    "dec_0": 0.0}],
+                   "kwargs_source": ks1, "kwargs_lens_light": kll})
+    scenes.append({"tag": "multipole_two_sources", "num_pix": 40, "delta_pix": 0.06, "s": 2,
+                   "psf": {"psf_type": "PIXEL", "kernel_point_source": moffat},
+                   "lens": ["EPL_MULTIPOLE_M1M3M4", "SHEAR"],
+                   "src": ["SERSIC_ELLIPSE", "SERSIC_ELLIPSE"], "ll": ["SERSIC_ELLIPSE"],
+                   "kwargs_lens": [{"theta_E": 1.05, "gamma": 2.08, "e1": 0.1, "e2": -0.05,
+                                    "center_x": 0.02, "center_y": 0.01, "a1_a": 0.01,
+                                    "delta_phi_m1": 0.5, "a3_a": -0.012,
+                                    "delta_phi_m3": 1.9, "a4_a": 0.009, "delta_phi_m4": 0.8},
+                                   {"gamma1": -0.01, "gamma2": 0.03, "ra_0": 0.0,
+                                    "dec_0": 0.0}],
+                   "kwargs_source": ks2, "kwargs_lens_light": kll})
+    scenes.append({"tag": "sie_convergence_no_psf", "num_pix": 32, "delta_pix": 0.07, "s": 3,
+                   "psf": {"psf_type": "NONE"},
+                   "lens": ["SIE", "CONVERGENCE", "SHEAR"], "src": ["SERSIC_ELLIPSE"],
+                   "ll": ["SERSIC_ELLIPSE"],
+                   "kwargs_lens": [{"theta_E": 0.95, "e1": -0.08, "e2": 0.11,
+                                    "center_x": -0.02, "center_y": 0.03},
+                                   {"kappa": 0.04, "ra_0": 0.1, "dec_0": -0.05},
+                                   {"gamma1": 0.03, "gamma2": 0.01, "ra_0": 0.0,
+                                    "dec_0": 0.0}],
+                   "kwargs_source": ks1, "kwargs_lens_light": kll})
+    k_super = W.moffat_pixel_kernel(0.12, 3.0, 0.06 / 3, 27)
+    scenes.append({"tag": "epl_supersampled_convolution", "num_pix": 30, "delta_pix": 0.06,
+                   "s": 3, "psf": {"psf_type": "PIXEL", "kernel_point_source": k_super,
+                                   "point_source_supersampling_factor": 3},
+                   "numerics": {"supersampling_convolution": True,
+                                "supersampling_kernel_size": 3},
+                   "lens": ["EPL", "SHEAR"], "src": ["SERSIC_ELLIPSE"], "ll": ["SERSIC_ELLIPSE"],
+                   "kwargs_lens": [{"theta_E": 1.0, "gamma": 1.95, "e1": -0.06, "e2": 0.09,
+                                    "center_x": 0.0, "center_y": 0.02},
+                                   {"gamma1": 0.02, "gamma2": 0.02, "ra_0": 0.0,
+                                    "dec_0": 0.0}],
+                   "kwargs_source": ks1, "kwargs_lens_light": kll})
+    scenes.append({"tag": "epl_gaussian_supersampled_convolution", "num_pix": 28,
+                   "delta_pix": 0.07, "s": 2,
+                   "psf": {"psf_type": "GAUSSIAN", "fwhm": 0.16, "truncation": 3.0},
+                   "numerics": {"supersampling_convolution": True},
+                   "lens": ["EPL", "SHEAR"], "src": ["SERSIC_ELLIPSE"], "ll": ["SERSIC_ELLIPSE"],
+                   "kwargs_lens": [{"theta_E": 0.9, "gamma": 2.12, "e1": 0.07, "e2": 0.03,
+                                    "center_x": -0.01, "center_y": 0.0},
+                                   {"gamma1": -0.02, "gamma2": 0.01, "ra_0": 0.0,
+                                    "dec_0": 0.0}],
+                   "kwargs_source": ks1, "kwargs_lens_light": kll})
+
+    out = []
+    for i, sc in enumerate(scenes):
+        kl, ks, kl2 = sc["kwargs_lens"], sc["kwargs_source"], sc["kwargs_lens_light"]
+        # simulated data: the reference's image at parameters 1 % off, plus noise
+        truth = copy.deepcopy(kl)
+        main = "theta_E" if "theta_E" in truth[0] else "Rs"
+        truth[0][main] *= 1.01
+        im0 = _image_model(sc["num_pix"], sc["delta_pix"], sc["s"], sc["psf"], sc["lens"],
+                           sc["src"], sc["ll"], numerics=sc.get("numerics"))
+        clean = np.asarray(im0.image(truth, ks, kl2))
+        data = W.noisy_data(clean[None], seed=3000 + i)[0]
+        im = _image_model(sc["num_pix"], sc["delta_pix"], sc["s"], sc["psf"], sc["lens"],
+                          sc["src"], sc["ll"], data=data, numerics=sc.get("numerics"))
+        order = _rows_order(sc["lens"], sc["src"], sc["ll"])
+        lists = [kl, ks, kl2]
+
+        def logl(li, pi, name, delta):
+            kw = copy.deepcopy(lists)
+            kw[li][pi][name] = kw[li][pi][name] + delta
+            return float(np.asarray(im.likelihood_data_given_model(kw[0], kw[1], kw[2])))
+
+        g5, g2 = [], []
+        for li, pi, name in order:
+            lists[li][pi].setdefault(name, 0.0)
+        for li, pi, name in order:
+            h = 1e-4
+            f = [logl(li, pi, name, d * h) for d in (-2, -1, 1, 2)]
+            g5.append((f[0] - 8 * f[1] + 8 * f[2] - f[3]) / (12 * h))
+            g2.append((logl(li, pi, name, 1e-6) - logl(li, pi, name, -1e-6)) / 2e-6)
+        logl0 = float(np.asarray(im.likelihood_data_given_model(kl, ks, kl2)))
+        rec = {k: v for k, v in sc.items() if k != "psf"}
+        psf = dict(sc["psf"])
+        rec["kernel"] = psf.pop("kernel_point_source", None)
+        rec["psf_kwargs"] = psf
+        rec.update({"data": data, "logL": logl0, "grad_5pt": np.array(g5),
+                    "grad_central_1e-6": np.array(g2),
+                    "param_order": [[li, pi, n] for li, pi, n in order]})
+        out.append(rec)
+        print("grad_fd", sc["tag"], "logL", logl0, "params", len(order))
+    return out
+
+
 def _save(path, arrays, meta):
     np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
 
 
-def main(reference_root):
+def main(reference_root, only=None):
     refshim.install(reference_root)
+    if only:
+        for name in only:
+            if name not in EXTRA:
+                raise SystemExit("unknown golden file %s (choose from %s)"
+                                 % (name, ", ".join(sorted(EXTRA))))
+            EXTRA[name]()
+        return
+    for fn in EXTRA.values():
+        fn()
     rng = np.random.default_rng(20240601)
     cases = gen_profiles(rng)
     arrays, meta = {}, []
@@ -703,5 +879,33 @@ def main(reference_root):
           "bulk cases,", len(mp), "multi-plane cases,", len(lin), "linear-solve cases")
 
 
+def write_serving_scenes():
+    arrays, meta = {}, []
+    for i, sc in enumerate(gen_serving_scenes()):
+        arrays["image_%d" % i] = sc.pop("image")
+        arrays["kernel_%d" % i] = sc.pop("kernel")
+        meta.append(sc)
+    _save(os.path.join(HERE, "serving_scenes.npz"), arrays, meta)
+
+
+def write_grad_fd():
+    arrays, meta = {}, []
+    for i, sc in enumerate(gen_grad_fd()):
+        for k in ("data", "kernel", "grad_5pt", "grad_central_1e-6"):
+            v = sc.pop(k)
+            if v is not None:
+                arrays["%s_%d" % (k, i)] = np.asarray(v)
+        meta.append(sc)
+    _save(os.path.join(HERE, "grad_fd.npz"), arrays, meta)
+
+
+# golden files that can be regenerated one at a time
+EXTRA = {"serving_scenes.npz": write_serving_scenes, "grad_fd.npz": write_grad_fd}
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("JAXTRONOMY_SOURCE")
+    if not root:
+        raise SystemExit("usage: make_golden.py <jaxtronomy source tree> [file ...] "
+                         "(or set JAXTRONOMY_SOURCE)")
+    main(root, sys.argv[2:])

@@ -147,3 +147,31 @@ def linear_scene(c):
         sc["fwhm"] = c["psf"]["fwhm"]
         sc["truncation"] = c["psf"]["truncation"]
     return sc
+
+
+def serving_scenes():
+    """The four serving lens stacks with two sources at 100x100, s = 4, 41x41
+    kernel: the reference's image per scene (tag = lens stack)."""
+    d, meta = load("serving_scenes.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        c["image"] = d["image_%d" % i]
+        c["kernel"] = d["kernel_%d" % i]
+        out.append(c)
+    return out
+
+
+def grad_fd_cases():
+    """Finite-difference gradients of the reference's likelihood (grad_fd.npz):
+    scene, data, PSF, the five-point and the step-1e-6 central differences in
+    the row order of ImageModel.pack_params."""
+    d, meta = load("grad_fd.npz")
+    out = []
+    for i, m in enumerate(meta):
+        c = dict(m)
+        for k in ("data", "kernel", "grad_5pt", "grad_central_1e-6"):
+            key = "%s_%d" % (k, i)
+            c[k] = d[key] if key in d.files else None
+        out.append(c)
+    return out

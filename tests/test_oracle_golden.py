@@ -58,6 +58,15 @@ def test_images_match_reference(sc):
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("sc", golden_io.serving_scenes(), ids=lambda s: s["tag"])
+def test_serving_scenes_match_reference(sc):
+    """The four serving stacks with two sources at s = 4 and a 41x41 kernel."""
+    scene = golden_io.oracle_scene(sc)
+    got = image.image(scene, sc["kwargs_lens"], sc["kwargs_source"], sc["kwargs_lens_light"])
+    ref = sc["image"]
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * np.abs(ref).max())
+
+
 def test_likelihood_matches_reference():
     scenes, like = golden_io.image_scenes()
     sc = [s for s in scenes if s["tag"] == like["scene"]][0]

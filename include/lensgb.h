@@ -339,8 +339,11 @@ int lensgb_loglike(lensgb_model* model, const double* params_dev, int n_inst,
  * returns for the kwargs (test_image_model.py:274-335) -- by a hand-written
  * adjoint that recomputes the ray grid.  Same arguments as lensgb_loglike plus
  * grad_dev: n_inst x param_count doubles, row layout.  FP64 models only; lens
- * stacks of EPL, SIE, NIE, NFW, TNFW and SHEAR, SERSIC / SERSIC_ELLIPSE light,
- * PSF NONE or PIXEL. */
+ * stacks of EPL, EPL_MULTIPOLE_M1M3M4, SIE, NIE, NFW, TNFW, NFW_ELLIPSE_CSE,
+ * CONVERGENCE and SHEAR, SERSIC / SERSIC_ELLIPSE light, at most 64 parameters
+ * per row; every PSF type (NONE, PIXEL, GAUSSIAN with its edge padding),
+ * convolution on the pixel or on the supersampled grid (with or without a
+ * split kernel), and sub-frame models (flux_evaluate_indexes). */
 int lensgb_loglike_grad(lensgb_model* model, const double* params_dev, int n_inst,
                         const void* psf_dev, long long psf_stride, const lensgb_noise_desc* noise,
                         void* image_out_dev, double* logl_dev, double* grad_dev, void* stream);
@@ -529,6 +532,17 @@ int lensgb_server_destroy(lensgb_server* server);
 
 /* Description of the last error on the calling thread ("" if none). */
 const char* lensgb_last_error(void);
+
+/* FMA-rate probe.  No counterpart in the reference: it measures the device's
+ * FP32 (precision LENSGB_FP32_SPLIT) or FP64 (LENSGB_FP64) fused multiply-add
+ * rate, the peak against which the roofline fractions of the compute-bound
+ * kernels are stated.  Launches `blocks` CTAs of 256 threads, each running 8
+ * independent chains of `iters` FMAs (iters a multiple of 16), and writes one
+ * value per thread to out_dev (blocks x 256 elements of that precision).
+ * *flops receives the launch's flop count (2 per FMA); time the launch with
+ * events on `stream`. */
+int lensgb_fma_chain(int precision, int blocks, int iters, void* out_dev, long long* flops,
+                     void* stream);
 
 /* ABI version of this header (major * 100 + minor). */
 int lensgb_version(void);

@@ -52,6 +52,7 @@ SYMBOLS = [
     "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
+    "lensgb_fma_chain",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -237,6 +238,8 @@ def load():
     lib.lensgb_loglike_image.restype = i
     lib.lensgb_point_sources_add.argtypes = [vp, dp, i, i, dp, i, ll, i, vp, vp]
     lib.lensgb_point_sources_add.restype = i
+    lib.lensgb_fma_chain.argtypes = [i, i, i, vp, ctypes.POINTER(ll), vp]
+    lib.lensgb_fma_chain.restype = i
     lib.lensgb_hessian.argtypes = [vp, dp, i, dp, dp, dp, ll, vp]
     lib.lensgb_hessian.restype = i
     lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]

@@ -7,8 +7,11 @@ kernel (``lensgb_loglike_grad``), computed together with the forward pass so
 the ray grid is traced twice in all (forward image, adjoint), never stored.
 This is what ``jax.grad`` through the reference's
 ``ImageModel.likelihood_data_given_model`` (``image_model.py:163-221``)
-provides, for the profiles the adjoint supports (EPL, SIE, NIE, NFW, TNFW,
-SHEAR lenses; Sersic light).
+provides, for the profiles the adjoint supports (EPL, EPL_MULTIPOLE_M1M3M4,
+SIE, NIE, NFW, TNFW, NFW_ELLIPSE_CSE, CONVERGENCE and SHEAR lenses; Sersic
+light) and every PSF and numerics option of the image path.  Without a
+gradient to compute (``torch.no_grad()`` or rows that do not require one) the
+forward likelihood runs alone.
 """
 
 import torch

@@ -69,19 +69,24 @@ struct lensgb_model {
     // gradient scratch (lensgb_loglike_grad), grow-only
     int grad_cap = 0;
     double* g_dcoef = nullptr;
-    double* g_psf = nullptr;
-    double* g_m = nullptr;
-    double* g_low = nullptr;
+    double* g_psf = nullptr;      // flipped kernels (pixel-scale or supersampled, then low-res)
+    double* g_m = nullptr;        // d logL / d model, full frame
+    double* g_a = nullptr;        // kernel-grid arrays (sub-frame crop, transposed convolution)
+    double* g_b = nullptr;
+    double* g_c = nullptr;        // supersampled-grid arrays (supersampled convolution)
+    double* g_d = nullptr;
+    double* g_pad_a = nullptr;    // edge-padded arrays (GAUSSIAN transposed convolution)
+    double* g_pad_b = nullptr;
     double* g_partial = nullptr;
 };
 
 static void free_grad_scratch(lensgb_model* m) {
-    cudaFree(m->g_dcoef);
-    cudaFree(m->g_psf);
-    cudaFree(m->g_m);
-    cudaFree(m->g_low);
-    cudaFree(m->g_partial);
-    m->g_dcoef = m->g_psf = m->g_m = m->g_low = m->g_partial = nullptr;
+    double** bufs[] = {&m->g_dcoef, &m->g_psf, &m->g_m, &m->g_a, &m->g_b,
+                       &m->g_c, &m->g_d, &m->g_pad_a, &m->g_pad_b, &m->g_partial};
+    for (double** b : bufs) {
+        cudaFree(*b);
+        *b = nullptr;
+    }
     m->grad_cap = 0;
 }
 
@@ -249,7 +254,7 @@ static int check_refine_size(const lensgb_model* m, int n_inst) {
 
 extern "C" {
 
-int lensgb_version(void) { return 115; }
+int lensgb_version(void) { return 116; }
 
 int lensgb_model_set_refine(lensgb_model* m, double tau, double kappa) {
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
@@ -1164,18 +1169,36 @@ static int ensure_grad_scratch(lensgb_model* m, int n_inst) {
     int cap = m->grad_cap > 0 ? m->grad_cap : 1;
     while (cap < n_inst) cap *= 2;
     free_grad_scratch(m);
-    const size_t npix = (size_t)m->grid.nx * m->grid.ny;
-    const size_t kk = (size_t)m->desc.kernel_size * m->desc.kernel_size;
+    const size_t full = (size_t)m->desc.nx * m->desc.ny;
+    const size_t kgrid = (size_t)m->grid.nx * m->grid.ny;
+    const bool hr = m->hr_conv;
+    const size_t hgrid = hr ? (size_t)m->grid_hr.nx * m->grid_hr.ny : 0;
+    const int K = m->desc.kernel_size, KL = m->desc.low_res_kernel_size;
+    const size_t kk = (size_t)K * K + (size_t)KL * KL;
     const size_t ncoef = (size_t)cap * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
-    const size_t npart = (size_t)cap * grad_chunks(m->grid) * (m->st.n_params > 0 ? m->st.n_params : 1);
-    if (cudaMalloc(&m->g_dcoef, ncoef * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&m->g_psf, (size_t)cap * (kk > 0 ? kk : 1) * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&m->g_m, (size_t)cap * npix * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&m->g_low, (size_t)cap * npix * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&m->g_partial, npart * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        free_grad_scratch(m);
-        return fail(LENSGB_ERR_OOM, "device allocation of gradient scratch failed");
+    const GridDesc& rg = hr ? m->grid_hr : m->grid;
+    const size_t npart = (size_t)cap * grad_chunks(rg) * (m->st.n_params > 0 ? m->st.n_params : 1);
+    size_t pad = 0;
+    if (m->desc.psf_type == LENSGB_PSF_GAUSSIAN) {
+        const size_t side = (size_t)(hr ? m->grid_hr.nx : m->grid.nx) + K - 1;
+        const size_t sidey = (size_t)(hr ? m->grid_hr.ny : m->grid.ny) + K - 1;
+        pad = side * sidey;
+    }
+    struct {
+        double** p;
+        size_t n;
+    } want[] = {{&m->g_dcoef, ncoef},         {&m->g_psf, (size_t)cap * (kk > 0 ? kk : 1)},
+                {&m->g_m, (size_t)cap * full}, {&m->g_a, (size_t)cap * kgrid},
+                {&m->g_b, (size_t)cap * kgrid}, {&m->g_c, (size_t)cap * hgrid},
+                {&m->g_d, (size_t)cap * hgrid}, {&m->g_pad_a, (size_t)cap * pad},
+                {&m->g_pad_b, (size_t)cap * pad}, {&m->g_partial, npart}};
+    for (auto& w : want) {
+        if (w.n == 0) continue;
+        if (cudaMalloc(w.p, w.n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            free_grad_scratch(m);
+            return fail(LENSGB_ERR_OOM, "device allocation of gradient scratch failed");
+        }
     }
     m->grad_cap = cap;
     return LENSGB_OK;
@@ -1187,17 +1210,10 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
     if (!m) return fail(LENSGB_ERR_INVALID, "null model");
     if (m->desc.precision != LENSGB_FP64)
         return fail(LENSGB_ERR_UNSUPPORTED, "the likelihood gradient needs an FP64 model");
-    if (m->desc.psf_type == LENSGB_PSF_GAUSSIAN)
-        return fail(LENSGB_ERR_UNSUPPORTED,
-                    "the likelihood gradient supports PSF types NONE and PIXEL (the transposed "
-                    "edge-padded convolution is not provided)");
-    if (m->hr_conv || m->sub)
-        return fail(LENSGB_ERR_UNSUPPORTED,
-                    "the likelihood gradient does not support supersampled convolution or "
-                    "sub-frames");
     if (!grad_supported(m->st))
         return fail(LENSGB_ERR_UNSUPPORTED,
-                    "the likelihood gradient supports lens stacks of EPL, SIE, NIE and SHEAR and Sersic "
+                    "the likelihood gradient supports lens stacks of EPL, EPL_MULTIPOLE_M1M3M4, "
+                    "SIE, NIE, NFW, TNFW, NFW_ELLIPSE_CSE, CONVERGENCE and SHEAR and Sersic "
                     "light profiles, with at most 64 parameters per system");
     if (!nd || !nd->data_dev) return fail(LENSGB_ERR_INVALID, "null noise description or data");
     if (!image_out || !logl || !grad) return fail(LENSGB_ERR_INVALID, "null output pointer");
@@ -1210,6 +1226,7 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
     if (rc) return rc;
     if (n_inst == 0) return LENSGB_OK;
     if ((rc = ensure_grad_scratch(m, n_inst))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
     LoglikeArgs a;
     a.data = nd->data_dev;
     a.data_stride = nd->data_stride;
@@ -1222,13 +1239,58 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
     a.exposure_time = nd->exposure_time;
     a.background_rms = nd->background_rms;
     a.error_map = nd->error_map_dev;
-    const bool conv = m->desc.psf_type == LENSGB_PSF_PIXEL;
-    if (launch_loglike_grad(m->grid, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef,
-                            (const double*)image_out, a, conv ? (const double*)psf : nullptr,
-                            psf_stride, m->desc.kernel_size, m->g_psf, m->g_m, m->g_low,
-                            m->g_partial, m->pixel_width * m->pixel_width, logl, grad,
-                            (cudaStream_t)stream))
-        return fail(LENSGB_ERR_CUDA, "transposed convolution shared-memory configuration failed");
+    // reverse of the forward path: logL and d logL / d image (full frame), the
+    // sub-frame crop, the transposed convolution(s) and re-binning, the
+    // evaluation mask, then the rays
+    const long long full = (long long)m->desc.nx * m->desc.ny;
+    launch_grad_weights((const double*)image_out, n_inst, full, a, m->g_m, logl, s);
+    const int n = m->grid.nx, ny = m->grid.ny, nx = m->grid.nx;
+    double* gk = m->g_m;  // d logL / d (image on the kernel grid)
+    if (m->sub) {
+        launch_crop(m->g_m, m->g_a, n_inst, n, m->sub_r0, m->sub_c0, m->desc.ny, m->desc.nx, s);
+        gk = m->g_a;
+    }
+    const bool conv = m->desc.psf_type != LENSGB_PSF_NONE;
+    const int edge = m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0;
+    const int K = m->desc.kernel_size, KL = m->desc.low_res_kernel_size;
+    const double area = m->pixel_width * m->pixel_width;
+    const double* psf_d = (const double*)psf;
+    const char* conv_err = "transposed convolution shared-memory configuration failed";
+    if (conv && m->hr_conv) {
+        const int S = m->grid.s;
+        const int hy = m->grid_hr.ny, hx = m->grid_hr.nx;
+        // d out / d hr_out: area / s^2 per supersampled element (re_size), then
+        // the supersampled kernel's transpose
+        launch_expand(gk, m->g_c, n_inst, ny, nx, S, area / ((double)S * S), 0, s);
+        if (launch_conv_transpose(m->g_c, m->g_d, psf_d, psf_stride, K, edge, n_inst, hy, hx,
+                                  m->g_psf, m->g_pad_a, m->g_pad_b, s))
+            return fail(LENSGB_ERR_CUDA, conv_err);
+        if (KL > 0) {
+            // split kernel: + re_size^T(conv_low^T(g area)), pixel-scale part
+            launch_scale(gk, (long long)n_inst * ny * nx, area, s);
+            if (launch_conv_transpose(gk, m->g_b, psf_d + (long long)K * K, psf_stride, KL, 0,
+                                      n_inst, ny, nx, m->g_psf + (long long)n_inst * K * K,
+                                      nullptr, nullptr, s))
+                return fail(LENSGB_ERR_CUDA, conv_err);
+            launch_expand(m->g_b, m->g_d, n_inst, ny, nx, S, 1.0 / ((double)S * S), 1, s);
+        }
+        if (m->sub_mask) launch_mask(m->g_d, n_inst, ny, nx, S, m->sub_mask, LENSGB_FP64, s);
+        if (launch_grad_rays(m->grid_hr, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef,
+                             m->g_d, 1.0, m->g_partial, grad, s))
+            return fail(LENSGB_ERR_CUDA, "gradient launch failed");
+        return check_cuda("likelihood gradient launch");
+    }
+    const double* gl = gk;
+    if (conv) {
+        if (launch_conv_transpose(gk, m->g_b, psf_d, psf_stride, K, edge, n_inst, ny, nx,
+                                  m->g_psf, m->g_pad_a, m->g_pad_b, s))
+            return fail(LENSGB_ERR_CUDA, conv_err);
+        gl = m->g_b;
+    }
+    if (m->sub_mask) launch_mask((void*)gl, n_inst, ny, nx, 1, m->sub_mask, LENSGB_FP64, s);
+    if (launch_grad_rays(m->grid, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef, gl,
+                         area, m->g_partial, grad, s))
+        return fail(LENSGB_ERR_CUDA, "gradient launch failed");
     return check_cuda("likelihood gradient launch");
 }
 

@@ -573,8 +573,17 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
                 int ny, int nx, int K, int edge, int precision, cudaStream_t stream,
                 int tile_rows) {
-    if (precision == LENSGB_FP64)
+    if (precision == LENSGB_FP64) {
+        // 32 x 64 tiles (4 x 4 outputs per thread); launches that would give
+        // fewer than 2 CTAs per SM take 8 x 16 tiles (one output per thread).
+        // Every output sums its K^2 products in the same (kernel row, kernel
+        // column) order in both, so the two give identical values.
+        const long long big = (long long)((nx + 31) / 32) * ((ny + 63) / 64) * n_inst;
+        if (big < 2LL * num_sms())
+            return run_conv<double, 1, 1, 4>(in, out, kernel, kstride, n_inst, ny, nx, K, edge,
+                                             stream);
         return run_conv<double, 4, 4, 4>(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream);
+    }
     return run_conv_f32(in, out, kernel, kstride, n_inst, ny, nx, K, edge, stream, tile_rows);
 }
 

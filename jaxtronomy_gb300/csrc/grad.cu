@@ -8,13 +8,22 @@
 //   1. logL and g_m = d logL / d m per pixel (residual weights of the
 //      model-dependent variance  C = max(m,0)/t_exp + sigma_bkg^2 (+|err|) or
 //      noise_map^2; imaging_data.py:159-182, image_noise.py:100-137);
-//   2. g_low = conv^T(g_m): the transposed "same"-mode zero-padded convolution
-//      is the convolution with the kernel rotated by 180 degrees;
+//   2. the transpose of the image's numerics: the sub-frame crop
+//      (numerics_subframe.py:87-149), the transposed "same"-mode convolution --
+//      the convolution with the kernel rotated by 180 degrees, with zero
+//      padding (PixelKernelConvolution, convolution.py:74-86) or through an
+//      explicit edge-padded image whose halo is folded back onto the edge
+//      pixels (GaussianConvolution, convolution.py:215-235) -- and for
+//      convolution on the supersampled grid the transposed block mean and the
+//      split kernel's pixel-scale part (SubgridKernelConvolution,
+//      convolution.py:154-166), then the evaluation mask;
 //   3. one thread per pixel recomputes its s^2 rays, forward-mode derivatives
-//      of each lens deflection (EPL through its hypergeometric series, with
-//      dF_n/dt tables; SHEAR) and of each Sersic profile, and accumulates
-//      w * d flux / d p with w = g_low * pixel_width^2 / s^2 * flux_scaling;
-//      the source terms reach the lens parameters through
+//      of each lens deflection (EPL and EPL_MULTIPOLE_M1M3M4 through the
+//      hypergeometric series with dF_n/dt tables, the multipoles analytically;
+//      SIE/NIE; NFW/TNFW; the 44 CSE terms of NFW_ELLIPSE_CSE; CONVERGENCE;
+//      SHEAR) and of each Sersic profile, and accumulates w * d flux / d p with
+//      w = g_low * pixel_width^2 / s^2 * flux_scaling; the source terms reach
+//      the lens parameters through
 //      d beta / d p = -alpha_scaling * deflection_scaling * d alpha / d p;
 //   4. per-CTA partial sums are reduced in a fixed order (deterministic).
 // The EPL derivative uses the series of the forward pass (nmax(f) terms); the
@@ -28,6 +37,7 @@ namespace lensgb {
 
 constexpr int GRAD_THREADS = 128;
 constexpr int GRAD_PPT = 2;  // pixels per thread
+constexpr int GJ = 12;       // parameters of the largest lens profile (EPL_MULTIPOLE_M1M3M4)
 
 // ---------------------------------------------------------------------------
 // forward-mode dual numbers with 5 tangent directions (b, t, q, x1, y1)
@@ -170,7 +180,7 @@ __device__ __forceinline__ void dphiq_de(double e1, double e2, double& dq1, doub
 // J[1][k] = d alpha_y / d p_k.  `a` is the profile's raw parameter row.
 __device__ void epl_alpha_grad(const double* rec, const double* F, const double* dF,
                                const double* a, double dx, double dy, double& ax, double& ay,
-                               double J[2][6]) {
+                               double J[2][GJ]) {
     const double b = rec[2], t = rec[3], q = rec[4], c = rec[5], sn = rec[6];
     const int nmax = (int)rec[8];
     const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
@@ -179,7 +189,7 @@ __device__ void epl_alpha_grad(const double* rec, const double* F, const double*
     const D5 Za = Q * X1, Zb = Y1;
     const D5 r2 = Za * Za + Zb * Zb;
     for (int i = 0; i < 2; ++i)
-        for (int k = 0; k < 6; ++k) J[i][k] = 0.0;
+        for (int k = 0; k < GJ; ++k) J[i][k] = 0.0;
     ax = 0.0;
     ay = 0.0;
     if (r2.v == 0.0) return;  // reference: 0/0 -> NaN -> nan_to_num -> 0
@@ -266,7 +276,7 @@ __device__ void epl_alpha_grad(const double* rec, const double* F, const double*
 // differentiated in (b, s, q, x1, y1), with q frozen where the q < 1 clamp
 // replaces it.
 __device__ void nie_alpha_grad(int code, const double* rec, const double* a, double dx, double dy,
-                               double& ax, double& ay, double J[2][6]) {
+                               double& ax, double& ay, double J[2][GJ]) {
     const double b = rec[2], s = rec[3], qc = rec[4], c = rec[5], sn = rec[6];
     const bool nie = code == LENSGB_LENS_NIE;
     const double e1 = a[1], e2 = a[2];
@@ -320,7 +330,7 @@ __device__ void nie_alpha_grad(int code, const double* rec, const double* a, dou
 // the same formulas and floors as the forward pass (a floor freezes its
 // argument's derivative).
 __device__ void nfw_alpha_grad(int code, const double* a, double dx, double dy, double& ax,
-                               double& ay, double J[2][6]) {
+                               double& ay, double J[2][GJ]) {
     const bool trunc = code == LENSGB_LENS_TNFW;
     const D5 RS = dvar(a[0], 0), ARS = dvar(a[1], 1);
     const D5 X1 = dvar(dx, 3), Y1 = dvar(dy, 4);
@@ -381,7 +391,7 @@ __device__ void nfw_alpha_grad(int code, const double* a, double dx, double dy, 
 
 // SHEAR (shear.py:39-53) and its Jacobian w.r.t. (gamma1, gamma2, ra_0, dec_0).
 __device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, double dy,
-                                                 double& ax, double& ay, double J[2][6]) {
+                                                 double& ax, double& ay, double J[2][GJ]) {
     const double g1 = rec[2], g2 = rec[3];
     ax = g1 * dx + g2 * dy;
     ay = g2 * dx - g1 * dy;
@@ -390,6 +400,164 @@ __device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, d
     J[0][2] = -g1; J[1][2] = -g2;
     J[0][3] = -g2; J[1][3] = g1;
     J[0][4] = J[0][5] = J[1][4] = J[1][5] = 0.0;
+}
+
+// CONVERGENCE (convergence.py:35-46): alpha = kappa (x - ra_0, y - dec_0), and
+// its Jacobian w.r.t. (kappa, ra_0, dec_0).
+__device__ __forceinline__ void convergence_alpha_grad(const double* rec, double dx, double dy,
+                                                       double& ax, double& ay, double J[2][GJ]) {
+    const double k = rec[2];
+    ax = k * dx;
+    ay = k * dy;
+    J[0][0] = dx;  J[1][0] = dy;
+    J[0][1] = -k;  J[1][1] = 0.0;
+    J[0][2] = 0.0; J[1][2] = -k;
+}
+
+// NFW_ELLIPSE_CSE (nfw_ellipse_cse.py:250-280 -> cored_steep_ellipsoid.py:
+// 227-245,434-477,536-564) and its Jacobian w.r.t. (Rs, alpha_Rs, e1, e2,
+// center_x, center_y): the 44-term CSE sum in the product-average frame as dual
+// numbers in (Rs, alpha_Rs, q, x1, y1), with the normalisation
+// 4 rho0 Rs^3 / Rs = alpha_Rs / (1 + ln 1/2) (nfw.py:386-395), rotated back and
+// chained to (e1, e2) through (phi, q) as for EPL.
+__device__ void cse_alpha_grad(const double* rec, const double* a, double dx, double dy,
+                               double& ax, double& ay, double J[2][GJ]) {
+    const double q = rec[4], c = rec[5], sn = rec[6];
+    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5 RS = dvar(a[0], 0), ARS = dvar(a[1], 1), Q = dvar(q, 2);
+    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5 iRS = dinv(RS);
+    const D5 sq = dsqrt(Q);
+    const D5 xa = X1 * iRS * sq, ya = Y1 * iRS * sq;
+    const D5 q2 = Q * Q, omq2 = 1.0 + (-1.0) * q2;
+    const D5 xa2 = xa * xa, ya2 = ya * ya;
+    const D5 iq = dinv(Q);
+    D5 fx = dconst(0.0), fy = dconst(0.0);
+    for (int k = 0; k < CSE_NFW_TERMS; ++k) {
+        const double s = kCseNfwS[k];
+        const D5 am = kCseNfwA[k] * iq;
+        const D5 psi = dsqrt(q2 * (xa2 + dconst(s * s)) + ya2);
+        const D5 ps = psi + dconst(s);
+        const D5 Phi = ps * ps + omq2 * xa2;
+        const D5 den = dinv(s * (psi * Phi));
+        fx = fx + am * (Q * xa * (psi + s * q2) * den);
+        fy = fy + am * (Q * ya * ps * den);
+    }
+    const D5 cst = (1.0 / (1.0 + log(0.5))) * ARS * sq;
+    fx = cst * fx;
+    fy = cst * fy;
+    ax = fx.v * c - fy.v * sn;
+    ay = fx.v * sn + fy.v * c;
+    double dA[2][5];
+    for (int k = 0; k < 5; ++k) {
+        dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
+        dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
+    }
+    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    double dq1, dq2, dp1, dp2;
+    dphiq_de(a[2], a[3], dq1, dq2, dp1, dp2);
+    for (int i = 0; i < 2; ++i) {
+        const double aph = i == 0 ? aphx : aphy;
+        J[i][0] = dA[i][0];
+        J[i][1] = dA[i][1];
+        J[i][2] = dA[i][2] * dq1 + aph * dp1;
+        J[i][3] = dA[i][2] * dq2 + aph * dp2;
+        J[i][4] = -(i == 0 ? jdx0 : jdx1);
+        J[i][5] = -(i == 0 ? jdy0 : jdy1);
+    }
+}
+
+// EPL_MULTIPOLE_M1M3M4 (epl_multipole_m1m3m4.py:463-535,608-678): the EPL part
+// (epl_alpha_grad on the shared record) plus the multipoles m = 1, 3, 4 of
+// multipole.py:72-119 with a_m = a{m}_a theta_E / sqrt(q), phi_m = phi +
+// delta_phi_m and r_E = theta_E.  Jacobian w.r.t. (theta_E, gamma, e1, e2,
+// center_x, center_y, a1_a, delta_phi_m1, a3_a, delta_phi_m3, a4_a,
+// delta_phi_m4).  The multipoles are linear in a_m; their position derivatives
+// go through the polar radius (m = 1 only, zero where r is floored at 1e-6)
+// and the polar angle (zero at the centre itself, where atan2 has none).
+__device__ void multipole_alpha_grad(const double* rec, const double* F, const double* dF,
+                                     const double* a, double dx, double dy, double& ax,
+                                     double& ay, double J[2][GJ]) {
+    epl_alpha_grad(rec, F, dF, a, dx, dy, ax, ay, J);
+    const double q = rec[4], rE = rec[31];
+    const double r0 = sqrt(dx * dx + dy * dy);
+    const double phi = atan2(dy, dx);
+    const double cph = cos(phi), sph = sin(phi);
+    const double r1 = r0 > 0.000001 ? r0 : 0.000001;
+    const double L = log(r1 / rE);
+    const double am[3] = {2.0 * rec[16], rec[27], rec[29]};
+    const double pm[3] = {rec[26], rec[28], rec[30]};
+    double fx = 0.0, fy = 0.0;
+    double dfa[3][2], dfp[3][2];    // d f / d a_m, d f / d phi_m
+    double dfr[2] = {0.0, 0.0};     // d f / d r (through ln r, m = 1)
+    double dfph[2] = {0.0, 0.0};    // d f / d (polar angle)
+    double dfrE[2];                 // d f / d r_E
+    {
+        const double A = am[0], P = pm[0];
+        const double cp = cos(P), sp = sin(P), cd = cos(phi - P), sd = sin(phi - P);
+        const double ux = 0.5 * (cp * L + cd * cph), uy = 0.5 * (sp * L + cd * sph);
+        fx += A * ux;
+        fy += A * uy;
+        dfa[0][0] = ux;
+        dfa[0][1] = uy;
+        dfp[0][0] = 0.5 * A * (-sp * L + sd * cph);
+        dfp[0][1] = 0.5 * A * (cp * L + sd * sph);
+        dfrE[0] = -0.5 * A * cp / rE;
+        dfrE[1] = -0.5 * A * sp / rE;
+        if (r0 > 0.000001) {
+            dfr[0] += 0.5 * A * cp / r0;
+            dfr[1] += 0.5 * A * sp / r0;
+        }
+        // d/dphi of cos(phi - P) cos(phi) and cos(phi - P) sin(phi)
+        dfph[0] += 0.5 * A * (-sd * cph - cd * sph);
+        dfph[1] += 0.5 * A * (-sd * sph + cd * cph);
+    }
+    for (int j = 1; j < 3; ++j) {
+        const double m = j == 1 ? 3.0 : 4.0, A = am[j], P = pm[j];
+        const double k = 1.0 / (1.0 - m * m);
+        const double C = cos(m * (phi - P)), S = sin(m * (phi - P));
+        const double ux = k * (cph * C + m * sph * S), uy = k * (sph * C - m * cph * S);
+        fx += A * ux;
+        fy += A * uy;
+        dfa[j][0] = ux;
+        dfa[j][1] = uy;
+        dfp[j][0] = A * k * m * (cph * S - m * sph * C);
+        dfp[j][1] = A * k * m * (sph * S + m * cph * C);
+        dfph[0] += -A * sph * C;
+        dfph[1] += A * cph * C;
+    }
+    ax += fx;
+    ay += fy;
+    // position: d/d(dx, dy) = d/dr (cos, sin) + d/dphi (-sin, cos) / r
+    double fdx[2], fdy[2];
+    const double ir = r0 > 0.0 ? 1.0 / r0 : 0.0;
+    for (int i = 0; i < 2; ++i) {
+        fdx[i] = dfr[i] * cph - dfph[i] * sph * ir;
+        fdy[i] = dfr[i] * sph + dfph[i] * cph * ir;
+    }
+    const double theta_E = a[0], sqq = sqrt(q);
+    double dq1, dq2, dp1, dp2;
+    dphiq_de(a[2], a[3], dq1, dq2, dp1, dp2);
+    for (int i = 0; i < 2; ++i) {
+        double dth = dfrE[i], dq = 0.0, dphi_epl = 0.0;
+        for (int j = 0; j < 3; ++j) {
+            const double araw = a[6 + 2 * j];
+            dth += dfa[j][i] * araw / sqq;
+            dq += dfa[j][i] * (-0.5 * am[j] / q);
+            dphi_epl += dfp[j][i];
+            J[i][6 + 2 * j] = dfa[j][i] * theta_E / sqq;
+            J[i][7 + 2 * j] = dfp[j][i];
+        }
+        J[i][0] += dth;
+        J[i][2] += dq * dq1 + dphi_epl * dp1;
+        J[i][3] += dq * dq2 + dphi_epl * dp2;
+        J[i][4] -= i == 0 ? fdx[0] : fdx[1];
+        J[i][5] -= i == 0 ? fdy[0] : fdy[1];
+    }
 }
 
 // Sersic / elliptical Sersic (sersic_ellipse.py:62-93, sersic_utils.py:69-110,
@@ -462,6 +630,9 @@ __device__ __host__ __forceinline__ int lens_np(int code) {
         case LENSGB_LENS_SHEAR: return 4;
         case LENSGB_LENS_NFW: return 4;
         case LENSGB_LENS_TNFW: return 5;
+        case LENSGB_LENS_CONVERGENCE: return 3;
+        case LENSGB_LENS_NFW_ELLIPSE_CSE: return 6;
+        case LENSGB_LENS_EPL_MULTIPOLE_M1M3M4: return 12;
         default: return 0;
     }
 }
@@ -475,7 +646,8 @@ __global__ void epl_dcoef_kernel(StackDesc st, int n_inst, const double* __restr
     if (gid >= n_inst * st.n_lens) return;
     const int inst = gid / st.n_lens, p = gid % st.n_lens;
     const int es = st.epl_slot[p];
-    if (es < 0 || st.lens[p] != LENSGB_LENS_EPL) return;
+    if (es < 0 || (st.lens[p] != LENSGB_LENS_EPL && st.lens[p] != LENSGB_LENS_EPL_MULTIPOLE_M1M3M4))
+        return;
     const double* d = rec_d + ((long long)inst * n_prof + p) * REC_D;
     const double* F = coef_d + ((long long)inst * st.n_epl + es) * EPL_NMAX;
     double* dF = dcoef + ((long long)inst * st.n_epl + es) * EPL_NMAX;
@@ -593,15 +765,22 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                     const double* r = srec + p * REC_D;
                     const int code = st.lens[p];
                     const int es = st.epl_slot[p];
-                    double ax, ay, J[2][6];
+                    double ax, ay, J[2][GJ];
                     const double ddx = X - r[RD_CX], ddy = Y - r[RD_CY];
                     if (code == LENSGB_LENS_EPL)
                         epl_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
                                        P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else if (code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4)
+                        multipole_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
+                                             P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE)
                         nie_alpha_grad(code, r, P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else if (code == LENSGB_LENS_NFW || code == LENSGB_LENS_TNFW)
                         nfw_alpha_grad(code, P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else if (code == LENSGB_LENS_NFW_ELLIPSE_CSE)
+                        cse_alpha_grad(r, P + st.lens_off[p], ddx, ddy, ax, ay, J);
+                    else if (code == LENSGB_LENS_CONVERGENCE)
+                        convergence_alpha_grad(r, ddx, ddy, ax, ay, J);
                     else
                         shear_alpha_grad(r, ddx, ddy, ax, ay, J);
                     axs += ax;
@@ -684,27 +863,128 @@ bool grad_supported(const StackDesc& st) {
     return lp <= GRAD_MAX_LENSP;
 }
 
-int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
-                        const double* rec_d, const double* coef_d, double* dcoef,
-                        const double* image, const LoglikeArgs& la, const double* psf,
-                        long long psf_stride, int K, double* psf_flip, double* gm, double* glow,
-                        double* partial, double pixel_area, double* logl, double* grad,
-                        cudaStream_t stream) {
-    const long long npix = (long long)g.nx * g.ny;
+int launch_grad_weights(const double* image, int n_inst, long long npix, const LoglikeArgs& la,
+                        double* gm, double* logl, cudaStream_t stream) {
+    if (n_inst <= 0) return 0;
+    loglike_weights_kernel<<<n_inst, 256, 0, stream>>>(image, npix, la, gm, logl);
+    return 0;
+}
+
+// Edge padding as an explicit (ny + 2h) x (nx + 2h) image: pad[p][q] =
+// in[clamp(p - h)][clamp(q - h)].  Its transpose folds the halo back onto the
+// edge pixels: fold_edge_kernel sums, for each pixel, the padded pixels that
+// clamp to it (its own, plus the halo rows / columns beyond an edge).
+__global__ void embed_pad_kernel(const double* __restrict__ in, double* __restrict__ pad,
+                                 int n_inst, int ny, int nx, int h) {
+    const int PW = nx + 2 * h, PH = ny + 2 * h;
+    const long long per = (long long)PW * PH;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= per * n_inst) return;
+    const long long inst = gid / per, e = gid - inst * per;
+    const int r = (int)(e / PW) - h, c = (int)(e % PW) - h;
+    pad[gid] = (r >= 0 && r < ny && c >= 0 && c < nx) ? in[(inst * ny + r) * nx + c] : 0.0;
+}
+
+__global__ void fold_edge_kernel(const double* __restrict__ pad, double* __restrict__ out,
+                                 int n_inst, int ny, int nx, int h) {
+    const long long per = (long long)nx * ny;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= per * n_inst) return;
+    const long long inst = gid / per, e = gid - inst * per;
+    const int row = (int)(e / nx), col = (int)(e % nx);
+    const int PW = nx + 2 * h, PH = ny + 2 * h;
+    const int r0 = row == 0 ? 0 : row + h, r1 = row == ny - 1 ? ny - 1 + 2 * h : row + h;
+    const int c0 = col == 0 ? 0 : col + h, c1 = col == nx - 1 ? nx - 1 + 2 * h : col + h;
+    const double* p = pad + inst * (long long)PW * PH;
+    double acc = 0.0;
+    for (int r = r0; r <= r1; ++r)
+        for (int c = c0; c <= c1; ++c) acc += p[(long long)r * PW + c];
+    out[gid] = acc;
+}
+
+int launch_conv_transpose(const double* in, double* out, const double* psf, long long psf_stride,
+                          int K, int edge, int n_inst, int ny, int nx, double* psf_flip,
+                          double* pad_a, double* pad_b, cudaStream_t stream) {
+    if (n_inst <= 0) return 0;
+    const long long kk = (long long)K * K;
+    const long long nk = kk * n_inst;
+    flip_psf_kernel<<<(unsigned)((nk + 255) / 256), 256, 0, stream>>>(psf, psf_flip, K, psf_stride,
+                                                                       n_inst);
+    if (!edge)
+        return launch_conv(in, out, psf_flip, kk, n_inst, ny, nx, K, 0, LENSGB_FP64, stream);
+    // edge padding: out = fold(conv_zero(pad(in)))
+    const int h = K / 2;
+    const long long np = (long long)(ny + 2 * h) * (nx + 2 * h) * n_inst;
+    embed_pad_kernel<<<(unsigned)((np + 255) / 256), 256, 0, stream>>>(in, pad_a, n_inst, ny, nx,
+                                                                        h);
+    if (launch_conv(pad_a, pad_b, psf_flip, kk, n_inst, ny + 2 * h, nx + 2 * h, K, 0, LENSGB_FP64,
+                    stream))
+        return -1;
+    const long long n = (long long)ny * nx * n_inst;
+    fold_edge_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(pad_b, out, n_inst, ny, nx,
+                                                                       h);
+    return 0;
+}
+
+__global__ void crop_kernel(const double* __restrict__ full, double* __restrict__ sub, int n_inst,
+                            int n, int r0, int c0, int ny_full, int nx_full) {
+    const long long per = (long long)n * n;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= per * n_inst) return;
+    const long long inst = gid / per, e = gid - inst * per;
+    const int r = (int)(e / n), c = (int)(e % n);
+    sub[gid] = full[(inst * ny_full + r0 + r) * (long long)nx_full + c0 + c];
+}
+
+int launch_crop(const double* full, double* sub, int n_inst, int n, int r0, int c0, int ny_full,
+                int nx_full, cudaStream_t stream) {
+    const long long total = (long long)n * n * n_inst;
+    if (total <= 0) return 0;
+    crop_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(full, sub, n_inst, n, r0, c0,
+                                                                      ny_full, nx_full);
+    return 0;
+}
+
+// hr (n_inst x ny*s x nx*s) = or += low (n_inst x ny x nx) x scale, each pixel
+// spread over its s x s block: the transpose of the block mean (times scale s^2).
+__global__ void expand_kernel(const double* __restrict__ low, double* __restrict__ hr,
+                              int n_inst, int ny, int nx, int s, double scale, int accumulate) {
+    const long long W = (long long)nx * s, per = W * ny * s;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= per * n_inst) return;
+    const long long inst = gid / per, e = gid - inst * per;
+    const int r = (int)(e / W) / s, c = (int)(e % W) / s;
+    const double v = low[(inst * ny + r) * (long long)nx + c] * scale;
+    hr[gid] = accumulate ? hr[gid] + v : v;
+}
+
+int launch_expand(const double* low, double* hr, int n_inst, int ny, int nx, int s, double scale,
+                  int accumulate, cudaStream_t stream) {
+    const long long total = (long long)ny * nx * s * s * n_inst;
+    if (total <= 0) return 0;
+    expand_kernel<<<(unsigned)((total + 255) / 256), 256, 0, stream>>>(low, hr, n_inst, ny, nx, s,
+                                                                        scale, accumulate);
+    return 0;
+}
+
+__global__ void scale_kernel(double* __restrict__ x, long long n, double a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= a;
+}
+
+int launch_scale(double* x, long long n, double a, cudaStream_t stream) {
+    if (n <= 0) return 0;
+    scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(x, n, a);
+    return 0;
+}
+
+int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
+                     const double* rec_d, const double* coef_d, double* dcoef, const double* gl,
+                     double w_scale, double* partial, double* grad, cudaStream_t stream) {
+    if (n_inst <= 0) return 0;
     if (st.n_lens > 0) {
         const int n = n_inst * st.n_lens;
         epl_dcoef_kernel<<<(n + 127) / 128, 128, 0, stream>>>(st, n_inst, rec_d, coef_d, dcoef);
-    }
-    loglike_weights_kernel<<<n_inst, 256, 0, stream>>>(image, npix, la, gm, logl);
-    const double* gl = gm;
-    if (psf) {
-        const long long kk = (long long)K * K;
-        const long long n = kk * n_inst;
-        flip_psf_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(psf, psf_flip, K,
-                                                                          psf_stride, n_inst);
-        if (launch_conv(gm, glow, psf_flip, kk, n_inst, g.ny, g.nx, K, 0, LENSGB_FP64, stream))
-            return -1;
-        gl = glow;
     }
     const int chunks = grad_chunks(g);
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
@@ -713,7 +993,7 @@ int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, cons
         cudaFuncSetAttribute(grad_ray_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     grad_ray_kernel<<<dim3((unsigned)chunks, (unsigned)n_inst), GRAD_THREADS, smem, stream>>>(
-        g, st, params, rec_d, coef_d, dcoef, gl, pixel_area, partial);
+        g, st, params, rec_d, coef_d, dcoef, gl, w_scale, partial);
     const int n = n_inst * st.n_params;
     grad_reduce_kernel<<<(n + 127) / 128, 128, 0, stream>>>(partial, chunks, st.n_params, n_inst,
                                                            grad);
@@ -749,13 +1029,19 @@ __global__ void hessian_points_kernel(StackDesc st, const double* __restrict__ r
             h[3] += r[2];
             continue;
         }
-        double ax, ay, J[2][6];
+        double ax, ay, J[2][GJ];
         int co;
-        if (code == LENSGB_LENS_EPL) {
+        if (code == LENSGB_LENS_EPL || code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4) {
             // dF/dt enters only the t direction of the duals: the coefficient table
             // stands in for it
             const double* F = coef_i + st.epl_slot[p] * EPL_NMAX;
-            epl_alpha_grad(r, F, F, a, dx, dy, ax, ay, J);
+            if (code == LENSGB_LENS_EPL)
+                epl_alpha_grad(r, F, F, a, dx, dy, ax, ay, J);
+            else
+                multipole_alpha_grad(r, F, F, a, dx, dy, ax, ay, J);
+            co = 4;
+        } else if (code == LENSGB_LENS_NFW_ELLIPSE_CSE) {
+            cse_alpha_grad(r, a, dx, dy, ax, ay, J);
             co = 4;
         } else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE) {
             nie_alpha_grad(code, r, a, dx, dy, ax, ay, J);

@@ -13,6 +13,25 @@ namespace lensgb {
 // Sets the calling thread's lensgb_last_error() text (defined in abi.cu).
 void set_last_error(const std::string& msg);
 
+// Streaming multiprocessors of the current device (launch shapes), read from
+// the device once per device.
+inline int num_sms() {
+    static int cached[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (cached[dev] <= 0) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            n <= 0) {
+            cudaGetLastError();
+            n = 1;
+        }
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
 // Per-system profile records of n_inst systems (grids: per-system grids of a
 // mixed launch; n_dev: device count of systems actually present, <= n_inst).
 int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params, int n_inst,
@@ -142,19 +161,36 @@ int launch_linear_solve(const void* A, int n_lin, int n_inst, long long npix, co
                         int flags, double* param, double* cov, void* image, double* logl,
                         int precision, cudaStream_t stream);
 
-// Adjoint gradient of logL (grad.cu): FP64 models whose lens stack holds only
-// EPL / SIE / NIE / SHEAR and whose light profiles are Sersic.  `image` is the model image
-// of the same params (lensgb_image output), rec_d / coef_d its prepared
-// records.  Scratch: dcoef (n_inst x n_epl x EPL_NMAX), psf_flip (n_inst x K^2),
-// gm and glow (n_inst x npix), partial (n_inst x grad_chunks x n_params).
+// Adjoint gradient of logL (grad.cu), FP64, in stages that lensgb_loglike_grad
+// chains (the reverse of the forward image path):
+//   launch_grad_weights: logL and g_m = d logL / d model per pixel;
+//   launch_crop: the sub-frame of a full-frame array (sub-frame models);
+//   launch_conv_transpose: the transposed "same" convolution (the PSF rotated
+//     by 180 degrees; edge = 1: edge padding, through pad_a / pad_b scratch of
+//     (ny + K - 1) x (nx + K - 1) per system); psf_flip: n_inst x K^2 scratch;
+//   launch_expand: the transposed s x s block mean (hr = low x scale per block);
+//   launch_grad_rays: forward-mode derivatives of every ray of grid g weighted
+//     by gl x w_scale / s^2 x flux_scaling, summed per parameter in a fixed
+//     order into grad (n_inst x n_params); dcoef: n_inst x n_epl x EPL_NMAX and
+//     partial: n_inst x grad_chunks(g) x n_params scratch.
+// grad_supported: every lens profile has a Jacobian (EPL, EPL_MULTIPOLE_M1M3M4,
+// SIE, NIE, NFW, TNFW, NFW_ELLIPSE_CSE, CONVERGENCE, SHEAR) and the row has at
+// most 64 parameters.
 bool grad_supported(const StackDesc& st);
 int grad_chunks(const GridDesc& g);
-int launch_loglike_grad(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
-                        const double* rec_d, const double* coef_d, double* dcoef,
-                        const double* image, const LoglikeArgs& la, const double* psf,
-                        long long psf_stride, int K, double* psf_flip, double* gm, double* glow,
-                        double* partial, double pixel_area, double* logl, double* grad,
-                        cudaStream_t stream);
+int launch_grad_weights(const double* image, int n_inst, long long npix, const LoglikeArgs& la,
+                        double* gm, double* logl, cudaStream_t stream);
+int launch_crop(const double* full, double* sub, int n_inst, int n, int r0, int c0, int ny_full,
+                int nx_full, cudaStream_t stream);
+int launch_conv_transpose(const double* in, double* out, const double* psf, long long psf_stride,
+                          int K, int edge, int n_inst, int ny, int nx, double* psf_flip,
+                          double* pad_a, double* pad_b, cudaStream_t stream);
+int launch_expand(const double* low, double* hr, int n_inst, int ny, int nx, int s, double scale,
+                  int accumulate, cudaStream_t stream);
+int launch_scale(double* x, long long n, double a, cudaStream_t stream);
+int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
+                     const double* rec_d, const double* coef_d, double* dcoef, const double* gl,
+                     double w_scale, double* partial, double* grad, cudaStream_t stream);
 
 // Point-wise single-parameter-set evaluation (FP64).
 int launch_ray_shoot_points(const StackDesc& st, const double* rec_d, const double* coef_d,
@@ -179,7 +215,8 @@ int launch_bulk_ray_shooting(const int* tag, const double* rec_d, const float* r
                              long long n, int precision, cudaStream_t stream);
 // LensModel.hessian at n points (out: f_xx, f_xy, f_yx, f_yy, n each) from the
 // lens records of one parameter row; hessian_supported: every lens profile has
-// position derivatives (EPL, SIE, NIE, NFW, TNFW, SHEAR, CONVERGENCE).
+// position derivatives (EPL, EPL_MULTIPOLE_M1M3M4, SIE, NIE, NFW, TNFW,
+// NFW_ELLIPSE_CSE, SHEAR, CONVERGENCE).
 bool hessian_supported(const StackDesc& st);
 int launch_hessian_points(const StackDesc& st, const double* rec, const double* coef,
                           const double* params, const double* x, const double* y, double* out,

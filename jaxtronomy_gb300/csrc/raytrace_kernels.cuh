@@ -192,6 +192,53 @@ raytrace_fp64_kernel(GridDesc g0, StackDesc st, int ppt, const double* __restric
     }
 }
 
+// FP64 kernel for launches too small to fill the GPU with one thread per
+// pixel (one system of 180x180 pixels is 127 CTAs of 256 pixel-threads on 152
+// SMs): one thread per supersampled ray.  A CTA takes RAY_PIX = 256 / s^2
+// consecutive pixels of one system, its threads trace their ray into shared
+// memory, and the first RAY_PIX threads combine each pixel's s^2 fluxes in the
+// order of pixel_value_d -- the same ray_flux_d code and the same sums, so a
+// pixel equals the one-thread-per-pixel kernel's value bit for bit.
+template <int C0, int C1, int NS, int NLL>
+__global__ void __launch_bounds__(256)
+raytrace_fp64_rays_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
+                          const double* __restrict__ coef, double* __restrict__ out, int flags,
+                          double out_scale) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    double* srec = (double*)smem_raw;
+    double* scoef = srec + n_prof * REC_D;
+    double* sub = scoef + st.n_epl * EPL_NMAX;  // 256 ray fluxes
+    const int inst = blockIdx.y;
+    load_records<double>(st, rec, coef, inst, srec, scoef);
+    const int s = g.s, s2 = s * s;
+    const int per = 256 / s2;
+    const long long npix = (long long)g.nx * g.ny;
+    const long long pix0 = (long long)blockIdx.x * per;
+    const int t = threadIdx.x;
+    const int el = t / s2, k = t - el * s2;
+    double v = 0.0;
+    if (el < per && pix0 + el < npix) {
+        const long long pix = pix0 + el;
+        const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
+        const int si = k / s, sj = k - si * s;
+        v = ray_flux_d<C0, C1, NS, NLL>(g, st, srec, scoef, row * s + si, col * s + sj, flags);
+    }
+    sub[t] = v;
+    __syncthreads();
+    if (t < per && pix0 + t < npix) {
+        const double* b = sub + t * s2;
+        double acc = 0;
+        for (int si = 0; si < s; ++si) {
+            double rs = 0;
+            for (int sj = 0; sj < s; ++sj) rs += b[si * s + sj];
+            acc += s == 1 ? rs : rs / (double)s;
+        }
+        if (s > 1) acc = acc / (double)s;
+        out[(long long)inst * npix + pix0 + t] = acc * out_scale;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP32 kernel (pass 1)
 // ---------------------------------------------------------------------------
@@ -456,17 +503,6 @@ refine_mixed_kernel(StackDesc st, const double* __restrict__ rec,
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
-inline int num_sms() {
-    static int g_num_sms = 0;
-    if (g_num_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 152;
-    }
-    return g_num_sms;
-}
-
 template <int C0, int C1, int NS, int NLL>
 void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const double* rec_d,
                            const float* rec_f, const double* coef_d, const float* coef_f,
@@ -488,6 +524,21 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     if (precision == LENSGB_FP64) {
         size_t smem = (size_t)(n_prof * REC_D + st.n_epl * EPL_NMAX) * sizeof(double);
+        // one thread per ray when one thread per pixel leaves the GPU under-filled
+        // (fewer than 4 CTAs per SM) and a CTA holds at least one pixel's rays
+        const long long pix_ctas = (long long)grid.x * grid.y;
+        if (!mt.grid && ppt_override <= 0 && g.s * g.s <= 256 &&
+            pix_ctas < 4LL * num_sms()) {
+            const int per = 256 / (g.s * g.s);
+            const dim3 rgrid((unsigned)((npix + per - 1) / per), (unsigned)n_inst);
+            const size_t rsmem = smem + 256 * sizeof(double);
+            if (rsmem > 48 * 1024)
+                cudaFuncSetAttribute(raytrace_fp64_rays_kernel<C0, C1, NS, NLL>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+            raytrace_fp64_rays_kernel<C0, C1, NS, NLL><<<rgrid, 256, rsmem, stream>>>(
+                g, st, rec_d, coef_d, (double*)out, flags, out_scale);
+            return;
+        }
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(raytrace_fp64_kernel<C0, C1, NS, NLL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -138,7 +138,7 @@ struct lensgb_server {
     std::mutex mu;
     std::condition_variable cv;
     int device = 0;
-    int n_sms = 152;                          // SMs of the device (launch shapes)
+    int n_sms = 1;                            // SMs of the device (launch shapes), read at create
     std::deque<Req> reqs;                     // stable storage, index = ticket
     std::vector<Req*> incoming;               // submitted, not yet released
     std::vector<Bucket*> buckets;             // guarded by mu (appended by submit)
@@ -900,11 +900,7 @@ int lensgb_server_create(const lensgb_server_config* cfg, lensgb_server** out) {
     lensgb_server* s = new lensgb_server();
     s->cfg = c;
     cudaGetDevice(&s->device);
-    int nsm = 0;
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device) == cudaSuccess &&
-        nsm > 0)
-        s->n_sms = nsm;
-    cudaGetLastError();
+    s->n_sms = lensgb::num_sms();
     memset(&s->stats, 0, sizeof s->stats);
     s->t0 = Clock::now();
     s->worker = std::thread(worker_main, s);

@@ -256,7 +256,7 @@ class ImageModel:
             self._ps_kernel = np.ascontiguousarray(ps_k, dtype=np.float64)
 
     # ------------------------------------------------------------------ models
-    def _desc(self, lens_idx, src_idx, ll_idx, lensed=True):
+    def _desc(self, lens_idx, src_idx, ll_idx, lensed=True, precision=None):
         d = _lib.ModelDesc()
         lm = self.LensModel.lens_model_list
         d.n_lens = len(lens_idx) if lensed else 0
@@ -281,17 +281,18 @@ class ImageModel:
         d.alpha_scaling = float(getattr(self.LensModel, "alpha_scaling", 1.0))
         d.psf_type = self._psf_type
         d.kernel_size = self._kernel_size
-        d.precision = self._precision
+        d.precision = self._precision if precision is None else precision
         d.supersampling_convolution = 1 if self._ssc else 0
         d.low_res_kernel_size = self._low_kernel_size
         return d
 
-    def _model(self, lens_idx, src_idx, ll_idx, lensed=True):
-        key = (tuple(lens_idx), tuple(src_idx), tuple(ll_idx), lensed)
+    def _model(self, lens_idx, src_idx, ll_idx, lensed=True, precision=None):
+        prec = self._precision if precision is None else precision
+        key = (tuple(lens_idx), tuple(src_idx), tuple(ll_idx), lensed, prec)
         if key not in self._models:
-            refine = self._refine if self._precision == _lib.FP32_SPLIT else None
-            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed), refine,
-                                           self._subframe)
+            refine = self._refine if prec == _lib.FP32_SPLIT else None
+            self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed, prec),
+                                           refine, self._subframe)
         return self._models[key]
 
     def refined_pixels(self, stream=None):
@@ -381,11 +382,15 @@ class ImageModel:
         profiles.pack(names_ll, profiles.LIGHT_PARAMS, kll, rows, c, "Lens light")
         return rows
 
-    def _psf_arg(self, psf_kernels, B):
+    def _psf_arg(self, psf_kernels, B, dtype=None):
         if self._psf_type == _lib.PSF_NONE:
             return None, 0, None
+        dtype = self._dtype if dtype is None else dtype
         if psf_kernels is None:
-            k = self._kernel_tensor()
+            if dtype == self._dtype:
+                k = self._kernel_tensor()
+            else:  # the FP64 twin of an FP32 model: the kernel at full precision
+                k = torch.as_tensor(self.pack_psf(self._kernel), dtype=dtype).cuda().contiguous()
             return k, 0, k
         k = psf_kernels
         K = int(self._kernel.shape[0])
@@ -396,11 +401,11 @@ class ImageModel:
                 raise ValueError("psf kernels must be %dx%d (supersampled)" % (K, K))
             arr = arr[None] if arr.ndim == 2 else arr
             packed = np.stack([self.pack_psf(a) for a in arr])
-            t = torch.as_tensor(packed).to(device="cuda", dtype=self._dtype).contiguous()
+            t = torch.as_tensor(packed).to(device="cuda", dtype=dtype).contiguous()
             return t, (0 if packed.shape[0] == 1 else self.psf_elements()), t
         if not isinstance(k, torch.Tensor):
             k = torch.as_tensor(np.ascontiguousarray(k))
-        k = k.to(device="cuda", dtype=self._dtype).contiguous()
+        k = k.to(device="cuda", dtype=dtype).contiguous()
         if k.dim() == 2:
             if tuple(k.shape) != (K, K):
                 raise ValueError("psf kernel must be %dx%d" % (K, K))
@@ -723,15 +728,19 @@ class ImageModel:
         (``lensgb_loglike_grad``).  The gradient has the layout of
         :meth:`pack_params`; :meth:`unpack_params` turns it into kwargs lists.
         This is ``jax.grad`` of the reference's ``likelihood_data_given_model``
-        (``image_model.py:163-221``) for FP64 models of EPL / SIE / NIE / NFW / TNFW /
-        SHEAR lenses and Sersic light."""
-        if self._precision != _lib.FP64:
-            raise ValueError("likelihood gradients need kwargs_numerics precision 'fp64'")
+        (``image_model.py:163-221``) for lens stacks of EPL,
+        EPL_MULTIPOLE_M1M3M4, SIE, NIE, NFW, TNFW, NFW_ELLIPSE_CSE, CONVERGENCE
+        and SHEAR with Sersic light, every PSF type, convolution on the pixel or
+        the supersampled grid and sub-frames (``flux_evaluate_indexes``).  The
+        gradient, its logL and ``image_out`` (float64) are computed in FP64
+        whatever the model's precision: an FP32 model differentiates through
+        its FP64 twin, because the gradient's sums over pixels mix signs."""
         if self._n_ps:
             raise ValueError("likelihood gradients with point sources are not supported")
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
-                            range(len(self.LensLightModel.profile_type_list)))
+                            range(len(self.LensLightModel.profile_type_list)),
+                            precision=_lib.FP64)
         if rows is None:
             rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
         rows_dev = _device.to_device_f64(rows)
@@ -742,7 +751,7 @@ class ImageModel:
             image_out = torch.empty((B, self._nx, self._ny), dtype=torch.float64, device="cuda")
         logl = torch.empty((B,), dtype=torch.float64, device="cuda")
         grad = torch.empty((B, model.param_count), dtype=torch.float64, device="cuda")
-        kt, kstride, keep = self._psf_arg(psf_kernels, B)
+        kt, kstride, keep = self._psf_arg(psf_kernels, B, dtype=torch.float64)
         kptr = ctypes.c_void_p(0) if kt is None else _device.ptr(kt)
         _lib.check(_lib.load().lensgb_loglike_grad(
             model.handle, _device.ptr(rows_dev), B, kptr, kstride, ctypes.byref(nd),

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_functions():
         assert hasattr(lib, name), name
-    assert lib.lensgb_version() == 115
+    assert lib.lensgb_version() == 116
 
 
 def _desc(**kw):

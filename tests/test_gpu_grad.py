@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 import torch
 
+import golden_io
 import jaxtronomy_gb300 as J
 from jaxtronomy_gb300 import autograd, workloads as W
 from oracle import image as oimage
@@ -51,7 +52,7 @@ def _fd(im, rows, kern, data):
         pert[:, 2 * k + 1, k] -= STEP
     pert = pert.reshape(B * 2 * P, P)
     d = np.repeat(data, 2 * P, axis=0)
-    kk = np.repeat(kern, 2 * P, axis=0)
+    kk = None if kern is None else np.repeat(kern, 2 * P, axis=0)
     ll = im.likelihood_batch(rows=pert, data=d, psf_kernels=kk).cpu().numpy().reshape(B, P, 2)
     return (ll[..., 0] - ll[..., 1]) / (2 * STEP)
 
@@ -184,12 +185,130 @@ def test_nfw_halos_match_central_differences(cuda):
     _check(grad.cpu().numpy(), _fd(im, rows, kern, data))
 
 
-def test_unsupported_models_raise(cuda):
+def test_too_many_parameters_raise(cuda):
+    """Rows above 64 parameters (here 12 + 4 + 7 x 7 = 65) are refused."""
     g = W.grid_kwargs(16, 0.05)
     data = J.ImageData(np.zeros((16, 16)), exposure_time=100.0, background_rms=0.01, **g)
-    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["NFW_ELLIPSE_CSE"]),
-                      J.LightModel(["SERSIC"]), J.LightModel([]))
-    kw = ([{"Rs": 1.0, "alpha_Rs": 0.5, "e1": 0.1, "e2": 0.0, "center_x": 0, "center_y": 0}],
-          [{"amp": 1.0, "R_sersic": 0.3, "n_sersic": 2, "center_x": 0, "center_y": 0}], [])
+    im = J.ImageModel(data, J.PSF("NONE"), J.LensModel(["EPL_MULTIPOLE_M1M3M4", "SHEAR"]),
+                      J.LightModel(["SERSIC_ELLIPSE"] * 7), J.LightModel([]))
+    kl = [{"theta_E": 1.0, "gamma": 2.0, "e1": 0.1, "e2": 0.0, "center_x": 0, "center_y": 0,
+           "a1_a": 0.0, "delta_phi_m1": 0.0, "a3_a": 0.0, "delta_phi_m3": 0.0, "a4_a": 0.0,
+           "delta_phi_m4": 0.0}, {"gamma1": 0.0, "gamma2": 0.0}]
+    ks = [{"amp": 1.0, "R_sersic": 0.3, "n_sersic": 2, "e1": 0.0, "e2": 0.0, "center_x": 0,
+           "center_y": 0}] * 7
     with pytest.raises(Exception):
-        im.likelihood_grad_batch(*kw, data=np.zeros((16, 16)))
+        im.likelihood_grad_batch(kl, ks, [], data=np.zeros((16, 16)))
+
+
+# ---------------------------------------------------------------------------
+# against finite differences of the reference's own likelihood
+# ---------------------------------------------------------------------------
+
+FD_CASES = golden_io.grad_fd_cases()
+
+
+def _fd_case_model(c, precision="fp64"):
+    n = c["num_pix"]
+    g = W.grid_kwargs(n, c["delta_pix"])
+    data = J.ImageData(np.asarray(c["data"]), exposure_time=1000.0, background_rms=0.01, **g)
+    pk = c["psf_kwargs"]
+    if pk["psf_type"] == "PIXEL":
+        psf = J.PSF("PIXEL", kernel_point_source=c["kernel"],
+                    point_source_supersampling_factor=pk.get("point_source_supersampling_factor",
+                                                             1))
+    elif pk["psf_type"] == "GAUSSIAN":
+        psf = J.PSF("GAUSSIAN", fwhm=pk["fwhm"], truncation=pk["truncation"])
+    else:
+        psf = J.PSF("NONE")
+    numerics = dict(c.get("numerics") or {}, supersampling_factor=c["s"], precision=precision)
+    return J.ImageModel(data, psf, J.LensModel(c["lens"]), J.LightModel(c["src"]),
+                        J.LightModel(c["ll"]), kwargs_numerics=numerics)
+
+
+@pytest.mark.parametrize("c", FD_CASES, ids=lambda c: c["tag"])
+def test_adjoint_matches_reference_finite_differences(cuda, c):
+    """The adjoint against finite differences of the reference's
+    likelihood_data_given_model run through the NumPy stand-in for jax
+    (tests/golden/grad_fd.npz): NFW_ELLIPSE_CSE with a GAUSSIAN PSF,
+    EPL_MULTIPOLE_M1M3M4 with two sources, SIE + CONVERGENCE + SHEAR without a
+    PSF, convolution on the supersampled grid with a split PIXEL kernel and
+    with a GAUSSIAN kernel, and the gradient workload's first system.  A
+    component passes when it matches the five-point stencil (step 1e-4) or the
+    central difference (step 1e-6), whichever a kink of the likelihood (the
+    Sersic core floor, max(m, 0) of the noise) spares."""
+    im = _fd_case_model(c)
+    rows = im.pack_params(c["kwargs_lens"], c["kwargs_source"], c["kwargs_lens_light"])
+    logl, grad = im.likelihood_grad_batch(rows=rows)
+    assert abs(float(logl[0]) - c["logL"]) <= 1e-10 * abs(c["logL"])
+    g = grad.cpu().numpy()[0]
+    g5, g2 = c["grad_5pt"], c["grad_central_1e-6"]
+    scale = np.abs(g5).max()
+    ok5 = np.abs(g - g5) <= RTOL * (np.abs(g5) + 1e-3 * scale)
+    ok2 = np.abs(g - g2) <= RTOL * (np.abs(g2) + 1e-3 * scale)
+    bad = ~(ok5 | ok2)
+    assert not bad.any(), [(c["param_order"][k], g[k], g5[k], g2[k]) for k in np.where(bad)[0]]
+
+
+def test_fp32_model_gradient_equals_fp64_model_gradient(cuda):
+    """An FP32 model differentiates through its FP64 twin: same logL and
+    gradient bits as the FP64 model."""
+    c = FD_CASES[1]
+    out = {}
+    for prec in ("fp64", "fp32"):
+        im = _fd_case_model(c, prec)
+        rows = im.pack_params(c["kwargs_lens"], c["kwargs_source"], c["kwargs_lens_light"])
+        out[prec] = [t.cpu().numpy() for t in im.likelihood_grad_batch(rows=rows)]
+    np.testing.assert_array_equal(out["fp32"][0], out["fp64"][0])
+    np.testing.assert_array_equal(out["fp32"][1], out["fp64"][1])
+
+
+def _batch_fd_model(lens_list, extra_kw, psf, numerics, num_pix=30, seed=1017):
+    model, lens_kw, src, ll, kern = W.gradient_batch(seed=seed, batch=3, num_pix=num_pix,
+                                                     supersampling=2, kernel_size=9)
+    g = W.grid_kwargs(num_pix, 0.05)
+    data_cls = J.ImageData(np.zeros((num_pix, num_pix)), exposure_time=1000.0,
+                           background_rms=0.01, **g)
+    im = J.ImageModel(data_cls, psf(kern), J.LensModel(lens_list),
+                      J.LightModel(["SERSIC_ELLIPSE"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                      kwargs_numerics=dict({"supersampling_factor": 2}, **numerics))
+    rows = im.pack_params(extra_kw(lens_kw), src, ll)
+    truth = rows.copy()
+    truth[:, 0] *= 1.01
+    kk = None if im._psf_type != 1 or numerics.get("supersampling_convolution") else kern
+    data = W.noisy_data(im.image_batch(rows=truth, psf_kernels=kk).cpu().numpy())
+    return im, rows, kk, data
+
+
+def test_cse_and_multipole_batches_match_central_differences(cuda):
+    """Batches of three systems: NFW_ELLIPSE_CSE + SHEAR and
+    EPL_MULTIPOLE_M1M3M4 + SHEAR against central differences of the GPU FP64
+    likelihood."""
+    rng = np.random.default_rng(11)
+    cases = [
+        (["NFW_ELLIPSE_CSE", "SHEAR"],
+         lambda kw: [{"Rs": rng.uniform(5, 20, 3), "alpha_Rs": rng.uniform(0.5, 2, 3),
+                      "e1": kw[0]["e1"], "e2": kw[0]["e2"], "center_x": kw[0]["center_x"],
+                      "center_y": kw[0]["center_y"]}, kw[1]]),
+        (["EPL_MULTIPOLE_M1M3M4", "SHEAR"],
+         lambda kw: [dict(kw[0], a1_a=rng.normal(0, 0.01, 3),
+                          delta_phi_m1=rng.uniform(0, np.pi, 3), a3_a=rng.normal(0, 0.01, 3),
+                          delta_phi_m3=rng.uniform(0, np.pi, 3), a4_a=rng.normal(0, 0.01, 3),
+                          delta_phi_m4=rng.uniform(0, np.pi, 3)), kw[1]]),
+    ]
+    for lens_list, extra in cases:
+        im, rows, kk, data = _batch_fd_model(
+            lens_list, extra, lambda k: J.PSF("PIXEL", kernel_point_source=k[0]), {})
+        _, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kk)
+        _check(grad.cpu().numpy(), _fd(im, rows, kk, data))
+
+
+def test_subframe_gradient_matches_central_differences(cuda):
+    """flux_evaluate_indexes (NumericsSubFrame): the full-frame residual cropped
+    to the sub-frame, the transposed convolution there and the evaluation mask."""
+    yy, xx = np.mgrid[0:30, 0:30]
+    fei = (yy - 13) ** 2 + (xx - 16) ** 2 <= 90
+    im, rows, kk, data = _batch_fd_model(
+        ["EPL", "SHEAR"], lambda kw: list(kw),
+        lambda k: J.PSF("PIXEL", kernel_point_source=k[0]), {"flux_evaluate_indexes": fei})
+    _, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kk)
+    _check(grad.cpu().numpy(), _fd(im, rows, kk, data))

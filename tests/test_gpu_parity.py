@@ -247,6 +247,20 @@ def test_batch_equals_single_bitwise_and_deterministic(cuda):
             assert torch.equal(one[0], a[i])
 
 
+def test_fp64_ray_per_thread_launch_equals_pixel_per_thread_launch(cuda):
+    """A single 180x180, s = 3 system runs the FP64 kernel with one thread per
+    ray (a per-pixel launch would fill less than one wave); a batch of eight runs
+    one thread per pixel.  Both combine each pixel's rays in the same order, and
+    the small-launch convolution tiles sum in the same order as the large ones:
+    the images must agree bit for bit."""
+    model, lens, src, ll, kern = W.batch_epl(seed=1001, batch=8, num_pix=180, kernel_size=31)
+    im = _batch_model(model, kern[0], 180, 0.04, 3, "fp64")
+    a = im.image_batch(lens, src, ll, psf_kernels=kern)
+    for i in (0, 5):
+        one = im.image_batch(*[W.instance(k, i) for k in (lens, src, ll)], psf_kernels=kern[i])
+        assert torch.equal(one[0], a[i])
+
+
 def test_empty_batch_and_edge_profiles(cuda):
     model, lens, src, ll, kern = W.batch_epl(seed=5, batch=3, num_pix=24, kernel_size=5)
     im = _batch_model(model, kern[0], 24, 0.04, 2, "fp64")
@@ -268,3 +282,17 @@ def test_empty_batch_and_edge_profiles(cuda):
         ref = oimage.image(scene, kl, W.instance(src, 0), W.instance(ll, 0))
         pp, mx = rel_err(got, ref, 1e-8)
         assert pp < FP64_RTOL and mx < FP64_RTOL, (e1, pp, mx)
+
+
+@pytest.mark.parametrize("name", ["NFW_ELLIPSE_CSE", "EPL_MULTIPOLE_M1M3M4"])
+def test_exact_hessian_of_cse_and_multipole_matches_differences(cuda, name):
+    """lensgb_hessian for NFW_ELLIPSE_CSE and EPL_MULTIPOLE_M1M3M4 (the
+    adjoint's dual-number deflections) against the reference's square finite
+    differences of alpha (lens_model.py:617-650) with step 1e-6, away from the
+    centre."""
+    for case in [c for c in golden_io.profile_cases() if c["kind"] == "lens" and c["name"] == name]:
+        lm = J.LensModel([name])
+        x, y = case["x"][4:], case["y"][4:]
+        got = np.array(lm.hessian(x, y, [case["kwargs"]]))
+        fd = np.array(lm.hessian(x, y, [case["kwargs"]], diff=1e-6))
+        np.testing.assert_allclose(got, fd, rtol=1e-5, atol=1e-6 * np.abs(fd).max())

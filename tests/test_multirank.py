@@ -1,6 +1,7 @@
 """The N-GPU bench path on CPU: world_size-2 gloo ranks run the bench's own
-host logic (max-over-ranks step time, whole-job throughput, per-rank seeds)
-and the reference arm's rank gating.  No GPU is involved."""
+host logic (max-over-ranks step time, whole-job throughput, per-rank seeds),
+the bench's replica launcher (``python bench.py --gpus N`` without torchrun)
+end to end, and the reference arm's rank gating.  No GPU is involved."""
 
 import os
 import socket
@@ -70,3 +71,37 @@ def test_reference_arm_other_ranks_do_no_work(monkeypatch, capsys):
         steps, warmup, gpus = 1, 1, 2
     assert bench.reference_arm(A()) == 0
     assert capsys.readouterr().out == ""
+
+
+def _launcher_worker(out_path):
+    """A replica of the launcher test: joins the group from the environment the
+    launcher set, takes the max over ranks of a per-rank step time and lets rank
+    0 write one bench-style line."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    assert os.environ["LOCAL_RANK"] == str(rank)
+    dist.init_process_group("gloo")
+    try:
+        ms = bench.max_over_ranks(2.0 + rank, dist, "cpu")
+        if rank == 0:
+            with open(out_path, "w") as f:
+                f.write(json.dumps({"n_gpus": world, "value": bench.job_rate(1024, world, ms),
+                                    "ms_per_step": ms}) + "\n")
+    finally:
+        dist.destroy_process_group()
+    return 0
+
+
+def test_replica_launcher_runs_two_ranks(tmp_path):
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    out = tmp_path / "line.json"
+    assert bench.launch_replicas(2, _launcher_worker, str(out)) == 0
+    lines = out.read_text().splitlines()
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    assert rec["n_gpus"] == 2 and rec["ms_per_step"] == 3.0
+    assert rec["value"] == pytest.approx(1024 * 2 / 3.0e-3)

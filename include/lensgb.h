@@ -265,6 +265,19 @@ int lensgb_image_noalloc(lensgb_model* model, const double* params_dev, int n_in
 int lensgb_convolve(const lensgb_model* model, const void* in_dev, int n_inst,
                     const void* psf_dev, long long psf_stride, void* out_dev, void* stream);
 
+/* Halo-tile staging of the FP32 zero-padded convolution (PixelKernelConvolution,
+ * jaxtronomy/ImSim/Numerics/convolution.py:74-86, as used by lensgb_image and
+ * lensgb_convolve): enable = 1 (the default) fills each CTA's tile with one
+ * tensor-memory-accelerator copy where the images allow it (rows a multiple of
+ * 16 bytes, 16-byte aligned base, K <= 48), enable = 0 with plain loads.  Both
+ * give the same values bit for bit.  Process-wide setting. */
+int lensgb_set_conv_tma(int enable);
+
+/* Number of CTAs whose bounded wait for an asynchronous copy gave up (each
+ * skips its tile's output) since the library was loaded; 0 in a healthy run.
+ * Synchronizes the device. */
+int lensgb_wait_timeouts(unsigned int* count);
+
 /* Noise model of the likelihood (ImageData / ImageNoise,
  * jaxtronomy/Data/imaging_data.py:159-182, image_noise.py:16-137).  Strides are
  * elements between consecutive systems; 0 shares one array across systems. */

@@ -52,7 +52,7 @@ SYMBOLS = [
     "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
-    "lensgb_fma_chain",
+    "lensgb_fma_chain", "lensgb_set_conv_tma", "lensgb_wait_timeouts",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -240,6 +240,10 @@ def load():
     lib.lensgb_point_sources_add.restype = i
     lib.lensgb_fma_chain.argtypes = [i, i, i, vp, ctypes.POINTER(ll), vp]
     lib.lensgb_fma_chain.restype = i
+    lib.lensgb_set_conv_tma.argtypes = [i]
+    lib.lensgb_set_conv_tma.restype = i
+    lib.lensgb_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    lib.lensgb_wait_timeouts.restype = i
     lib.lensgb_hessian.argtypes = [vp, dp, i, dp, dp, dp, ll, vp]
     lib.lensgb_hessian.restype = i
     lib.lensgb_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(vp)]

@@ -1040,6 +1040,17 @@ int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const voi
     return check_cuda("convolution launch");
 }
 
+int lensgb_set_conv_tma(int enable) {
+    set_conv_tma(enable);
+    return LENSGB_OK;
+}
+
+int lensgb_wait_timeouts(unsigned int* count) {
+    if (!count) return fail(LENSGB_ERR_INVALID, "null count pointer");
+    *count = conv_wait_timeouts();
+    return check_cuda("wait-timeout counter read");
+}
+
 int lensgb_loglike(lensgb_model* m, const double* params, int n_inst, const void* psf,
                    long long psf_stride, const lensgb_noise_desc* nd, void* image_out,
                    double* logl, void* stream) {

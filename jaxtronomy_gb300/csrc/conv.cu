@@ -13,6 +13,8 @@
 // memory.  Each thread accumulates an RY x CX register block, streaming one
 // input row segment at a time through registers and reusing it for every
 // output row of its block that the row touches.
+#include <cuda.h>  // CUtensorMap and its encoder's types (the encoder is fetched at run time)
+
 #include <map>
 #include <mutex>
 #include <type_traits>
@@ -228,6 +230,59 @@ conv_f32_kernel(const float* __restrict__ in, float* __restrict__ out,
     CONV_RUN_TILES(C32_W)
 }
 
+// The compute of one thread's 4 x 8 output block of the fixed-width kernels:
+// `base` is the halo tile at the block's first input row and column (row
+// pitch 64 + 8 NSEG + 4 floats, 16-byte aligned), `sk` the flipped kernel
+// rows zero-padded to 8 NSEG columns.  Every output sums its products in
+// (kernel row, kernel column) order.
+template <int NSEG>
+__device__ __forceinline__ void conv_f32_fixed_tile(const float* base, const float* sk, int K,
+                                                    float (&acc)[C32_RY][C32_CX]) {
+    constexpr int KP = 8 * NSEG;
+    constexpr int SW = C32_W + KP + 4;
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i)
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
+    // input row ir feeds output row i through kernel row ir - i
+    auto row_step = [&](int ir, int ilo, int ihi) {
+        const float4* row = reinterpret_cast<const float4*>(base + ir * SW);
+#pragma unroll
+        for (int sg = 0; sg < NSEG; ++sg) {
+            float seg[16];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 q = row[2 * sg + j];
+                seg[4 * j] = q.x;
+                seg[4 * j + 1] = q.y;
+                seg[4 * j + 2] = q.z;
+                seg[4 * j + 3] = q.w;
+            }
+#pragma unroll
+            for (int i = 0; i < C32_RY; ++i) {
+                if (i < ilo || i > ihi) continue;
+                const float4* kr = reinterpret_cast<const float4*>(sk + (ir - i) * KP + 8 * sg);
+                const float4 k0 = kr[0], k1 = kr[1];
+                const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+#pragma unroll
+                for (int vv = 0; vv < 8; ++vv)
+#pragma unroll
+                    for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
+            }
+        }
+    };
+    // output row i takes input rows i .. i+K-1, i.e. input row ir serves the
+    // output rows max(0, ir-K+1) .. min(RY-1, ir)
+    // head: input rows 0 .. RY-2
+    for (int ir = 0; ir < C32_RY - 1; ++ir)
+        row_step(ir, ir - K + 1 > 0 ? ir - K + 1 : 0, ir);
+    // body: rows RY-1 .. K-1 serve every output row (branch-free)
+    for (int ir = C32_RY - 1; ir < K; ++ir) row_step(ir, 0, C32_RY - 1);
+    // tail: rows max(K, RY-1) .. K+RY-2
+    for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
+        row_step(ir, ir - K + 1, C32_RY - 1);
+}
+
 // FP32 variant with the kernel width fixed at compile time (NSEG segments of 8
 // columns, K <= 8 NSEG): the same tiles and shared-memory layout as
 // conv_f32_kernel, but the input-row loop is split so that its middle part --
@@ -279,49 +334,8 @@ conv_f32_fixed_kernel(const float* __restrict__ in, float* __restrict__ out,
         __syncthreads();
 
         float acc[C32_RY][C32_CX];
-#pragma unroll
-        for (int i = 0; i < C32_RY; ++i)
-#pragma unroll
-            for (int c = 0; c < C32_CX; ++c) acc[i][c] = 0.f;
         const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
-        const float* base = si + r0 * SW + c0;
-        // input row ir feeds output row i through kernel row ir - i
-        auto row_step = [&](int ir, int ilo, int ihi) {
-            const float4* row = reinterpret_cast<const float4*>(base + ir * SW);
-#pragma unroll
-            for (int sg = 0; sg < NSEG; ++sg) {
-                float seg[16];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float4 q = row[2 * sg + j];
-                    seg[4 * j] = q.x;
-                    seg[4 * j + 1] = q.y;
-                    seg[4 * j + 2] = q.z;
-                    seg[4 * j + 3] = q.w;
-                }
-#pragma unroll
-                for (int i = 0; i < C32_RY; ++i) {
-                    if (i < ilo || i > ihi) continue;
-                    const float4* kr = reinterpret_cast<const float4*>(sk + (ir - i) * KP + 8 * sg);
-                    const float4 k0 = kr[0], k1 = kr[1];
-                    const float w[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
-#pragma unroll
-                    for (int vv = 0; vv < 8; ++vv)
-#pragma unroll
-                        for (int c = 0; c < C32_CX; ++c) acc[i][c] = fmaf(w[vv], seg[c + vv], acc[i][c]);
-                }
-            }
-        };
-        // output row i takes input rows i .. i+K-1, i.e. input row ir serves the
-        // output rows max(0, ir-K+1) .. min(RY-1, ir)
-        // head: input rows 0 .. RY-2
-        for (int ir = 0; ir < C32_RY - 1; ++ir)
-            row_step(ir, ir - K + 1 > 0 ? ir - K + 1 : 0, ir);
-        // body: rows RY-1 .. K-1 serve every output row (branch-free)
-        for (int ir = C32_RY - 1; ir < K; ++ir) row_step(ir, 0, C32_RY - 1);
-        // tail: rows max(K, RY-1) .. K+RY-2
-        for (int ir = (K > C32_RY - 1 ? K : C32_RY - 1); ir < K + C32_RY - 1; ++ir)
-            row_step(ir, ir - K + 1, C32_RY - 1);
+        conv_f32_fixed_tile<NSEG>(si + r0 * SW + c0, sk, K, acc);
         float* o = out + ioff;
 #pragma unroll
         for (int i = 0; i < C32_RY; ++i) {
@@ -355,6 +369,177 @@ static bool raise_smem_limit(const void* fn, size_t smem) {
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// TMA-staged halo tile (zero padding, uniform launches)
+// ---------------------------------------------------------------------------
+// The halo tile of conv_f32_fixed_kernel filled by one tensor-memory-
+// accelerator copy per CTA: a 3-D tensor map over the batch (x = column,
+// y = row, z = system) and one box of SW x SH floats.  The box's out-of-range
+// elements -- negative coordinates included -- arrive as zeros, which is the
+// zero padding of PixelKernelConvolution.  A tiled copy must start at an x
+// coordinate that is a multiple of 4 floats (16 bytes); the halo starts at
+// ox0 - h, so the box starts d = (ox0 - h) mod 4 columns to its left, and the
+// kernel rows carry d leading zero columns instead: input column ox0 + c + v - h
+// is tile column c + v + d, read against kernel column v + d.  Because
+// ox0 is a multiple of 64, d depends only on K, and 8 NSEG >= K + d holds for
+// every odd K, so no FMA is added; the non-zero products of every output are
+// summed in the same order as in conv_f32_fixed_kernel, which therefore gives
+// the same values bit for bit.
+//
+// The wait on the copy's mbarrier is bounded: after CONV_TMA_SPIN_LIMIT failed
+// polls a CTA counts a timeout in g_conv_wait_timeouts (read by
+// lensgb_wait_timeouts) and leaves without computing.
+constexpr unsigned int CONV_TMA_SPIN_LIMIT = 1u << 22;
+__device__ unsigned int g_conv_wait_timeouts = 0;
+
+template <int NSEG>
+__global__ void __launch_bounds__(C32_TX * 16)
+conv_f32_tma_kernel(const __grid_constant__ CUtensorMap tmap, float* __restrict__ out,
+                    const float* __restrict__ ker, long long kstride, int ny, int nx, int K,
+                    int d) {
+    constexpr int KP = 8 * NSEG;
+    constexpr int SW = C32_W + KP + 4;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) unsigned long long bar;
+    float* si = reinterpret_cast<float*>(
+        (reinterpret_cast<size_t>(smem_raw) + 127) & ~static_cast<size_t>(127));
+    // opaque launch values, as in CONV_RUN_TILES: the body is scheduled for
+    // register values rather than for expressions of blockIdx
+    int bxi = blockIdx.x, byi = blockIdx.y, bzi = blockIdx.z;
+    asm volatile("" : "+r"(bxi), "+r"(byi), "+r"(bzi), "+r"(nx), "+r"(ny), "+r"(K), "+r"(d));
+    const int TY = blockDim.y;
+    const int H = TY * C32_RY;
+    const int SH = H + K - 1;
+    float* sk = si + SH * SW;
+    const int ox0 = bxi * C32_W, oy0 = byi * H;
+    const int h = K / 2;
+    const int tid = threadIdx.y * C32_TX + threadIdx.x;
+    const int nthr = C32_TX * TY;
+    const unsigned int bar_s = static_cast<unsigned int>(__cvta_generic_to_shared(&bar));
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const unsigned int bytes = static_cast<unsigned int>(SH * SW * sizeof(float));
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s),
+                     "r"(bytes)
+                     : "memory");
+        const int x = ox0 - h - d, y = oy0 - h, z = bzi;
+        const unsigned int dst = static_cast<unsigned int>(__cvta_generic_to_shared(si));
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+            "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(x), "r"(y), "r"(z),
+            "r"(bar_s)
+            : "memory");
+    }
+    // the flipped kernel, shifted right by d zero columns, while the copy runs
+    const float* kk = ker + (long long)bzi * kstride;
+    for (int e = tid; e < K * KP; e += nthr) {
+        const int u = e / KP, v = e % KP - d;
+        sk[e] = (v >= 0 && v < K) ? kk[(K - 1 - u) * K + (K - 1 - v)] : 0.f;
+    }
+    __syncthreads();  // kernel rows written; the barrier is initialised
+    unsigned int done = 0;
+    for (unsigned int it = 0; it < CONV_TMA_SPIN_LIMIT && !done; ++it) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar_s)
+            : "memory");
+    }
+    if (!done) {
+        if (tid == 0) atomicAdd(&g_conv_wait_timeouts, 1u);
+        return;
+    }
+    float acc[C32_RY][C32_CX];
+    const int c0 = threadIdx.x * C32_CX, r0 = threadIdx.y * C32_RY;
+    conv_f32_fixed_tile<NSEG>(si + r0 * SW + c0, sk, K, acc);
+    float* o = out + (long long)bzi * ny * nx;
+#pragma unroll
+    for (int i = 0; i < C32_RY; ++i) {
+        const int y = oy0 + r0 + i;
+        if (y >= ny) continue;
+#pragma unroll
+        for (int c = 0; c < C32_CX; ++c) {
+            const int x = ox0 + c0 + c;
+            if (x < nx) o[(long long)y * nx + x] = acc[i][c];
+        }
+    }
+}
+
+static int g_conv_tma = 1;  // lensgb_set_conv_tma
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// The TMA path of run_conv_f32: returns 1 when it does not apply (edge padding,
+// a row pitch that is not a multiple of 16 bytes, an unaligned base, a kernel
+// wider than the compile-time widths, a box above 256 rows or columns, or no
+// tensor-map encoder), 0 when launched, -1 on a configuration error.
+static int run_conv_f32_tma(const float* in, float* out, const float* kernel, long long kstride,
+                            int n_inst, int ny, int nx, int K, int TY, cudaStream_t stream) {
+    const int h = K / 2;
+    const int d = ((-h) % 4 + 4) % 4;
+    const int KP = ((K + d + 7) / 8) * 8;
+    const int NSEG = KP / 8;
+    const int SW = C32_W + KP + 4, H = 4 * TY, SH = H + K - 1;
+    if (!g_conv_tma || NSEG > 6 || nx % 4 != 0 || (reinterpret_cast<size_t>(in) & 15) ||
+        SW > 256 || SH > 256)
+        return 1;
+    EncodeTiledFn enc = encode_tiled();
+    if (!enc) return 1;
+    CUtensorMap tmap;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)n_inst};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)SW, (cuuint32_t)SH, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(in), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return 1;
+    const size_t smem = (size_t)(SH * SW + K * KP) * sizeof(float) + 128;
+    const dim3 grid((unsigned)((nx + C32_W - 1) / C32_W), (unsigned)((ny + H - 1) / H),
+                    (unsigned)n_inst);
+    const dim3 block(C32_TX, TY);
+    auto go = [&](auto nseg_tag) {
+        constexpr int NS = decltype(nseg_tag)::value;
+        const void* fn = (const void*)conv_f32_tma_kernel<NS>;
+        if (smem > 48 * 1024 && !raise_smem_limit(fn, smem)) return -1;
+        conv_f32_tma_kernel<NS><<<grid, block, smem, stream>>>(tmap, out, kernel, kstride, ny, nx,
+                                                               K, d);
+        return 0;
+    };
+    switch (NSEG) {
+        case 1: return go(std::integral_constant<int, 1>());
+        case 2: return go(std::integral_constant<int, 2>());
+        case 3: return go(std::integral_constant<int, 3>());
+        case 4: return go(std::integral_constant<int, 4>());
+        case 5: return go(std::integral_constant<int, 5>());
+        case 6: return go(std::integral_constant<int, 6>());
+        default: return 1;
+    }
+}
+
 static int run_conv_f32(const void* in, void* out, const void* kernel, long long kstride,
                         int n_inst, int ny, int nx, int K, int edge, cudaStream_t stream,
                         int tile_rows) {
@@ -371,6 +556,11 @@ static int run_conv_f32(const void* in, void* out, const void* kernel, long long
         }
     }
     if (tile_rows >= 32 && tile_rows <= 64 && tile_rows % 4 == 0) best_ty = tile_rows / 4;
+    if (!edge) {
+        const int r = run_conv_f32_tma((const float*)in, (float*)out, (const float*)kernel,
+                                       kstride, n_inst, ny, nx, K, best_ty, stream);
+        if (r <= 0) return r;
+    }
     const int H = 4 * best_ty;
     const int KP = ((K + 7) / 8) * 8;
     const int SW = C32_W + KP + 4;
@@ -568,6 +758,14 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
     if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel<true>, smem)) return -1;
     conv_f32_kernel<true><<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
     return 0;
+}
+
+void set_conv_tma(int enable) { g_conv_tma = enable ? 1 : 0; }
+
+unsigned int conv_wait_timeouts() {
+    unsigned int v = 0;
+    cudaMemcpyFromSymbol(&v, g_conv_wait_timeouts, sizeof(v));
+    return v;
 }
 
 int launch_conv(const void* in, void* out, const void* kernel, long long kstride, int n_inst,

@@ -53,6 +53,12 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
                     cudaStream_t stream, const MixedTab* mixed = nullptr, int mixed_ctas = 0,
                     int ppt = 0);
 
+// FP32 zero-padded uniform convolutions stage their halo tiles with a TMA copy
+// when the images allow it (set_conv_tma(0): plain loads everywhere);
+// conv_wait_timeouts: CTAs whose bounded wait for that copy gave up (synchronous).
+void set_conv_tma(int enable);
+unsigned int conv_wait_timeouts();
+
 // "same"-mode 2-D convolution of n_inst (ny, nx) images with K x K kernels
 // (kernel stride 0 = shared).  edge = 0: zero padding; 1: edge padding.
 // tile_rows (FP32; a multiple of 4 in 32..64, 0: the built-in choice): output

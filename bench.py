@@ -703,6 +703,88 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
     }
 
 
+def convolution_section(reps=3):
+    """Direct halo-tile convolution against the FP64 FFT convolution, per image,
+    on the serving workload's grids and PSF sizes (pixel scale) and on a 4x
+    supersampled 300x300 grid (1200x1200, kernels 4 K + 1): CUDA-event time of
+    one lensgb_convolve call over a batch (L2 flushed before each), min of
+    `reps`, and the FFT result's error against the FP64 direct result."""
+    import numpy as np
+    import scipy.signal
+    import torch
+    import jaxtronomy_gb300 as J
+    from jaxtronomy_gb300 import _device, _lib, workloads as W
+    lib = _lib.load()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    cases = [(n, k) for n in (60, 180, 300) for k in (11, 21, 41)] + \
+            [(1200, 45), (1200, 85), (1200, 165)]
+    rows = []
+    rng = np.random.default_rng(5)
+    for n, K in cases:
+        B = 64 if n <= 300 else 4
+        img = rng.random((B, n, n)) * np.exp(rng.normal(0, 2, (B, n, n)))
+        kern = np.stack([W.moffat_pixel_kernel(0.12 * K / 11, 3.0, 0.05, K)] * B)
+        res = {"n": n, "K": K, "batch": B}
+        outs = {}
+        for prec in ("fp32", "fp64"):
+            dt = torch.float32 if prec == "fp32" else torch.float64
+            x = torch.as_tensor(img, dtype=dt).cuda().contiguous()
+            k = torch.as_tensor(kern, dtype=dt).cuda().contiguous()
+            for method in ("direct", "fft"):
+                g = W.grid_kwargs(n, 0.05)
+                data = J.ImageData(np.zeros((n, n)), exposure_time=1000.0,
+                                   background_rms=0.01, **g)
+                im = J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                                  J.LensModel(["SIE"]), J.LightModel(["SERSIC"]),
+                                  J.LightModel([]),
+                                  kwargs_numerics={"supersampling_factor": 1, "precision": prec,
+                                                   "convolution_method": method})
+                m = im._model(range(1), range(1), range(0))
+                out = torch.empty_like(x)
+                best = None
+                for r in range(reps + 1):
+                    flush.zero_()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    rc = lib.lensgb_convolve(m.handle, _device.ptr(x), B, _device.ptr(k), K * K,
+                                             _device.ptr(out), _device.stream_handle())
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    if rc != 0:
+                        best = None
+                        res["%s_%s" % (prec, method)] = "not possible: %s" % \
+                            lib.lensgb_last_error().decode()
+                        break
+                    ms = e0.elapsed_time(e1)
+                    if r > 0 and (best is None or ms < best):
+                        best = ms
+                if best is not None:
+                    res["%s_%s_ms_per_image" % (prec, method)] = best / B
+                    outs[(prec, method)] = out.double().cpu().numpy()
+                m.close()
+        ref = outs.get(("fp64", "direct"))
+        if ref is None:
+            ref = np.stack([scipy.signal.fftconvolve(img[i], kern[i], mode="same")
+                            for i in range(2)])
+        for prec in ("fp32", "fp64"):
+            got = outs.get((prec, "fft"))
+            if got is None:
+                continue
+            nb = ref.shape[0]
+            scale = np.abs(ref).reshape(nb, -1).max(axis=1)[:, None, None]
+            res["%s_fft_vs_fp64_direct_maxnorm" % prec] = float((np.abs(got[:nb] - ref)
+                                                                 / scale).max())
+        rows.append(res)
+        del outs
+    return {"cases": rows,
+            "timing": "CUDA events around one lensgb_convolve call of `batch` images (L2 "
+                      "flushed before each), min of %d, divided by the batch" % reps,
+            "error": "max |fft - fp64 direct| / max |fp64 direct| (fftconvolve on the CPU "
+                     "when the FP64 direct kernel cannot run)"}
+
+
 def serving_accuracy_section(seed=1002, per_bucket=4):
     """FP32-split accuracy of served requests: for each serving bucket (lens
     stack x number of sources), per_bucket requests of the stream -- the first
@@ -1242,6 +1324,10 @@ def gpu_arm(args):
                                 "each step's D2H on a second stream, overlapping the next "
                                 "step; the timed region ends after the last D2H)"}
 
+        # --- direct vs FFT convolution
+        if args.conv_table:
+            extra["convolution"] = convolution_section()
+
         # --- plain single image (60x60, SIE+SHEAR, s=1, 11x11)
         extra["single_image"] = single_image_section()
 
@@ -1341,6 +1427,7 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--oracle-systems", type=int, default=8)
+    ap.add_argument("--no-conv-table", dest="conv_table", action="store_false")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-sub", action="store_true")
     ap.add_argument("--no-grad", action="store_true")

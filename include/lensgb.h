@@ -265,6 +265,25 @@ int lensgb_image_noalloc(lensgb_model* model, const double* params_dev, int n_in
 int lensgb_convolve(const lensgb_model* model, const void* in_dev, int n_inst,
                     const void* psf_dev, long long psf_stride, void* out_dev, void* stream);
 
+/* How a model convolves (PIXEL: zero padding; GAUSSIAN: edge padding).  The
+ * reference computes jax.scipy.signal.fftconvolve(image, kernel, mode="same")
+ * (jaxtronomy/ImSim/Numerics/convolution.py:80-81) or convolve2d (:85); both
+ * give the same image up to rounding.  LENSGB_CONV_DIRECT: the shared-memory
+ * halo-tile kernels, 2 K^2 flop per pixel.  LENSGB_CONV_FFT: FP64 FFT in shared
+ * memory on a P x P grid, P the power of two >= N + K - 1 (plus K - 1 with edge
+ * padding, which runs on the explicitly edge-padded image; up to 4096),
+ * ~15 P^2 log2(P) flop per image whatever K; its scratch grows with the batch
+ * and is allocated on first use.  LENSGB_CONV_AUTO (the default): direct, and
+ * the FFT only where the direct kernels' tile does not fit in shared memory
+ * (K above ~140 in FP32, ~100 in FP64), so that a model's images keep one
+ * summation order in every launch form.  Measured on GB300, direct wins every
+ * FP32 case it can run; FP64 models are faster with LENSGB_CONV_FFT from
+ * K ~ 21 at 180x180 (3x at K = 41, 11x at K = 85 on 1200x1200). */
+#define LENSGB_CONV_AUTO 0
+#define LENSGB_CONV_DIRECT 1
+#define LENSGB_CONV_FFT 2
+int lensgb_model_set_convolution(lensgb_model* model, int method);
+
 /* Halo-tile staging of the FP32 zero-padded convolution (PixelKernelConvolution,
  * jaxtronomy/ImSim/Numerics/convolution.py:74-86, as used by lensgb_image and
  * lensgb_convolve): enable = 1 (the default) fills each CTA's tile with one

@@ -30,6 +30,8 @@ LIGHT_CODES = {"SERSIC": 1, "SERSIC_ELLIPSE": 2}
 PSF_NONE, PSF_PIXEL, PSF_GAUSSIAN = 0, 1, 2
 FP64, FP32_SPLIT = 0, 1
 
+CONV_METHODS = {"auto": 0, "direct": 1, "fft": 2}
+
 UNCONVOLVED = 1
 NO_SOURCE = 2
 NO_LENS_LIGHT = 4
@@ -53,6 +55,7 @@ SYMBOLS = [
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
     "lensgb_fma_chain", "lensgb_set_conv_tma", "lensgb_wait_timeouts",
+    "lensgb_model_set_convolution",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -240,6 +243,8 @@ def load():
     lib.lensgb_point_sources_add.restype = i
     lib.lensgb_fma_chain.argtypes = [i, i, i, vp, ctypes.POINTER(ll), vp]
     lib.lensgb_fma_chain.restype = i
+    lib.lensgb_model_set_convolution.argtypes = [vp, i]
+    lib.lensgb_model_set_convolution.restype = i
     lib.lensgb_set_conv_tma.argtypes = [i]
     lib.lensgb_set_conv_tma.restype = i
     lib.lensgb_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint)]
@@ -283,11 +288,13 @@ def check(rc):
 class Model:
     """Owner of one lensgb_model handle."""
 
-    def __init__(self, desc, refine=None, subframe=None):
+    def __init__(self, desc, refine=None, subframe=None, conv_method=0):
         lib = load()
         h = ctypes.c_void_p()
         check(lib.lensgb_model_create(ctypes.byref(desc), ctypes.byref(h)))
         self._h = h
+        if conv_method:
+            check(lib.lensgb_model_set_convolution(h, int(conv_method)))
         self.desc = desc
         self.param_count = lib.lensgb_model_param_count(h)
         self.subframe = subframe

@@ -66,6 +66,10 @@ struct lensgb_model {
     int tune_ppt = 0, tune_rows = 0;      // launch shapes (lensgb_model_autotune; 0: built-in)
     long long tune_pix = 0;               // pixels of the tuned call; tuned ppt applies from 1/4 of it
     float refine_kappa = 3e-7f;
+    // convolution method (lensgb_model_set_convolution) and the FFT path's scratch
+    int conv_method = LENSGB_CONV_AUTO;
+    void* fft_scratch = nullptr;
+    size_t fft_cap = 0;
     // gradient scratch (lensgb_loglike_grad), grow-only
     int grad_cap = 0;
     double* g_dcoef = nullptr;
@@ -433,6 +437,7 @@ int lensgb_model_destroy(lensgb_model* m) {
     cudaFree(m->pipe_psf);
     cudaFree(m->pipe_out[0]);
     cudaFree(m->pipe_out[1]);
+    cudaFree(m->fft_scratch);
     delete m;
     return LENSGB_OK;
 }
@@ -456,6 +461,51 @@ static int tuned_ppt(const lensgb_model* m, int n_inst) {
     return (m->tune_ppt > 0 && 4 * pix >= m->tune_pix) ? m->tune_ppt : 0;
 }
 
+// Whether a convolution of this model runs by FFT (fftconv.cu) rather than by
+// the direct halo-tile kernels (conv.cu).  LENSGB_CONV_AUTO: the FFT only where
+// the direct kernels' tile does not fit in shared memory (kernels wider than
+// ~140 pixels in FP32, ~100 in FP64), so that every image a model computes
+// with the direct kernels -- alone, batched, in mixed-grid launches and served
+// -- keeps one summation order.  Measured on GB300 (the bench's convolution
+// table), the direct kernels win every FP32 case they can run; FP64 models
+// gain from LENSGB_CONV_FFT from K ~ 21 at 180 x 180 (3x at K = 41, 11x at
+// K = 85 on 1200 x 1200).
+static bool conv_by_fft(const lensgb_model* m, int ny, int nx, int K, int edge) {
+    if (m->conv_method == LENSGB_CONV_DIRECT) return false;
+    if (fft_conv_size(ny, nx, K, edge) > 4096) return false;
+    if (m->conv_method == LENSGB_CONV_FFT) return true;
+    return !direct_conv_fits(K, m->desc.precision);
+}
+
+// The model's "same"-mode convolution of n_inst (ny, nx) images: FFT or direct.
+static int model_conv(lensgb_model* m, const void* in, void* out, const void* psf,
+                      long long psf_stride, int n_inst, int ny, int nx, int K, int edge,
+                      cudaStream_t s, int tile_rows = 0) {
+    if (!conv_by_fft(m, ny, nx, K, edge))
+        return launch_conv(in, out, psf, psf_stride, n_inst, ny, nx, K, edge, m->desc.precision,
+                           s, tile_rows);
+    const size_t need = fft_conv_scratch_bytes(n_inst, ny, nx, K, psf_stride, edge);
+    if (need > m->fft_cap) {
+        // the previous scratch may still be in use by queued work on this stream
+        if (m->fft_scratch) cudaStreamSynchronize(s);
+        cudaFree(m->fft_scratch);
+        m->fft_scratch = nullptr;
+        m->fft_cap = 0;
+        if (cudaMalloc(&m->fft_scratch, need) != cudaSuccess) {
+            cudaGetLastError();
+            return -3;
+        }
+        m->fft_cap = need;
+    }
+    return launch_conv_fft(in, out, psf, psf_stride, n_inst, ny, nx, K, edge, m->desc.precision,
+                           m->fft_scratch, s);
+}
+
+static int conv_fail(int rc) {
+    return rc == -3 ? fail(LENSGB_ERR_OOM, "device allocation of FFT convolution scratch failed")
+                    : fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+}
+
 static int image_core(lensgb_model* m, const double* params, int n_inst, const void* psf,
                       long long psf_stride, void* out, int flags, cudaStream_t s) {
     const bool conv = !(flags & LENSGB_UNCONVOLVED) && m->desc.psf_type != LENSGB_PSF_NONE;
@@ -477,10 +527,10 @@ static int image_core(lensgb_model* m, const double* params, int n_inst, const v
         if (m->sub_mask)
             launch_mask(m->hr_img, n_inst, m->grid.ny, m->grid.nx, m->grid.s, m->sub_mask,
                         m->desc.precision, s);
-        if (launch_conv(m->hr_img, m->hr_out, psf, psf_stride, n_inst, m->grid_hr.ny,
-                        m->grid_hr.nx, m->desc.kernel_size,
-                        m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0, m->desc.precision, s))
-            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = model_conv(m, m->hr_img, m->hr_out, psf, psf_stride, n_inst, m->grid_hr.ny,
+                             m->grid_hr.nx, m->desc.kernel_size,
+                             m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0, s)))
+            return conv_fail(rc);
         if ((rc = check_cuda("convolution launch"))) return rc;
         const double area = m->pixel_width * m->pixel_width;
         const int KL = m->desc.low_res_kernel_size;
@@ -497,9 +547,9 @@ static int image_core(lensgb_model* m, const double* params, int n_inst, const v
                       m->desc.precision, s);
         launch_resize(m->hr_img, m->lowres, n_inst, m->grid.ny, m->grid.nx, m->grid.s, 1.0,
                       m->desc.precision, s);
-        if (launch_conv(m->lowres, m->hr_out, klow, psf_stride, n_inst, m->grid.ny, m->grid.nx,
-                        KL, 0, m->desc.precision, s))
-            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = model_conv(m, m->lowres, m->hr_out, klow, psf_stride, n_inst, m->grid.ny,
+                             m->grid.nx, KL, 0, s)))
+            return conv_fail(rc);
         launch_add_scaled(out, m->hr_out, (long long)n_inst * m->grid.nx * m->grid.ny, area,
                           m->desc.precision, s);
         return check_cuda("re-binning launch");
@@ -515,10 +565,10 @@ static int image_core(lensgb_model* m, const double* params, int n_inst, const v
     if (m->sub_mask)
         launch_mask(target, n_inst, m->grid.ny, m->grid.nx, 1, m->sub_mask, m->desc.precision, s);
     if (conv) {
-        if (launch_conv(m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
-                        m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
-                        m->desc.precision, s, m->tune_rows))
-            return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+        if ((rc = model_conv(m, m->lowres, out, psf, psf_stride, n_inst, m->grid.ny, m->grid.nx,
+                             m->desc.kernel_size,
+                             m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0, s, m->tune_rows)))
+            return conv_fail(rc);
         if ((rc = check_cuda("convolution launch"))) return rc;
     }
     return LENSGB_OK;
@@ -1033,11 +1083,20 @@ int lensgb_convolve(const lensgb_model* m, const void* in, int n_inst, const voi
     if (!in || !out || !psf) return fail(LENSGB_ERR_INVALID, "null image or PSF pointer");
     if (in == out) return fail(LENSGB_ERR_INVALID, "in-place convolution is not supported");
     if (psf_stride < 0) return fail(LENSGB_ERR_INVALID, "negative PSF stride");
-    if (launch_conv(in, out, psf, psf_stride, n_inst, m->desc.ny, m->desc.nx,
-                    m->desc.kernel_size, m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
-                    m->desc.precision, (cudaStream_t)stream, m->tune_rows))
-        return fail(LENSGB_ERR_CUDA, "convolution shared-memory configuration failed");
+    const int rc = model_conv(const_cast<lensgb_model*>(m), in, out, psf, psf_stride, n_inst,
+                              m->desc.ny, m->desc.nx, m->desc.kernel_size,
+                              m->desc.psf_type == LENSGB_PSF_GAUSSIAN ? 1 : 0,
+                              (cudaStream_t)stream, m->tune_rows);
+    if (rc) return conv_fail(rc);
     return check_cuda("convolution launch");
+}
+
+int lensgb_model_set_convolution(lensgb_model* m, int method) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (method != LENSGB_CONV_AUTO && method != LENSGB_CONV_DIRECT && method != LENSGB_CONV_FFT)
+        return fail(LENSGB_ERR_INVALID, "method must be LENSGB_CONV_AUTO, _DIRECT or _FFT");
+    m->conv_method = method;
+    return LENSGB_OK;
 }
 
 int lensgb_set_conv_tma(int enable) {

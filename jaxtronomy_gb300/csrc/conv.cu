@@ -363,8 +363,10 @@ static bool raise_smem_limit(const void* fn, size_t smem) {
     size_t& g = granted[std::make_pair(fn, dev)];
     if (smem <= g) return true;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+        cudaSuccess) {
+        cudaGetLastError();  // a refused size leaves no error behind for later calls
         return false;
+    }
     g = smem;
     return true;
 }
@@ -758,6 +760,26 @@ int launch_conv_mixed(const void* in, void* out, const void* kernel, const ConvM
     if (smem > 48 * 1024 && !raise_smem_limit((const void*)conv_f32_kernel<true>, smem)) return -1;
     conv_f32_kernel<true><<<grid, block, smem, stream>>>(fin, (float*)out, fk, 0, 0, 0, 0, edge, cm);
     return 0;
+}
+
+bool direct_conv_fits(int K, int precision) {
+    int dev = 0, limit = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess ||
+        limit <= 0) {
+        cudaGetLastError();
+        limit = 48 * 1024;
+    }
+    size_t smem;
+    if (precision == LENSGB_FP64) {  // run_conv<double, 4, 4, 4>: 32 x 64 tiles
+        const int KP = ((K + 3) / 4) * 4;
+        smem = (size_t)(K * KP + (64 + K - 1) * (32 + KP)) * sizeof(double);
+    } else {  // run_conv_f32 at its tallest tile (64 rows)
+        const int KP = ((K + 7) / 8) * 8;
+        smem = (size_t)(K * KP + (64 + K - 1) * (C32_W + KP + 4)) * sizeof(float);
+    }
+    return smem <= (size_t)limit;
 }
 
 void set_conv_tma(int enable) { g_conv_tma = enable ? 1 : 0; }

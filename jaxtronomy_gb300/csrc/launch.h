@@ -53,6 +53,18 @@ int launch_raytrace(const GridDesc& g, const StackDesc& st, int n_inst, const do
                     cudaStream_t stream, const MixedTab* mixed = nullptr, int mixed_ctas = 0,
                     int ppt = 0);
 
+// "same"-mode convolution by FP64 FFT (fftconv.cu), zero (edge = 0) or edge
+// padding (edge = 1): P (a power of two >= max(ny, nx) + K - 1, plus K - 1 with
+// edge padding; at most 4096) and the scratch it needs; returns 0, -1
+// (shared-memory configuration) or -2 (P above 4096).
+int fft_conv_size(int ny, int nx, int K, int edge);
+size_t fft_conv_scratch_bytes(int n_inst, int ny, int nx, int K, long long kstride, int edge);
+int launch_conv_fft(const void* in, void* out, const void* kernel, long long kstride, int n_inst,
+                    int ny, int nx, int K, int edge, int precision, void* scratch,
+                    cudaStream_t stream);
+// Whether the direct kernels' shared-memory tile fits for a K x K kernel.
+bool direct_conv_fits(int K, int precision);
+
 // FP32 zero-padded uniform convolutions stage their halo tiles with a TMA copy
 // when the images allow it (set_conv_tma(0): plain loads everywhere);
 // conv_wait_timeouts: CTAs whose bounded wait for that copy gave up (synchronous).

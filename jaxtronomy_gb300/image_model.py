@@ -34,6 +34,7 @@ _NUMERICS_KEYS = {
     "supersampling_kernel_size", "flux_evaluate_indexes", "supersampled_indexes",
     "compute_indexes", "point_source_supersampling_factor", "convolution_kernel_size",
     "convolution_type", "truncation_conv", "precision", "fp32_refine_tol", "fp32_refine_kappa",
+    "convolution_method",
 }
 
 
@@ -163,6 +164,15 @@ class ImageModel:
         conv_type = kn.get("convolution_type", "fft")
         if conv_type not in ("fft", "grid", "fft_static"):
             raise ValueError("convolution_type %s not supported!" % conv_type)
+        # how the GPU convolves (an option of this library; every convolution_type
+        # of the reference gives the same image up to rounding): "auto" (the
+        # direct halo-tile kernels, and the FP64 FFT where a kernel is too wide
+        # for their shared-memory tile), "direct" or "fft" (FP64 FFT always; the
+        # faster choice for FP64 models from K ~ 21)
+        method = kn.get("convolution_method", "auto")
+        if method not in _lib.CONV_METHODS:
+            raise ValueError("convolution_method must be one of %s" % sorted(_lib.CONV_METHODS))
+        self._conv_method = _lib.CONV_METHODS[method]
         self._s = s
         self._kwargs_numerics = dict(kwargs_numerics or {})
         if kwargs_pixelbased is not None:
@@ -292,7 +302,7 @@ class ImageModel:
         if key not in self._models:
             refine = self._refine if prec == _lib.FP32_SPLIT else None
             self._models[key] = _lib.Model(self._desc(lens_idx, src_idx, ll_idx, lensed, prec),
-                                           refine, self._subframe)
+                                           refine, self._subframe, self._conv_method)
         return self._models[key]
 
     def refined_pixels(self, stream=None):

@@ -504,15 +504,23 @@ typedef struct {
                                    buckets                                             */
 } lensgb_server_config;
 
+/* One serving request.  psf, data, noise_map, mask and image_out may be host
+ * memory (pageable: staged through page-locked buffers; page-locked: read and
+ * written by the device in place) or memory of the server's device, which
+ * stays resident across requests -- the form of ImageData.update_data /
+ * ImageNoise.C_D_model keeping a model's data on the device
+ * (jaxtronomy/Data/imaging_data.py:135-157, image_noise.py:100-110): the gather
+ * kernels read it where it is, with no host copy per batch.  A request whose
+ * PSF is in device memory runs in an exact-model bucket. */
 typedef struct {
     lensgb_model_desc desc;     /* the request's model (its bucket key)                    */
     const double* params;       /* host: lensgb_model_param_count doubles (one system row) */
-    const void* psf;            /* host: kernel_size^2 values in the model precision       */
-    void* image_out;            /* host: ny x nx result in the model precision, or NULL;
-                                   page-locked buffers receive asynchronous copies          */
-    const double* data;         /* host, optional: ny x nx data -> likelihood request      */
-    const double* noise_map;    /* host, optional with data: ny x nx 1-sigma noise map     */
-    const double* mask;         /* host, optional with data: ny x nx likelihood mask       */
+    const void* psf;            /* kernel_size^2 values in the model precision             */
+    void* image_out;            /* ny x nx result in the model precision, or NULL;
+                                   page-locked / device buffers are written by the device  */
+    const double* data;         /* optional: ny x nx data -> likelihood request            */
+    const double* noise_map;    /* optional with data: ny x nx 1-sigma noise map           */
+    const double* mask;         /* optional with data: ny x nx likelihood mask             */
     double background_rms;      /* with data (part of the bucket key)                      */
     double exposure_time;       /* with data (part of the bucket key)                      */
     double* logl_out;           /* host, optional with data: log-likelihood                */
@@ -523,6 +531,7 @@ typedef struct {
 #define LENSGB_REQ_RUNNING 1
 #define LENSGB_REQ_DONE 2
 #define LENSGB_REQ_FAILED 3
+#define LENSGB_REQ_CANCELLED 4
 
 typedef struct {
     long long batches;
@@ -548,7 +557,15 @@ int lensgb_server_submit(lensgb_server* server, const lensgb_request* requests, 
                          long long* tickets);
 /* *state = LENSGB_REQ_*; returns the request's error code once it FAILED. */
 int lensgb_server_poll(lensgb_server* server, long long ticket, int* state);
-/* Polls until the request is done or failed, or timeout_s elapses. */
+/* Withdraws a request that has not been admitted to a batch yet: *cancelled = 1
+ * and the request ends in state LENSGB_REQ_CANCELLED (it never runs and its
+ * buffers are not touched again); *cancelled = 0 when it is already running or
+ * finished.  A request the server cannot fit in hbm_budget_bytes even with
+ * every idle context evicted and nothing in flight ends FAILED with
+ * LENSGB_ERR_OOM. */
+int lensgb_server_cancel(lensgb_server* server, long long ticket, int* cancelled);
+/* Polls until the request is done, failed or cancelled, or timeout_s elapses
+ * (then returns LENSGB_OK with the state it has). */
 int lensgb_server_wait(lensgb_server* server, long long ticket, double timeout_s, int* state);
 /* Waits until every submitted request is done or failed. */
 int lensgb_server_drain(lensgb_server* server, double timeout_s);

@@ -52,6 +52,7 @@ SYMBOLS = [
     "lensgb_bulk_ray_shooting", "lensgb_bulk_multi_plane_ray_shooting",
     "lensgb_loglike_image", "lensgb_point_sources_add", "lensgb_hessian",
     "lensgb_server_create", "lensgb_server_submit", "lensgb_server_poll", "lensgb_server_wait",
+    "lensgb_server_cancel",
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
     "lensgb_fma_chain", "lensgb_set_conv_tma", "lensgb_wait_timeouts",
@@ -158,7 +159,7 @@ class ServerStats(ctypes.Structure):
         "mixed_batches")]
 
 
-REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
 
 LINEAR_MAX, LINEAR_INVERSE, LINEAR_POSITIVE = 8, 1, 2
 
@@ -260,6 +261,8 @@ def load():
     lib.lensgb_server_poll.restype = i
     lib.lensgb_server_wait.argtypes = [vp, ll, ctypes.c_double, ctypes.POINTER(i)]
     lib.lensgb_server_wait.restype = i
+    lib.lensgb_server_cancel.argtypes = [vp, ll, ctypes.POINTER(i)]
+    lib.lensgb_server_cancel.restype = i
     lib.lensgb_server_drain.argtypes = [vp, ctypes.c_double]
     lib.lensgb_server_drain.restype = i
     lib.lensgb_server_clock_ns.argtypes = [vp]

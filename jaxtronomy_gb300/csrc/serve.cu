@@ -54,8 +54,10 @@ struct Req {
     int bucket = -1;
     std::atomic<int> state{LENSGB_REQ_QUEUED};
     int rc = LENSGB_OK;
-    bool out_pinned = false;  // image_out is page-locked: the device writes it directly
-    int in_pinned = 0;        // bits 0..2: data / noise_map / mask are page-locked
+    bool out_pinned = false;  // image_out is device-readable (page-locked host or device
+                              // memory): the device writes it directly
+    int in_pinned = 0;        // bits 0..2: data / noise_map / mask, bit 4: psf are
+                              // device-readable, read in place by the gather kernels
     long long npix = 0;       // ny x nx of the request's grid
     int k2 = 0;               // PSF elements of the request
     long long t_submit = 0, t_release = 0, t_admit = 0, t_done = 0;
@@ -66,9 +68,11 @@ struct BucketKey {
     int likelihood;      // 0: image only; 1: image + logL
     int has_noise, has_mask;
     double background_rms, exposure_time;
+    int psf_on_device;   // PSFs in device memory: exact-model buckets gather them in place
     bool operator<(const BucketKey& o) const {
         int c = memcmp(&desc, &o.desc, sizeof desc);
         if (c) return c < 0;
+        if (psf_on_device != o.psf_on_device) return psf_on_device < o.psf_on_device;
         if (likelihood != o.likelihood) return likelihood < o.likelihood;
         if (has_noise != o.has_noise) return has_noise < o.has_noise;
         if (has_mask != o.has_mask) return has_mask < o.has_mask;
@@ -76,6 +80,9 @@ struct BucketKey {
         return exposure_time < o.exposure_time;
     }
 };
+
+// Pointer-table planes of a context: image outputs, data, noise map, mask, PSF.
+constexpr int PTR_PLANES = 5, PSF_PLANE = 4;
 
 struct Context {
     int bucket = -1;
@@ -99,7 +106,7 @@ struct Context {
     unsigned char* img_host = nullptr;  // pinned staging for pageable caller buffers
     unsigned char* in_host = nullptr;   // pinned staging of pageable data / noise / mask
     void** ptr_host = nullptr;          // pinned pointer tables: out[cap], data, noise, mask,
-    void** ptr_dev = nullptr;           // then (mixed buckets) cap + 1 image byte offsets
+    void** ptr_dev = nullptr;           // psf, then (mixed buckets) cap + 1 image byte offsets
     long long* boff_host = nullptr;     // the byte-offset part of ptr_host / ptr_dev
     long long* boff_dev = nullptr;
     // mixed buckets: one page-locked staging block -- rows | PSFs | output
@@ -288,7 +295,7 @@ int grow_context(lensgb_server* s, Context* c, const Need& d) {
     s->bytes_held -= c->bytes;
     c->bytes = 0;
     const size_t P = (size_t)b.n_params, np = (size_t)pix_cap, nk = (size_t)kel_cap;
-    const size_t ptr_bytes = (size_t)cap * 4 * sizeof(void*) + ((size_t)cap + 1) * 8;
+    const size_t ptr_bytes = (size_t)cap * PTR_PLANES * sizeof(void*) + ((size_t)cap + 1) * 8;
     bool ok;
     if (b.mixed) {
         auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -337,8 +344,8 @@ int grow_context(lensgb_server* s, Context* c, const Need& d) {
         free_context_buffers(c);
         return LENSGB_ERR_OOM;
     }
-    c->boff_host = (long long*)(c->ptr_host + (size_t)cap * 4);
-    c->boff_dev = (long long*)(c->ptr_dev + (size_t)cap * 4);  // in the staging block when mixed
+    c->boff_host = (long long*)(c->ptr_host + (size_t)cap * PTR_PLANES);
+    c->boff_dev = (long long*)(c->ptr_dev + (size_t)cap * PTR_PLANES);  // staging block when mixed
     c->cap = cap;
     c->pix_cap = pix_cap;
     c->kel_cap = kel_cap;
@@ -449,11 +456,14 @@ int launch_batch(lensgb_server* s, Context* c, int n) {
     const int planes = b.key.likelihood ? 1 + b.key.has_noise + b.key.has_mask : 0;
     if (cudaMemcpyAsync(c->rows_dev, c->rows_host, n * P * 8, cudaMemcpyHostToDevice, st) !=
             cudaSuccess ||
-        (b.k2 > 0 && cudaMemcpyAsync(c->psf_dev, c->psf_host, n * (size_t)b.k2 * b.esz,
-                                     cudaMemcpyHostToDevice, st) != cudaSuccess) ||
-        cudaMemcpyAsync(c->ptr_dev, c->ptr_host, (size_t)c->cap * (1 + planes) * sizeof(void*),
+        cudaMemcpyAsync(c->ptr_dev, c->ptr_host, (size_t)c->cap * PTR_PLANES * sizeof(void*),
                         cudaMemcpyHostToDevice, st) != cudaSuccess)
         return LENSGB_ERR_CUDA;
+    // PSFs gathered through the table: device-resident ones in place, host ones
+    // from their pinned staging slots
+    if (b.k2 > 0)
+        table_copy((unsigned char*)c->psf_dev, c->ptr_dev + (size_t)PSF_PLANE * c->cap,
+                   (size_t)b.k2 * b.esz, n, 0, st);
     int rc;
     if (!b.key.likelihood) {
         rc = lensgb_image(c->model, c->rows_dev, n, c->psf_dev, b.k2, c->img_dev, 0, st);
@@ -607,7 +617,14 @@ int run_batch(lensgb_server* s, Context* c, int n) {
         const Req* q = c->batch[i];
         const lensgb_request& r = q->r;
         memcpy(c->rows_host + i * P, r.params, P * 8);
-        if (b.k2 > 0) memcpy(c->psf_host + i * (size_t)b.k2 * b.esz, r.psf, (size_t)b.k2 * b.esz);
+        if (b.k2 > 0) {
+            void* kp = (void*)r.psf;
+            if (!(q->in_pinned & 16)) {
+                kp = c->psf_host + i * (size_t)b.k2 * b.esz;
+                memcpy(kp, r.psf, (size_t)b.k2 * b.esz);
+            }
+            c->ptr_host[(size_t)PSF_PLANE * c->cap + i] = kp;
+        }
         c->ptr_host[i] = (r.image_out && q->out_pinned) ? r.image_out : (void*)(c->img_host + i * ib);
         const void* src[3] = {r.data, r.noise_map, r.mask};
         const bool use[3] = {true, b.key.has_noise != 0, b.key.has_mask != 0};
@@ -652,9 +669,35 @@ void finish_batch(lensgb_server* s, Context* c, int rc) {
     s->inflight--;
 }
 
+// Ends the first m queued requests of a bucket with status rc (FAILED), except
+// those a caller cancelled meanwhile (already ended and counted).
+void fail_head(lensgb_server* s, Bucket& b, int m, int rc) {
+    for (int i = 0; i < m && !b.queue.empty(); ++i) {
+        Req* q = b.queue.front();
+        b.queue.pop_front();
+        int expected = LENSGB_REQ_QUEUED;
+        if (!q->state.compare_exchange_strong(expected, LENSGB_REQ_RUNNING,
+                                              std::memory_order_acq_rel))
+            continue;
+        q->rc = rc;
+        q->t_done = s->now();
+        q->state.store(LENSGB_REQ_FAILED, std::memory_order_release);
+        s->n_done++;
+    }
+}
+
+// Drops cancelled requests from the front of every bucket queue.
+void drop_cancelled(lensgb_server* s) {
+    for (Bucket* b : s->wb)
+        while (!b->queue.empty() &&
+               b->queue.front()->state.load(std::memory_order_acquire) == LENSGB_REQ_CANCELLED)
+            b->queue.pop_front();
+}
+
 // Pick the bucket whose oldest waiting request is oldest and that can get a
 // context; form and launch one batch.  Returns false if nothing was launched.
 bool launch_one(lensgb_server* s) {
+    drop_cancelled(s);
     int best = -1;
     long long best_t = 0;
     for (size_t k = 0; k < s->wb.size(); ++k) {
@@ -689,17 +732,19 @@ bool launch_one(lensgb_server* s) {
     }
     auto need = [&](int m) { return Need{m, pp[(size_t)m], pk[(size_t)m]}; };
     if (!c) {
-        if (!make_room(s, context_bytes(b, need(n)), nullptr)) return false;  // wait for memory
+        if (!make_room(s, context_bytes(b, need(n)), nullptr) &&
+            !make_room(s, context_bytes(b, need(1)), nullptr)) {
+            if (s->inflight > 0) return false;  // wait for memory
+            // nothing in flight can free memory and no idle context is left to
+            // evict: the head request can never fit the budget (in a uniform
+            // bucket, neither can any other of its queue)
+            fail_head(s, b, b.mixed ? 1 : (int)b.queue.size(), LENSGB_ERR_OOM);
+            return true;
+        }
         c = new_context(s, best);
         if (!c) {
             // cannot build the model: fail the queued requests of this bucket
-            for (Req* q : b.queue) {
-                q->rc = LENSGB_ERR_UNSUPPORTED;
-                q->t_done = s->now();
-                q->state.store(LENSGB_REQ_FAILED, std::memory_order_release);
-                s->n_done++;
-            }
-            b.queue.clear();
+            fail_head(s, b, (int)b.queue.size(), LENSGB_ERR_UNSUPPORTED);
             return true;
         }
     }
@@ -711,15 +756,7 @@ bool launch_one(lensgb_server* s) {
         if (c->cap == 0 && s->inflight == 0) {
             // nothing in flight can free memory: the request can never fit (in a
             // uniform bucket, neither can any other of its queue)
-            const int m = b.mixed ? 1 : (int)b.queue.size();
-            for (int i = 0; i < m; ++i) {
-                Req* q = b.queue.front();
-                b.queue.pop_front();
-                q->rc = LENSGB_ERR_OOM;
-                q->t_done = s->now();
-                q->state.store(LENSGB_REQ_FAILED, std::memory_order_release);
-                s->n_done++;
-            }
+            fail_head(s, b, b.mixed ? 1 : (int)b.queue.size(), LENSGB_ERR_OOM);
             return true;
         }
         return false;
@@ -731,10 +768,16 @@ bool launch_one(lensgb_server* s) {
     for (int i = 0; i < nb; ++i) {
         Req* q = b.queue.front();
         b.queue.pop_front();
+        // admission and lensgb_server_cancel race for the QUEUED state
+        int expected = LENSGB_REQ_QUEUED;
+        if (!q->state.compare_exchange_strong(expected, LENSGB_REQ_RUNNING,
+                                              std::memory_order_acq_rel))
+            continue;  // cancelled
         q->t_admit = t;
-        q->state.store(LENSGB_REQ_RUNNING, std::memory_order_release);
         c->batch.push_back(q);
     }
+    nb = (int)c->batch.size();
+    if (nb == 0) return true;  // every request of the head was cancelled
     c->busy = true;
     c->last_used = t;
     s->inflight++;
@@ -802,26 +845,41 @@ void worker_main(lensgb_server* s) {
         }
 }
 
-// Page-locked (cudaHostAlloc / registered) host memory, which the device can
-// read and write through the same address.
-bool is_pinned(const void* p) {
+// Memory the server's device reads and writes through the same address:
+// page-locked (cudaHostAlloc / registered) host memory, managed memory, or
+// device memory of that device (inputs kept resident on the GPU by the caller).
+bool device_readable(const void* p, int device) {
     cudaPointerAttributes pa;
-    const bool ok = cudaPointerGetAttributes(&pa, p) == cudaSuccess &&
-                    pa.type == cudaMemoryTypeHost && pa.devicePointer == p;
+    bool ok = false;
+    if (cudaPointerGetAttributes(&pa, p) == cudaSuccess) {
+        ok = (pa.type == cudaMemoryTypeHost && pa.devicePointer == p) ||
+             pa.type == cudaMemoryTypeManaged ||
+             (pa.type == cudaMemoryTypeDevice && pa.device == device);
+    }
     cudaGetLastError();
     return ok;
 }
 
-// Requests that a mixed bucket can take: image only, no supersampled convolution.
-bool mixable(const lensgb_server* s, const lensgb_request& r) {
-    return s->cfg.mixed_grids && !r.data &&
+bool on_device(const void* p) {
+    cudaPointerAttributes pa;
+    const bool ok = cudaPointerGetAttributes(&pa, p) == cudaSuccess &&
+                    pa.type == cudaMemoryTypeDevice;
+    cudaGetLastError();
+    return ok;
+}
+
+// Requests that a mixed bucket can take: image only, no supersampled
+// convolution, PSF in host memory.
+bool mixable(const lensgb_server* s, const lensgb_request& r, bool psf_dev) {
+    return s->cfg.mixed_grids && !r.data && !psf_dev &&
            !(r.desc.supersampling_convolution && r.desc.supersampling > 1);
 }
 
-int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
+int bucket_for(lensgb_server* s, const lensgb_request& r, bool psf_dev, int* out) {
     BucketKey k;
     memset(&k, 0, sizeof k);
     k.desc = r.desc;
+    k.psf_on_device = psf_dev ? 1 : 0;
     k.likelihood = r.data ? 1 : 0;
     k.has_noise = r.data && r.noise_map ? 1 : 0;
     k.has_mask = r.data && r.mask ? 1 : 0;
@@ -838,7 +896,7 @@ int bucket_for(lensgb_server* s, const lensgb_request& r, int* out) {
     if (rc) return serr(rc, std::string("request model: ") + lensgb_last_error());
     const int n_params = lensgb_model_param_count(m);
     lensgb_model_destroy(m);
-    const bool mixed = mixable(s, r);
+    const bool mixed = mixable(s, r, psf_dev);
     BucketKey bk = k;
     if (mixed) {
         // the bucket's model: the request's profile stack, precision, PSF type
@@ -925,8 +983,13 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
             return serr(LENSGB_ERR_INVALID, "likelihood request needs exposure_time > 0");
         const void* in[3] = {r.data, r.noise_map, r.mask};
         for (int k = 0; k < 3; ++k)
-            if (in[k] && is_pinned(in[k])) pinned[(size_t)i] |= 1 << k;
-        if (r.image_out && is_pinned(r.image_out)) pinned[(size_t)i] |= 8;
+            if (in[k] && device_readable(in[k], s->device)) pinned[(size_t)i] |= 1 << k;
+        if (r.image_out && device_readable(r.image_out, s->device)) pinned[(size_t)i] |= 8;
+        if (r.psf && on_device(r.psf)) {
+            if (!device_readable(r.psf, s->device))
+                return serr(LENSGB_ERR_INVALID, "PSF kernel in another device's memory");
+            pinned[(size_t)i] |= 16 | 32;  // 32: the PSF is in device memory
+        }
     }
     // enqueue in chunks, so that a large submission does not stall the worker
     constexpr int CHUNK = 256;
@@ -936,7 +999,7 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
         for (int i = i0; i < n && i < i0 + CHUNK; ++i) {
             const lensgb_request& r = reqs[i];
             int bucket = -1;
-            int rc = bucket_for(s, r, &bucket);
+            int rc = bucket_for(s, r, (pinned[(size_t)i] & 32) != 0, &bucket);
             if (rc) return rc;
             s->reqs.emplace_back();
             Req& q = s->reqs.back();
@@ -946,7 +1009,7 @@ int lensgb_server_submit(lensgb_server* s, const lensgb_request* reqs, int n, lo
             q.t_submit = t;
             q.t_release = r.release_ns > t ? r.release_ns : t;
             q.out_pinned = (pinned[(size_t)i] & 8) != 0;
-            q.in_pinned = pinned[(size_t)i] & 7;
+            q.in_pinned = pinned[(size_t)i] & 23;
             q.npix = (long long)r.desc.nx * r.desc.ny;
             q.k2 = r.desc.psf_type == LENSGB_PSF_NONE
                        ? 0
@@ -973,12 +1036,33 @@ int lensgb_server_poll(lensgb_server* s, long long ticket, int* state) {
     return *state == LENSGB_REQ_FAILED ? q->rc : LENSGB_OK;
 }
 
+int lensgb_server_cancel(lensgb_server* s, long long ticket, int* cancelled) {
+    if (!s) return serr(LENSGB_ERR_INVALID, "null server");
+    Req* q;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (ticket < 0 || ticket >= (long long)s->reqs.size())
+            return serr(LENSGB_ERR_INVALID, "unknown ticket");
+        q = &s->reqs[(size_t)ticket];
+    }
+    int expected = LENSGB_REQ_QUEUED;
+    const bool ok = q->state.compare_exchange_strong(expected, LENSGB_REQ_CANCELLED,
+                                                     std::memory_order_acq_rel);
+    if (ok) {
+        q->t_done = s->now();
+        s->n_done++;
+        s->cv.notify_one();
+    }
+    if (cancelled) *cancelled = ok ? 1 : 0;
+    return LENSGB_OK;
+}
+
 int lensgb_server_wait(lensgb_server* s, long long ticket, double timeout_s, int* state) {
     if (!s || !state) return serr(LENSGB_ERR_INVALID, "null server or state");
     const auto until = Clock::now() + std::chrono::duration<double>(timeout_s);
     for (;;) {
         int rc = lensgb_server_poll(s, ticket, state);
-        if (rc || *state == LENSGB_REQ_DONE) return rc;
+        if (rc || *state == LENSGB_REQ_DONE || *state == LENSGB_REQ_CANCELLED) return rc;
         if (Clock::now() > until) return LENSGB_OK;
         std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
@@ -1011,7 +1095,8 @@ int lensgb_server_request_times(lensgb_server* s, long long ticket, long long* r
     }
     const int st = q->state.load(std::memory_order_acquire);
     if (release_ns) *release_ns = q->t_release;
-    if (admit_ns) *admit_ns = st >= LENSGB_REQ_RUNNING ? q->t_admit : -1;
+    if (admit_ns)
+        *admit_ns = st >= LENSGB_REQ_RUNNING && st != LENSGB_REQ_CANCELLED ? q->t_admit : -1;
     if (done_ns) *done_ns = st >= LENSGB_REQ_DONE ? q->t_done : -1;
     return LENSGB_OK;
 }

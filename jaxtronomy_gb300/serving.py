@@ -41,12 +41,25 @@ class Ticket:
     def done(self):
         return self.state() == _lib.REQ_DONE
 
+    def cancel(self):
+        """Withdraws the request if no batch has taken it yet; True if it will not
+        run (state REQ_CANCELLED), False if it is already running or finished."""
+        self.server._check_open()
+        c = ctypes.c_int(0)
+        _lib.check(_lib.load().lensgb_server_cancel(self.server._h, self.ticket,
+                                                    ctypes.byref(c)))
+        if c.value:
+            self._keep = None
+        return bool(c.value)
+
     def result(self, timeout=60.0):
         """Waits for the request; returns the image (and logL for likelihood requests)."""
         self.server._check_open()
         st = ctypes.c_int(0)
         _lib.check(_lib.load().lensgb_server_wait(self.server._h, self.ticket, float(timeout),
                                                   ctypes.byref(st)))
+        if st.value == _lib.REQ_CANCELLED:
+            raise RuntimeError("request %d was cancelled" % self.ticket)
         if st.value != _lib.REQ_DONE:
             raise TimeoutError("request %d not done after %.1f s" % (self.ticket, timeout))
         self._keep = None
@@ -91,9 +104,14 @@ class Server:
     def request(self, image_model, kwargs_lens=None, kwargs_source=None, kwargs_lens_light=None,
                 psf_kernel=None, data=None, noise_map=None, mask=None, release_s=None,
                 out=None):
-        """Builds (without submitting) one request and the host buffers it names.
+        """Builds (without submitting) one request and the buffers it names.
         ``data`` makes it a likelihood request using the model's ImageData
-        ``background_rms`` / ``exposure_time``.  Returns (Request, keep, image, logl)."""
+        ``background_rms`` / ``exposure_time``.  ``psf_kernel``, ``data``,
+        ``noise_map``, ``mask`` and ``out`` may be CUDA tensors on the server's
+        device (contiguous, float64 for data / noise / mask, the model's dtype
+        for the PSF -- already in :meth:`ImageModel.pack_psf` layout -- and the
+        image): they stay resident and are read or written in place, with no
+        host copy per batch.  Returns (Request, keep, image, logl)."""
         if getattr(image_model, "_n_ps", 0):
             raise ValueError("serving requests with point sources are not supported")
         if getattr(image_model, "_subframe", None) is not None:
@@ -110,38 +128,59 @@ class Server:
         req.desc = model.desc
         req.params = keep[0].ctypes.data
         if image_model._psf_type != _lib.PSF_NONE:
-            k = image_model._kernel if psf_kernel is None else psf_kernel
-            if np.shape(k) != image_model._kernel.shape:
-                raise ValueError("psf kernel must have shape %s" % (image_model._kernel.shape,))
-            k = np.ascontiguousarray(image_model.pack_psf(k), dtype=np_dtype)
-            keep.append(k)
-            req.psf = k.ctypes.data
+            if isinstance(psf_kernel, torch.Tensor) and psf_kernel.is_cuda:
+                tdt = torch.float64 if np_dtype == np.float64 else torch.float32
+                if (psf_kernel.dtype != tdt or not psf_kernel.is_contiguous()
+                        or psf_kernel.numel() != image_model.psf_elements()):
+                    raise ValueError("a device PSF must be a contiguous %s tensor of %d values "
+                                     "(ImageModel.pack_psf layout)"
+                                     % (tdt, image_model.psf_elements()))
+                keep.append(psf_kernel)
+                req.psf = psf_kernel.data_ptr()
+            else:
+                k = image_model._kernel if psf_kernel is None else psf_kernel
+                if np.shape(k) != image_model._kernel.shape:
+                    raise ValueError("psf kernel must have shape %s"
+                                     % (image_model._kernel.shape,))
+                k = np.ascontiguousarray(image_model.pack_psf(k), dtype=np_dtype)
+                keep.append(k)
+                req.psf = k.ctypes.data
         shape = (image_model._nx, image_model._ny)
         if out is None:
             out = np.empty(shape, dtype=np_dtype)
+        elif isinstance(out, torch.Tensor):
+            tdt = torch.float64 if np_dtype == np.float64 else torch.float32
+            if out.dtype != tdt or tuple(out.shape) != shape or not out.is_contiguous():
+                raise ValueError("out must be a contiguous %s tensor of shape %s" % (tdt, shape))
         elif out.dtype != np_dtype or out.shape != shape or not out.flags.c_contiguous:
             raise ValueError("out must be a contiguous %s array of shape %s" % (np_dtype, shape))
         req.image_out = out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()
+
+        def plane(x, what):
+            # a (ny, nx) float64 input: a resident CUDA tensor, or host memory
+            if isinstance(x, torch.Tensor) and x.is_cuda:
+                if x.dtype != torch.float64 or tuple(x.shape) != shape or not x.is_contiguous():
+                    raise ValueError("%s must be a contiguous float64 tensor of shape %s"
+                                     % (what, shape))
+                keep.append(x)
+                return x.data_ptr()
+            a = np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), shape))
+            keep.append(a)
+            return a.ctypes.data
         logl = None
         if data is not None:
-            d = np.ascontiguousarray(data, dtype=np.float64)
-            if d.shape != shape:
+            if not (isinstance(data, torch.Tensor) and data.is_cuda) and np.shape(data) != shape:
                 raise ValueError("data must have shape %s" % (shape,))
-            keep.append(d)
-            req.data = d.ctypes.data
+            req.data = plane(data, "data")
             D = image_model.Data
             if noise_map is None:
                 noise_map = D.noise_map
             if mask is None and not np.all(image_model.likelihood_mask == 1):
                 mask = image_model.likelihood_mask
             if noise_map is not None:
-                nm = np.ascontiguousarray(np.broadcast_to(noise_map, shape), dtype=np.float64)
-                keep.append(nm)
-                req.noise_map = nm.ctypes.data
+                req.noise_map = plane(noise_map, "noise_map")
             if mask is not None:
-                mk = np.ascontiguousarray(np.broadcast_to(mask, shape), dtype=np.float64)
-                keep.append(mk)
-                req.mask = mk.ctypes.data
+                req.mask = plane(mask, "mask")
             em = D.exposure_map
             if noise_map is None and em is None:
                 raise ValueError("likelihood requests need an exposure time or a noise map")

@@ -13,6 +13,8 @@ the image maximum, and a request served alone and in a mix must agree bit for
 bit in both modes.
 """
 
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -172,3 +174,106 @@ def test_bad_request_is_rejected_at_submit(cuda):
         req.desc.supersampling = 0
         with pytest.raises(Exception):
             srv.submit_requests([(req, keep, out, logl)])
+
+
+# ---------------------------------------------------------------------------
+# failure paths, cancellation and device-resident inputs
+# ---------------------------------------------------------------------------
+
+def test_request_over_the_hbm_budget_fails_with_oom(cuda):
+    """A request whose context cannot fit hbm_budget_bytes, with nothing in flight
+    and nothing left to evict, ends FAILED with LENSGB_ERR_OOM instead of
+    waiting forever; a later request that fits is still served."""
+    from jaxtronomy_gb300 import _lib
+    reqs, psfs = W.serving_stream(seed=13, n=40, sides=(100,), supersampling=(2,),
+                                  kernel_sizes=(11,), psf_pool=2)
+    models = _models(reqs[:1])
+    with serving.Server(n_streams=1, max_batch=4, hbm_budget_bytes=64 << 10,
+                        mixed_grids=False) as srv:
+        t = _submit(srv, models, reqs[:1], psfs)[0]
+        st = ctypes.c_int(0)
+        rc = _lib.load().lensgb_server_wait(srv._h, t.ticket, 30.0, ctypes.byref(st))
+        assert rc == _lib.ERR_OOM and st.value == _lib.REQ_FAILED
+        with pytest.raises(_lib.LensgbError):
+            t.result()
+        assert srv.stats()["requests_done"] == 1
+    small, spsf = _stream(4)
+    sm = _models(small)
+    with serving.Server(n_streams=1, max_batch=4, hbm_budget_bytes=64 << 20) as srv:
+        ok = _submit(srv, sm, small, spsf)
+        for r, tk in zip(small, ok):
+            _check(tk.result(), _alone(sm, r, spsf), True)
+
+
+def test_wait_times_out_without_blocking_and_cancel(cuda):
+    """A request released 30 s in the future: a wait with a 50 ms timeout returns
+    (TimeoutError from Ticket.result) without blocking; cancelling it ends it
+    CANCELLED before it ever runs, and the server drains at once.  A request
+    that has finished cannot be cancelled."""
+    import time as _time
+    from jaxtronomy_gb300 import _lib
+    reqs, psfs = _stream(3, seed=17)
+    models = _models(reqs)
+    with serving.Server(n_streams=1, max_batch=4) as srv:
+        later = _submit(srv, models, reqs[:1], psfs, release=[srv.clock() + 30.0])[0]
+        t0 = _time.perf_counter()
+        with pytest.raises(TimeoutError):
+            later.result(timeout=0.05)
+        assert _time.perf_counter() - t0 < 2.0
+        assert later.state() == _lib.REQ_QUEUED
+        assert later.cancel() is True
+        assert later.state() == _lib.REQ_CANCELLED
+        with pytest.raises(RuntimeError):
+            later.result(timeout=1.0)
+        assert later.times()[1] == -1  # never admitted
+        now = _submit(srv, models, reqs[1:2], psfs)[0]
+        img = now.result()
+        assert now.cancel() is False
+        srv.drain(10.0)
+        _check(img, _alone(models, reqs[1], psfs), True)
+        assert srv.stats()["requests_done"] == 2
+
+
+@pytest.mark.parametrize("on_device", ["psf", "data", "all"])
+def test_device_resident_inputs_equal_host_inputs(cuda, on_device):
+    """Likelihood requests whose PSF, data, noise map and mask (and output image)
+    are CUDA tensors kept on the device: the gather kernels read them in place,
+    and the results equal the host-buffer requests and likelihood_batch bit for
+    bit."""
+    reqs, psfs = _stream(12, seed=19)
+    rng = np.random.default_rng(5)
+    models = _models(reqs)
+    host, dev = [], []
+    for r in reqs:
+        img = _alone(models, r, psfs).astype(np.float64)
+        d = img + rng.normal(0, 0.01, img.shape)
+        nm = np.full(img.shape, 0.012)
+        mk = (rng.random(img.shape) > 0.1).astype(np.float64)
+        host.append((d, nm, mk))
+    with serving.Server(n_streams=2, max_batch=8) as srv:
+        bh, bd = [], []
+        for r, (d, nm, mk) in zip(reqs, host):
+            im = models[r["key"]]
+            kern = psfs[r["key"][2]][r["psf"]]
+            bh.append(srv.request(im, r["kwargs_lens"], r["kwargs_source"],
+                                  r["kwargs_lens_light"], psf_kernel=kern, data=d,
+                                  noise_map=nm, mask=mk))
+            dt = torch.float32
+            kd = (torch.as_tensor(im.pack_psf(kern), dtype=dt).cuda().contiguous()
+                  if on_device in ("psf", "all") else kern)
+            dd, nmd, mkd = ((torch.as_tensor(x).cuda().contiguous() for x in (d, nm, mk))
+                            if on_device in ("data", "all") else (d, nm, mk))
+            out = (torch.empty((r["key"][0],) * 2, dtype=dt, device="cuda")
+                   if on_device == "all" else None)
+            bd.append(srv.request(im, r["kwargs_lens"], r["kwargs_source"],
+                                  r["kwargs_lens_light"], psf_kernel=kd, data=dd, noise_map=nmd,
+                                  mask=mkd, out=out))
+        th = srv.submit_requests(bh)
+        td = srv.submit_requests(bd)
+        srv.drain(120)
+        for r, (d, nm, mk), a, b in zip(reqs, host, th, td):
+            ia, la = a.result()
+            ib, lb = b.result()
+            ib = ib.cpu().numpy() if isinstance(ib, torch.Tensor) else ib
+            assert la == lb
+            np.testing.assert_array_equal(ia, ib)

@@ -287,6 +287,7 @@ def fma_peaks(reps=5):
     out = {"sms": sms, "blocks": blocks, "threads_per_block": 256, "chains_per_thread": 8}
     stream = torch.cuda.current_stream()
     for name, prec, iters, dtype in (("fp32", _lib.FP32_SPLIT, 65536, torch.float32),
+                                     ("fp32_pairs", 2, 32768, torch.float32),
                                      ("fp64", _lib.FP64, 1024, torch.float64)):
         buf = torch.empty(blocks * 256, dtype=dtype, device="cuda")
         flops = ctypes.c_longlong(0)

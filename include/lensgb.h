@@ -583,13 +583,15 @@ int lensgb_server_destroy(lensgb_server* server);
 const char* lensgb_last_error(void);
 
 /* FMA-rate probe.  No counterpart in the reference: it measures the device's
- * FP32 (precision LENSGB_FP32_SPLIT) or FP64 (LENSGB_FP64) fused multiply-add
- * rate, the peak against which the roofline fractions of the compute-bound
- * kernels are stated.  Launches `blocks` CTAs of 256 threads, each running 8
+ * FP32 (precision LENSGB_FP32_SPLIT), FP64 (LENSGB_FP64) or packed-pair FP32
+ * (LENSGB_FP32_PAIRS: fma.rn.f32x2, two FMAs per instruction) fused
+ * multiply-add rate, the peak against which the roofline fractions of the
+ * compute-bound kernels are stated.  Launches `blocks` CTAs of 256 threads, each running 8
  * independent chains of `iters` FMAs (iters a multiple of 16), and writes one
  * value per thread to out_dev (blocks x 256 elements of that precision).
  * *flops receives the launch's flop count (2 per FMA); time the launch with
  * events on `stream`. */
+#define LENSGB_FP32_PAIRS 2
 int lensgb_fma_chain(int precision, int blocks, int iters, void* out_dev, long long* flops,
                      void* stream);
 

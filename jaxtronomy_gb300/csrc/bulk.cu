@@ -15,9 +15,19 @@
 
 namespace lensgb {
 
+// Launch shapes (compile-time; -D overrides serve shape sweeps).
+#ifndef LENSGB_BULK_RPT
+#define LENSGB_BULK_RPT 2
+#endif
+#ifndef LENSGB_MP_RPT
+#define LENSGB_MP_RPT 3
+#endif
+#ifndef LENSGB_MP_MAXNREG
+#define LENSGB_MP_MAXNREG 160
+#endif
 constexpr int BULK_CHUNK = 64;
 constexpr int BULK_THREADS = 256;
-constexpr int BULK_RPT = 2;  // rays per thread (i and i + BULK_THREADS of the CTA span)
+constexpr int BULK_RPT = LENSGB_BULK_RPT;  // rays per thread (i, i + BULK_THREADS, ...)
 
 template <bool F32>
 __global__ void __launch_bounds__(BULK_THREADS)
@@ -148,7 +158,7 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
 // FP64 from an FP64 offset, both summed as FP32 pairs.
 // ---------------------------------------------------------------------------
 constexpr int MP_THREADS = 64;
-constexpr int MP_RPT = 3;
+constexpr int MP_RPT = LENSGB_MP_RPT;
 constexpr int MP_CHUNK = 64;
 constexpr int PL_F = 8;  // per-step floats: dT hi/lo, 1/T_z hi/lo, eps, r2p hi/lo, tag bits
 
@@ -235,7 +245,7 @@ __device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl,
 // threads) is resident in one wave at 6 CTAs per SM with no spills; fewer
 // registers made the compiler rebuild ray state in FP64 or spill.
 template <bool F32>
-__global__ void __maxnreg__(160)
+__global__ void __maxnreg__(LENSGB_MP_MAXNREG)
 multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
                    const float* __restrict__ rec_f, const double* __restrict__ coef_d,
                    const float* __restrict__ coef_f, const float* __restrict__ pl_f,

@@ -25,6 +25,8 @@ Outputs (all .npz, metadata as a JSON string under key ``meta``):
                 sources at 100x100, supersampling 4, a 41x41 Moffat kernel
   grad_fd.npz   central differences of likelihood_data_given_model (the
                 reference's own likelihood) on gradient-workload scenes
+  hessians.npz  LensModel.hessian of EPL_MULTIPOLE_M1M3M4, NFW_ELLIPSE_CSE and
+                CONVERGENCE
 """
 
 import json
@@ -667,6 +669,38 @@ def gen_serving_scenes():
     return scenes
 
 
+def gen_hessians():
+    """LensModel.hessian of the profiles whose exact Hessian comes from the
+    adjoint's dual numbers beyond the round-one set: EPL_MULTIPOLE_M1M3M4 (the
+    reference's analytic EPL + multipole Hessians), NFW_ELLIPSE_CSE (its
+    analytic CSE Hessian) and CONVERGENCE, at seeded points away from the
+    centre."""
+    from jaxtronomy.LensModel.lens_model import LensModel
+
+    rng = np.random.default_rng(20240607)
+    cases = []
+    for name, kw in [
+        ("EPL_MULTIPOLE_M1M3M4", {"theta_E": 1.2, "gamma": 2.05, "e1": 0.1, "e2": 0.05,
+                                  "center_x": 0.02, "center_y": -0.01, "a1_a": 0.01,
+                                  "delta_phi_m1": 0.3, "a3_a": -0.012, "delta_phi_m3": 1.1,
+                                  "a4_a": 0.008, "delta_phi_m4": 2.0}),
+        ("EPL_MULTIPOLE_M1M3M4", {"theta_E": 0.9, "gamma": 1.9, "e1": -0.3, "e2": 0.25,
+                                  "center_x": 0.0, "center_y": 0.0, "a1_a": -0.02,
+                                  "delta_phi_m1": 2.9, "a3_a": 0.005, "delta_phi_m3": 0.2,
+                                  "a4_a": -0.015, "delta_phi_m4": 0.7}),
+        ("NFW_ELLIPSE_CSE", {"Rs": 8.0, "alpha_Rs": 1.3, "e1": 0.1, "e2": -0.2,
+                             "center_x": 0.1, "center_y": 0.0}),
+        ("NFW_ELLIPSE_CSE", {"Rs": 0.5, "alpha_Rs": 0.2, "e1": -0.05, "e2": 0.02,
+                             "center_x": -0.3, "center_y": 0.4}),
+        ("CONVERGENCE", {"kappa": 0.07, "ra_0": 0.1, "dec_0": -0.2}),
+    ]:
+        x = rng.uniform(-2.5, 2.5, 64)
+        y = rng.uniform(-2.5, 2.5, 64)
+        out = np.stack([np.asarray(v) for v in LensModel([name]).hessian(x, y, [kw])])
+        cases.append({"name": name, "kwargs": kw, "x": x, "y": y, "out": out})
+    return cases
+
+
 def _rows_order(lens, src, ll):
     """(list index, profile index, parameter name) in the row layout of
     ImageModel.pack_params: lens, source, lens-light profiles in order, each
@@ -899,8 +933,18 @@ def write_grad_fd():
     _save(os.path.join(HERE, "grad_fd.npz"), arrays, meta)
 
 
+def write_hessians():
+    arrays, meta = {}, []
+    for i, c in enumerate(gen_hessians()):
+        for k in ("x", "y", "out"):
+            arrays["%s_%d" % (k, i)] = c.pop(k)
+        meta.append(c)
+    _save(os.path.join(HERE, "hessians.npz"), arrays, meta)
+
+
 # golden files that can be regenerated one at a time
-EXTRA = {"serving_scenes.npz": write_serving_scenes, "grad_fd.npz": write_grad_fd}
+EXTRA = {"serving_scenes.npz": write_serving_scenes, "grad_fd.npz": write_grad_fd,
+         "hessians.npz": write_hessians}
 
 
 if __name__ == "__main__":

@@ -175,3 +175,11 @@ def grad_fd_cases():
             c[k] = d[key] if key in d.files else None
         out.append(c)
     return out
+
+
+def hessian_cases():
+    """The reference's LensModel.hessian of EPL_MULTIPOLE_M1M3M4, NFW_ELLIPSE_CSE
+    and CONVERGENCE at seeded points (hessians.npz): f_xx, f_xy, f_yx, f_yy."""
+    d, meta = load("hessians.npz")
+    return [dict(m, x=d["x_%d" % i], y=d["y_%d" % i], out=d["out_%d" % i])
+            for i, m in enumerate(meta)]

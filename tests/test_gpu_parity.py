@@ -296,3 +296,13 @@ def test_exact_hessian_of_cse_and_multipole_matches_differences(cuda, name):
         got = np.array(lm.hessian(x, y, [case["kwargs"]]))
         fd = np.array(lm.hessian(x, y, [case["kwargs"]], diff=1e-6))
         np.testing.assert_allclose(got, fd, rtol=1e-5, atol=1e-6 * np.abs(fd).max())
+
+
+@pytest.mark.parametrize("case", golden_io.hessian_cases(),
+                         ids=lambda c: "%s-%g" % (c["name"], c["kwargs"].get("e1", 0.0)))
+def test_exact_hessian_matches_reference_hessian(cuda, case):
+    """lensgb_hessian against the reference's own Hessians (analytic EPL +
+    multipole, analytic CSE sum, constant CONVERGENCE)."""
+    got = np.array(J.LensModel([case["name"]]).hessian(case["x"], case["y"], [case["kwargs"]]))
+    ref = case["out"]
+    np.testing.assert_allclose(got, ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())

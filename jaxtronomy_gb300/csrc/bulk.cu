@@ -388,7 +388,10 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
             } else if (t & BULK_TAG_FP64) {
                 const double* rd = rec_d + g * REC_D;
                 const double* cd = coef_d ? coef_d + g * EPL_NMAX : nullptr;
-                const double ep = eps_d[g], itz = 1.0 / Tz[g];
+                // 1 / T_z from the step table's FP32 pair (to ~2^-48 relative), so
+                // no FP64 division runs per deflector
+                const float* pl = spl + j * PL_F;
+                const double ep = eps_d[g], itz = (double)pl[2] + (double)pl[3];
 #pragma unroll
                 for (int k = 0; k < MP_RPT; ++k) {
                     double o[2];
@@ -403,7 +406,7 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                     if (code == LENSGB_LENS_TNFW && u >= rd[10]) {
                         // far field of a strong TNFW halo: the record's 16-term series
                         // (truncation below 1e-8 relative, far inside this path's error)
-                        const double e = 1.0 / sqrt(u), z = rd[12] * e;
+                        const double e = rsqrt(u), z = rd[12] * e;
                         double bs = rd[29];
                         for (int q = 14; q >= 0; --q) bs = fma(bs, z, rd[14 + q]);
                         const double a = rd[11] * bs * (e * e);
@@ -434,7 +437,7 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
 #pragma unroll
                     for (int k = 0; k < MP_RPT; ++k) {
                         float ax, ay;
-                        tnfw_pair_f(rf, ox[k], oy[k], ax, ay);
+                        tnfw_pair_f<true>(rf, ox[k], oy[k], ax, ay);
                         s32[0][k] += ax;
                         s32[1][k] += ay;
                     }

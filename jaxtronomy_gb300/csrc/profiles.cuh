@@ -504,6 +504,12 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
 // subhalo (x >= 3 max(tau, 1): f12 holds that bound squared) the bracket is the
 // convergent series sum_k c_k z^k in z = max(tau, 1)/x (f16..f31 = c_0..c_15,
 // f14 = max(tau, 1), f13 = 4 rho0 Rs tau^2/(tau^2+1)^2; within 1e-8 relative).
+// ESTRIN: the far-field polynomial by Estrin's scheme (depth 4 instead of 15,
+// three more multiplies) rather than Horner's.  The multi-plane kernel, whose
+// 2-warp CTAs stall on dependent FMAs, gains (same-box A/B on GB300: 3.37 ->
+// 3.29 ms on the 400^2-ray, 5501-step workload); the single-plane bulk kernel,
+// with more warps per SM, keeps Horner's.
+template <bool ESTRIN = false>
 __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy, float& ax,
                                             float& ay) {
     const float tau = rec[6], a4 = rec[7], inv_rs = rec[8], inv_tau = rec[9];
@@ -516,9 +522,20 @@ __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy
         const float4 q0 = cv[0], q1 = cv[1], q2 = cv[2], q3 = cv[3];
         const float c[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
                              q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
-        float b = c[15];
+        float b;
+        if (ESTRIN) {
+            const float z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
+            float p[8];
 #pragma unroll
-        for (int k = 14; k >= 0; --k) b = fmaf(b, z, c[k]);
+            for (int k = 0; k < 8; ++k) p[k] = fmaf(c[2 * k + 1], z, c[2 * k]);
+            const float e0 = fmaf(p[1], z2, p[0]), e1 = fmaf(p[3], z2, p[2]);
+            const float e2 = fmaf(p[5], z2, p[4]), e3 = fmaf(p[7], z2, p[6]);
+            b = fmaf(fmaf(e3, z4, e2), z8, fmaf(e1, z4, e0));
+        } else {
+            b = c[15];
+#pragma unroll
+            for (int k = 14; k >= 0; --k) b = fmaf(b, z, c[k]);
+        }
         const float a = rec[13] * b * (e * e);
         ax = a * dx;
         ay = a * dy;

@@ -911,10 +911,12 @@ def sampler_section(steps, seed=1003, n_walkers=256, linear_solver=False):
     }
 
 
-def gradient_section(steps, seed=1003):
+def gradient_section(steps, seed=1003, peaks=None):
     """Adjoint gradient of logL for 256 systems (120^2, s=2, PSF 21, EPL+SHEAR,
     Sersic source and lens light): time per batch, and the worst component
-    error against central finite differences (step 1e-6) on a sample."""
+    error against central finite differences (step 1e-6) on a sample; then the
+    same batch with FP32 per-ray derivatives (gradient_precision "fp32"), its
+    time and its error against the FP64 adjoint."""
     import numpy as np
     import torch
     import jaxtronomy_gb300 as J
@@ -970,6 +972,24 @@ def gradient_section(steps, seed=1003):
     scale = np.abs(fd).max(axis=1, keepdims=True)
     sig = np.abs(fd) > 1e-3 * scale
     rel = np.abs(gs - fd)[sig] / np.abs(fd)[sig]
+    # FP32 per-ray derivatives, flagged pixels recomputed in FP64
+    im32 = J.ImageModel(data_cls, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                        J.LensModel(["EPL", "SHEAR"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                        J.LightModel(["SERSIC_ELLIPSE"]),
+                        kwargs_numerics={"supersampling_factor": S, "precision": "fp64",
+                                         "gradient_precision": "fp32"})
+    for _ in range(2):
+        im32.likelihood_grad_batch(rows=rows_d, data=data_d, psf_kernels=kern_d)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(n):
+        logl32, grad32 = im32.likelihood_grad_batch(rows=rows_d, data=data_d, psf_kernels=kern_d)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / n
+    g64, g32 = grad.cpu().numpy(), grad32.cpu().numpy()
+    floor = 1e-3 * np.abs(g64).max(axis=1, keepdims=True)
+    rel32 = np.abs(g32 - g64) / (np.abs(g64) + floor)
     return {
         "workload": "gradient_epl_256x120x120_s2_psf21",
         "systems": B, "params_per_system": P,
@@ -978,25 +998,45 @@ def gradient_section(steps, seed=1003):
         "fd_rel_err_max": float(rel.max()), "fd_rel_err_median": float(np.median(rel)),
         "fd_components_checked": int(sig.sum()),
         "precision": "FP64 (forward image, adjoint and reduction)",
-        "roofline": grad_roofline(B, N, S, K, P, ms),
+        "roofline": grad_roofline(B, N, S, K, P, ms, peaks, "fp64"),
         "timing": "CUDA events, mean over %d batches after 2 warm-ups" % n,
+        "fp32_adjoint": {
+            "ms_per_batch": ms32, "systems_per_s": B / (ms32 / 1e3),
+            "speedup_over_fp64_adjoint": ms / ms32,
+            "rel_err_vs_fp64_adjoint_max": float(rel32.max()),
+            "rel_err_vs_fp64_adjoint_median": float(np.median(rel32)),
+            "logL_bits_equal": bool(torch.equal(logl32, logl)),
+            "err_floor": "per component over |fp64| + 1e-3 of the system's largest component",
+            "precision": "FP32 dual numbers from FP64 offsets; pixels whose predicted FP32 "
+                         "derivative error exceeds 1e-5 recomputed in FP64; forward image, "
+                         "weights and reduction FP64",
+            "roofline": grad_roofline(B, N, S, K, P, ms32, peaks, "fp32"),
+        },
     }
 
 
-def grad_roofline(B, N, S, K, P, ms):
-    """Algorithmic FP64 work of one adjoint batch: every ray's EPL + SHEAR + two
+def grad_roofline(B, N, S, K, P, ms, peaks=None, kind="fp64"):
+    """Algorithmic work of one adjoint batch: every ray's EPL + SHEAR + two
     Sersic evaluation (~220 flop) carried with 5 tangent directions (~6x), plus
     the per-parameter accumulation (2 P flop per ray); the forward image and
     likelihood (ray work + 2 K^2 per pixel), and the transposed convolution
-    (2 K^2 per pixel).  Peak: the nominal GB300 FP64 rate (no measured FP64 figure)."""
+    (2 K^2 per pixel).  Peak: the FMA rate of the dominant kernel's arithmetic
+    (FP64, or FP32 for FP32 per-ray derivatives), measured in this run by the
+    FMA-chain kernel when available, else nominal."""
     rays = B * (N * S) ** 2
     flop = rays * (220 * 6 + 2 * P) + rays * 220 + 2 * (2 * K * K) * B * N * N
-    peak = 1.25  # TFLOP/s, nominal FP64 (CUDA cores) of GB300
+    key = "fp64_tflops" if kind == "fp64" else "fp32_tflops"
+    if peaks and peaks.get(key):
+        peak, src = peaks[key], "measured %s FMA rate of this device (fma_peaks, of measured)" \
+            % kind.upper()
+    else:
+        peak = 1.25 if kind == "fp64" else 78.3
+        src = "nominal %s rate (no FMA measurement in this run)" % kind.upper()
     achieved = flop / (ms / 1e3) / 1e12
     return {"kernel": "grad_ray_kernel (+ forward image, weights, transposed conv)",
-            "bound": "fp64", "unit": "TFLOP/s", "algorithmic_gflop_per_batch": flop / 1e9,
+            "bound": kind, "unit": "TFLOP/s", "algorithmic_gflop_per_batch": flop / 1e9,
             "achieved": achieved, "peak": peak, "frac": achieved / peak,
-            "peak_source": "nominal FP64 rate; MEASURED_PEAKS.json has no FP64 figure"}
+            "peak_source": src}
 
 
 def max_over_ranks(ms, dist=None, device="cpu"):
@@ -1341,7 +1381,7 @@ def gpu_arm(args):
 
         # --- adjoint likelihood gradient
         if not args.no_grad:
-            extra["gradient"] = gradient_section(args.steps)
+            extra["gradient"] = gradient_section(args.steps, peaks=peaks)
             extra["sampler"] = sampler_section(args.steps)
             extra["sampler_linear_solve"] = sampler_section(args.steps, linear_solver=True)
 

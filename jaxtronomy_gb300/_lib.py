@@ -56,7 +56,7 @@ SYMBOLS = [
     "lensgb_server_drain", "lensgb_server_clock_ns", "lensgb_server_request_times",
     "lensgb_server_get_stats", "lensgb_server_destroy",
     "lensgb_fma_chain", "lensgb_set_conv_tma", "lensgb_wait_timeouts",
-    "lensgb_model_set_convolution",
+    "lensgb_model_set_convolution", "lensgb_model_set_grad_precision",
     "lensgb_last_error", "lensgb_version",
 ]
 
@@ -246,6 +246,8 @@ def load():
     lib.lensgb_fma_chain.restype = i
     lib.lensgb_model_set_convolution.argtypes = [vp, i]
     lib.lensgb_model_set_convolution.restype = i
+    lib.lensgb_model_set_grad_precision.argtypes = [vp, i]
+    lib.lensgb_model_set_grad_precision.restype = i
     lib.lensgb_set_conv_tma.argtypes = [i]
     lib.lensgb_set_conv_tma.restype = i
     lib.lensgb_wait_timeouts.argtypes = [ctypes.POINTER(ctypes.c_uint)]

@@ -68,6 +68,7 @@ struct lensgb_model {
     float refine_kappa = 3e-7f;
     // convolution method (lensgb_model_set_convolution) and the FFT path's scratch
     int conv_method = LENSGB_CONV_AUTO;
+    int grad_precision = LENSGB_FP64;  // lensgb_model_set_grad_precision
     void* fft_scratch = nullptr;
     size_t fft_cap = 0;
     // gradient scratch (lensgb_loglike_grad), grow-only
@@ -82,11 +83,14 @@ struct lensgb_model {
     double* g_pad_a = nullptr;    // edge-padded arrays (GAUSSIAN transposed convolution)
     double* g_pad_b = nullptr;
     double* g_partial = nullptr;
+    double* g_flag = nullptr;     // FP32 adjoint: one byte per ray-grid pixel (flagged for FP64)
+    float grad_tau = 1e-5f;       // FP32 adjoint: predicted relative error that flags a pixel
 };
 
 static void free_grad_scratch(lensgb_model* m) {
     double** bufs[] = {&m->g_dcoef, &m->g_psf, &m->g_m, &m->g_a, &m->g_b,
-                       &m->g_c, &m->g_d, &m->g_pad_a, &m->g_pad_b, &m->g_partial};
+                       &m->g_c, &m->g_d, &m->g_pad_a, &m->g_pad_b, &m->g_partial,
+                       &m->g_flag};
     for (double** b : bufs) {
         cudaFree(*b);
         *b = nullptr;
@@ -1099,6 +1103,14 @@ int lensgb_model_set_convolution(lensgb_model* m, int method) {
     return LENSGB_OK;
 }
 
+int lensgb_model_set_grad_precision(lensgb_model* m, int precision) {
+    if (!m) return fail(LENSGB_ERR_INVALID, "null model");
+    if (precision != LENSGB_FP64 && precision != LENSGB_FP32_SPLIT)
+        return fail(LENSGB_ERR_INVALID, "precision must be LENSGB_FP64 or LENSGB_FP32_SPLIT");
+    m->grad_precision = precision;
+    return LENSGB_OK;
+}
+
 int lensgb_set_conv_tma(int enable) {
     set_conv_tma(enable);
     return LENSGB_OK;
@@ -1247,7 +1259,10 @@ static int ensure_grad_scratch(lensgb_model* m, int n_inst) {
     const size_t kk = (size_t)K * K + (size_t)KL * KL;
     const size_t ncoef = (size_t)cap * (m->st.n_epl > 0 ? m->st.n_epl : 1) * EPL_NMAX;
     const GridDesc& rg = hr ? m->grid_hr : m->grid;
-    const size_t npart = (size_t)cap * grad_chunks(rg) * (m->st.n_params > 0 ? m->st.n_params : 1);
+    // two sets of partials: the FP32 pass and the FP64 pass over flagged pixels
+    const size_t npart =
+        2 * (size_t)cap * grad_chunks(rg) * (m->st.n_params > 0 ? m->st.n_params : 1);
+    const size_t nflag = ((size_t)cap * rg.nx * rg.ny + 7) / 8;  // bytes, in doubles
     size_t pad = 0;
     if (m->desc.psf_type == LENSGB_PSF_GAUSSIAN) {
         const size_t side = (size_t)(hr ? m->grid_hr.nx : m->grid.nx) + K - 1;
@@ -1261,7 +1276,8 @@ static int ensure_grad_scratch(lensgb_model* m, int n_inst) {
                 {&m->g_m, (size_t)cap * full}, {&m->g_a, (size_t)cap * kgrid},
                 {&m->g_b, (size_t)cap * kgrid}, {&m->g_c, (size_t)cap * hgrid},
                 {&m->g_d, (size_t)cap * hgrid}, {&m->g_pad_a, (size_t)cap * pad},
-                {&m->g_pad_b, (size_t)cap * pad}, {&m->g_partial, npart}};
+                {&m->g_pad_b, (size_t)cap * pad}, {&m->g_partial, npart},
+                {&m->g_flag, nflag}};
     for (auto& w : want) {
         if (w.n == 0) continue;
         if (cudaMalloc(w.p, w.n * sizeof(double)) != cudaSuccess) {
@@ -1346,7 +1362,8 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
         }
         if (m->sub_mask) launch_mask(m->g_d, n_inst, ny, nx, S, m->sub_mask, LENSGB_FP64, s);
         if (launch_grad_rays(m->grid_hr, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef,
-                             m->g_d, 1.0, m->g_partial, grad, s))
+                             m->g_d, 1.0, m->g_partial, grad, m->grad_precision,
+                             (unsigned char*)m->g_flag, m->grad_tau, s))
             return fail(LENSGB_ERR_CUDA, "gradient launch failed");
         return check_cuda("likelihood gradient launch");
     }
@@ -1359,7 +1376,8 @@ int lensgb_loglike_grad(lensgb_model* m, const double* params, int n_inst, const
     }
     if (m->sub_mask) launch_mask((void*)gl, n_inst, ny, nx, 1, m->sub_mask, LENSGB_FP64, s);
     if (launch_grad_rays(m->grid, m->st, n_inst, params, m->rec_d, m->coef_d, m->g_dcoef, gl,
-                         area, m->g_partial, grad, s))
+                         area, m->g_partial, grad, m->grad_precision,
+                         (unsigned char*)m->g_flag, m->grad_tau, s))
         return fail(LENSGB_ERR_CUDA, "gradient launch failed");
     return check_cuda("likelihood gradient launch");
 }

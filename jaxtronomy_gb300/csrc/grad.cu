@@ -42,116 +42,132 @@ constexpr int GJ = 12;       // parameters of the largest lens profile (EPL_MULT
 // ---------------------------------------------------------------------------
 // forward-mode dual numbers with 5 tangent directions (b, t, q, x1, y1)
 // ---------------------------------------------------------------------------
+template <typename T>
 struct D5 {
-    double v;
-    double d[5];
+    T v;
+    T d[5];
 };
 
-__device__ __forceinline__ D5 dconst(double v) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dconst(T v) {
+    D5<T> r;
     r.v = v;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) r.d[k] = 0.0;
+    for (int k = 0; k < 5; ++k) r.d[k] = T(0.0);
     return r;
 }
-__device__ __forceinline__ D5 dvar(double v, int k) {
-    D5 r = dconst(v);
-    r.d[k] = 1.0;
+template <typename T>
+__device__ __forceinline__ D5<T> dvar(T v, int k) {
+    D5<T> r = dconst(v);
+    r.d[k] = T(1.0);
     return r;
 }
-__device__ __forceinline__ D5 operator+(const D5& a, const D5& b) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> operator+(const D5<T>& a, const D5<T>& b) {
+    D5<T> r;
     r.v = a.v + b.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] + b.d[k];
     return r;
 }
-__device__ __forceinline__ D5 operator-(const D5& a, const D5& b) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> operator-(const D5<T>& a, const D5<T>& b) {
+    D5<T> r;
     r.v = a.v - b.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] - b.d[k];
     return r;
 }
-__device__ __forceinline__ D5 operator*(const D5& a, const D5& b) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> operator*(const D5<T>& a, const D5<T>& b) {
+    D5<T> r;
     r.v = a.v * b.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = a.v * b.d[k] + b.v * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 operator*(double s, const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> operator*(T s, const D5<T>& a) {
+    D5<T> r;
     r.v = s * a.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = s * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 operator+(double s, const D5& a) {
-    D5 r = a;
+template <typename T>
+__device__ __forceinline__ D5<T> operator+(T s, const D5<T>& a) {
+    D5<T> r = a;
     r.v += s;
     return r;
 }
-__device__ __forceinline__ D5 dinv(const D5& a) {
-    D5 r;
-    r.v = 1.0 / a.v;
-    const double g = -r.v * r.v;
+template <typename T>
+__device__ __forceinline__ D5<T> dinv(const D5<T>& a) {
+    D5<T> r;
+    r.v = T(1.0) / a.v;
+    const T g = -r.v * r.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 dlog(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dlog(const D5<T>& a) {
+    D5<T> r;
     r.v = log(a.v);
-    const double g = 1.0 / a.v;
+    const T g = T(1.0) / a.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 dexp(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dexp(const D5<T>& a) {
+    D5<T> r;
     r.v = exp(a.v);
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = r.v * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 dsqrt(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dsqrt(const D5<T>& a) {
+    D5<T> r;
     r.v = sqrt(a.v);
-    const double g = 0.5 / r.v;
+    const T g = T(0.5) / r.v;
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 datan(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> datan(const D5<T>& a) {
+    D5<T> r;
     r.v = atan(a.v);
-    const double g = 1.0 / (1.0 + a.v * a.v);
+    const T g = T(1.0) / (T(1.0) + a.v * a.v);
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 datanh(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> datanh(const D5<T>& a) {
+    D5<T> r;
     r.v = atanh(a.v);
-    const double g = 1.0 / (1.0 - a.v * a.v);
+    const T g = T(1.0) / (T(1.0) - a.v * a.v);
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
 
-__device__ __forceinline__ D5 dacosh(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dacosh(const D5<T>& a) {
+    D5<T> r;
     r.v = acosh(a.v);
-    const double g = 1.0 / sqrt(a.v * a.v - 1.0);
+    const T g = T(1.0) / sqrt(a.v * a.v - T(1.0));
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
 }
-__device__ __forceinline__ D5 dacos(const D5& a) {
-    D5 r;
+template <typename T>
+__device__ __forceinline__ D5<T> dacos(const D5<T>& a) {
+    D5<T> r;
     r.v = acos(a.v);
-    const double g = -1.0 / sqrt(1.0 - a.v * a.v);
+    const T g = -T(1.0) / sqrt(T(1.0) - a.v * a.v);
 #pragma unroll
     for (int k = 0; k < 5; ++k) r.d[k] = g * a.d[k];
     return r;
@@ -159,107 +175,109 @@ __device__ __forceinline__ D5 dacos(const D5& a) {
 
 // (phi, q) = ellipticity2phi_q(e1, e2) (param_util.py:88-99): dq/de and dphi/de
 // (zero at e = 0 and where the axis-ratio clamp c < 0.9999 holds it).
-__device__ __forceinline__ void dphiq_de(double e1, double e2, double& dq1, double& dq2,
-                                         double& dp1, double& dp2) {
-    const double cc2 = e1 * e1 + e2 * e2;
-    const double cc = sqrt(cc2);
-    dq1 = dq2 = dp1 = dp2 = 0.0;
-    if (cc > 0.0) {
-        if (cc < 0.9999) {
-            const double dqdc = -2.0 / ((1.0 + cc) * (1.0 + cc));
+template <typename T>
+__device__ __forceinline__ void dphiq_de(T e1, T e2, T& dq1, T& dq2,
+                                         T& dp1, T& dp2) {
+    const T cc2 = e1 * e1 + e2 * e2;
+    const T cc = sqrt(cc2);
+    dq1 = dq2 = dp1 = dp2 = T(0.0);
+    if (cc > T(0.0)) {
+        if (cc < T(0.9999)) {
+            const T dqdc = -T(2.0) / ((T(1.0) + cc) * (T(1.0) + cc));
             dq1 = dqdc * e1 / cc;
             dq2 = dqdc * e2 / cc;
         }
-        dp1 = -e2 / (2.0 * cc2);
-        dp2 = e1 / (2.0 * cc2);
+        dp1 = -e2 / (T(2.0) * cc2);
+        dp2 = e1 / (T(2.0) * cc2);
     }
 }
 
 // EPL deflection (epl.py:179-200,366-394) and its Jacobian with respect to
 // (theta_E, gamma, e1, e2, center_x, center_y): J[0][k] = d alpha_x / d p_k,
 // J[1][k] = d alpha_y / d p_k.  `a` is the profile's raw parameter row.
-__device__ void epl_alpha_grad(const double* rec, const double* F, const double* dF,
-                               const double* a, double dx, double dy, double& ax, double& ay,
-                               double J[2][GJ]) {
-    const double b = rec[2], t = rec[3], q = rec[4], c = rec[5], sn = rec[6];
+template <typename T>
+__device__ void epl_alpha_grad(const T* rec, const T* F, const T* dF,
+                               const T* a, T dx, T dy, T& ax, T& ay,
+                               T J[2][GJ]) {
+    const T b = rec[2], t = rec[3], q = rec[4], c = rec[5], sn = rec[6];
     const int nmax = (int)rec[8];
-    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
-    const D5 B = dvar(b, 0), T = dvar(t, 1), Q = dvar(q, 2);
-    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
-    const D5 Za = Q * X1, Zb = Y1;
-    const D5 r2 = Za * Za + Zb * Zb;
+    const T x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5<T> B = dvar(b, 0), Tt = dvar(t, 1), Q = dvar(q, 2);
+    const D5<T> X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5<T> Za = Q * X1, Zb = Y1;
+    const D5<T> r2 = Za * Za + Zb * Zb;
     for (int i = 0; i < 2; ++i)
-        for (int k = 0; k < GJ; ++k) J[i][k] = 0.0;
-    ax = 0.0;
-    ay = 0.0;
-    if (r2.v == 0.0) return;  // reference: 0/0 -> NaN -> nan_to_num -> 0
-    D5 hr = dconst(1.0), hi = dconst(0.0);
+        for (int k = 0; k < GJ; ++k) J[i][k] = T(0.0);
+    ax = T(0.0);
+    ay = T(0.0);
+    if (r2.v == T(0.0)) return;  // reference: 0/0 -> NaN -> nan_to_num -> 0
+    D5<T> hr = dconst(T(1.0)), hi = dconst(T(0.0));
     if (nmax > 0) {
-        const D5 f = (1.0 + (-1.0) * Q) * dinv(1.0 + Q);
-        const D5 inv = dinv(r2);
-        const D5 zr = (-1.0) * f * (Za * Za - Zb * Zb) * inv;
-        const D5 zi = (-2.0) * f * Za * Zb * inv;
-        const D5 dr = zr + dconst(-2.0), di = zi;
-        const D5 dd = dinv(dr * dr + di * di);
-        const D5 wr = (zr * dr + zi * di) * dd;
-        const D5 wi = (zi * dr - zr * di) * dd;
-        D5 sr = dconst(F[nmax - 1]);
+        const D5<T> f = (T(1.0) + (-T(1.0)) * Q) * dinv(T(1.0) + Q);
+        const D5<T> inv = dinv(r2);
+        const D5<T> zr = (-T(1.0)) * f * (Za * Za - Zb * Zb) * inv;
+        const D5<T> zi = (-T(2.0)) * f * Za * Zb * inv;
+        const D5<T> dr = zr + dconst(-T(2.0)), di = zi;
+        const D5<T> dd = dinv(dr * dr + di * di);
+        const D5<T> wr = (zr * dr + zi * di) * dd;
+        const D5<T> wi = (zi * dr - zr * di) * dd;
+        D5<T> sr = dconst(F[nmax - 1]);
         sr.d[1] = dF[nmax - 1];
-        D5 si = dconst(0.0);
+        D5<T> si = dconst(T(0.0));
         for (int n = nmax - 2; n >= 0; --n) {
-            D5 fn = dconst(F[n]);
+            D5<T> fn = dconst(F[n]);
             fn.d[1] = dF[n];
-            const D5 nr = sr * wr - si * wi + fn;
-            const D5 ni = sr * wi + si * wr;
+            const D5<T> nr = sr * wr - si * wi + fn;
+            const D5<T> ni = sr * wi + si * wr;
             sr = nr;
             si = ni;
         }
-        const D5 er = 1.0 + (-0.5) * zr, ei = (-0.5) * zi;
-        const D5 ee = dinv(er * er + ei * ei);
+        const D5<T> er = T(1.0) + (-T(0.5)) * zr, ei = (-T(0.5)) * zi;
+        const D5<T> ee = dinv(er * er + ei * ei);
         hr = (sr * er + si * ei) * ee;
         hi = (si * er - sr * ei) * ee;
     }
-    D5 R = dsqrt(r2);
-    if (R.v < 1e-9) R = dconst(1e-9);
+    D5<T> R = dsqrt(r2);
+    if (R.v < T(1e-9)) R = dconst(T(1e-9));
     // 2/(1+q) (b/R)^t
-    const D5 amp = 2.0 * dinv(1.0 + Q) * dexp(T * (dlog(B) - dlog(R)));
-    const D5 fx = amp * (Za * hr - Zb * hi);
-    const D5 fy = amp * (Za * hi + Zb * hr);
+    const D5<T> amp = T(2.0) * dinv(T(1.0) + Q) * dexp(Tt * (dlog(B) - dlog(R)));
+    const D5<T> fx = amp * (Za * hr - Zb * hi);
+    const D5<T> fy = amp * (Za * hi + Zb * hr);
     ax = fx.v * c - fy.v * sn;
     ay = fx.v * sn + fy.v * c;
     // rotate the major-axis derivatives back
-    double dA[2][5];
+    T dA[2][5];
     for (int k = 0; k < 5; ++k) {
         dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
         dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
     }
     // d alpha / d phi = Rot(phi) [ (-fy, fx) + J_maj (y1, -x1) ]
-    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
-    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
-    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    const T gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const T gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const T aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
     // d alpha / d (dx, dy) = Rot(phi) J_maj Rot(-phi); (x1, y1) = Rot(-phi) (dx, dy)
-    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
-    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    const T jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const T jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
     // chain to (theta_E, gamma, e1, e2): b = theta_E sqrt(q), t = gamma - 1,
     // (phi, q) from (e1, e2) (param_util.py:88-99, epl.py:111-124)
-    const double theta_E = a[0], e1 = a[2], e2 = a[3];
-    const double sq = sqrt(q);
-    const double cc2 = e1 * e1 + e2 * e2;
-    const double cc = sqrt(cc2);
-    double dq1 = 0.0, dq2 = 0.0, dp1 = 0.0, dp2 = 0.0;
-    if (cc > 0.0) {
-        if (cc < 0.9999) {
-            const double dqdc = -2.0 / ((1.0 + cc) * (1.0 + cc));
+    const T theta_E = a[0], e1 = a[2], e2 = a[3];
+    const T sq = sqrt(q);
+    const T cc2 = e1 * e1 + e2 * e2;
+    const T cc = sqrt(cc2);
+    T dq1 = T(0.0), dq2 = T(0.0), dp1 = T(0.0), dp2 = T(0.0);
+    if (cc > T(0.0)) {
+        if (cc < T(0.9999)) {
+            const T dqdc = -T(2.0) / ((T(1.0) + cc) * (T(1.0) + cc));
             dq1 = dqdc * e1 / cc;
             dq2 = dqdc * e2 / cc;
         }
-        dp1 = -e2 / (2.0 * cc2);
-        dp2 = e1 / (2.0 * cc2);
+        dp1 = -e2 / (T(2.0) * cc2);
+        dp2 = e1 / (T(2.0) * cc2);
     }
-    const double dbdq = theta_E / (2.0 * sq);
+    const T dbdq = theta_E / (T(2.0) * sq);
     for (int i = 0; i < 2; ++i) {
-        const double aph = i == 0 ? aphx : aphy;
-        const double aq = dA[i][0] * dbdq + dA[i][2];
+        const T aph = i == 0 ? aphx : aphy;
+        const T aq = dA[i][0] * dbdq + dA[i][2];
         J[i][0] = dA[i][0] * sq;
         J[i][1] = dA[i][1];
         J[i][2] = aq * dq1 + aph * dp1;
@@ -275,45 +293,46 @@ __device__ void epl_alpha_grad(const double* rec, const double* F, const double*
 // times sqrt((1 + q^2) / 2)), s = s_scale / sqrt(q); the major-axis formula is
 // differentiated in (b, s, q, x1, y1), with q frozen where the q < 1 clamp
 // replaces it.
-__device__ void nie_alpha_grad(int code, const double* rec, const double* a, double dx, double dy,
-                               double& ax, double& ay, double J[2][GJ]) {
-    const double b = rec[2], s = rec[3], qc = rec[4], c = rec[5], sn = rec[6];
+template <typename T>
+__device__ void nie_alpha_grad(int code, const T* rec, const T* a, T dx, T dy,
+                               T& ax, T& ay, T J[2][GJ]) {
+    const T b = rec[2], s = rec[3], qc = rec[4], c = rec[5], sn = rec[6];
     const bool nie = code == LENSGB_LENS_NIE;
-    const double e1 = a[1], e2 = a[2];
-    const double cc = sqrt(e1 * e1 + e2 * e2);
-    const double q = (1.0 - fmin(cc, 0.9999)) / (1.0 + fmin(cc, 0.9999));
-    const bool clamped = q >= 1.0;
-    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
-    const D5 B = dvar(b, 0), S = dvar(s, 1), Q = clamped ? dconst(qc) : dvar(qc, 2);
-    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
-    const D5 Q2 = Q * Q;
-    const D5 psi = dsqrt(Q2 * (S * S + X1 * X1) + Y1 * Y1);
-    const D5 sq = dsqrt(1.0 + (-1.0) * Q2);
-    const D5 bs = B * dinv(sq);
-    const D5 fx = bs * datan(sq * X1 * dinv(psi + S));
-    const D5 fy = bs * datanh(sq * Y1 * dinv(psi + Q2 * S));
+    const T e1 = a[1], e2 = a[2];
+    const T cc = sqrt(e1 * e1 + e2 * e2);
+    const T q = (T(1.0) - fmin(cc, T(0.9999))) / (T(1.0) + fmin(cc, T(0.9999)));
+    const bool clamped = q >= T(1.0);
+    const T x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5<T> B = dvar(b, 0), S = dvar(s, 1), Q = clamped ? dconst(qc) : dvar(qc, 2);
+    const D5<T> X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5<T> Q2 = Q * Q;
+    const D5<T> psi = dsqrt(Q2 * (S * S + X1 * X1) + Y1 * Y1);
+    const D5<T> sq = dsqrt(T(1.0) + (-T(1.0)) * Q2);
+    const D5<T> bs = B * dinv(sq);
+    const D5<T> fx = bs * datan(sq * X1 * dinv(psi + S));
+    const D5<T> fy = bs * datanh(sq * Y1 * dinv(psi + Q2 * S));
     ax = fx.v * c - fy.v * sn;
     ay = fx.v * sn + fy.v * c;
-    double dA[2][5];
+    T dA[2][5];
     for (int k = 0; k < 5; ++k) {
         dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
         dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
     }
     // d alpha / d phi = Rot(phi) [ (-fy, fx) + J_maj (y1, -x1) ]
-    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
-    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
-    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
-    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
-    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
-    double dq1, dq2, dp1, dp2;
+    const T gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const T gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const T aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    const T jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const T jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    T dq1, dq2, dp1, dp2;
     dphiq_de(e1, e2, dq1, dq2, dp1, dp2);
-    const double theta_E = a[0], s_scale = nie ? a[3] : 0.0000000001;
-    const double sqq = sqrt(q);
-    const double dbdq = theta_E / (2.0 * sqq), dsdq = -s_scale / (2.0 * q * sqq);
+    const T theta_E = a[0], s_scale = nie ? a[3] : T(0.0000000001);
+    const T sqq = sqrt(q);
+    const T dbdq = theta_E / (T(2.0) * sqq), dsdq = -s_scale / (T(2.0) * q * sqq);
     const int co = nie ? 4 : 3;
     for (int i = 0; i < 2; ++i) {
-        const double aph = i == 0 ? aphx : aphy;
-        const double aq = dA[i][0] * dbdq + dA[i][1] * dsdq + dA[i][2];
+        const T aph = i == 0 ? aphx : aphy;
+        const T aq = dA[i][0] * dbdq + dA[i][1] * dsdq + dA[i][2];
         J[i][0] = dA[i][0] * sqq;
         J[i][1] = aq * dq1 + aph * dp1;
         J[i][2] = aq * dq2 + aph * dp2;
@@ -329,58 +348,59 @@ __device__ void nie_alpha_grad(int code, const double* rec, const double* a, dou
 // center_x, center_y), as dual numbers in (Rs, alpha_Rs, r_trunc, x, y) through
 // the same formulas and floors as the forward pass (a floor freezes its
 // argument's derivative).
-__device__ void nfw_alpha_grad(int code, const double* a, double dx, double dy, double& ax,
-                               double& ay, double J[2][GJ]) {
+template <typename T>
+__device__ void nfw_alpha_grad(int code, const T* a, T dx, T dy, T& ax,
+                               T& ay, T J[2][GJ]) {
     const bool trunc = code == LENSGB_LENS_TNFW;
-    const D5 RS = dvar(a[0], 0), ARS = dvar(a[1], 1);
-    const D5 X1 = dvar(dx, 3), Y1 = dvar(dy, 4);
+    const D5<T> RS = dvar(a[0], 0), ARS = dvar(a[1], 1);
+    const D5<T> X1 = dvar(dx, 3), Y1 = dvar(dy, 4);
     // rho0 from the unfloored Rs, as alpha2rho0 does (nfw.py:386-395)
-    const D5 rho0 = ARS * dinv((4.0 * (1.0 + log(0.5))) * (RS * RS));
-    D5 R = dsqrt(X1 * X1 + Y1 * Y1);
-    D5 g, X, RSF;
+    const D5<T> rho0 = ARS * dinv((T(4.0) * (T(1.0) + log(T(0.5)))) * (RS * RS));
+    D5<T> R = dsqrt(X1 * X1 + Y1 * Y1);
+    D5<T> g, X, RSF;
     if (!trunc) {
-        RSF = a[0] < 0.0000001 ? dconst(0.0000001) : RS;
-        if (!(R.v > 0.00000001)) R = dconst(0.00000001);
+        RSF = a[0] < T(0.0000001) ? dconst(T(0.0000001)) : RS;
+        if (!(R.v > T(0.00000001))) R = dconst(T(0.00000001));
         X = R * dinv(RSF);
-        if (X.v < 0.000001) X = dconst(0.000001);
-        if (X.v < 1.0)
-            g = dlog(0.5 * X) + dinv(dsqrt(1.0 + (-1.0) * X * X)) * dacosh(dinv(X));
-        else if (X.v == 1.0)
-            g = dconst(1.0 + log(0.5));
+        if (X.v < T(0.000001)) X = dconst(T(0.000001));
+        if (X.v < T(1.0))
+            g = dlog(T(0.5) * X) + dinv(dsqrt(T(1.0) + (-T(1.0)) * X * X)) * dacosh(dinv(X));
+        else if (X.v == T(1.0))
+            g = dconst(T(1.0) + log(T(0.5)));
         else
-            g = dlog(0.5 * X) + dinv(dsqrt(X * X + dconst(-1.0))) * dacos(dinv(X));
+            g = dlog(T(0.5) * X) + dinv(dsqrt(X * X + dconst(-T(1.0)))) * dacos(dinv(X));
     } else {
         RSF = RS;
-        const D5 tau = dvar(a[2], 2) * dinv(RS);
-        if (!(R.v > 0.001 * a[0])) R = 0.001 * RS;
+        const D5<T> tau = dvar(a[2], 2) * dinv(RS);
+        if (!(R.v > T(0.001) * a[0])) R = T(0.001) * RS;
         X = R * dinv(RS);
-        if (!(X.v > 0.001)) X = dconst(0.001);
-        const D5 x2 = X * X;
-        D5 F;
-        if (X.v < 1.0) {
-            const D5 w = dsqrt(1.0 + (-1.0) * x2);
+        if (!(X.v > T(0.001))) X = dconst(T(0.001));
+        const D5<T> x2 = X * X;
+        D5<T> F;
+        if (X.v < T(1.0)) {
+            const D5<T> w = dsqrt(T(1.0) + (-T(1.0)) * x2);
             F = dinv(w) * datanh(w);
-        } else if (X.v > 1.0) {
-            const D5 w = dsqrt(x2 + dconst(-1.0));
+        } else if (X.v > T(1.0)) {
+            const D5<T> w = dsqrt(x2 + dconst(-T(1.0)));
             F = dinv(w) * datan(w);
         } else {
             F = X;
         }
-        const D5 t2 = tau * tau;
-        const D5 r = dsqrt(t2 + x2);
-        const D5 L = dlog(X * dinv(tau + r));
-        const D5 tp1 = t2 + dconst(1.0), tm1 = t2 + dconst(-1.0);
-        const D5 br = (tp1 + 2.0 * (x2 + dconst(-1.0))) * F + M_PI * tau + tm1 * dlog(tau) +
-                      r * (dconst(-M_PI) + L * tm1 * dinv(tau));
+        const D5<T> t2 = tau * tau;
+        const D5<T> r = dsqrt(t2 + x2);
+        const D5<T> L = dlog(X * dinv(tau + r));
+        const D5<T> tp1 = t2 + dconst(T(1.0)), tm1 = t2 + dconst(-T(1.0));
+        const D5<T> br = (tp1 + T(2.0) * (x2 + dconst(-T(1.0)))) * F + T(M_PI) * tau + tm1 * dlog(tau) +
+                      r * (dconst(-T(M_PI)) + L * tm1 * dinv(tau));
         g = t2 * dinv(tp1 * tp1) * br;
     }
-    const D5 al = 4.0 * rho0 * RSF * g * dinv(X * X);
-    const D5 fx = al * X1, fy = al * Y1;
+    const D5<T> al = T(4.0) * rho0 * RSF * g * dinv(X * X);
+    const D5<T> fx = al * X1, fy = al * Y1;
     ax = fx.v;
     ay = fy.v;
     const int co = trunc ? 3 : 2;
     for (int i = 0; i < 2; ++i) {
-        const D5& f = i == 0 ? fx : fy;
+        const D5<T>& f = i == 0 ? fx : fy;
         J[i][0] = f.d[0];
         J[i][1] = f.d[1];
         if (trunc) J[i][2] = f.d[2];
@@ -390,28 +410,30 @@ __device__ void nfw_alpha_grad(int code, const double* a, double dx, double dy, 
 }
 
 // SHEAR (shear.py:39-53) and its Jacobian w.r.t. (gamma1, gamma2, ra_0, dec_0).
-__device__ __forceinline__ void shear_alpha_grad(const double* rec, double dx, double dy,
-                                                 double& ax, double& ay, double J[2][GJ]) {
-    const double g1 = rec[2], g2 = rec[3];
+template <typename T>
+__device__ __forceinline__ void shear_alpha_grad(const T* rec, T dx, T dy,
+                                                 T& ax, T& ay, T J[2][GJ]) {
+    const T g1 = rec[2], g2 = rec[3];
     ax = g1 * dx + g2 * dy;
     ay = g2 * dx - g1 * dy;
     J[0][0] = dx;  J[1][0] = -dy;
     J[0][1] = dy;  J[1][1] = dx;
     J[0][2] = -g1; J[1][2] = -g2;
     J[0][3] = -g2; J[1][3] = g1;
-    J[0][4] = J[0][5] = J[1][4] = J[1][5] = 0.0;
+    J[0][4] = J[0][5] = J[1][4] = J[1][5] = T(0.0);
 }
 
 // CONVERGENCE (convergence.py:35-46): alpha = kappa (x - ra_0, y - dec_0), and
 // its Jacobian w.r.t. (kappa, ra_0, dec_0).
-__device__ __forceinline__ void convergence_alpha_grad(const double* rec, double dx, double dy,
-                                                       double& ax, double& ay, double J[2][GJ]) {
-    const double k = rec[2];
+template <typename T>
+__device__ __forceinline__ void convergence_alpha_grad(const T* rec, T dx, T dy,
+                                                       T& ax, T& ay, T J[2][GJ]) {
+    const T k = rec[2];
     ax = k * dx;
     ay = k * dy;
     J[0][0] = dx;  J[1][0] = dy;
-    J[0][1] = -k;  J[1][1] = 0.0;
-    J[0][2] = 0.0; J[1][2] = -k;
+    J[0][1] = -k;  J[1][1] = T(0.0);
+    J[0][2] = T(0.0); J[1][2] = -k;
 }
 
 // NFW_ELLIPSE_CSE (nfw_ellipse_cse.py:250-280 -> cored_steep_ellipsoid.py:
@@ -420,48 +442,49 @@ __device__ __forceinline__ void convergence_alpha_grad(const double* rec, double
 // numbers in (Rs, alpha_Rs, q, x1, y1), with the normalisation
 // 4 rho0 Rs^3 / Rs = alpha_Rs / (1 + ln 1/2) (nfw.py:386-395), rotated back and
 // chained to (e1, e2) through (phi, q) as for EPL.
-__device__ void cse_alpha_grad(const double* rec, const double* a, double dx, double dy,
-                               double& ax, double& ay, double J[2][GJ]) {
-    const double q = rec[4], c = rec[5], sn = rec[6];
-    const double x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
-    const D5 RS = dvar(a[0], 0), ARS = dvar(a[1], 1), Q = dvar(q, 2);
-    const D5 X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
-    const D5 iRS = dinv(RS);
-    const D5 sq = dsqrt(Q);
-    const D5 xa = X1 * iRS * sq, ya = Y1 * iRS * sq;
-    const D5 q2 = Q * Q, omq2 = 1.0 + (-1.0) * q2;
-    const D5 xa2 = xa * xa, ya2 = ya * ya;
-    const D5 iq = dinv(Q);
-    D5 fx = dconst(0.0), fy = dconst(0.0);
+template <typename T>
+__device__ void cse_alpha_grad(const T* rec, const T* a, T dx, T dy,
+                               T& ax, T& ay, T J[2][GJ]) {
+    const T q = rec[4], c = rec[5], sn = rec[6];
+    const T x1 = c * dx + sn * dy, y1 = -sn * dx + c * dy;
+    const D5<T> RS = dvar(a[0], 0), ARS = dvar(a[1], 1), Q = dvar(q, 2);
+    const D5<T> X1 = dvar(x1, 3), Y1 = dvar(y1, 4);
+    const D5<T> iRS = dinv(RS);
+    const D5<T> sq = dsqrt(Q);
+    const D5<T> xa = X1 * iRS * sq, ya = Y1 * iRS * sq;
+    const D5<T> q2 = Q * Q, omq2 = T(1.0) + (-T(1.0)) * q2;
+    const D5<T> xa2 = xa * xa, ya2 = ya * ya;
+    const D5<T> iq = dinv(Q);
+    D5<T> fx = dconst(T(0.0)), fy = dconst(T(0.0));
     for (int k = 0; k < CSE_NFW_TERMS; ++k) {
-        const double s = kCseNfwS[k];
-        const D5 am = kCseNfwA[k] * iq;
-        const D5 psi = dsqrt(q2 * (xa2 + dconst(s * s)) + ya2);
-        const D5 ps = psi + dconst(s);
-        const D5 Phi = ps * ps + omq2 * xa2;
-        const D5 den = dinv(s * (psi * Phi));
+        const T s = T(kCseNfwS[k]);
+        const D5<T> am = T(kCseNfwA[k]) * iq;
+        const D5<T> psi = dsqrt(q2 * (xa2 + dconst(s * s)) + ya2);
+        const D5<T> ps = psi + dconst(s);
+        const D5<T> Phi = ps * ps + omq2 * xa2;
+        const D5<T> den = dinv(s * (psi * Phi));
         fx = fx + am * (Q * xa * (psi + s * q2) * den);
         fy = fy + am * (Q * ya * ps * den);
     }
-    const D5 cst = (1.0 / (1.0 + log(0.5))) * ARS * sq;
+    const D5<T> cst = (T(1.0) / (T(1.0) + log(T(0.5)))) * ARS * sq;
     fx = cst * fx;
     fy = cst * fy;
     ax = fx.v * c - fy.v * sn;
     ay = fx.v * sn + fy.v * c;
-    double dA[2][5];
+    T dA[2][5];
     for (int k = 0; k < 5; ++k) {
         dA[0][k] = fx.d[k] * c - fy.d[k] * sn;
         dA[1][k] = fx.d[k] * sn + fy.d[k] * c;
     }
-    const double gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
-    const double gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
-    const double aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
-    const double jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
-    const double jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
-    double dq1, dq2, dp1, dp2;
+    const T gx = -fy.v + fx.d[3] * y1 - fx.d[4] * x1;
+    const T gy = fx.v + fy.d[3] * y1 - fy.d[4] * x1;
+    const T aphx = gx * c - gy * sn, aphy = gx * sn + gy * c;
+    const T jdx0 = dA[0][3] * c - dA[0][4] * sn, jdx1 = dA[1][3] * c - dA[1][4] * sn;
+    const T jdy0 = dA[0][3] * sn + dA[0][4] * c, jdy1 = dA[1][3] * sn + dA[1][4] * c;
+    T dq1, dq2, dp1, dp2;
     dphiq_de(a[2], a[3], dq1, dq2, dp1, dp2);
     for (int i = 0; i < 2; ++i) {
-        const double aph = i == 0 ? aphx : aphy;
+        const T aph = i == 0 ? aphx : aphy;
         J[i][0] = dA[i][0];
         J[i][1] = dA[i][1];
         J[i][2] = dA[i][2] * dq1 + aph * dp1;
@@ -479,48 +502,49 @@ __device__ void cse_alpha_grad(const double* rec, const double* a, double dx, do
 // delta_phi_m4).  The multipoles are linear in a_m; their position derivatives
 // go through the polar radius (m = 1 only, zero where r is floored at 1e-6)
 // and the polar angle (zero at the centre itself, where atan2 has none).
-__device__ void multipole_alpha_grad(const double* rec, const double* F, const double* dF,
-                                     const double* a, double dx, double dy, double& ax,
-                                     double& ay, double J[2][GJ]) {
+template <typename T>
+__device__ void multipole_alpha_grad(const T* rec, const T* F, const T* dF,
+                                     const T* a, T dx, T dy, T& ax,
+                                     T& ay, T J[2][GJ]) {
     epl_alpha_grad(rec, F, dF, a, dx, dy, ax, ay, J);
-    const double q = rec[4], rE = rec[31];
-    const double r0 = sqrt(dx * dx + dy * dy);
-    const double phi = atan2(dy, dx);
-    const double cph = cos(phi), sph = sin(phi);
-    const double r1 = r0 > 0.000001 ? r0 : 0.000001;
-    const double L = log(r1 / rE);
-    const double am[3] = {2.0 * rec[16], rec[27], rec[29]};
-    const double pm[3] = {rec[26], rec[28], rec[30]};
-    double fx = 0.0, fy = 0.0;
-    double dfa[3][2], dfp[3][2];    // d f / d a_m, d f / d phi_m
-    double dfr[2] = {0.0, 0.0};     // d f / d r (through ln r, m = 1)
-    double dfph[2] = {0.0, 0.0};    // d f / d (polar angle)
-    double dfrE[2];                 // d f / d r_E
+    const T q = rec[4], rE = rec[31];
+    const T r0 = sqrt(dx * dx + dy * dy);
+    const T phi = atan2(dy, dx);
+    const T cph = cos(phi), sph = sin(phi);
+    const T r1 = r0 > T(0.000001) ? r0 : T(0.000001);
+    const T L = log(r1 / rE);
+    const T am[3] = {T(2.0) * rec[16], rec[27], rec[29]};
+    const T pm[3] = {rec[26], rec[28], rec[30]};
+    T fx = T(0.0), fy = T(0.0);
+    T dfa[3][2], dfp[3][2];    // d f / d a_m, d f / d phi_m
+    T dfr[2] = {T(0.0), T(0.0)};     // d f / d r (through ln r, m = 1)
+    T dfph[2] = {T(0.0), T(0.0)};    // d f / d (polar angle)
+    T dfrE[2];                 // d f / d r_E
     {
-        const double A = am[0], P = pm[0];
-        const double cp = cos(P), sp = sin(P), cd = cos(phi - P), sd = sin(phi - P);
-        const double ux = 0.5 * (cp * L + cd * cph), uy = 0.5 * (sp * L + cd * sph);
+        const T A = am[0], P = pm[0];
+        const T cp = cos(P), sp = sin(P), cd = cos(phi - P), sd = sin(phi - P);
+        const T ux = T(0.5) * (cp * L + cd * cph), uy = T(0.5) * (sp * L + cd * sph);
         fx += A * ux;
         fy += A * uy;
         dfa[0][0] = ux;
         dfa[0][1] = uy;
-        dfp[0][0] = 0.5 * A * (-sp * L + sd * cph);
-        dfp[0][1] = 0.5 * A * (cp * L + sd * sph);
-        dfrE[0] = -0.5 * A * cp / rE;
-        dfrE[1] = -0.5 * A * sp / rE;
-        if (r0 > 0.000001) {
-            dfr[0] += 0.5 * A * cp / r0;
-            dfr[1] += 0.5 * A * sp / r0;
+        dfp[0][0] = T(0.5) * A * (-sp * L + sd * cph);
+        dfp[0][1] = T(0.5) * A * (cp * L + sd * sph);
+        dfrE[0] = -T(0.5) * A * cp / rE;
+        dfrE[1] = -T(0.5) * A * sp / rE;
+        if (r0 > T(0.000001)) {
+            dfr[0] += T(0.5) * A * cp / r0;
+            dfr[1] += T(0.5) * A * sp / r0;
         }
         // d/dphi of cos(phi - P) cos(phi) and cos(phi - P) sin(phi)
-        dfph[0] += 0.5 * A * (-sd * cph - cd * sph);
-        dfph[1] += 0.5 * A * (-sd * sph + cd * cph);
+        dfph[0] += T(0.5) * A * (-sd * cph - cd * sph);
+        dfph[1] += T(0.5) * A * (-sd * sph + cd * cph);
     }
     for (int j = 1; j < 3; ++j) {
-        const double m = j == 1 ? 3.0 : 4.0, A = am[j], P = pm[j];
-        const double k = 1.0 / (1.0 - m * m);
-        const double C = cos(m * (phi - P)), S = sin(m * (phi - P));
-        const double ux = k * (cph * C + m * sph * S), uy = k * (sph * C - m * cph * S);
+        const T m = j == 1 ? T(3.0) : T(4.0), A = am[j], P = pm[j];
+        const T k = T(1.0) / (T(1.0) - m * m);
+        const T C = cos(m * (phi - P)), S = sin(m * (phi - P));
+        const T ux = k * (cph * C + m * sph * S), uy = k * (sph * C - m * cph * S);
         fx += A * ux;
         fy += A * uy;
         dfa[j][0] = ux;
@@ -533,21 +557,21 @@ __device__ void multipole_alpha_grad(const double* rec, const double* F, const d
     ax += fx;
     ay += fy;
     // position: d/d(dx, dy) = d/dr (cos, sin) + d/dphi (-sin, cos) / r
-    double fdx[2], fdy[2];
-    const double ir = r0 > 0.0 ? 1.0 / r0 : 0.0;
+    T fdx[2], fdy[2];
+    const T ir = r0 > T(0.0) ? T(1.0) / r0 : T(0.0);
     for (int i = 0; i < 2; ++i) {
         fdx[i] = dfr[i] * cph - dfph[i] * sph * ir;
         fdy[i] = dfr[i] * sph + dfph[i] * cph * ir;
     }
-    const double theta_E = a[0], sqq = sqrt(q);
-    double dq1, dq2, dp1, dp2;
+    const T theta_E = a[0], sqq = sqrt(q);
+    T dq1, dq2, dp1, dp2;
     dphiq_de(a[2], a[3], dq1, dq2, dp1, dp2);
     for (int i = 0; i < 2; ++i) {
-        double dth = dfrE[i], dq = 0.0, dphi_epl = 0.0;
+        T dth = dfrE[i], dq = T(0.0), dphi_epl = T(0.0);
         for (int j = 0; j < 3; ++j) {
-            const double araw = a[6 + 2 * j];
+            const T araw = a[6 + 2 * j];
             dth += dfa[j][i] * araw / sqq;
-            dq += dfa[j][i] * (-0.5 * am[j] / q);
+            dq += dfa[j][i] * (-T(0.5) * am[j] / q);
             dphi_epl += dfp[j][i];
             J[i][6 + 2 * j] = dfa[j][i] * theta_E / sqq;
             J[i][7 + 2 * j] = dfp[j][i];
@@ -564,51 +588,52 @@ __device__ void multipole_alpha_grad(const double* rec, const double* F, const d
 // 239-267) at offset (dx, dy): value, gradient with respect to the offset,
 // and derivatives with respect to the raw parameters (amp, R_sersic, n_sersic,
 // [e1, e2,] center_x, center_y).
-__device__ void sersic_grad(int code, const double* rec, const double* a, double dx, double dy,
-                            double& I, double& gx, double& gy, double dI[7]) {
+template <typename T>
+__device__ void sersic_grad(int code, const T* rec, const T* a, T dx, T dy,
+                            T& I, T& gx, T& gy, T dI[7]) {
     const bool ell = code == LENSGB_LIGHT_SERSIC_ELLIPSE;
     const int np = ell ? 7 : 5;
-    for (int k = 0; k < np; ++k) dI[k] = 0.0;
-    I = 0.0;
-    gx = 0.0;
-    gy = 0.0;
-    const double amp = rec[2], Rs = rec[3], inv_n = rec[5], bn = rec[6];
-    const double m00 = rec[7], m01 = rec[8], m10 = rec[9], m11 = rec[10];
-    const double xp = m00 * dx + m01 * dy, yp = m10 * dx + m11 * dy;
-    const double Rraw = sqrt(xp * xp + yp * yp);
-    const bool floored = !(Rraw > 0.0001);
-    const double R = floored ? 0.0001 : Rraw;
-    const double frac = R / Rs;
-    if (!(frac <= 1000.0)) return;
-    const double v = pow(frac, inv_n);
-    const double res = exp(-bn * (v - 1.0));
+    for (int k = 0; k < np; ++k) dI[k] = T(0.0);
+    I = T(0.0);
+    gx = T(0.0);
+    gy = T(0.0);
+    const T amp = rec[2], Rs = rec[3], inv_n = rec[5], bn = rec[6];
+    const T m00 = rec[7], m01 = rec[8], m10 = rec[9], m11 = rec[10];
+    const T xp = m00 * dx + m01 * dy, yp = m10 * dx + m11 * dy;
+    const T Rraw = sqrt(xp * xp + yp * yp);
+    const bool floored = !(Rraw > T(0.0001));
+    const T R = floored ? T(0.0001) : Rraw;
+    const T frac = R / Rs;
+    if (!(frac <= T(1000.0))) return;
+    const T v = pow(frac, inv_n);
+    const T res = exp(-bn * (v - T(1.0)));
     I = amp * res;
     // d ln I / d R (zero inside the smoothing floor)
-    const double dlR = floored ? 0.0 : -bn * inv_n * v / R;
-    double dRdx = 0.0, dRdy = 0.0;
+    const T dlR = floored ? T(0.0) : -bn * inv_n * v / R;
+    T dRdx = T(0.0), dRdy = T(0.0);
     if (!floored) {
         dRdx = (xp * m00 + yp * m10) / R;
         dRdy = (xp * m01 + yp * m11) / R;
     }
     gx = I * dlR * dRdx;
     gy = I * dlR * dRdy;
-    const double n = a[2];
+    const T n = a[2];
     dI[0] = res;                                                  // amp
-    dI[1] = a[1] > 0.0001 ? I * bn * inv_n * v / Rs : 0.0;        // R_sersic (floors)
-    const double dbn = (1.9992 * n - 0.3271) > 0.00001 ? 1.9992 : 0.0;
-    dI[2] = I * (-dbn * (v - 1.0) + bn * v * log(frac) * inv_n * inv_n);  // n_sersic
+    dI[1] = a[1] > T(0.0001) ? I * bn * inv_n * v / Rs : T(0.0);        // R_sersic (floors)
+    const T dbn = (T(1.9992) * n - T(0.3271)) > T(0.00001) ? T(1.9992) : T(0.0);
+    dI[2] = I * (-dbn * (v - T(1.0)) + bn * v * log(frac) * inv_n * inv_n);  // n_sersic
     int k = 3;
     if (ell) {
-        const double e1 = a[3], e2 = a[4];
-        const double n2 = 1.0 - e1 * e1 - e2 * e2;
-        const double nrm_raw = sqrt(fabs(n2));
-        const bool nfl = !(nrm_raw > 0.000001);
-        const double nrm = nfl ? 0.000001 : nrm_raw;
-        const double sgn = n2 > 0 ? -1.0 : 1.0;
-        const double dn1 = nfl ? 0.0 : sgn * e1 / nrm, dn2 = nfl ? 0.0 : sgn * e2 / nrm;
+        const T e1 = a[3], e2 = a[4];
+        const T n2 = T(1.0) - e1 * e1 - e2 * e2;
+        const T nrm_raw = sqrt(fabs(n2));
+        const bool nfl = !(nrm_raw > T(0.000001));
+        const T nrm = nfl ? T(0.000001) : nrm_raw;
+        const T sgn = n2 > 0 ? -T(1.0) : T(1.0);
+        const T dn1 = nfl ? T(0.0) : sgn * e1 / nrm, dn2 = nfl ? T(0.0) : sgn * e2 / nrm;
         // x' = ((1-e1) dx - e2 dy)/norm, y' = (-e2 dx + (1+e1) dy)/norm
-        const double dxp1 = -dx / nrm - xp * dn1 / nrm, dyp1 = dy / nrm - yp * dn1 / nrm;
-        const double dxp2 = -dy / nrm - xp * dn2 / nrm, dyp2 = -dx / nrm - yp * dn2 / nrm;
+        const T dxp1 = -dx / nrm - xp * dn1 / nrm, dyp1 = dy / nrm - yp * dn1 / nrm;
+        const T dxp2 = -dy / nrm - xp * dn2 / nrm, dyp2 = -dx / nrm - yp * dn2 / nrm;
         if (!floored) {
             dI[3] = I * dlR * (xp * dxp1 + yp * dyp1) / R;
             dI[4] = I * dlR * (xp * dxp2 + yp * dyp2) / R;
@@ -718,15 +743,34 @@ __global__ void flip_psf_kernel(const double* __restrict__ in, double* __restric
     out[inst * kk + j] = in[inst * in_stride + (kk - 1 - j)];
 }
 
-// Step 3: per-CTA partial gradients of one system.
+// Step 3: per-CTA partial gradients of one system.  T = double: every ray
+// derivative in FP64.  T = float (FP32 split): the records, EPL tables and the
+// parameter row are copied to FP32 once per CTA; each pixel's offsets of its
+// first ray from every profile centre are formed in FP64 and rounded once,
+// the sub-ray displacements (below a pixel) are added in FP32, the dual numbers
+// run in FP32, and each thread's sums go to the FP64 block reduction.
+//
+// Pixels whose FP32 derivatives would be ill-conditioned -- rays landing near a
+// steep source centre, where beta = theta - alpha cancels and FP32's few-ulp
+// error of alpha moves d I / d beta by (|grad ln I| + 1/R) kappa |alpha| in
+// relative terms -- are flagged (FLAG_PASS: flag[pix] = 1, the pixel's FP32
+// terms dropped) and recomputed by the FP64 instantiation over the flagged
+// pixels only (ONLY_FLAGGED), into a second set of partial sums.
+constexpr int GRAD_ALL = 0, GRAD_FLAG_PASS = 1, GRAD_ONLY_FLAGGED = 2;
+constexpr float GRAD_KAPPA = 3e-7f;  // FP32 relative error bound of a deflection
+
+template <typename T>
 __global__ void __launch_bounds__(GRAD_THREADS)
 grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                 const double* __restrict__ rec, const double* __restrict__ coef,
                 const double* __restrict__ dcoef, const double* __restrict__ glow,
-                double w_scale, double* __restrict__ partial) {
+                double w_scale, double* __restrict__ partial, unsigned char* __restrict__ flag,
+                float tau, int mode) {
+    constexpr bool F32 = sizeof(T) == 4;
     extern __shared__ double smem[];
     const int inst = blockIdx.y;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
+    const int NP = st.n_params;
     double* srec = smem;
     double* scoef = srec + n_prof * REC_D;
     double* sdcoef = scoef + st.n_epl * EPL_NMAX;
@@ -739,39 +783,95 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
         for (int k = threadIdx.x; k < nmax; k += blockDim.x) sdcoef[es * EPL_NMAX + k] = gc[k];
     }
     __syncthreads();
-    const double* P = params + (long long)inst * st.n_params;
-    const int NP = st.n_params;
-    double acc[GRAD_MAXP];
-    for (int k = 0; k < NP; ++k) acc[k] = 0.0;
+    const double* Pd = params + (long long)inst * NP;
+    const T* trec = reinterpret_cast<const T*>(srec);
+    const T* tcoef = reinterpret_cast<const T*>(scoef);
+    const T* tdcoef = reinterpret_cast<const T*>(sdcoef);
+    const T* P = reinterpret_cast<const T*>(Pd);
+    if (F32) {
+        // FP32 copies after the FP64 arrays
+        float* f = reinterpret_cast<float*>(sdcoef + st.n_epl * EPL_NMAX);
+        const int nr = n_prof * REC_D, nc = st.n_epl * EPL_NMAX;
+        for (int k = threadIdx.x; k < nr; k += blockDim.x) f[k] = (float)srec[k];
+        for (int k = threadIdx.x; k < nc; k += blockDim.x) {
+            f[nr + k] = (float)scoef[k];
+            f[nr + nc + k] = (float)sdcoef[k];
+        }
+        for (int k = threadIdx.x; k < NP; k += blockDim.x) f[nr + 2 * nc + k] = (float)Pd[k];
+        __syncthreads();
+        trec = reinterpret_cast<const T*>(f);
+        tcoef = reinterpret_cast<const T*>(f + nr);
+        tdcoef = reinterpret_cast<const T*>(f + nr + nc);
+        P = reinterpret_cast<const T*>(f + nr + 2 * nc);
+    }
+    T acc[GRAD_MAXP], pacc[GRAD_MAXP];
+    for (int k = 0; k < NP; ++k) acc[k] = T(0);
     const long long npix = (long long)g.nx * g.ny;
     const long long base = (long long)blockIdx.x * GRAD_THREADS * GRAD_PPT;
     const double* gl = glow + (long long)inst * npix;
     const double inv_s2 = 1.0 / ((double)g.s * g.s);
+    const T alpha_scaling = (T)st.alpha_scaling;
+    const T axf = (T)g.ax, bxf = (T)g.bx, ayf = (T)g.ay, byf = (T)g.by;
     for (int kk = 0; kk < GRAD_PPT; ++kk) {
         const long long pix = base + (long long)kk * GRAD_THREADS + threadIdx.x;
         if (pix >= npix) break;
         const int row = (int)(pix / g.nx), col = (int)(pix % g.nx);
-        const double w = gl[pix] * w_scale * inv_s2 * st.flux_scaling;
-        if (w == 0.0) continue;
+        const double wd = gl[pix] * w_scale * inv_s2 * st.flux_scaling;
+        if (wd == 0.0) continue;
+        if (mode == GRAD_ONLY_FLAGGED && !flag[(long long)inst * npix + pix]) continue;
+        const T w = (T)wd;
+        // this pixel's terms, kept apart until its rays are known well-conditioned
+        T* tgt = mode == GRAD_FLAG_PASS ? pacc : acc;
+        if (mode == GRAD_FLAG_PASS)
+            for (int k = 0; k < NP; ++k) pacc[k] = T(0);
+        bool ill = false;
+        // FP32: the first ray's offsets from every profile centre, in FP64, rounded once
+        T ox[MAX_PROF * 3], oy[MAX_PROF * 3];
+        if (F32) {
+            const double X0 = g.ra00 + (double)(col * g.s) * g.ax + (double)(row * g.s) * g.bx;
+            const double Y0 = g.dec00 + (double)(col * g.s) * g.ay + (double)(row * g.s) * g.by;
+            for (int p = 0; p < n_prof; ++p) {
+                ox[p] = (T)(X0 - srec[p * REC_D + RD_CX]);
+                oy[p] = (T)(Y0 - srec[p * REC_D + RD_CY]);
+            }
+        }
         for (int si = 0; si < g.s; ++si) {
             for (int sj = 0; sj < g.s; ++sj) {
                 const int I = row * g.s + si, Jc = col * g.s + sj;
-                const double X = g.ra00 + (double)Jc * g.ax + (double)I * g.bx;
-                const double Y = g.dec00 + (double)Jc * g.ay + (double)I * g.by;
-                double axs = 0.0, ays = 0.0;
-                double dA[2][GRAD_MAX_LENSP];
+                double X = 0.0, Y = 0.0;
+                T ddx_s = T(0), ddy_s = T(0);
+                if (F32) {
+                    ddx_s = (T)sj * axf + (T)si * bxf;
+                    ddy_s = (T)sj * ayf + (T)si * byf;
+                } else {
+                    X = g.ra00 + (double)Jc * g.ax + (double)I * g.bx;
+                    Y = g.dec00 + (double)Jc * g.ay + (double)I * g.by;
+                }
+                // offset of this ray from the centre of profile p
+                auto off = [&](int p, T& dx, T& dy) {
+                    if (F32) {
+                        dx = ox[p] + ddx_s;
+                        dy = oy[p] + ddy_s;
+                    } else {
+                        dx = (T)(X - srec[p * REC_D + RD_CX]);
+                        dy = (T)(Y - srec[p * REC_D + RD_CY]);
+                    }
+                };
+                T axs = T(0), ays = T(0);
+                T dA[2][GRAD_MAX_LENSP];
                 int lp = 0;
                 for (int p = 0; p < st.n_lens; ++p) {
-                    const double* r = srec + p * REC_D;
+                    const T* r = trec + p * REC_D;
                     const int code = st.lens[p];
                     const int es = st.epl_slot[p];
-                    double ax, ay, J[2][GJ];
-                    const double ddx = X - r[RD_CX], ddy = Y - r[RD_CY];
+                    T ax, ay, J[2][GJ];
+                    T ddx, ddy;
+                    off(p, ddx, ddy);
                     if (code == LENSGB_LENS_EPL)
-                        epl_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
+                        epl_alpha_grad(r, tcoef + es * EPL_NMAX, tdcoef + es * EPL_NMAX,
                                        P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else if (code == LENSGB_LENS_EPL_MULTIPOLE_M1M3M4)
-                        multipole_alpha_grad(r, scoef + es * EPL_NMAX, sdcoef + es * EPL_NMAX,
+                        multipole_alpha_grad(r, tcoef + es * EPL_NMAX, tdcoef + es * EPL_NMAX,
                                              P + st.lens_off[p], ddx, ddy, ax, ay, J);
                     else if (code == LENSGB_LENS_SIE || code == LENSGB_LENS_NIE)
                         nie_alpha_grad(code, r, P + st.lens_off[p], ddx, ddy, ax, ay, J);
@@ -792,40 +892,58 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
                     }
                     lp += np;
                 }
-                axs *= st.alpha_scaling;
-                ays *= st.alpha_scaling;
+                axs *= alpha_scaling;
+                ays *= alpha_scaling;
                 // sources at beta; G = sum_k (-alpha_scaling s_k) grad_beta I_k
-                double Gx = 0.0, Gy = 0.0;
+                T Gx = T(0), Gy = T(0);
                 for (int k = 0; k < st.n_src; ++k) {
-                    const double* r = srec + (st.n_lens + k) * REC_D;
-                    const double sc = st.src_scale[k];
-                    double Iv, gx, gy, dI[7];
-                    sersic_grad(st.src[k], r, P + st.src_off[k], X - sc * axs - r[RD_CX],
-                                Y - sc * ays - r[RD_CY], Iv, gx, gy, dI);
+                    const int pp = st.n_lens + k;
+                    const T* r = trec + pp * REC_D;
+                    const T sc = (T)st.src_scale[k];
+                    T Iv, gx, gy, dI[7], ddx, ddy;
+                    off(pp, ddx, ddy);
+                    const T bdx = ddx - sc * axs, bdy = ddy - sc * ays;
+                    sersic_grad(st.src[k], r, P + st.src_off[k], bdx, bdy, Iv, gx, gy, dI);
                     const int np = st.src[k] == LENSGB_LIGHT_SERSIC_ELLIPSE ? 7 : 5;
-                    for (int j = 0; j < np; ++j) acc[st.src_off[k] + j] += w * dI[j];
-                    Gx -= st.alpha_scaling * sc * gx;
-                    Gy -= st.alpha_scaling * sc * gy;
+                    for (int j = 0; j < np; ++j) tgt[st.src_off[k] + j] += w * dI[j];
+                    Gx -= alpha_scaling * sc * gx;
+                    Gy -= alpha_scaling * sc * gy;
+                    if (mode == GRAD_FLAG_PASS && Iv > T(0)) {
+                        // relative error of d I / d beta from the FP32 error of beta
+                        const T xp = r[7] * bdx + r[8] * bdy, yp = r[9] * bdx + r[10] * bdy;
+                        const T R = fmax(sqrt(xp * xp + yp * yp), T(0.0001));
+                        const T gl_ = sqrt(gx * gx + gy * gy) / Iv;
+                        const T pred = (gl_ + T(1) / R) * (T)GRAD_KAPPA * sc *
+                                       (fabs(axs) + fabs(ays));
+                        ill |= pred > (T)tau;
+                    }
                 }
                 for (int c = 0; c < lp; ++c)
-                    acc[st.lens_off[0] + c] += w * (Gx * dA[0][c] + Gy * dA[1][c]);
+                    tgt[st.lens_off[0] + c] += w * (Gx * dA[0][c] + Gy * dA[1][c]);
                 // lens light at theta
                 for (int k = 0; k < st.n_ll; ++k) {
-                    const double* r = srec + (st.n_lens + st.n_src + k) * REC_D;
-                    double Iv, gx, gy, dI[7];
-                    sersic_grad(st.ll[k], r, P + st.ll_off[k], X - r[RD_CX], Y - r[RD_CY], Iv, gx,
-                                gy, dI);
+                    const int pp = st.n_lens + st.n_src + k;
+                    const T* r = trec + pp * REC_D;
+                    T Iv, gx, gy, dI[7], ddx, ddy;
+                    off(pp, ddx, ddy);
+                    sersic_grad(st.ll[k], r, P + st.ll_off[k], ddx, ddy, Iv, gx, gy, dI);
                     const int np = st.ll[k] == LENSGB_LIGHT_SERSIC_ELLIPSE ? 7 : 5;
-                    for (int j = 0; j < np; ++j) acc[st.ll_off[k] + j] += w * dI[j];
+                    for (int j = 0; j < np; ++j) tgt[st.ll_off[k] + j] += w * dI[j];
                 }
             }
+        }
+        if (mode == GRAD_FLAG_PASS) {
+            if (ill)
+                flag[(long long)inst * npix + pix] = 1;  // the FP64 pass takes this pixel
+            else
+                for (int k = 0; k < NP; ++k) acc[k] += pacc[k];
         }
     }
     // fixed-order block reduction, one parameter at a time
     __shared__ double red[GRAD_THREADS];
     double* out = partial + ((long long)inst * gridDim.x + blockIdx.x) * NP;
     for (int k = 0; k < NP; ++k) {
-        red[threadIdx.x] = acc[k];
+        red[threadIdx.x] = (double)acc[k];
         __syncthreads();
         for (int s2 = GRAD_THREADS / 2; s2 > 0; s2 >>= 1) {
             if (threadIdx.x < s2) red[threadIdx.x] += red[threadIdx.x + s2];
@@ -836,13 +954,22 @@ grad_ray_kernel(GridDesc g, StackDesc st, const double* __restrict__ params,
     }
 }
 
-__global__ void grad_reduce_kernel(const double* __restrict__ partial, int n_chunks, int NP,
+// Sums the per-CTA partials in a fixed order; partial2 (or null): the partials
+// of the FP64 pass over flagged pixels, added after the first set.
+__global__ void grad_reduce_kernel(const double* __restrict__ partial,
+                                   const double* __restrict__ partial2, int n_chunks, int NP,
                                    int n_inst, double* __restrict__ grad) {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= n_inst * NP) return;
     const int inst = gid / NP, k = gid % NP;
     double s = 0.0;
     for (int c = 0; c < n_chunks; ++c) s += partial[((long long)inst * n_chunks + c) * NP + k];
+    if (partial2) {
+        double s2 = 0.0;
+        for (int c = 0; c < n_chunks; ++c)
+            s2 += partial2[((long long)inst * n_chunks + c) * NP + k];
+        s += s2;
+    }
     grad[gid] = s;
 }
 
@@ -980,7 +1107,8 @@ int launch_scale(double* x, long long n, double a, cudaStream_t stream) {
 
 int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
                      const double* rec_d, const double* coef_d, double* dcoef, const double* gl,
-                     double w_scale, double* partial, double* grad, cudaStream_t stream) {
+                     double w_scale, double* partial, double* grad, int precision,
+                     unsigned char* flag, float tau, cudaStream_t stream) {
     if (n_inst <= 0) return 0;
     if (st.n_lens > 0) {
         const int n = n_inst * st.n_lens;
@@ -988,15 +1116,35 @@ int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const d
     }
     const int chunks = grad_chunks(g);
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
-    const size_t smem = (size_t)(n_prof * REC_D + 2 * st.n_epl * EPL_NMAX) * sizeof(double);
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(grad_ray_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    grad_ray_kernel<<<dim3((unsigned)chunks, (unsigned)n_inst), GRAD_THREADS, smem, stream>>>(
-        g, st, params, rec_d, coef_d, dcoef, gl, w_scale, partial);
+    const size_t nd = (size_t)(n_prof * REC_D + 2 * st.n_epl * EPL_NMAX);
+    const dim3 grid((unsigned)chunks, (unsigned)n_inst);
+    const size_t smem64 = nd * sizeof(double);
+    if (smem64 > 48 * 1024)
+        cudaFuncSetAttribute(grad_ray_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem64);
+    double* partial2 = nullptr;
+    if (precision == LENSGB_FP64) {
+        grad_ray_kernel<double><<<grid, GRAD_THREADS, smem64, stream>>>(
+            g, st, params, rec_d, coef_d, dcoef, gl, w_scale, partial, nullptr, 0.f, GRAD_ALL);
+    } else {
+        // the FP64 arrays, then their FP32 copies and the FP32 parameter row
+        const size_t smem = nd * sizeof(double) + (nd + (size_t)st.n_params) * sizeof(float);
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(grad_ray_kernel<float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const long long npix = (long long)g.nx * g.ny;
+        if (cudaMemsetAsync(flag, 0, (size_t)n_inst * npix, stream) != cudaSuccess) return -1;
+        partial2 = partial + (size_t)n_inst * chunks * st.n_params;
+        grad_ray_kernel<float><<<grid, GRAD_THREADS, smem, stream>>>(
+            g, st, params, rec_d, coef_d, dcoef, gl, w_scale, partial, flag, tau,
+            GRAD_FLAG_PASS);
+        grad_ray_kernel<double><<<grid, GRAD_THREADS, smem64, stream>>>(
+            g, st, params, rec_d, coef_d, dcoef, gl, w_scale, partial2, flag, tau,
+            GRAD_ONLY_FLAGGED);
+    }
     const int n = n_inst * st.n_params;
-    grad_reduce_kernel<<<(n + 127) / 128, 128, 0, stream>>>(partial, chunks, st.n_params, n_inst,
-                                                           grad);
+    grad_reduce_kernel<<<(n + 127) / 128, 128, 0, stream>>>(partial, partial2, chunks,
+                                                           st.n_params, n_inst, grad);
     return 0;
 }
 

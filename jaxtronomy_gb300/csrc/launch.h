@@ -187,7 +187,10 @@ int launch_linear_solve(const void* A, int n_lin, int n_inst, long long npix, co
 //     by 180 degrees; edge = 1: edge padding, through pad_a / pad_b scratch of
 //     (ny + K - 1) x (nx + K - 1) per system); psf_flip: n_inst x K^2 scratch;
 //   launch_expand: the transposed s x s block mean (hr = low x scale per block);
-//   launch_grad_rays: forward-mode derivatives of every ray of grid g weighted
+//   launch_grad_rays: forward-mode derivatives (precision LENSGB_FP64, or
+//     LENSGB_FP32_SPLIT: FP32 dual numbers from FP64-accurate offsets, pixels
+//     predicted ill-conditioned recomputed in FP64; `flag`: n_inst x pixels of g
+//     bytes, `partial` then twice its FP64 size) of every ray of grid g weighted
 //     by gl x w_scale / s^2 x flux_scaling, summed per parameter in a fixed
 //     order into grad (n_inst x n_params); dcoef: n_inst x n_epl x EPL_NMAX and
 //     partial: n_inst x grad_chunks(g) x n_params scratch.
@@ -208,7 +211,8 @@ int launch_expand(const double* low, double* hr, int n_inst, int ny, int nx, int
 int launch_scale(double* x, long long n, double a, cudaStream_t stream);
 int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const double* params,
                      const double* rec_d, const double* coef_d, double* dcoef, const double* gl,
-                     double w_scale, double* partial, double* grad, cudaStream_t stream);
+                     double w_scale, double* partial, double* grad, int precision,
+                     unsigned char* flag, float tau, cudaStream_t stream);
 
 // Point-wise single-parameter-set evaluation (FP64).
 int launch_ray_shoot_points(const StackDesc& st, const double* rec_d, const double* coef_d,

@@ -34,7 +34,7 @@ _NUMERICS_KEYS = {
     "supersampling_kernel_size", "flux_evaluate_indexes", "supersampled_indexes",
     "compute_indexes", "point_source_supersampling_factor", "convolution_kernel_size",
     "convolution_type", "truncation_conv", "precision", "fp32_refine_tol", "fp32_refine_kappa",
-    "convolution_method",
+    "convolution_method", "gradient_precision",
 }
 
 
@@ -173,6 +173,13 @@ class ImageModel:
         if method not in _lib.CONV_METHODS:
             raise ValueError("convolution_method must be one of %s" % sorted(_lib.CONV_METHODS))
         self._conv_method = _lib.CONV_METHODS[method]
+        # arithmetic of the adjoint's ray derivatives (an option of this library):
+        # "fp64" (default) or "fp32" (FP32 dual numbers from FP64-accurate
+        # offsets, FP64 forward image, weights and reduction)
+        gp = kn.get("gradient_precision", "fp64")
+        if gp not in ("fp64", "fp32"):
+            raise ValueError("gradient_precision must be 'fp64' or 'fp32'")
+        self._grad_precision = _lib.FP64 if gp == "fp64" else _lib.FP32_SPLIT
         self._s = s
         self._kwargs_numerics = dict(kwargs_numerics or {})
         if kwargs_pixelbased is not None:
@@ -744,13 +751,17 @@ class ImageModel:
         the supersampled grid and sub-frames (``flux_evaluate_indexes``).  The
         gradient, its logL and ``image_out`` (float64) are computed in FP64
         whatever the model's precision: an FP32 model differentiates through
-        its FP64 twin, because the gradient's sums over pixels mix signs."""
+        its FP64 twin, because the gradient's sums over pixels mix signs.
+        ``kwargs_numerics["gradient_precision"] = "fp32"`` runs the per-ray
+        derivatives in FP32 (the forward image, weights and reduction stay FP64)."""
         if self._n_ps:
             raise ValueError("likelihood gradients with point sources are not supported")
         model = self._model(range(len(self.LensModel.lens_model_list)),
                             range(len(self.SourceModel.profile_type_list)),
                             range(len(self.LensLightModel.profile_type_list)),
                             precision=_lib.FP64)
+        _lib.check(_lib.load().lensgb_model_set_grad_precision(model.handle,
+                                                                self._grad_precision))
         if rows is None:
             rows = self.pack_params(kwargs_lens, kwargs_source, kwargs_lens_light)
         rows_dev = _device.to_device_f64(rows)

@@ -312,3 +312,49 @@ def test_subframe_gradient_matches_central_differences(cuda):
         lambda k: J.PSF("PIXEL", kernel_point_source=k[0]), {"flux_evaluate_indexes": fei})
     _, grad = im.likelihood_grad_batch(rows=rows, data=data, psf_kernels=kk)
     _check(grad.cpu().numpy(), _fd(im, rows, kk, data))
+
+
+# ---------------------------------------------------------------------------
+# FP32 per-ray derivatives (gradient_precision "fp32")
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("c", FD_CASES, ids=lambda c: c["tag"])
+def test_fp32_adjoint_matches_reference_finite_differences(cuda, c):
+    """FP32 dual numbers from FP64-accurate offsets (FP64 forward image, weights
+    and reduction) against the reference's finite differences: the same 1e-4
+    bar as the FP64 adjoint."""
+    c = dict(c, numerics=dict(c.get("numerics") or {}, gradient_precision="fp32"))
+    im = _fd_case_model(c)
+    rows = im.pack_params(c["kwargs_lens"], c["kwargs_source"], c["kwargs_lens_light"])
+    logl, grad = im.likelihood_grad_batch(rows=rows)
+    assert abs(float(logl[0]) - c["logL"]) <= 1e-10 * abs(c["logL"])
+    g = grad.cpu().numpy()[0]
+    g5, g2 = c["grad_5pt"], c["grad_central_1e-6"]
+    scale = np.abs(g5).max()
+    ok5 = np.abs(g - g5) <= RTOL * (np.abs(g5) + 1e-3 * scale)
+    ok2 = np.abs(g - g2) <= RTOL * (np.abs(g2) + 1e-3 * scale)
+    bad = ~(ok5 | ok2)
+    assert not bad.any(), [(c["param_order"][k], g[k], g5[k], g2[k]) for k in np.where(bad)[0]]
+
+
+def test_fp32_adjoint_batch_matches_fp64_adjoint(cuda):
+    """The gradient workload's shapes (120x120, s = 2, 21x21): FP32 per-ray
+    derivatives within 1e-4 of the FP64 adjoint (relative, floor 1e-3 of the
+    largest component), and the same logL bits (the forward stays FP64)."""
+    model, lens, src, ll, kern = W.gradient_batch(seed=1003, batch=8)
+    out = {}
+    for gp in ("fp64", "fp32"):
+        g = W.grid_kwargs(120, 0.05)
+        data = J.ImageData(np.zeros((120, 120)), exposure_time=1000.0, background_rms=0.01, **g)
+        im = J.ImageModel(data, J.PSF("PIXEL", kernel_point_source=kern[0]),
+                          J.LensModel(["EPL", "SHEAR"]), J.LightModel(["SERSIC_ELLIPSE"]),
+                          J.LightModel(["SERSIC_ELLIPSE"]),
+                          kwargs_numerics={"supersampling_factor": 2, "gradient_precision": gp})
+        rows = im.pack_params(lens, src, ll)
+        truth = rows.copy()
+        truth[:, 0] *= 1.01
+        d = W.noisy_data(im.image_batch(rows=truth, psf_kernels=kern).cpu().numpy())
+        out[gp] = [t.cpu().numpy() for t in im.likelihood_grad_batch(rows=rows, data=d,
+                                                                     psf_kernels=kern)]
+    np.testing.assert_array_equal(out["fp32"][0], out["fp64"][0])
+    _check(out["fp32"][1], out["fp64"][1])

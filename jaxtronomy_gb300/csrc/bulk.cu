@@ -404,11 +404,11 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                     double ax, ay;
                     const double u = (o[0] * o[0] + o[1] * o[1]) * (rd[6] * rd[6]);
                     if (code == LENSGB_LENS_TNFW && u >= rd[10]) {
-                        // far field of a strong TNFW halo: the record's 16-term series
-                        // (truncation below 1e-8 relative, far inside this path's error)
-                        const double e = rsqrt(u), z = rd[12] * e;
-                        double bs = rd[29];
-                        for (int q = 14; q >= 0; --q) bs = fma(bs, z, rd[14 + q]);
+                        // a strong TNFW halo outside x = max(tau, 1): the record's
+                        // polynomial of the bracket (within 1.3e-9 relative)
+                        const double e = rsqrt(u), t = fma(rd[12], e, -1.0);
+                        double bs = rd[14 + TNFW_NC - 1];
+                        for (int q = TNFW_NC - 2; q >= 0; --q) bs = fma(bs, t, rd[14 + q]);
                         const double a = rd[11] * bs * (e * e);
                         ax = a * o[0];
                         ay = a * o[1];

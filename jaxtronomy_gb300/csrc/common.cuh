@@ -13,6 +13,7 @@ namespace lensgb {
 // serve the FP64 kernels and FP64 set-up; floats serve the FP32 kernels.
 constexpr int REC_D = 32;
 constexpr int REC_F = 36;  // float slot k + 2 mirrors double slot k >= 2
+constexpr int TNFW_NC = 12;  // terms of the TNFW bracket polynomial (record slots d14..)
 // EPL series coefficient table length (largest reference nmax, epl.py:311-319)
 constexpr int EPL_NMAX = 500;
 constexpr int MAX_PROF = LENSGB_MAX_PROFILES;

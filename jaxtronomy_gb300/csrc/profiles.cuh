@@ -28,8 +28,8 @@ namespace lensgb {
 // SHEAR   : d2 gamma1, d3 gamma2
 // NFW     : d2 Rs (floored), d3 rho0, d4 4 rho0 Rs, d5 1/Rs
 // TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs, d7 1/tau,
-//           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1, d10..d12 and d14..d29 far-field
-//           series (tnfw_pair_f)
+//           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1, d10..d12 and d14..d25 the
+//           bracket's polynomial outside x = max(tau, 1) (tnfw_pair_f)
 // SERSIC* : d2 amp, d3 R_sersic (floored), d4 1/R_sersic, d5 1/n, d6 b_n,
 //           d7..d10 product-average transform (m00 m01 m10 m11)
 constexpr int F_OFF = 2;  // float slot = double slot + F_OFF
@@ -470,13 +470,19 @@ __device__ __forceinline__ double tnfw_F_d(double x) {
     return x;
 }
 
-__device__ __forceinline__ double tnfw_g_d(double x, double tau) {
+// The bracket b(x) of g(x) = tau^2/(tau^2+1)^2 b(x) (tnfw.py:339-348).
+__device__ __forceinline__ double tnfw_bracket_d(double x, double tau) {
     x = x > 0.001 ? x : 0.001;
-    double t2 = tau * tau;
-    double L = log(x / (tau + sqrt(t2 + x * x)));
-    return t2 / ((t2 + 1) * (t2 + 1)) *
-           ((t2 + 1 + 2 * (x * x - 1)) * tnfw_F_d(x) + tau * M_PI + (t2 - 1) * log(tau) +
-            sqrt(t2 + x * x) * (-M_PI + L * (t2 - 1) / tau));
+    const double t2 = tau * tau;
+    const double r = sqrt(t2 + x * x);
+    const double L = log(x / (tau + r));
+    return (t2 + 1 + 2 * (x * x - 1)) * tnfw_F_d(x) + tau * M_PI + (t2 - 1) * log(tau) +
+           r * (-M_PI + L * (t2 - 1) / tau);
+}
+
+__device__ __forceinline__ double tnfw_g_d(double x, double tau) {
+    const double t2 = tau * tau;
+    return t2 / ((t2 + 1) * (t2 + 1)) * tnfw_bracket_d(x, tau);
 }
 
 // FP32 TNFW g.  The reference bracket (tnfw.py:339-348) cancels to O(x^2 ln x)
@@ -500,15 +506,19 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
 // shooting: the same regrouped forms as tnfw_g_f / nfw_g_f / nfw_G_f with G(x)
 // evaluated once, one reciprocal of tau + r shared by L and x^2/(tau (tau+r)),
 // and the per-deflector constants of the record (f6 tau, f7 4 rho0 Rs,
-// f8 1/Rs, f9 1/tau, f10 tau^2/(tau^2+1)^2, f11 tau^2 - 1).  Far from the
-// subhalo (x >= 3 max(tau, 1): f12 holds that bound squared) the bracket is the
-// convergent series sum_k c_k z^k in z = max(tau, 1)/x (f16..f31 = c_0..c_15,
-// f14 = max(tau, 1), f13 = 4 rho0 Rs tau^2/(tau^2+1)^2; within 1e-8 relative).
-// ESTRIN: the far-field polynomial by Estrin's scheme (depth 4 instead of 15,
-// three more multiplies) rather than Horner's.  The multi-plane kernel, whose
-// 2-warp CTAs stall on dependent FMAs, gains (same-box A/B on GB300: 3.37 ->
-// 3.29 ms on the 400^2-ray, 5501-step workload); the single-plane bulk kernel,
-// with more warps per SM, keeps Horner's.
+// f8 1/Rs, f9 1/tau, f10 tau^2/(tau^2+1)^2, f11 tau^2 - 1).  Outside the
+// truncation scale (x >= s = max(tau, 1): f12 holds s^2) the bracket b is the
+// record's polynomial of degree TNFW_NC - 1 in t = 2 s/x - 1 (f16.., f14 = 2 s,
+// f13 = 4 rho0 Rs tau^2/(tau^2+1)^2): b is analytic in z = s/x on the whole
+// disk |z| < 1 (its nearest singularities are x = +-i tau), so its Chebyshev
+// interpolant on z in [0, 1] converges geometrically -- 12 terms are within
+// 1.3e-9 relative of b for tau in [0.05, 300] -- and that one polynomial covers
+// both the far field and the 8/9 of the area inside 3 s that used to need the
+// closed form's logarithms.
+// ESTRIN: the polynomial by Estrin's scheme (depth 4 instead of 11, two more
+// multiplies) rather than Horner's.  The multi-plane kernel, whose 2-warp
+// CTAs stall on dependent FMAs, gains; the single-plane bulk kernel, with more
+// warps per SM, keeps Horner's.
 template <bool ESTRIN = false>
 __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy, float& ax,
                                             float& ay) {
@@ -516,25 +526,26 @@ __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy
     const float c0 = rec[10], tm1 = rec[11];
     const float u = fmaf(dx, dx, dy * dy) * (inv_rs * inv_rs);  // x^2
     if (u >= rec[12]) {
+        static_assert(TNFW_NC == 12, "three float4 loads of coefficients");
         const float e = rsqrtf(u);
-        const float z = rec[14] * e;
+        const float t = fmaf(rec[14], e, -1.f);
         const float4* cv = reinterpret_cast<const float4*>(rec + 16);
-        const float4 q0 = cv[0], q1 = cv[1], q2 = cv[2], q3 = cv[3];
-        const float c[16] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
-                             q2.x, q2.y, q2.z, q2.w, q3.x, q3.y, q3.z, q3.w};
+        const float4 q0 = cv[0], q1 = cv[1], q2 = cv[2];
+        const float c[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                             q2.x, q2.y, q2.z, q2.w};
         float b;
         if (ESTRIN) {
-            const float z2 = z * z, z4 = z2 * z2, z8 = z4 * z4;
-            float p[8];
+            const float t2 = t * t, t4 = t2 * t2, t8 = t4 * t4;
+            float p[6];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) p[k] = fmaf(c[2 * k + 1], z, c[2 * k]);
-            const float e0 = fmaf(p[1], z2, p[0]), e1 = fmaf(p[3], z2, p[2]);
-            const float e2 = fmaf(p[5], z2, p[4]), e3 = fmaf(p[7], z2, p[6]);
-            b = fmaf(fmaf(e3, z4, e2), z8, fmaf(e1, z4, e0));
+            for (int k = 0; k < 6; ++k) p[k] = fmaf(c[2 * k + 1], t, c[2 * k]);
+            const float e0 = fmaf(p[1], t2, p[0]), e1 = fmaf(p[3], t2, p[2]);
+            const float e2 = fmaf(p[5], t2, p[4]);
+            b = fmaf(e2, t8, fmaf(e1, t4, e0));
         } else {
-            b = c[15];
+            b = c[11];
 #pragma unroll
-            for (int k = 14; k >= 0; --k) b = fmaf(b, z, c[k]);
+            for (int k = 10; k >= 0; --k) b = fmaf(b, t, c[k]);
         }
         const float a = rec[13] * b * (e * e);
         ax = a * dx;

@@ -157,14 +157,15 @@ def test_bulk_matches_lens_model_for_short_lists(cuda):
 @pytest.mark.parametrize("tau", [0.5, 3.0, 10.0, 40.0])
 def test_bulk_fp32_tnfw_near_and_far_field(cuda, tau):
     """FP32 subhalo deflections against FP64 from the core through the switch to
-    the far-field series (x = 3 max(tau, 1)) and far beyond: |d alpha| <= 2e-6
+    the bracket polynomial (x = max(tau, 1)) and far beyond: |d alpha| <= 2e-6
     of max(|alpha|, alpha_Rs).  (Near the R = 0.001 Rs floor the reference
     formula, which the FP64 path follows, cancels to ~1e-5 relative; there alpha
     itself is below 1e-5 alpha_Rs.)"""
     Rs = 0.05
-    xs = Rs * np.concatenate([np.geomspace(1e-4, 2.0, 40), np.geomspace(0.5, 4.0, 40) * max(tau, 1),
-                              [3 * max(tau, 1) * (1 - 1e-6), 3 * max(tau, 1) * (1 + 1e-6)],
-                              np.geomspace(5, 2000, 30)])
+    s = max(tau, 1)
+    xs = Rs * np.concatenate([np.geomspace(1e-4, 2.0, 40), np.geomspace(0.5, 4.0, 40) * s,
+                              [s * (1 - 1e-6), s * (1 + 1e-6), 3 * s],
+                              np.geomspace(5, 2000, 30), [1e5 * s]])
     ang = np.linspace(0, 2 * np.pi, xs.size)
     x, y = 0.3 + xs * np.cos(ang), -0.2 + xs * np.sin(ang)
     kw = [{"Rs": Rs, "alpha_Rs": 0.004, "r_trunc": tau * Rs, "center_x": 0.3, "center_y": -0.2}]

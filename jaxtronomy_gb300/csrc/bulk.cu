@@ -92,15 +92,26 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
                 const float* rf = srec + j * REC_F;
                 const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh = rf[RF_Y0H], dl = rf[RF_Y0L];
                 if (code == LENSGB_LENS_TNFW) {
-                    // the subhalo case: fused FP32 pair evaluation
+                    // the subhalo case: the rays' polynomials as straight-line code,
+                    // then the closed form for rays inside x = max(tau, 1)
+                    float dx[BULK_RPT], dy[BULK_RPT], ax[BULK_RPT], ay[BULK_RPT];
+                    bool in[BULK_RPT], any = false;
 #pragma unroll
                     for (int k = 0; k < BULK_RPT; ++k) {
-                        const float dx = __fadd_rn(__fsub_rn(xh[k], ch), __fsub_rn(xl[k], cl));
-                        const float dy = __fadd_rn(__fsub_rn(yh[k], dh), __fsub_rn(yl[k], dl));
-                        float ax, ay;
-                        tnfw_pair_f(rf, dx, dy, ax, ay);
-                        sx[k] += ax;
-                        sy[k] += ay;
+                        dx[k] = __fadd_rn(__fsub_rn(xh[k], ch), __fsub_rn(xl[k], cl));
+                        dy[k] = __fadd_rn(__fsub_rn(yh[k], dh), __fsub_rn(yl[k], dl));
+                        in[k] = tnfw_far_f(rf, dx[k], dy[k], ax[k], ay[k]);
+                        any |= in[k];
+                    }
+                    if (any) {
+#pragma unroll
+                        for (int k = 0; k < BULK_RPT; ++k)
+                            if (in[k]) tnfw_near_f(rf, dx[k], dy[k], ax[k], ay[k]);
+                    }
+#pragma unroll
+                    for (int k = 0; k < BULK_RPT; ++k) {
+                        sx[k] += ax[k];
+                        sy[k] += ay[k];
                     }
                 } else {
                     const float* cf = coef_f ? coef_f + g * EPL_NMAX : nullptr;
@@ -434,12 +445,22 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                 // the profile switch outside the ray loop, so that the rays'
                 // evaluations interleave
                 if (code == LENSGB_LENS_TNFW) {
+                    float ax[MP_RPT], ay[MP_RPT];
+                    bool in[MP_RPT], any = false;
 #pragma unroll
                     for (int k = 0; k < MP_RPT; ++k) {
-                        float ax, ay;
-                        tnfw_pair_f<true>(rf, ox[k], oy[k], ax, ay);
-                        s32[0][k] += ax;
-                        s32[1][k] += ay;
+                        in[k] = tnfw_far_f<true>(rf, ox[k], oy[k], ax[k], ay[k]);
+                        any |= in[k];
+                    }
+                    if (any) {
+#pragma unroll
+                        for (int k = 0; k < MP_RPT; ++k)
+                            if (in[k]) tnfw_near_f(rf, ox[k], oy[k], ax[k], ay[k]);
+                    }
+#pragma unroll
+                    for (int k = 0; k < MP_RPT; ++k) {
+                        s32[0][k] += ax[k];
+                        s32[1][k] += ay[k];
                     }
                 } else {
                     const float* cf = coef_f ? coef_f + g * EPL_NMAX : nullptr;

@@ -29,7 +29,7 @@ namespace lensgb {
 // NFW     : d2 Rs (floored), d3 rho0, d4 4 rho0 Rs, d5 1/Rs
 // TNFW    : d2 Rs, d3 rho0, d4 tau, d5 4 rho0 Rs, d6 1/Rs, d7 1/tau,
 //           d8 tau^2/(tau^2+1)^2, d9 tau^2 - 1, d10..d12 and d14..d25 the
-//           bracket's polynomial outside x = max(tau, 1) (tnfw_pair_f)
+//           bracket's polynomial outside x = max(tau, 1) (tnfw_far_f)
 // SERSIC* : d2 amp, d3 R_sersic (floored), d4 1/R_sersic, d5 1/n, d6 b_n,
 //           d7..d10 product-average transform (m00 m01 m10 m11)
 constexpr int F_OFF = 2;  // float slot = double slot + F_OFF
@@ -515,17 +515,20 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
 // 1.3e-9 relative of b for tau in [0.05, 300] -- and that one polynomial covers
 // both the far field and the 8/9 of the area inside 3 s that used to need the
 // closed form's logarithms.
+// The pair is split in two so that a thread's rays run the polynomial as
+// straight-line code that interleaves: tnfw_far_f evaluates it whatever x and
+// returns true when x < max(tau, 1), where the caller then overwrites the
+// result with tnfw_near_f's closed form (a branch taken by ~1% of pairs).
 // ESTRIN: the polynomial by Estrin's scheme (depth 4 instead of 11, two more
 // multiplies) rather than Horner's.  The multi-plane kernel, whose 2-warp
 // CTAs stall on dependent FMAs, gains; the single-plane bulk kernel, with more
 // warps per SM, keeps Horner's.
 template <bool ESTRIN = false>
-__device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy, float& ax,
-                                            float& ay) {
-    const float tau = rec[6], a4 = rec[7], inv_rs = rec[8], inv_tau = rec[9];
-    const float c0 = rec[10], tm1 = rec[11];
+__device__ __forceinline__ bool tnfw_far_f(const float* rec, float dx, float dy, float& ax,
+                                           float& ay) {
+    const float inv_rs = rec[8];
     const float u = fmaf(dx, dx, dy * dy) * (inv_rs * inv_rs);  // x^2
-    if (u >= rec[12]) {
+    {
         static_assert(TNFW_NC == 12, "three float4 loads of coefficients");
         const float e = rsqrtf(u);
         const float t = fmaf(rec[14], e, -1.f);
@@ -550,8 +553,14 @@ __device__ __forceinline__ void tnfw_pair_f(const float* rec, float dx, float dy
         const float a = rec[13] * b * (e * e);
         ax = a * dx;
         ay = a * dy;
-        return;
     }
+    return !(u >= rec[12]);
+}
+
+__device__ __forceinline__ void tnfw_near_f(const float* rec, float dx, float dy, float& ax,
+                                            float& ay) {
+    const float tau = rec[6], a4 = rec[7], inv_rs = rec[8], inv_tau = rec[9];
+    const float c0 = rec[10], tm1 = rec[11];
     const float t2 = tau * tau;
     // R >= 0.001 Rs and x >= 0.001 (tnfw.py:85, :335)
     float X = sqrtf(fmaf(dx, dx, dy * dy)) * inv_rs;

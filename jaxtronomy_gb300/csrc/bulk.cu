@@ -25,6 +25,9 @@ namespace lensgb {
 #ifndef LENSGB_MP_MAXNREG
 #define LENSGB_MP_MAXNREG 160
 #endif
+#ifndef LENSGB_MP_THREADS
+#define LENSGB_MP_THREADS 128
+#endif
 constexpr int BULK_CHUNK = 64;
 constexpr int BULK_THREADS = 256;
 constexpr int BULK_RPT = LENSGB_BULK_RPT;  // rays per thread (i, i + BULK_THREADS, ...)
@@ -168,7 +171,7 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
 // in the offset) is evaluated as an FP32-pair product and FP64-tagged terms in
 // FP64 from an FP64 offset, both summed as FP32 pairs.
 // ---------------------------------------------------------------------------
-constexpr int MP_THREADS = 64;
+constexpr int MP_THREADS = LENSGB_MP_THREADS;
 constexpr int MP_RPT = LENSGB_MP_RPT;
 constexpr int MP_CHUNK = 64;
 constexpr int PL_F = 8;  // per-step floats: dT hi/lo, 1/T_z hi/lo, eps, r2p hi/lo, tag bits
@@ -252,9 +255,12 @@ __device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl,
     pl = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, pl));
 }
 
-// 3 rays per thread and 160 registers: a 400^2-ray call (834 CTAs of 64
-// threads) is resident in one wave at 6 CTAs per SM with no spills; fewer
-// registers made the compiler rebuild ray state in FP64 or spill.
+// 3 rays per thread, 160 registers and 128 threads: a 400^2-ray call (417
+// CTAs) is resident in one wave at 3 CTAs per SM with no spills; fewer
+// registers made the compiler rebuild ray state in FP64 or spill.  Launch-shape
+// sweep on GB300 (400^2 rays, 5501 steps): 128 threads 2.32 ms, 96 2.37, 64
+// 2.41, 192 2.51, 32 3.16, 256 3.69 (two CTAs on some SMs, one on others);
+// 4 rays / 168 registers 2.74, 2 rays / 128 registers 3.08.
 template <bool F32>
 __global__ void __maxnreg__(LENSGB_MP_MAXNREG)
 multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,

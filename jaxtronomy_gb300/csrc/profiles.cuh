@@ -113,25 +113,31 @@ __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, 
         // maximum FP32-vs-FP64 image error unchanged (5.69e-6)
         const float ee = __fdividef(1.f, fmaf(2.f * fh, ur, 1.f + f2q));
         const float wr = fmaf(fh, ur, f2q) * ee, wi = fh * ui * ee;
-        float sr = F[nmax - 1], si = 0.f;
+        // S(w) = sum_n F_n w^n with real F_n by division by the real quadratic
+        // (x - w)(x - conj w) = x^2 - rr x - ss (Knuth, TAOCP 4.6.4):
+        //   b_n = F_n + rr b_{n+1} + ss b_{n+2},  S(w) = (b_0 - wr b_1) + i wi b_1,
+        // two real FMAs per term instead of a complex multiply-add's four; the
+        // recurrence damps rounding errors by |w| <= f/(2 - f) < 1 per step.
+        const float rr = 2.f * wr, ss = -fmaf(wr, wr, wi * wi);
+        float b1 = F[nmax - 1], b2 = 0.f;  // b_{n+1}, b_{n+2}
         int n = nmax - 2;
         if ((nmax & 1) == 0) {  // odd number of remaining terms: one step first
-            const float nr = fmaf(sr, wr, F[n]) - si * wi;
-            si = fmaf(sr, wi, si * wr);
-            sr = nr;
+            const float bn = fmaf(rr, b1, fmaf(ss, b2, F[n]));
+            b2 = b1;
+            b1 = bn;
             --n;
         }
-        // two pairs of terms per trip: 2.141 -> 1.966 ms for the ray kernel of
-        // the 1024-system EPL workload (the loop's own instructions halve)
+        // two terms per trip (the loop's own instructions halve)
 #pragma unroll 2
         for (; n >= 1; n -= 2) {
             // n is odd here, so (F[n-1], F[n]) is an aligned pair
             const float2 fp = *reinterpret_cast<const float2*>(F + n - 1);
-            float nr = fmaf(sr, wr, fp.y) - si * wi;
-            float ni = fmaf(sr, wi, si * wr);
-            sr = fmaf(nr, wr, fp.x) - ni * wi;
-            si = fmaf(nr, wi, ni * wr);
+            const float bn = fmaf(rr, b1, fmaf(ss, b2, fp.y));
+            const float bm = fmaf(rr, bn, fmaf(ss, b1, fp.x));
+            b2 = bn;
+            b1 = bm;
         }
+        const float sr = fmaf(-wr, b2, b1), si = wi * b2;
         // times (1 + (f/2) conj(u)) / |1 - z/2|^2
         const float gr = fmaf(fh, ur, 1.f), gi = -fh * ui;
         hr = (sr * gr - si * gi) * ee;

@@ -73,7 +73,8 @@ __device__ void prepare_lens_record(int code, const double* a, double* d, double
         d[RD_CY] = a[5];
         d[2] = b; d[3] = t; d[4] = q; d[5] = cos(phi); d[6] = sin(phi); d[7] = fq;
         d[8] = (double)nmax; d[9] = 2.0 / (1.0 + q) * pow(b, t);
-        // FP32-path constants: f^2/4, f/2, -t/2
+        // FP32-path constants: q cos, q sin, f^2/4, f/2, -t/2
+        d[10] = q * d[5]; d[11] = q * d[6];
         d[12] = 0.25 * fq * fq; d[13] = 0.5 * fq; d[14] = -0.5 * t;
         // F_0 = 1, F_1 = 1 - 2B/C, F_n = ((n-1) F_{n-2} - (2B-C) F_{n-1}) / (C+n-1)
         double B = t / 2.0, C = 2.0 - B;

@@ -86,19 +86,18 @@ __device__ __forceinline__ void nie_deflect(const R* rec, R dx, R dy, R& ax, R& 
 //   2F1 = S(w) (1 + (f/2) conj(u)) / |1 - z/2|^2,
 // so one reciprocal serves both divisions, and (b/R)^t = b^t 2^(-t/2 log2 R^2)
 // needs no square root.  Record: f4 b, f5 t, f6 q, f7 cos, f8 sin, f9 f,
-// f10 nmax, f11 2/(1+q) b^t, f14 f^2/4, f15 f/2, f16 -t/2.
+// f10 nmax, f11 2/(1+q) b^t, f12 q cos, f13 q sin, f14 f^2/4, f15 f/2, f16 -t/2.
 __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, float dx, float dy,
                                               float& ax, float& ay) {
-    const float q = rec[6], c = rec[7], sn = rec[8];
+    const float c = rec[7], sn = rec[8], qc = rec[12], qs = rec[13];
     // FP32 series length (f17): the reference's nmax shortened to where the
     // remaining terms fall below FP32 resolution (set by the prepare kernel)
     const int nmax = (int)rec[17];
     const float pref = rec[11], f2q = rec[14], fh = rec[15], mth = rec[16];
-    const float x = dx * c + dy * sn;
-    const float y = -dx * sn + dy * c;
-    const float za = q * x, zb = y;
+    // Z = q x + i y in the profile frame
+    const float za = fmaf(dx, qc, dy * qs), zb = fmaf(dy, c, -dx * sn);
     const float r2 = za * za + zb * zb;
-    float hr = 1.f, hi = 0.f;
+    float hr = 1.f, hi = 0.f, ee = 1.f;
     if (nmax > 0) {
         if (r2 == 0.f) {  // reference: 0/0 at the centre -> NaN -> nan_to_num -> 0
             ax = 0.f;
@@ -111,7 +110,7 @@ __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, 
         // 1/|1 - z/2|^2 by the hardware reciprocal (~1 ulp): measured on the
         // 1024-system EPL workload, the ray kernel 2.223 -> 2.141 ms with the
         // maximum FP32-vs-FP64 image error unchanged (5.69e-6)
-        const float ee = __fdividef(1.f, fmaf(2.f * fh, ur, 1.f + f2q));
+        ee = __fdividef(1.f, fmaf(2.f * fh, ur, 1.f + f2q));
         const float wr = fmaf(fh, ur, f2q) * ee, wi = fh * ui * ee;
         // S(w) = sum_n F_n w^n with real F_n by division by the real quadratic
         // (x - w)(x - conj w) = x^2 - rr x - ss (Knuth, TAOCP 4.6.4):
@@ -140,14 +139,15 @@ __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, 
         const float sr = fmaf(-wr, b2, b1), si = wi * b2;
         // times (1 + (f/2) conj(u)) / |1 - z/2|^2
         const float gr = fmaf(fh, ur, 1.f), gi = -fh * ui;
-        hr = (sr * gr - si * gi) * ee;
-        hi = (sr * gi + si * gr) * ee;
+        // (the factor 1/|1 - z/2|^2 goes into the amplitude below)
+        hr = sr * gr - si * gi;
+        hi = sr * gi + si * gr;
     }
     const float r2m = r2 > 1e-18f ? r2 : 1e-18f;  // R = max(|Z|, 1e-9)
     // hardware lg2/ex2: on the 1024-system EPL workload this moved the maximum
     // FP32 image error from 5.58e-6 to 5.69e-6 (rays it disturbs most are the
     // ones the FP64 refine pass recomputes)
-    const float amp = pref * ex2_approx(mth * lg2_approx(r2m));
+    const float amp = (pref * ee) * ex2_approx(mth * lg2_approx(r2m));
     const float fx = amp * (za * hr - zb * hi);
     const float fy = amp * (za * hi + zb * hr);
     ax = fx * c - fy * sn;

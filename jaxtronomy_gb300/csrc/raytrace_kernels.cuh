@@ -346,16 +346,17 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
                             axs += ax;
                             ays += ay;
                         }
-                        axs *= st.alpha_scaling_f;
-                        ays *= st.alpha_scaling_f;
+                        // alpha_scaling is folded into each source's scale (and
+                        // its magnitude into the refine predictor's kappa)
                         float fsrc = 0.f, gsum = 0.f;
 #pragma unroll (LS::generic ? 1 : 8)
                         for (int k = 0; k < MS; ++k) {
                             if (k >= n_src) break;
                             const float sc = st.src_scale_f[k];
+                            const float sca = sc * st.alpha_scaling_f;
                             float gk;
-                            const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sc * axs,
-                                                              os[k].by + ddy - sc * ays, gk);
+                            const float fk = sersic_flux_grad(REC(n_lens + k), os[k].bx + ddx - sca * axs,
+                                                              os[k].by + ddy - sca * ays, gk);
                             fsrc += fk;
                             gsum += fk * gk * sc;
                         }
@@ -371,7 +372,8 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
                         if (refine) {
                             // predicted relative error of this ray's flux from the FP32
                             // error of beta (kappa * |alpha|) through the source gradients
-                            const float dbeta = rf.kappa * (fabsf(axs) + fabsf(ays));
+                            const float dbeta = (rf.kappa * fabsf(st.alpha_scaling_f)) *
+                                                (fabsf(axs) + fabsf(ays));
                             flag |= gsum * dbeta > rf.tau * flux;
                         }
                     } else if (do_ll) {

@@ -115,6 +115,67 @@ __device__ __forceinline__ double ray_flux_d(const GridDesc& g, const StackDesc&
     return flux * st.flux_scaling;
 }
 
+// Flux of one supersampled ray for the FP32 path's refine pass: the ray, the
+// deflections and beta in FP64 (beta = theta - alpha is what cancels in FP32),
+// then each light profile in FP32 (sersic_f, the FP32 kernel's own arithmetic)
+// from its FP64 offset rounded once.  The Sersic evaluations are most of the
+// FP64 ray's work, and their FP32 rounding (~1e-7 relative here) is far below
+// the FP32 path's bar; only the cancelling difference needs FP64.
+template <int C0, int C1, int NS, int NLL>
+__device__ __forceinline__ double ray_flux_refine(const GridDesc& g, const StackDesc& st,
+                                                  const double* srec, const double* scoef,
+                                                  const float* frec, int I, int J, int flags) {
+    using LS = LensStackT<C0, C1>;
+    const double X = g.ra00 + (double)J * g.ax + (double)I * g.bx;
+    const double Y = g.dec00 + (double)J * g.ay + (double)I * g.by;
+    const int n_lens = LS::generic ? st.n_lens : LS::n;
+    const int n_src = NS >= 0 ? NS : st.n_src;
+    const int n_ll = NLL >= 0 ? NLL : st.n_ll;
+    double flux = 0;
+    if (!(flags & LENSGB_NO_SOURCE) && n_src > 0) {
+        double axs = 0, ays = 0;
+#pragma unroll (LS::generic ? 1 : 8)
+        for (int p = 0; p < (LS::generic ? MAX_PROF : LS::n); ++p) {
+            if (p >= n_lens) break;
+            const double* rec = srec + p * REC_D;
+            const int code = LS::generic ? st.lens[p] : LS::code(p);
+            const int es = st.epl_slot[p];
+            double ax, ay;
+            lens_deflect<double>(code, rec, es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                                 X - rec[RD_CX], Y - rec[RD_CY], ax, ay);
+            axs += ax;
+            ays += ay;
+        }
+        axs *= st.alpha_scaling;
+        ays *= st.alpha_scaling;
+        float fs = 0.f;
+#pragma unroll (LS::generic ? 1 : 8)
+        for (int k = 0; k < (NS >= 0 ? NS : MAX_PROF); ++k) {
+            if (k >= n_src) break;
+            const double* rec = srec + (n_lens + k) * REC_D;
+            const double sc = st.src_scale[k];
+            const double bxv = X - sc * axs, byv = Y - sc * ays;
+            float gk;
+            fs += sersic_f<false>(frec + (n_lens + k) * REC_F, (float)(bxv - rec[RD_CX]),
+                                  (float)(byv - rec[RD_CY]), gk);
+        }
+        flux += (double)fs;
+    }
+    if (!(flags & LENSGB_NO_LENS_LIGHT)) {
+        float fl = 0.f;
+#pragma unroll (LS::generic ? 1 : 8)
+        for (int k = 0; k < (NLL >= 0 ? NLL : MAX_PROF); ++k) {
+            if (k >= n_ll) break;
+            const double* rec = srec + (n_lens + n_src + k) * REC_D;
+            float gk;
+            fl += sersic_f<false>(frec + (n_lens + n_src + k) * REC_F, (float)(X - rec[RD_CX]),
+                                  (float)(Y - rec[RD_CY]), gk);
+        }
+        flux += (double)fl;
+    }
+    return flux * st.flux_scaling;
+}
+
 // FP64 value of pixel (row, col): mean over sub-columns then sub-rows
 // (image_util.py:93), times out_scale.
 template <int C0, int C1, int NS, int NLL>
@@ -401,19 +462,18 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Refine pass: recompute the listed pixels in FP64 (records read from global
-// memory, one thread per listed pixel).
+// Refine pass: recompute the listed pixels with FP64 rays, deflections and
+// beta (ray_flux_refine; records read from global memory).
 // ---------------------------------------------------------------------------
 // One thread per (listed pixel, sub-ray); the s^2 sub-ray fluxes of a pixel are
-// combined in shared memory in the order of pixel_value_d, so a refined pixel
-// equals the FP64 kernel's value.
+// combined in shared memory in the order of pixel_value_d.
 constexpr int REFINE_THREADS = 128;
 
 template <int C0, int C1, int NS, int NLL>
 __global__ void __launch_bounds__(REFINE_THREADS)
 refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
-              const double* __restrict__ coef, float* __restrict__ out, int flags,
-              double out_scale, RefineArgs rf) {
+              const double* __restrict__ coef, const float* __restrict__ frec,
+              float* __restrict__ out, int flags, double out_scale, RefineArgs rf) {
     __shared__ double sub[32 * 32];  // s <= 32
     const unsigned int n = *rf.count;
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
@@ -429,9 +489,10 @@ refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
                 const long long pix = e - (long long)inst * g.nx * g.ny;
                 const int row = (int)(pix / g.nx), col = (int)(pix - (long long)row * g.nx);
                 const int si = k / s, sj = k - si * s;
-                v = ray_flux_d<C0, C1, NS, NLL>(g, st, rec + (long long)inst * n_prof * REC_D,
-                                                coef + (long long)inst * st.n_epl * EPL_NMAX,
-                                                row * s + si, col * s + sj, flags);
+                v = ray_flux_refine<C0, C1, NS, NLL>(
+                    g, st, rec + (long long)inst * n_prof * REC_D,
+                    coef + (long long)inst * st.n_epl * EPL_NMAX,
+                    frec + (long long)inst * n_prof * REC_F, row * s + si, col * s + sj, flags);
             }
             sub[w] = v;
         }
@@ -455,12 +516,12 @@ refine_kernel(GridDesc g, StackDesc st, const double* __restrict__ rec,
 // Refine pass of a mixed launch (systems of different grids and supersampling
 // factors): one warp per listed pixel, its lanes evaluating the pixel's s^2
 // sub-rays (system s from the pixel's grid), combined by lane 0 in the order
-// of pixel_value_d, so a refined pixel again equals the FP64 kernel's value.
+// of pixel_value_d.
 template <int C0, int C1, int NS, int NLL>
 __global__ void __launch_bounds__(REFINE_THREADS)
 refine_mixed_kernel(StackDesc st, const double* __restrict__ rec,
-                    const double* __restrict__ coef, float* __restrict__ out, int flags,
-                    RefineArgs rf, MixedTab mt) {
+                    const double* __restrict__ coef, const float* __restrict__ frec,
+                    float* __restrict__ out, int flags, RefineArgs rf, MixedTab mt) {
     constexpr int WARPS = REFINE_THREADS / 32;
     __shared__ double sub[WARPS][32 * 32];  // s <= 32
     const unsigned int n = *rf.count;
@@ -483,8 +544,9 @@ refine_mixed_kernel(StackDesc st, const double* __restrict__ rec,
         const double* cf = coef + (long long)lo * st.n_epl * EPL_NMAX;
         for (int k = lane; k < s2; k += 32) {
             const int si = k / s, sj = k - si * s;
-            sub[warp][k] = ray_flux_d<C0, C1, NS, NLL>(g, st, r, cf, row * s + si, col * s + sj,
-                                                       flags);
+            sub[warp][k] = ray_flux_refine<C0, C1, NS, NLL>(
+                g, st, r, cf, frec + (long long)lo * n_prof * REC_F, row * s + si, col * s + sj,
+                flags);
         }
         __syncwarp();
         if (lane == 0) {
@@ -578,10 +640,10 @@ void launch_variant(const GridDesc& g, const StackDesc& st, int n_inst, const do
             const int rblocks = num_sms() * 4;
             if (mt.grid)
                 refine_mixed_kernel<C0, C1, NS, NLL><<<rblocks, REFINE_THREADS, 0, stream>>>(
-                    st, rec_d, coef_d, (float*)out, flags, rf, mt);
+                    st, rec_d, coef_d, rec_f, (float*)out, flags, rf, mt);
             else
                 refine_kernel<C0, C1, NS, NLL><<<rblocks, REFINE_THREADS, 0, stream>>>(
-                    g, st, rec_d, coef_d, (float*)out, flags, out_scale, rf);
+                    g, st, rec_d, coef_d, rec_f, (float*)out, flags, out_scale, rf);
         }
     }
 }

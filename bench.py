@@ -1319,7 +1319,7 @@ def gpu_arm(args):
             pass
         conv_bytes = B * N_PIX * N_PIX * 4 * 2 + B * KSIZE * KSIZE * 4
         extra["roofline_conv"] = {
-            "kernel": "conv_f32_fixed_kernel (K <= 48: compile-time width)", "bound": "fp32", "unit": "TFLOP/s",
+            "kernel": "conv_f32_tma_kernel (TMA-staged halo tile, K <= 48: compile-time width)", "bound": "fp32", "unit": "TFLOP/s",
             "achieved": flop_conv / cv / 1e12, "peak": fp32_peak,
             "frac": flop_conv / cv / 1e12 / fp32_peak, "launch_ms": cv * 1e3,
             "peak_source": "measured FP32 FMA rate of this device (fma_peaks, of measured)",

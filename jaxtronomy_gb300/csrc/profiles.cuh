@@ -161,64 +161,62 @@ __device__ __forceinline__ void epl_deflect(const R* rec, const R* F, R dx, R dy
                       (float&)ay);
         return;
     }
-    const R t = rec[slot<R>(3)], q = rec[slot<R>(4)];
-    const R c = rec[slot<R>(5)], sn = rec[slot<R>(6)], f = rec[slot<R>(7)];
-    const int nmax = (int)rec[slot<R>(8)];
-    const R pref = rec[slot<R>(9)];
-    R x = dx * c + dy * sn;
-    R y = -dx * sn + dy * c;
-    R za = q * x, zb = y;               // Z = q x + i y
-    R r2 = za * za + zb * zb;
-    R Ra = (sizeof(R) == 8) ? hypot(za, zb) : sqrtf(r2);
-    R Rm = Ra > R(1e-9) ? Ra : R(1e-9);  // R = max(|Z|, 1e-9)
-    R hr = 1, hi = 0;                     // 2F1 value
+    // FP64: the reference's z = -f Z / conj(Z), w = z / (z - 2), 2F1 = S(w) / (1 - z/2)
+    // and alpha = 2/(1+q) (b/R)^t Z 2F1 (epl.py:321-392, hyp2f1_util.py:135-176),
+    // arranged for the FP64 pipe: one reciprocal serves |z - 2|^2 and
+    // |1 - z/2|^2 = |z - 2|^2 / 4; the series S(w) = sum_n F_n w^n (real F_n) by
+    // division by the real quadratic (x - w)(x - conj w) = x^2 - rr x - ss (two
+    // FMAs per term instead of a complex multiply-add's four; |w| <= f/(2-f) < 1
+    // damps its rounding); (b/R)^t = b^t exp(-t/2 ln max(|Z|^2, 1e-18)), i.e. the
+    // reference's R = max(|Z|, 1e-9), without hypot or pow.
+    const double t = rec[3], q = rec[4];
+    const double c = rec[5], sn = rec[6], f = rec[7];
+    const int nmax = (int)rec[8];
+    const double pref = rec[9];
+    const double x = dx * c + dy * sn;
+    const double y = -dx * sn + dy * c;
+    const double za = q * x, zb = y;  // Z = q x + i y
+    const double r2 = za * za + zb * zb;
+    double hr = 1, hi = 0;  // 2F1 value
     bool nan_case = false;
     if (nmax > 0) {
-        if (r2 == R(0)) {
+        if (r2 == 0.0) {
             nan_case = true;  // -f Z / conj(Z) is 0/0 at the centre -> NaN -> 0
         } else {
-            // z = -f Z / conj(Z) = -f Z^2 / |Z|^2
-            R inv = R(1) / r2;
-            R zr = -f * (za * za - zb * zb) * inv;
-            R zi = -f * (R(2) * za * zb) * inv;
-            // w = z / (z - 2)
-            R dr = zr - R(2), di = zi;
-            R dd = R(1) / (dr * dr + di * di);
-            R wr = (zr * dr + zi * di) * dd;
-            R wi = (zi * dr - zr * di) * dd;
-            // Horner over the coefficient table
-            R sr = F[nmax - 1], si = 0;
+            const double inv = 1.0 / r2;
+            const double zr = -f * (za * za - zb * zb) * inv;
+            const double zi = -f * (2.0 * za * zb) * inv;
+            const double dr = zr - 2.0, di = zi;
+            const double dd = 1.0 / (dr * dr + di * di);
+            const double wr = (zr * dr + zi * di) * dd;
+            const double wi = (zi * dr - zr * di) * dd;
+            const double rr = 2.0 * wr, ss = -(wr * wr + wi * wi);
+            double b1 = F[nmax - 1], b2 = 0.0;  // b_{n+1}, b_{n+2}
             for (int n = nmax - 2; n >= 0; --n) {
-                R nr = sr * wr - si * wi + F[n];
-                R ni = sr * wi + si * wr;
-                sr = nr;
-                si = ni;
+                const double bn = fma(rr, b1, fma(ss, b2, F[n]));
+                b2 = b1;
+                b1 = bn;
             }
-            // divide by (1 - z/2)
-            R er = R(1) - R(0.5) * zr, ei = -R(0.5) * zi;
-            R ee = R(1) / (er * er + ei * ei);
+            const double sr = fma(-wr, b2, b1), si = wi * b2;
+            const double er = 1.0 - 0.5 * zr, ei = -0.5 * zi;
+            const double ee = 4.0 * dd;  // 1 / |1 - z/2|^2
             hr = (sr * er + si * ei) * ee;
             hi = (si * er - sr * ei) * ee;
         }
     }
-    R fx, fy;
+    double fx, fy;
     if (nan_case) {
         fx = 0;
         fy = 0;
     } else {
-        // alpha = 2/(1+q) (b/R)^t Z 2F1
-        R amp;
-        if (sizeof(R) == 8)
-            amp = pref * pow(Rm, -t);
-        else
-            amp = pref * exp2f(-t * log2f(Rm));
-        R omr = za * hr - zb * hi;
-        R omi = za * hi + zb * hr;
+        const double amp = pref * exp(-0.5 * t * log(r2 > 1e-18 ? r2 : 1e-18));
+        const double omr = za * hr - zb * hi;
+        const double omi = za * hi + zb * hr;
         fx = nan_to_num_1e10(amp * omr);
         fy = nan_to_num_1e10(amp * omi);
     }
-    ax = fx * c - fy * sn;
-    ay = fx * sn + fy * c;
+    ax = (R)(fx * c - fy * sn);
+    ay = (R)(fx * sn + fy * c);
 }
 
 // ---------------------------------------------------------------------------

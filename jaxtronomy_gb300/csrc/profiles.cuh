@@ -156,6 +156,84 @@ __device__ __forceinline__ void epl_deflect_f(const float* rec, const float* F, 
     ay = fx * sn + fy * c;
 }
 
+// epl_deflect_f for NR rays of one profile at once (a row of a pixel's
+// sub-rays): the same operations per ray, but one series loop for all NR
+// (the trip count is the profile's), so the loop's control, moves and address
+// arithmetic are shared and the rays' recurrences interleave.  A ray at Z = 0
+// takes the same NaN-free zero as epl_deflect_f, by a select at the end.
+template <int NR>
+__device__ __forceinline__ void epl_deflect_f_row(const float* rec, const float* F,
+                                                  const float* dx, const float* dy, float* ax,
+                                                  float* ay) {
+    const float c = rec[7], sn = rec[8], qc = rec[12], qs = rec[13];
+    const int nmax = (int)rec[17];
+    const float pref = rec[11], f2q = rec[14], fh = rec[15], mth = rec[16];
+    float za[NR], zb[NR], r2[NR], hr[NR], hi[NR], ee[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        za[r] = fmaf(dx[r], qc, dy[r] * qs);
+        zb[r] = fmaf(dy[r], c, -dx[r] * sn);
+        r2[r] = za[r] * za[r] + zb[r] * zb[r];
+        hr[r] = 1.f;
+        hi[r] = 0.f;
+        ee[r] = 1.f;
+    }
+    if (nmax > 0) {
+        float ur[NR], ui[NR], wr[NR], wi[NR], rr[NR], ss[NR], b1[NR], b2[NR];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            const float inv = __fdividef(1.f, r2[r]);
+            ur[r] = (za[r] * za[r] - zb[r] * zb[r]) * inv;
+            ui[r] = 2.f * za[r] * zb[r] * inv;
+            ee[r] = __fdividef(1.f, fmaf(2.f * fh, ur[r], 1.f + f2q));
+            wr[r] = fmaf(fh, ur[r], f2q) * ee[r];
+            wi[r] = fh * ui[r] * ee[r];
+            rr[r] = 2.f * wr[r];
+            ss[r] = -fmaf(wr[r], wr[r], wi[r] * wi[r]);
+            b1[r] = F[nmax - 1];
+            b2[r] = 0.f;
+        }
+        int n = nmax - 2;
+        if ((nmax & 1) == 0) {
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const float bn = fmaf(rr[r], b1[r], fmaf(ss[r], b2[r], F[n]));
+                b2[r] = b1[r];
+                b1[r] = bn;
+            }
+            --n;
+        }
+#pragma unroll 1
+        for (; n >= 1; n -= 2) {
+            const float2 fp = *reinterpret_cast<const float2*>(F + n - 1);
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const float bn = fmaf(rr[r], b1[r], fmaf(ss[r], b2[r], fp.y));
+                const float bm = fmaf(rr[r], bn, fmaf(ss[r], b1[r], fp.x));
+                b2[r] = bn;
+                b1[r] = bm;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            const float sr = fmaf(-wr[r], b2[r], b1[r]), si = wi[r] * b2[r];
+            const float gr = fmaf(fh, ur[r], 1.f), gi = -fh * ui[r];
+            hr[r] = sr * gr - si * gi;
+            hi[r] = sr * gi + si * gr;
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r) {
+        const float r2m = r2[r] > 1e-18f ? r2[r] : 1e-18f;
+        const float amp = (pref * ee[r]) * ex2_approx(mth * lg2_approx(r2m));
+        const float fx = amp * (za[r] * hr[r] - zb[r] * hi[r]);
+        const float fy = amp * (za[r] * hi[r] + zb[r] * hr[r]);
+        const bool zero = nmax > 0 && r2[r] == 0.f;  // reference: 0/0 -> NaN -> 0
+        ax[r] = zero ? 0.f : fx * c - fy * sn;
+        ay[r] = zero ? 0.f : fx * sn + fy * c;
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ void epl_deflect(const R* rec, const R* F, R dx, R dy, R& ax, R& ay) {
     if (sizeof(R) == 4) {
@@ -707,6 +785,20 @@ __device__ __forceinline__ void lens_deflect(int code, const R* rec, const R* F,
             break;
         default: ax = 0; ay = 0; break;
     }
+}
+
+// Deflections of NR rays by one profile of a compile-time stack: EPL by
+// epl_deflect_f_row, any other profile ray by ray.
+template <int NR>
+__device__ __forceinline__ void lens_deflect_row_f(int code, const float* rec, const float* F,
+                                                   const float* dx, const float* dy, float* ax,
+                                                   float* ay) {
+    if (code == LENSGB_LENS_EPL) {
+        epl_deflect_f_row<NR>(rec, F, dx, dy, ax, ay);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r) lens_deflect<float>(code, rec, F, dx[r], dy[r], ax[r], ay[r]);
 }
 
 }  // namespace lensgb

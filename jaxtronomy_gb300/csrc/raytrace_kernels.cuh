@@ -386,6 +386,38 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
             for (int si = 0; si < (SS > 0 ? SS : s); ++si) {
                 float rs = 0.f;
                 const float fi = (float)si;
+                // compile-time stack and supersampling: the row's SS sub-rays are
+                // deflected together (lens_deflect_row_f), in the same per-ray
+                // order of profiles as the per-ray loop below
+                constexpr bool ROW = SS > 0 && !LS::generic;
+                constexpr int NRW = ROW ? SS : 1;
+                float rax[NRW], ray_[NRW];
+                if constexpr (ROW) {
+                    if (do_src) {
+#pragma unroll
+                        for (int sj = 0; sj < NRW; ++sj) rax[sj] = ray_[sj] = 0.f;
+#pragma unroll
+                        for (int p = 0; p < ML; ++p) {
+                            if (p >= n_lens) break;
+                            const int es = st.epl_slot[p];
+                            float dxr[NRW], dyr[NRW], axr[NRW], ayr[NRW];
+#pragma unroll
+                            for (int sj = 0; sj < NRW; ++sj) {
+                                const float fj = (float)sj;
+                                dxr[sj] = ol[p].bx + fmaf(fi, bxf, fj * axf);
+                                dyr[sj] = ol[p].by + fmaf(fi, byf, fj * ayf);
+                            }
+                            lens_deflect_row_f<NRW>(LS::code(p), REC(p),
+                                                    es >= 0 ? scoef + es * EPL_NMAX : nullptr, dxr,
+                                                    dyr, axr, ayr);
+#pragma unroll
+                            for (int sj = 0; sj < NRW; ++sj) {
+                                rax[sj] += axr[sj];
+                                ray_[sj] += ayr[sj];
+                            }
+                        }
+                    }
+                }
 #pragma unroll (SS > 0 ? SS : 1)
                 for (int sj = 0; sj < (SS > 0 ? SS : s); ++sj) {
                     // sub-ray displacement from the base ray: below one pixel, so a
@@ -396,16 +428,22 @@ raytrace_fp32_kernel(GridDesc g0, StackDesc st, int ppt, const float* __restrict
                     float flux = 0.f;
                     if (do_src) {
                         float axs = 0.f, ays = 0.f;
+                        if constexpr (ROW) {
+                            axs = rax[sj];
+                            ays = ray_[sj];
+                        } else {
 #pragma unroll (LS::generic ? 1 : 8)
-                        for (int p = 0; p < ML; ++p) {
-                            if (p >= n_lens) break;
-                            const int code = LS::generic ? st.lens[p] : LS::code(p);
-                            const int es = st.epl_slot[p];
-                            float ax, ay;
-                            lens_deflect<float>(code, REC(p), es >= 0 ? scoef + es * EPL_NMAX : nullptr,
-                                                ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
-                            axs += ax;
-                            ays += ay;
+                            for (int p = 0; p < ML; ++p) {
+                                if (p >= n_lens) break;
+                                const int code = LS::generic ? st.lens[p] : LS::code(p);
+                                const int es = st.epl_slot[p];
+                                float ax, ay;
+                                lens_deflect<float>(code, REC(p),
+                                                    es >= 0 ? scoef + es * EPL_NMAX : nullptr,
+                                                    ol[p].bx + ddx, ol[p].by + ddy, ax, ay);
+                                axs += ax;
+                                ays += ay;
+                            }
                         }
                         // alpha_scaling is folded into each source's scale (and
                         // its magnitude into the refine predictor's kappa)

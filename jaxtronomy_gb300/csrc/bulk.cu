@@ -310,6 +310,37 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
         }
     }
     float rh = 0.f, rl = 0.f;  // the current plane's r2p
+    // An FP32 TNFW step: the rays' polynomials as straight-line code, then the
+    // closed form for rays inside x = max(tau, 1); sums into s32.
+    auto tnfw_rays = [&](const float* rf, const float* ox, const float* oy) {
+        float ax[MP_RPT], ay[MP_RPT];
+        bool in[MP_RPT], any = false;
+#pragma unroll
+        for (int k = 0; k < MP_RPT; ++k) {
+            in[k] = tnfw_far_f<true>(rf, ox[k], oy[k], ax[k], ay[k]);
+            any |= in[k];
+        }
+        if (any) {
+#pragma unroll
+            for (int k = 0; k < MP_RPT; ++k)
+                if (in[k]) tnfw_near_f(rf, ox[k], oy[k], ax[k], ay[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < MP_RPT; ++k) {
+            s32[0][k] += ax[k];
+            s32[1][k] += ay[k];
+        }
+    };
+    // FP32 offsets of the rays from deflector record rf's split centre
+    auto offsets = [&](const float* rf, float* ox, float* oy) {
+        const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh0 = rf[RF_Y0H], dl0 = rf[RF_Y0L];
+#pragma unroll
+        for (int k = 0; k < MP_RPT; ++k) {
+            ox[k] = __fadd_rn(__fsub_rn(tH[0][k], ch), __fadd_rn(__fsub_rn(tL[0][k], cl), corr[0][k]));
+            oy[k] = __fadd_rn(__fsub_rn(tH[1][k], dh0),
+                              __fadd_rn(__fsub_rn(tL[1][k], dl0), corr[1][k]));
+        }
+    };
     if (F32) issue_chunk(0, 0);
     for (int c0 = 0, it = 0; c0 < n_steps; c0 += MP_CHUNK, ++it) {
         const int cnt = n_steps - c0 < MP_CHUNK ? n_steps - c0 : MP_CHUNK;
@@ -331,6 +362,14 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
         __syncthreads();
         for (int j = 0; j < cnt; ++j) {
             const int t = F32 ? __float_as_int(spl[j * PL_F + 7]) : stag[j];
+            if (F32 && t == LENSGB_LENS_TNFW) {
+                // the common step (an FP32 subhalo inside the current plane),
+                // decided by one comparison
+                float ox[MP_RPT], oy[MP_RPT];
+                offsets(srec + j * REC_F, ox, oy);
+                tnfw_rays(srec + j * REC_F, ox, oy);
+                continue;
+            }
             const int code = t & BULK_CODE_MASK;
             const long long g = c0 + j;
             if (!F32) {
@@ -439,35 +478,12 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                     pair_add(ph[1][k], pq[1][k], h, l);
                 }
             } else {
-                const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh0 = rf[RF_Y0H], dl0 = rf[RF_Y0L];
                 float ox[MP_RPT], oy[MP_RPT];
-#pragma unroll
-                for (int k = 0; k < MP_RPT; ++k) {
-                    ox[k] = __fadd_rn(__fsub_rn(tH[0][k], ch),
-                                      __fadd_rn(__fsub_rn(tL[0][k], cl), corr[0][k]));
-                    oy[k] = __fadd_rn(__fsub_rn(tH[1][k], dh0),
-                                      __fadd_rn(__fsub_rn(tL[1][k], dl0), corr[1][k]));
-                }
+                offsets(rf, ox, oy);
                 // the profile switch outside the ray loop, so that the rays'
                 // evaluations interleave
                 if (code == LENSGB_LENS_TNFW) {
-                    float ax[MP_RPT], ay[MP_RPT];
-                    bool in[MP_RPT], any = false;
-#pragma unroll
-                    for (int k = 0; k < MP_RPT; ++k) {
-                        in[k] = tnfw_far_f<true>(rf, ox[k], oy[k], ax[k], ay[k]);
-                        any |= in[k];
-                    }
-                    if (any) {
-#pragma unroll
-                        for (int k = 0; k < MP_RPT; ++k)
-                            if (in[k]) tnfw_near_f(rf, ox[k], oy[k], ax[k], ay[k]);
-                    }
-#pragma unroll
-                    for (int k = 0; k < MP_RPT; ++k) {
-                        s32[0][k] += ax[k];
-                        s32[1][k] += ay[k];
-                    }
+                    tnfw_rays(rf, ox, oy);
                 } else {
                     const float* cf = coef_f ? coef_f + g * EPL_NMAX : nullptr;
 #pragma unroll

@@ -62,6 +62,30 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
         axd[k] = 0.0;
         ayd[k] = 0.0;
     }
+    // An FP32 TNFW subhalo: the rays' polynomials as straight-line code, then the
+    // closed form for rays inside x = max(tau, 1); sums into (sx, sy).
+    auto tnfw_rays = [&](const float* rf, float* sx, float* sy) {
+        const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh = rf[RF_Y0H], dl = rf[RF_Y0L];
+        float dx[BULK_RPT], dy[BULK_RPT], ax[BULK_RPT], ay[BULK_RPT];
+        bool in[BULK_RPT], any = false;
+#pragma unroll
+        for (int k = 0; k < BULK_RPT; ++k) {
+            dx[k] = __fadd_rn(__fsub_rn(xh[k], ch), __fsub_rn(xl[k], cl));
+            dy[k] = __fadd_rn(__fsub_rn(yh[k], dh), __fsub_rn(yl[k], dl));
+            in[k] = tnfw_far_f(rf, dx[k], dy[k], ax[k], ay[k]);
+            any |= in[k];
+        }
+        if (any) {
+#pragma unroll
+            for (int k = 0; k < BULK_RPT; ++k)
+                if (in[k]) tnfw_near_f(rf, dx[k], dy[k], ax[k], ay[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < BULK_RPT; ++k) {
+            sx[k] += ax[k];
+            sy[k] += ay[k];
+        }
+    };
     for (int c0 = 0; c0 < n_defl; c0 += BULK_CHUNK) {
         const int cnt = n_defl - c0 < BULK_CHUNK ? n_defl - c0 : BULK_CHUNK;
         __syncthreads();
@@ -76,6 +100,11 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
         for (int k = 0; k < BULK_RPT; ++k) sx[k] = sy[k] = 0.f;
         for (int j = 0; j < cnt; ++j) {
             const int t = stag[j];
+            if (F32 && t == LENSGB_LENS_TNFW) {
+                // the common deflector (an FP32 subhalo), decided by one comparison
+                tnfw_rays(srec + j * REC_F, sx, sy);
+                continue;
+            }
             const int code = t & BULK_CODE_MASK;
             if (code == LENSGB_LENS_NULL) continue;
             const long long g = c0 + j;
@@ -95,27 +124,7 @@ bulk_ray_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d,
                 const float* rf = srec + j * REC_F;
                 const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh = rf[RF_Y0H], dl = rf[RF_Y0L];
                 if (code == LENSGB_LENS_TNFW) {
-                    // the subhalo case: the rays' polynomials as straight-line code,
-                    // then the closed form for rays inside x = max(tau, 1)
-                    float dx[BULK_RPT], dy[BULK_RPT], ax[BULK_RPT], ay[BULK_RPT];
-                    bool in[BULK_RPT], any = false;
-#pragma unroll
-                    for (int k = 0; k < BULK_RPT; ++k) {
-                        dx[k] = __fadd_rn(__fsub_rn(xh[k], ch), __fsub_rn(xl[k], cl));
-                        dy[k] = __fadd_rn(__fsub_rn(yh[k], dh), __fsub_rn(yl[k], dl));
-                        in[k] = tnfw_far_f(rf, dx[k], dy[k], ax[k], ay[k]);
-                        any |= in[k];
-                    }
-                    if (any) {
-#pragma unroll
-                        for (int k = 0; k < BULK_RPT; ++k)
-                            if (in[k]) tnfw_near_f(rf, dx[k], dy[k], ax[k], ay[k]);
-                    }
-#pragma unroll
-                    for (int k = 0; k < BULK_RPT; ++k) {
-                        sx[k] += ax[k];
-                        sy[k] += ay[k];
-                    }
+                    tnfw_rays(rf, sx, sy);
                 } else {
                     const float* cf = coef_f ? coef_f + g * EPL_NMAX : nullptr;
 #pragma unroll

@@ -154,7 +154,7 @@ def test_bulk_matches_lens_model_for_short_lists(cuda):
     assert_beta_close(by, ly, rtol=1e-13)
 
 
-@pytest.mark.parametrize("tau", [0.5, 3.0, 10.0, 40.0])
+@pytest.mark.parametrize("tau", [0.1, 0.5, 3.0, 10.0, 40.0, 200.0])
 def test_bulk_fp32_tnfw_near_and_far_field(cuda, tau):
     """FP32 subhalo deflections against FP64 from the core through the switch to
     the bracket polynomial (x = max(tau, 1)) and far beyond: |d alpha| <= 2e-6

@@ -1262,7 +1262,8 @@ static int ensure_grad_scratch(lensgb_model* m, int n_inst) {
     // two sets of partials: the FP32 pass and the FP64 pass over flagged pixels
     const size_t npart =
         2 * (size_t)cap * grad_chunks(rg) * (m->st.n_params > 0 ? m->st.n_params : 1);
-    const size_t nflag = ((size_t)cap * rg.nx * rg.ny + 7) / 8;  // bytes, in doubles
+    // one flag byte per ray-grid pixel of each system, allocated as doubles
+    const size_t nflag = ((size_t)cap * rg.nx * rg.ny + 7) / 8;
     size_t pad = 0;
     if (m->desc.psf_type == LENSGB_PSF_GAUSSIAN) {
         const size_t side = (size_t)(hr ? m->grid_hr.nx : m->grid.nx) + K - 1;

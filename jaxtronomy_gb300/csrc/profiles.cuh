@@ -596,9 +596,8 @@ __device__ __forceinline__ float tnfw_g_f(float x, float tau) {
 // f13 = 4 rho0 Rs tau^2/(tau^2+1)^2): b is analytic in z = s/x on the whole
 // disk |z| < 1 (its nearest singularities are x = +-i tau), so its Chebyshev
 // interpolant on z in [0, 1] converges geometrically -- 12 terms are within
-// 1.3e-9 relative of b for tau in [0.05, 300] -- and that one polynomial covers
-// both the far field and the 8/9 of the area inside 3 s that used to need the
-// closed form's logarithms.
+// 1.3e-9 relative of b for tau in [0.05, 300] -- so the closed form, with its
+// logarithms, is needed only inside x = s.
 // The pair is split in two so that a thread's rays run the polynomial as
 // straight-line code that interleaves: tnfw_far_f evaluates it whatever x and
 // returns true when x < max(tau, 1), where the caller then overwrites the

@@ -608,11 +608,15 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
         rel = ((t0 + np.asarray(offsets)) * 1e9).astype(np.int64)
         for i in range(len(built)):
             arr[i].release_ns = int(rel[i])
+        st0 = srv.stats()
         ts = time.perf_counter()
         tickets = srv.submit_requests(built, array=arr)
         run.submit_s = time.perf_counter() - ts
         run_lead[0] = 0.05 + 2 * run.submit_s
         srv.drain(900)
+        st1 = srv.stats()
+        run.captures = st1["graph_captures"] - st0["graph_captures"]
+        run.capture_ms = (st1["capture_ns"] - st0["capture_ns"]) / 1e6
         times = np.array([t.times() for t in tickets])
         lat = (times[:, 2] - times[:, 0]) * 1e3
         span = times[:, 2].max() - times[:, 0].min()
@@ -644,7 +648,8 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
                 "latency_ms_p99": float(np.percentile(lat, 99)),
                 "queue_wait_ms_p50": float(np.percentile(run.wait_ms, 50)),
                 "service_ms_p50": float(np.percentile(run.service_ms, 50)),
-                "submit_call_s": run.submit_s})
+                "submit_call_s": run.submit_s,
+                "graph_captures": run.captures, "capture_ms": run.capture_ms})
     med = lambda v: float(np.median(v))  # noqa: E731
     load_lines = []
     for f in sorted(runs):
@@ -653,7 +658,9 @@ def serving_section(n_req, seed=1002, n_streams=32, max_batch=64, contexts_per_b
                            "repeats": len(rr),
                            "served_over_offered_min": min(r["served_per_s"] / r["offered_per_s"]
                                                           for r in rr),
-                           **{k: med([r[k] for r in rr]) for k in rr[0]}})
+                           **{k: med([r[k] for r in rr]) for k in rr[0]},
+                           "latency_ms_p99_repeats": [r["latency_ms_p99"] for r in rr],
+                           "graph_captures_repeats": [r["graph_captures"] for r in rr]})
     ok = [ln for ln in load_lines if ln["served_over_offered_min"] >= 0.99]
     best = max(ok, key=lambda ln: ln["load"]) if ok else None
     sustained = None if best is None else {

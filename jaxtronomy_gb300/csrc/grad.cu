@@ -1111,8 +1111,9 @@ int launch_grad_rays(const GridDesc& g, const StackDesc& st, int n_inst, const d
                      unsigned char* flag, float tau, cudaStream_t stream) {
     if (n_inst <= 0) return 0;
     if (st.n_lens > 0) {
+        // one warp per CTA: FP64 recurrences, spread over as many SMs as possible
         const int n = n_inst * st.n_lens;
-        epl_dcoef_kernel<<<(n + 127) / 128, 128, 0, stream>>>(st, n_inst, rec_d, coef_d, dcoef);
+        epl_dcoef_kernel<<<(n + 31) / 32, 32, 0, stream>>>(st, n_inst, rec_d, coef_d, dcoef);
     }
     const int chunks = grad_chunks(g);
     const int n_prof = st.n_lens + st.n_src + st.n_ll;

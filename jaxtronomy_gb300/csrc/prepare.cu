@@ -281,7 +281,10 @@ int launch_prepare(const GridDesc& g, const StackDesc& st, const double* params,
     const int n_prof = st.n_lens + st.n_src + st.n_ll;
     long long n = (long long)n_inst * n_prof;
     if (n == 0) return 0;
-    int threads = 128;
+    // one warp per CTA: each thread's FP64 set-up (EPL tables, transcendentals)
+    // runs on GB300's FP64 units at 1/64 of the FP32 rate, so the threads are
+    // spread over as many SMs as possible rather than packed four warps per SM
+    int threads = 32;
     int blocks = (int)((n + threads - 1) / threads);
     prepare_kernel<<<blocks, threads, 0, stream>>>(g, st, params, n_inst, rec_d, rec_f, coef_d,
                                                    coef_f, grids, n_dev);
@@ -347,7 +350,9 @@ int launch_bulk_prepare(const BulkUnique& u, const int* index, const double* par
                         double fp32_alpha_max, int* tag, double* rec_d, float* rec_f,
                         double* coef_d, float* coef_f, cudaStream_t stream) {
     if (n_defl <= 0) return 0;
-    const int threads = 128;
+    // one warp per CTA, spreading the FP64 set-up (the TNFW bracket polynomial's
+    // 12 closed-form evaluations per deflector) over as many SMs as possible
+    const int threads = 32;
     bulk_prepare_kernel<<<(n_defl + threads - 1) / threads, threads, 0, stream>>>(
         u, index, params, n_defl, fp32_alpha_max, tag, rec_d, rec_f, coef_d, coef_f);
     return 0;

@@ -298,11 +298,12 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
     };
     // FP64 state: x (position) and alpha.  FP32_SPLIT state: the start angle theta
     // as an FP32 pair (tH + tL equals theta to 2^-48 relative), v, d, the plane's
-    // pending sums and the plane's offset correction -- no FP64 value stays live
+    // pending sums and lc = tL + the plane's offset correction (folded once per
+    // plane, so an offset costs three additions) -- no FP64 value stays live
     // through the loop, so none of it is recomputed there in FP64.
     double xs[2][MP_RPT], al[2][MP_RPT];
     float tH[2][MP_RPT], tL[2][MP_RPT], vh[2][MP_RPT], vl[2][MP_RPT], dh[2][MP_RPT],
-        dl[2][MP_RPT], ph[2][MP_RPT], pq[2][MP_RPT], s32[2][MP_RPT], corr[2][MP_RPT];
+        dl[2][MP_RPT], ph[2][MP_RPT], pq[2][MP_RPT], s32[2][MP_RPT], lc[2][MP_RPT];
 #pragma unroll
     for (int k = 0; k < MP_RPT; ++k) {
         const long long i = i0 + (long long)k * MP_THREADS;
@@ -315,7 +316,8 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
             // opaque to the optimiser: kept as registers, never rebuilt from theta
             asm volatile("" : "+f"(tH[c][k]), "+f"(tL[c][k]));
             vh[c][k] = vl[c][k] = dh[c][k] = dl[c][k] = 0.f;
-            ph[c][k] = pq[c][k] = s32[c][k] = corr[c][k] = 0.f;
+            ph[c][k] = pq[c][k] = s32[c][k] = 0.f;
+            lc[c][k] = tL[c][k];
         }
     }
     float rh = 0.f, rl = 0.f;  // the current plane's r2p
@@ -345,9 +347,8 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
         const float ch = rf[RF_X0H], cl = rf[RF_X0L], dh0 = rf[RF_Y0H], dl0 = rf[RF_Y0L];
 #pragma unroll
         for (int k = 0; k < MP_RPT; ++k) {
-            ox[k] = __fadd_rn(__fsub_rn(tH[0][k], ch), __fadd_rn(__fsub_rn(tL[0][k], cl), corr[0][k]));
-            oy[k] = __fadd_rn(__fsub_rn(tH[1][k], dh0),
-                              __fadd_rn(__fsub_rn(tL[1][k], dl0), corr[1][k]));
+            ox[k] = __fadd_rn(__fsub_rn(tH[0][k], ch), __fsub_rn(lc[0][k], cl));
+            oy[k] = __fadd_rn(__fsub_rn(tH[1][k], dh0), __fsub_rn(lc[1][k], dl0));
         }
     };
     if (F32) issue_chunk(0, 0);
@@ -425,7 +426,7 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                         const float disp =
                             __fmaf_rn(dh[c][k], pl[2], __fmaf_rn(dh[c][k], pl[3],
                                                                  __fmul_rn(dl[c][k], pl[2])));
-                        corr[c][k] = __fmaf_rn(tH[c][k], pl[4], -disp);
+                        lc[c][k] = __fadd_rn(tL[c][k], __fmaf_rn(tH[c][k], pl[4], -disp));
                     }
                 }
                 rh = pl[5];
@@ -442,7 +443,7 @@ multi_plane_kernel(const int* __restrict__ tag, const double* __restrict__ rec_d
                     for (int c = 0; c < 2; ++c) {
                         float e;
                         const float a = two_sum(tH[c][k], -ch[c], e);
-                        const float b = __fadd_rn(__fsub_rn(tL[c][k], cl[c]), corr[c][k]);
+                        const float b = __fsub_rn(lc[c][k], cl[c]);
                         float e2;
                         const float xh = two_sum(a, __fadd_rn(e, b), e2);
                         float qh, ql;

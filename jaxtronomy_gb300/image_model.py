@@ -175,7 +175,8 @@ class ImageModel:
         self._conv_method = _lib.CONV_METHODS[method]
         # arithmetic of the adjoint's ray derivatives (an option of this library):
         # "fp64" (default) or "fp32" (FP32 dual numbers from FP64-accurate
-        # offsets, FP64 forward image, weights and reduction)
+        # offsets with an FP64 re-pass of ill-conditioned pixels; FP64 forward
+        # image, weights and reduction)
         gp = kn.get("gradient_precision", "fp64")
         if gp not in ("fp64", "fp32"):
             raise ValueError("gradient_precision must be 'fp64' or 'fp32'")
@@ -753,7 +754,9 @@ class ImageModel:
         whatever the model's precision: an FP32 model differentiates through
         its FP64 twin, because the gradient's sums over pixels mix signs.
         ``kwargs_numerics["gradient_precision"] = "fp32"`` runs the per-ray
-        derivatives in FP32 (the forward image, weights and reduction stay FP64)."""
+        derivatives in FP32 (the forward image, weights and reduction stay FP64;
+        pixels whose FP32 derivatives are predicted ill-conditioned are
+        recomputed in FP64), within 1e-4 of the FP64 adjoint."""
         if self._n_ps:
             raise ValueError("likelihood gradients with point sources are not supported")
         model = self._model(range(len(self.LensModel.lens_model_list)),

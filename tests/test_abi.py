@@ -173,3 +173,20 @@ def test_host_call_arguments_are_validated_without_a_gpu():
     assert lib.lensgb_image_host(h, None, 2, None, 0, None, 0, 0, None) == _lib.ERR_INVALID
     assert lib.lensgb_image_host(h, None, 0, None, 0, None, 0, 0, None) == _lib.OK
     lib.lensgb_model_destroy(h)
+
+
+def test_model_options_are_validated_without_a_gpu():
+    """The adjoint-precision and convolution-method setters accept their
+    documented values and refuse others with LENSGB_ERR_INVALID."""
+    lib = _lib.load()
+    rc, h, _ = _create(_desc(precision=_lib.FP64))
+    assert rc == _lib.OK
+    assert lib.lensgb_model_set_grad_precision(h, _lib.FP64) == _lib.OK
+    assert lib.lensgb_model_set_grad_precision(h, _lib.FP32_SPLIT) == _lib.OK
+    assert lib.lensgb_model_set_grad_precision(h, 7) == _lib.ERR_INVALID
+    assert "precision" in lib.lensgb_last_error().decode()
+    assert lib.lensgb_model_set_grad_precision(None, _lib.FP64) == _lib.ERR_INVALID
+    for m in _lib.CONV_METHODS.values():
+        assert lib.lensgb_model_set_convolution(h, m) == _lib.OK
+    assert lib.lensgb_model_set_convolution(h, 99) == _lib.ERR_INVALID
+    lib.lensgb_model_destroy(h)

@@ -78,6 +78,8 @@ def batch_size(*kwargs_lists):
     for kl in kwargs_lists:
         for kw in kl or []:
             for v in kw.values():
+                if isinstance(v, (float, int)):  # Python and NumPy float scalars
+                    continue
                 a = np.asarray(v)
                 if a.ndim == 0:
                     continue
@@ -101,7 +103,11 @@ def pack(model_list, table, kwargs_list, rows, col0, what):
     for name, kw in zip(model_list, kwargs_list):
         for key in table[name]:
             if key in kw:
-                rows[:, col] = np.asarray(kw[key], dtype=np.float64).reshape(-1)
+                v = kw[key]
+                if isinstance(v, (float, int)):  # a scalar: broadcast without an array
+                    rows[:, col] = v
+                else:
+                    rows[:, col] = np.asarray(v, dtype=np.float64).reshape(-1)
             elif key in DEFAULTS:
                 rows[:, col] = DEFAULTS[key]
             else:

@@ -619,7 +619,7 @@ class ImageModel:
                               unconvolved=unconvolved, source_add=source_add,
                               lens_light_add=lens_light_add, kwargs_ps=kwargs_ps,
                               kwargs_special=kwargs_special, point_source_add=point_source_add)
-        return im[0].to(torch.float64).cpu().numpy()
+        return im[0].cpu().numpy().astype(np.float64, copy=False)
 
     def source_surface_brightness(self, kwargs_source, kwargs_lens=None, kwargs_extinction=None,
                                   kwargs_special=None, unconvolved=False, de_lensed=False, k=None,
@@ -638,7 +638,7 @@ class ImageModel:
                                 src_idx=src_idx, ll_idx=[], lensed=lensed)
         flags = (_lib.UNCONVOLVED if unconvolved else 0) | _lib.NO_LENS_LIGHT
         im = self._launch(model, _device.to_device_f64(rows), rows.shape[0], flags)
-        return im[0].to(torch.float64).cpu().numpy()
+        return im[0].cpu().numpy().astype(np.float64, copy=False)
 
     def lens_surface_brightness(self, kwargs_lens_light, unconvolved=False, k=None):
         """``image_model.py:371-393``."""
@@ -651,7 +651,7 @@ class ImageModel:
                                 ll_idx=ll_idx)
         flags = (_lib.UNCONVOLVED if unconvolved else 0) | _lib.NO_SOURCE
         im = self._launch(model, _device.to_device_f64(rows), rows.shape[0], flags)
-        return im[0].to(torch.float64).cpu().numpy()
+        return im[0].cpu().numpy().astype(np.float64, copy=False)
 
     def _noise_tensors(self, data=None):
         """Device copies of data, mask and noise model (cached for the model's own
@@ -823,7 +823,7 @@ class ImageModel:
         rows = self.point_source_rows(kwargs_ps, kwargs_special, k=k, kwargs_lens=kwargs_lens)
         out = torch.zeros((rows.shape[0], self._nx, self._ny), dtype=self._dtype, device="cuda")
         self._render_point_rows(out, rows, unconvolved)
-        return out[0].to(torch.float64).cpu().numpy()
+        return out[0].cpu().numpy().astype(np.float64, copy=False)
 
     def reduced_residuals(self, model, error_map=0):
         """(data - model) / sqrt(C_D_model + |error_map|) on the host."""
